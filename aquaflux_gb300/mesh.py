@@ -1,0 +1,271 @@
+"""Host-side mesh data: structured generators, seeded node recipes, cell relabelling.
+
+The mesh is plain struct-of-arrays numpy data (:class:`MeshData`) that the device handle
+(:class:`aquaflux_gb300.residual.DeviceMesh`) uploads once.  Topology follows the reference's
+conventions exactly, because connectivity must be bit-identical to it:
+
+* owner / neighbour per face with ``-1`` marking a boundary face
+  (``aquaflux/mesh/connectivity.py:81-140``);
+* ragged CSR face->node lists in perimeter order (``aquaflux/mesh/connectivity.py:362-475``);
+* structured grids emit face *families* normal to x, then y, then z, each family enumerated in
+  ``meshgrid(..., indexing="ij")`` ravel order, owner = the low-side cell when it exists
+  (``aquaflux/mesh/structured.py:63-152, 155-375``);
+* relabelling keeps the face order and maps cell ``c`` to ``perm[c]``
+  (``aquaflux/mesh/reorder.py:38-98``).
+"""
+from __future__ import annotations
+
+import dataclasses
+
+import numpy as np
+
+
+@dataclasses.dataclass
+class MeshData:
+    """An unstructured cell-centred mesh as host arrays (int32 indices, float64 coordinates)."""
+
+    nodes: np.ndarray  # (n_nodes, dim) float64
+    fn_offsets: np.ndarray  # (n_faces + 1,) int32, CSR row pointers of the face->node lists
+    fn_indices: np.ndarray  # (n_incidences,) int32, node indices in perimeter order
+    owner: np.ndarray  # (n_faces,) int32
+    neighbour: np.ndarray  # (n_faces,) int32, -1 on boundary faces
+    n_cells: int
+    patches: dict  # patch name -> int32 array of boundary face indices (ordered)
+
+    @property
+    def dim(self) -> int:
+        return int(self.nodes.shape[1])
+
+    @property
+    def n_faces(self) -> int:
+        return int(self.owner.shape[0])
+
+    @property
+    def n_nodes(self) -> int:
+        return int(self.nodes.shape[0])
+
+    @property
+    def n_interior(self) -> int:
+        return int(np.count_nonzero(self.neighbour >= 0))
+
+    def with_nodes(self, nodes: np.ndarray) -> "MeshData":
+        nodes = np.ascontiguousarray(nodes, dtype=np.float64)
+        if nodes.shape != self.nodes.shape:
+            raise ValueError(f"node array must have shape {self.nodes.shape}, got {nodes.shape}")
+        return dataclasses.replace(self, nodes=nodes)
+
+    def validate(self) -> "MeshData":
+        """Topological checks of ``aquaflux/mesh/mesh.py:208-319`` that matter to the kernels."""
+        n_faces = self.n_faces
+        if self.fn_offsets.shape != (n_faces + 1,) or int(self.fn_offsets[0]) != 0:
+            raise ValueError("fn_offsets must be a CSR pointer array of length n_faces + 1")
+        if int(self.fn_offsets[-1]) != self.fn_indices.shape[0]:
+            raise ValueError("fn_offsets[-1] must equal len(fn_indices)")
+        counts = np.diff(self.fn_offsets)
+        if self.dim == 2 and np.any(counts != 2):
+            raise ValueError("a 2D face must be an edge (exactly 2 nodes)")
+        if self.dim == 3 and np.any(counts < 3):
+            raise ValueError("a 3D face needs >= 3 nodes")
+        if self.owner.min() < 0 or self.owner.max() >= self.n_cells:
+            raise ValueError(f"owner index out of range [0, {self.n_cells})")
+        if self.neighbour.min() < -1 or self.neighbour.max() >= self.n_cells:
+            raise ValueError(f"neighbour index out of range [-1, {self.n_cells})")
+        interior = self.neighbour >= 0
+        if np.any(self.owner[interior] == self.neighbour[interior]):
+            raise ValueError("an interior face has the same cell as owner and neighbour")
+        referenced = np.zeros(self.n_cells, dtype=bool)
+        referenced[self.owner] = True
+        referenced[self.neighbour[interior]] = True
+        if not referenced.all():
+            raise ValueError(f"cell {int(np.argmin(referenced))} is not referenced by any face")
+        if not np.isfinite(self.nodes).all():
+            raise ValueError("node coordinates contain a non-finite value")
+        return self
+
+
+def graded_nodes(n: int, length: float, growth: float, *, both_sides: bool = True) -> np.ndarray:
+    """Geometric wall grading, the node recipe of ``aquaflux/mesh/structured.py:19-60``."""
+    if n < 1:
+        raise ValueError(f"n must be >= 1, got {n}")
+    if growth <= 0.0:
+        raise ValueError(f"growth must be > 0, got {growth}")
+    i = np.arange(n)
+    power = np.minimum(i, n - 1 - i) if both_sides else i
+    cum = np.concatenate([[0.0], np.cumsum(np.asarray(growth, dtype=float) ** power)])
+    return length * cum / cum[-1]
+
+
+def _family(owner_parts, nb_parts, node_parts, patches, counter, lo_cell, hi_cell, lo_ok, hi_ok,
+            corners, lo_name, hi_name):
+    owner_parts.append(np.where(lo_ok, lo_cell, hi_cell))
+    nb_parts.append(np.where(lo_ok & hi_ok, hi_cell, -1))
+    node_parts.append(np.stack(corners, axis=1))
+    ids = counter[0] + np.arange(lo_ok.size)
+    patches[lo_name] = ids[~lo_ok].astype(np.int32)
+    patches[hi_name] = ids[~hi_ok].astype(np.int32)
+    counter[0] += lo_ok.size
+
+
+def _assemble(nodes, n_cells, owner_parts, nb_parts, node_parts, patches) -> MeshData:
+    fnodes = np.concatenate(node_parts, axis=0)
+    n_faces, k = fnodes.shape
+    return MeshData(
+        nodes=np.ascontiguousarray(nodes, dtype=np.float64),
+        fn_offsets=(np.arange(n_faces + 1) * k).astype(np.int32),
+        fn_indices=fnodes.ravel().astype(np.int32),
+        owner=np.concatenate(owner_parts).astype(np.int32),
+        neighbour=np.concatenate(nb_parts).astype(np.int32),
+        n_cells=int(n_cells),
+        patches=patches,
+    ).validate()
+
+
+def structured_grid_2d(nx: int, ny: int, lx: float = 1.0, ly: float = 1.0, *,
+                       x_nodes: np.ndarray | None = None,
+                       y_nodes: np.ndarray | None = None) -> MeshData:
+    """Quad grid on ``[0,lx]x[0,ly]`` with patches left/right/bottom/top.
+
+    Same face numbering as ``aquaflux/mesh/structured.py:155-282`` (non-periodic form): the
+    ``(nx+1)*ny`` x-normal edges ordered by ``(i, j)`` with ``j`` fastest, then the ``nx*(ny+1)``
+    y-normal edges likewise.
+    """
+    x = np.linspace(0.0, lx, nx + 1) if x_nodes is None else np.asarray(x_nodes, dtype=float)
+    y = np.linspace(0.0, ly, ny + 1) if y_nodes is None else np.asarray(y_nodes, dtype=float)
+    if x.shape != (nx + 1,) or y.shape != (ny + 1,):
+        raise ValueError("node coordinate arrays must have n + 1 entries")
+
+    def node(i, j):
+        return j * (nx + 1) + i
+
+    def cell(i, j):
+        return j * nx + i
+
+    jj, ii = np.meshgrid(np.arange(ny + 1), np.arange(nx + 1), indexing="ij")
+    nodes = np.stack([x[ii].ravel(), y[jj].ravel()], axis=1)
+    own, nb, fn, patches, counter = [], [], [], {}, [0]
+    i, j = (a.ravel() for a in np.meshgrid(np.arange(nx + 1), np.arange(ny), indexing="ij"))
+    _family(own, nb, fn, patches, counter, cell(np.clip(i - 1, 0, nx - 1), j),
+            cell(np.clip(i, 0, nx - 1), j), i > 0, i < nx, [node(i, j), node(i, j + 1)],
+            "left", "right")
+    i, j = (a.ravel() for a in np.meshgrid(np.arange(nx), np.arange(ny + 1), indexing="ij"))
+    _family(own, nb, fn, patches, counter, cell(i, np.clip(j - 1, 0, ny - 1)),
+            cell(i, np.clip(j, 0, ny - 1)), j > 0, j < ny, [node(i, j), node(i + 1, j)],
+            "bottom", "top")
+    return _assemble(nodes, nx * ny, own, nb, fn, patches)
+
+
+def structured_grid_3d(nx: int, ny: int, nz: int, lx: float = 1.0, ly: float = 1.0,
+                       lz: float = 1.0) -> MeshData:
+    """Hex grid on ``[0,lx]x[0,ly]x[0,lz]`` with patches left/right/bottom/top/back/front.
+
+    Same face numbering as ``aquaflux/mesh/structured.py:285-375``: x-, then y-, then z-normal
+    quad families, each in ``(i, j, k)`` ij-ravel order, with the reference's perimeter winding.
+    """
+    hx, hy, hz = lx / nx, ly / ny, lz / nz
+
+    def node(i, j, k):
+        return (k * (ny + 1) + j) * (nx + 1) + i
+
+    def cell(i, j, k):
+        return (k * ny + j) * nx + i
+
+    kk, jj, ii = np.meshgrid(np.arange(nz + 1), np.arange(ny + 1), np.arange(nx + 1), indexing="ij")
+    nodes = np.stack([(ii * hx).ravel(), (jj * hy).ravel(), (kk * hz).ravel()], axis=1)
+    own, nb, fn, patches, counter = [], [], [], {}, [0]
+    i, j, k = (a.ravel() for a in np.meshgrid(np.arange(nx + 1), np.arange(ny), np.arange(nz),
+                                              indexing="ij"))
+    _family(own, nb, fn, patches, counter, cell(np.clip(i - 1, 0, nx - 1), j, k),
+            cell(np.clip(i, 0, nx - 1), j, k), i > 0, i < nx,
+            [node(i, j, k), node(i, j + 1, k), node(i, j + 1, k + 1), node(i, j, k + 1)],
+            "left", "right")
+    i, j, k = (a.ravel() for a in np.meshgrid(np.arange(nx), np.arange(ny + 1), np.arange(nz),
+                                              indexing="ij"))
+    _family(own, nb, fn, patches, counter, cell(i, np.clip(j - 1, 0, ny - 1), k),
+            cell(i, np.clip(j, 0, ny - 1), k), j > 0, j < ny,
+            [node(i, j, k), node(i + 1, j, k), node(i + 1, j, k + 1), node(i, j, k + 1)],
+            "bottom", "top")
+    i, j, k = (a.ravel() for a in np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz + 1),
+                                              indexing="ij"))
+    _family(own, nb, fn, patches, counter, cell(i, j, np.clip(k - 1, 0, nz - 1)),
+            cell(i, j, np.clip(k, 0, nz - 1)), k > 0, k < nz,
+            [node(i, j, k), node(i + 1, j, k), node(i + 1, j + 1, k), node(i, j + 1, k)],
+            "back", "front")
+    return _assemble(nodes, nx * ny * nz, own, nb, fn, patches)
+
+
+def jitter_interior_nodes(nodes: np.ndarray, n_per_axis, extent_per_axis, perturb: float,
+                          seed: int) -> np.ndarray:
+    """Displace strictly-interior lattice nodes by seeded uniform noise, ``+-perturb*h`` per axis.
+
+    The recipe of the reference's skewed-grid helper (``tests/support/meshes.py:39-83``): the
+    lattice is indexed slowest-to-fastest over the reversed axes, one ``rng.uniform`` draw of the
+    whole lattice per axis in x, y[, z] order, masked to interior nodes.  ``h`` is the uniform
+    spacing ``extent / n`` on each axis.
+    """
+    if not perturb:
+        return np.array(nodes, dtype=np.float64, copy=True)
+    steps = [length / n for length, n in zip(extent_per_axis, n_per_axis)]
+    counts = [n + 1 for n in reversed(n_per_axis)]
+    grids = np.meshgrid(*[np.arange(c) for c in counts], indexing="ij")
+    interior = np.ones(grids[0].shape, dtype=bool)
+    for g, n in zip(grids, reversed(n_per_axis)):
+        interior &= (g > 0) & (g < n)
+    rng = np.random.default_rng(seed)
+    offsets = np.stack([(interior * rng.uniform(-perturb * h, perturb * h, interior.shape)).ravel()
+                        for h in steps], axis=1)
+    return np.asarray(nodes, dtype=np.float64) + offsets
+
+
+def bump_channel_nodes_3d(shape, extent, bump_height: float, jitter: float, seed: int) -> np.ndarray:
+    """Node coordinates of a hex channel with a seeded Gaussian bump on the lower (y = 0) wall.
+
+    The bump ``h(x, z) = bump_height * exp(-((x-xc)^2 + (z-zc)^2) / (2 s^2))`` lifts every node
+    by ``h(x, z) * (1 - y / ly)``, so the lower wall carries the full bump and the upper wall none.
+    Its centre and width are drawn from ``default_rng(seed)``: ``xc = lx (0.3 + 0.2 u0)``,
+    ``zc = lz (0.4 + 0.2 u1)``, ``s = 0.12 lx (0.8 + 0.4 u2)``.  Interior nodes are then jittered
+    by :func:`jitter_interior_nodes` with amplitude ``jitter`` and seed ``seed + 1``.
+    """
+    nx, ny, nz = shape
+    lx, ly, lz = extent
+    hx, hy, hz = lx / nx, ly / ny, lz / nz
+    kk, jj, ii = np.meshgrid(np.arange(nz + 1), np.arange(ny + 1), np.arange(nx + 1), indexing="ij")
+    x = (ii * hx).ravel()
+    y = (jj * hy).ravel()
+    z = (kk * hz).ravel()
+    u = np.random.default_rng(seed).random(3)
+    xc, zc, s = lx * (0.3 + 0.2 * u[0]), lz * (0.4 + 0.2 * u[1]), 0.12 * lx * (0.8 + 0.4 * u[2])
+    bump = bump_height * np.exp(-((x - xc) ** 2 + (z - zc) ** 2) / (2.0 * s * s))
+    nodes = np.stack([x, y + bump * (1.0 - y / ly), z], axis=1)
+    return jitter_interior_nodes(nodes, shape, extent, jitter, seed + 1)
+
+
+def permute_cells(mesh: MeshData, perm: np.ndarray) -> MeshData:
+    """Relabel cell ``c`` as ``perm[c]``; faces keep their order (``aquaflux/mesh/reorder.py:38-98``)."""
+    perm = np.asarray(perm)
+    if perm.shape != (mesh.n_cells,) or not np.array_equal(np.sort(perm), np.arange(mesh.n_cells)):
+        raise ValueError(f"perm must be a permutation of [0, {mesh.n_cells})")
+    owner = perm[mesh.owner].astype(np.int32)
+    nb = np.where(mesh.neighbour >= 0, perm[np.clip(mesh.neighbour, 0, None)], -1).astype(np.int32)
+    return dataclasses.replace(mesh, owner=owner, neighbour=nb).validate()
+
+
+def random_permutation(n_cells: int, seed: int = 0) -> np.ndarray:
+    """``RandomReordering.permutation`` (``aquaflux/mesh/reorder.py:162-176``)."""
+    return np.random.default_rng(seed).permutation(n_cells)
+
+
+def cell_adjacency_csr(mesh: MeshData) -> tuple[np.ndarray, np.ndarray]:
+    """Symmetric cell graph of the interior faces as sorted CSR (``aquaflux/mesh/graph.py:29-91``)."""
+    interior = mesh.neighbour >= 0
+    o = mesh.owner[interior].astype(np.int64)
+    n = mesh.neighbour[interior].astype(np.int64)
+    rows = np.concatenate([o, n])
+    cols = np.concatenate([n, o])
+    order = np.lexsort((cols, rows))
+    rows, cols = rows[order], cols[order]
+    keep = np.ones(rows.size, dtype=bool)
+    keep[1:] = (rows[1:] != rows[:-1]) | (cols[1:] != cols[:-1])
+    rows, cols = rows[keep], cols[keep]
+    indptr = np.zeros(mesh.n_cells + 1, dtype=np.int64)
+    np.add.at(indptr, rows + 1, 1)
+    return np.cumsum(indptr).astype(np.int32), cols.astype(np.int32)

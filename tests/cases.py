@@ -1,0 +1,73 @@
+"""Golden-fixture loaders and the case descriptions shared by the CPU and GPU tests."""
+from __future__ import annotations
+
+import os
+import types
+
+import numpy as np
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+_cache: dict = {}
+
+
+def golden(name: str):
+    if name not in _cache:
+        _cache[name] = dict(np.load(os.path.join(GOLDEN, name + ".npz")))
+    return _cache[name]
+
+
+def mesh_from(d: dict, prefix: str):
+    """A mesh namespace (nodes, CSR face nodes, owner/neighbour, patches) from fixture arrays."""
+    patches = {k[len(prefix) + 6:]: d[k] for k in d if k.startswith(prefix + "patch_")}
+    return types.SimpleNamespace(
+        nodes=d[prefix + "nodes"], fn_offsets=d[prefix + "fn_offsets"],
+        fn_indices=d[prefix + "fn_indices"], owner=d[prefix + "owner"],
+        neighbour=d[prefix + "neighbour"], n_cells=len(d[prefix + "volume"]), patches=patches)
+
+
+CAVITY_BC = {"top": ("moving", (1.0, 0.0)), "bottom": ("wall",), "left": ("wall",),
+             "right": ("wall",)}
+DUCT3_BC = {"left": ("inlet", (1.0, 0.0, 0.0)), "right": ("outlet", 0.0), "bottom": ("wall",),
+            "top": ("wall",), "back": ("wall",), "front": ("wall",)}
+
+
+def sst_spec(dim, nu, k_in, w_in, walls):
+    fb = {"left": ("inlet", (1.0,) + (0.0,) * (dim - 1)), "right": ("outlet", 0.0)}
+    fb.update({w: ("wall",) for w in walls})
+    kb = {"left": ("dirichlet", k_in), "right": ("zerograd",)}
+    kb.update({w: ("dirichlet", 0.0) for w in walls})
+    wb = {"left": ("dirichlet", w_in), "right": ("zerograd",)}
+    wb.update({w: ("zerograd",) for w in walls})
+    return fb, {"nu": nu, "walls": list(walls), "k": kb, "omega": wb}
+
+
+# (fixture file, prefix, description) of every residual case pinned by the reference.
+LAMINAR = {
+    "cav8": dict(prefix="cav8_", mu=0.01, bc=CAVITY_BC, pin=0),
+    "cavj": dict(prefix="cavj_", mu=0.01, bc=CAVITY_BC, pin=0),
+    "lam3": dict(prefix="lam3_", mu=0.02, bc=DUCT3_BC, pin=None),
+}
+SST = {
+    "sst2": dict(prefix="sst2_", dim=2, nu=2e-5, walls=["bottom", "top"]),
+    "sst3": dict(prefix="sst3_", dim=3, nu=1e-3, walls=["bottom", "top", "back", "front"]),
+}
+
+
+def oracle_case(name: str):
+    """(oracle case dict, fixture dict, prefix) for a named golden residual case."""
+    from oracle import fv_oracle as fo
+
+    if name in LAMINAR:
+        spec = LAMINAR[name]
+        d = golden("laminar")
+        mesh = mesh_from(d, spec["prefix"])
+        case = fo.make_case(mesh, mu=spec["mu"], rho=1.0, flow_bc=spec["bc"],
+                            pressure_pin=spec["pin"])
+        return case, d, spec["prefix"]
+    spec = SST[name]
+    d = golden("sst")
+    mesh = mesh_from(d, spec["prefix"])
+    k_in, w_in = d[spec["prefix"] + "inlet"]
+    fb, sst = sst_spec(spec["dim"], spec["nu"], float(k_in), float(w_in), spec["walls"])
+    case = fo.make_case(mesh, mu=spec["nu"], rho=1.0, flow_bc=fb, sst=sst)
+    return case, d, spec["prefix"]

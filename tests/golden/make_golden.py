@@ -1,0 +1,318 @@
+"""Generate the golden vectors in this folder by running the reference package itself.
+
+Run from the repository root, in a container that has the reference source checked out:
+
+    python tests/golden/make_golden.py /root/reference
+
+JAX is not installed there, so the reference's forward code runs on :mod:`refshim` (numpy float64
+stand-ins for ``jax.numpy`` / ``equinox``).  Everything written here is produced by the reference's
+own functions:
+
+* mesh topology and geometry: ``aquaflux.mesh.structured_grid_2d/3d`` and ``Mesh.geometry()``
+  (``aquaflux/mesh/structured.py:155-375``, ``aquaflux/mesh/mesh.py:341-387``);
+* residuals: ``MomentumContinuity.residual`` (``aquaflux/flow/momentum.py:880``) and
+  ``CoupledRANS.residual`` (``aquaflux/turbulence/coupled.py:437``), plus intermediate fields from
+  ``MomentumContinuity.flow_fields`` (``momentum.py:822``);
+* JVP goldens: central finite differences of those reference residuals;
+* ILU(0): the reference's pure-Python twin (``aquaflux/solve/ilu0.py:76-150``) on the fixture
+  operator of ``tests/unit/test_ilu0.py:17-37``.
+
+The only inputs this script invents are node coordinates (seeded jitter and a Gaussian bump) and the
+seeded states; the same recipes are restated in ``aquaflux_gb300.mesh`` so the GPU tests rebuild
+identical meshes without the reference.
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+import refshim  # noqa: E402
+
+refshim.install()
+
+REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+sys.path.insert(0, REF)
+sys.path.insert(0, os.path.join(REF, "tests"))
+
+import jax.numpy as jnp  # noqa: E402  (the shim)
+from aquaflux.boundary import BoundaryConditions, Dirichlet, ZeroGradient  # noqa: E402
+from aquaflux.discretization import FirstOrderUpwind  # noqa: E402
+from aquaflux.flow import (  # noqa: E402
+    MomentumContinuity,
+    MovingWall,
+    NoSlipWall,
+    PressureOutlet,
+    VelocityInlet,
+)
+from aquaflux.mesh import graded_nodes, structured_grid_2d, structured_grid_3d  # noqa: E402
+from aquaflux.properties import Constant, PropertyModel  # noqa: E402
+from aquaflux.schemes import CompactGreenGauss  # noqa: E402
+from aquaflux.solve import ilu0 as ref_ilu0  # noqa: E402
+from aquaflux.turbulence import SSTModel, SSTTurbulence, inlet_k, inlet_omega  # noqa: E402
+from aquaflux.turbulence.coupled import CoupledRANS  # noqa: E402
+
+sys.path.insert(0, os.path.join(REF, "tests", "unit"))
+
+# The node-coordinate recipes live in the package (restated there for the GPU machine); importing
+# them here guarantees that the fixtures and the GPU tests see the same coordinates.
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+from aquaflux_gb300.mesh import bump_channel_nodes_3d, jitter_interior_nodes  # noqa: E402
+
+
+def _with_nodes(mesh, nodes):
+    return refshim._tree_at(lambda m: m.node_coords, mesh, jnp.asarray(nodes))
+
+
+def _mesh_arrays(prefix, mesh, geom):
+    fc = mesh.face_cells
+    fn = mesh.face_nodes
+    out = {
+        f"{prefix}nodes": np.asarray(mesh.node_coords),
+        f"{prefix}owner": np.asarray(fc.owner).astype(np.int32),
+        f"{prefix}neighbour": np.asarray(fc.neighbour).astype(np.int32),
+        f"{prefix}fn_offsets": np.asarray(fn.offsets).astype(np.int32),
+        f"{prefix}fn_indices": np.asarray(fn.face_node_indices).astype(np.int32),
+        f"{prefix}area": np.asarray(geom.face.area),
+        f"{prefix}normal": np.asarray(geom.face.normal),
+        f"{prefix}face_centroid": np.asarray(geom.face.centroid),
+        f"{prefix}volume": np.asarray(geom.cell.volume),
+        f"{prefix}cell_centroid": np.asarray(geom.cell.centroid),
+    }
+    patches = mesh.face_patches
+    for name in patches.names:
+        out[f"{prefix}patch_{name}"] = np.asarray(patches.indices(name)).astype(np.int32)
+    return out
+
+
+def _fd_jvp(fn, state, direction, h):
+    return (np.asarray(fn(jnp.asarray(state + h * direction)))
+            - np.asarray(fn(jnp.asarray(state - h * direction)))) / (2.0 * h)
+
+
+# --------------------------------------------------------------------------- meshes
+def mesh_cases():
+    out = {}
+    m = structured_grid_2d(5, 4, lx=2.0, ly=1.0, named_boundaries=True)
+    m = _with_nodes(m, jitter_interior_nodes(np.asarray(m.node_coords), (5, 4), (2.0, 1.0), 0.15, 3))
+    out.update(_mesh_arrays("m2d_", m, m.geometry()))
+    m = structured_grid_3d(4, 3, 3, lx=2.0, ly=1.0, lz=1.0, named_boundaries=True)
+    nodes = bump_channel_nodes_3d((4, 3, 3), (2.0, 1.0, 1.0), bump_height=0.1, jitter=0.1, seed=5)
+    m = _with_nodes(m, nodes)
+    out.update(_mesh_arrays("m3d_", m, m.geometry()))
+    yn = graded_nodes(6, 1.0, 1.3)
+    m = structured_grid_2d(7, 6, lx=3.0, ly=1.0, named_boundaries=True, y_nodes=yn)
+    out.update(_mesh_arrays("mgr_", m, m.geometry()))
+    out["mgr_y_nodes"] = np.asarray(yn)
+    return out
+
+
+# --------------------------------------------------------------------------- laminar flow
+def _cavity(n, perturb=0.0, seed=0, mu=0.01):
+    mesh = structured_grid_2d(n, n, lx=1.0, ly=1.0, named_boundaries=True)
+    if perturb:
+        mesh = _with_nodes(mesh, jitter_interior_nodes(np.asarray(mesh.node_coords), (n, n),
+                                                       (1.0, 1.0), perturb, seed))
+    geom = mesh.geometry()
+    asm = MomentumContinuity.build(
+        mesh, geom, PropertyModel({"viscosity": Constant(mu), "density": Constant(1.0)}),
+        CompactGreenGauss(),
+        BoundaryConditions({"top": MovingWall(velocity=(1.0, 0.0)), "bottom": NoSlipWall(),
+                            "left": NoSlipWall(), "right": NoSlipWall()}),
+        advection_scheme=FirstOrderUpwind(), pressure_pin=0)
+    return mesh, geom, asm
+
+
+def _laminar_channel3d(shape, mu=0.02, rho=1.0, u_in=1.0):
+    nx, ny, nz = shape
+    mesh = structured_grid_3d(nx, ny, nz, lx=2.0, ly=1.0, lz=1.0, named_boundaries=True)
+    mesh = _with_nodes(mesh, bump_channel_nodes_3d(shape, (2.0, 1.0, 1.0), 0.1, 0.1, 7))
+    geom = mesh.geometry()
+    bcs = {"left": VelocityInlet(velocity=(u_in, 0.0, 0.0)), "right": PressureOutlet(pressure=0.0),
+           "bottom": NoSlipWall(), "top": NoSlipWall(), "back": NoSlipWall(), "front": NoSlipWall()}
+    asm = MomentumContinuity.build(
+        mesh, geom, PropertyModel({"viscosity": Constant(mu), "density": Constant(rho)}),
+        CompactGreenGauss(), BoundaryConditions(bcs), advection_scheme=FirstOrderUpwind())
+    return mesh, geom, asm
+
+
+def _flow_fields(prefix, asm, state):
+    f = asm.flow_fields(jnp.asarray(state))
+    a_p = asm.momentum_matrix_diagonal(f.velocity_fields.velocity, f.velocity_fields.gradient)
+    return {
+        f"{prefix}grad_u": np.asarray(f.velocity_fields.gradient),
+        f"{prefix}grad_p": np.asarray(f.grad_pressure),
+        f"{prefix}mdot": np.asarray(f.mdot),
+        f"{prefix}a_p": np.asarray(a_p)[:, 0],
+        f"{prefix}bvel": np.asarray(f.velocity_fields.boundary_velocity),
+        f"{prefix}bp": np.asarray(f.boundary_pressure),
+    }
+
+
+def laminar_cases():
+    out = {}
+    rng = np.random.default_rng(11)
+    # 8x8 cavity (structured): zero state + two random states (+ FD JVP for the second).
+    mesh, geom, asm = _cavity(8)
+    out.update(_mesh_arrays("cav8_", mesh, geom))
+    states = [np.zeros(3 * 64), rng.standard_normal(3 * 64) * 0.3, rng.standard_normal(3 * 64)]
+    out["cav8_states"] = np.stack(states)
+    out["cav8_residuals"] = np.stack([np.asarray(asm.residual(jnp.asarray(s))) for s in states])
+    out.update(_flow_fields("cav8_s1_", asm, states[1]))
+    v = rng.standard_normal(3 * 64)
+    out["cav8_jvp_dir"] = v
+    out["cav8_jvp_fd"] = _fd_jvp(asm.residual, states[1], v, 1e-6)
+    # Config-1 size (64x64, structured): zero state and one random state.
+    mesh, geom, asm = _cavity(64)
+    s = rng.standard_normal(3 * 4096) * 0.2
+    out["cav64_states"] = np.stack([np.zeros(3 * 4096), s])
+    out["cav64_residuals"] = np.stack([np.asarray(asm.residual(jnp.asarray(x)))
+                                       for x in out["cav64_states"]])
+    # Jittered 10x10 cavity (non-orthogonal corrections active).
+    mesh, geom, asm = _cavity(10, perturb=0.15, seed=0)
+    out.update(_mesh_arrays("cavj_", mesh, geom))
+    states = [rng.standard_normal(300) * 0.3, rng.standard_normal(300)]
+    out["cavj_states"] = np.stack(states)
+    out["cavj_residuals"] = np.stack([np.asarray(asm.residual(jnp.asarray(s))) for s in states])
+    out.update(_flow_fields("cavj_s0_", asm, states[0]))
+    v = rng.standard_normal(300)
+    out["cavj_jvp_dir"] = v
+    out["cavj_jvp_fd"] = _fd_jvp(asm.residual, states[0], v, 1e-6)
+    # 3D laminar channel with a bump, inlet/outlet/walls.
+    mesh, geom, asm = _laminar_channel3d((4, 3, 3))
+    out.update(_mesh_arrays("lam3_", mesh, geom))
+    n = mesh.n_cells
+    states = []
+    for _ in range(2):
+        u = 1.0 + 0.3 * rng.standard_normal(n)
+        states.append(np.concatenate([u, 0.2 * rng.standard_normal(2 * n), 0.1 * rng.standard_normal(n)]))
+    out["lam3_states"] = np.stack(states)
+    out["lam3_residuals"] = np.stack([np.asarray(asm.residual(jnp.asarray(s))) for s in states])
+    out.update(_flow_fields("lam3_s0_", asm, states[0]))
+    v = rng.standard_normal(4 * n)
+    out["lam3_jvp_dir"] = v
+    out["lam3_jvp_fd"] = _fd_jvp(asm.residual, states[0], v, 1e-6)
+    return out
+
+
+# --------------------------------------------------------------------------- k-omega SST
+def _rans(mesh, geom, dim, nu, u_in, walls, inlet="left", outlet="right", intensity=0.05,
+          length_scale=0.07):
+    rho = 1.0
+    model = SSTModel()
+    k_in = float(inlet_k(jnp.array(u_in), intensity))
+    omega_in = float(inlet_omega(jnp.array(k_in), length_scale, model))
+    vel = (u_in,) + (0.0,) * (dim - 1)
+    flow_bc = {inlet: VelocityInlet(velocity=vel), outlet: PressureOutlet(pressure=0.0)}
+    flow_bc.update({w: NoSlipWall() for w in walls})
+    k_bc = {inlet: Dirichlet(k_in), outlet: ZeroGradient()}
+    k_bc.update({w: Dirichlet(0.0) for w in walls})
+    w_bc = {inlet: Dirichlet(omega_in), outlet: ZeroGradient()}
+    w_bc.update({w: ZeroGradient() for w in walls})
+    momentum = MomentumContinuity.build(
+        mesh, geom, PropertyModel({"viscosity": Constant(rho * nu), "density": Constant(rho)}),
+        CompactGreenGauss(), BoundaryConditions(flow_bc), advection_scheme=FirstOrderUpwind())
+    turb = SSTTurbulence.build(
+        model, mesh, geom, CompactGreenGauss(), FirstOrderUpwind(), density=rho,
+        molecular_viscosity=jnp.full(mesh.n_cells, nu), wall_patches=list(walls),
+        k_boundary=BoundaryConditions(k_bc), omega_boundary=BoundaryConditions(w_bc))
+    return CoupledRANS.build(momentum, turb), turb, k_in, omega_in
+
+
+def _rans_states(rng, n, dim, k_in, omega_in, count, negative_k=False):
+    states = []
+    for i in range(count):
+        u = 1.0 + 0.3 * rng.standard_normal(n)
+        rest = 0.2 * rng.standard_normal((dim - 1) * n)
+        p = 0.1 * rng.standard_normal(n)
+        k = k_in * (0.3 + rng.random(n)) * (1.0 + 20.0 * rng.random(n))
+        om = omega_in * (0.3 + rng.random(n)) * (1.0 + 5.0 * rng.random(n))
+        if negative_k and i == count - 1:
+            k[rng.choice(n, size=max(1, n // 10), replace=False)] *= -0.5
+        states.append(np.concatenate([u, rest, p, k, om]))
+    return states
+
+
+def sst_cases():
+    out = {}
+    rng = np.random.default_rng(23)
+    # 2D graded, jittered channel (the backward-step configuration's physics at fixture size).
+    nx, ny = 12, 8
+    yn = graded_nodes(ny, 1.0, 1.2)
+    mesh = structured_grid_2d(nx, ny, lx=4.0, ly=1.0, named_boundaries=True, y_nodes=yn)
+    mesh = _with_nodes(mesh, jitter_interior_nodes(np.asarray(mesh.node_coords), (nx, ny),
+                                                   (4.0, 1.0), 0.1, 4))
+    geom = mesh.geometry()
+    coupled, turb, k_in, omega_in = _rans(mesh, geom, 2, 2e-5, 1.0, ["bottom", "top"])
+    out.update(_mesh_arrays("sst2_", mesh, geom))
+    out["sst2_y_nodes"] = np.asarray(yn)
+    out["sst2_wall_distance"] = np.asarray(turb.wall_distance)
+    out["sst2_wall_distance_gradient"] = np.asarray(turb.wall_distance_gradient)
+    out["sst2_inlet"] = np.array([k_in, omega_in])
+    n = mesh.n_cells
+    states = _rans_states(rng, n, 2, k_in, omega_in, 3, negative_k=True)
+    out["sst2_states"] = np.stack(states)
+    out["sst2_residuals"] = np.stack([np.asarray(coupled.residual(jnp.asarray(s))) for s in states])
+    v = rng.standard_normal(5 * n)
+    scale = np.abs(states[0]) + 1e-3
+    out["sst2_jvp_dir"] = v * scale
+    out["sst2_jvp_fd"] = _fd_jvp(coupled.residual, states[0], v * scale, 1e-7)
+    # 3D duct with a bump.
+    shape = (5, 4, 3)
+    mesh = structured_grid_3d(*shape, lx=2.0, ly=1.0, lz=1.0, named_boundaries=True)
+    mesh = _with_nodes(mesh, bump_channel_nodes_3d(shape, (2.0, 1.0, 1.0), 0.1, 0.1, 9))
+    geom = mesh.geometry()
+    walls = ["bottom", "top", "back", "front"]
+    coupled, turb, k_in, omega_in = _rans(mesh, geom, 3, 1e-3, 1.0, walls)
+    out.update(_mesh_arrays("sst3_", mesh, geom))
+    out["sst3_wall_distance"] = np.asarray(turb.wall_distance)
+    out["sst3_wall_distance_gradient"] = np.asarray(turb.wall_distance_gradient)
+    out["sst3_inlet"] = np.array([k_in, omega_in])
+    n = mesh.n_cells
+    states = _rans_states(rng, n, 3, k_in, omega_in, 2)
+    out["sst3_states"] = np.stack(states)
+    out["sst3_residuals"] = np.stack([np.asarray(coupled.residual(jnp.asarray(s))) for s in states])
+    v = rng.standard_normal(6 * n)
+    scale = np.abs(states[0]) + 1e-3
+    out["sst3_jvp_dir"] = v * scale
+    out["sst3_jvp_fd"] = _fd_jvp(coupled.residual, states[0], v * scale, 1e-7)
+    return out
+
+
+# --------------------------------------------------------------------------- ILU(0)
+def ilu_cases():
+    import test_ilu0  # the reference's own unit test module (its fixture operator)
+
+    a = test_ilu0._nonsymmetric()
+    a.sort_indices()
+    n = a.shape[0]
+    indptr = a.indptr.astype(np.int32)
+    indices = a.indices.astype(np.int32)
+    diag = ref_ilu0._diagonal_positions(indptr, indices, n)
+    data = a.data.astype(np.float64).copy()
+    ref_ilu0._reference_factor(indptr, indices, data, diag, n)
+    rng = np.random.default_rng(31)
+    rhs = rng.standard_normal(n)
+    x = rhs.copy()
+    ref_ilu0._reference_solve(indptr, indices, data, diag, x, n)
+    xt = rhs.copy()
+    ref_ilu0._reference_solve_transpose(indptr, indices, data, diag, xt, n)
+    return {"ilu_indptr": indptr, "ilu_indices": indices, "ilu_values": a.data.astype(np.float64),
+            "ilu_diag": diag.astype(np.int32), "ilu_factor": data, "ilu_rhs": rhs,
+            "ilu_solve": x, "ilu_solve_t": xt}
+
+
+def main():
+    np.savez_compressed(os.path.join(HERE, "meshes.npz"), **mesh_cases())
+    np.savez_compressed(os.path.join(HERE, "laminar.npz"), **laminar_cases())
+    np.savez_compressed(os.path.join(HERE, "sst.npz"), **sst_cases())
+    np.savez_compressed(os.path.join(HERE, "ilu0.npz"), **ilu_cases())
+    for f in ("meshes", "laminar", "sst", "ilu0"):
+        print(f, os.path.getsize(os.path.join(HERE, f + ".npz")))
+
+
+if __name__ == "__main__":
+    main()
