@@ -1,0 +1,232 @@
+// C ABI for cases: boundary tables, SST wall data, and the residual / JVP entry points.
+#include <cstring>
+#include <vector>
+
+#include "internal.cuh"
+
+size_t fv_residual_work_bytes(int dim, int turb, long nc, long nf);
+int fv_residual_init_constants();
+
+namespace {
+
+template <class X>
+int upload_face_table(const FvMesh* m, const X* host, int width, X fill, X** dev, cudaStream_t s) {
+  // reference face order (nf, width) row-major -> internal order (width, nf)
+  std::vector<X> h((size_t)m->nf * width, fill);
+  if (host) {
+    for (int i = 0; i < m->nf; ++i) {
+      int r = m->h_face_old[i];
+      for (int j = 0; j < width; ++j) h[(size_t)j * m->nf + i] = host[(size_t)r * width + j];
+    }
+  }
+  FV_CUDA_TRY(cudaMalloc(dev, sizeof(X) * h.size()));
+  FV_CUDA_TRY(cudaMemcpyAsync(*dev, h.data(), sizeof(X) * h.size(), cudaMemcpyHostToDevice, s));
+  return FV_OK;
+}
+
+__global__ void k_axpy_shift(long n, const double* shift, const double* v, double* out) {
+  long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] += shift[i] * v[i];
+}
+
+__global__ void k_cell_to_rowmajor(int nc, int dim, const double* in, double* out) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  for (int j = 0; j < dim; ++j) out[(long)c * dim + j] = in[(long)j * nc + c];
+}
+
+}  // namespace
+
+extern "C" int fv_case_create(const FvMesh* mesh, const FvCaseDesc* desc,
+                              const signed char* flow_kind, const double* flow_vel,
+                              const double* flow_p, const signed char* k_kind, const double* k_val,
+                              const signed char* omega_kind, const double* omega_val,
+                              const unsigned char* sst_wall, void* stream, FvCase** out) {
+  if (!mesh || !desc || !out || !flow_kind) {
+    fv_set_error("fv_case_create: bad arguments");
+    return FV_ERR_ARG;
+  }
+  if (!(desc->rho > 0.0) || !(desc->mu > 0.0)) {
+    fv_set_error("fv_case_create: viscosity and density must be positive");
+    return FV_ERR_ARG;
+  }
+  if (desc->pressure_pin >= mesh->nc || desc->pressure_pin < -1) {
+    fv_set_error("fv_case_create: pressure pin %d out of range", desc->pressure_pin);
+    return FV_ERR_ARG;
+  }
+  if (desc->turbulent && (!k_kind || !omega_kind || !sst_wall)) {
+    fv_set_error("fv_case_create: a turbulent case needs k / omega boundary tables and SST walls");
+    return FV_ERR_ARG;
+  }
+  if (fv_residual_init_constants() != FV_OK) return FV_ERR_CUDA;
+  cudaStream_t s = (cudaStream_t)stream;
+  FvMesh* m = const_cast<FvMesh*>(mesh);
+  FvCase* c = new FvCase();
+  c->mesh = m;
+  c->desc = *desc;
+  c->mu = desc->mu;
+  c->inlet_scale = 1.0;
+  c->nfld = m->dim + 1 + (desc->turbulent ? 2 : 0);
+  int rc = FV_OK;
+  rc |= upload_face_table<signed char>(m, flow_kind, 1, (signed char)-1, &c->fkind, s);
+  rc |= upload_face_table<double>(m, flow_vel, m->dim, 0.0, &c->fvel, s);
+  rc |= upload_face_table<double>(m, flow_p, 1, 0.0, &c->fp, s);
+  rc |= upload_face_table<signed char>(m, k_kind, 1, (signed char)-1, &c->kkind, s);
+  rc |= upload_face_table<double>(m, k_val, 1, 0.0, &c->kval, s);
+  rc |= upload_face_table<signed char>(m, omega_kind, 1, (signed char)-1, &c->wkind, s);
+  rc |= upload_face_table<double>(m, omega_val, 1, 0.0, &c->wval, s);
+  rc |= upload_face_table<unsigned char>(m, sst_wall, 1, (unsigned char)0, &c->swall, s);
+  if (rc != FV_OK) {
+    fv_case_destroy(c);
+    return FV_ERR_CUDA;
+  }
+  // SST wall cells: owners of SST wall faces (aquaflux/turbulence/transport.py:226-227)
+  std::vector<unsigned char> wcell(m->nc, 0);
+  int n_wall = 0;
+  if (desc->turbulent) {
+    for (int i = 0; i < m->nf; ++i) {
+      int r = m->h_face_old[i];
+      if (sst_wall[r]) {
+        if (m->h_nb[i] >= 0) {
+          fv_set_error("fv_case_create: SST wall face %d is an interior face", r);
+          fv_case_destroy(c);
+          return FV_ERR_ARG;
+        }
+        wcell[m->h_owner[i]] = 1;
+        ++n_wall;
+      }
+    }
+  }
+  FV_CUDA_TRY(cudaMalloc(&c->wcell, m->nc));
+  FV_CUDA_TRY(cudaMemcpyAsync(c->wcell, wcell.data(), m->nc, cudaMemcpyHostToDevice, s));
+  FV_CUDA_TRY(cudaMalloc(&c->wd, sizeof(double) * m->nc));
+  FV_CUDA_TRY(cudaMalloc(&c->wdg, sizeof(double) * m->nc * m->dim));
+  FV_CUDA_TRY(cudaMemsetAsync(c->wd, 0, sizeof(double) * m->nc, s));
+  FV_CUDA_TRY(cudaMemsetAsync(c->wdg, 0, sizeof(double) * m->nc * m->dim, s));
+  if (desc->turbulent) {
+    rc = fv_wall_distance_compute(m, c->swall, n_wall, c->wd, c->wdg, s);
+    if (rc != FV_OK) {
+      fv_case_destroy(c);
+      return rc;
+    }
+  }
+  c->work_bytes = fv_residual_work_bytes(m->dim, desc->turbulent, m->nc, m->nf);
+  FV_CUDA_TRY(cudaMalloc(&c->work, c->work_bytes));
+  FV_CUDA_TRY(cudaMalloc(&c->tmp, sizeof(double) * (size_t)c->nfld * m->nc));
+  CaseView& v = c->view;
+  v.turb = desc->turbulent;
+  v.rho = desc->rho;
+  v.pin = desc->pressure_pin;
+  v.pin_value = desc->pressure_pin_value;
+  v.fkind = c->fkind;
+  v.fvel = c->fvel;
+  v.fp = c->fp;
+  v.kkind = c->kkind;
+  v.kval = c->kval;
+  v.wkind = c->wkind;
+  v.wval = c->wval;
+  v.swall = c->swall;
+  v.wcell = c->wcell;
+  v.wd = c->wd;
+  v.wdg = c->wdg;
+  FV_CUDA_TRY(cudaStreamSynchronize(s));
+  *out = c;
+  return FV_OK;
+}
+
+extern "C" int fv_case_destroy(FvCase* c) {
+  if (!c) return FV_OK;
+  cudaFree(c->fkind);
+  cudaFree(c->fvel);
+  cudaFree(c->fp);
+  cudaFree(c->kkind);
+  cudaFree(c->kval);
+  cudaFree(c->wkind);
+  cudaFree(c->wval);
+  cudaFree(c->swall);
+  cudaFree(c->wcell);
+  cudaFree(c->wd);
+  cudaFree(c->wdg);
+  cudaFree(c->work);
+  cudaFree(c->tmp);
+  delete c;
+  return FV_OK;
+}
+
+extern "C" int fv_case_set_params(FvCase* c, double mu, double inlet_scale) {
+  if (!c || !(mu > 0.0)) {
+    fv_set_error("fv_case_set_params: viscosity must be positive");
+    return FV_ERR_ARG;
+  }
+  c->mu = mu;
+  c->inlet_scale = inlet_scale;
+  return FV_OK;
+}
+
+extern "C" int fv_case_wall_distance(const FvCase* c, double* distance, double* gradient,
+                                     void* stream) {
+  if (!c) {
+    fv_set_error("fv_case_wall_distance: null case");
+    return FV_ERR_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  const int nc = c->mesh->nc, dim = c->mesh->dim;
+  if (distance) FV_CUDA_TRY(cudaMemcpyAsync(distance, c->wd, sizeof(double) * nc, cudaMemcpyDeviceToDevice, s));
+  if (gradient) k_cell_to_rowmajor<<<fv_blocks(nc, 256), 256, 0, s>>>(nc, dim, c->wdg, gradient);
+  FV_CUDA_TRY(cudaGetLastError());
+  return FV_OK;
+}
+
+extern "C" long fv_case_n_unknowns(const FvCase* c) {
+  return c ? (long)c->nfld * c->mesh->nc : -1;
+}
+
+extern "C" int fv_residual(FvCase* c, const double* state, double* residual, void* stream) {
+  if (!c || !state || !residual) {
+    fv_set_error("fv_residual: bad arguments");
+    return FV_ERR_ARG;
+  }
+  return fv_case_run(c, state, nullptr, FV_TAN_NONE, residual, nullptr, (cudaStream_t)stream);
+}
+
+extern "C" int fv_jvp(FvCase* c, const double* state, const double* v, double* residual,
+                      double* jv, void* stream) {
+  if (!c || !state || !v || !jv) {
+    fv_set_error("fv_jvp: bad arguments");
+    return FV_ERR_ARG;
+  }
+  return fv_case_run(c, state, v, FV_TAN_STATE, residual, jv, (cudaStream_t)stream);
+}
+
+extern "C" int fv_jvp_shift(FvCase* c, const double* state, const double* v, const double* shift,
+                            double* jv, void* stream) {
+  if (!c || !state || !v || !shift || !jv) {
+    fv_set_error("fv_jvp_shift: bad arguments");
+    return FV_ERR_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  int rc = fv_case_run(c, state, v, FV_TAN_STATE, nullptr, jv, s);
+  if (rc != FV_OK) return rc;
+  long n = fv_case_n_unknowns(c);
+  k_axpy_shift<<<fv_blocks(n, 256), 256, 0, s>>>(n, shift, v, jv);
+  FV_CUDA_TRY(cudaGetLastError());
+  return FV_OK;
+}
+
+extern "C" int fv_param_jvp(FvCase* c, const double* state, double* out_mu, double* out_inlet,
+                            void* stream) {
+  if (!c || !state) {
+    fv_set_error("fv_param_jvp: bad arguments");
+    return FV_ERR_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  if (out_mu) {
+    int rc = fv_case_run(c, state, nullptr, FV_TAN_MU, nullptr, out_mu, s);
+    if (rc != FV_OK) return rc;
+  }
+  if (out_inlet) {
+    int rc = fv_case_run(c, state, nullptr, FV_TAN_INLET, nullptr, out_inlet, s);
+    if (rc != FV_OK) return rc;
+  }
+  return FV_OK;
+}

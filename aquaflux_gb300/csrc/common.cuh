@@ -1,0 +1,113 @@
+// Shared device helpers for the finite-volume kernels: status codes, launch helpers and the
+// forward-mode dual number used by the Jacobian-vector product.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cmath>
+
+#include "../../include/fvgb.h"
+
+#define FV_HD __host__ __device__ __forceinline__
+
+// ------------------------------------------------------------------------------------------------
+// Forward-mode dual number.  ``Dual`` carries one tangent; the kernels are templates over the
+// scalar type, so the residual pipeline evaluated with ``Dual`` is exactly the JVP of the residual
+// pipeline evaluated with ``double``.
+//
+// max / min follow JAX's convention at a tie (each argument gets half the tangent), so that the
+// JVP at a state with ties (e.g. the zero state, where every mass flux is exactly 0) equals the
+// reference's ``jax.jvp``.
+// ------------------------------------------------------------------------------------------------
+struct Dual {
+  double v, d;
+};
+
+FV_HD Dual mk(double v, double d) { return Dual{v, d}; }
+FV_HD double val(double x) { return x; }
+FV_HD double val(const Dual& x) { return x.v; }
+FV_HD double tan(const Dual& x) { return x.d; }
+
+FV_HD Dual operator+(Dual a, Dual b) { return {a.v + b.v, a.d + b.d}; }
+FV_HD Dual operator-(Dual a, Dual b) { return {a.v - b.v, a.d - b.d}; }
+FV_HD Dual operator*(Dual a, Dual b) { return {a.v * b.v, a.d * b.v + a.v * b.d}; }
+FV_HD Dual operator/(Dual a, Dual b) {
+  double q = a.v / b.v;
+  return {q, (a.d - q * b.d) / b.v};
+}
+FV_HD Dual operator-(Dual a) { return {-a.v, -a.d}; }
+FV_HD Dual operator+(Dual a, double b) { return {a.v + b, a.d}; }
+FV_HD Dual operator+(double a, Dual b) { return {a + b.v, b.d}; }
+FV_HD Dual operator-(Dual a, double b) { return {a.v - b, a.d}; }
+FV_HD Dual operator-(double a, Dual b) { return {a - b.v, -b.d}; }
+FV_HD Dual operator*(Dual a, double b) { return {a.v * b, a.d * b}; }
+FV_HD Dual operator*(double a, Dual b) { return {a * b.v, a * b.d}; }
+FV_HD Dual operator/(Dual a, double b) { return {a.v / b, a.d / b}; }
+FV_HD Dual operator/(double a, Dual b) {
+  double q = a / b.v;
+  return {q, -q * b.d / b.v};
+}
+FV_HD Dual& operator+=(Dual& a, Dual b) { a = a + b; return a; }
+FV_HD Dual& operator-=(Dual& a, Dual b) { a = a - b; return a; }
+
+// Scalar-generic elementary functions.
+FV_HD double cst(double x, double) { return x; }
+FV_HD Dual cst(double x, Dual) { return {x, 0.0}; }
+
+FV_HD double fv_max(double a, double b) { return a > b ? a : b; }
+FV_HD double fv_min(double a, double b) { return a < b ? a : b; }
+FV_HD Dual fv_max(Dual a, Dual b) {
+  if (a.v > b.v) return a;
+  if (a.v < b.v) return b;
+  return {a.v, 0.5 * (a.d + b.d)};
+}
+FV_HD Dual fv_min(Dual a, Dual b) {
+  if (a.v < b.v) return a;
+  if (a.v > b.v) return b;
+  return {a.v, 0.5 * (a.d + b.d)};
+}
+FV_HD Dual fv_max(Dual a, double b) { return fv_max(a, Dual{b, 0.0}); }
+FV_HD Dual fv_min(Dual a, double b) { return fv_min(a, Dual{b, 0.0}); }
+
+FV_HD double fv_sqrt(double x) { return sqrt(x); }
+FV_HD Dual fv_sqrt(Dual x) {
+  double s = sqrt(x.v);
+  return {s, 0.5 * x.d / s};
+}
+FV_HD double fv_tanh(double x) { return tanh(x); }
+FV_HD Dual fv_tanh(Dual x) {
+  double t = tanh(x.v);
+  return {t, (1.0 - t * t) * x.d};
+}
+FV_HD double fv_log(double x) { return log(x); }
+FV_HD Dual fv_log(Dual x) { return {log(x.v), x.d / x.v}; }
+
+// sqrt with the reference's guard (``aquaflux/turbulence/strain.py:32-43``): 0 (and a zero
+// tangent) for a non-positive argument.
+template <class T>
+FV_HD T safe_sqrt(T x) {
+  return val(x) > 0.0 ? fv_sqrt(x) : cst(0.0, x);
+}
+// max(x, 0) with the JAX tie rule.
+template <class T>
+FV_HD T pos(T x) {
+  return fv_max(x, cst(0.0, x));
+}
+
+// ------------------------------------------------------------------------------------------------
+// Launch helpers.
+// ------------------------------------------------------------------------------------------------
+static inline int fv_blocks(long n, int threads) { return (int)((n + threads - 1) / threads); }
+
+#define FV_CUDA_TRY(expr)                                    \
+  do {                                                       \
+    cudaError_t _e = (expr);                                 \
+    if (_e != cudaSuccess) {                                 \
+      fv_set_error("%s: %s", #expr, cudaGetErrorString(_e)); \
+      return FV_ERR_CUDA;                                    \
+    }                                                        \
+  } while (0)
+
+// Records a formatted message returned by ``fv_last_error``.
+void fv_set_error(const char* fmt, ...);

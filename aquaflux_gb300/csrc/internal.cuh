@@ -1,0 +1,114 @@
+// Library-internal structures shared by the .cu files of libfvgb.
+#pragma once
+
+#include <vector>
+
+#include "common.cuh"
+
+// Bit set in a cell->face incidence entry when the cell is the face's neighbour (its sums take
+// the face flux with a minus sign, the conservative scatter of aquaflux/mesh/connectivity.py:262).
+#define FV_NB_BIT 0x80000000u
+
+// Read-only view of the device mesh passed by value to kernels.  Faces are stored in the
+// internal order: interior faces first, sorted by (owner, neighbour), then boundary faces sorted
+// by owner.  Vector quantities are struct-of-arrays: component j of face f is at [j * nf + f].
+struct MeshView {
+  int dim, nc, nf, nfi, nn;
+  const int* owner;
+  const int* nb;
+  const int* cf_ptr;           // (nc + 1) cell -> face incidence, faces ascending
+  const unsigned* cf_face;     // face index | FV_NB_BIT when the cell is the neighbour
+  const int* fn_ptr;           // (nf + 1) face -> node CSR (internal face order)
+  const int* fn_idx;
+  const double* nodes;         // (nn, dim) row-major
+  // geometry
+  const double* area;          // (nf)
+  const double* normal;        // (dim, nf) owner-outward unit normal
+  const double* xf;            // (dim, nf) face centroid
+  const double* vol;           // (nc)
+  const double* xc;            // (dim, nc) cell centroid
+  // geometry-derived per-face factors (aquaflux/flow/momentum.py:266-279,
+  // aquaflux/schemes/interpolation.py:27-176, aquaflux/discretization/diffusion.py:85-199)
+  const double* g;             // (nf) projection factor, 0 on boundary faces
+  const double* nd;            // (nf) normal distance: d.n (interior), (x_f - x_P).n (boundary)
+  const double* dpn;           // (nf) (x_f - x_P).n
+  const double* dnn;           // (nf) (x_f - x_N).n (boundary: = dpn)
+  const double* dvec;          // (dim, nf) x_N - x_P (0 on boundary faces)
+  const double* skew;          // (dim, nf) x_f - (x_P + g d)
+  const double* tP;            // (dim, nf) (x_f - x_P) - dpn n
+  const double* tN;            // (dim, nf) (x_f - x_N) - dnn n
+  const double* nn2;           // (nf) sum_j n_j n_j
+};
+
+struct FvMesh {
+  int dim = 0, nc = 0, nf = 0, nfi = 0, nn = 0;
+  std::vector<int> h_face_old;  // internal face -> reference face
+  std::vector<int> h_face_new;  // reference face -> internal face
+  std::vector<int> h_owner, h_nb;  // internal order
+  std::vector<int> h_cf_ptr;
+  std::vector<unsigned> h_cf_face;
+  int* owner = nullptr;
+  int* nb = nullptr;
+  int* cf_ptr = nullptr;
+  unsigned* cf_face = nullptr;
+  int* fn_ptr = nullptr;
+  int* fn_idx = nullptr;
+  int* face_old = nullptr;  // device copy of h_face_old
+  double* nodes = nullptr;
+  double* geo = nullptr;  // one allocation holding every geometry / factor array
+  double* approx = nullptr;  // (dim, nc) approximate centroids (work)
+  MeshView view;
+};
+
+// Geometry pipeline (mesh.cu).
+int fv_mesh_compute_geometry(FvMesh* m, cudaStream_t s);
+
+// Device case tables (internal face order) and the residual workspace (residual.cu).
+struct CaseView {
+  int turb;
+  double rho;
+  int pin;
+  double pin_value;
+  const signed char* fkind;   // (nf) flow boundary kind
+  const double* fvel;         // (dim, nf)
+  const double* fp;           // (nf)
+  const signed char* kkind;   // (nf)
+  const double* kval;         // (nf)
+  const signed char* wkind;   // (nf)
+  const double* wval;         // (nf)
+  const unsigned char* swall; // (nf) SST wall face
+  const unsigned char* wcell; // (nc) SST wall cell
+  const double* wd;           // (nc) wall distance
+  const double* wdg;          // (dim, nc) wall-distance gradient
+};
+
+struct FvCase {
+  FvMesh* mesh = nullptr;
+  FvCaseDesc desc{};
+  int nfld = 0;            // dim + 1 (+ 2 when turbulent)
+  double mu = 0.0;         // current molecular viscosity
+  double inlet_scale = 1.0;
+  signed char* fkind = nullptr;
+  double* fvel = nullptr;
+  double* fp = nullptr;
+  signed char* kkind = nullptr;
+  double* kval = nullptr;
+  signed char* wkind = nullptr;
+  double* wval = nullptr;
+  unsigned char* swall = nullptr;
+  unsigned char* wcell = nullptr;
+  double* wd = nullptr;
+  double* wdg = nullptr;
+  void* work = nullptr;     // residual scratch, sized for the Dual pipeline
+  size_t work_bytes = 0;
+  double* tmp = nullptr;    // (n_unknowns) scratch vector
+  CaseView view;
+};
+
+int fv_case_run(FvCase* c, const double* state, const double* tangent, int tangent_kind,
+                double* residual, double* jv, cudaStream_t s);
+enum { FV_TAN_NONE = 0, FV_TAN_STATE = 1, FV_TAN_MU = 2, FV_TAN_INLET = 3 };
+
+// Wall distance + gradient for a turbulent case (mesh.cu).
+int fv_wall_distance_compute(FvMesh* m, const unsigned char* swall_dev, int n_wall_faces,
+                             double* wd, double* wdg, cudaStream_t s);

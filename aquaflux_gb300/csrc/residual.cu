@@ -1,0 +1,686 @@
+// The finite-volume residual pipeline (laminar Rhie-Chow momentum/continuity, optionally coupled
+// to k-omega SST), written once as templates over the scalar type:
+//   T = double -> R(state)
+//   T = Dual   -> R(state) and J v (forward-mode tangent through the same arithmetic)
+//
+// Pipeline (each stage one kernel; face stages run one thread per face in the internal face
+// order, cell stages one thread per cell summing its faces in ascending order, so every
+// face-to-cell accumulation is deterministic without atomics):
+//   k_grad      cell  compact Green-Gauss gradients of every field
+//               (aquaflux/schemes/gradient.py:129-153 with the leading-order boundary values of
+//               aquaflux/flow/momentum.py:445-469 / discretization/residual.py:252-291)
+//   k_closure   cell  SST closure: strain with the wall-cell log-layer blend, imposed wall-cell
+//               omega gradient, F1, nu_t, wall shear rate (aquaflux/turbulence/transport.py:369-579)
+//   k_apcoef    face  momentum-diagonal face coefficients: flux-continuous viscous conductance +
+//               upwind part of the lagged mass-flux estimate, boundary closures
+//               (aquaflux/flow/momentum.py:556-693, aquaflux/flow/rhie_chow.py:81-271)
+//   k_dcoeff    cell  a_P and d = V / a_P
+//   k_flux      face  Rhie-Chow mass flux (rhie_chow.py:274-353, flow/boundary.py:381-435), face
+//               pressure, momentum diffusion + pressure + upwind advection fluxes, k / omega
+//               advection + diffusion fluxes (discretization/diffusion.py:163-199,
+//               advection.py:99-187, turbulence/transport.py:581-718)
+//   k_sum       cell  conservative face-to-cell sums, pressure pin, SST sources and the omega
+//               wall-cell fixation (turbulence/sources.py:60-412, fixed_value.py:124-158)
+#include "internal.cuh"
+
+namespace {
+
+// SST constants, aquaflux/turbulence/sst.py:69-82 and sources.py:52-57.
+constexpr double A1 = 0.31, BETA_STAR = 0.09, ALPHA_1 = 5.0 / 9.0, BETA_1 = 3.0 / 40.0;
+constexpr double SIGMA_K1 = 0.85, SIGMA_W1 = 0.5, ALPHA_2 = 0.44, BETA_2 = 0.0828;
+constexpr double SIGMA_K2 = 1.0, SIGMA_W2 = 0.856, KAPPA = 0.41, E_WALL = 9.8;
+constexpr double CROSS_FLOOR = 1e-10, PROD_RATIO = 10.0, NUT_FLOOR = 1e-30;
+
+struct SstConst {
+  double bs4;   // beta_star ** 0.25
+  double ylam;  // laminar-sublayer y* (fixed point of y = ln(E y) / kappa, 10 sweeps from 11)
+};
+__constant__ SstConst c_sst;
+
+template <class T>
+struct Src;
+template <>
+struct Src<double> {
+  const double* v;
+  __device__ __forceinline__ double operator()(long i) const { return v[i]; }
+};
+template <>
+struct Src<Dual> {
+  const double* v;
+  const double* t;  // may be null: zero tangent
+  __device__ __forceinline__ Dual operator()(long i) const { return {v[i], t ? t[i] : 0.0}; }
+};
+
+template <class T>
+struct Par {
+  T mu;      // molecular dynamic viscosity
+  T iscale;  // inlet-velocity factor
+};
+
+template <class T>
+__device__ __forceinline__ void put(double* r, double* t, long i, const T& x);
+template <>
+__device__ __forceinline__ void put<double>(double* r, double*, long i, const double& x) {
+  r[i] = x;
+}
+template <>
+__device__ __forceinline__ void put<Dual>(double* r, double* t, long i, const Dual& x) {
+  if (r) r[i] = x.v;
+  t[i] = x.d;
+}
+
+// ---------------------------------------------------------------- SST wall functions
+// aquaflux/turbulence/boundary.py:45-589.
+template <class T>
+__device__ __forceinline__ T y_star(T nu, double d, T k) {
+  return c_sst.bs4 * safe_sqrt(pos(k)) * d / nu;
+}
+template <class T>
+__device__ __forceinline__ T wall_weight(T nu, double d, T k) {
+  T r = y_star(nu, d, k) / c_sst.ylam;
+  T r2 = r * r;
+  return fv_tanh(r2 * r2);
+}
+template <class T>
+__device__ __forceinline__ T log_shear(double d, T k) {
+  return c_sst.bs4 * safe_sqrt(pos(k)) / (KAPPA * d);
+}
+template <class T>
+__device__ __forceinline__ T omega_wall(T nu, double d, T k) {
+  T vis = 6.0 * nu / (BETA_1 * (d * d));
+  T lg = safe_sqrt(pos(k)) / (c_sst.bs4 * KAPPA * d);
+  T m = fv_max(vis, lg);
+  T ra = vis / m, rb = lg / m;
+  T bt = val(rb) > 0.0 ? rb * rb : cst(0.0, rb);
+  return m * fv_sqrt(ra * ra + bt);
+}
+template <class T>
+__device__ __forceinline__ T nut_wall(T nu, double d, T k) {
+  T ys = y_star(nu, d, k);
+  T arg = E_WALL * fv_max(ys, cst(c_sst.ylam, ys));
+  T ratio = ys * KAPPA / fv_log(arg) - 1.0;
+  return val(ys) > c_sst.ylam ? nu * ratio : cst(0.0, ys);
+}
+// d omega_wall / d d and d omega_wall / d k in closed form (the reference obtains them with
+// jax.grad, boundary.py:585-589); written in T so the JVP differentiates them once more.
+template <class T>
+__device__ __forceinline__ void omega_wall_partials(T nu, double d, T k, T* dwdd, T* dwdk) {
+  T vis = 6.0 * nu / (BETA_1 * (d * d));
+  T kp = pos(k);
+  T sk = safe_sqrt(kp);
+  double c = c_sst.bs4 * KAPPA;
+  T lg = sk / (c * d);
+  T w = omega_wall(nu, d, k);
+  T dvis_dd = -2.0 * vis / d;
+  T dlog_dd = -lg / d;
+  T dsk = val(kp) > 0.0 ? 0.5 / sk : cst(0.0, sk);
+  T dlog_dk = dsk / (c * d);
+  T a = vis / w, b = lg / w;
+  *dwdd = a * dvis_dd + b * dlog_dd;
+  *dwdk = b * dlog_dk;
+}
+
+// ---------------------------------------------------------------- boundary values
+// Leading-order flow boundary velocity / pressure (aquaflux/flow/boundary.py:43-120, 278-446).
+template <class T>
+__device__ __forceinline__ T bvel(const CaseView& cv, int nf, int f, int j, signed char kind,
+                                  T u_owner, const Par<T>& par) {
+  if (kind == 1) return cst(cv.fvel[(long)j * nf + f], u_owner);
+  if (kind == 2) return cv.fvel[(long)j * nf + f] * par.iscale;
+  if (kind == 3) return u_owner;
+  return cst(0.0, u_owner);
+}
+template <class T>
+__device__ __forceinline__ T bpress(const CaseView& cv, int f, signed char kind, T p_owner) {
+  if (kind == 3) return cst(cv.fp[f], p_owner);
+  if (kind >= 0) return p_owner;
+  return cst(0.0, p_owner);
+}
+// Scalar closure Dirichlet / ZeroGradient (aquaflux/boundary/conditions.py:111-160); `corr` is
+// the tangential correction (zero for the leading-order values used by the gradient).
+template <class T>
+__device__ __forceinline__ T bscalar(signed char kind, double value, T phi_owner, T corr) {
+  if (kind == 0) return cst(value, phi_owner);
+  if (kind == 1) return phi_owner + corr;
+  return cst(0.0, phi_owner);
+}
+
+template <int DIM, bool TURB>
+struct Layout {
+  static constexpr int NFLD = DIM + 1 + (TURB ? 2 : 0);
+  static constexpr int P = DIM, K = DIM + 1, W = DIM + 2;
+};
+
+// ---------------------------------------------------------------- k_grad
+template <class T, int DIM, bool TURB>
+__global__ void __launch_bounds__(128) k_grad(MeshView m, CaseView cv, Src<T> st, Par<T> par, T* G) {
+  using L = Layout<DIM, TURB>;
+  constexpr int NF = L::NFLD;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nc) return;
+  const int nc = m.nc, nf = m.nf;
+  T phic[NF];
+#pragma unroll
+  for (int q = 0; q < NF; ++q) phic[q] = st((long)q * nc + c);
+  T acc[NF][DIM];
+#pragma unroll
+  for (int q = 0; q < NF; ++q)
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) acc[q][j] = cst(0.0, phic[0]);
+  const int b = m.cf_ptr[c], e = m.cf_ptr[c + 1];
+  for (int i = b; i < e; ++i) {
+    const unsigned ent = m.cf_face[i];
+    const int f = (int)(ent & ~FV_NB_BIT);
+    const bool isnb = (ent & FV_NB_BIT) != 0;
+    const double A = m.area[f];
+    double S[DIM];
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) S[j] = m.normal[(long)j * nf + f] * A;
+    T phif[NF];
+    if (f < m.nfi) {
+      const double g = m.g[f];
+      const int other = isnb ? m.owner[f] : m.nb[f];
+#pragma unroll
+      for (int q = 0; q < NF; ++q) {
+        T po = st((long)q * nc + other);
+        T pn = phic[q];
+        if (!isnb) {
+          T t = po;
+          po = pn;
+          pn = t;
+        }
+        phif[q] = (1.0 - g) * po + g * pn;
+      }
+    } else {
+      const signed char kind = cv.fkind[f];
+#pragma unroll
+      for (int j = 0; j < DIM; ++j) phif[j] = bvel(cv, nf, f, j, kind, phic[j], par);
+      phif[L::P] = bpress(cv, f, kind, phic[L::P]);
+      if (TURB) {
+        T z = cst(0.0, phic[0]);
+        phif[L::K] = bscalar(cv.kkind[f], cv.kval[f], phic[L::K], z);
+        phif[L::W] = bscalar(cv.wkind[f], cv.wval[f], phic[L::W], z);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < NF; ++q) {
+      T s = isnb ? -phif[q] : phif[q];
+#pragma unroll
+      for (int j = 0; j < DIM; ++j) acc[q][j] += S[j] * s;
+    }
+  }
+  const double inv = 1.0 / m.vol[c];
+#pragma unroll
+  for (int q = 0; q < NF; ++q)
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) G[((long)q * DIM + j) * nc + c] = acc[q][j] * inv;
+}
+
+// ---------------------------------------------------------------- k_closure (SST)
+// cl layout: [strain, F1, nu_t, wall shear rate] x nc;  Gwi: (DIM, nc) omega gradient with the
+// wall-cell value imposed.
+template <class T, int DIM>
+__global__ void __launch_bounds__(128) k_closure(MeshView m, CaseView cv, Src<T> st, Par<T> par, const T* G, T* cl,
+                                                 T* Gwi) {
+  using L = Layout<DIM, true>;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nc) return;
+  const int nc = m.nc, nf = m.nf;
+  T gu[DIM][DIM];
+#pragma unroll
+  for (int i = 0; i < DIM; ++i)
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) gu[i][j] = G[((long)i * DIM + j) * nc + c];
+  T sum = cst(0.0, gu[0][0]);
+#pragma unroll
+  for (int i = 0; i < DIM; ++i)
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) {
+      T sij = 0.5 * (gu[i][j] + gu[j][i]);
+      sum += sij * sij;
+    }
+  T S = safe_sqrt(2.0 * sum);
+  const T k = st((long)L::K * nc + c);
+  const T w = st((long)L::W * nc + c);
+  const T nu = par.mu / cv.rho;
+  const double d = cv.wd[c];
+  T gk[DIM], gw[DIM];
+#pragma unroll
+  for (int j = 0; j < DIM; ++j) {
+    gk[j] = G[((long)L::K * DIM + j) * nc + c];
+    gw[j] = G[((long)L::W * DIM + j) * nc + c];
+  }
+  T shear = cst(0.0, k);
+  if (cv.wcell[c]) {
+    T wgt = wall_weight(nu, d, k);
+    S = (1.0 - wgt) * S + wgt * log_shear(d, k);
+    T dwdd, dwdk;
+    omega_wall_partials(nu, d, k, &dwdd, &dwdk);
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) gw[j] = cv.wdg[(long)j * nc + c] * dwdd + gk[j] * dwdk;
+    T num = cst(0.0, k);
+    double den = 0.0;
+    T u[DIM];
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) u[j] = st((long)j * nc + c);
+    const int b = m.cf_ptr[c], e = m.cf_ptr[c + 1];
+    for (int i = b; i < e; ++i) {
+      const int f = (int)(m.cf_face[i] & ~FV_NB_BIT);
+      if (f < m.nfi || !cv.swall[f]) continue;
+      const signed char kind = cv.fkind[f];
+      T s2 = cst(0.0, k);
+#pragma unroll
+      for (int j = 0; j < DIM; ++j) {
+        T sl = u[j] - bvel(cv, nf, f, j, kind, u[j], par);
+        s2 += sl * sl;
+      }
+      T rate = safe_sqrt(s2) / d;
+      num += rate * m.area[f];
+      den += m.area[f];
+    }
+    shear = num / den;
+  }
+  // F1 (sst.py:166-202) and the eddy viscosity with F2 (sst.py:152-164, 204-239)
+  T kp = pos(k);
+  T dot_kw = gk[0] * gw[0];
+#pragma unroll
+  for (int j = 1; j < DIM; ++j) dot_kw += gk[j] * gw[j];
+  T cd = fv_max(2.0 * SIGMA_W2 * dot_kw / w, cst(CROSS_FLOOR, w));
+  T sk = safe_sqrt(kp);
+  T visc_term = 500.0 * nu / ((d * d) * w);
+  T arg1 = fv_min(fv_max(sk / (BETA_STAR * w * d), visc_term), 4.0 * SIGMA_W2 * kp / (cd * (d * d)));
+  T a1sq = arg1 * arg1;
+  T F1 = fv_tanh(a1sq * a1sq);
+  T arg2 = fv_max(2.0 * sk / (BETA_STAR * w * d), visc_term);
+  T F2 = fv_tanh(arg2 * arg2);
+  T nut = A1 * kp / fv_max(A1 * w, S * F2);
+  cl[c] = S;
+  cl[(long)nc + c] = F1;
+  cl[2L * nc + c] = nut;
+  cl[3L * nc + c] = shear;
+#pragma unroll
+  for (int j = 0; j < DIM; ++j) Gwi[(long)j * nc + c] = gw[j];
+}
+
+// effective dynamic viscosity mu + rho nu_t (aquaflux/flow/momentum.py:357-368)
+template <class T, bool TURB>
+__device__ __forceinline__ T mu_eff(const Par<T>& par, double rho, const T* cl, int nc, int c) {
+  if (TURB) return par.mu + rho * cl[2L * nc + c];
+  return par.mu;
+}
+
+// lagged advective momentum flux (rho u)_f . n with the skew-corrected face value
+// (aquaflux/flow/rhie_chow.py:220-271)
+template <class T, int DIM, bool TURB>
+__device__ __forceinline__ T mom_normal(const MeshView& m, const Src<T>& st, const T* G, double rho,
+                                        int f, int o, int n, double g) {
+  const int nc = m.nc, nf = m.nf;
+  T mn;
+#pragma unroll
+  for (int j = 0; j < DIM; ++j) {
+    T uf = (1.0 - g) * (rho * st((long)j * nc + o)) + g * (rho * st((long)j * nc + n));
+    T cor;
+#pragma unroll
+    for (int q = 0; q < DIM; ++q) {
+      T gf = (1.0 - g) * (rho * G[((long)j * DIM + q) * nc + o]) +
+             g * (rho * G[((long)j * DIM + q) * nc + n]);
+      T t = gf * m.skew[(long)q * nf + f];
+      cor = q == 0 ? t : cor + t;
+    }
+    T term = (uf + cor) * m.normal[(long)j * nf + f];
+    mn = j == 0 ? term : mn + term;
+  }
+  return mn;
+}
+
+// ---------------------------------------------------------------- k_apcoef
+template <class T, int DIM, bool TURB>
+__global__ void __launch_bounds__(128) k_apcoef(MeshView m, CaseView cv, Src<T> st, Par<T> par, const T* G, const T* cl,
+                                                T* ac_own, T* ac_nb) {
+  using L = Layout<DIM, TURB>;
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= m.nf) return;
+  const int nc = m.nc;
+  const int o = m.owner[f];
+  const bool interior = f < m.nfi;
+  const int n = interior ? m.nb[f] : o;
+  const double g = m.g[f], A = m.area[f];
+  const double rho = cv.rho;
+  T mdot = mom_normal<T, DIM, TURB>(m, st, G, rho, f, o, n, g) * A;
+  T mo = mu_eff<T, TURB>(par, rho, cl, nc, o);
+  if (interior) {
+    T mnb = mu_eff<T, TURB>(par, rho, cl, nc, n);
+    T visc = mo * A / (m.dpn[f] - mo / mnb * m.dnn[f]);
+    ac_own[f] = visc + pos(mdot);
+    ac_nb[f] = visc + pos(-mdot);
+  } else {
+    const signed char kind = cv.fkind[f];
+    T bv = mo;
+    if (TURB && (kind == 0 || kind == 1)) {
+      T nutw = cst(0.0, mo);
+      if (cv.swall[f]) {
+        T nu = par.mu / rho;
+        nutw = nut_wall(nu, cv.wd[o], st((long)L::K * nc + o));
+      }
+      bv = par.mu + rho * nutw;
+    }
+    T vo = bv * A / m.nd[f];
+    T conv = pos(mdot);
+    T coef = kind == 0 || kind == 1 ? vo : (kind == 2 ? vo + conv : (kind == 3 ? conv : cst(0.0, vo)));
+    ac_own[f] = coef;
+    ac_nb[f] = cst(0.0, vo);
+  }
+}
+
+// ---------------------------------------------------------------- k_dcoeff
+template <class T>
+__global__ void k_dcoeff(MeshView m, const T* ac_own, const T* ac_nb, T* dco) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nc) return;
+  const int b = m.cf_ptr[c], e = m.cf_ptr[c + 1];
+  T a;
+  for (int i = b; i < e; ++i) {
+    const unsigned ent = m.cf_face[i];
+    const int f = (int)(ent & ~FV_NB_BIT);
+    T x = (ent & FV_NB_BIT) ? ac_nb[f] : ac_own[f];
+    a = i == b ? x : a + x;
+  }
+  dco[c] = m.vol[c] / a;
+}
+
+// ---------------------------------------------------------------- k_flux
+template <class T, int DIM, bool TURB>
+__global__ void __launch_bounds__(128) k_flux(MeshView m, CaseView cv, Src<T> st, Par<T> par, const T* G, const T* cl,
+                                              const T* dco, T* FL) {
+  using L = Layout<DIM, TURB>;
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= m.nf) return;
+  const int nc = m.nc, nf = m.nf;
+  const int o = m.owner[f];
+  const double A = m.area[f], rho = cv.rho;
+  double nrm[DIM], tP[DIM];
+#pragma unroll
+  for (int j = 0; j < DIM; ++j) {
+    nrm[j] = m.normal[(long)j * nf + f];
+    tP[j] = m.tP[(long)j * nf + f];
+  }
+  const T po = st((long)L::P * nc + o);
+  T mo = mu_eff<T, TURB>(par, rho, cl, nc, o);
+  if (f < m.nfi) {
+    const int n = m.nb[f];
+    const double g = m.g[f];
+    double tN[DIM];
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) tN[j] = m.tN[(long)j * nf + f];
+    const T pn = st((long)L::P * nc + n);
+    T mn = mom_normal<T, DIM, TURB>(m, st, G, rho, f, o, n, g);
+    const double rho_f = (1.0 - g) * rho + g * rho;
+    T gpf[DIM];
+#pragma unroll
+    for (int j = 0; j < DIM; ++j)
+      gpf[j] = (1.0 - g) * G[((long)L::P * DIM + j) * nc + o] + g * G[((long)L::P * DIM + j) * nc + n];
+    T dcf = (1.0 - g) * dco[o] + g * dco[n];
+    T dhat = (nrm[0] * nrm[0]) * dcf;
+#pragma unroll
+    for (int j = 1; j < DIM; ++j) dhat += (nrm[j] * nrm[j]) * dcf;
+    T gd = gpf[0] * m.dvec[f];
+    T gs = gpf[0] * m.skew[f];
+#pragma unroll
+    for (int j = 1; j < DIM; ++j) {
+      gd += gpf[j] * m.dvec[(long)j * nf + f];
+      gs += gpf[j] * m.skew[(long)j * nf + f];
+    }
+    T damping = ((pn - po) - gd) / m.nd[f];
+    T mdot = (mn - rho_f * dhat * damping) * A;
+    T pf = (1.0 - g) * po + g * pn + gs;
+    T mnb = mu_eff<T, TURB>(par, rho, cl, nc, n);
+    T denom = m.dpn[f] - mo / mnb * m.dnn[f];
+    const bool out = val(mdot) >= 0.0;
+#pragma unroll
+    for (int i = 0; i < DIM; ++i) {
+      const T uo = st((long)i * nc + o), un = st((long)i * nc + n);
+      T cp = G[((long)i * DIM) * nc + o] * tP[0];
+      T cn = G[((long)i * DIM) * nc + n] * tN[0];
+#pragma unroll
+      for (int j = 1; j < DIM; ++j) {
+        cp += G[((long)i * DIM + j) * nc + o] * tP[j];
+        cn += G[((long)i * DIM + j) * nc + n] * tN[j];
+      }
+      T diff = -mo * (((un - uo) + cn - cp) / denom) * A;
+      T press = pf * nrm[i] * A;
+      T adv = mdot * (out ? uo : un);
+      FL[(long)i * nf + f] = (diff + press) + adv;
+    }
+    FL[(long)L::P * nf + f] = mdot;
+    if (TURB) {
+      T vflux = mdot / rho;
+      const bool vout = val(vflux) >= 0.0;
+      T nu = par.mu / rho;
+      T F1o = cl[(long)nc + o], F1n = cl[(long)nc + n];
+      T nto = cl[2L * nc + o], ntn = cl[2L * nc + n];
+#pragma unroll
+      for (int s = 0; s < 2; ++s) {
+        const int q = s == 0 ? L::K : L::W;
+        const double in = s == 0 ? SIGMA_K1 : SIGMA_W1, ou = s == 0 ? SIGMA_K2 : SIGMA_W2;
+        T go = nu + (F1o * in + (1.0 - F1o) * ou) * nto;
+        T gn = nu + (F1n * in + (1.0 - F1n) * ou) * ntn;
+        const T phio = st((long)q * nc + o), phin = st((long)q * nc + n);
+        T cp = G[((long)q * DIM) * nc + o] * tP[0];
+        T cn = G[((long)q * DIM) * nc + n] * tN[0];
+#pragma unroll
+        for (int j = 1; j < DIM; ++j) {
+          cp += G[((long)q * DIM + j) * nc + o] * tP[j];
+          cn += G[((long)q * DIM + j) * nc + n] * tN[j];
+        }
+        T adv = vflux * (vout ? phio : phin);
+        T diff = -go * (((phin - phio) + cn - cp) / (m.dpn[f] - go / gn * m.dnn[f])) * A;
+        FL[(long)q * nf + f] = adv + diff;
+      }
+    }
+  } else {
+    const signed char kind = cv.fkind[f];
+    T uo[DIM], bu[DIM];
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) {
+      uo[j] = st((long)j * nc + o);
+      bu[j] = bvel(cv, nf, f, j, kind, uo[j], par);
+    }
+    T mdot;
+    if (kind == 2) {
+      T un = bu[0] * nrm[0];
+#pragma unroll
+      for (int j = 1; j < DIM; ++j) un += bu[j] * nrm[j];
+      mdot = rho * un * A;
+    } else if (kind == 3) {
+      T un = uo[0] * nrm[0];
+      T interp = G[((long)L::P * DIM) * nc + o] * nrm[0];
+#pragma unroll
+      for (int j = 1; j < DIM; ++j) {
+        un += uo[j] * nrm[j];
+        interp += G[((long)L::P * DIM + j) * nc + o] * nrm[j];
+      }
+      T dh = (nrm[0] * nrm[0]) * dco[o];
+#pragma unroll
+      for (int j = 1; j < DIM; ++j) dh += (nrm[j] * nrm[j]) * dco[o];
+      T compact = (cv.fp[f] - po) / m.nd[f];
+      mdot = rho * (un - dh * (compact - interp)) * A;
+    } else {
+      mdot = cst(0.0, po);
+    }
+    T pf = bpress(cv, f, kind, po);
+    T gb = mo;
+    if (TURB) {
+      if (kind == 0 || kind == 1) {
+        T nutw = cst(0.0, mo);
+        if (cv.swall[f]) nutw = nut_wall(par.mu / rho, cv.wd[o], st((long)L::K * nc + o));
+        gb = par.mu + rho * nutw;
+      }
+    }
+    const bool out = val(mdot) >= 0.0;
+#pragma unroll
+    for (int i = 0; i < DIM; ++i) {
+      T cp = G[((long)i * DIM) * nc + o] * tP[0];
+#pragma unroll
+      for (int j = 1; j < DIM; ++j) cp += G[((long)i * DIM + j) * nc + o] * tP[j];
+      T diff = -gb * ((bu[i] - uo[i] - cp) / m.dpn[f]) * A;
+      T press = pf * nrm[i] * A;
+      T adv = mdot * (out ? uo[i] : bu[i]);
+      FL[(long)i * nf + f] = (diff + press) + adv;
+    }
+    FL[(long)L::P * nf + f] = mdot;
+    if (TURB) {
+      T vflux = mdot / rho;
+      const bool vout = val(vflux) >= 0.0;
+      T nu = par.mu / rho;
+      T F1o = cl[(long)nc + o], nto = cl[2L * nc + o];
+#pragma unroll
+      for (int s = 0; s < 2; ++s) {
+        const int q = s == 0 ? L::K : L::W;
+        const double in = s == 0 ? SIGMA_K1 : SIGMA_W1, ou = s == 0 ? SIGMA_K2 : SIGMA_W2;
+        T go = nu + (F1o * in + (1.0 - F1o) * ou) * nto;
+        const T phio = st((long)q * nc + o);
+        T cp = G[((long)q * DIM) * nc + o] * tP[0];
+#pragma unroll
+        for (int j = 1; j < DIM; ++j) cp += G[((long)q * DIM + j) * nc + o] * tP[j];
+        T bphi = s == 0 ? bscalar(cv.kkind[f], cv.kval[f], phio, cp)
+                        : bscalar(cv.wkind[f], cv.wval[f], phio, cp);
+        T gface = go;
+        if (s == 0 && cv.swall[f]) gface = (1.0 - wall_weight(nu, cv.wd[o], phio)) * go;
+        T adv = vflux * (vout ? phio : bphi);
+        T diff = -gface * ((bphi - phio - cp) / m.dpn[f]) * A;
+        FL[(long)q * nf + f] = adv + diff;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------- k_sum
+template <class T, int DIM, bool TURB>
+__global__ void __launch_bounds__(128) k_sum(MeshView m, CaseView cv, Src<T> st, Par<T> par, const T* FL, const T* cl,
+                                             const T* G, const T* Gwi, double* R, double* JV) {
+  using L = Layout<DIM, TURB>;
+  constexpr int NF = L::NFLD;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nc) return;
+  const int nc = m.nc, nf = m.nf;
+  T r[NF];
+  const int b = m.cf_ptr[c], e = m.cf_ptr[c + 1];
+  for (int i = b; i < e; ++i) {
+    const unsigned ent = m.cf_face[i];
+    const int f = (int)(ent & ~FV_NB_BIT);
+    const bool isnb = (ent & FV_NB_BIT) != 0;
+#pragma unroll
+    for (int q = 0; q < NF; ++q) {
+      T x = FL[(long)q * nf + f];
+      if (isnb) x = -x;
+      r[q] = i == b ? x : r[q] + x;
+    }
+  }
+  if (c == cv.pin) r[L::P] = st((long)L::P * nc + c) - cv.pin_value;
+  if (TURB) {
+    const double V = m.vol[c];
+    const T k = st((long)L::K * nc + c), w = st((long)L::W * nc + c);
+    const T S = cl[c], F1 = cl[(long)nc + c], nut = cl[2L * nc + c];
+    const T nu = par.mu / cv.rho;
+    const double d = cv.wd[c];
+    const bool wall = cv.wcell[c] != 0;
+    T prod = nut * (S * S);
+    T limit = PROD_RATIO * BETA_STAR * pos(k) * w;
+    T lim = fv_min(prod, limit);
+    T weff = w;
+    if (wall) {
+      T lw = wall_weight(nu, d, k);
+      T tau = (nu + nut_wall(nu, d, k)) * cl[3L * nc + c];
+      T pw = tau * log_shear(d, k);
+      lim = (1.0 - lw) * lim + lw * pw;
+      weff = omega_wall(nu, d, k);
+    }
+    r[L::K] = r[L::K] - lim * V;
+    r[L::K] = r[L::K] - (-BETA_STAR * k * weff * V);
+    T alpha = F1 * ALPHA_1 + (1.0 - F1) * ALPHA_2;
+    T cap = PROD_RATIO * BETA_STAR * pos(k) * w / fv_max(nut, cst(NUT_FLOOR, nut));
+    r[L::W] = r[L::W] - alpha * fv_min(S * S, cap) * V;
+    T beta = F1 * BETA_1 + (1.0 - F1) * BETA_2;
+    r[L::W] = r[L::W] - (-beta * (w * w) * V);
+    T dkw = G[((long)L::K * DIM) * nc + c] * Gwi[c];
+#pragma unroll
+    for (int j = 1; j < DIM; ++j) dkw += G[((long)L::K * DIM + j) * nc + c] * Gwi[(long)j * nc + c];
+    T cross = 2.0 * (1.0 - F1) * SIGMA_W2 * dkw / w;
+    r[L::W] = r[L::W] - cross * V;
+    if (wall) r[L::W] = w - omega_wall(nu, d, k);
+  }
+#pragma unroll
+  for (int q = 0; q < NF; ++q) put<T>(R, JV, (long)q * nc + c, r[q]);
+}
+
+template <class T, int DIM, bool TURB>
+int run(FvCase* cs, Src<T> st, Par<T> par, double* R, double* JV, cudaStream_t s) {
+  using L = Layout<DIM, TURB>;
+  const MeshView& m = cs->mesh->view;
+  const CaseView& cv = cs->view;
+  const long nc = m.nc, nf = m.nf;
+  T* G = (T*)cs->work;
+  T* cl = G + (long)L::NFLD * DIM * nc;
+  T* Gwi = cl + 4 * nc;
+  T* acown = Gwi + DIM * nc;
+  T* acnb = acown + nf;
+  T* dco = acnb + nf;
+  T* FL = dco + nc;
+  constexpr int TB = 128;
+  const int bc = fv_blocks(nc, TB), bf = fv_blocks(nf, TB);
+  k_grad<T, DIM, TURB><<<bc, TB, 0, s>>>(m, cv, st, par, G);
+  if (TURB) k_closure<T, DIM><<<bc, TB, 0, s>>>(m, cv, st, par, G, cl, Gwi);
+  k_apcoef<T, DIM, TURB><<<bf, TB, 0, s>>>(m, cv, st, par, G, cl, acown, acnb);
+  k_dcoeff<T><<<bc, TB, 0, s>>>(m, acown, acnb, dco);
+  k_flux<T, DIM, TURB><<<bf, TB, 0, s>>>(m, cv, st, par, G, cl, dco, FL);
+  k_sum<T, DIM, TURB><<<bc, TB, 0, s>>>(m, cv, st, par, FL, cl, G, Gwi, R, JV);
+  FV_CUDA_TRY(cudaGetLastError());
+  return FV_OK;
+}
+
+template <int DIM, bool TURB>
+int dispatch_t(FvCase* cs, const double* state, const double* tangent, int kind, double* R,
+               double* JV, cudaStream_t s) {
+  if (kind == FV_TAN_NONE) {
+    return run<double, DIM, TURB>(cs, Src<double>{state}, Par<double>{cs->mu, cs->inlet_scale}, R,
+                                  nullptr, s);
+  }
+  Par<Dual> par{{cs->mu, kind == FV_TAN_MU ? 1.0 : 0.0},
+                {cs->inlet_scale, kind == FV_TAN_INLET ? 1.0 : 0.0}};
+  Src<Dual> st{state, kind == FV_TAN_STATE ? tangent : nullptr};
+  return run<Dual, DIM, TURB>(cs, st, par, R, JV, s);
+}
+
+bool g_const_ready = false;
+
+}  // namespace
+
+size_t fv_residual_work_bytes(int dim, int turb, long nc, long nf) {
+  long nfld = dim + 1 + (turb ? 2 : 0);
+  long n = nfld * dim * nc + 4 * nc + dim * nc + 2 * nf + nc + nfld * nf;
+  return (size_t)n * sizeof(Dual);
+}
+
+int fv_residual_init_constants() {
+  if (g_const_ready) return FV_OK;
+  SstConst h;
+  h.bs4 = pow(BETA_STAR, 0.25);
+  double y = 11.0;
+  for (int i = 0; i < 10; ++i) y = log(E_WALL * y) / KAPPA;
+  h.ylam = y;
+  FV_CUDA_TRY(cudaMemcpyToSymbol(c_sst, &h, sizeof(h)));
+  g_const_ready = true;
+  return FV_OK;
+}
+
+int fv_case_run(FvCase* cs, const double* state, const double* tangent, int kind, double* R,
+                double* JV, cudaStream_t s) {
+  const int dim = cs->mesh->dim;
+  const bool turb = cs->desc.turbulent != 0;
+  if (dim == 2) {
+    return turb ? dispatch_t<2, true>(cs, state, tangent, kind, R, JV, s)
+                : dispatch_t<2, false>(cs, state, tangent, kind, R, JV, s);
+  }
+  return turb ? dispatch_t<3, true>(cs, state, tangent, kind, R, JV, s)
+              : dispatch_t<3, false>(cs, state, tangent, kind, R, JV, s);
+}

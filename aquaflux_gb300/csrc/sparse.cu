@@ -1,0 +1,606 @@
+// Block-sparse (BSR) SpMV, zero-fill ILU(0) and deterministic reductions.
+//
+// ILU(0) restates aquaflux/solve/_ilu0.pyx (factor :68-121, solve :124-147, solve_transpose
+// :150-178) for b x b dense blocks.  On a block-dense pattern, scalar IKJ ILU(0) over the
+// block-expanded (cell-major interleaved) ordering is the same elimination as:
+//   for each lower block (i, j), ascending j:   L_ij = A_ij U_jj^-1   (U_jj: upper triangle of the
+//                                                factored diagonal block of row j)
+//                                                A_ik -= L_ij A_jk   for k > j stored in both rows
+//   then the in-place unit-lower / upper LU of A_ii and A_ik = L_ii^-1 A_ik for k > i,
+// which is what one thread does per block row here.  Rows run in level-set order (a row's level
+// is one more than the deepest row it depends on), so the factor and the triangular sweeps
+// reproduce the sequential algorithm's dependencies exactly.  With b = 1 this is the reference's
+// scalar CSR ILU(0).
+#include <algorithm>
+#include <cstdio>
+#include <vector>
+
+#include "internal.cuh"
+
+void fv_set_error_index(long i);
+
+namespace {
+
+constexpr int kThreads = 256;
+
+// ------------------------------------------------------------------------------ BSR SpMV
+template <class V>
+__global__ void k_bsr_spmv(int nbr, int b, const int* __restrict__ ptr, const int* __restrict__ idx,
+                           const V* __restrict__ val, const V* __restrict__ x, V* __restrict__ y) {
+  // one thread per scalar row: row r = (block row i, component a)
+  long r = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= (long)nbr * b) return;
+  int i = (int)(r / b), a = (int)(r % b);
+  V acc = 0;
+  const long bb = (long)b * b;
+  for (int q = ptr[i]; q < ptr[i + 1]; ++q) {
+    const V* blk = val + (long)q * bb + (long)a * b;
+    const V* xs = x + (long)idx[q] * b;
+    for (int c = 0; c < b; ++c) acc += blk[c] * xs[c];
+  }
+  y[r] = acc;
+}
+
+// Transposed product through the precomputed transpose map: for block row j of A^T, gather
+// blocks (i, j) of A (tptr/tidx list rows i, tblk the block index in A).
+template <class V>
+__global__ void k_bsr_spmv_t(int nbc, int b, const int* __restrict__ tptr, const int* __restrict__ tidx,
+                             const int* __restrict__ tblk, const V* __restrict__ val,
+                             const V* __restrict__ x, V* __restrict__ y) {
+  long r = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= (long)nbc * b) return;
+  int j = (int)(r / b), a = (int)(r % b);
+  V acc = 0;
+  const long bb = (long)b * b;
+  for (int q = tptr[j]; q < tptr[j + 1]; ++q) {
+    const V* blk = val + (long)tblk[q] * bb;
+    const V* xs = x + (long)tidx[q] * b;
+    for (int c = 0; c < b; ++c) acc += blk[(long)c * b + a] * xs[c];
+  }
+  y[r] = acc;
+}
+
+// Host-built transpose of a BSR pattern (cached per pattern pointer for the SpMV entry points).
+struct Transpose {
+  std::vector<int> ptr, idx, blk;
+};
+void build_transpose(int nbr, int nbc, const int* ptr, const int* idx, Transpose* t) {
+  t->ptr.assign(nbc + 1, 0);
+  for (int i = 0; i < nbr; ++i)
+    for (int q = ptr[i]; q < ptr[i + 1]; ++q) t->ptr[idx[q] + 1]++;
+  for (int j = 0; j < nbc; ++j) t->ptr[j + 1] += t->ptr[j];
+  t->idx.assign(t->ptr[nbc], 0);
+  t->blk.assign(t->ptr[nbc], 0);
+  std::vector<int> fill(t->ptr.begin(), t->ptr.end() - 1);
+  for (int i = 0; i < nbr; ++i)
+    for (int q = ptr[i]; q < ptr[i + 1]; ++q) {
+      int s = fill[idx[q]]++;
+      t->idx[s] = i;
+      t->blk[s] = q;
+    }
+}
+
+// ------------------------------------------------------------------------------ ILU(0)
+template <class V>
+struct IluView {
+  int n, b;
+  const int* ptr;
+  const int* idx;
+  const int* diag;  // block index of the diagonal block of each row
+  V* val;
+};
+
+__device__ __forceinline__ void note_zero_pivot(unsigned long long* flag, int row, int col) {
+  unsigned long long key = ((unsigned long long)(unsigned)row << 32) | (unsigned)col;
+  atomicMin(flag, key);
+}
+
+// Factor the block rows of one level.  One thread per block row.
+template <class V>
+__global__ void k_ilu_factor_level(IluView<V> F, const int* rows, int count,
+                                   unsigned long long* zero_flag) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  const int i = rows[t];
+  const int b = F.b;
+  const long bb = (long)b * b;
+  const int rb = F.ptr[i], re = F.ptr[i + 1], di = F.diag[i];
+  // lower blocks, ascending column
+  for (int q = rb; q < di; ++q) {
+    const int j = F.idx[q];
+    V* Lij = F.val + (long)q * bb;
+    const V* Ujj = F.val + (long)F.diag[j] * bb;
+    // L_ij = A_ij U_jj^-1, column by column (scalar columns jb ascending)
+    for (int cb = 0; cb < b; ++cb) {
+      const V piv = Ujj[(long)cb * b + cb];
+      if (piv == V(0)) note_zero_pivot(zero_flag, i * b, j * b + cb);
+      for (int a = 0; a < b; ++a) {
+        V l = Lij[(long)a * b + cb] / piv;
+        Lij[(long)a * b + cb] = l;
+        for (int c2 = cb + 1; c2 < b; ++c2) Lij[(long)a * b + c2] -= l * Ujj[(long)cb * b + c2];
+      }
+    }
+    // A_ik -= L_ij A_jk for k > j present in both rows (merge of sorted column lists)
+    int p = q + 1;
+    for (int s = F.diag[j] + 1; s < F.ptr[j + 1]; ++s) {
+      const int k = F.idx[s];
+      while (p < re && F.idx[p] < k) ++p;
+      if (p >= re) break;
+      if (F.idx[p] != k) continue;
+      V* Aik = F.val + (long)p * bb;
+      const V* Ajk = F.val + (long)s * bb;
+      for (int a = 0; a < b; ++a)
+        for (int c = 0; c < b; ++c) {
+          V acc = Aik[(long)a * b + c];
+          for (int m = 0; m < b; ++m) acc -= Lij[(long)a * b + m] * Ajk[(long)m * b + c];
+          Aik[(long)a * b + c] = acc;
+        }
+    }
+  }
+  // diagonal block: in-place LU (unit lower), and L_ii^-1 applied to the upper blocks
+  V* D = F.val + (long)di * bb;
+  for (int cb = 0; cb < b; ++cb) {
+    const V piv = D[(long)cb * b + cb];
+    for (int a = cb + 1; a < b; ++a) {
+      if (piv == V(0)) note_zero_pivot(zero_flag, i * b + a, i * b + cb);
+      V l = D[(long)a * b + cb] / piv;
+      D[(long)a * b + cb] = l;
+      for (int c = cb + 1; c < b; ++c) D[(long)a * b + c] -= l * D[(long)cb * b + c];
+      for (int q = di + 1; q < re; ++q) {
+        V* U = F.val + (long)q * bb;
+        for (int c = 0; c < b; ++c) U[(long)a * b + c] -= l * U[(long)cb * b + c];
+      }
+    }
+  }
+}
+
+// Forward sweep (L y = r, unit lower) for one level; y holds r on entry.
+template <class V>
+__global__ void k_ilu_lower(IluView<V> F, const int* rows, int count, V* y) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  const int i = rows[t], b = F.b;
+  const long bb = (long)b * b;
+  V acc[8];
+  for (int a = 0; a < b; ++a) acc[a] = y[(long)i * b + a];
+  for (int q = F.ptr[i]; q < F.diag[i]; ++q) {
+    const V* L = F.val + (long)q * bb;
+    const V* yj = y + (long)F.idx[q] * b;
+    for (int a = 0; a < b; ++a)
+      for (int c = 0; c < b; ++c) acc[a] -= L[(long)a * b + c] * yj[c];
+  }
+  const V* D = F.val + (long)F.diag[i] * bb;
+  for (int a = 0; a < b; ++a) {
+    V s = acc[a];
+    for (int c = 0; c < a; ++c) s -= D[(long)a * b + c] * acc[c];
+    acc[a] = s;
+    y[(long)i * b + a] = s;
+  }
+}
+
+// Backward sweep (U x = y) for one level; x holds y on entry.  Per scalar row the upper entries
+// are consumed in ascending column order (in-block first, then the blocks k > i), as in
+// aquaflux/solve/_ilu0.pyx:143-147.
+template <class V>
+__global__ void k_ilu_upper(IluView<V> F, const int* rows, int count, V* x) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  const int i = rows[t], b = F.b;
+  const long bb = (long)b * b;
+  const V* D = F.val + (long)F.diag[i] * bb;
+  V* xi = x + (long)i * b;
+  for (int a = b - 1; a >= 0; --a) {
+    V s = xi[a];
+    for (int c = a + 1; c < b; ++c) s -= D[(long)a * b + c] * xi[c];
+    for (int q = F.diag[i] + 1; q < F.ptr[i + 1]; ++q) {
+      const V* U = F.val + (long)q * bb + (long)a * b;
+      const V* xk = x + (long)F.idx[q] * b;
+      for (int c = 0; c < b; ++c) s -= U[c] * xk[c];
+    }
+    xi[a] = s / D[(long)a * b + a];
+  }
+}
+
+// Transposed sweeps use the transpose map: tptr/tidx/tblk list, for block column i, the rows j
+// and block indices of the stored blocks (j, i).
+// U^T z = r: forward over block columns; z_i = U_ii^-T (r_i - sum_{j<i} U_ji^T z_j).
+template <class V>
+__global__ void k_ilu_upper_t(IluView<V> F, const int* tptr, const int* tidx, const int* tblk,
+                              const int* rows, int count, V* z) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  const int i = rows[t], b = F.b;
+  const long bb = (long)b * b;
+  V acc[8];
+  for (int a = 0; a < b; ++a) acc[a] = z[(long)i * b + a];
+  for (int q = tptr[i]; q < tptr[i + 1]; ++q) {
+    const int j = tidx[q];
+    if (j >= i) continue;
+    const V* U = F.val + (long)tblk[q] * bb;  // block (j, i)
+    const V* zj = z + (long)j * b;
+    for (int a = 0; a < b; ++a)
+      for (int c = 0; c < b; ++c) acc[a] -= U[(long)c * b + a] * zj[c];
+  }
+  const V* D = F.val + (long)F.diag[i] * bb;
+  for (int a = 0; a < b; ++a) {
+    V s = acc[a];
+    for (int c = 0; c < a; ++c) s -= D[(long)c * b + a] * acc[c];
+    s = s / D[(long)a * b + a];
+    acc[a] = s;
+    z[(long)i * b + a] = s;
+  }
+}
+
+// L^T x = z: backward over block columns; x_i = L_ii^-T (z_i - sum_{k>i} L_ki^T x_k).  The
+// contributions are taken in descending row order, the order of the reference's scatter form
+// (aquaflux/solve/_ilu0.pyx:174-178).
+template <class V>
+__global__ void k_ilu_lower_t(IluView<V> F, const int* tptr, const int* tidx, const int* tblk,
+                              const int* rows, int count, V* x) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  const int i = rows[t], b = F.b;
+  const long bb = (long)b * b;
+  const V* D = F.val + (long)F.diag[i] * bb;
+  V* xi = x + (long)i * b;
+  for (int a = b - 1; a >= 0; --a) {
+    V s = xi[a];
+    for (int q = tptr[i + 1] - 1; q >= tptr[i]; --q) {
+      const int k = tidx[q];
+      if (k <= i) continue;
+      const V* L = F.val + (long)tblk[q] * bb;  // block (k, i)
+      const V* xk = x + (long)k * b;
+      for (int c = b - 1; c >= 0; --c) s -= L[(long)c * b + a] * xk[c];
+    }
+    for (int c = b - 1; c > a; --c) s -= D[(long)c * b + a] * xi[c];
+    xi[a] = s;
+  }
+}
+
+template <class V>
+__global__ void k_copy(long n, const V* a, V* b) {
+  long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = a[i];
+}
+__global__ void k_to_f32(long n, const double* a, float* b) {
+  long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (float)a[i];
+}
+
+// ------------------------------------------------------------------------------ reductions
+constexpr int kRedBlocks = 304;  // 2 x 152 SMs, fixed so the summation order never changes
+__global__ void k_dot_partial(long n, const double* x, const double* y, double* part) {
+  __shared__ double sh[kThreads];
+  double s = 0.0;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    s += x[i] * y[i];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+__global__ void k_dot_final(int nparts, const double* part, double* out) {
+  __shared__ double sh[kThreads];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < nparts; i += blockDim.x) s += part[i];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = sh[0];
+}
+
+double* g_dot_parts = nullptr;
+
+}  // namespace
+
+// ------------------------------------------------------------------------------ FvIlu0
+struct FvIlu0 {
+  int n = 0, b = 0, nnzb = 0, precision = 64;
+  int *ptr = nullptr, *idx = nullptr, *diag = nullptr;
+  int *tptr = nullptr, *tidx = nullptr, *tblk = nullptr;
+  void* val = nullptr;
+  unsigned long long* zero_flag = nullptr;
+  // level sets: rows grouped by level (device), level boundaries (host)
+  int* rows_fwd = nullptr;   // L / factor order
+  int* rows_bwd = nullptr;   // U order (from the last row)
+  int* rows_tfwd = nullptr;  // U^T order
+  int* rows_tbwd = nullptr;  // L^T order
+  std::vector<int> lv_fwd, lv_bwd, lv_tfwd, lv_tbwd;
+};
+
+namespace {
+
+// Level sets of a dependency DAG given as "row i depends on rows deps(i)".
+template <class DepFn>
+void levels(int n, bool ascending, DepFn deps, std::vector<int>* rows, std::vector<int>* bounds) {
+  std::vector<int> lev(n, 0);
+  int maxl = 0;
+  if (ascending) {
+    for (int i = 0; i < n; ++i) {
+      int l = 0;
+      deps(i, [&](int j) { l = std::max(l, lev[j] + 1); });
+      lev[i] = l;
+      maxl = std::max(maxl, l);
+    }
+  } else {
+    for (int i = n - 1; i >= 0; --i) {
+      int l = 0;
+      deps(i, [&](int j) { l = std::max(l, lev[j] + 1); });
+      lev[i] = l;
+      maxl = std::max(maxl, l);
+    }
+  }
+  bounds->assign(maxl + 2, 0);
+  for (int i = 0; i < n; ++i) (*bounds)[lev[i] + 1]++;
+  for (int l = 0; l <= maxl; ++l) (*bounds)[l + 1] += (*bounds)[l];
+  rows->assign(n, 0);
+  std::vector<int> fill(bounds->begin(), bounds->end() - 1);
+  for (int i = 0; i < n; ++i) (*rows)[fill[lev[i]]++] = i;
+}
+
+template <class V>
+IluView<V> view(FvIlu0* f) {
+  return IluView<V>{f->n, f->b, f->ptr, f->idx, f->diag, (V*)f->val};
+}
+
+template <class V>
+int ilu_factor(FvIlu0* f, cudaStream_t s) {
+  IluView<V> F = view<V>(f);
+  unsigned long long init = ~0ull;
+  FV_CUDA_TRY(cudaMemcpyAsync(f->zero_flag, &init, sizeof(init), cudaMemcpyHostToDevice, s));
+  for (size_t l = 0; l + 1 < f->lv_fwd.size(); ++l) {
+    int cnt = f->lv_fwd[l + 1] - f->lv_fwd[l];
+    if (cnt == 0) continue;
+    k_ilu_factor_level<V><<<fv_blocks(cnt, 128), 128, 0, s>>>(F, f->rows_fwd + f->lv_fwd[l], cnt,
+                                                              f->zero_flag);
+  }
+  FV_CUDA_TRY(cudaGetLastError());
+  unsigned long long flag;
+  FV_CUDA_TRY(cudaMemcpyAsync(&flag, f->zero_flag, sizeof(flag), cudaMemcpyDeviceToHost, s));
+  FV_CUDA_TRY(cudaStreamSynchronize(s));
+  if (flag != ~0ull) {
+    long col = (long)(flag & 0xffffffffull);
+    fv_set_error_index(col);
+    fv_set_error(
+        "ILU(0) met an exactly zero pivot at row %ld; the operator needs a different ordering or "
+        "an explicit shift, neither of which this routine applies silently.",
+        col);
+    return FV_ERR_ZERO_PIVOT;
+  }
+  return FV_OK;
+}
+
+template <class V>
+int ilu_apply(FvIlu0* f, const V* r, V* x, int transpose, cudaStream_t s) {
+  IluView<V> F = view<V>(f);
+  const long n = (long)f->n * f->b;
+  if (r != x) k_copy<V><<<fv_blocks(n, kThreads), kThreads, 0, s>>>(n, r, x);
+  if (!transpose) {
+    for (size_t l = 0; l + 1 < f->lv_fwd.size(); ++l) {
+      int cnt = f->lv_fwd[l + 1] - f->lv_fwd[l];
+      if (cnt) k_ilu_lower<V><<<fv_blocks(cnt, 128), 128, 0, s>>>(F, f->rows_fwd + f->lv_fwd[l], cnt, x);
+    }
+    for (size_t l = 0; l + 1 < f->lv_bwd.size(); ++l) {
+      int cnt = f->lv_bwd[l + 1] - f->lv_bwd[l];
+      if (cnt) k_ilu_upper<V><<<fv_blocks(cnt, 128), 128, 0, s>>>(F, f->rows_bwd + f->lv_bwd[l], cnt, x);
+    }
+  } else {
+    for (size_t l = 0; l + 1 < f->lv_tfwd.size(); ++l) {
+      int cnt = f->lv_tfwd[l + 1] - f->lv_tfwd[l];
+      if (cnt)
+        k_ilu_upper_t<V><<<fv_blocks(cnt, 128), 128, 0, s>>>(F, f->tptr, f->tidx, f->tblk,
+                                                             f->rows_tfwd + f->lv_tfwd[l], cnt, x);
+    }
+    for (size_t l = 0; l + 1 < f->lv_tbwd.size(); ++l) {
+      int cnt = f->lv_tbwd[l + 1] - f->lv_tbwd[l];
+      if (cnt)
+        k_ilu_lower_t<V><<<fv_blocks(cnt, 128), 128, 0, s>>>(F, f->tptr, f->tidx, f->tblk,
+                                                             f->rows_tbwd + f->lv_tbwd[l], cnt, x);
+    }
+  }
+  FV_CUDA_TRY(cudaGetLastError());
+  return FV_OK;
+}
+
+int upload(const std::vector<int>& h, int** d, cudaStream_t s) {
+  FV_CUDA_TRY(cudaMalloc(d, sizeof(int) * std::max<size_t>(1, h.size())));
+  if (!h.empty())
+    FV_CUDA_TRY(cudaMemcpyAsync(*d, h.data(), sizeof(int) * h.size(), cudaMemcpyHostToDevice, s));
+  return FV_OK;
+}
+
+}  // namespace
+
+extern "C" int fv_ilu0_create(int n, int b, const int* indptr, const int* indices, int precision,
+                              void* stream, FvIlu0** out) {
+  if (!out || n <= 0 || b <= 0 || b > 8 || !indptr || !indices ||
+      (precision != 32 && precision != 64)) {
+    fv_set_error("fv_ilu0_create: bad arguments (1 <= b <= 8, precision 32 or 64)");
+    return FV_ERR_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  const int nnzb = indptr[n];
+  std::vector<int> diag(n, -1);
+  for (int i = 0; i < n; ++i) {
+    for (int q = indptr[i]; q < indptr[i + 1]; ++q) {
+      if (indices[q] < 0 || indices[q] >= n || (q > indptr[i] && indices[q] <= indices[q - 1])) {
+        fv_set_error("fv_ilu0_create: row %d has unsorted or out-of-range column indices", i);
+        return FV_ERR_ARG;
+      }
+      if (indices[q] == i) diag[i] = q;
+    }
+  }
+  // reference message: aquaflux/solve/_ilu0.pyx:56-63 (the first rows missing a diagonal)
+  std::vector<int> missing;
+  for (int i = 0; i < n; ++i)
+    if (diag[i] < 0) missing.push_back(i);
+  if (!missing.empty()) {
+    char buf[256];
+    int len = snprintf(buf, sizeof(buf), "rows [");
+    for (size_t k = 0; k < missing.size() && k < 5; ++k)
+      len += snprintf(buf + len, sizeof(buf) - len, "%s%d", k ? ", " : "", missing[k] * b);
+    snprintf(buf + len, sizeof(buf) - len, "]%s", missing.size() > 5 ? " \xe2\x80\xa6" : "");
+    fv_set_error_index((long)missing[0] * b);
+    fv_set_error("%s store no diagonal entry; ILU(0) eliminates in place and cannot introduce one.",
+                 buf);
+    return FV_ERR_NO_DIAG;
+  }
+  FvIlu0* f = new FvIlu0();
+  f->n = n;
+  f->b = b;
+  f->nnzb = nnzb;
+  f->precision = precision;
+  Transpose T;
+  build_transpose(n, n, indptr, indices, &T);
+  std::vector<int> rows;
+  levels(n, true, [&](int i, auto&& use) {
+    for (int q = indptr[i]; q < diag[i]; ++q) use(indices[q]);
+  }, &rows, &f->lv_fwd);
+  if (upload(rows, &f->rows_fwd, s)) return FV_ERR_CUDA;
+  levels(n, false, [&](int i, auto&& use) {
+    for (int q = diag[i] + 1; q < indptr[i + 1]; ++q) use(indices[q]);
+  }, &rows, &f->lv_bwd);
+  if (upload(rows, &f->rows_bwd, s)) return FV_ERR_CUDA;
+  levels(n, true, [&](int i, auto&& use) {  // U^T: column i depends on rows j < i with (j, i)
+    for (int q = T.ptr[i]; q < T.ptr[i + 1]; ++q)
+      if (T.idx[q] < i) use(T.idx[q]);
+  }, &rows, &f->lv_tfwd);
+  if (upload(rows, &f->rows_tfwd, s)) return FV_ERR_CUDA;
+  levels(n, false, [&](int i, auto&& use) {  // L^T: column i depends on rows k > i with (k, i)
+    for (int q = T.ptr[i]; q < T.ptr[i + 1]; ++q)
+      if (T.idx[q] > i) use(T.idx[q]);
+  }, &rows, &f->lv_tbwd);
+  if (upload(rows, &f->rows_tbwd, s)) return FV_ERR_CUDA;
+  std::vector<int> hp(indptr, indptr + n + 1), hi(indices, indices + nnzb);
+  if (upload(hp, &f->ptr, s) || upload(hi, &f->idx, s) || upload(diag, &f->diag, s) ||
+      upload(T.ptr, &f->tptr, s) || upload(T.idx, &f->tidx, s) || upload(T.blk, &f->tblk, s))
+    return FV_ERR_CUDA;
+  size_t vs = precision == 64 ? sizeof(double) : sizeof(float);
+  FV_CUDA_TRY(cudaMalloc(&f->val, vs * (size_t)nnzb * b * b));
+  FV_CUDA_TRY(cudaMalloc(&f->zero_flag, sizeof(unsigned long long)));
+  FV_CUDA_TRY(cudaStreamSynchronize(s));
+  *out = f;
+  return FV_OK;
+}
+
+extern "C" int fv_ilu0_destroy(FvIlu0* f) {
+  if (!f) return FV_OK;
+  cudaFree(f->ptr);
+  cudaFree(f->idx);
+  cudaFree(f->diag);
+  cudaFree(f->tptr);
+  cudaFree(f->tidx);
+  cudaFree(f->tblk);
+  cudaFree(f->val);
+  cudaFree(f->zero_flag);
+  cudaFree(f->rows_fwd);
+  cudaFree(f->rows_bwd);
+  cudaFree(f->rows_tfwd);
+  cudaFree(f->rows_tbwd);
+  delete f;
+  return FV_OK;
+}
+
+extern "C" int fv_ilu0_factor(FvIlu0* f, const void* values, int values_f64, void* stream) {
+  if (!f || !values) {
+    fv_set_error("fv_ilu0_factor: bad arguments");
+    return FV_ERR_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  const long n = (long)f->nnzb * f->b * f->b;
+  if (f->precision == 64) {
+    FV_CUDA_TRY(cudaMemcpyAsync(f->val, values, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+    return ilu_factor<double>(f, s);
+  }
+  if (values_f64)
+    k_to_f32<<<fv_blocks(n, kThreads), kThreads, 0, s>>>(n, (const double*)values, (float*)f->val);
+  else
+    FV_CUDA_TRY(cudaMemcpyAsync(f->val, values, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+  return ilu_factor<float>(f, s);
+}
+
+extern "C" int fv_ilu0_apply(FvIlu0* f, const void* r, void* x, int transpose, void* stream) {
+  if (!f || !r || !x) {
+    fv_set_error("fv_ilu0_apply: bad arguments");
+    return FV_ERR_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  if (f->precision == 64) return ilu_apply<double>(f, (const double*)r, (double*)x, transpose, s);
+  return ilu_apply<float>(f, (const float*)r, (float*)x, transpose, s);
+}
+
+extern "C" int fv_ilu0_factor_values(const FvIlu0* f, void* out, void* stream) {
+  if (!f || !out) {
+    fv_set_error("fv_ilu0_factor_values: bad arguments");
+    return FV_ERR_ARG;
+  }
+  size_t vs = f->precision == 64 ? sizeof(double) : sizeof(float);
+  FV_CUDA_TRY(cudaMemcpyAsync(out, f->val, vs * (size_t)f->nnzb * f->b * f->b,
+                              cudaMemcpyDeviceToDevice, (cudaStream_t)stream));
+  return FV_OK;
+}
+
+// ------------------------------------------------------------------------------ SpMV entry points
+namespace {
+template <class V>
+int spmv(int nbr, int b, const int* indptr, const int* indices, const V* values, const V* x, V* y,
+         int transpose, cudaStream_t s) {
+  if (nbr <= 0 || b <= 0 || !indptr || !indices || !values || !x || !y) {
+    fv_set_error("fv_bsr_spmv: bad arguments");
+    return FV_ERR_ARG;
+  }
+  const long rows = (long)nbr * b;
+  if (!transpose) {
+    k_bsr_spmv<V><<<fv_blocks(rows, kThreads), kThreads, 0, s>>>(nbr, b, indptr, indices, values, x, y);
+    FV_CUDA_TRY(cudaGetLastError());
+    return FV_OK;
+  }
+  // transposed product: build the transpose map of the (device) pattern on the host once per call
+  std::vector<int> hp(nbr + 1);
+  FV_CUDA_TRY(cudaMemcpyAsync(hp.data(), indptr, sizeof(int) * (nbr + 1), cudaMemcpyDeviceToHost, s));
+  FV_CUDA_TRY(cudaStreamSynchronize(s));
+  std::vector<int> hi(hp[nbr]);
+  FV_CUDA_TRY(cudaMemcpy(hi.data(), indices, sizeof(int) * hp[nbr], cudaMemcpyDeviceToHost));
+  Transpose T;
+  build_transpose(nbr, nbr, hp.data(), hi.data(), &T);
+  int *tp, *ti, *tb;
+  if (upload(T.ptr, &tp, s) || upload(T.idx, &ti, s) || upload(T.blk, &tb, s)) return FV_ERR_CUDA;
+  k_bsr_spmv_t<V><<<fv_blocks(rows, kThreads), kThreads, 0, s>>>(nbr, b, tp, ti, tb, values, x, y);
+  FV_CUDA_TRY(cudaGetLastError());
+  FV_CUDA_TRY(cudaStreamSynchronize(s));
+  cudaFree(tp);
+  cudaFree(ti);
+  cudaFree(tb);
+  return FV_OK;
+}
+}  // namespace
+
+extern "C" int fv_bsr_spmv_f64(int nbr, int b, const int* indptr, const int* indices,
+                               const double* values, const double* x, double* y, int transpose,
+                               void* stream) {
+  return spmv<double>(nbr, b, indptr, indices, values, x, y, transpose, (cudaStream_t)stream);
+}
+extern "C" int fv_bsr_spmv_f32(int nbr, int b, const int* indptr, const int* indices,
+                               const float* values, const float* x, float* y, int transpose,
+                               void* stream) {
+  return spmv<float>(nbr, b, indptr, indices, values, x, y, transpose, (cudaStream_t)stream);
+}
+
+extern "C" int fv_dot_f64(long n, const double* x, const double* y, double* out, void* stream) {
+  if (n < 0 || !x || !y || !out) {
+    fv_set_error("fv_dot_f64: bad arguments");
+    return FV_ERR_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  if (!g_dot_parts) FV_CUDA_TRY(cudaMalloc(&g_dot_parts, sizeof(double) * kRedBlocks));
+  k_dot_partial<<<kRedBlocks, kThreads, 0, s>>>(n, x, y, g_dot_parts);
+  k_dot_final<<<1, kThreads, 0, s>>>(kRedBlocks, g_dot_parts, out);
+  FV_CUDA_TRY(cudaGetLastError());
+  return FV_OK;
+}

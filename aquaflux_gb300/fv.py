@@ -1,0 +1,200 @@
+"""Device handles over the C ABI: :class:`DeviceMesh` and :class:`FlowCase`.
+
+These own the library objects (``FvMesh``, ``FvCase``) and pass torch CUDA tensors to the kernels
+on torch's current stream.  Every call goes to ``libfvgb.so``; there is no CPU path.
+
+Boundary conditions are given per named patch, as in the reference's ``BoundaryConditions``
+(``aquaflux/boundary/collection.py:72-137``):
+
+* ``flow_bc``: ``{patch: ("wall",) | ("moving", U) | ("inlet", U) | ("outlet", p)}`` -- the
+  ``NoSlipWall`` / ``MovingWall`` / ``VelocityInlet`` / ``PressureOutlet`` closures of
+  ``aquaflux/flow/boundary.py:278-446``;
+* ``sst``: ``None`` or ``{"walls": [patches], "k": {patch: ("dirichlet", v) | ("zerograd",)},
+  "omega": {...}}`` -- ``SSTTurbulence.build``'s wall patches and scalar closures
+  (``aquaflux/turbulence/transport.py:198-243``).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from ._lib import FvCaseDesc, check, lib, ptr
+from .mesh import MeshData
+
+FLOW_KIND = {"wall": 0, "moving": 1, "inlet": 2, "outlet": 3}
+
+
+def _stream() -> int:
+    return int(torch.cuda.current_stream().cuda_stream)
+
+
+class DeviceMesh:
+    """A mesh resident on the GPU with its geometry (``Mesh`` + ``Mesh.geometry()``)."""
+
+    def __init__(self, mesh: MeshData):
+        mesh.validate()
+        self.mesh = mesh
+        self.dim, self.n_cells, self.n_faces = mesh.dim, mesh.n_cells, mesh.n_faces
+        h = ctypes.c_void_p()
+        nodes = np.ascontiguousarray(mesh.nodes, dtype=np.float64)
+        off = np.ascontiguousarray(mesh.fn_offsets, dtype=np.int32)
+        idx = np.ascontiguousarray(mesh.fn_indices, dtype=np.int32)
+        own = np.ascontiguousarray(mesh.owner, dtype=np.int32)
+        nb = np.ascontiguousarray(mesh.neighbour, dtype=np.int32)
+        check(lib().fv_mesh_create(mesh.dim, mesh.n_cells, mesh.n_faces, mesh.n_nodes, ptr(nodes),
+                                   ptr(off), ptr(idx), ptr(own), ptr(nb), _stream(),
+                                   ctypes.byref(h)))
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def geometry(self) -> dict:
+        """Face area / normal / centroid and cell volume / centroid (reference face order)."""
+        dev = torch.device("cuda")
+        F, C, D = self.n_faces, self.n_cells, self.dim
+        out = {"area": torch.empty(F, dtype=torch.float64, device=dev),
+               "normal": torch.empty(F, D, dtype=torch.float64, device=dev),
+               "face_centroid": torch.empty(F, D, dtype=torch.float64, device=dev),
+               "volume": torch.empty(C, dtype=torch.float64, device=dev),
+               "cell_centroid": torch.empty(C, D, dtype=torch.float64, device=dev)}
+        check(lib().fv_mesh_geometry(self._h, ptr(out["area"]), ptr(out["normal"]),
+                                     ptr(out["face_centroid"]), ptr(out["volume"]),
+                                     ptr(out["cell_centroid"]), _stream()))
+        return out
+
+    def set_nodes(self, nodes: torch.Tensor) -> None:
+        nodes = nodes.to(device="cuda", dtype=torch.float64).contiguous()
+        check(lib().fv_mesh_set_nodes(self._h, ptr(nodes), _stream()))
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                lib().fv_mesh_destroy(h)
+            except Exception:
+                pass
+
+
+def case_tables(mesh: MeshData, flow_bc: dict, sst: dict | None):
+    """Per-face boundary tables (reference face order) for ``fv_case_create``."""
+    F, D = mesh.n_faces, mesh.dim
+    kind = np.full(F, -1, dtype=np.int8)
+    vel = np.zeros((F, D))
+    pb = np.zeros(F)
+    for name, spec in flow_bc.items():
+        faces = np.asarray(mesh.patches[name], dtype=np.int64)
+        if np.any(mesh.neighbour[faces] >= 0):
+            raise ValueError(f"patch {name!r} contains interior faces")
+        kind[faces] = FLOW_KIND[spec[0]]
+        if spec[0] in ("moving", "inlet"):
+            vel[faces] = np.asarray(spec[1], dtype=float)
+        elif spec[0] == "outlet":
+            pb[faces] = float(spec[1])
+    t = {"flow_kind": kind, "flow_vel": vel, "flow_p": pb}
+    if sst is not None:
+        for fld in ("k", "omega"):
+            kk = np.full(F, -1, dtype=np.int8)
+            vv = np.zeros(F)
+            for name, spec in sst[fld].items():
+                faces = np.asarray(mesh.patches[name], dtype=np.int64)
+                kk[faces] = 0 if spec[0] == "dirichlet" else 1
+                if spec[0] == "dirichlet":
+                    vv[faces] = float(spec[1])
+            t[fld + "_kind"], t[fld + "_val"] = kk, vv
+        wall = np.zeros(F, dtype=np.uint8)
+        for name in sst["walls"]:
+            wall[np.asarray(mesh.patches[name], dtype=np.int64)] = 1
+        t["sst_wall"] = wall
+    return t
+
+
+class FlowCase:
+    """``MomentumContinuity`` (laminar) or ``CoupledRANS`` (k-omega SST) on the GPU.
+
+    Compact Green-Gauss gradients and first-order upwind advection; constant viscosity ``mu`` and
+    density ``rho``; optional pressure pin (``FixedValueCells`` on the continuity row).
+    """
+
+    def __init__(self, dmesh: DeviceMesh, *, mu: float, rho: float, flow_bc: dict,
+                 pressure_pin: int | None = None, pressure_pin_value: float = 0.0,
+                 sst: dict | None = None):
+        self.dmesh = dmesh
+        mesh = dmesh.mesh
+        self.dim, self.n_cells = mesh.dim, mesh.n_cells
+        self.turbulent = sst is not None
+        t = case_tables(mesh, flow_bc, sst)
+        desc = FvCaseDesc(1 if sst is not None else 0, float(mu), float(rho),
+                          -1 if pressure_pin is None else int(pressure_pin),
+                          float(pressure_pin_value))
+        h = ctypes.c_void_p()
+        arrs = [np.ascontiguousarray(t.get(k)) if t.get(k) is not None else None
+                for k in ("flow_kind", "flow_vel", "flow_p", "k_kind", "k_val", "omega_kind",
+                          "omega_val", "sst_wall")]
+        check(lib().fv_case_create(dmesh.handle, ctypes.byref(desc), *[ptr(a) for a in arrs],
+                                   _stream(), ctypes.byref(h)))
+        self._h = h
+        self._keep = arrs
+        self.n_unknowns = int(lib().fv_case_n_unknowns(h))
+        self.mu, self.rho, self.inlet_scale = float(mu), float(rho), 1.0
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_params(self, mu: float | None = None, inlet_scale: float | None = None) -> None:
+        if mu is not None:
+            self.mu = float(mu)
+        if inlet_scale is not None:
+            self.inlet_scale = float(inlet_scale)
+        check(lib().fv_case_set_params(self._h, self.mu, self.inlet_scale))
+
+    def _vec(self, x) -> torch.Tensor:
+        x = torch.as_tensor(x, dtype=torch.float64, device="cuda").contiguous()
+        if x.shape != (self.n_unknowns,):
+            raise ValueError(f"expected a state of shape ({self.n_unknowns},), got {tuple(x.shape)}")
+        return x
+
+    def residual(self, state, out: torch.Tensor | None = None) -> torch.Tensor:
+        s = self._vec(state)
+        r = torch.empty_like(s) if out is None else out
+        check(lib().fv_residual(self._h, ptr(s), ptr(r), _stream()))
+        return r
+
+    def jvp(self, state, v, *, return_residual: bool = False):
+        s, vv = self._vec(state), self._vec(v)
+        jv = torch.empty_like(s)
+        r = torch.empty_like(s) if return_residual else None
+        check(lib().fv_jvp(self._h, ptr(s), ptr(vv), ptr(r), ptr(jv), _stream()))
+        return (r, jv) if return_residual else jv
+
+    def jvp_shift(self, state, v, shift) -> torch.Tensor:
+        s, vv, sh = self._vec(state), self._vec(v), self._vec(shift)
+        jv = torch.empty_like(s)
+        check(lib().fv_jvp_shift(self._h, ptr(s), ptr(vv), ptr(sh), ptr(jv), _stream()))
+        return jv
+
+    def param_jvp(self, state):
+        """``(dR/dmu, dR/d inlet_scale)`` at ``state``."""
+        s = self._vec(state)
+        a, b = torch.empty_like(s), torch.empty_like(s)
+        check(lib().fv_param_jvp(self._h, ptr(s), ptr(a), ptr(b), _stream()))
+        return a, b
+
+    def wall_distance(self):
+        C, D = self.n_cells, self.dim
+        d = torch.empty(C, dtype=torch.float64, device="cuda")
+        g = torch.empty(C, D, dtype=torch.float64, device="cuda")
+        check(lib().fv_case_wall_distance(self._h, ptr(d), ptr(g), _stream()))
+        return d, g
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                lib().fv_case_destroy(h)
+            except Exception:
+                pass

@@ -1,0 +1,161 @@
+/* fvgb.h -- C ABI of the GB300 finite-volume hot path (libfvgb.so).
+ *
+ * A drop-in for the data-parallel path of the reference solver: the cell-centred finite-volume
+ * residual R(state, params) of the coupled Rhie-Chow (u, v[, w], p) system with optional
+ * k-omega SST, its Jacobian-vector product, and the block-sparse SpMV / zero-fill ILU(0) the
+ * Newton-Krylov driver applies.
+ *
+ * Conventions
+ *  - Every entry point returns an int status (FV_OK = 0); fv_last_error() gives the message.
+ *  - Array arguments documented "device" are CUDA device pointers owned by the caller; "host"
+ *    arrays are read once during the call.  Index arrays are int32, values float64 unless stated.
+ *  - `stream` is a cudaStream_t passed as void* (NULL = the legacy default stream).  All device
+ *    work is stream-ordered; no entry point synchronizes the host except the *_create calls.
+ *  - State vectors are field-major, [u(C), v(C), (w(C)), p(C), (k(C), omega(C))], the layout of
+ *    aquaflux/flow/state.py:36-69 and aquaflux/turbulence/coupled.py:239-269.
+ *  - Faces are identified by their index in the caller's (reference) face order.
+ *  - Handles are not thread-safe across concurrent streams.  Evaluation calls allocate nothing.
+ */
+#ifndef FVGB_H
+#define FVGB_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  FV_OK = 0,
+  FV_ERR_ARG = 1,        /* bad argument / shape (reference: ValueError) */
+  FV_ERR_CUDA = 2,       /* a CUDA runtime call failed */
+  FV_ERR_NO_DIAG = 3,    /* ILU(0): a row stores no diagonal entry (reference: ValueError) */
+  FV_ERR_ZERO_PIVOT = 4, /* ILU(0): exactly zero pivot (reference: ZeroDivisionError) */
+  FV_ERR_NONFINITE = 5,  /* a non-finite value where a finite one is required */
+  FV_ERR_NOT_CONVERGED = 6,
+  FV_ERR_TIMEOUT = 7
+};
+
+/* Last error message of the calling thread ("" if none). */
+const char* fv_last_error(void);
+/* Row / index associated with the last FV_ERR_NO_DIAG / FV_ERR_ZERO_PIVOT (else -1). */
+long fv_last_error_index(void);
+/* Library version string. */
+const char* fv_version(void);
+
+/* ------------------------------------------------------------------------------------------
+ * Mesh.  Replaces Mesh.from_csr + Mesh.geometry (aquaflux/mesh/mesh.py:137-206, 341-387):
+ * uploads the connectivity, renumbers faces internally by owner for coalesced gathers, builds the
+ * cell->face incidence used for deterministic face-to-cell sums, and computes the geometry on the
+ * GPU (edge / centre-fan face geometry, owner-outward normals, recentred divergence-theorem
+ * cell volume and centroid).
+ * ------------------------------------------------------------------------------------------ */
+typedef struct FvMesh FvMesh;
+
+int fv_mesh_create(int dim, int n_cells, int n_faces, int n_nodes,
+                   const double* nodes,      /* host (n_nodes, dim) row-major */
+                   const int* fn_offsets,    /* host (n_faces + 1) CSR pointers */
+                   const int* fn_indices,    /* host (fn_offsets[n_faces]) node indices */
+                   const int* owner,         /* host (n_faces) */
+                   const int* neighbour,     /* host (n_faces), -1 = boundary face */
+                   void* stream, FvMesh** out);
+int fv_mesh_destroy(FvMesh* mesh);
+/* Replace the node coordinates (device (n_nodes, dim) row-major) and recompute the geometry. */
+int fv_mesh_set_nodes(FvMesh* mesh, const double* nodes_device, void* stream);
+/* Copy the geometry out in reference face order, device outputs (any may be NULL):
+ * area (F), normal (F, dim), face_centroid (F, dim), volume (C), cell_centroid (C, dim). */
+int fv_mesh_geometry(const FvMesh* mesh, double* area, double* normal, double* face_centroid,
+                     double* volume, double* cell_centroid, void* stream);
+int fv_mesh_sizes(const FvMesh* mesh, int* dim, int* n_cells, int* n_faces, int* n_nodes);
+
+/* ------------------------------------------------------------------------------------------
+ * Case.  Replaces MomentumContinuity.build (aquaflux/flow/momentum.py:233-293) and, with
+ * turbulent = 1, SSTTurbulence.build + CoupledRANS.build (aquaflux/turbulence/transport.py:198-243,
+ * coupled.py:311-340).  Schemes: compact Green-Gauss gradients, first-order upwind advection.
+ * Boundary tables are per face in reference face order (entries of interior faces ignored):
+ *   flow_kind: -1 none, 0 NoSlipWall, 1 MovingWall, 2 VelocityInlet, 3 PressureOutlet
+ *   flow_vel (F, dim): the MovingWall / VelocityInlet velocity;  flow_p (F): outlet pressure
+ *   k_kind / omega_kind: -1 none, 0 Dirichlet (value in *_val), 1 ZeroGradient
+ *   sst_wall (F): 1 on faces of the SST wall patches (wall distance, wall functions)
+ * ------------------------------------------------------------------------------------------ */
+typedef struct FvCase FvCase;
+
+typedef struct FvCaseDesc {
+  int turbulent;             /* 0: MomentumContinuity, 1: CoupledRANS (direct k, omega) */
+  double mu;                 /* molecular dynamic viscosity (Constant) */
+  double rho;                /* density (Constant) */
+  int pressure_pin;          /* cell index whose pressure row is fixed, -1 for none */
+  double pressure_pin_value;
+} FvCaseDesc;
+
+int fv_case_create(const FvMesh* mesh, const FvCaseDesc* desc,
+                   const signed char* flow_kind, const double* flow_vel, const double* flow_p,
+                   const signed char* k_kind, const double* k_val,
+                   const signed char* omega_kind, const double* omega_val,
+                   const unsigned char* sst_wall, void* stream, FvCase** out);
+int fv_case_destroy(FvCase* c);
+/* Change the differentiable physical parameters: molecular viscosity and a factor applied to
+ * every prescribed inlet velocity.  Takes effect for later calls on `stream`. */
+int fv_case_set_params(FvCase* c, double mu, double inlet_scale);
+/* Device copies (C) and (C, dim) of the SST wall distance and its gradient (turbulent cases). */
+int fv_case_wall_distance(const FvCase* c, double* distance, double* gradient, void* stream);
+/* Number of unknowns: (dim + 1) * C, or (dim + 3) * C when turbulent. */
+long fv_case_n_unknowns(const FvCase* c);
+
+/* R = residual(state).  MomentumContinuity.residual (aquaflux/flow/momentum.py:880) or
+ * CoupledRANS.residual (aquaflux/turbulence/coupled.py:437).  Device in/out. */
+int fv_residual(FvCase* c, const double* state, double* residual, void* stream);
+/* jv = J(state) v, the directional derivative jax.jvp(R, (state,), (v,)) of
+ * aquaflux/solve/newton.py:110-111.  `residual` (may be NULL) receives R(state).  Device. */
+int fv_jvp(FvCase* c, const double* state, const double* v, double* residual, double* jv,
+           void* stream);
+/* jv = J v + shift * v (the pseudo-transient operator of aquaflux/solve/continuation.py:111-112);
+ * `shift` is a device vector of the state's length. */
+int fv_jvp_shift(FvCase* c, const double* state, const double* v, const double* shift, double* jv,
+                 void* stream);
+/* Directional derivative of the residual with respect to the scalar parameters:
+ * out_mu = dR/dmu, out_inlet = dR/d(inlet_scale) (either may be NULL).  Device. */
+int fv_param_jvp(FvCase* c, const double* state, double* out_mu, double* out_inlet, void* stream);
+
+/* ------------------------------------------------------------------------------------------
+ * Block-sparse (BSR, b x b dense blocks, row-major inside a block) operators.
+ * Replaces _CsrOperator.apply (aquaflux/solve/multigrid.py:1302-1390).
+ * ------------------------------------------------------------------------------------------ */
+/* y = A x (transpose = 0) or y = A^T x (transpose = 1); fp64. Device arrays. */
+int fv_bsr_spmv_f64(int n_block_rows, int b, const int* indptr, const int* indices,
+                    const double* values, const double* x, double* y, int transpose,
+                    void* stream);
+/* fp32 values and vectors. */
+int fv_bsr_spmv_f32(int n_block_rows, int b, const int* indptr, const int* indices,
+                    const float* values, const float* x, float* y, int transpose, void* stream);
+
+/* ------------------------------------------------------------------------------------------
+ * Zero-fill ILU(0) over a BSR pattern.  Replaces Ilu0 (aquaflux/solve/ilu0.py:153-255) and the
+ * compiled kernel aquaflux/solve/_ilu0.pyx (diagonal_positions :35-65, factor :68-121, solve
+ * :124-147, solve_transpose :150-178).  With b = 1 it is the reference's scalar CSR ILU(0); with
+ * b > 1 the b x b blocks are dense and the elimination is the same scalar ILU(0) over the
+ * block-expanded pattern (cell-major interleaved ordering, aquaflux/solve/ordering.py:195-242).
+ * Rows are eliminated in level-set order on the GPU, which reproduces the sequential result.
+ * ------------------------------------------------------------------------------------------ */
+typedef struct FvIlu0 FvIlu0;
+
+/* Analyse the pattern (host CSR/BSR arrays, sorted column indices); precision: 32 or 64. */
+int fv_ilu0_create(int n_block_rows, int b, const int* indptr, const int* indices, int precision,
+                   void* stream, FvIlu0** out);
+int fv_ilu0_destroy(FvIlu0* f);
+/* Numeric factorization of new values (device, nnzb * b * b, same dtype as `precision`, or
+ * float64 when values_f64 != 0 and precision == 32: converted on the fly). */
+int fv_ilu0_factor(FvIlu0* f, const void* values, int values_f64, void* stream);
+/* x = (LU)^-1 r, or (LU)^-T r when transpose != 0.  Device vectors of `precision`. */
+int fv_ilu0_apply(FvIlu0* f, const void* r, void* x, int transpose, void* stream);
+/* Copy the factor (device, nnzb * b * b, `precision`) -- combined L (unit diagonal) and U. */
+int fv_ilu0_factor_values(const FvIlu0* f, void* out, void* stream);
+
+/* ------------------------------------------------------------------------------------------
+ * Deterministic reductions for the Krylov solver (fixed blocking, fixed order: run-to-run
+ * bit-identical).  Device arrays; `out` is a device scalar.
+ * ------------------------------------------------------------------------------------------ */
+int fv_dot_f64(long n, const double* x, const double* y, double* out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FVGB_H */

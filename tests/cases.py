@@ -71,3 +71,32 @@ def oracle_case(name: str):
     fb, sst = sst_spec(spec["dim"], spec["nu"], float(k_in), float(w_in), spec["walls"])
     case = fo.make_case(mesh, mu=spec["nu"], rho=1.0, flow_bc=fb, sst=sst)
     return case, d, spec["prefix"]
+
+
+def mesh_data(d: dict, prefix: str):
+    """The fixture mesh as the package's :class:`MeshData`."""
+    from aquaflux_gb300.mesh import MeshData
+
+    ns = mesh_from(d, prefix)
+    return MeshData(nodes=np.ascontiguousarray(ns.nodes, dtype=np.float64),
+                    fn_offsets=ns.fn_offsets.astype(np.int32), fn_indices=ns.fn_indices.astype(np.int32),
+                    owner=ns.owner.astype(np.int32), neighbour=ns.neighbour.astype(np.int32),
+                    n_cells=int(ns.n_cells), patches={k: v.astype(np.int32) for k, v in ns.patches.items()})
+
+
+def device_case(name: str):
+    """(FlowCase on the GPU, oracle case dict, fixture dict, prefix) for a golden case."""
+    from aquaflux_gb300 import fv
+
+    case, d, p = oracle_case(name)
+    m = mesh_data(d, p)
+    dm = fv.DeviceMesh(m)
+    if name in LAMINAR:
+        spec = LAMINAR[name]
+        fc = fv.FlowCase(dm, mu=spec["mu"], rho=1.0, flow_bc=spec["bc"], pressure_pin=spec["pin"])
+    else:
+        spec = SST[name]
+        k_in, w_in = d[p + "inlet"]
+        fb, sst = sst_spec(spec["dim"], spec["nu"], float(k_in), float(w_in), spec["walls"])
+        fc = fv.FlowCase(dm, mu=spec["nu"], rho=1.0, flow_bc=fb, sst=sst)
+    return fc, case, d, p

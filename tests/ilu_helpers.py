@@ -1,0 +1,83 @@
+"""ctypes access to the CPU ILU(0) checkers (C restatement, and the reference's own kernel)."""
+from __future__ import annotations
+
+import ctypes
+import glob
+import importlib.util
+import os
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def c_oracle():
+    path = os.path.join(ROOT, "oracle", "libilu0_oracle.so")
+    if not os.path.exists(path):
+        import subprocess
+        import sys
+
+        subprocess.run([sys.executable, os.path.join(ROOT, "oracle", "build_oracle.py")], check=True)
+    return ctypes.CDLL(path)
+
+
+def reference_kernel():
+    """The reference's compiled ``_ilu0`` module built into ``oracle/_ref``, or None."""
+    hits = glob.glob(os.path.join(ROOT, "oracle", "_ref", "_ilu0*.so"))
+    if not hits:
+        return None
+    spec = importlib.util.spec_from_file_location("_ilu0", hits[0])
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def oracle_factor_solve(indptr, indices, values, rhs):
+    """(diag, factor, solve, solve_transpose) from the C oracle; raises like the reference."""
+    L = c_oracle()
+    n = len(indptr) - 1
+    ip = np.ascontiguousarray(indptr, dtype=np.int32)
+    ix = np.ascontiguousarray(indices, dtype=np.int32)
+    diag = np.zeros(n, dtype=np.int32)
+    bad = ctypes.c_int(-1)
+    rc = L.ilu0_diagonal_positions(_p(ip), _p(ix), n, _p(diag), ctypes.byref(bad))
+    if rc == 3:
+        raise ValueError(f"row {bad.value} stores no diagonal entry")
+    data = np.array(values, dtype=np.float64)
+    rc = L.ilu0_factor(_p(ip), _p(ix), _p(data), _p(diag), n, ctypes.byref(bad))
+    if rc == 4:
+        raise ZeroDivisionError(f"ILU(0) met an exactly zero pivot at row {bad.value}")
+    x = np.array(rhs, dtype=np.float64)
+    L.ilu0_solve(_p(ip), _p(ix), _p(data), _p(diag), _p(x), n)
+    xt = np.array(rhs, dtype=np.float64)
+    L.ilu0_solve_transpose(_p(ip), _p(ix), _p(data), _p(diag), _p(xt), n)
+    return diag, data, x, xt
+
+
+def cell_major(indptr, indices, values, n_cells, n_fields):
+    """Permute a field-major operator to the cell-major interleaved order (cell * nf + field)."""
+    import scipy.sparse as sp
+
+    n = n_cells * n_fields
+    a = sp.csr_matrix((values, indices, indptr), shape=(n, n))
+    old = np.arange(n)
+    new = (old % n_cells) * n_fields + old // n_cells
+    perm = np.empty(n, dtype=np.int64)
+    perm[new] = old
+    b = a[perm][:, perm].tocsr()
+    b.sort_indices()
+    return b.indptr.astype(np.int32), b.indices.astype(np.int32), b.data.astype(np.float64)
+
+
+def to_bsr(indptr, indices, values, b):
+    """Scalar CSR with block-dense b x b structure -> BSR (row-major blocks)."""
+    import scipy.sparse as sp
+
+    n = len(indptr) - 1
+    a = sp.csr_matrix((values, indices, indptr), shape=(n, n)).tobsr(blocksize=(b, b))
+    a.sort_indices()
+    return a.indptr.astype(np.int32), a.indices.astype(np.int32), a.data.reshape(-1).astype(np.float64)

@@ -1,0 +1,124 @@
+"""CUDA BSR SpMV and ILU(0) against the CPU oracle (bitwise in fp64) and the reference fixture."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import torch
+
+from tests.cases import golden
+from tests.ilu_helpers import cell_major, oracle_factor_solve, to_bsr
+
+pytestmark = pytest.mark.gpu
+
+
+def _dev(a, dtype=None):
+    t = torch.as_tensor(np.asarray(a))
+    return t.to("cuda", dtype=dtype) if dtype is not None else t.to("cuda")
+
+
+def test_scalar_ilu0_fp64_bitwise_equals_oracle():
+    from aquaflux_gb300.ilu0 import Ilu0
+
+    d = golden("ilu0")
+    ip, ix, vals, rhs = d["ilu_indptr"], d["ilu_indices"], d["ilu_values"], d["ilu_rhs"]
+    _, data, x, xt = oracle_factor_solve(ip, ix, vals, rhs)
+    f = Ilu0.from_csr(ip, ix, vals, block_size=1, precision=64)
+    np.testing.assert_array_equal(f.factor_values().cpu().numpy(), data)
+    np.testing.assert_array_equal(f.solve(rhs).cpu().numpy(), x)
+    np.testing.assert_array_equal(f.solve(rhs, transpose=True).cpu().numpy(), xt)
+
+
+def test_block_ilu0_fp64_bitwise_equals_scalar_on_cell_major_order():
+    from aquaflux_gb300.ilu0 import Ilu0
+
+    d = golden("ilu0")
+    ip, ix, vals = cell_major(d["ilu_indptr"], d["ilu_indices"], d["ilu_values"], 40, 3)
+    rhs = d["ilu_rhs"]
+    _, data, x, xt = oracle_factor_solve(ip, ix, vals, rhs)
+    bp, bi, bv = to_bsr(ip, ix, vals, 3)
+    f = Ilu0.from_csr(bp, bi, bv, block_size=3, precision=64)
+    # the block factor, read back through the scalar pattern, equals the scalar factor
+    sp_ip, sp_ix, sp_data = to_scalar(bp, bi, f.factor_values().cpu().numpy(), 3)
+    np.testing.assert_array_equal(sp_ip, ip)
+    np.testing.assert_array_equal(sp_ix, ix)
+    np.testing.assert_array_equal(sp_data, data)
+    np.testing.assert_array_equal(f.solve(rhs).cpu().numpy(), x)
+    np.testing.assert_array_equal(f.solve(rhs, transpose=True).cpu().numpy(), xt)
+
+
+def to_scalar(bp, bi, bv, b):
+    import scipy.sparse as sp
+
+    n = (len(bp) - 1) * b
+    a = sp.bsr_matrix((bv.reshape(-1, b, b), bi, bp), shape=(n, n)).tocsr()
+    a.sort_indices()
+    return a.indptr.astype(np.int32), a.indices.astype(np.int32), a.data
+
+
+def test_fp32_ilu0_close_to_fp64():
+    from aquaflux_gb300.ilu0 import Ilu0
+
+    d = golden("ilu0")
+    ip, ix, vals = cell_major(d["ilu_indptr"], d["ilu_indices"], d["ilu_values"], 40, 3)
+    bp, bi, bv = to_bsr(ip, ix, vals, 3)
+    f64 = Ilu0.from_csr(bp, bi, bv, block_size=3, precision=64)
+    f32 = Ilu0.from_csr(bp, bi, bv, block_size=3, precision=32)
+    rhs = d["ilu_rhs"]
+    a = f64.solve(rhs).cpu().numpy()
+    b = f32.solve(rhs).cpu().numpy()
+    assert np.abs(a - b).max() <= 1e-5 * np.abs(a).max()
+
+
+def test_transpose_identity():
+    """<y, M r> = <M^T y, r> (tests/unit/test_ilu0.py:92-107)."""
+    from aquaflux_gb300.ilu0 import Ilu0
+
+    d = golden("ilu0")
+    f = Ilu0.from_csr(d["ilu_indptr"], d["ilu_indices"], d["ilu_values"], block_size=1)
+    rng = np.random.default_rng(1)
+    y, r = rng.standard_normal((2, len(d["ilu_rhs"])))
+    lhs = float(np.dot(y, f.solve(r).cpu().numpy()))
+    rhs = float(np.dot(f.solve(y, transpose=True).cpu().numpy(), r))
+    assert abs(lhs - rhs) <= 1e-12 * abs(lhs)
+
+
+def test_missing_diagonal_and_zero_pivot_raise_like_the_reference():
+    from aquaflux_gb300.ilu0 import Ilu0
+
+    with pytest.raises(ValueError, match="store no diagonal entry"):
+        Ilu0.from_csr(np.array([0, 1, 2]), np.array([0, 0]), np.array([1.0, 2.0]), block_size=1)
+    with pytest.raises(ZeroDivisionError, match="zero pivot at row 0"):
+        Ilu0.from_csr(np.array([0, 2, 4]), np.array([0, 1, 0, 1]), np.array([0.0, 1.0, 1.0, 1.0]),
+                      block_size=1)
+
+
+@pytest.mark.parametrize("b", [1, 3, 6])
+@pytest.mark.parametrize("transpose", [False, True])
+def test_bsr_spmv_matches_scipy(b, transpose):
+    import scipy.sparse as sp
+
+    from aquaflux_gb300.sparse import bsr_spmv
+
+    rng = np.random.default_rng(b)
+    nb = 50
+    a = sp.random(nb, nb, density=0.1, random_state=b, format="csr") + sp.eye(nb)
+    a.sort_indices()
+    vals = rng.standard_normal((a.nnz, b, b))
+    dense = sp.bsr_matrix((vals, a.indices, a.indptr), shape=(nb * b, nb * b))
+    x = rng.standard_normal(nb * b)
+    want = (dense.T if transpose else dense) @ x
+    got = bsr_spmv(a.indptr, a.indices, vals.reshape(-1), b, x, transpose=transpose)
+    np.testing.assert_allclose(got.cpu().numpy(), want, rtol=1e-12, atol=1e-12)
+    got32 = bsr_spmv(a.indptr, a.indices, vals.reshape(-1).astype(np.float32), b,
+                     x.astype(np.float32), transpose=transpose)
+    np.testing.assert_allclose(got32.cpu().numpy(), want, rtol=1e-4, atol=1e-4)
+
+
+def test_dot_is_deterministic():
+    from aquaflux_gb300.sparse import dot
+
+    x = torch.randn(1_000_003, dtype=torch.float64, device="cuda")
+    y = torch.randn(1_000_003, dtype=torch.float64, device="cuda")
+    a, b = dot(x, y), dot(x, y)
+    assert float(a) == float(b)
+    assert abs(float(a) - float(torch.dot(x, y))) <= 1e-10 * float(torch.dot(x.abs(), y.abs()))
