@@ -40,6 +40,8 @@ SIGNATURES = {
     "fv_case_set_params": (c_int, [P, c_double, c_double]),
     "fv_case_wall_distance": (c_int, [P, P, P, P]),
     "fv_case_n_unknowns": (c_long, [P]),
+    "fv_case_profile_begin": (c_int, [P, c_int]),
+    "fv_case_profile_end": (c_int, [P, P, c_int, P]),
     "fv_residual": (c_int, [P, P, P, P]),
     "fv_jvp": (c_int, [P, P, P, P, P, P]),
     "fv_jvp_shift": (c_int, [P, P, P, P, P, P]),

@@ -230,3 +230,47 @@ extern "C" int fv_param_jvp(FvCase* c, const double* state, double* out_mu, doub
   }
   return FV_OK;
 }
+
+// ------------------------------------------------------------------------------ profiling
+void fv_prof_mark(FvCase* c, int k, cudaStream_t s) {
+  if (c->prof_max_runs == 0 || c->prof_runs >= c->prof_max_runs) return;
+  if (k + 1 > c->prof_stages) c->prof_stages = k + 1;
+  cudaEventRecord(c->prof_events[(size_t)c->prof_runs * (FV_MAX_STAGES + 1) + k], s);
+  if (k == 6) c->prof_runs++;  // the last boundary of a pipeline run
+}
+
+extern "C" int fv_case_profile_begin(FvCase* c, int max_runs) {
+  if (!c || max_runs <= 0 || max_runs > 4096) {
+    fv_set_error("fv_case_profile_begin: bad arguments");
+    return FV_ERR_ARG;
+  }
+  for (cudaEvent_t e : c->prof_events) cudaEventDestroy(e);
+  c->prof_events.assign((size_t)max_runs * (FV_MAX_STAGES + 1), nullptr);
+  for (auto& e : c->prof_events) FV_CUDA_TRY(cudaEventCreate(&e));
+  c->prof_max_runs = max_runs;
+  c->prof_runs = 0;
+  c->prof_stages = 0;
+  return FV_OK;
+}
+
+extern "C" int fv_case_profile_end(FvCase* c, float* stage_ms, int n_stages, int* n_runs) {
+  if (!c || !stage_ms || n_stages <= 0) {
+    fv_set_error("fv_case_profile_end: bad arguments");
+    return FV_ERR_ARG;
+  }
+  for (int k = 0; k < n_stages; ++k) stage_ms[k] = 0.0f;
+  for (int r = 0; r < c->prof_runs; ++r) {
+    cudaEvent_t* ev = &c->prof_events[(size_t)r * (FV_MAX_STAGES + 1)];
+    FV_CUDA_TRY(cudaEventSynchronize(ev[c->prof_stages - 1]));
+    for (int k = 0; k + 1 < c->prof_stages && k < n_stages; ++k) {
+      float ms = 0.0f;
+      FV_CUDA_TRY(cudaEventElapsedTime(&ms, ev[k], ev[k + 1]));
+      stage_ms[k] += ms;
+    }
+  }
+  if (n_runs) *n_runs = c->prof_runs;
+  for (cudaEvent_t e : c->prof_events) cudaEventDestroy(e);
+  c->prof_events.clear();
+  c->prof_max_runs = c->prof_runs = c->prof_stages = 0;
+  return FV_OK;
+}

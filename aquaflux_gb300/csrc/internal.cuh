@@ -103,7 +103,13 @@ struct FvCase {
   size_t work_bytes = 0;
   double* tmp = nullptr;    // (n_unknowns) scratch vector
   CaseView view;
+  // optional per-stage CUDA-event profiling (fv_case_profile_begin / _end)
+  std::vector<cudaEvent_t> prof_events;  // max_runs * (FV_MAX_STAGES + 1)
+  int prof_max_runs = 0, prof_runs = 0, prof_stages = 0;
 };
+#define FV_MAX_STAGES 8
+// Record the stage boundary `k` of the current profiled run (no-op when profiling is off).
+void fv_prof_mark(FvCase* c, int k, cudaStream_t s);
 
 int fv_case_run(FvCase* c, const double* state, const double* tangent, int tangent_kind,
                 double* residual, double* jv, cudaStream_t s);

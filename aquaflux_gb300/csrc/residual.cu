@@ -628,12 +628,19 @@ int run(FvCase* cs, Src<T> st, Par<T> par, double* R, double* JV, cudaStream_t s
   T* FL = dco + nc;
   constexpr int TB = 128;
   const int bc = fv_blocks(nc, TB), bf = fv_blocks(nf, TB);
+  fv_prof_mark(cs, 0, s);
   k_grad<T, DIM, TURB><<<bc, TB, 0, s>>>(m, cv, st, par, G);
+  fv_prof_mark(cs, 1, s);
   if (TURB) k_closure<T, DIM><<<bc, TB, 0, s>>>(m, cv, st, par, G, cl, Gwi);
+  fv_prof_mark(cs, 2, s);
   k_apcoef<T, DIM, TURB><<<bf, TB, 0, s>>>(m, cv, st, par, G, cl, acown, acnb);
+  fv_prof_mark(cs, 3, s);
   k_dcoeff<T><<<bc, TB, 0, s>>>(m, acown, acnb, dco);
+  fv_prof_mark(cs, 4, s);
   k_flux<T, DIM, TURB><<<bf, TB, 0, s>>>(m, cv, st, par, G, cl, dco, FL);
+  fv_prof_mark(cs, 5, s);
   k_sum<T, DIM, TURB><<<bc, TB, 0, s>>>(m, cv, st, par, FL, cl, G, Gwi, R, JV);
+  fv_prof_mark(cs, 6, s);
   FV_CUDA_TRY(cudaGetLastError());
   return FV_OK;
 }

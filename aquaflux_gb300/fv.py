@@ -184,6 +184,18 @@ class FlowCase:
         check(lib().fv_param_jvp(self._h, ptr(s), ptr(a), ptr(b), _stream()))
         return a, b
 
+    STAGES = ("grad", "closure", "apcoef", "dcoeff", "flux", "sum")
+
+    def profile_begin(self, max_runs: int) -> None:
+        check(lib().fv_case_profile_begin(self._h, int(max_runs)))
+
+    def profile_end(self) -> tuple[dict, int]:
+        """Summed per-stage milliseconds of the profiled runs, and the run count."""
+        ms = (ctypes.c_float * len(self.STAGES))()
+        n = ctypes.c_int(0)
+        check(lib().fv_case_profile_end(self._h, ms, len(self.STAGES), ctypes.byref(n)))
+        return {k: float(ms[i]) for i, k in enumerate(self.STAGES)}, int(n.value)
+
     def wall_distance(self):
         C, D = self.n_cells, self.dim
         d = torch.empty(C, dtype=torch.float64, device="cuda")

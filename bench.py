@@ -1,0 +1,339 @@
+"""Benchmark of the finite-volume hot path on GB300.
+
+Workload: the 2,097,152-cell 3D channel with a bump, coupled (u, v, w, p) + k-omega SST
+(``aquaflux_gb300.workloads.channel3d(128)``: 6,340,608 faces, seeded bump / jitter, randomly
+permuted then RCM-renumbered cells).  One step = one evaluation of the residual and its
+Jacobian-vector product at a fixed state (the operator applied every Krylov iteration of the
+Newton solve).  ``value`` is faces processed per second (Gfaces/s) with inputs resident in HBM;
+``e2e`` is the same step through the C ABI with host (pinned) inputs / outputs copied inside the
+timed region.
+
+``--impl reference`` times the reference algorithm on the host CPU instead (the float64 CPU
+oracle restating the reference's residual, autograd JVP, all host threads) on a bounded sample of
+the same workload.
+
+Run: ``python bench.py [--gpus N] [--steps K] [--warmup W] [--size 128]``.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Newton-solve s & residual+VJP Gfaces/s at 2M cells: FP32-precond vs FP64, 1 GB300"
+UNIT = "Gfaces/s"
+CLOCK_QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+
+def _args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--size", type=int, default=128, help="cells per axis of the 3D channel")
+    ap.add_argument("--cpu-sample", type=int, default=24, help="cells per axis of the CPU sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+# ----------------------------------------------------------------------------- clocks
+class ClockSampler:
+    """``nvidia-smi`` sampled every 200 ms while the timed region runs."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={CLOCK_QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        rows = []
+        if self.path and os.path.exists(self.path):
+            for line in open(self.path):
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+            os.remove(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        power = [float(r[3]) for r in rows if r[3].replace(".", "").isdigit()]
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": reasons,
+                "samples": len(rows), "power_w_max": max(power) if power else None}
+
+
+# ----------------------------------------------------------------------------- algorithmic bytes
+def step_bytes_per_face(wl) -> float:
+    """Compulsory bytes of one residual + JVP evaluation per face.
+
+    Per face: owner + neighbour indices (8 B) and the area vector and centroid (2 dim 8 B).  Per
+    cell: the state and its tangent (2 n_f 8 B), centroid (dim 8 B), volume (8 B), wall distance
+    (8 B, SST) in; residual and J v (2 n_f 8 B) out.  Each distinct value counted once.
+    """
+    m = wl.mesh
+    dim, nf = m.dim, m.dim + (3 if wl.sst else 1)
+    per_face = 8 + 2 * dim * 8
+    per_cell = 2 * nf * 8 + dim * 8 + 8 + (8 if wl.sst else 0) + 2 * nf * 8
+    return per_face + per_cell * m.n_cells / m.n_faces
+
+
+def flux_kernel_bytes(wl) -> float:
+    """Compulsory bytes of one launch of the dual-number face-flux kernel (``k_flux<Dual>``).
+
+    Per face: indices (8 B), the geometric factors it reads (area, normal, g, normal distance,
+    dpn, dnn, n.n, d, skew, tP, tN: 5 + 6 dim doubles) and the n_f dual fluxes written (16 B each);
+    per cell: the n_f dual state values, n_f * dim dual gradients, the dual d-coefficient and (SST)
+    the dual F1 and nu_t, each read once.
+    """
+    m = wl.mesh
+    dim, nf = m.dim, m.dim + (3 if wl.sst else 1)
+    per_face = 8 + (6 + 6 * dim) * 8 + nf * 16
+    per_cell = (nf + nf * dim + 1 + (2 if wl.sst else 0)) * 16
+    return m.n_faces * per_face + m.n_cells * per_cell
+
+
+def measured_peaks() -> dict:
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+# ----------------------------------------------------------------------------- CPU reference
+def cpu_residual_jvp_rate(size: int, min_seconds: float = 8.0) -> dict:
+    """Faces/s of the float64 CPU oracle (the reference algorithm restated; residual + autograd JVP)
+    on a ``size^3`` sample of the channel workload, all host threads."""
+    import numpy as np
+    import torch
+
+    from aquaflux_gb300 import workloads
+    from oracle import fv_oracle as fo
+
+    threads = os.cpu_count() or 1
+    torch.set_num_threads(threads)
+    wl = workloads.channel3d(size)
+    walls = wl.sst["walls"]
+    case = fo.make_case(wl.mesh, mu=wl.mu, rho=wl.rho, flow_bc=wl.flow_bc,
+                        sst={"nu": wl.mu / wl.rho, "walls": walls, "k": wl.sst["k"],
+                             "omega": wl.sst["omega"]})
+    orc = fo.Oracle(case)
+    s = wl.initial_state(seed=1, noise=0.05)
+    v = np.random.default_rng(2).standard_normal(s.size)
+    orc.jvp(s, v)  # warm
+    n, t0 = 0, time.perf_counter()
+    while True:
+        orc.residual(torch.as_tensor(s))
+        orc.jvp(s, v)
+        n += 1
+        el = time.perf_counter() - t0
+        if el >= min_seconds:
+            break
+    return {"faces_per_s": n * wl.mesh.n_faces / el, "cores": threads,
+            "sample": f"{size}^3 channel ({wl.mesh.n_cells} cells, {wl.mesh.n_faces} faces), "
+                      f"{n} residual+JVP evaluations in {el:.1f} s"}
+
+
+# ----------------------------------------------------------------------------- GPU arm
+def run_gpu(args, rank: int, world: int, local_rank: int) -> dict | None:
+    import numpy as np
+    import torch
+
+    from aquaflux_gb300 import workloads
+
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    wl = workloads.channel3d(args.size)
+    case = wl.device_case()
+    F = wl.mesh.n_faces
+    state = torch.tensor(wl.initial_state(seed=rank, noise=0.05), device="cuda")
+    vec = torch.tensor(np.random.default_rng(100 + rank).standard_normal(state.numel()),
+                       device="cuda")
+    r = torch.empty_like(state)
+    jv = torch.empty_like(state)
+
+    from aquaflux_gb300._lib import check, lib, ptr
+
+    L = lib()
+    stream = torch.cuda.current_stream()
+
+    def step():
+        check(L.fv_jvp(case.handle, ptr(state), ptr(vec), ptr(r), ptr(jv), stream.cuda_stream))
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    case.profile_begin(args.steps)
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local_rank) as clk:
+        torch.cuda.synchronize()
+        start.record(stream)
+        for _ in range(args.steps):
+            step()
+        end.record(stream)
+        torch.cuda.synchronize()
+    ms = start.elapsed_time(end)
+    stage_ms, runs = case.profile_end()
+    if not torch.isfinite(jv).all() or not torch.isfinite(r).all():
+        raise RuntimeError("non-finite residual / JVP in the benchmark step")
+    t = torch.tensor([ms], device="cuda", dtype=torch.float64)
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms = float(t)
+    value = world * F * args.steps / (ms * 1e-3) / 1e9
+
+    # end to end through the C ABI with pinned host buffers (copies inside the timed region)
+    h_state = state.cpu().pin_memory()
+    h_vec = vec.cpu().pin_memory()
+    h_r = torch.empty_like(h_state).pin_memory()
+    h_jv = torch.empty_like(h_state).pin_memory()
+    d_state, d_vec = torch.empty_like(state), torch.empty_like(vec)
+
+    def e2e_step():
+        d_state.copy_(h_state, non_blocking=True)
+        d_vec.copy_(h_vec, non_blocking=True)
+        check(L.fv_jvp(case.handle, ptr(d_state), ptr(d_vec), ptr(r), ptr(jv), stream.cuda_stream))
+        h_r.copy_(r, non_blocking=True)
+        h_jv.copy_(jv, non_blocking=True)
+
+    for _ in range(3):
+        e2e_step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        e2e_step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1)
+    te = torch.tensor([e2e_ms], device="cuda", dtype=torch.float64)
+    if dist is not None:
+        dist.all_reduce(te, op=dist.ReduceOp.MAX)
+        dist.barrier()
+    e2e_ms = float(te)
+    if rank != 0:
+        return None
+
+    peaks = measured_peaks()
+    dom = max(stage_ms, key=stage_ms.get)
+    flux_avg_ms = stage_ms["flux"] / max(runs, 1)
+    flux_bytes = flux_kernel_bytes(wl)
+    achieved = flux_bytes / (flux_avg_ms * 1e-3) / 1e9
+    traffic_path = os.path.join(ROOT, "profiles", "flux_traffic.json")
+    traffic = None
+    if os.path.exists(traffic_path):
+        with open(traffic_path) as f:
+            tr = json.load(f)
+        traffic = tr.get("bytes_per_face", 0.0) * F if tr.get("size") else None
+    bpf = step_bytes_per_face(wl)
+    out = {
+        "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": f"channel3d {args.size}^3 k-omega SST (u,v,w,p,k,omega), "
+                               f"{wl.mesh.n_cells} cells, {F} faces",
+                   "step": "residual + JVP (Krylov operator) at a fixed state",
+                   "cells": wl.mesh.n_cells, "faces": F,
+                   "l2": "working set > 2 GB per step (inputs larger than the 129 MB L2)",
+                   "parallelism": f"replicas x{world}"},
+        "e2e": {"value": round(world * F * args.steps / (e2e_ms * 1e-3) / 1e9, 4), "unit": UNIT,
+                "h2d_bytes_per_step": 2 * state.numel() * 8,
+                "d2h_bytes_per_step": 2 * state.numel() * 8},
+        "gpu_launches": 6 * args.steps,
+        "stage_ms_per_step": {k: round(v / max(runs, 1), 4) for k, v in stage_ms.items()},
+        "algorithmic_bytes_per_face": round(bpf, 2),
+        "step_achieved_gbs": round(bpf * F / (ms / args.steps * 1e-3) / 1e9, 1),
+        "roofline": {"bound": "hbm", "kernel": "k_flux<Dual>", "dominant_stage": dom,
+                     "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": traffic,
+                     "peak_source": f"{peaks['source']} (MEASURED_PEAKS.json hbm_gbs)"},
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu_baseline:
+        cb = cpu_residual_jvp_rate(args.cpu_sample)
+        out["cpu_baseline"] = {"value": round(cb["faces_per_s"] / 1e9, 6), "unit": UNIT,
+                               "cores": cb["cores"], "kind": "port", "sample": cb["sample"]}
+    return out
+
+
+def run_reference(args) -> dict:
+    cb = cpu_residual_jvp_rate(args.cpu_sample, min_seconds=4.0)
+    rates = [cb["faces_per_s"]]
+    for _ in range(max(args.steps, 1) - 1):
+        rates.append(cpu_residual_jvp_rate(args.cpu_sample, min_seconds=2.0)["faces_per_s"])
+    v = statistics.median(rates) / 1e9
+    return {
+        "impl": "reference", "metric": METRIC, "value": round(v, 6), "unit": UNIT, "n_gpus": 0,
+        "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"channel3d {args.size}^3 k-omega SST; CPU sample "
+                               f"{args.cpu_sample}^3 per step",
+                   "step": "residual + JVP (Krylov operator) at a fixed state"},
+        "cpu_baseline": {"value": round(v, 6), "unit": UNIT, "cores": cb["cores"], "kind": "port",
+                         "sample": cb["sample"]},
+        "e2e": {"value": round(v, 6), "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    args = _args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", str(args.gpus if args.gpus == 1 else 1)))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps(run_reference(args)))
+        return
+    import __graft_entry__
+
+    __graft_entry__.build()
+    out = run_gpu(args, rank, world, local_rank)
+    if out is not None:
+        print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

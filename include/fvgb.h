@@ -115,6 +115,12 @@ int fv_jvp_shift(FvCase* c, const double* state, const double* v, const double* 
  * out_mu = dR/dmu, out_inlet = dR/d(inlet_scale) (either may be NULL).  Device. */
 int fv_param_jvp(FvCase* c, const double* state, double* out_mu, double* out_inlet, void* stream);
 
+/* Per-stage CUDA-event timing of the next `max_runs` pipeline runs on this case (diagnostics;
+ * no reference counterpart).  profile_end synchronizes, writes the summed milliseconds of each
+ * stage (grad, closure, apcoef, dcoeff, flux, sum) and the number of runs recorded. */
+int fv_case_profile_begin(FvCase* c, int max_runs);
+int fv_case_profile_end(FvCase* c, float* stage_ms, int n_stages, int* n_runs);
+
 /* ------------------------------------------------------------------------------------------
  * Block-sparse (BSR, b x b dense blocks, row-major inside a block) operators.
  * Replaces _CsrOperator.apply (aquaflux/solve/multigrid.py:1302-1390).
