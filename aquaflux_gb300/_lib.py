@@ -46,6 +46,8 @@ SIGNATURES = {
     "fv_jvp": (c_int, [P, P, P, P, P, P]),
     "fv_jvp_shift": (c_int, [P, P, P, P, P, P]),
     "fv_param_jvp": (c_int, [P, P, P, P, P]),
+    "fv_vjp": (c_int, [P, P, P, P, P, P]),
+    "fv_param_vjp": (c_int, [P, P, P, P, P]),
     "fv_bsr_spmv_f64": (c_int, [c_int, c_int, P, P, P, P, P, c_int, P]),
     "fv_bsr_spmv_f32": (c_int, [c_int, c_int, P, P, P, P, P, c_int, P]),
     "fv_ilu0_create": (c_int, [c_int, c_int, P, P, c_int, P, P]),

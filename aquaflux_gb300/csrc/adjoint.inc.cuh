@@ -1,0 +1,816 @@
+// Reverse-mode (vector-Jacobian product) of the residual pipeline, hand-written.
+//
+// Included inside residual.cu's anonymous namespace: it reuses the forward helpers (SST wall
+// functions, boundary closures, Layout) and the forward workspace (G, closure fields, momentum-
+// diagonal coefficients, d) that a double-precision forward pass leaves behind.
+//
+// Given w = dL/dR, the kernels accumulate dL/dstate backwards through the stages
+//   a_sum      cell  replaced rows (pressure pin, omega wall fixation) and the SST sources
+//                    -> effective flux cotangents Wt, state / closure / gradient adjoints
+//   a_flux     cell  adjoint of the face fluxes (Rhie-Chow mass flux, diffusion, pressure,
+//                    upwind advection, k / omega transport) for this cell's side of each face
+//   a_apcoef   cell  adjoint of a_P through d = V / a_P and the face coefficients
+//   a_closure  cell  adjoint of the SST closure (strain, wall blends, F1, F2, nu_t, shear rate)
+//   a_grad     cell  adjoint of the compact Green-Gauss gradients; writes dL/dstate
+// Every accumulation is a per-cell sum over the cell's faces in ascending order (deterministic,
+// no atomics).  Subgradients follow the forward pass: a max / min tie splits the cotangent in
+// half (JAX's rule), safe_sqrt and the k >= 0 clamps have zero derivative where clamped.
+
+// d max(x, 0) / dx with the tie rule.
+__device__ __forceinline__ double dpos(double x) { return x > 0.0 ? 1.0 : (x == 0.0 ? 0.5 : 0.0); }
+// Split the cotangent `bar` of max(a, b) (or min with `is_min`) onto a and b.
+__device__ __forceinline__ void split_ext(double a, double b, double bar, bool is_min, double* abar,
+                                          double* bbar) {
+  bool pick_a = is_min ? a < b : a > b;
+  bool pick_b = is_min ? a > b : a < b;
+  if (pick_a) {
+    *abar += bar;
+  } else if (pick_b) {
+    *bbar += bar;
+  } else {
+    *abar += 0.5 * bar;
+    *bbar += 0.5 * bar;
+  }
+}
+
+struct AdjWork {
+  double* Wt;    // (NF, nc) effective flux-sum cotangent (0 on replaced rows)
+  double* sb;    // (NF, nc) state adjoint (accumulated)
+  double* Gb;    // (NF, D, nc) gradient adjoint
+  double* dcob;  // (nc) d-coefficient adjoint
+  double* clb;   // (4, nc) strain, F1, nu_t, shear-rate adjoints
+  double* Gwib;  // (D, nc) imposed omega-gradient adjoint
+};
+
+// ---------------------------------------------------------------- a_sum
+template <int DIM, bool TURB>
+__global__ void __launch_bounds__(128) a_sum(MeshView m, CaseView cv, Src<double> st, Par<double> par,
+                                             const double* W, const double* cl, const double* G,
+                                             const double* Gwi, AdjWork aw) {
+  using L = Layout<DIM, TURB>;
+  constexpr int NF = L::NFLD;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nc) return;
+  const int nc = m.nc;
+  double wr[NF], sb[NF];
+#pragma unroll
+  for (int q = 0; q < NF; ++q) {
+    wr[q] = W[(long)q * nc + c];
+    sb[q] = 0.0;
+  }
+  if (c == cv.pin) {
+    sb[L::P] += wr[L::P];
+    wr[L::P] = 0.0;
+  }
+  double Sb = 0.0, F1b = 0.0, ntb = 0.0, shb = 0.0;
+  double gkb[DIM], gwib[DIM];
+#pragma unroll
+  for (int j = 0; j < DIM; ++j) gkb[j] = gwib[j] = 0.0;
+  if (TURB) {
+    const double V = m.vol[c];
+    const double k = st((long)L::K * nc + c), w = st((long)L::W * nc + c);
+    const double S = cl[c], F1 = cl[(long)nc + c], nut = cl[2L * nc + c], shear = cl[3L * nc + c];
+    const double nu = par.mu / cv.rho;
+    const double d = cv.wd[c];
+    const bool wall = cv.wcell[c] != 0;
+    const Dual kd{k, 1.0};
+    const Dual nud{nu, 0.0};
+    // ---- omega row
+    double Ww = wr[L::W];
+    if (wall) {
+      // R_w = w - omega_wall(nu, d, k): the flux sum and the sources are overwritten
+      Dual ow = omega_wall(nud, d, kd);
+      sb[L::W] += Ww;
+      sb[L::K] += -Ww * ow.d;
+      Ww = 0.0;
+      wr[L::W] = 0.0;
+    }
+    if (Ww != 0.0) {
+      const double alpha = F1 * ALPHA_1 + (1.0 - F1) * ALPHA_2;
+      const double kp = fmax(k, 0.0);
+      const double num = PROD_RATIO * BETA_STAR * kp * w;
+      const double den = fmax(nut, NUT_FLOOR);
+      const double cap = num / den;
+      const double S2 = S * S;
+      const double mn = fmin(S2, cap);
+      // R_w -= alpha * min(S^2, cap) * V
+      const double mbar = -Ww * alpha * V;
+      F1b += -Ww * mn * V * (ALPHA_1 - ALPHA_2);
+      double S2b = 0.0, capb = 0.0;
+      split_ext(S2, cap, mbar, true, &S2b, &capb);
+      Sb += S2b * 2.0 * S;
+      double numb = capb / den, denb = -capb * num / (den * den);
+      double nutb_f = 0.0, flb = 0.0;
+      split_ext(nut, NUT_FLOOR, denb, false, &nutb_f, &flb);
+      ntb += nutb_f;
+      sb[L::K] += numb * PROD_RATIO * BETA_STAR * w * dpos(k);
+      sb[L::W] += numb * PROD_RATIO * BETA_STAR * kp;
+      // R_w += beta * w^2 * V
+      const double beta = F1 * BETA_1 + (1.0 - F1) * BETA_2;
+      F1b += Ww * w * w * V * (BETA_1 - BETA_2);
+      sb[L::W] += Ww * beta * 2.0 * w * V;
+      // R_w -= cross * V,  cross = 2 (1 - F1) sigma_w2 (gk . gwi) / w
+      double dkw = 0.0;
+      double gk[DIM], gwi[DIM];
+#pragma unroll
+      for (int j = 0; j < DIM; ++j) {
+        gk[j] = G[((long)L::K * DIM + j) * nc + c];
+        gwi[j] = Gwi[(long)j * nc + c];
+        dkw += gk[j] * gwi[j];
+      }
+      const double cross = 2.0 * (1.0 - F1) * SIGMA_W2 * dkw / w;
+      const double crb = -Ww * V;
+      F1b += crb * (-2.0 * SIGMA_W2 * dkw / w);
+      const double dotb = crb * 2.0 * (1.0 - F1) * SIGMA_W2 / w;
+#pragma unroll
+      for (int j = 0; j < DIM; ++j) {
+        gkb[j] += dotb * gwi[j];
+        gwib[j] += dotb * gk[j];
+      }
+      sb[L::W] += crb * (-cross / w);
+    }
+    // ---- k row: R_k -= lim * V;  R_k += beta* k weff V
+    const double Wk = wr[L::K];
+    if (Wk != 0.0) {
+      const double kp = fmax(k, 0.0);
+      const double prod = nut * (S * S);
+      const double limit = PROD_RATIO * BETA_STAR * kp * w;
+      const double lim0 = fmin(prod, limit);
+      double weff = w;
+      const double limb = -Wk * V;
+      double lim0b = limb;
+      if (wall) {
+        Dual lw = wall_weight(nud, d, kd);
+        Dual ntw = nut_wall(nud, d, kd);
+        Dual ls = log_shear(d, kd);
+        const double tau = (nu + ntw.v) * shear;
+        const double pw = tau * ls.v;
+        lim0b = (1.0 - lw.v) * limb;
+        const double lwb = (pw - lim0) * limb;
+        const double pwb = lw.v * limb;
+        const double taub = pwb * ls.v;
+        sb[L::K] += lwb * lw.d + pwb * tau * ls.d + taub * shear * ntw.d;
+        shb += taub * (nu + ntw.v);
+        Dual ow = omega_wall(nud, d, kd);
+        weff = ow.v;
+        const double weffb = Wk * BETA_STAR * k * V;
+        sb[L::K] += weffb * ow.d;
+      } else {
+        sb[L::W] += Wk * BETA_STAR * k * V;
+      }
+      sb[L::K] += Wk * BETA_STAR * weff * V;
+      double prodb = 0.0, limitb = 0.0;
+      split_ext(prod, limit, lim0b, true, &prodb, &limitb);
+      ntb += prodb * S * S;
+      Sb += prodb * 2.0 * nut * S;
+      sb[L::K] += limitb * PROD_RATIO * BETA_STAR * w * dpos(k);
+      sb[L::W] += limitb * PROD_RATIO * BETA_STAR * kp;
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < NF; ++q) {
+    aw.Wt[(long)q * nc + c] = wr[q];
+    aw.sb[(long)q * nc + c] = sb[q];
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) aw.Gb[((long)q * DIM + j) * nc + c] = 0.0;
+  }
+  if (TURB) {
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) {
+      aw.Gb[((long)L::K * DIM + j) * nc + c] = gkb[j];
+      aw.Gwib[(long)j * nc + c] = gwib[j];
+    }
+    aw.clb[c] = Sb;
+    aw.clb[(long)nc + c] = F1b;
+    aw.clb[2L * nc + c] = ntb;
+    aw.clb[3L * nc + c] = shb;
+  }
+  aw.dcob[c] = 0.0;
+}
+
+// momentum-normal flux mn(f) = sum_j n_j ((rho u_j)_f + (rho grad u_j)_f . skew) -- its partial
+// derivatives are n_j w rho (u) and n_j w rho skew_q (grad u), w = 1 - g (owner) or g (neighbour).
+template <int DIM>
+__device__ __forceinline__ void mn_adjoint(const MeshView& m, int f, double wgt, double rho,
+                                           double mnb, double* ub, double* Gub /*[DIM][DIM]*/) {
+  const int nf = m.nf;
+#pragma unroll
+  for (int j = 0; j < DIM; ++j) {
+    const double nj = m.normal[(long)j * nf + f];
+    const double t = mnb * nj * wgt * rho;
+    ub[j] += t;
+#pragma unroll
+    for (int q = 0; q < DIM; ++q) Gub[j * DIM + q] += t * m.skew[(long)q * nf + f];
+  }
+}
+
+// ---------------------------------------------------------------- a_flux
+template <int DIM, bool TURB>
+__global__ void __launch_bounds__(128) a_flux(MeshView m, CaseView cv, Src<double> st, Par<double> par,
+                                              const double* G, const double* cl, const double* dco,
+                                              AdjWork aw) {
+  using L = Layout<DIM, TURB>;
+  constexpr int NF = L::NFLD;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nc) return;
+  const int nc = m.nc, nf = m.nf;
+  const double rho = cv.rho;
+  const double nu = par.mu / rho;
+  double sb[NF], Gb[NF][DIM];
+#pragma unroll
+  for (int q = 0; q < NF; ++q) {
+    sb[q] = 0.0;
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) Gb[q][j] = 0.0;
+  }
+  double dcb = 0.0, F1b = 0.0, ntb = 0.0;
+  const int b = m.cf_ptr[c], e = m.cf_ptr[c + 1];
+  for (int it = b; it < e; ++it) {
+    const unsigned ent = m.cf_face[it];
+    const int f = (int)(ent & ~FV_NB_BIT);
+    const bool isnb = (ent & FV_NB_BIT) != 0;
+    const int o = m.owner[f];
+    const double A = m.area[f];
+    double nrm[DIM], tP[DIM];
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) {
+      nrm[j] = m.normal[(long)j * nf + f];
+      tP[j] = m.tP[(long)j * nf + f];
+    }
+    const double mo = TURB ? par.mu + rho * cl[2L * nc + o] : par.mu;
+    const double po = st((long)L::P * nc + o);
+    if (f < m.nfi) {
+      const int n = m.nb[f];
+      const double g = m.g[f];
+      const double sgn_w = isnb ? g : 1.0 - g;  // this side's interpolation weight
+      double tN[DIM];
+#pragma unroll
+      for (int j = 0; j < DIM; ++j) tN[j] = m.tN[(long)j * nf + f];
+      double FLb[NF];
+#pragma unroll
+      for (int q = 0; q < NF; ++q) FLb[q] = aw.Wt[(long)q * nc + o] - aw.Wt[(long)q * nc + n];
+      // forward recomputation
+      const double pn = st((long)L::P * nc + n);
+      const double mn = mom_normal<double, DIM, TURB>(m, st, G, rho, f, o, n, g);
+      const double rho_f = (1.0 - g) * rho + g * rho;
+      double gpf[DIM];
+#pragma unroll
+      for (int j = 0; j < DIM; ++j)
+        gpf[j] = (1.0 - g) * G[((long)L::P * DIM + j) * nc + o] + g * G[((long)L::P * DIM + j) * nc + n];
+      const double dcf = (1.0 - g) * dco[o] + g * dco[n];
+      double dhat = (nrm[0] * nrm[0]) * dcf;
+#pragma unroll
+      for (int j = 1; j < DIM; ++j) dhat += (nrm[j] * nrm[j]) * dcf;
+      double gd = gpf[0] * m.dvec[f];
+#pragma unroll
+      for (int j = 1; j < DIM; ++j) gd += gpf[j] * m.dvec[(long)j * nf + f];
+      const double nd = m.nd[f];
+      const double damping = ((pn - po) - gd) / nd;
+      const double mdot = (mn - rho_f * dhat * damping) * A;
+      const double mnbv = TURB ? par.mu + rho * cl[2L * nc + n] : par.mu;
+      const double denom = m.dpn[f] - mo / mnbv * m.dnn[f];
+      const bool out = mdot >= 0.0;
+      // reverse
+      double mdotb = FLb[L::P];
+      double pfb = 0.0, denomb = 0.0, mob = 0.0;
+#pragma unroll
+      for (int i = 0; i < DIM; ++i) {
+        const double uo = st((long)i * nc + o), un = st((long)i * nc + n);
+        double cp = 0.0, cn = 0.0;
+#pragma unroll
+        for (int j = 0; j < DIM; ++j) {
+          cp += G[((long)i * DIM + j) * nc + o] * tP[j];
+          cn += G[((long)i * DIM + j) * nc + n] * tN[j];
+        }
+        const double num = (un - uo) + cn - cp;
+        const double fb = FLb[i];
+        mdotb += fb * (out ? uo : un);
+        const double k1 = fb * mo * A / denom;  // d diff / d num = -mo A / denom
+        if (!isnb) {
+          sb[i] += k1 + (out ? fb * mdot : 0.0);
+#pragma unroll
+          for (int j = 0; j < DIM; ++j) Gb[i][j] += k1 * tP[j];
+        } else {
+          sb[i] += -k1 + (!out ? fb * mdot : 0.0);
+#pragma unroll
+          for (int j = 0; j < DIM; ++j) Gb[i][j] += -k1 * tN[j];
+        }
+        denomb += fb * mo * num * A / (denom * denom);
+        mob += fb * (-num * A / denom);
+        pfb += fb * nrm[i] * A;
+      }
+      mob += denomb * (-m.dnn[f] / mnbv);
+      const double mnbb = denomb * (mo * m.dnn[f] / (mnbv * mnbv));
+      // pf = (1-g) po + g pn + gpf . skew
+      double gpfb[DIM];
+#pragma unroll
+      for (int j = 0; j < DIM; ++j) gpfb[j] = pfb * m.skew[(long)j * nf + f];
+      sb[L::P] += sgn_w * pfb;
+      if (TURB) {
+        const double vflux = mdot / rho;
+        const bool vout = vflux >= 0.0;
+        const double F1o = cl[(long)nc + o], F1n = cl[(long)nc + n];
+        const double nto = cl[2L * nc + o], ntn = cl[2L * nc + n];
+#pragma unroll
+        for (int s = 0; s < 2; ++s) {
+          const int q = s == 0 ? L::K : L::W;
+          const double in = s == 0 ? SIGMA_K1 : SIGMA_W1, ou = s == 0 ? SIGMA_K2 : SIGMA_W2;
+          const double bo = F1o * in + (1.0 - F1o) * ou, bn = F1n * in + (1.0 - F1n) * ou;
+          const double go = nu + bo * nto, gn = nu + bn * ntn;
+          const double phio = st((long)q * nc + o), phin = st((long)q * nc + n);
+          double cp = 0.0, cn = 0.0;
+#pragma unroll
+          for (int j = 0; j < DIM; ++j) {
+            cp += G[((long)q * DIM + j) * nc + o] * tP[j];
+            cn += G[((long)q * DIM + j) * nc + n] * tN[j];
+          }
+          const double num = (phin - phio) + cn - cp;
+          const double den = m.dpn[f] - go / gn * m.dnn[f];
+          const double fb = FLb[q];
+          mdotb += fb * (vout ? phio : phin) / rho;
+          const double k1 = fb * go * A / den;
+          if (!isnb) {
+            sb[q] += k1 + (vout ? fb * vflux : 0.0);
+#pragma unroll
+            for (int j = 0; j < DIM; ++j) Gb[q][j] += k1 * tP[j];
+          } else {
+            sb[q] += -k1 + (!vout ? fb * vflux : 0.0);
+#pragma unroll
+            for (int j = 0; j < DIM; ++j) Gb[q][j] += -k1 * tN[j];
+          }
+          const double denb = fb * go * num * A / (den * den);
+          const double gob = fb * (-num * A / den) + denb * (-m.dnn[f] / gn);
+          const double gnb = denb * (go * m.dnn[f] / (gn * gn));
+          if (!isnb) {
+            F1b += gob * (in - ou) * nto;
+            ntb += gob * bo;
+          } else {
+            F1b += gnb * (in - ou) * ntn;
+            ntb += gnb * bn;
+          }
+        }
+        if (!isnb) ntb += mob * rho;
+        else ntb += mnbb * rho;
+      }
+      // mdot = (mn - rho_f dhat damping) A
+      const double mnb = mdotb * A;
+      const double dhatb = -mdotb * A * rho_f * damping;
+      const double dampb = -mdotb * A * rho_f * dhat;
+      sb[L::P] += isnb ? dampb / nd : -dampb / nd;
+#pragma unroll
+      for (int j = 0; j < DIM; ++j) gpfb[j] += -dampb / nd * m.dvec[(long)j * nf + f];
+#pragma unroll
+      for (int j = 0; j < DIM; ++j) Gb[L::P][j] += sgn_w * gpfb[j];
+      dcb += dhatb * m.nn2[f] * sgn_w;
+      double ub[DIM], Gub[DIM * DIM];
+#pragma unroll
+      for (int j = 0; j < DIM; ++j) ub[j] = 0.0;
+#pragma unroll
+      for (int j = 0; j < DIM * DIM; ++j) Gub[j] = 0.0;
+      mn_adjoint<DIM>(m, f, sgn_w, rho, mnb, ub, Gub);
+#pragma unroll
+      for (int j = 0; j < DIM; ++j) {
+        sb[j] += ub[j];
+#pragma unroll
+        for (int q = 0; q < DIM; ++q) Gb[j][q] += Gub[j * DIM + q];
+      }
+    } else {
+      // boundary face: this cell is the owner
+      const signed char kind = cv.fkind[f];
+      double FLb[NF];
+#pragma unroll
+      for (int q = 0; q < NF; ++q) FLb[q] = aw.Wt[(long)q * nc + o];
+      double uo[DIM], bu[DIM];
+#pragma unroll
+      for (int j = 0; j < DIM; ++j) {
+        uo[j] = st((long)j * nc + o);
+        bu[j] = bvel(cv, nf, f, j, kind, uo[j], par);
+      }
+      double mdot = 0.0, dh = 0.0, compact = 0.0, interp = 0.0;
+      if (kind == 2) {
+        double un = bu[0] * nrm[0];
+#pragma unroll
+        for (int j = 1; j < DIM; ++j) un += bu[j] * nrm[j];
+        mdot = rho * un * A;
+      } else if (kind == 3) {
+        double un = uo[0] * nrm[0];
+        interp = G[((long)L::P * DIM) * nc + o] * nrm[0];
+#pragma unroll
+        for (int j = 1; j < DIM; ++j) {
+          un += uo[j] * nrm[j];
+          interp += G[((long)L::P * DIM + j) * nc + o] * nrm[j];
+        }
+        dh = (nrm[0] * nrm[0]) * dco[o];
+#pragma unroll
+        for (int j = 1; j < DIM; ++j) dh += (nrm[j] * nrm[j]) * dco[o];
+        compact = (cv.fp[f] - po) / m.nd[f];
+        mdot = rho * (un - dh * (compact - interp)) * A;
+      }
+      double gbv = mo;
+      double dgb_dk = 0.0;  // d gamma_b / d k_owner (SST wall faces)
+      bool gb_is_mo = true;
+      if (TURB && (kind == 0 || kind == 1)) {
+        gb_is_mo = false;
+        if (cv.swall[f]) {
+          Dual nw = nut_wall(Dual{nu, 0.0}, cv.wd[o], Dual{st((long)L::K * nc + o), 1.0});
+          gbv = par.mu + rho * nw.v;
+          dgb_dk = rho * nw.d;
+        } else {
+          gbv = par.mu;
+        }
+      }
+      const bool out = mdot >= 0.0;
+      double mdotb = FLb[L::P], pfb = 0.0, gbb = 0.0;
+#pragma unroll
+      for (int i = 0; i < DIM; ++i) {
+        double cp = 0.0;
+#pragma unroll
+        for (int j = 0; j < DIM; ++j) cp += G[((long)i * DIM + j) * nc + o] * tP[j];
+        const double num = bu[i] - uo[i] - cp;
+        const double fb = FLb[i];
+        mdotb += fb * (out ? uo[i] : bu[i]);
+        const double numb = fb * (-gbv * A / m.dpn[f]);
+        gbb += fb * (-num * A / m.dpn[f]);
+        const double bub = numb + (!out ? fb * mdot : 0.0);
+        sb[i] += -numb + (out ? fb * mdot : 0.0);
+        if (kind == 3) sb[i] += bub;
+#pragma unroll
+        for (int j = 0; j < DIM; ++j) Gb[i][j] += -numb * tP[j];
+        pfb += fb * nrm[i] * A;
+      }
+      if (kind >= 0 && kind <= 2) sb[L::P] += pfb;
+      if (TURB) {
+        if (gb_is_mo) ntb += gbb * rho;
+        else sb[L::K] += gbb * dgb_dk;
+        const double vflux = mdot / rho;
+        const bool vout = vflux >= 0.0;
+        const double F1o = cl[(long)nc + o], nto = cl[2L * nc + o];
+#pragma unroll
+        for (int s = 0; s < 2; ++s) {
+          const int q = s == 0 ? L::K : L::W;
+          const double in = s == 0 ? SIGMA_K1 : SIGMA_W1, ou = s == 0 ? SIGMA_K2 : SIGMA_W2;
+          const double bo = F1o * in + (1.0 - F1o) * ou;
+          const double go = nu + bo * nto;
+          const double phio = st((long)q * nc + o);
+          double cp = 0.0;
+#pragma unroll
+          for (int j = 0; j < DIM; ++j) cp += G[((long)q * DIM + j) * nc + o] * tP[j];
+          const signed char sk = s == 0 ? cv.kkind[f] : cv.wkind[f];
+          const double sval = s == 0 ? cv.kval[f] : cv.wval[f];
+          const double bphi = bscalar(sk, sval, phio, cp);
+          double gface = go, wwd = 0.0, wwv = 0.0;
+          const bool wallk = s == 0 && cv.swall[f];
+          if (wallk) {
+            Dual ww = wall_weight(Dual{nu, 0.0}, cv.wd[o], Dual{phio, 1.0});
+            wwv = ww.v;
+            wwd = ww.d;
+            gface = (1.0 - wwv) * go;
+          }
+          const double num = bphi - phio - cp;
+          const double fb = FLb[q];
+          mdotb += fb * (vout ? phio : bphi) / rho;
+          const double numb = fb * (-gface * A / m.dpn[f]);
+          const double gfb = fb * (-num * A / m.dpn[f]);
+          const double bphib = numb + (!vout ? fb * vflux : 0.0);
+          sb[q] += -numb + (vout ? fb * vflux : 0.0);
+#pragma unroll
+          for (int j = 0; j < DIM; ++j) Gb[q][j] += -numb * tP[j];
+          if (sk == 1) {
+            sb[q] += bphib;
+#pragma unroll
+            for (int j = 0; j < DIM; ++j) Gb[q][j] += bphib * tP[j];
+          }
+          double gob = gfb;
+          if (wallk) {
+            gob = gfb * (1.0 - wwv);
+            sb[L::K] += -gfb * go * wwd;
+          }
+          F1b += gob * (in - ou) * nto;
+          ntb += gob * bo;
+        }
+      }
+      if (kind == 3) {
+        const double base = mdotb * rho * A;
+#pragma unroll
+        for (int j = 0; j < DIM; ++j) sb[j] += base * nrm[j];
+        const double dhb = -base * (compact - interp);
+        dcb += dhb * m.nn2[f];
+        const double compb = -base * dh;
+        sb[L::P] += -compb / m.nd[f];
+        const double interpb = base * dh;
+#pragma unroll
+        for (int j = 0; j < DIM; ++j) Gb[L::P][j] += interpb * nrm[j];
+      }
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < NF; ++q) {
+    aw.sb[(long)q * nc + c] += sb[q];
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) aw.Gb[((long)q * DIM + j) * nc + c] += Gb[q][j];
+  }
+  aw.dcob[c] = dcb;
+  if (TURB) {
+    aw.clb[(long)nc + c] += F1b;
+    aw.clb[2L * nc + c] += ntb;
+  }
+}
+
+// ---------------------------------------------------------------- a_apcoef
+// a_P(c) = sum of face coefficients; d = V / a_P  =>  abar = -dbar d^2 / V.
+template <int DIM, bool TURB>
+__global__ void __launch_bounds__(128) a_apcoef(MeshView m, CaseView cv, Src<double> st, Par<double> par,
+                                                const double* G, const double* cl, const double* dco,
+                                                AdjWork aw) {
+  using L = Layout<DIM, TURB>;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nc) return;
+  const int nc = m.nc, nf = m.nf;
+  const double rho = cv.rho;
+  double ub[DIM], Gub[DIM * DIM];
+#pragma unroll
+  for (int j = 0; j < DIM; ++j) ub[j] = 0.0;
+#pragma unroll
+  for (int j = 0; j < DIM * DIM; ++j) Gub[j] = 0.0;
+  double ntb = 0.0, kb = 0.0;
+  const int b = m.cf_ptr[c], e = m.cf_ptr[c + 1];
+  for (int it = b; it < e; ++it) {
+    const unsigned ent = m.cf_face[it];
+    const int f = (int)(ent & ~FV_NB_BIT);
+    const bool isnb = (ent & FV_NB_BIT) != 0;
+    const int o = m.owner[f];
+    const double A = m.area[f];
+    const double abo = -aw.dcob[o] * dco[o] * dco[o] / m.vol[o];
+    const double mo = TURB ? par.mu + rho * cl[2L * nc + o] : par.mu;
+    if (f < m.nfi) {
+      const int n = m.nb[f];
+      const double g = m.g[f];
+      const double abn = -aw.dcob[n] * dco[n] * dco[n] / m.vol[n];
+      const double mdot = mom_normal<double, DIM, TURB>(m, st, G, rho, f, o, n, g) * A;
+      const double mnbv = TURB ? par.mu + rho * cl[2L * nc + n] : par.mu;
+      const double den = m.dpn[f] - mo / mnbv * m.dnn[f];
+      const double viscb = abo + abn;
+      const double mdotb = abo * dpos(mdot) - abn * dpos(-mdot);
+      const double denb = -viscb * mo * A / (den * den);
+      const double mob = viscb * A / den + denb * (-m.dnn[f] / mnbv);
+      const double mnbb = denb * (mo * m.dnn[f] / (mnbv * mnbv));
+      if (TURB) ntb += (isnb ? mnbb : mob) * rho;
+      mn_adjoint<DIM>(m, f, isnb ? g : 1.0 - g, rho, mdotb * A, ub, Gub);
+    } else {
+      const signed char kind = cv.fkind[f];
+      const double mdot = mom_normal<double, DIM, TURB>(m, st, G, rho, f, o, o, 0.0) * A;
+      const double vob = (kind >= 0 && kind <= 2) ? abo : 0.0;
+      const double convb = (kind == 2 || kind == 3) ? abo : 0.0;
+      mn_adjoint<DIM>(m, f, 1.0, rho, convb * dpos(mdot) * A, ub, Gub);
+      if (TURB && vob != 0.0) {
+        if (kind == 0 || kind == 1) {
+          if (cv.swall[f]) {
+            Dual nw = nut_wall(Dual{par.mu / rho, 0.0}, cv.wd[o],
+                               Dual{st((long)L::K * nc + o), 1.0});
+            kb += vob * A / m.nd[f] * rho * nw.d;
+          }
+        } else {
+          ntb += vob * A / m.nd[f] * rho;
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < DIM; ++j) {
+    aw.sb[(long)j * nc + c] += ub[j];
+#pragma unroll
+    for (int q = 0; q < DIM; ++q) aw.Gb[((long)j * DIM + q) * nc + c] += Gub[j * DIM + q];
+  }
+  if (TURB) {
+    aw.clb[2L * nc + c] += ntb;
+    aw.sb[(long)L::K * nc + c] += kb;
+  }
+}
+
+// ---------------------------------------------------------------- a_closure (SST)
+template <int DIM>
+__global__ void __launch_bounds__(128) a_closure(MeshView m, CaseView cv, Src<double> st, Par<double> par,
+                                                 const double* G, const double* cl, AdjWork aw) {
+  using L = Layout<DIM, true>;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nc) return;
+  const int nc = m.nc, nf = m.nf;
+  const double k = st((long)L::K * nc + c), w = st((long)L::W * nc + c);
+  const double nu = par.mu / cv.rho;
+  const double d = cv.wd[c];
+  const bool wall = cv.wcell[c] != 0;
+  double Sb = aw.clb[c], F1b = aw.clb[(long)nc + c], ntb = aw.clb[2L * nc + c];
+  const double shb = aw.clb[3L * nc + c];
+  double gu[DIM][DIM], gk[DIM], gw[DIM];
+#pragma unroll
+  for (int i = 0; i < DIM; ++i)
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) gu[i][j] = G[((long)i * DIM + j) * nc + c];
+#pragma unroll
+  for (int j = 0; j < DIM; ++j) {
+    gk[j] = G[((long)L::K * DIM + j) * nc + c];
+    gw[j] = G[((long)L::W * DIM + j) * nc + c];
+  }
+  // forward recomputation
+  double sum = 0.0;
+#pragma unroll
+  for (int i = 0; i < DIM; ++i)
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) {
+      double sij = 0.5 * (gu[i][j] + gu[j][i]);
+      sum += sij * sij;
+    }
+  const double S0 = 2.0 * sum > 0.0 ? sqrt(2.0 * sum) : 0.0;
+  double S = S0;
+  Dual wgt{0.0, 0.0}, ls{0.0, 0.0}, dwdd{0.0, 0.0}, dwdk{0.0, 0.0};
+  if (wall) {
+    const Dual kd{k, 1.0}, nud{nu, 0.0};
+    wgt = wall_weight(nud, d, kd);
+    ls = log_shear(d, kd);
+    S = (1.0 - wgt.v) * S0 + wgt.v * ls.v;
+    omega_wall_partials(nud, d, kd, &dwdd, &dwdk);
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) gw[j] = cv.wdg[(long)j * nc + c] * dwdd.v + gk[j] * dwdk.v;
+  }
+  const double kp = fmax(k, 0.0);
+  double dot_kw = gk[0] * gw[0];
+#pragma unroll
+  for (int j = 1; j < DIM; ++j) dot_kw += gk[j] * gw[j];
+  const double cd0 = 2.0 * SIGMA_W2 * dot_kw / w;
+  const double cd = fmax(cd0, CROSS_FLOOR);
+  const double sk = kp > 0.0 ? sqrt(kp) : 0.0;
+  const double vt = 500.0 * nu / ((d * d) * w);
+  const double c1 = sk / (BETA_STAR * w * d);
+  const double inner = fmax(c1, vt);
+  const double c2 = 4.0 * SIGMA_W2 * kp / (cd * (d * d));
+  const double arg1 = fmin(inner, c2);
+  const double a1sq = arg1 * arg1;
+  const double F1 = tanh(a1sq * a1sq);
+  const double a2 = 2.0 * sk / (BETA_STAR * w * d);
+  const double arg2 = fmax(a2, vt);
+  const double F2 = tanh(arg2 * arg2);
+  const double Mx = fmax(A1 * w, S * F2);
+  // reverse: nut = A1 kp / M
+  double kpb = ntb * A1 / Mx;
+  const double Mb = -ntb * A1 * kp / (Mx * Mx);
+  double awb = 0.0, sfb = 0.0;
+  split_ext(A1 * w, S * F2, Mb, false, &awb, &sfb);
+  double wb = awb * A1;
+  Sb += sfb * F2;
+  const double F2b = sfb * S;
+  const double arg2b = F2b * (1.0 - F2 * F2) * 2.0 * arg2;
+  double a2b = 0.0, vtb = 0.0;
+  split_ext(a2, vt, arg2b, false, &a2b, &vtb);
+  double skb = a2b * 2.0 / (BETA_STAR * w * d);
+  wb += a2b * (-a2 / w);
+  // F1 = tanh(arg1^4)
+  const double arg1b = F1b * (1.0 - F1 * F1) * 4.0 * a1sq * arg1;
+  double innerb = 0.0, c2b = 0.0;
+  split_ext(inner, c2, arg1b, true, &innerb, &c2b);
+  double c1b = 0.0;
+  split_ext(c1, vt, innerb, false, &c1b, &vtb);
+  skb += c1b / (BETA_STAR * w * d);
+  wb += c1b * (-c1 / w);
+  wb += vtb * (-vt / w);
+  kpb += c2b * 4.0 * SIGMA_W2 / (cd * (d * d));
+  const double cdb = -c2b * c2 / cd;
+  double cd0b = 0.0, flb = 0.0;
+  split_ext(cd0, CROSS_FLOOR, cdb, false, &cd0b, &flb);
+  const double dotb = cd0b * 2.0 * SIGMA_W2 / w;
+  wb += cd0b * (-cd0 / w);
+  double gkb[DIM], gwb[DIM];
+#pragma unroll
+  for (int j = 0; j < DIM; ++j) {
+    gkb[j] = dotb * gw[j];
+    gwb[j] = dotb * gk[j] + aw.Gwib[(long)j * nc + c];
+  }
+  kpb += skb * (kp > 0.0 ? 0.5 / sk : 0.0);
+  double kb = kpb * dpos(k);
+  double S0b = Sb;
+  double ub[DIM];
+#pragma unroll
+  for (int j = 0; j < DIM; ++j) ub[j] = 0.0;
+  if (wall) {
+    S0b = Sb * (1.0 - wgt.v);
+    const double wgtb = Sb * (ls.v - S0);
+    const double lsb = Sb * wgt.v;
+    kb += wgtb * wgt.d + lsb * ls.d;
+    // imposed omega gradient: gw = wdg * dwdd(k) + gk * dwdk(k)
+    double ddb = 0.0, dkb = 0.0;
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) {
+      ddb += gwb[j] * cv.wdg[(long)j * nc + c];
+      dkb += gwb[j] * gk[j];
+      gkb[j] += gwb[j] * dwdk.v;
+      gwb[j] = 0.0;  // the reconstructed omega gradient does not reach an imposed cell
+    }
+    kb += ddb * dwdd.d + dkb * dwdk.d;
+    // wall shear rate: sum(rate A) / sum(A), rate = |u - u_b| / d
+    if (shb != 0.0) {
+      double den = 0.0;
+      const int b = m.cf_ptr[c], e = m.cf_ptr[c + 1];
+      for (int it = b; it < e; ++it) {
+        const int f = (int)(m.cf_face[it] & ~FV_NB_BIT);
+        if (f < m.nfi || !cv.swall[f]) continue;
+        den += m.area[f];
+      }
+      for (int it = b; it < e; ++it) {
+        const int f = (int)(m.cf_face[it] & ~FV_NB_BIT);
+        if (f < m.nfi || !cv.swall[f]) continue;
+        const signed char kind = cv.fkind[f];
+        if (kind == 3) continue;  // zero-gradient velocity: slip identically zero
+        double sl[DIM], s2 = 0.0;
+#pragma unroll
+        for (int j = 0; j < DIM; ++j) {
+          const double u = st((long)j * nc + c);
+          sl[j] = u - bvel(cv, nf, f, j, kind, u, par);
+          s2 += sl[j] * sl[j];
+        }
+        if (s2 > 0.0) {
+          const double rb = shb * m.area[f] / den;
+          const double s2b = rb * 0.5 / (sqrt(s2) * d);
+#pragma unroll
+          for (int j = 0; j < DIM; ++j) ub[j] += s2b * 2.0 * sl[j];
+        }
+      }
+    }
+  }
+  // S0 = safe_sqrt(2 sum s_ij^2)
+  if (S0 > 0.0 && S0b != 0.0) {
+    const double sumb = S0b / S0;
+#pragma unroll
+    for (int i = 0; i < DIM; ++i)
+#pragma unroll
+      for (int j = 0; j < DIM; ++j) {
+        const double sij = 0.5 * (gu[i][j] + gu[j][i]);
+        const double sijb = sumb * 2.0 * sij;
+        aw.Gb[((long)i * DIM + j) * nc + c] += 0.5 * sijb;
+        aw.Gb[((long)j * DIM + i) * nc + c] += 0.5 * sijb;
+      }
+  }
+#pragma unroll
+  for (int j = 0; j < DIM; ++j) {
+    aw.Gb[((long)L::K * DIM + j) * nc + c] += gkb[j];
+    aw.Gb[((long)L::W * DIM + j) * nc + c] += gwb[j];
+    aw.sb[(long)j * nc + c] += ub[j];
+  }
+  aw.sb[(long)L::K * nc + c] += kb;
+  aw.sb[(long)L::W * nc + c] += wb;
+}
+
+// ---------------------------------------------------------------- a_grad
+template <int DIM, bool TURB>
+__global__ void __launch_bounds__(128) a_grad(MeshView m, CaseView cv, AdjWork aw, double* out) {
+  using L = Layout<DIM, TURB>;
+  constexpr int NF = L::NFLD;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nc) return;
+  const int nc = m.nc, nf = m.nf;
+  double acc[NF];
+#pragma unroll
+  for (int q = 0; q < NF; ++q) acc[q] = aw.sb[(long)q * nc + c];
+  const int b = m.cf_ptr[c], e = m.cf_ptr[c + 1];
+  for (int it = b; it < e; ++it) {
+    const unsigned ent = m.cf_face[it];
+    const int f = (int)(ent & ~FV_NB_BIT);
+    const bool isnb = (ent & FV_NB_BIT) != 0;
+    const int o = m.owner[f];
+    const double A = m.area[f];
+    double S[DIM];
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) S[j] = m.normal[(long)j * nf + f] * A;
+    const double ivo = 1.0 / m.vol[o];
+    if (f < m.nfi) {
+      const int n = m.nb[f];
+      const double ivn = 1.0 / m.vol[n];
+      const double g = m.g[f];
+      const double wgt = isnb ? g : 1.0 - g;
+#pragma unroll
+      for (int q = 0; q < NF; ++q) {
+        double phib = 0.0;
+#pragma unroll
+        for (int j = 0; j < DIM; ++j)
+          phib += S[j] * (aw.Gb[((long)q * DIM + j) * nc + o] * ivo -
+                          aw.Gb[((long)q * DIM + j) * nc + n] * ivn);
+        acc[q] += wgt * phib;
+      }
+    } else {
+      const signed char kind = cv.fkind[f];
+#pragma unroll
+      for (int q = 0; q < NF; ++q) {
+        bool dep;
+        if (q < DIM) dep = kind == 3;
+        else if (q == L::P) dep = kind >= 0 && kind <= 2;
+        else if (q == L::K) dep = cv.kkind[f] == 1;
+        else dep = cv.wkind[f] == 1;
+        if (!dep) continue;
+        double phib = 0.0;
+#pragma unroll
+        for (int j = 0; j < DIM; ++j) phib += S[j] * aw.Gb[((long)q * DIM + j) * nc + o] * ivo;
+        acc[q] += phib;
+      }
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < NF; ++q) out[(long)q * nc + c] = acc[q];
+}

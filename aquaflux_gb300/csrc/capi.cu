@@ -5,6 +5,8 @@
 #include "internal.cuh"
 
 size_t fv_residual_work_bytes(int dim, int turb, long nc, long nf);
+size_t fv_adjoint_work_bytes(int dim, int turb, long nc);
+extern "C" int fv_dot_f64(long n, const double* x, const double* y, double* out, void* stream);
 int fv_residual_init_constants();
 
 namespace {
@@ -113,6 +115,9 @@ extern "C" int fv_case_create(const FvMesh* mesh, const FvCaseDesc* desc,
   c->work_bytes = fv_residual_work_bytes(m->dim, desc->turbulent, m->nc, m->nf);
   FV_CUDA_TRY(cudaMalloc(&c->work, c->work_bytes));
   FV_CUDA_TRY(cudaMalloc(&c->tmp, sizeof(double) * (size_t)c->nfld * m->nc));
+  FV_CUDA_TRY(cudaMalloc(&c->tmp2, sizeof(double) * (size_t)c->nfld * m->nc));
+  FV_CUDA_TRY(cudaMalloc(&c->adj, fv_adjoint_work_bytes(m->dim, desc->turbulent, m->nc)));
+  FV_CUDA_TRY(cudaMalloc(&c->dscalar, sizeof(double) * 4));
   CaseView& v = c->view;
   v.turb = desc->turbulent;
   v.rho = desc->rho;
@@ -149,6 +154,10 @@ extern "C" int fv_case_destroy(FvCase* c) {
   cudaFree(c->wdg);
   cudaFree(c->work);
   cudaFree(c->tmp);
+  cudaFree(c->tmp2);
+  cudaFree(c->adj);
+  cudaFree(c->dscalar);
+  for (cudaEvent_t e : c->prof_events) cudaEventDestroy(e);
   delete c;
   return FV_OK;
 }
@@ -229,6 +238,30 @@ extern "C" int fv_param_jvp(FvCase* c, const double* state, double* out_mu, doub
     if (rc != FV_OK) return rc;
   }
   return FV_OK;
+}
+
+extern "C" int fv_vjp(FvCase* c, const double* state, const double* w, double* residual,
+                      double* vjp, void* stream) {
+  if (!c || !state || !w || !vjp) {
+    fv_set_error("fv_vjp: bad arguments");
+    return FV_ERR_ARG;
+  }
+  return fv_case_vjp_run(c, state, w, residual, vjp, (cudaStream_t)stream);
+}
+
+extern "C" int fv_param_vjp(FvCase* c, const double* state, const double* w, double* out,
+                            void* stream) {
+  if (!c || !state || !w || !out) {
+    fv_set_error("fv_param_vjp: bad arguments");
+    return FV_ERR_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  long n = fv_case_n_unknowns(c);
+  int rc = fv_case_run(c, state, nullptr, FV_TAN_MU, nullptr, c->tmp2, s);
+  if (rc == FV_OK) rc = fv_dot_f64(n, w, c->tmp2, out, stream);
+  if (rc == FV_OK) rc = fv_case_run(c, state, nullptr, FV_TAN_INLET, nullptr, c->tmp2, s);
+  if (rc == FV_OK) rc = fv_dot_f64(n, w, c->tmp2, out + 1, stream);
+  return rc;
 }
 
 // ------------------------------------------------------------------------------ profiling

@@ -102,6 +102,9 @@ struct FvCase {
   void* work = nullptr;     // residual scratch, sized for the Dual pipeline
   size_t work_bytes = 0;
   double* tmp = nullptr;    // (n_unknowns) scratch vector
+  double* tmp2 = nullptr;   // (n_unknowns) scratch vector
+  double* adj = nullptr;    // adjoint workspace
+  double* dscalar = nullptr; // (4) device scalars
   CaseView view;
   // optional per-stage CUDA-event profiling (fv_case_profile_begin / _end)
   std::vector<cudaEvent_t> prof_events;  // max_runs * (FV_MAX_STAGES + 1)
@@ -113,6 +116,8 @@ void fv_prof_mark(FvCase* c, int k, cudaStream_t s);
 
 int fv_case_run(FvCase* c, const double* state, const double* tangent, int tangent_kind,
                 double* residual, double* jv, cudaStream_t s);
+int fv_case_vjp_run(FvCase* c, const double* state, const double* w, double* residual, double* out,
+                    cudaStream_t s);
 enum { FV_TAN_NONE = 0, FV_TAN_STATE = 1, FV_TAN_MU = 2, FV_TAN_INLET = 3 };
 
 // Wall distance + gradient for a turbulent case (mesh.cu).

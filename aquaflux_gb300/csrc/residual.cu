@@ -658,9 +658,64 @@ int dispatch_t(FvCase* cs, const double* state, const double* tangent, int kind,
   return run<Dual, DIM, TURB>(cs, st, par, R, JV, s);
 }
 
+#include "adjoint.inc.cuh"
+
+template <int DIM, bool TURB>
+int run_vjp(FvCase* cs, const double* state, const double* W, double* R, double* out,
+            cudaStream_t s) {
+  using L = Layout<DIM, TURB>;
+  const MeshView& m = cs->mesh->view;
+  const CaseView& cv = cs->view;
+  const long nc = m.nc, nf = m.nf;
+  Src<double> st{state};
+  Par<double> par{cs->mu, cs->inlet_scale};
+  int rc = run<double, DIM, TURB>(cs, st, par, R ? R : cs->tmp, nullptr, s);
+  if (rc != FV_OK) return rc;
+  // forward workspace (double layout, as written by run<double>)
+  double* G = (double*)cs->work;
+  double* cl = G + (long)L::NFLD * DIM * nc;
+  double* Gwi = cl + 4 * nc;
+  double* acown = Gwi + DIM * nc;
+  double* acnb = acown + nf;
+  double* dco = acnb + nf;
+  (void)acown;
+  (void)acnb;
+  AdjWork aw;
+  double* p = cs->adj;
+  aw.Wt = p; p += L::NFLD * nc;
+  aw.sb = p; p += L::NFLD * nc;
+  aw.Gb = p; p += L::NFLD * DIM * nc;
+  aw.dcob = p; p += nc;
+  aw.clb = p; p += 4 * nc;
+  aw.Gwib = p; p += DIM * nc;
+  constexpr int TB = 128;
+  const int bc = fv_blocks(nc, TB);
+  a_sum<DIM, TURB><<<bc, TB, 0, s>>>(m, cv, st, par, W, cl, G, Gwi, aw);
+  a_flux<DIM, TURB><<<bc, TB, 0, s>>>(m, cv, st, par, G, cl, dco, aw);
+  a_apcoef<DIM, TURB><<<bc, TB, 0, s>>>(m, cv, st, par, G, cl, dco, aw);
+  if (TURB) a_closure<DIM><<<bc, TB, 0, s>>>(m, cv, st, par, G, cl, aw);
+  a_grad<DIM, TURB><<<bc, TB, 0, s>>>(m, cv, aw, out);
+  FV_CUDA_TRY(cudaGetLastError());
+  return FV_OK;
+}
+
 bool g_const_ready = false;
 
 }  // namespace
+
+size_t fv_adjoint_work_bytes(int dim, int turb, long nc) {
+  long nfld = dim + 1 + (turb ? 2 : 0);
+  return sizeof(double) * (size_t)(2 * nfld * nc + nfld * dim * nc + nc + 4 * nc + dim * nc);
+}
+
+int fv_case_vjp_run(FvCase* cs, const double* state, const double* W, double* R, double* out,
+                    cudaStream_t s) {
+  const int dim = cs->mesh->dim;
+  const bool turb = cs->desc.turbulent != 0;
+  if (dim == 2)
+    return turb ? run_vjp<2, true>(cs, state, W, R, out, s) : run_vjp<2, false>(cs, state, W, R, out, s);
+  return turb ? run_vjp<3, true>(cs, state, W, R, out, s) : run_vjp<3, false>(cs, state, W, R, out, s);
+}
 
 size_t fv_residual_work_bytes(int dim, int turb, long nc, long nf) {
   long nfld = dim + 1 + (turb ? 2 : 0);

@@ -177,6 +177,21 @@ class FlowCase:
         check(lib().fv_jvp_shift(self._h, ptr(s), ptr(vv), ptr(sh), ptr(jv), _stream()))
         return jv
 
+    def vjp(self, state, w, *, return_residual: bool = False):
+        """``J(state)^T w`` (hand-written adjoint kernels); optionally also ``R(state)``."""
+        s, ww = self._vec(state), self._vec(w)
+        g = torch.empty_like(s)
+        r = torch.empty_like(s) if return_residual else None
+        check(lib().fv_vjp(self._h, ptr(s), ptr(ww), ptr(r), ptr(g), _stream()))
+        return (r, g) if return_residual else g
+
+    def param_vjp(self, state, w) -> torch.Tensor:
+        """``(w . dR/dmu, w . dR/d inlet_scale)`` as a 2-vector on the device."""
+        s, ww = self._vec(state), self._vec(w)
+        out = torch.empty(2, dtype=torch.float64, device="cuda")
+        check(lib().fv_param_vjp(self._h, ptr(s), ptr(ww), ptr(out), _stream()))
+        return out
+
     def param_jvp(self, state):
         """``(dR/dmu, dR/d inlet_scale)`` at ``state``."""
         s = self._vec(state)

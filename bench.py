@@ -2,9 +2,9 @@
 
 Workload: the 2,097,152-cell 3D channel with a bump, coupled (u, v, w, p) + k-omega SST
 (``aquaflux_gb300.workloads.channel3d(128)``: 6,340,608 faces, seeded bump / jitter, randomly
-permuted then RCM-renumbered cells).  One step = one evaluation of the residual and its
-Jacobian-vector product at a fixed state (the operator applied every Krylov iteration of the
-Newton solve).  ``value`` is faces processed per second (Gfaces/s) with inputs resident in HBM;
+permuted then RCM-renumbered cells).  One step (default ``--step vjp``) = one evaluation of the
+residual and its vector-Jacobian product (hand-written adjoint kernels) at a fixed state;
+``--step jvp`` times the residual + Jacobian-vector product (the Krylov operator) instead.  ``value`` is faces processed per second (Gfaces/s) with inputs resident in HBM;
 ``e2e`` is the same step through the C ABI with host (pinned) inputs / outputs copied inside the
 timed region.
 
@@ -30,6 +30,8 @@ sys.path.insert(0, ROOT)
 
 METRIC = "Newton-solve s & residual+VJP Gfaces/s at 2M cells: FP32-precond vs FP64, 1 GB300"
 UNIT = "Gfaces/s"
+STEP_DESC = {"vjp": "residual + VJP (hand-written adjoint) at a fixed state",
+             "jvp": "residual + JVP (Krylov operator) at a fixed state"}
 CLOCK_QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
                "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
                "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -44,6 +46,7 @@ def _args():
     ap.add_argument("--size", type=int, default=128, help="cells per axis of the 3D channel")
     ap.add_argument("--cpu-sample", type=int, default=24, help="cells per axis of the CPU sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--step", default="vjp", choices=["vjp", "jvp"])
     return ap.parse_args()
 
 
@@ -136,9 +139,9 @@ def measured_peaks() -> dict:
 
 
 # ----------------------------------------------------------------------------- CPU reference
-def cpu_residual_jvp_rate(size: int, min_seconds: float = 8.0) -> dict:
-    """Faces/s of the float64 CPU oracle (the reference algorithm restated; residual + autograd JVP)
-    on a ``size^3`` sample of the channel workload, all host threads."""
+def cpu_residual_jvp_rate(size: int, min_seconds: float = 8.0, step: str = "vjp") -> dict:
+    """Faces/s of the float64 CPU oracle (the reference algorithm restated; residual + autograd
+    VJP or JVP) on a ``size^3`` sample of the channel workload, all host threads."""
     import numpy as np
     import torch
 
@@ -155,18 +158,26 @@ def cpu_residual_jvp_rate(size: int, min_seconds: float = 8.0) -> dict:
     orc = fo.Oracle(case)
     s = wl.initial_state(seed=1, noise=0.05)
     v = np.random.default_rng(2).standard_normal(s.size)
-    orc.jvp(s, v)  # warm
+    def one():
+        if step == "vjp":
+            x = torch.as_tensor(s).requires_grad_(True)
+            r = orc.residual(x)
+            torch.autograd.grad(r, x, torch.as_tensor(v))
+        else:
+            orc.residual(torch.as_tensor(s))
+            orc.jvp(s, v)
+
+    one()  # warm
     n, t0 = 0, time.perf_counter()
     while True:
-        orc.residual(torch.as_tensor(s))
-        orc.jvp(s, v)
+        one()
         n += 1
         el = time.perf_counter() - t0
         if el >= min_seconds:
             break
     return {"faces_per_s": n * wl.mesh.n_faces / el, "cores": threads,
             "sample": f"{size}^3 channel ({wl.mesh.n_cells} cells, {wl.mesh.n_faces} faces), "
-                      f"{n} residual+JVP evaluations in {el:.1f} s"}
+                      f"{n} residual+{step.upper()} evaluations in {el:.1f} s"}
 
 
 # ----------------------------------------------------------------------------- GPU arm
@@ -196,8 +207,10 @@ def run_gpu(args, rank: int, world: int, local_rank: int) -> dict | None:
     L = lib()
     stream = torch.cuda.current_stream()
 
+    fn = L.fv_vjp if args.step == "vjp" else L.fv_jvp
+
     def step():
-        check(L.fv_jvp(case.handle, ptr(state), ptr(vec), ptr(r), ptr(jv), stream.cuda_stream))
+        check(fn(case.handle, ptr(state), ptr(vec), ptr(r), ptr(jv), stream.cuda_stream))
 
     for _ in range(max(args.warmup, 3)):
         step()
@@ -216,7 +229,7 @@ def run_gpu(args, rank: int, world: int, local_rank: int) -> dict | None:
     ms = start.elapsed_time(end)
     stage_ms, runs = case.profile_end()
     if not torch.isfinite(jv).all() or not torch.isfinite(r).all():
-        raise RuntimeError("non-finite residual / JVP in the benchmark step")
+        raise RuntimeError("non-finite residual / derivative in the benchmark step")
     t = torch.tensor([ms], device="cuda", dtype=torch.float64)
     if dist is not None:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -233,7 +246,7 @@ def run_gpu(args, rank: int, world: int, local_rank: int) -> dict | None:
     def e2e_step():
         d_state.copy_(h_state, non_blocking=True)
         d_vec.copy_(h_vec, non_blocking=True)
-        check(L.fv_jvp(case.handle, ptr(d_state), ptr(d_vec), ptr(r), ptr(jv), stream.cuda_stream))
+        check(fn(case.handle, ptr(d_state), ptr(d_vec), ptr(r), ptr(jv), stream.cuda_stream))
         h_r.copy_(r, non_blocking=True)
         h_jv.copy_(jv, non_blocking=True)
 
@@ -274,14 +287,14 @@ def run_gpu(args, rank: int, world: int, local_rank: int) -> dict | None:
         "data": "synthetic",
         "config": {"workload": f"channel3d {args.size}^3 k-omega SST (u,v,w,p,k,omega), "
                                f"{wl.mesh.n_cells} cells, {F} faces",
-                   "step": "residual + JVP (Krylov operator) at a fixed state",
+                   "step": STEP_DESC[args.step],
                    "cells": wl.mesh.n_cells, "faces": F,
                    "l2": "working set > 2 GB per step (inputs larger than the 129 MB L2)",
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": round(world * F * args.steps / (e2e_ms * 1e-3) / 1e9, 4), "unit": UNIT,
                 "h2d_bytes_per_step": 2 * state.numel() * 8,
                 "d2h_bytes_per_step": 2 * state.numel() * 8},
-        "gpu_launches": 6 * args.steps,
+        "gpu_launches": (6 + (5 if args.step == "vjp" else 0)) * args.steps,
         "stage_ms_per_step": {k: round(v / max(runs, 1), 4) for k, v in stage_ms.items()},
         "algorithmic_bytes_per_face": round(bpf, 2),
         "step_achieved_gbs": round(bpf * F / (ms / args.steps * 1e-3) / 1e9, 1),
@@ -292,17 +305,18 @@ def run_gpu(args, rank: int, world: int, local_rank: int) -> dict | None:
         "clocks": clk.summary(),
     }
     if not args.no_cpu_baseline:
-        cb = cpu_residual_jvp_rate(args.cpu_sample)
+        cb = cpu_residual_jvp_rate(args.cpu_sample, step=args.step)
         out["cpu_baseline"] = {"value": round(cb["faces_per_s"] / 1e9, 6), "unit": UNIT,
                                "cores": cb["cores"], "kind": "port", "sample": cb["sample"]}
     return out
 
 
 def run_reference(args) -> dict:
-    cb = cpu_residual_jvp_rate(args.cpu_sample, min_seconds=4.0)
+    cb = cpu_residual_jvp_rate(args.cpu_sample, min_seconds=4.0, step=args.step)
     rates = [cb["faces_per_s"]]
     for _ in range(max(args.steps, 1) - 1):
-        rates.append(cpu_residual_jvp_rate(args.cpu_sample, min_seconds=2.0)["faces_per_s"])
+        rates.append(cpu_residual_jvp_rate(args.cpu_sample, min_seconds=2.0,
+                                           step=args.step)["faces_per_s"])
     v = statistics.median(rates) / 1e9
     return {
         "impl": "reference", "metric": METRIC, "value": round(v, 6), "unit": UNIT, "n_gpus": 0,
@@ -310,7 +324,7 @@ def run_reference(args) -> dict:
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"channel3d {args.size}^3 k-omega SST; CPU sample "
                                f"{args.cpu_sample}^3 per step",
-                   "step": "residual + JVP (Krylov operator) at a fixed state"},
+                   "step": STEP_DESC[args.step]},
         "cpu_baseline": {"value": round(v, 6), "unit": UNIT, "cores": cb["cores"], "kind": "port",
                          "sample": cb["sample"]},
         "e2e": {"value": round(v, 6), "unit": UNIT, "h2d_bytes_per_step": 0,

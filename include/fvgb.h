@@ -115,6 +115,15 @@ int fv_jvp_shift(FvCase* c, const double* state, const double* v, const double* 
  * out_mu = dR/dmu, out_inlet = dR/d(inlet_scale) (either may be NULL).  Device. */
 int fv_param_jvp(FvCase* c, const double* state, double* out_mu, double* out_inlet, void* stream);
 
+/* vjp = J(state)^T w, the vector-Jacobian product jax.vjp(R(., theta), state) of
+ * aquaflux/solve/implicit.py:753 (hand-written adjoint kernels; geometry is held fixed).
+ * `residual` (may be NULL) receives R(state), computed by the same forward pass.  Device. */
+int fv_vjp(FvCase* c, const double* state, const double* w, double* residual, double* vjp,
+           void* stream);
+/* Parameter cotangents w^T dR/dtheta for theta = (mu, inlet_scale): the vjp_theta of
+ * aquaflux/solve/implicit.py:759-760.  `out` is a device array of 2 doubles. */
+int fv_param_vjp(FvCase* c, const double* state, const double* w, double* out, void* stream);
+
 /* Per-stage CUDA-event timing of the next `max_runs` pipeline runs on this case (diagnostics;
  * no reference counterpart).  profile_end synchronizes, writes the summed milliseconds of each
  * stage (grad, closure, apcoef, dcoeff, flux, sum) and the number of runs recorded. */

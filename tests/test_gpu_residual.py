@@ -134,3 +134,62 @@ def test_bad_state_shape_rejected():
     fc, case, d, p = device_case("cav8")
     with pytest.raises(ValueError):
         fc.residual(np.zeros(fc.n_unknowns + 1))
+
+
+@pytest.mark.parametrize("name", ALL)
+def test_vjp_matches_oracle(name):
+    fc, case, d, p = device_case(name)
+    orc = fo.Oracle(case)
+    rng = np.random.default_rng(11)
+    for s in d[p + "states"][:2]:
+        w = rng.standard_normal(s.size)
+        r, g = fc.vjp(s, w, return_residual=True)
+        ref = orc.vjp(s, w).numpy()
+        assert _rel(g, ref) <= 1e-11, name
+        assert _rel(r, orc.residual(torch.as_tensor(s)).numpy()) <= 1e-12
+
+
+@pytest.mark.parametrize("name", ALL)
+def test_vjp_is_the_transpose_of_jvp_on_gpu(name):
+    fc, case, d, p = device_case(name)
+    rng = np.random.default_rng(13)
+    s = d[p + "states"][0]
+    v = rng.standard_normal(s.size)
+    w = rng.standard_normal(s.size)
+    jv = fc.jvp(s, v).cpu().numpy()
+    g = fc.vjp(s, w).cpu().numpy()
+    lhs, rhs = float(np.dot(w, jv)), float(np.dot(g, v))
+    scale = float(np.abs(w * jv).sum())
+    assert abs(lhs - rhs) <= 1e-12 * scale
+
+
+@pytest.mark.parametrize("name", ["cavj", "lam3", "sst2", "sst3"])
+def test_param_vjp_matches_oracle(name):
+    fc, case, d, p = device_case(name)
+    orc = fo.Oracle(case)
+    s = torch.as_tensor(d[p + "states"][0])
+    w = torch.randn(s.numel(), dtype=torch.float64)
+    mu = torch.tensor(case["mu"], dtype=torch.float64, requires_grad=True)
+    scale = torch.tensor(1.0, dtype=torch.float64, requires_grad=True)
+    r = orc.residual(s, mu=mu, inlet_scale=scale)
+    gmu, gsc = torch.autograd.grad((r * w).sum(), (mu, scale), allow_unused=True)
+    got = fc.param_vjp(s.numpy(), w.numpy()).cpu().numpy()
+    assert abs(got[0] - float(gmu)) <= 1e-10 * max(1.0, abs(float(gmu)))
+    gsc = 0.0 if gsc is None else float(gsc)
+    assert abs(got[1] - gsc) <= 1e-10 * max(1.0, abs(gsc))
+
+
+def test_vjp_at_negative_k_and_zero_state():
+    """Clamped k (max(k, 0)) and the zero state's mass-flux ties take the forward subgradients."""
+    fc, case, d, p = device_case("sst2")
+    orc = fo.Oracle(case)
+    s = d[p + "states"][2]  # contains negative k cells
+    w = np.random.default_rng(17).standard_normal(s.size)
+    assert _rel(fc.vjp(s, w), orc.vjp(s, w).numpy()) <= 1e-11
+    fc0, case0, d0, p0 = device_case("cav8")
+    z = np.zeros(fc0.n_unknowns)
+    v = np.random.default_rng(19).standard_normal(z.size)
+    w = np.random.default_rng(23).standard_normal(z.size)
+    lhs = float(np.dot(w, fc0.jvp(z, v).cpu().numpy()))
+    rhs = float(np.dot(fc0.vjp(z, w).cpu().numpy(), v))
+    assert abs(lhs - rhs) <= 1e-12 * max(1.0, abs(lhs))
