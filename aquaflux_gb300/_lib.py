@@ -56,6 +56,7 @@ SIGNATURES = {
     "fv_ilu0_apply": (c_int, [P, P, P, c_int, P]),
     "fv_ilu0_factor_values": (c_int, [P, P, P]),
     "fv_dot_f64": (c_int, [c_long, P, P, P, P]),
+    "fv_saturation_colouring": (c_int, [c_int, P, P, P, P]),
 }
 
 _lib = None

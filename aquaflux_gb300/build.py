@@ -15,7 +15,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 ROOT = os.path.dirname(HERE)
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-UNITS = {"mesh.cu": [], "residual.cu": [], "capi.cu": [], "sparse.cu": ["-fmad=false"]}
+UNITS = {"mesh.cu": [], "residual.cu": [], "capi.cu": [], "sparse.cu": ["-fmad=false"],
+         "colour.cu": []}
 
 
 def _nvcc() -> str:

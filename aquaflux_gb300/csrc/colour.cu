@@ -1,0 +1,102 @@
+// Saturation-degree greedy colouring of a conflict graph (host code).
+//
+// Restates the bucket-queue algorithm of aquaflux/solve/sparse_jacobian.py:409-534
+// (_saturation_colouring) so that the colours are identical to the reference's for the same
+// conflict graph (same CSR neighbour order):
+//   * rank(v) = saturation(v) * (max_degree + 1) + degree(v); vertices sit in one bucket per
+//     rank, each bucket a doubly linked list with insertion at the head;
+//   * initially every vertex is inserted in index order into the bucket of its degree;
+//   * each step takes the head of the highest non-empty bucket, gives it the smallest colour not
+//     taken by a coloured neighbour, then, for every still-uncoloured neighbour (in CSR order)
+//     seeing that colour for the first time, moves it to the head of its new (higher) bucket.
+// Runs in O(n + m) with a bitset of taken colours per vertex.
+#include <cstdint>
+#include <vector>
+
+#include "internal.cuh"
+
+extern "C" int fv_saturation_colouring(int n, const int* indptr, const int* indices, int* colour,
+                                       int* n_colours) {
+  if (n < 0 || (n > 0 && (!indptr || !indices || !colour))) {
+    fv_set_error("fv_saturation_colouring: bad arguments");
+    return FV_ERR_ARG;
+  }
+  if (n == 0) {
+    if (n_colours) *n_colours = 0;
+    return FV_OK;
+  }
+  std::vector<long> degree(n);
+  long max_degree = 0;
+  for (int v = 0; v < n; ++v) {
+    degree[v] = indptr[v + 1] - indptr[v];
+    if (degree[v] > max_degree) max_degree = degree[v];
+  }
+  for (long q = 0; q < indptr[n]; ++q)
+    if (indices[q] < 0 || indices[q] >= n) {
+      fv_set_error("fv_saturation_colouring: neighbour index out of range");
+      return FV_ERR_ARG;
+    }
+  const long words = max_degree / 64 + 2;
+  const long tie = max_degree + 1;
+  std::vector<uint64_t> taken((size_t)n * words, 0);
+  std::vector<long> sat(n, 0);
+  std::vector<long> head((size_t)(tie * max_degree + max_degree + 1), -1);
+  std::vector<long> next(n, -1), prev(n, -1);
+  for (int v = 0; v < n; ++v) colour[v] = -1;
+  long top = 0;
+  for (int v = 0; v < n; ++v) {
+    long r = degree[v];
+    long h = head[r];
+    next[v] = h;
+    if (h >= 0) prev[h] = v;
+    head[r] = v;
+    if (r > top) top = r;
+  }
+  int ncol = 0;
+  std::vector<int> gained;
+  for (int step = 0; step < n; ++step) {
+    while (head[top] < 0) --top;
+    const long v = head[top];
+    const long f = next[v];
+    head[top] = f;
+    if (f >= 0) prev[f] = -1;
+    int chosen = -1;
+    for (long w = 0; w < words; ++w) {
+      uint64_t freeb = ~taken[(size_t)v * words + w];
+      if (freeb) {
+        chosen = (int)(w * 64 + __builtin_ctzll(freeb));
+        break;
+      }
+    }
+    colour[v] = chosen;
+    if (chosen + 1 > ncol) ncol = chosen + 1;
+    const long word = chosen / 64;
+    const uint64_t bit = 1ull << (chosen % 64);
+    gained.clear();
+    for (int q = indptr[v]; q < indptr[v + 1]; ++q) {
+      const int u = indices[q];
+      uint64_t& t = taken[(size_t)u * words + word];
+      const bool had = (t & bit) != 0;
+      t |= bit;
+      if (!had) gained.push_back(u);
+    }
+    for (int u : gained) {
+      if (colour[u] >= 0) continue;
+      const long r_old = sat[u] * tie + degree[u];
+      sat[u] += 1;
+      const long r_new = sat[u] * tie + degree[u];
+      const long p = prev[u], fo = next[u];
+      if (p >= 0) next[p] = fo;
+      else head[r_old] = fo;
+      if (fo >= 0) prev[fo] = p;
+      const long h = head[r_new];
+      next[u] = h;
+      prev[u] = -1;
+      if (h >= 0) prev[h] = u;
+      head[r_new] = u;
+      if (r_new > top) top = r_new;
+    }
+  }
+  if (n_colours) *n_colours = ncol;
+  return FV_OK;
+}

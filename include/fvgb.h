@@ -165,6 +165,15 @@ int fv_ilu0_apply(FvIlu0* f, const void* r, void* x, int transpose, void* stream
 int fv_ilu0_factor_values(const FvIlu0* f, void* out, void* stream);
 
 /* ------------------------------------------------------------------------------------------
+ * Graph colouring for compressed Jacobian probing.  Replaces _saturation_colouring
+ * (aquaflux/solve/sparse_jacobian.py:409-534): saturation-degree greedy colouring of the conflict
+ * graph given as host CSR (the same neighbour order gives the same colours).  Host arrays;
+ * `colour` receives n ints, `n_colours` the number of colours.
+ * ------------------------------------------------------------------------------------------ */
+int fv_saturation_colouring(int n, const int* indptr, const int* indices, int* colour,
+                            int* n_colours);
+
+/* ------------------------------------------------------------------------------------------
  * Deterministic reductions for the Krylov solver (fixed blocking, fixed order: run-to-run
  * bit-identical).  Device arrays; `out` is a device scalar.
  * ------------------------------------------------------------------------------------------ */

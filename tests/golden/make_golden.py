@@ -305,12 +305,38 @@ def ilu_cases():
             "ilu_solve": x, "ilu_solve_t": xt}
 
 
+# --------------------------------------------------------------------------- colouring
+def colouring_cases():
+    """``block_stencil_colouring`` (``aquaflux/solve/sparse_jacobian.py:338-402``) on the interior
+    face graphs of small 2D / 3D meshes (one relabelled at random), reaches 1-3."""
+    from aquaflux.mesh import RandomReordering, permute_cells
+    from aquaflux.solve.sparse_jacobian import block_stencil_colouring
+
+    out = {}
+    meshes = {"c2d": structured_grid_2d(9, 7, named_boundaries=True),
+              "c3d": structured_grid_3d(5, 4, 3, named_boundaries=True)}
+    m = structured_grid_3d(4, 4, 3, named_boundaries=True)
+    meshes["c3p"] = permute_cells(m, RandomReordering(seed=3).permutation(m))
+    for name, mesh in meshes.items():
+        o, nb, _ = mesh.face_cells.interior_edges()
+        out[f"{name}_owner"] = o.astype(np.int32)
+        out[f"{name}_nb"] = nb.astype(np.int32)
+        out[f"{name}_n"] = np.array(mesh.n_cells)
+        for reach in (1, 2, 3):
+            col = block_stencil_colouring(o, nb, mesh.n_cells, reach)
+            out[f"{name}_r{reach}_colour"] = np.asarray(col.colour).astype(np.int32)
+            out[f"{name}_r{reach}_rows"] = np.asarray(col.pattern_rows).astype(np.int32)
+            out[f"{name}_r{reach}_cols"] = np.asarray(col.pattern_cols).astype(np.int32)
+    return out
+
+
 def main():
+    np.savez_compressed(os.path.join(HERE, "colouring.npz"), **colouring_cases())
     np.savez_compressed(os.path.join(HERE, "meshes.npz"), **mesh_cases())
     np.savez_compressed(os.path.join(HERE, "laminar.npz"), **laminar_cases())
     np.savez_compressed(os.path.join(HERE, "sst.npz"), **sst_cases())
     np.savez_compressed(os.path.join(HERE, "ilu0.npz"), **ilu_cases())
-    for f in ("meshes", "laminar", "sst", "ilu0"):
+    for f in ("colouring", "meshes", "laminar", "sst", "ilu0"):
         print(f, os.path.getsize(os.path.join(HERE, f + ".npz")))
 
 

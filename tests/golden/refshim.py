@@ -163,6 +163,10 @@ class _JnpModule(types.ModuleType):
         return np.asarray(_unwrap(x), dtype=dtype).view(JArr)
 
     @staticmethod
+    def clip(a, a_min=None, a_max=None, **_):
+        return _wrap(np.clip(_unwrap(a), a_min, a_max))
+
+    @staticmethod
     def array(x, dtype=None):
         return np.array(_unwrap(x), dtype=dtype).view(JArr)
 
