@@ -45,6 +45,8 @@ SIGNATURES = {
     "fv_residual": (c_int, [P, P, P, P]),
     "fv_jvp": (c_int, [P, P, P, P, P, P]),
     "fv_jvp_shift": (c_int, [P, P, P, P, P, P]),
+    "fv_jvp_frozen": (c_int, [P, P, P, P, P]),
+    "fv_probe_jacobian": (c_int, [P, P, c_int, P, c_int, P, P, P, P]),
     "fv_param_jvp": (c_int, [P, P, P, P, P]),
     "fv_vjp": (c_int, [P, P, P, P, P, P]),
     "fv_param_vjp": (c_int, [P, P, P, P, P]),

@@ -207,6 +207,62 @@ extern "C" int fv_jvp(FvCase* c, const double* state, const double* v, double* r
   return fv_case_run(c, state, v, FV_TAN_STATE, residual, jv, (cudaStream_t)stream);
 }
 
+extern "C" int fv_jvp_frozen(FvCase* c, const double* state, const double* v, double* jv,
+                             void* stream) {
+  if (!c || !state || !v || !jv) {
+    fv_set_error("fv_jvp_frozen: bad arguments");
+    return FV_ERR_ARG;
+  }
+  return fv_case_run(c, state, v, FV_TAN_FROZEN, nullptr, jv, (cudaStream_t)stream);
+}
+
+namespace {
+// values[q][a][field] = jv[a * n + i] for every block q = (i, j) of the pattern whose column cell
+// j has colour `colour_id` (one coloured probe of column field `field`).
+__global__ void k_probe_scatter(int n, int b, const int* ptr, const int* idx, const int* colour,
+                                int colour_id, int field, const double* jv, double* values) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const long bb = (long)b * b;
+  for (int q = ptr[i]; q < ptr[i + 1]; ++q) {
+    if (colour[idx[q]] != colour_id) continue;
+    double* blk = values + (long)q * bb;
+    for (int a = 0; a < b; ++a) blk[(long)a * b + field] = jv[(long)a * n + i];
+  }
+}
+// seed[f * n + c] = 1 where colour[c] == colour_id and f == field, else 0
+__global__ void k_probe_seed(int n, int b, const int* colour, int colour_id, int field, double* seed) {
+  long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long)n * b) return;
+  int f = (int)(t / n), c = (int)(t % n);
+  seed[t] = (f == field && colour[c] == colour_id) ? 1.0 : 0.0;
+}
+}  // namespace
+
+extern "C" int fv_probe_jacobian(FvCase* c, const double* state, int frozen, const int* colour,
+                                 int n_colours, const int* indptr, const int* indices,
+                                 double* values, void* stream) {
+  if (!c || !state || !colour || n_colours <= 0 || !indptr || !indices || !values) {
+    fv_set_error("fv_probe_jacobian: bad arguments");
+    return FV_ERR_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  const int n = c->mesh->nc, b = c->nfld;
+  const long len = (long)n * b;
+  for (int field = 0; field < b; ++field) {
+    for (int col = 0; col < n_colours; ++col) {
+      k_probe_seed<<<fv_blocks(len, 256), 256, 0, s>>>(n, b, colour, col, field, c->tmp);
+      int rc = fv_case_run(c, state, c->tmp, frozen ? FV_TAN_FROZEN : FV_TAN_STATE, nullptr,
+                           c->tmp2, s);
+      if (rc != FV_OK) return rc;
+      k_probe_scatter<<<fv_blocks(n, 256), 256, 0, s>>>(n, b, indptr, indices, colour, col, field,
+                                                          c->tmp2, values);
+    }
+  }
+  FV_CUDA_TRY(cudaGetLastError());
+  return FV_OK;
+}
+
 extern "C" int fv_jvp_shift(FvCase* c, const double* state, const double* v, const double* shift,
                             double* jv, void* stream) {
   if (!c || !state || !v || !shift || !jv) {

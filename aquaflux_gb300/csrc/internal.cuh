@@ -118,7 +118,7 @@ int fv_case_run(FvCase* c, const double* state, const double* tangent, int tange
                 double* residual, double* jv, cudaStream_t s);
 int fv_case_vjp_run(FvCase* c, const double* state, const double* w, double* residual, double* out,
                     cudaStream_t s);
-enum { FV_TAN_NONE = 0, FV_TAN_STATE = 1, FV_TAN_MU = 2, FV_TAN_INLET = 3 };
+enum { FV_TAN_NONE = 0, FV_TAN_STATE = 1, FV_TAN_MU = 2, FV_TAN_INLET = 3, FV_TAN_FROZEN = 4 };
 
 // Wall distance + gradient for a turbulent case (mesh.cu).
 int fv_wall_distance_compute(FvMesh* m, const unsigned char* swall_dev, int n_wall_faces,

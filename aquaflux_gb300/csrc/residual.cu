@@ -613,8 +613,21 @@ __global__ void __launch_bounds__(128) k_sum(MeshView m, CaseView cv, Src<T> st,
   for (int q = 0; q < NF; ++q) put<T>(R, JV, (long)q * nc + c, r[q]);
 }
 
+// Zero the tangent of n dual values (the "frozen" JVP holds gradients, closure and a_P fixed).
+__global__ void k_freeze(long n, Dual* x) {
+  long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) x[i].d = 0.0;
+}
+template <class T>
+void freeze(T*, long, cudaStream_t) {}
+template <>
+void freeze<Dual>(Dual* x, long n, cudaStream_t s) {
+  k_freeze<<<fv_blocks(n, 256), 256, 0, s>>>(n, x);
+}
+
 template <class T, int DIM, bool TURB>
-int run(FvCase* cs, Src<T> st, Par<T> par, double* R, double* JV, cudaStream_t s) {
+int run(FvCase* cs, Src<T> st, Par<T> par, double* R, double* JV, cudaStream_t s,
+        bool frozen = false) {
   using L = Layout<DIM, TURB>;
   const MeshView& m = cs->mesh->view;
   const CaseView& cv = cs->view;
@@ -636,6 +649,7 @@ int run(FvCase* cs, Src<T> st, Par<T> par, double* R, double* JV, cudaStream_t s
   k_apcoef<T, DIM, TURB><<<bf, TB, 0, s>>>(m, cv, st, par, G, cl, acown, acnb);
   fv_prof_mark(cs, 3, s);
   k_dcoeff<T><<<bc, TB, 0, s>>>(m, acown, acnb, dco);
+  if (frozen) freeze<T>(G, (long)(dco + nc - G), s);  // G, closure, Gwi, a_P coefficients, d
   fv_prof_mark(cs, 4, s);
   k_flux<T, DIM, TURB><<<bf, TB, 0, s>>>(m, cv, st, par, G, cl, dco, FL);
   fv_prof_mark(cs, 5, s);
@@ -654,8 +668,8 @@ int dispatch_t(FvCase* cs, const double* state, const double* tangent, int kind,
   }
   Par<Dual> par{{cs->mu, kind == FV_TAN_MU ? 1.0 : 0.0},
                 {cs->inlet_scale, kind == FV_TAN_INLET ? 1.0 : 0.0}};
-  Src<Dual> st{state, kind == FV_TAN_STATE ? tangent : nullptr};
-  return run<Dual, DIM, TURB>(cs, st, par, R, JV, s);
+  Src<Dual> st{state, (kind == FV_TAN_STATE || kind == FV_TAN_FROZEN) ? tangent : nullptr};
+  return run<Dual, DIM, TURB>(cs, st, par, R, JV, s, kind == FV_TAN_FROZEN);
 }
 
 #include "adjoint.inc.cuh"

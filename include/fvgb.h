@@ -107,6 +107,19 @@ int fv_residual(FvCase* c, const double* state, double* residual, void* stream);
  * aquaflux/solve/newton.py:110-111.  `residual` (may be NULL) receives R(state).  Device. */
 int fv_jvp(FvCase* c, const double* state, const double* v, double* residual, double* jv,
            void* stream);
+/* jv = J_direct v: the derivative with the gradients, the SST closure fields and the momentum
+ * diagonal a_P held at their values for `state` (a reach-1 operator: the "frozen" Jacobian the
+ * preconditioner is built from).  No reference counterpart as an entry point; it is the
+ * linearisation a Picard / SIMPLE-type preconditioner uses.  Device. */
+int fv_jvp_frozen(FvCase* c, const double* state, const double* v, double* jv, void* stream);
+/* Materialise the Jacobian (frozen = 1: J_direct; 0: the full J, exact on the pattern only when
+ * the colouring's reach covers J's) into a cell-major BSR matrix with b = number of fields, by
+ * coloured JVP probes: materialize_block_jacobian (aquaflux/solve/sparse_jacobian.py:722-847).
+ * colour (device, C) and n_colours from fv_saturation_colouring; indptr / indices (device) the
+ * block pattern over cells (sorted); values (device, nnzb * b * b) row-major blocks. */
+int fv_probe_jacobian(FvCase* c, const double* state, int frozen, const int* colour,
+                      int n_colours, const int* indptr, const int* indices, double* values,
+                      void* stream);
 /* jv = J v + shift * v (the pseudo-transient operator of aquaflux/solve/continuation.py:111-112);
  * `shift` is a device vector of the state's length. */
 int fv_jvp_shift(FvCase* c, const double* state, const double* v, const double* shift, double* jv,
