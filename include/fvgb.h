@@ -151,6 +151,19 @@ int fv_case_profile_end(FvCase* c, float* stage_ms, int n_stages, int* n_runs);
 int fv_bsr_spmv_f64(int n_block_rows, int b, const int* indptr, const int* indices,
                     const double* values, const double* x, double* y, int transpose,
                     void* stream);
+/* y = A^T x for a square BSR matrix (fp64) WITHOUT allocating device memory.  No counterpart in
+ * the reference: it serves callers that cannot allocate while they run (a CUDA-graph capture, an
+ * FFI custom call inside a framework that owns all device memory, an embedded solver that forbids
+ * allocation after start-up), where fv_bsr_spmv_f64(transpose = 1) would allocate its transpose
+ * map.  The map is built in a fixed 16 MiB static device array that every GPU loading the library
+ * holds until exit; patterns needing more than 4,194,304 ints (2 * n_block_rows + 1 + 2 * nnzb)
+ * are rejected with FV_ERR_ARG.  nnzb must equal indptr[n_block_rows].  The first call on each
+ * device looks the array's address up (cudaGetSymbolAddress) and must come before any stream
+ * capture.  All calls share the one array: calls that overlap on the GPU (different streams, or
+ * concurrent host threads) race and give wrong results.  Device arrays. */
+int fv_bsr_spmv_t_f64_noalloc(int n_block_rows, long nnzb, int b, const int* indptr,
+                              const int* indices, const double* values, const double* x,
+                              double* y, void* stream);
 /* fp32 values and vectors. */
 int fv_bsr_spmv_f32(int n_block_rows, int b, const int* indptr, const int* indices,
                     const float* values, const float* x, float* y, int transpose, void* stream);
