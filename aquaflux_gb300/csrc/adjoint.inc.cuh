@@ -70,7 +70,7 @@ __global__ void __launch_bounds__(128) a_sum(MeshView m, CaseView cv, Src<double
     const double V = m.vol[c];
     const double k = st((long)L::K * nc + c), w = st((long)L::W * nc + c);
     const double S = cl[c], F1 = cl[(long)nc + c], nut = cl[2L * nc + c], shear = cl[3L * nc + c];
-    const double nu = par.mu / cv.rho;
+    const double nu = par.nu;
     const double d = cv.wd[c];
     const bool wall = cv.wcell[c] != 0;
     const Dual kd{k, 1.0};
@@ -205,17 +205,23 @@ __device__ __forceinline__ void mn_adjoint(const MeshView& m, int f, double wgt,
 }
 
 // ---------------------------------------------------------------- a_flux
+// Forward relations reversed here (interior face, o = owner, n = neighbour, w_o = 1 - g, w_n = g):
+//   mdot = me - rho A dhat damping,  dhat = nn2 (w_o d_o + w_n d_n),
+//   damping = ((p_n - p_o) - gpf . dvec) / nd,  gpf = w_o gp_o + w_n gp_n,  pf = lerp(p) + gpf . skew
+//   F_i = pf n_i A - c (u_n - u_o + G_n . tN - G_o . tP) + mdot upwind(u),  c = m_o m_n A / den,
+//   den = dpn m_n - m_o dnn  (m = mu + rho nu_t);  F_p = mdot;
+//   F_s = (mdot / rho) upwind(phi) - c_s (phi_n - phi_o + ...), c_s from the cell diffusivities.
 template <int DIM, bool TURB>
 __global__ void __launch_bounds__(128) a_flux(MeshView m, CaseView cv, Src<double> st, Par<double> par,
                                               const double* G, const double* cl, const double* dco,
-                                              AdjWork aw) {
+                                              const double* me, AdjWork aw) {
   using L = Layout<DIM, TURB>;
   constexpr int NF = L::NFLD;
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= m.nc) return;
   const int nc = m.nc, nf = m.nf;
-  const double rho = cv.rho;
-  const double nu = par.mu / rho;
+  const double rho = cv.rho, irho = 1.0 / cv.rho;
+  const double nu = par.nu;
   double sb[NF], Gb[NF][DIM];
 #pragma unroll
   for (int q = 0; q < NF; ++q) {
@@ -242,50 +248,42 @@ __global__ void __launch_bounds__(128) a_flux(MeshView m, CaseView cv, Src<doubl
     if (f < m.nfi) {
       const int n = m.nb[f];
       const double g = m.g[f];
-      const double sgn_w = isnb ? g : 1.0 - g;  // this side's interpolation weight
+      const double wgt = isnb ? g : 1.0 - g;  // this side's interpolation weight
       double tN[DIM];
 #pragma unroll
       for (int j = 0; j < DIM; ++j) tN[j] = m.tN[(long)j * nf + f];
       double FLb[NF];
 #pragma unroll
       for (int q = 0; q < NF; ++q) FLb[q] = aw.Wt[(long)q * nc + o] - aw.Wt[(long)q * nc + n];
-      // forward recomputation
+      // forward recomputation of the face
       const double pn = st((long)L::P * nc + n);
-      const double mn = mom_normal<double, DIM, TURB>(m, st, G, rho, f, o, n, g);
-      const double rho_f = (1.0 - g) * rho + g * rho;
-      double gpf[DIM];
+      double gd = 0.0;
 #pragma unroll
       for (int j = 0; j < DIM; ++j)
-        gpf[j] = (1.0 - g) * G[((long)L::P * DIM + j) * nc + o] + g * G[((long)L::P * DIM + j) * nc + n];
-      const double dcf = (1.0 - g) * dco[o] + g * dco[n];
-      double dhat = (nrm[0] * nrm[0]) * dcf;
-#pragma unroll
-      for (int j = 1; j < DIM; ++j) dhat += (nrm[j] * nrm[j]) * dcf;
-      double gd = gpf[0] * m.dvec[f];
-#pragma unroll
-      for (int j = 1; j < DIM; ++j) gd += gpf[j] * m.dvec[(long)j * nf + f];
-      const double nd = m.nd[f];
-      const double damping = ((pn - po) - gd) / nd;
-      const double mdot = (mn - rho_f * dhat * damping) * A;
+        gd += lerp(G[((long)L::P * DIM + j) * nc + o], G[((long)L::P * DIM + j) * nc + n], g) *
+              m.dvec[(long)j * nf + f];
+      const double inv_nd = m.inv_nd[f];
+      const double dhat = m.nn2[f] * lerp(dco[o], dco[n], g);
+      const double damping = ((pn - po) - gd) * inv_nd;
+      const double mdot = me[f] - (rho * A) * dhat * damping;
       const double mnbv = TURB ? par.mu + rho * cl[2L * nc + n] : par.mu;
-      const double denom = m.dpn[f] - mo / mnbv * m.dnn[f];
+      const double iden = 1.0 / (m.dpn[f] * mnbv - mo * m.dnn[f]);
+      const double cmo = mo * mnbv * A * iden;
       const bool out = mdot >= 0.0;
       // reverse
       double mdotb = FLb[L::P];
-      double pfb = 0.0, denomb = 0.0, mob = 0.0;
+      double pfb = 0.0, cb = 0.0;
 #pragma unroll
       for (int i = 0; i < DIM; ++i) {
         const double uo = st((long)i * nc + o), un = st((long)i * nc + n);
-        double cp = 0.0, cn = 0.0;
+        double cpn = un - uo;
 #pragma unroll
-        for (int j = 0; j < DIM; ++j) {
-          cp += G[((long)i * DIM + j) * nc + o] * tP[j];
-          cn += G[((long)i * DIM + j) * nc + n] * tN[j];
-        }
-        const double num = (un - uo) + cn - cp;
+        for (int j = 0; j < DIM; ++j)
+          cpn += G[((long)i * DIM + j) * nc + n] * tN[j] - G[((long)i * DIM + j) * nc + o] * tP[j];
         const double fb = FLb[i];
         mdotb += fb * (out ? uo : un);
-        const double k1 = fb * mo * A / denom;  // d diff / d num = -mo A / denom
+        const double k1 = fb * cmo;  // F_i = ... - c cpn
+        cb -= fb * cpn;
         if (!isnb) {
           sb[i] += k1 + (out ? fb * mdot : 0.0);
 #pragma unroll
@@ -293,42 +291,40 @@ __global__ void __launch_bounds__(128) a_flux(MeshView m, CaseView cv, Src<doubl
         } else {
           sb[i] += -k1 + (!out ? fb * mdot : 0.0);
 #pragma unroll
-          for (int j = 0; j < DIM; ++j) Gb[i][j] += -k1 * tN[j];
+          for (int j = 0; j < DIM; ++j) Gb[i][j] -= k1 * tN[j];
         }
-        denomb += fb * mo * num * A / (denom * denom);
-        mob += fb * (-num * A / denom);
         pfb += fb * nrm[i] * A;
       }
-      mob += denomb * (-m.dnn[f] / mnbv);
-      const double mnbb = denomb * (mo * m.dnn[f] / (mnbv * mnbv));
-      // pf = (1-g) po + g pn + gpf . skew
+      if (TURB) {
+        // c = m_o m_n A / (dpn m_n - m_o dnn): dc/dm_o = c (1/m_o + dnn/den), dc/dm_n = c (1/m_n - dpn/den)
+        const double mXb = isnb ? cb * cmo * (1.0 / mnbv - m.dpn[f] * iden)
+                                : cb * cmo * (1.0 / mo + m.dnn[f] * iden);
+        ntb += mXb * rho;
+      }
+      // pf = lerp(p) + gpf . skew
       double gpfb[DIM];
 #pragma unroll
       for (int j = 0; j < DIM; ++j) gpfb[j] = pfb * m.skew[(long)j * nf + f];
-      sb[L::P] += sgn_w * pfb;
+      sb[L::P] += wgt * pfb;
       if (TURB) {
-        const double vflux = mdot / rho;
+        const double vflux = mdot * irho;
         const bool vout = vflux >= 0.0;
-        const double F1o = cl[(long)nc + o], F1n = cl[(long)nc + n];
-        const double nto = cl[2L * nc + o], ntn = cl[2L * nc + n];
+        const double F1X = cl[(long)nc + (isnb ? n : o)], ntX = cl[2L * nc + (isnb ? n : o)];
 #pragma unroll
         for (int s = 0; s < 2; ++s) {
           const int q = s == 0 ? L::K : L::W;
           const double in = s == 0 ? SIGMA_K1 : SIGMA_W1, ou = s == 0 ? SIGMA_K2 : SIGMA_W2;
-          const double bo = F1o * in + (1.0 - F1o) * ou, bn = F1n * in + (1.0 - F1n) * ou;
-          const double go = nu + bo * nto, gn = nu + bn * ntn;
+          const double go = cl[(4L + s) * nc + o], gn = cl[(4L + s) * nc + n];
           const double phio = st((long)q * nc + o), phin = st((long)q * nc + n);
-          double cp = 0.0, cn = 0.0;
+          double cpn = phin - phio;
 #pragma unroll
-          for (int j = 0; j < DIM; ++j) {
-            cp += G[((long)q * DIM + j) * nc + o] * tP[j];
-            cn += G[((long)q * DIM + j) * nc + n] * tN[j];
-          }
-          const double num = (phin - phio) + cn - cp;
-          const double den = m.dpn[f] - go / gn * m.dnn[f];
+          for (int j = 0; j < DIM; ++j)
+            cpn += G[((long)q * DIM + j) * nc + n] * tN[j] - G[((long)q * DIM + j) * nc + o] * tP[j];
+          const double idn = 1.0 / (m.dpn[f] * gn - go * m.dnn[f]);
+          const double cs_ = go * gn * A * idn;
           const double fb = FLb[q];
-          mdotb += fb * (vout ? phio : phin) / rho;
-          const double k1 = fb * go * A / den;
+          mdotb += fb * (vout ? phio : phin) * irho;
+          const double k1 = fb * cs_;
           if (!isnb) {
             sb[q] += k1 + (vout ? fb * vflux : 0.0);
 #pragma unroll
@@ -336,43 +332,32 @@ __global__ void __launch_bounds__(128) a_flux(MeshView m, CaseView cv, Src<doubl
           } else {
             sb[q] += -k1 + (!vout ? fb * vflux : 0.0);
 #pragma unroll
-            for (int j = 0; j < DIM; ++j) Gb[q][j] += -k1 * tN[j];
+            for (int j = 0; j < DIM; ++j) Gb[q][j] -= k1 * tN[j];
           }
-          const double denb = fb * go * num * A / (den * den);
-          const double gob = fb * (-num * A / den) + denb * (-m.dnn[f] / gn);
-          const double gnb = denb * (go * m.dnn[f] / (gn * gn));
-          if (!isnb) {
-            F1b += gob * (in - ou) * nto;
-            ntb += gob * bo;
-          } else {
-            F1b += gnb * (in - ou) * ntn;
-            ntb += gnb * bn;
-          }
+          const double csb = -fb * cpn;
+          const double gXb = isnb ? csb * cs_ * (1.0 / gn - m.dpn[f] * idn)
+                                  : csb * cs_ * (1.0 / go + m.dnn[f] * idn);
+          // gamma_X = nu + (sig_out + F1 (sig_in - sig_out)) nu_t
+          F1b += gXb * (in - ou) * ntX;
+          ntb += gXb * (ou + F1X * (in - ou));
         }
-        if (!isnb) ntb += mob * rho;
-        else ntb += mnbb * rho;
       }
-      // mdot = (mn - rho_f dhat damping) A
-      const double mnb = mdotb * A;
-      const double dhatb = -mdotb * A * rho_f * damping;
-      const double dampb = -mdotb * A * rho_f * dhat;
-      sb[L::P] += isnb ? dampb / nd : -dampb / nd;
+      // mdot = me - rho A dhat damping
+      const double dhatb = -mdotb * (rho * A) * damping;
+      const double dampb = -mdotb * (rho * A) * dhat;
+      sb[L::P] += isnb ? dampb * inv_nd : -dampb * inv_nd;
 #pragma unroll
-      for (int j = 0; j < DIM; ++j) gpfb[j] += -dampb / nd * m.dvec[(long)j * nf + f];
+      for (int j = 0; j < DIM; ++j) gpfb[j] -= dampb * inv_nd * m.dvec[(long)j * nf + f];
 #pragma unroll
-      for (int j = 0; j < DIM; ++j) Gb[L::P][j] += sgn_w * gpfb[j];
-      dcb += dhatb * m.nn2[f] * sgn_w;
-      double ub[DIM], Gub[DIM * DIM];
-#pragma unroll
-      for (int j = 0; j < DIM; ++j) ub[j] = 0.0;
-#pragma unroll
-      for (int j = 0; j < DIM * DIM; ++j) Gub[j] = 0.0;
-      mn_adjoint<DIM>(m, f, sgn_w, rho, mnb, ub, Gub);
+      for (int j = 0; j < DIM; ++j) Gb[L::P][j] += wgt * gpfb[j];
+      dcb += dhatb * m.nn2[f] * wgt;
+      // me = rho A (sum_j n_j lerp(u_j) + sum_jq ns_jq lerp(G_jq))
+      const double meb = mdotb * rho * A * wgt;
 #pragma unroll
       for (int j = 0; j < DIM; ++j) {
-        sb[j] += ub[j];
+        sb[j] += meb * nrm[j];
 #pragma unroll
-        for (int q = 0; q < DIM; ++q) Gb[j][q] += Gub[j * DIM + q];
+        for (int q = 0; q < DIM; ++q) Gb[j][q] += meb * m.ns[(long)(j * DIM + q) * nf + f];
       }
     } else {
       // boundary face: this cell is the owner
@@ -391,7 +376,7 @@ __global__ void __launch_bounds__(128) a_flux(MeshView m, CaseView cv, Src<doubl
         double un = bu[0] * nrm[0];
 #pragma unroll
         for (int j = 1; j < DIM; ++j) un += bu[j] * nrm[j];
-        mdot = rho * un * A;
+        mdot = (rho * A) * un;
       } else if (kind == 3) {
         double un = uo[0] * nrm[0];
         interp = G[((long)L::P * DIM) * nc + o] * nrm[0];
@@ -400,11 +385,9 @@ __global__ void __launch_bounds__(128) a_flux(MeshView m, CaseView cv, Src<doubl
           un += uo[j] * nrm[j];
           interp += G[((long)L::P * DIM + j) * nc + o] * nrm[j];
         }
-        dh = (nrm[0] * nrm[0]) * dco[o];
-#pragma unroll
-        for (int j = 1; j < DIM; ++j) dh += (nrm[j] * nrm[j]) * dco[o];
-        compact = (cv.fp[f] - po) / m.nd[f];
-        mdot = rho * (un - dh * (compact - interp)) * A;
+        dh = m.nn2[f] * dco[o];
+        compact = (cv.fp[f] - po) * m.inv_nd[f];
+        mdot = (rho * A) * (un - dh * (compact - interp));
       }
       double gbv = mo;
       double dgb_dk = 0.0;  // d gamma_b / d k_owner (SST wall faces)
@@ -419,6 +402,7 @@ __global__ void __launch_bounds__(128) a_flux(MeshView m, CaseView cv, Src<doubl
           gbv = par.mu;
         }
       }
+      const double Ad = A * m.inv_dpn[f];
       const bool out = mdot >= 0.0;
       double mdotb = FLb[L::P], pfb = 0.0, gbb = 0.0;
 #pragma unroll
@@ -429,28 +413,27 @@ __global__ void __launch_bounds__(128) a_flux(MeshView m, CaseView cv, Src<doubl
         const double num = bu[i] - uo[i] - cp;
         const double fb = FLb[i];
         mdotb += fb * (out ? uo[i] : bu[i]);
-        const double numb = fb * (-gbv * A / m.dpn[f]);
-        gbb += fb * (-num * A / m.dpn[f]);
+        const double numb = -fb * gbv * Ad;
+        gbb -= fb * num * Ad;
         const double bub = numb + (!out ? fb * mdot : 0.0);
         sb[i] += -numb + (out ? fb * mdot : 0.0);
         if (kind == 3) sb[i] += bub;
 #pragma unroll
-        for (int j = 0; j < DIM; ++j) Gb[i][j] += -numb * tP[j];
+        for (int j = 0; j < DIM; ++j) Gb[i][j] -= numb * tP[j];
         pfb += fb * nrm[i] * A;
       }
       if (kind >= 0 && kind <= 2) sb[L::P] += pfb;
       if (TURB) {
         if (gb_is_mo) ntb += gbb * rho;
         else sb[L::K] += gbb * dgb_dk;
-        const double vflux = mdot / rho;
+        const double vflux = mdot * irho;
         const bool vout = vflux >= 0.0;
         const double F1o = cl[(long)nc + o], nto = cl[2L * nc + o];
 #pragma unroll
         for (int s = 0; s < 2; ++s) {
           const int q = s == 0 ? L::K : L::W;
           const double in = s == 0 ? SIGMA_K1 : SIGMA_W1, ou = s == 0 ? SIGMA_K2 : SIGMA_W2;
-          const double bo = F1o * in + (1.0 - F1o) * ou;
-          const double go = nu + bo * nto;
+          const double go = cl[(4L + s) * nc + o];
           const double phio = st((long)q * nc + o);
           double cp = 0.0;
 #pragma unroll
@@ -468,13 +451,13 @@ __global__ void __launch_bounds__(128) a_flux(MeshView m, CaseView cv, Src<doubl
           }
           const double num = bphi - phio - cp;
           const double fb = FLb[q];
-          mdotb += fb * (vout ? phio : bphi) / rho;
-          const double numb = fb * (-gface * A / m.dpn[f]);
-          const double gfb = fb * (-num * A / m.dpn[f]);
+          mdotb += fb * (vout ? phio : bphi) * irho;
+          const double numb = -fb * gface * Ad;
+          const double gfb = -fb * num * Ad;
           const double bphib = numb + (!vout ? fb * vflux : 0.0);
           sb[q] += -numb + (vout ? fb * vflux : 0.0);
 #pragma unroll
-          for (int j = 0; j < DIM; ++j) Gb[q][j] += -numb * tP[j];
+          for (int j = 0; j < DIM; ++j) Gb[q][j] -= numb * tP[j];
           if (sk == 1) {
             sb[q] += bphib;
 #pragma unroll
@@ -483,23 +466,20 @@ __global__ void __launch_bounds__(128) a_flux(MeshView m, CaseView cv, Src<doubl
           double gob = gfb;
           if (wallk) {
             gob = gfb * (1.0 - wwv);
-            sb[L::K] += -gfb * go * wwd;
+            sb[L::K] -= gfb * go * wwd;
           }
           F1b += gob * (in - ou) * nto;
-          ntb += gob * bo;
+          ntb += gob * (ou + F1o * (in - ou));
         }
       }
       if (kind == 3) {
         const double base = mdotb * rho * A;
 #pragma unroll
         for (int j = 0; j < DIM; ++j) sb[j] += base * nrm[j];
-        const double dhb = -base * (compact - interp);
-        dcb += dhb * m.nn2[f];
-        const double compb = -base * dh;
-        sb[L::P] += -compb / m.nd[f];
-        const double interpb = base * dh;
+        dcb -= base * (compact - interp) * m.nn2[f];
+        sb[L::P] += base * dh * m.inv_nd[f];
 #pragma unroll
-        for (int j = 0; j < DIM; ++j) Gb[L::P][j] += interpb * nrm[j];
+        for (int j = 0; j < DIM; ++j) Gb[L::P][j] += base * dh * nrm[j];
       }
     }
   }
@@ -521,7 +501,7 @@ __global__ void __launch_bounds__(128) a_flux(MeshView m, CaseView cv, Src<doubl
 template <int DIM, bool TURB>
 __global__ void __launch_bounds__(128) a_apcoef(MeshView m, CaseView cv, Src<double> st, Par<double> par,
                                                 const double* G, const double* cl, const double* dco,
-                                                AdjWork aw) {
+                                                const double* me, AdjWork aw) {
   using L = Layout<DIM, TURB>;
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= m.nc) return;
@@ -540,39 +520,47 @@ __global__ void __launch_bounds__(128) a_apcoef(MeshView m, CaseView cv, Src<dou
     const bool isnb = (ent & FV_NB_BIT) != 0;
     const int o = m.owner[f];
     const double A = m.area[f];
-    const double abo = -aw.dcob[o] * dco[o] * dco[o] / m.vol[o];
-    const double mo = TURB ? par.mu + rho * cl[2L * nc + o] : par.mu;
+    const double abo = -aw.dcob[o] * dco[o] * dco[o] * m.inv_vol[o];
+    const double mdot = me[f];
+    double meb;
     if (f < m.nfi) {
       const int n = m.nb[f];
       const double g = m.g[f];
-      const double abn = -aw.dcob[n] * dco[n] * dco[n] / m.vol[n];
-      const double mdot = mom_normal<double, DIM, TURB>(m, st, G, rho, f, o, n, g) * A;
-      const double mnbv = TURB ? par.mu + rho * cl[2L * nc + n] : par.mu;
-      const double den = m.dpn[f] - mo / mnbv * m.dnn[f];
-      const double viscb = abo + abn;
-      const double mdotb = abo * dpos(mdot) - abn * dpos(-mdot);
-      const double denb = -viscb * mo * A / (den * den);
-      const double mob = viscb * A / den + denb * (-m.dnn[f] / mnbv);
-      const double mnbb = denb * (mo * m.dnn[f] / (mnbv * mnbv));
-      if (TURB) ntb += (isnb ? mnbb : mob) * rho;
-      mn_adjoint<DIM>(m, f, isnb ? g : 1.0 - g, rho, mdotb * A, ub, Gub);
+      const double abn = -aw.dcob[n] * dco[n] * dco[n] * m.inv_vol[n];
+      meb = (abo * dpos(mdot) - abn * dpos(-mdot)) * (isnb ? g : 1.0 - g);
+      if (TURB) {
+        const double mo = par.mu + rho * cl[2L * nc + o];
+        const double mnbv = par.mu + rho * cl[2L * nc + n];
+        const double iden = 1.0 / (m.dpn[f] * mnbv - mo * m.dnn[f]);
+        const double cv_ = mo * mnbv * A * iden;
+        const double viscb = abo + abn;
+        ntb += rho * viscb * cv_ * (isnb ? (1.0 / mnbv - m.dpn[f] * iden)
+                                          : (1.0 / mo + m.dnn[f] * iden));
+      }
     } else {
       const signed char kind = cv.fkind[f];
-      const double mdot = mom_normal<double, DIM, TURB>(m, st, G, rho, f, o, o, 0.0) * A;
       const double vob = (kind >= 0 && kind <= 2) ? abo : 0.0;
       const double convb = (kind == 2 || kind == 3) ? abo : 0.0;
-      mn_adjoint<DIM>(m, f, 1.0, rho, convb * dpos(mdot) * A, ub, Gub);
+      meb = convb * dpos(mdot);
       if (TURB && vob != 0.0) {
+        const double Ad = A * m.inv_nd[f];
         if (kind == 0 || kind == 1) {
           if (cv.swall[f]) {
-            Dual nw = nut_wall(Dual{par.mu / rho, 0.0}, cv.wd[o],
-                               Dual{st((long)L::K * nc + o), 1.0});
-            kb += vob * A / m.nd[f] * rho * nw.d;
+            Dual nw = nut_wall(Dual{par.nu, 0.0}, cv.wd[o], Dual{st((long)L::K * nc + o), 1.0});
+            kb += vob * Ad * rho * nw.d;
           }
         } else {
-          ntb += vob * A / m.nd[f] * rho;
+          ntb += vob * Ad * rho;
         }
       }
+    }
+    // me = rho A (sum_j n_j lerp(u_j) + sum_jq ns_jq lerp(G_jq)); meb already carries the weight
+    const double t = meb * rho * A;
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) {
+      ub[j] += t * m.normal[(long)j * nf + f];
+#pragma unroll
+      for (int q = 0; q < DIM; ++q) Gub[j * DIM + q] += t * m.ns[(long)(j * DIM + q) * nf + f];
     }
   }
 #pragma unroll
@@ -596,7 +584,7 @@ __global__ void __launch_bounds__(128) a_closure(MeshView m, CaseView cv, Src<do
   if (c >= m.nc) return;
   const int nc = m.nc, nf = m.nf;
   const double k = st((long)L::K * nc + c), w = st((long)L::W * nc + c);
-  const double nu = par.mu / cv.rho;
+  const double nu = par.nu;
   const double d = cv.wd[c];
   const bool wall = cv.wcell[c] != 0;
   double Sb = aw.clb[c], F1b = aw.clb[(long)nc + c], ntb = aw.clb[2L * nc + c];

@@ -31,6 +31,14 @@ __global__ void k_axpy_shift(long n, const double* shift, const double* v, doubl
   if (i < n) out[i] += shift[i] * v[i];
 }
 
+__global__ void k_inv_distance(int nc, const double* wd, double* inv) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  const double r = wd[c] > 0.0 ? 1.0 / wd[c] : 0.0;
+  inv[c] = r;
+  inv[nc + c] = r * r;
+}
+
 __global__ void k_cell_to_rowmajor(int nc, int dim, const double* in, double* out) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nc) return;
@@ -105,12 +113,15 @@ extern "C" int fv_case_create(const FvMesh* mesh, const FvCaseDesc* desc,
   FV_CUDA_TRY(cudaMalloc(&c->wdg, sizeof(double) * m->nc * m->dim));
   FV_CUDA_TRY(cudaMemsetAsync(c->wd, 0, sizeof(double) * m->nc, s));
   FV_CUDA_TRY(cudaMemsetAsync(c->wdg, 0, sizeof(double) * m->nc * m->dim, s));
+  FV_CUDA_TRY(cudaMalloc(&c->inv_wd, sizeof(double) * 2 * m->nc));
+  FV_CUDA_TRY(cudaMemsetAsync(c->inv_wd, 0, sizeof(double) * 2 * m->nc, s));
   if (desc->turbulent) {
     rc = fv_wall_distance_compute(m, c->swall, n_wall, c->wd, c->wdg, s);
     if (rc != FV_OK) {
       fv_case_destroy(c);
       return rc;
     }
+    k_inv_distance<<<fv_blocks(m->nc, 256), 256, 0, s>>>(m->nc, c->wd, c->inv_wd);
   }
   c->work_bytes = fv_residual_work_bytes(m->dim, desc->turbulent, m->nc, m->nf);
   FV_CUDA_TRY(cudaMalloc(&c->work, c->work_bytes));
@@ -134,6 +145,8 @@ extern "C" int fv_case_create(const FvMesh* mesh, const FvCaseDesc* desc,
   v.wcell = c->wcell;
   v.wd = c->wd;
   v.wdg = c->wdg;
+  v.inv_wd = c->inv_wd;
+  v.inv_wd2 = c->inv_wd + m->nc;
   FV_CUDA_TRY(cudaStreamSynchronize(s));
   *out = c;
   return FV_OK;
@@ -152,6 +165,7 @@ extern "C" int fv_case_destroy(FvCase* c) {
   cudaFree(c->wcell);
   cudaFree(c->wd);
   cudaFree(c->wdg);
+  cudaFree(c->inv_wd);
   cudaFree(c->work);
   cudaFree(c->tmp);
   cudaFree(c->tmp2);
@@ -324,8 +338,12 @@ extern "C" int fv_param_vjp(FvCase* c, const double* state, const double* w, dou
 void fv_prof_mark(FvCase* c, int k, cudaStream_t s) {
   if (c->prof_max_runs == 0 || c->prof_runs >= c->prof_max_runs) return;
   if (k + 1 > c->prof_stages) c->prof_stages = k + 1;
+  if (k + 1 > c->prof_run_marks[c->prof_runs]) c->prof_run_marks[c->prof_runs] = k + 1;
   cudaEventRecord(c->prof_events[(size_t)c->prof_runs * (FV_MAX_STAGES + 1) + k], s);
-  if (k == 6) c->prof_runs++;  // the last boundary of a pipeline run
+}
+void fv_prof_end_run(FvCase* c) {
+  if (c->prof_max_runs == 0 || c->prof_runs >= c->prof_max_runs) return;
+  c->prof_runs++;
 }
 
 extern "C" int fv_case_profile_begin(FvCase* c, int max_runs) {
@@ -339,6 +357,7 @@ extern "C" int fv_case_profile_begin(FvCase* c, int max_runs) {
   c->prof_max_runs = max_runs;
   c->prof_runs = 0;
   c->prof_stages = 0;
+  c->prof_run_marks.assign(max_runs, 0);
   return FV_OK;
 }
 
@@ -350,8 +369,10 @@ extern "C" int fv_case_profile_end(FvCase* c, float* stage_ms, int n_stages, int
   for (int k = 0; k < n_stages; ++k) stage_ms[k] = 0.0f;
   for (int r = 0; r < c->prof_runs; ++r) {
     cudaEvent_t* ev = &c->prof_events[(size_t)r * (FV_MAX_STAGES + 1)];
-    FV_CUDA_TRY(cudaEventSynchronize(ev[c->prof_stages - 1]));
-    for (int k = 0; k + 1 < c->prof_stages && k < n_stages; ++k) {
+    const int marks = c->prof_run_marks[r];
+    if (marks < 2) continue;
+    FV_CUDA_TRY(cudaEventSynchronize(ev[marks - 1]));
+    for (int k = 0; k + 1 < marks && k < n_stages; ++k) {
       float ms = 0.0f;
       FV_CUDA_TRY(cudaEventElapsedTime(&ms, ev[k], ev[k + 1]));
       stage_ms[k] += ms;

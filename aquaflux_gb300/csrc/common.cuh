@@ -33,8 +33,9 @@ FV_HD Dual operator+(Dual a, Dual b) { return {a.v + b.v, a.d + b.d}; }
 FV_HD Dual operator-(Dual a, Dual b) { return {a.v - b.v, a.d - b.d}; }
 FV_HD Dual operator*(Dual a, Dual b) { return {a.v * b.v, a.d * b.v + a.v * b.d}; }
 FV_HD Dual operator/(Dual a, Dual b) {
-  double q = a.v / b.v;
-  return {q, (a.d - q * b.d) / b.v};
+  double r = 1.0 / b.v;  // one fp64 division per dual division
+  double q = a.v * r;
+  return {q, (a.d - q * b.d) * r};
 }
 FV_HD Dual operator-(Dual a) { return {-a.v, -a.d}; }
 FV_HD Dual operator+(Dual a, double b) { return {a.v + b, a.d}; }
@@ -43,13 +44,21 @@ FV_HD Dual operator-(Dual a, double b) { return {a.v - b, a.d}; }
 FV_HD Dual operator-(double a, Dual b) { return {a - b.v, -b.d}; }
 FV_HD Dual operator*(Dual a, double b) { return {a.v * b, a.d * b}; }
 FV_HD Dual operator*(double a, Dual b) { return {a * b.v, a * b.d}; }
-FV_HD Dual operator/(Dual a, double b) { return {a.v / b, a.d / b}; }
+FV_HD Dual operator/(Dual a, double b) {
+  double r = 1.0 / b;
+  return {a.v * r, a.d * r};
+}
 FV_HD Dual operator/(double a, Dual b) {
-  double q = a / b.v;
-  return {q, -q * b.d / b.v};
+  double r = 1.0 / b.v;
+  double q = a * r;
+  return {q, -q * b.d * r};
 }
 FV_HD Dual& operator+=(Dual& a, Dual b) { a = a + b; return a; }
 FV_HD Dual& operator-=(Dual& a, Dual b) { a = a - b; return a; }
+
+// a + g (b - a): the linear owner / neighbour blend (1 - g) a + g b with one multiply-add.
+FV_HD double lerp(double a, double b, double g) { return fma(g, b - a, a); }
+FV_HD Dual lerp(Dual a, Dual b, double g) { return {fma(g, b.v - a.v, a.v), fma(g, b.d - a.d, a.d)}; }
 
 // Scalar-generic elementary functions.
 FV_HD double cst(double x, double) { return x; }

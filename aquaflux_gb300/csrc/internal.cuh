@@ -38,6 +38,10 @@ struct MeshView {
   const double* tP;            // (dim, nf) (x_f - x_P) - dpn n
   const double* tN;            // (dim, nf) (x_f - x_N) - dnn n
   const double* nn2;           // (nf) sum_j n_j n_j
+  const double* inv_nd;        // (nf) 1 / nd
+  const double* inv_dpn;       // (nf) 1 / dpn
+  const double* ns;            // (dim * dim, nf) n_j skew_q at [(j * dim + q) * nf + f]
+  const double* inv_vol;       // (nc) 1 / V
 };
 
 struct FvMesh {
@@ -80,6 +84,8 @@ struct CaseView {
   const unsigned char* wcell; // (nc) SST wall cell
   const double* wd;           // (nc) wall distance
   const double* wdg;          // (dim, nc) wall-distance gradient
+  const double* inv_wd;       // (nc) 1 / wall distance
+  const double* inv_wd2;      // (nc) 1 / wall distance^2
 };
 
 struct FvCase {
@@ -99,6 +105,7 @@ struct FvCase {
   unsigned char* wcell = nullptr;
   double* wd = nullptr;
   double* wdg = nullptr;
+  double* inv_wd = nullptr;   // (2, nc): 1 / d and 1 / d^2
   void* work = nullptr;     // residual scratch, sized for the Dual pipeline
   size_t work_bytes = 0;
   double* tmp = nullptr;    // (n_unknowns) scratch vector
@@ -109,10 +116,14 @@ struct FvCase {
   // optional per-stage CUDA-event profiling (fv_case_profile_begin / _end)
   std::vector<cudaEvent_t> prof_events;  // max_runs * (FV_MAX_STAGES + 1)
   int prof_max_runs = 0, prof_runs = 0, prof_stages = 0;
+  std::vector<int> prof_run_marks;  // boundaries recorded per run
 };
-#define FV_MAX_STAGES 8
-// Record the stage boundary `k` of the current profiled run (no-op when profiling is off).
+#define FV_MAX_STAGES 12
+// Record the stage boundary `k` of the current profiled run (no-op when profiling is off);
+// fv_prof_end_run closes the run.  Boundaries 0..6 delimit the six forward stages, 7..11 the
+// five adjoint stages of a VJP.
 void fv_prof_mark(FvCase* c, int k, cudaStream_t s);
+void fv_prof_end_run(FvCase* c);
 
 int fv_case_run(FvCase* c, const double* state, const double* tangent, int tangent_kind,
                 double* residual, double* jv, cudaStream_t s);

@@ -119,7 +119,8 @@ __global__ void k_orient(MeshView m, const double* xf, const double* approx, dou
 
 template <int DIM>
 __global__ void k_cell_geometry(MeshView m, const double* area, const double* normal,
-                                const double* xf, const double* approx, double* vol, double* xc) {
+                                const double* xf, const double* approx, double* vol, double* xc,
+                                double* inv_vol) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= m.nc) return;
   double a[DIM], cs[DIM];
@@ -144,13 +145,15 @@ __global__ void k_cell_geometry(MeshView m, const double* area, const double* no
   }
   double volume = v / (double)DIM;
   vol[c] = volume;
+  inv_vol[c] = 1.0 / volume;
   double inv = 1.0 / ((double)(DIM + 1) * volume);
   for (int j = 0; j < DIM; ++j) xc[j * m.nc + c] = cs[j] * inv + a[j];
 }
 
 template <int DIM>
 __global__ void k_face_factors(MeshView m, double* g, double* nd, double* dpn, double* dnn,
-                               double* dvec, double* skew, double* tP, double* tN, double* nn2) {
+                               double* dvec, double* skew, double* tP, double* tN, double* nn2,
+                               double* inv_nd, double* inv_dpn, double* ns) {
   int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= m.nf) return;
   const int nf = m.nf, nc = m.nc;
@@ -175,16 +178,23 @@ __global__ void k_face_factors(MeshView m, double* g, double* nd, double* dpn, d
   double dn_ = 0.0;
   for (int j = 0; j < DIM; ++j) dn_ += d[j] * n_[j];
   g[f] = gg;
-  nd[f] = interior ? dn_ : vpn;
+  const double ndv = interior ? dn_ : vpn;
+  nd[f] = ndv;
   dpn[f] = vpn;
   dnn[f] = vnn;
   nn2[f] = s2;
+  inv_nd[f] = 1.0 / ndv;
+  inv_dpn[f] = 1.0 / vpn;
+  double sk[DIM];
   for (int j = 0; j < DIM; ++j) {
     dvec[j * nf + f] = d[j];
-    skew[j * nf + f] = m.xf[j * nf + f] - (m.xc[j * nc + o] + d[j] * gg);
+    sk[j] = m.xf[j * nf + f] - (m.xc[j * nc + o] + d[j] * gg);
+    skew[j * nf + f] = sk[j];
     tP[j * nf + f] = dp[j] - n_[j] * vpn;
     tN[j * nf + f] = dn[j] - n_[j] * vnn;
   }
+  for (int j = 0; j < DIM; ++j)
+    for (int q = 0; q < DIM; ++q) ns[(long)(j * DIM + q) * nf + f] = n_[j] * sk[q];
 }
 
 // Scatter an internal-order face array (dim, nf) SoA to reference order (nf, dim) row-major.
@@ -295,20 +305,24 @@ int fv_mesh_compute_geometry(FvMesh* m, cudaStream_t s) {
     k_face_geometry<2><<<bf, kThreads, 0, s>>>(v, area, normal, xf);
     k_approx_centroid<2><<<bc, kThreads, 0, s>>>(v, xf, m->approx);
     k_orient<2><<<bf, kThreads, 0, s>>>(v, xf, m->approx, normal);
-    k_cell_geometry<2><<<bc, kThreads, 0, s>>>(v, area, normal, xf, m->approx, vol, xc);
+    k_cell_geometry<2><<<bc, kThreads, 0, s>>>(v, area, normal, xf, m->approx, vol, xc,
+                                                 const_cast<double*>(v.inv_vol));
     k_face_factors<2><<<bf, kThreads, 0, s>>>(
         v, const_cast<double*>(v.g), const_cast<double*>(v.nd), const_cast<double*>(v.dpn),
         const_cast<double*>(v.dnn), const_cast<double*>(v.dvec), const_cast<double*>(v.skew),
-        const_cast<double*>(v.tP), const_cast<double*>(v.tN), const_cast<double*>(v.nn2));
+        const_cast<double*>(v.tP), const_cast<double*>(v.tN), const_cast<double*>(v.nn2),
+        const_cast<double*>(v.inv_nd), const_cast<double*>(v.inv_dpn), const_cast<double*>(v.ns));
   } else {
     k_face_geometry<3><<<bf, kThreads, 0, s>>>(v, area, normal, xf);
     k_approx_centroid<3><<<bc, kThreads, 0, s>>>(v, xf, m->approx);
     k_orient<3><<<bf, kThreads, 0, s>>>(v, xf, m->approx, normal);
-    k_cell_geometry<3><<<bc, kThreads, 0, s>>>(v, area, normal, xf, m->approx, vol, xc);
+    k_cell_geometry<3><<<bc, kThreads, 0, s>>>(v, area, normal, xf, m->approx, vol, xc,
+                                                 const_cast<double*>(v.inv_vol));
     k_face_factors<3><<<bf, kThreads, 0, s>>>(
         v, const_cast<double*>(v.g), const_cast<double*>(v.nd), const_cast<double*>(v.dpn),
         const_cast<double*>(v.dnn), const_cast<double*>(v.dvec), const_cast<double*>(v.skew),
-        const_cast<double*>(v.tP), const_cast<double*>(v.tN), const_cast<double*>(v.nn2));
+        const_cast<double*>(v.tP), const_cast<double*>(v.tN), const_cast<double*>(v.nn2),
+        const_cast<double*>(v.inv_nd), const_cast<double*>(v.inv_dpn), const_cast<double*>(v.ns));
   }
   FV_CUDA_TRY(cudaGetLastError());
   return FV_OK;
@@ -446,7 +460,8 @@ extern "C" int fv_mesh_create(int dim, int n_cells, int n_faces, int n_nodes, co
   FV_CUDA_TRY(cudaMalloc(&m->approx, sizeof(double) * nc * dim));
   // geometry block: area, dpn, dnn, g, nd, nn2 (6 nf) + normal, xf, dvec, skew, tP, tN (6 dim nf)
   // + vol (nc) + xc (dim nc)
-  size_t geo_n = 6 * nf + 6 * (size_t)dim * nf + nc + (size_t)dim * nc;
+  size_t geo_n = 8 * nf + 6 * (size_t)dim * nf + (size_t)dim * dim * nf + 2 * nc +
+                 (size_t)dim * nc;
   FV_CUDA_TRY(cudaMalloc(&m->geo, sizeof(double) * geo_n));
   FV_CUDA_TRY(cudaMemcpyAsync(m->owner, m->h_owner.data(), sizeof(int) * nf, cudaMemcpyHostToDevice, s));
   FV_CUDA_TRY(cudaMemcpyAsync(m->nb, m->h_nb.data(), sizeof(int) * nf, cudaMemcpyHostToDevice, s));
@@ -476,6 +491,9 @@ extern "C" int fv_mesh_create(int dim, int n_cells, int n_faces, int n_nodes, co
   v.g = p; p += nf;
   v.nd = p; p += nf;
   v.nn2 = p; p += nf;
+  v.inv_nd = p; p += nf;
+  v.inv_dpn = p; p += nf;
+  v.ns = p; p += dim * dim * nf;
   v.normal = p; p += dim * nf;
   v.xf = p; p += dim * nf;
   v.dvec = p; p += dim * nf;
@@ -483,6 +501,7 @@ extern "C" int fv_mesh_create(int dim, int n_cells, int n_faces, int n_nodes, co
   v.tP = p; p += dim * nf;
   v.tN = p; p += dim * nf;
   v.vol = p; p += nc;
+  v.inv_vol = p; p += nc;
   v.xc = p; p += dim * nc;
   int rc = fv_mesh_compute_geometry(m, s);
   if (rc != FV_OK) {

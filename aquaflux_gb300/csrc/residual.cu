@@ -55,6 +55,7 @@ template <class T>
 struct Par {
   T mu;      // molecular dynamic viscosity
   T iscale;  // inlet-velocity factor
+  T nu;      // molecular kinematic viscosity mu / rho
 };
 
 template <class T>
@@ -151,6 +152,35 @@ struct Layout {
   static constexpr int P = DIM, K = DIM + 1, W = DIM + 2;
 };
 
+// ---------------------------------------------------------------- workspace
+// Forward workspace of one residual evaluation (elements of type T), carved from FvCase::work.
+template <class T>
+struct Work {
+  T* G;      // (NF, DIM, nc) gradients
+  T* cl;     // (6, nc) strain, F1, nu_t, wall shear rate, k diffusivity, omega diffusivity
+  T* Gwi;    // (DIM, nc) omega gradient with the wall-cell value imposed
+  T* acown;  // (nf) momentum-diagonal coefficient, owner side
+  T* acnb;   // (nf) neighbour side
+  T* dco;    // (nc) d = V / a_P
+  T* me;     // (nf) lagged mass-flux estimate (rho u)_f . n A
+  T* FL;     // (NF, nf) face fluxes
+};
+template <class T, int DIM, bool TURB>
+Work<T> work_layout(void* base, long nc, long nf) {
+  constexpr int NF = Layout<DIM, TURB>::NFLD;
+  T* p = (T*)base;
+  Work<T> w;
+  w.G = p; p += (long)NF * DIM * nc;
+  w.cl = p; p += 6 * nc;
+  w.Gwi = p; p += DIM * nc;
+  w.acown = p; p += nf;
+  w.acnb = p; p += nf;
+  w.dco = p; p += nc;
+  w.me = p; p += nf;
+  w.FL = p;
+  return w;
+}
+
 // ---------------------------------------------------------------- k_grad
 template <class T, int DIM, bool TURB>
 __global__ void __launch_bounds__(128) k_grad(MeshView m, CaseView cv, Src<T> st, Par<T> par, T* G) {
@@ -172,7 +202,7 @@ __global__ void __launch_bounds__(128) k_grad(MeshView m, CaseView cv, Src<T> st
     const unsigned ent = m.cf_face[i];
     const int f = (int)(ent & ~FV_NB_BIT);
     const bool isnb = (ent & FV_NB_BIT) != 0;
-    const double A = m.area[f];
+    const double A = isnb ? -m.area[f] : m.area[f];  // the neighbour takes -S_f phi_f
     double S[DIM];
 #pragma unroll
     for (int j = 0; j < DIM; ++j) S[j] = m.normal[(long)j * nf + f] * A;
@@ -182,14 +212,8 @@ __global__ void __launch_bounds__(128) k_grad(MeshView m, CaseView cv, Src<T> st
       const int other = isnb ? m.owner[f] : m.nb[f];
 #pragma unroll
       for (int q = 0; q < NF; ++q) {
-        T po = st((long)q * nc + other);
-        T pn = phic[q];
-        if (!isnb) {
-          T t = po;
-          po = pn;
-          pn = t;
-        }
-        phif[q] = (1.0 - g) * po + g * pn;
+        const T po = st((long)q * nc + other);
+        phif[q] = isnb ? lerp(po, phic[q], g) : lerp(phic[q], po, g);
       }
     } else {
       const signed char kind = cv.fkind[f];
@@ -203,13 +227,11 @@ __global__ void __launch_bounds__(128) k_grad(MeshView m, CaseView cv, Src<T> st
       }
     }
 #pragma unroll
-    for (int q = 0; q < NF; ++q) {
-      T s = isnb ? -phif[q] : phif[q];
+    for (int q = 0; q < NF; ++q)
 #pragma unroll
-      for (int j = 0; j < DIM; ++j) acc[q][j] += S[j] * s;
-    }
+      for (int j = 0; j < DIM; ++j) acc[q][j] += S[j] * phif[q];
   }
-  const double inv = 1.0 / m.vol[c];
+  const double inv = m.inv_vol[c];
 #pragma unroll
   for (int q = 0; q < NF; ++q)
 #pragma unroll
@@ -217,11 +239,9 @@ __global__ void __launch_bounds__(128) k_grad(MeshView m, CaseView cv, Src<T> st
 }
 
 // ---------------------------------------------------------------- k_closure (SST)
-// cl layout: [strain, F1, nu_t, wall shear rate] x nc;  Gwi: (DIM, nc) omega gradient with the
-// wall-cell value imposed.
 template <class T, int DIM>
-__global__ void __launch_bounds__(128) k_closure(MeshView m, CaseView cv, Src<T> st, Par<T> par, const T* G, T* cl,
-                                                 T* Gwi) {
+__global__ void __launch_bounds__(128) k_closure(MeshView m, CaseView cv, Src<T> st, Par<T> par,
+                                                 const T* G, T* cl, T* Gwi) {
   using L = Layout<DIM, true>;
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= m.nc) return;
@@ -242,8 +262,8 @@ __global__ void __launch_bounds__(128) k_closure(MeshView m, CaseView cv, Src<T>
   T S = safe_sqrt(2.0 * sum);
   const T k = st((long)L::K * nc + c);
   const T w = st((long)L::W * nc + c);
-  const T nu = par.mu / cv.rho;
-  const double d = cv.wd[c];
+  const T nu = par.nu;
+  const double d = cv.wd[c], id = cv.inv_wd[c], id2 = cv.inv_wd2[c];
   T gk[DIM], gw[DIM];
 #pragma unroll
   for (int j = 0; j < DIM; ++j) {
@@ -274,30 +294,33 @@ __global__ void __launch_bounds__(128) k_closure(MeshView m, CaseView cv, Src<T>
         T sl = u[j] - bvel(cv, nf, f, j, kind, u[j], par);
         s2 += sl * sl;
       }
-      T rate = safe_sqrt(s2) / d;
-      num += rate * m.area[f];
+      num += safe_sqrt(s2) * m.area[f];
       den += m.area[f];
     }
-    shear = num / den;
+    shear = num * (id / den);
   }
   // F1 (sst.py:166-202) and the eddy viscosity with F2 (sst.py:152-164, 204-239)
-  T kp = pos(k);
+  const T kp = pos(k);
+  const T iw = 1.0 / w;
   T dot_kw = gk[0] * gw[0];
 #pragma unroll
   for (int j = 1; j < DIM; ++j) dot_kw += gk[j] * gw[j];
-  T cd = fv_max(2.0 * SIGMA_W2 * dot_kw / w, cst(CROSS_FLOOR, w));
-  T sk = safe_sqrt(kp);
-  T visc_term = 500.0 * nu / ((d * d) * w);
-  T arg1 = fv_min(fv_max(sk / (BETA_STAR * w * d), visc_term), 4.0 * SIGMA_W2 * kp / (cd * (d * d)));
-  T a1sq = arg1 * arg1;
-  T F1 = fv_tanh(a1sq * a1sq);
-  T arg2 = fv_max(2.0 * sk / (BETA_STAR * w * d), visc_term);
-  T F2 = fv_tanh(arg2 * arg2);
-  T nut = A1 * kp / fv_max(A1 * w, S * F2);
+  const T cd = fv_max((2.0 * SIGMA_W2) * dot_kw * iw, cst(CROSS_FLOOR, w));
+  const T sk = safe_sqrt(kp);
+  const T vt = (500.0 * id2) * nu * iw;
+  const T c1 = sk * iw * (id / BETA_STAR);
+  const T arg1 = fv_min(fv_max(c1, vt), (4.0 * SIGMA_W2 * id2) * kp / cd);
+  const T a1sq = arg1 * arg1;
+  const T F1 = fv_tanh(a1sq * a1sq);
+  const T arg2 = fv_max(2.0 * c1, vt);
+  const T F2 = fv_tanh(arg2 * arg2);
+  const T nut = A1 * kp / fv_max(A1 * w, S * F2);
   cl[c] = S;
   cl[(long)nc + c] = F1;
   cl[2L * nc + c] = nut;
   cl[3L * nc + c] = shear;
+  cl[4L * nc + c] = nu + (SIGMA_K2 + F1 * (SIGMA_K1 - SIGMA_K2)) * nut;
+  cl[5L * nc + c] = nu + (SIGMA_W2 + F1 * (SIGMA_W1 - SIGMA_W2)) * nut;
 #pragma unroll
   for (int j = 0; j < DIM; ++j) Gwi[(long)j * nc + c] = gw[j];
 }
@@ -310,33 +333,35 @@ __device__ __forceinline__ T mu_eff(const Par<T>& par, double rho, const T* cl, 
 }
 
 // lagged advective momentum flux (rho u)_f . n with the skew-corrected face value
-// (aquaflux/flow/rhie_chow.py:220-271)
+// (aquaflux/flow/rhie_chow.py:220-271): rho (sum_j n_j u_j,f + sum_jq n_j skew_q (grad u)_jq,f)
 template <class T, int DIM, bool TURB>
 __device__ __forceinline__ T mom_normal(const MeshView& m, const Src<T>& st, const T* G, double rho,
                                         int f, int o, int n, double g) {
   const int nc = m.nc, nf = m.nf;
-  T mn;
+  T mn = cst(0.0, st(o));
 #pragma unroll
   for (int j = 0; j < DIM; ++j) {
-    T uf = (1.0 - g) * (rho * st((long)j * nc + o)) + g * (rho * st((long)j * nc + n));
-    T cor;
+    mn += m.normal[(long)j * nf + f] * lerp(st((long)j * nc + o), st((long)j * nc + n), g);
 #pragma unroll
-    for (int q = 0; q < DIM; ++q) {
-      T gf = (1.0 - g) * (rho * G[((long)j * DIM + q) * nc + o]) +
-             g * (rho * G[((long)j * DIM + q) * nc + n]);
-      T t = gf * m.skew[(long)q * nf + f];
-      cor = q == 0 ? t : cor + t;
-    }
-    T term = (uf + cor) * m.normal[(long)j * nf + f];
-    mn = j == 0 ? term : mn + term;
+    for (int q = 0; q < DIM; ++q)
+      mn += m.ns[(long)(j * DIM + q) * nf + f] *
+            lerp(G[((long)j * DIM + q) * nc + o], G[((long)j * DIM + q) * nc + n], g);
   }
-  return mn;
+  return rho * mn;
+}
+
+// flux-continuous conductance g_o A / (dpn - g_o / g_n dnn), one division
+// (aquaflux/discretization/diffusion.py:85-134)
+template <class T>
+__device__ __forceinline__ T conductance(T go, T gn, double A, double dpn, double dnn) {
+  return go * gn * A / (dpn * gn - go * dnn);
 }
 
 // ---------------------------------------------------------------- k_apcoef
 template <class T, int DIM, bool TURB>
-__global__ void __launch_bounds__(128) k_apcoef(MeshView m, CaseView cv, Src<T> st, Par<T> par, const T* G, const T* cl,
-                                                T* ac_own, T* ac_nb) {
+__global__ void __launch_bounds__(128) k_apcoef(MeshView m, CaseView cv, Src<T> st, Par<T> par,
+                                                const T* G, const T* cl, T* ac_own, T* ac_nb,
+                                                T* me) {
   using L = Layout<DIM, TURB>;
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= m.nf) return;
@@ -346,11 +371,12 @@ __global__ void __launch_bounds__(128) k_apcoef(MeshView m, CaseView cv, Src<T> 
   const int n = interior ? m.nb[f] : o;
   const double g = m.g[f], A = m.area[f];
   const double rho = cv.rho;
-  T mdot = mom_normal<T, DIM, TURB>(m, st, G, rho, f, o, n, g) * A;
-  T mo = mu_eff<T, TURB>(par, rho, cl, nc, o);
+  const T mdot = mom_normal<T, DIM, TURB>(m, st, G, rho, f, o, n, g) * A;
+  me[f] = mdot;
+  const T mo = mu_eff<T, TURB>(par, rho, cl, nc, o);
   if (interior) {
-    T mnb = mu_eff<T, TURB>(par, rho, cl, nc, n);
-    T visc = mo * A / (m.dpn[f] - mo / mnb * m.dnn[f]);
+    const T mnb = mu_eff<T, TURB>(par, rho, cl, nc, n);
+    const T visc = conductance(mo, mnb, A, m.dpn[f], m.dnn[f]);
     ac_own[f] = visc + pos(mdot);
     ac_nb[f] = visc + pos(-mdot);
   } else {
@@ -358,16 +384,12 @@ __global__ void __launch_bounds__(128) k_apcoef(MeshView m, CaseView cv, Src<T> 
     T bv = mo;
     if (TURB && (kind == 0 || kind == 1)) {
       T nutw = cst(0.0, mo);
-      if (cv.swall[f]) {
-        T nu = par.mu / rho;
-        nutw = nut_wall(nu, cv.wd[o], st((long)L::K * nc + o));
-      }
+      if (cv.swall[f]) nutw = nut_wall(par.nu, cv.wd[o], st((long)L::K * nc + o));
       bv = par.mu + rho * nutw;
     }
-    T vo = bv * A / m.nd[f];
-    T conv = pos(mdot);
-    T coef = kind == 0 || kind == 1 ? vo : (kind == 2 ? vo + conv : (kind == 3 ? conv : cst(0.0, vo)));
-    ac_own[f] = coef;
+    const T vo = bv * (A * m.inv_nd[f]);
+    const T conv = pos(mdot);
+    ac_own[f] = kind == 0 || kind == 1 ? vo : (kind == 2 ? vo + conv : (kind == 3 ? conv : cst(0.0, vo)));
     ac_nb[f] = cst(0.0, vo);
   }
 }
@@ -390,14 +412,15 @@ __global__ void k_dcoeff(MeshView m, const T* ac_own, const T* ac_nb, T* dco) {
 
 // ---------------------------------------------------------------- k_flux
 template <class T, int DIM, bool TURB>
-__global__ void __launch_bounds__(128) k_flux(MeshView m, CaseView cv, Src<T> st, Par<T> par, const T* G, const T* cl,
-                                              const T* dco, T* FL) {
+__global__ void __launch_bounds__(128) k_flux(MeshView m, CaseView cv, Src<T> st, Par<T> par,
+                                              const T* G, const T* cl, const T* dco, const T* me,
+                                              bool recompute_me, T* FL) {
   using L = Layout<DIM, TURB>;
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= m.nf) return;
   const int nc = m.nc, nf = m.nf;
   const int o = m.owner[f];
-  const double A = m.area[f], rho = cv.rho;
+  const double A = m.area[f], rho = cv.rho, irho = 1.0 / cv.rho;
   double nrm[DIM], tP[DIM];
 #pragma unroll
   for (int j = 0; j < DIM; ++j) {
@@ -405,7 +428,7 @@ __global__ void __launch_bounds__(128) k_flux(MeshView m, CaseView cv, Src<T> st
     tP[j] = m.tP[(long)j * nf + f];
   }
   const T po = st((long)L::P * nc + o);
-  T mo = mu_eff<T, TURB>(par, rho, cl, nc, o);
+  const T mo = mu_eff<T, TURB>(par, rho, cl, nc, o);
   if (f < m.nfi) {
     const int n = m.nb[f];
     const double g = m.g[f];
@@ -413,68 +436,44 @@ __global__ void __launch_bounds__(128) k_flux(MeshView m, CaseView cv, Src<T> st
 #pragma unroll
     for (int j = 0; j < DIM; ++j) tN[j] = m.tN[(long)j * nf + f];
     const T pn = st((long)L::P * nc + n);
-    T mn = mom_normal<T, DIM, TURB>(m, st, G, rho, f, o, n, g);
-    const double rho_f = (1.0 - g) * rho + g * rho;
-    T gpf[DIM];
+    const T mest = recompute_me ? mom_normal<T, DIM, TURB>(m, st, G, rho, f, o, n, g) * A : me[f];
+    T gd = cst(0.0, po), gs = cst(0.0, po);
 #pragma unroll
-    for (int j = 0; j < DIM; ++j)
-      gpf[j] = (1.0 - g) * G[((long)L::P * DIM + j) * nc + o] + g * G[((long)L::P * DIM + j) * nc + n];
-    T dcf = (1.0 - g) * dco[o] + g * dco[n];
-    T dhat = (nrm[0] * nrm[0]) * dcf;
-#pragma unroll
-    for (int j = 1; j < DIM; ++j) dhat += (nrm[j] * nrm[j]) * dcf;
-    T gd = gpf[0] * m.dvec[f];
-    T gs = gpf[0] * m.skew[f];
-#pragma unroll
-    for (int j = 1; j < DIM; ++j) {
-      gd += gpf[j] * m.dvec[(long)j * nf + f];
-      gs += gpf[j] * m.skew[(long)j * nf + f];
+    for (int j = 0; j < DIM; ++j) {
+      const T gpf = lerp(G[((long)L::P * DIM + j) * nc + o], G[((long)L::P * DIM + j) * nc + n], g);
+      gd += gpf * m.dvec[(long)j * nf + f];
+      gs += gpf * m.skew[(long)j * nf + f];
     }
-    T damping = ((pn - po) - gd) / m.nd[f];
-    T mdot = (mn - rho_f * dhat * damping) * A;
-    T pf = (1.0 - g) * po + g * pn + gs;
-    T mnb = mu_eff<T, TURB>(par, rho, cl, nc, n);
-    T denom = m.dpn[f] - mo / mnb * m.dnn[f];
+    const T dhat = m.nn2[f] * lerp(dco[o], dco[n], g);
+    const T damping = ((pn - po) - gd) * m.inv_nd[f];
+    const T mdot = mest - (rho * A) * dhat * damping;
+    const T pf = lerp(po, pn, g) + gs;
+    const T cmo = conductance(mo, mu_eff<T, TURB>(par, rho, cl, nc, n), A, m.dpn[f], m.dnn[f]);
     const bool out = val(mdot) >= 0.0;
+    const T pA = pf * A;
 #pragma unroll
     for (int i = 0; i < DIM; ++i) {
       const T uo = st((long)i * nc + o), un = st((long)i * nc + n);
-      T cp = G[((long)i * DIM) * nc + o] * tP[0];
-      T cn = G[((long)i * DIM) * nc + n] * tN[0];
+      T cpn = (un - uo);
 #pragma unroll
-      for (int j = 1; j < DIM; ++j) {
-        cp += G[((long)i * DIM + j) * nc + o] * tP[j];
-        cn += G[((long)i * DIM + j) * nc + n] * tN[j];
-      }
-      T diff = -mo * (((un - uo) + cn - cp) / denom) * A;
-      T press = pf * nrm[i] * A;
-      T adv = mdot * (out ? uo : un);
-      FL[(long)i * nf + f] = (diff + press) + adv;
+      for (int j = 0; j < DIM; ++j)
+        cpn += G[((long)i * DIM + j) * nc + n] * tN[j] - G[((long)i * DIM + j) * nc + o] * tP[j];
+      FL[(long)i * nf + f] = (pA * nrm[i] - cmo * cpn) + mdot * (out ? uo : un);
     }
     FL[(long)L::P * nf + f] = mdot;
     if (TURB) {
-      T vflux = mdot / rho;
+      const T vflux = mdot * irho;
       const bool vout = val(vflux) >= 0.0;
-      T nu = par.mu / rho;
-      T F1o = cl[(long)nc + o], F1n = cl[(long)nc + n];
-      T nto = cl[2L * nc + o], ntn = cl[2L * nc + n];
 #pragma unroll
       for (int s = 0; s < 2; ++s) {
         const int q = s == 0 ? L::K : L::W;
-        const double in = s == 0 ? SIGMA_K1 : SIGMA_W1, ou = s == 0 ? SIGMA_K2 : SIGMA_W2;
-        T go = nu + (F1o * in + (1.0 - F1o) * ou) * nto;
-        T gn = nu + (F1n * in + (1.0 - F1n) * ou) * ntn;
+        const T go = cl[(4L + s) * nc + o], gn = cl[(4L + s) * nc + n];
         const T phio = st((long)q * nc + o), phin = st((long)q * nc + n);
-        T cp = G[((long)q * DIM) * nc + o] * tP[0];
-        T cn = G[((long)q * DIM) * nc + n] * tN[0];
+        T cpn = (phin - phio);
 #pragma unroll
-        for (int j = 1; j < DIM; ++j) {
-          cp += G[((long)q * DIM + j) * nc + o] * tP[j];
-          cn += G[((long)q * DIM + j) * nc + n] * tN[j];
-        }
-        T adv = vflux * (vout ? phio : phin);
-        T diff = -go * (((phin - phio) + cn - cp) / (m.dpn[f] - go / gn * m.dnn[f])) * A;
-        FL[(long)q * nf + f] = adv + diff;
+        for (int j = 0; j < DIM; ++j)
+          cpn += G[((long)q * DIM + j) * nc + n] * tN[j] - G[((long)q * DIM + j) * nc + o] * tP[j];
+        FL[(long)q * nf + f] = vflux * (vout ? phio : phin) - conductance(go, gn, A, m.dpn[f], m.dnn[f]) * cpn;
       }
     }
   } else {
@@ -490,7 +489,7 @@ __global__ void __launch_bounds__(128) k_flux(MeshView m, CaseView cv, Src<T> st
       T un = bu[0] * nrm[0];
 #pragma unroll
       for (int j = 1; j < DIM; ++j) un += bu[j] * nrm[j];
-      mdot = rho * un * A;
+      mdot = (rho * A) * un;
     } else if (kind == 3) {
       T un = uo[0] * nrm[0];
       T interp = G[((long)L::P * DIM) * nc + o] * nrm[0];
@@ -499,56 +498,46 @@ __global__ void __launch_bounds__(128) k_flux(MeshView m, CaseView cv, Src<T> st
         un += uo[j] * nrm[j];
         interp += G[((long)L::P * DIM + j) * nc + o] * nrm[j];
       }
-      T dh = (nrm[0] * nrm[0]) * dco[o];
-#pragma unroll
-      for (int j = 1; j < DIM; ++j) dh += (nrm[j] * nrm[j]) * dco[o];
-      T compact = (cv.fp[f] - po) / m.nd[f];
-      mdot = rho * (un - dh * (compact - interp)) * A;
+      const T dh = m.nn2[f] * dco[o];
+      const T compact = (cv.fp[f] - po) * m.inv_nd[f];
+      mdot = (rho * A) * (un - dh * (compact - interp));
     } else {
       mdot = cst(0.0, po);
     }
-    T pf = bpress(cv, f, kind, po);
+    const T pf = bpress(cv, f, kind, po);
     T gb = mo;
-    if (TURB) {
-      if (kind == 0 || kind == 1) {
-        T nutw = cst(0.0, mo);
-        if (cv.swall[f]) nutw = nut_wall(par.mu / rho, cv.wd[o], st((long)L::K * nc + o));
-        gb = par.mu + rho * nutw;
-      }
+    if (TURB && (kind == 0 || kind == 1)) {
+      T nutw = cst(0.0, mo);
+      if (cv.swall[f]) nutw = nut_wall(par.nu, cv.wd[o], st((long)L::K * nc + o));
+      gb = par.mu + rho * nutw;
     }
+    const T gA = gb * (A * m.inv_dpn[f]);
     const bool out = val(mdot) >= 0.0;
+    const T pA = pf * A;
 #pragma unroll
     for (int i = 0; i < DIM; ++i) {
       T cp = G[((long)i * DIM) * nc + o] * tP[0];
 #pragma unroll
       for (int j = 1; j < DIM; ++j) cp += G[((long)i * DIM + j) * nc + o] * tP[j];
-      T diff = -gb * ((bu[i] - uo[i] - cp) / m.dpn[f]) * A;
-      T press = pf * nrm[i] * A;
-      T adv = mdot * (out ? uo[i] : bu[i]);
-      FL[(long)i * nf + f] = (diff + press) + adv;
+      FL[(long)i * nf + f] = (pA * nrm[i] - gA * (bu[i] - uo[i] - cp)) + mdot * (out ? uo[i] : bu[i]);
     }
     FL[(long)L::P * nf + f] = mdot;
     if (TURB) {
-      T vflux = mdot / rho;
+      const T vflux = mdot * irho;
       const bool vout = val(vflux) >= 0.0;
-      T nu = par.mu / rho;
-      T F1o = cl[(long)nc + o], nto = cl[2L * nc + o];
 #pragma unroll
       for (int s = 0; s < 2; ++s) {
         const int q = s == 0 ? L::K : L::W;
-        const double in = s == 0 ? SIGMA_K1 : SIGMA_W1, ou = s == 0 ? SIGMA_K2 : SIGMA_W2;
-        T go = nu + (F1o * in + (1.0 - F1o) * ou) * nto;
+        const T go = cl[(4L + s) * nc + o];
         const T phio = st((long)q * nc + o);
         T cp = G[((long)q * DIM) * nc + o] * tP[0];
 #pragma unroll
         for (int j = 1; j < DIM; ++j) cp += G[((long)q * DIM + j) * nc + o] * tP[j];
-        T bphi = s == 0 ? bscalar(cv.kkind[f], cv.kval[f], phio, cp)
-                        : bscalar(cv.wkind[f], cv.wval[f], phio, cp);
+        const T bphi = s == 0 ? bscalar(cv.kkind[f], cv.kval[f], phio, cp)
+                              : bscalar(cv.wkind[f], cv.wval[f], phio, cp);
         T gface = go;
-        if (s == 0 && cv.swall[f]) gface = (1.0 - wall_weight(nu, cv.wd[o], phio)) * go;
-        T adv = vflux * (vout ? phio : bphi);
-        T diff = -gface * ((bphi - phio - cp) / m.dpn[f]) * A;
-        FL[(long)q * nf + f] = adv + diff;
+        if (s == 0 && cv.swall[f]) gface = (1.0 - wall_weight(par.nu, cv.wd[o], phio)) * go;
+        FL[(long)q * nf + f] = vflux * (vout ? phio : bphi) - gface * (A * m.inv_dpn[f]) * (bphi - phio - cp);
       }
     }
   }
@@ -581,33 +570,33 @@ __global__ void __launch_bounds__(128) k_sum(MeshView m, CaseView cv, Src<T> st,
     const double V = m.vol[c];
     const T k = st((long)L::K * nc + c), w = st((long)L::W * nc + c);
     const T S = cl[c], F1 = cl[(long)nc + c], nut = cl[2L * nc + c];
-    const T nu = par.mu / cv.rho;
+    const T nu = par.nu;
     const double d = cv.wd[c];
     const bool wall = cv.wcell[c] != 0;
-    T prod = nut * (S * S);
-    T limit = PROD_RATIO * BETA_STAR * pos(k) * w;
-    T lim = fv_min(prod, limit);
+    const T kp = pos(k);
+    const T limit = (PROD_RATIO * BETA_STAR) * kp * w;
+    T lim = fv_min(nut * (S * S), limit);
     T weff = w;
     if (wall) {
-      T lw = wall_weight(nu, d, k);
-      T tau = (nu + nut_wall(nu, d, k)) * cl[3L * nc + c];
-      T pw = tau * log_shear(d, k);
+      const T lw = wall_weight(nu, d, k);
+      const T pw = (nu + nut_wall(nu, d, k)) * cl[3L * nc + c] * log_shear(d, k);
       lim = (1.0 - lw) * lim + lw * pw;
       weff = omega_wall(nu, d, k);
     }
     r[L::K] = r[L::K] - lim * V;
-    r[L::K] = r[L::K] - (-BETA_STAR * k * weff * V);
-    T alpha = F1 * ALPHA_1 + (1.0 - F1) * ALPHA_2;
-    T cap = PROD_RATIO * BETA_STAR * pos(k) * w / fv_max(nut, cst(NUT_FLOOR, nut));
-    r[L::W] = r[L::W] - alpha * fv_min(S * S, cap) * V;
-    T beta = F1 * BETA_1 + (1.0 - F1) * BETA_2;
-    r[L::W] = r[L::W] - (-beta * (w * w) * V);
-    T dkw = G[((long)L::K * DIM) * nc + c] * Gwi[c];
+    r[L::K] = r[L::K] + BETA_STAR * V * k * weff;
+    if (wall) {
+      r[L::W] = w - omega_wall(nu, d, k);
+    } else {
+      const T alpha = ALPHA_2 + F1 * (ALPHA_1 - ALPHA_2);
+      const T cap = limit / fv_max(nut, cst(NUT_FLOOR, nut));
+      const T beta = BETA_2 + F1 * (BETA_1 - BETA_2);
+      T dkw = G[((long)L::K * DIM) * nc + c] * Gwi[c];
 #pragma unroll
-    for (int j = 1; j < DIM; ++j) dkw += G[((long)L::K * DIM + j) * nc + c] * Gwi[(long)j * nc + c];
-    T cross = 2.0 * (1.0 - F1) * SIGMA_W2 * dkw / w;
-    r[L::W] = r[L::W] - cross * V;
-    if (wall) r[L::W] = w - omega_wall(nu, d, k);
+      for (int j = 1; j < DIM; ++j) dkw += G[((long)L::K * DIM + j) * nc + c] * Gwi[(long)j * nc + c];
+      const T cross = (2.0 * SIGMA_W2) * (1.0 - F1) * dkw / w;
+      r[L::W] = r[L::W] + V * (beta * (w * w) - alpha * fv_min(S * S, cap) - cross);
+    }
   }
 #pragma unroll
   for (int q = 0; q < NF; ++q) put<T>(R, JV, (long)q * nc + c, r[q]);
@@ -627,34 +616,28 @@ void freeze<Dual>(Dual* x, long n, cudaStream_t s) {
 
 template <class T, int DIM, bool TURB>
 int run(FvCase* cs, Src<T> st, Par<T> par, double* R, double* JV, cudaStream_t s,
-        bool frozen = false) {
-  using L = Layout<DIM, TURB>;
+        bool frozen = false, bool end_profile_run = true) {
   const MeshView& m = cs->mesh->view;
   const CaseView& cv = cs->view;
   const long nc = m.nc, nf = m.nf;
-  T* G = (T*)cs->work;
-  T* cl = G + (long)L::NFLD * DIM * nc;
-  T* Gwi = cl + 4 * nc;
-  T* acown = Gwi + DIM * nc;
-  T* acnb = acown + nf;
-  T* dco = acnb + nf;
-  T* FL = dco + nc;
+  Work<T> w = work_layout<T, DIM, TURB>(cs->work, nc, nf);
   constexpr int TB = 128;
   const int bc = fv_blocks(nc, TB), bf = fv_blocks(nf, TB);
   fv_prof_mark(cs, 0, s);
-  k_grad<T, DIM, TURB><<<bc, TB, 0, s>>>(m, cv, st, par, G);
+  k_grad<T, DIM, TURB><<<bc, TB, 0, s>>>(m, cv, st, par, w.G);
   fv_prof_mark(cs, 1, s);
-  if (TURB) k_closure<T, DIM><<<bc, TB, 0, s>>>(m, cv, st, par, G, cl, Gwi);
+  if (TURB) k_closure<T, DIM><<<bc, TB, 0, s>>>(m, cv, st, par, w.G, w.cl, w.Gwi);
   fv_prof_mark(cs, 2, s);
-  k_apcoef<T, DIM, TURB><<<bf, TB, 0, s>>>(m, cv, st, par, G, cl, acown, acnb);
+  k_apcoef<T, DIM, TURB><<<bf, TB, 0, s>>>(m, cv, st, par, w.G, w.cl, w.acown, w.acnb, w.me);
   fv_prof_mark(cs, 3, s);
-  k_dcoeff<T><<<bc, TB, 0, s>>>(m, acown, acnb, dco);
-  if (frozen) freeze<T>(G, (long)(dco + nc - G), s);  // G, closure, Gwi, a_P coefficients, d
+  k_dcoeff<T><<<bc, TB, 0, s>>>(m, w.acown, w.acnb, w.dco);
+  if (frozen) freeze<T>(w.G, (long)(w.dco + nc - w.G), s);  // G, closure, Gwi, a_P, d
   fv_prof_mark(cs, 4, s);
-  k_flux<T, DIM, TURB><<<bf, TB, 0, s>>>(m, cv, st, par, G, cl, dco, FL);
+  k_flux<T, DIM, TURB><<<bf, TB, 0, s>>>(m, cv, st, par, w.G, w.cl, w.dco, w.me, frozen, w.FL);
   fv_prof_mark(cs, 5, s);
-  k_sum<T, DIM, TURB><<<bc, TB, 0, s>>>(m, cv, st, par, FL, cl, G, Gwi, R, JV);
+  k_sum<T, DIM, TURB><<<bc, TB, 0, s>>>(m, cv, st, par, w.FL, w.cl, w.G, w.Gwi, R, JV);
   fv_prof_mark(cs, 6, s);
+  if (end_profile_run) fv_prof_end_run(cs);
   FV_CUDA_TRY(cudaGetLastError());
   return FV_OK;
 }
@@ -662,12 +645,14 @@ int run(FvCase* cs, Src<T> st, Par<T> par, double* R, double* JV, cudaStream_t s
 template <int DIM, bool TURB>
 int dispatch_t(FvCase* cs, const double* state, const double* tangent, int kind, double* R,
                double* JV, cudaStream_t s) {
+  const double irho = 1.0 / cs->desc.rho;
   if (kind == FV_TAN_NONE) {
-    return run<double, DIM, TURB>(cs, Src<double>{state}, Par<double>{cs->mu, cs->inlet_scale}, R,
-                                  nullptr, s);
+    return run<double, DIM, TURB>(
+        cs, Src<double>{state}, Par<double>{cs->mu, cs->inlet_scale, cs->mu * irho}, R, nullptr, s);
   }
-  Par<Dual> par{{cs->mu, kind == FV_TAN_MU ? 1.0 : 0.0},
-                {cs->inlet_scale, kind == FV_TAN_INLET ? 1.0 : 0.0}};
+  const double dmu = kind == FV_TAN_MU ? 1.0 : 0.0;
+  Par<Dual> par{{cs->mu, dmu}, {cs->inlet_scale, kind == FV_TAN_INLET ? 1.0 : 0.0},
+                {cs->mu * irho, dmu * irho}};
   Src<Dual> st{state, (kind == FV_TAN_STATE || kind == FV_TAN_FROZEN) ? tangent : nullptr};
   return run<Dual, DIM, TURB>(cs, st, par, R, JV, s, kind == FV_TAN_FROZEN);
 }
@@ -682,18 +667,15 @@ int run_vjp(FvCase* cs, const double* state, const double* W, double* R, double*
   const CaseView& cv = cs->view;
   const long nc = m.nc, nf = m.nf;
   Src<double> st{state};
-  Par<double> par{cs->mu, cs->inlet_scale};
-  int rc = run<double, DIM, TURB>(cs, st, par, R ? R : cs->tmp, nullptr, s);
+  Par<double> par{cs->mu, cs->inlet_scale, cs->mu / cs->desc.rho};
+  int rc = run<double, DIM, TURB>(cs, st, par, R ? R : cs->tmp, nullptr, s, false, false);
   if (rc != FV_OK) return rc;
   // forward workspace (double layout, as written by run<double>)
-  double* G = (double*)cs->work;
-  double* cl = G + (long)L::NFLD * DIM * nc;
-  double* Gwi = cl + 4 * nc;
-  double* acown = Gwi + DIM * nc;
-  double* acnb = acown + nf;
-  double* dco = acnb + nf;
-  (void)acown;
-  (void)acnb;
+  Work<double> fw = work_layout<double, DIM, TURB>(cs->work, nc, nf);
+  double* G = fw.G;
+  double* cl = fw.cl;
+  double* Gwi = fw.Gwi;
+  double* dco = fw.dco;
   AdjWork aw;
   double* p = cs->adj;
   aw.Wt = p; p += L::NFLD * nc;
@@ -705,10 +687,16 @@ int run_vjp(FvCase* cs, const double* state, const double* W, double* R, double*
   constexpr int TB = 128;
   const int bc = fv_blocks(nc, TB);
   a_sum<DIM, TURB><<<bc, TB, 0, s>>>(m, cv, st, par, W, cl, G, Gwi, aw);
-  a_flux<DIM, TURB><<<bc, TB, 0, s>>>(m, cv, st, par, G, cl, dco, aw);
-  a_apcoef<DIM, TURB><<<bc, TB, 0, s>>>(m, cv, st, par, G, cl, dco, aw);
+  fv_prof_mark(cs, 7, s);
+  a_flux<DIM, TURB><<<bc, TB, 0, s>>>(m, cv, st, par, G, cl, dco, fw.me, aw);
+  fv_prof_mark(cs, 8, s);
+  a_apcoef<DIM, TURB><<<bc, TB, 0, s>>>(m, cv, st, par, G, cl, dco, fw.me, aw);
+  fv_prof_mark(cs, 9, s);
   if (TURB) a_closure<DIM><<<bc, TB, 0, s>>>(m, cv, st, par, G, cl, aw);
+  fv_prof_mark(cs, 10, s);
   a_grad<DIM, TURB><<<bc, TB, 0, s>>>(m, cv, aw, out);
+  fv_prof_mark(cs, 11, s);
+  fv_prof_end_run(cs);
   FV_CUDA_TRY(cudaGetLastError());
   return FV_OK;
 }
@@ -733,7 +721,7 @@ int fv_case_vjp_run(FvCase* cs, const double* state, const double* W, double* R,
 
 size_t fv_residual_work_bytes(int dim, int turb, long nc, long nf) {
   long nfld = dim + 1 + (turb ? 2 : 0);
-  long n = nfld * dim * nc + 4 * nc + dim * nc + 2 * nf + nc + nfld * nf;
+  long n = nfld * dim * nc + 6 * nc + dim * nc + 3 * nf + nc + nfld * nf;
   return (size_t)n * sizeof(Dual);
 }
 

@@ -199,7 +199,8 @@ class FlowCase:
         check(lib().fv_param_jvp(self._h, ptr(s), ptr(a), ptr(b), _stream()))
         return a, b
 
-    STAGES = ("grad", "closure", "apcoef", "dcoeff", "flux", "sum")
+    STAGES = ("grad", "closure", "apcoef", "dcoeff", "flux", "sum",
+              "a_sum", "a_flux", "a_apcoef", "a_closure", "a_grad")
 
     def profile_begin(self, max_runs: int) -> None:
         check(lib().fv_case_profile_begin(self._h, int(max_runs)))

@@ -47,6 +47,9 @@ def _args():
     ap.add_argument("--cpu-sample", type=int, default=24, help="cells per axis of the CPU sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--step", default="vjp", choices=["vjp", "jvp"])
+    ap.add_argument("--no-newton", action="store_true", help="skip the Newton-solve timing")
+    ap.add_argument("--newton-oracle-check", action="store_true",
+                    help="also evaluate the converged fp32-preconditioned state with the CPU oracle")
     return ap.parse_args()
 
 
@@ -304,10 +307,52 @@ def run_gpu(args, rank: int, world: int, local_rank: int) -> dict | None:
                      "peak_source": f"{peaks['source']} (MEASURED_PEAKS.json hbm_gbs)"},
         "clocks": clk.summary(),
     }
+    if not args.no_newton:
+        out["newton"] = newton_block(args, wl, case)
     if not args.no_cpu_baseline:
         cb = cpu_residual_jvp_rate(args.cpu_sample, step=args.step)
         out["cpu_baseline"] = {"value": round(cb["faces_per_s"] / 1e9, 6), "unit": UNIT,
                                "cores": cb["cores"], "kind": "port", "sample": cb["sample"]}
+    return out
+
+
+def newton_block(args, wl, case) -> dict:
+    """Newton-solve seconds, fp64-preconditioned (plain) vs fp32-preconditioned (mixed) form.
+
+    Both forms: fp64 residual, fp64 JVP operator, fp64 FGMRES(30) with Krylov orthogonalisation,
+    fp64 Newton update and line search; they differ only in the precision of the ILU(0)
+    preconditioner of the materialised reach-1 Jacobian.  Stops at ||R|| <= 1e-12 + 1e-10 ||R0||.
+    """
+    import numpy as np
+    import torch
+
+    from aquaflux_gb300 import solve
+
+    out = {}
+    states = {}
+    for prec in (64, 32):
+        torch.cuda.synchronize()
+        res = solve.newton_solve(case, wl.initial_state(), precision=prec, max_steps=40)
+        out[f"fp{prec}"] = {
+            "seconds": round(res.seconds, 3), "converged": bool(res.converged),
+            "newton_steps": res.steps, "krylov_iterations": int(sum(res.krylov_iterations)),
+            "final_rel_residual": res.residual_norms[-1] / res.residual_norms[0],
+            "phase_seconds": {k: round(v, 3) for k, v in res.phase_seconds.items()}}
+        states[prec] = res.state
+    a, b = states[64], states[32]
+    out["fp32_vs_fp64_field_max_rel_diff"] = float((a - b).abs().max() / a.abs().max())
+    out["speedup_fp32_vs_fp64"] = round(out["fp64"]["seconds"] / out["fp32"]["seconds"], 3)
+    if args.newton_oracle_check:
+        from oracle import fv_oracle as fo
+
+        torch.set_num_threads(os.cpu_count() or 1)
+        c = fo.make_case(wl.mesh, mu=wl.mu, rho=wl.rho, flow_bc=wl.flow_bc,
+                         sst={"nu": wl.mu / wl.rho, "walls": wl.sst["walls"], "k": wl.sst["k"],
+                              "omega": wl.sst["omega"]})
+        orc = fo.Oracle(c)
+        r0 = float(np.linalg.norm(orc.residual(torch.as_tensor(wl.initial_state())).numpy()))
+        r32 = float(np.linalg.norm(orc.residual(b.cpu()).numpy()))
+        out["fp32_oracle_rel_residual"] = r32 / r0
     return out
 
 

@@ -139,7 +139,8 @@ int fv_param_vjp(FvCase* c, const double* state, const double* w, double* out, v
 
 /* Per-stage CUDA-event timing of the next `max_runs` pipeline runs on this case (diagnostics;
  * no reference counterpart).  profile_end synchronizes, writes the summed milliseconds of each
- * stage (grad, closure, apcoef, dcoeff, flux, sum) and the number of runs recorded. */
+ * stage (grad, closure, apcoef, dcoeff, flux, sum, and for a VJP a_sum, a_flux, a_apcoef,
+ * a_closure, a_grad) and the number of runs recorded. */
 int fv_case_profile_begin(FvCase* c, int max_runs);
 int fv_case_profile_end(FvCase* c, float* stage_ms, int n_stages, int* n_runs);
 
