@@ -65,4 +65,4 @@ def build_oracle() -> None:
     reference's own ILU(0) kernel) -- test infrastructure, see ``oracle/build_ref.py``."""
     script = os.path.join(ROOT, "oracle", "build_oracle.py")
     if os.path.exists(script):
-        subprocess.run(["python3", script], check=True)
+        subprocess.run(["python3", script], check=True, stdout=subprocess.DEVNULL)

@@ -257,6 +257,177 @@ __global__ void k_ilu_lower_t(IluView<V> F, const int* tptr, const int* tidx, co
   }
 }
 
+// ---- lane-group kernels: an 8-lane group per block row, lane a owns scalar row / column a of
+// the block (b <= 8), so the b x b block work of a row runs on b lanes instead of one thread.
+// Element-wise operation orders are those of the one-thread kernels above, except the forward
+// solve's upper sweep, which subtracts the off-diagonal blocks before the in-block terms (the
+// reference subtracts in ascending column order); b = 1 uses the one-thread kernels.
+#define FV_LG 8
+__device__ __forceinline__ unsigned lg_mask() { return 0xffu << ((threadIdx.x & 31) & ~(FV_LG - 1)); }
+
+template <class V>
+__global__ void k_ilu_factor_lg(IluView<V> F, const int* rows, int count,
+                                unsigned long long* zero_flag) {
+  const int gid = (blockIdx.x * blockDim.x + threadIdx.x) / FV_LG;
+  const int a = threadIdx.x & (FV_LG - 1);
+  if (gid >= count) return;  // whole groups exit together
+  const unsigned mask = lg_mask();
+  const int i = rows[gid];
+  const int b = F.b;
+  const bool live = a < b;
+  const long bb = (long)b * b;
+  const int re = F.ptr[i + 1], di = F.diag[i];
+  for (int q = F.ptr[i]; q < di; ++q) {
+    const int j = F.idx[q];
+    V* Lij = F.val + (long)q * bb;
+    const V* Ujj = F.val + (long)F.diag[j] * bb;
+    if (live) {
+      for (int cb = 0; cb < b; ++cb) {
+        const V piv = Ujj[(long)cb * b + cb];
+        if (piv == V(0) && a == 0) note_zero_pivot(zero_flag, i * b, j * b + cb);
+        const V l = Lij[(long)a * b + cb] / piv;
+        Lij[(long)a * b + cb] = l;
+        for (int c2 = cb + 1; c2 < b; ++c2) Lij[(long)a * b + c2] -= l * Ujj[(long)cb * b + c2];
+      }
+      int p = q + 1;
+      for (int s2 = F.diag[j] + 1; s2 < F.ptr[j + 1]; ++s2) {
+        const int k = F.idx[s2];
+        while (p < re && F.idx[p] < k) ++p;
+        if (p >= re) break;
+        if (F.idx[p] != k) continue;
+        V* Aik = F.val + (long)p * bb + (long)a * b;
+        const V* Ajk = F.val + (long)s2 * bb;
+        for (int c = 0; c < b; ++c) {
+          V acc = Aik[c];
+          for (int mm = 0; mm < b; ++mm) acc -= Lij[(long)a * b + mm] * Ajk[(long)mm * b + c];
+          Aik[c] = acc;
+        }
+      }
+    }
+  }
+  __syncwarp(mask);
+  V* D = F.val + (long)di * bb;
+  for (int cb = 0; cb < b; ++cb) {
+    // row cb of the diagonal block (and of the upper blocks) is final here
+    if (live && a > cb) {
+      const V piv = D[(long)cb * b + cb];
+      if (piv == V(0)) note_zero_pivot(zero_flag, i * b + a, i * b + cb);
+      const V l = D[(long)a * b + cb] / piv;
+      D[(long)a * b + cb] = l;
+      for (int c = cb + 1; c < b; ++c) D[(long)a * b + c] -= l * D[(long)cb * b + c];
+      for (int q = di + 1; q < re; ++q) {
+        V* U = F.val + (long)q * bb;
+        for (int c = 0; c < b; ++c) U[(long)a * b + c] -= l * U[(long)cb * b + c];
+      }
+    }
+    __syncwarp(mask);
+  }
+}
+
+template <class V>
+__global__ void k_ilu_lower_lg(IluView<V> F, const int* rows, int count, V* y) {
+  const int gid = (blockIdx.x * blockDim.x + threadIdx.x) / FV_LG;
+  const int a = threadIdx.x & (FV_LG - 1);
+  if (gid >= count) return;
+  const unsigned mask = lg_mask();
+  const int i = rows[gid], b = F.b;
+  const bool live = a < b;
+  const long bb = (long)b * b;
+  V acc = live ? y[(long)i * b + a] : V(0);
+  if (live)
+    for (int q = F.ptr[i]; q < F.diag[i]; ++q) {
+      const V* L = F.val + (long)q * bb + (long)a * b;
+      const V* yj = y + (long)F.idx[q] * b;
+      for (int c = 0; c < b; ++c) acc -= L[c] * yj[c];
+    }
+  const V* D = F.val + (long)F.diag[i] * bb;
+  for (int c = 0; c < b; ++c) {
+    const V vc = __shfl_sync(mask, acc, c, FV_LG);
+    if (live && a > c) acc -= D[(long)a * b + c] * vc;
+  }
+  if (live) y[(long)i * b + a] = acc;
+}
+
+template <class V>
+__global__ void k_ilu_upper_lg(IluView<V> F, const int* rows, int count, V* x) {
+  const int gid = (blockIdx.x * blockDim.x + threadIdx.x) / FV_LG;
+  const int a = threadIdx.x & (FV_LG - 1);
+  if (gid >= count) return;
+  const unsigned mask = lg_mask();
+  const int i = rows[gid], b = F.b;
+  const bool live = a < b;
+  const long bb = (long)b * b;
+  V acc = live ? x[(long)i * b + a] : V(0);
+  if (live)
+    for (int q = F.diag[i] + 1; q < F.ptr[i + 1]; ++q) {
+      const V* U = F.val + (long)q * bb + (long)a * b;
+      const V* xk = x + (long)F.idx[q] * b;
+      for (int c = 0; c < b; ++c) acc -= U[c] * xk[c];
+    }
+  const V* D = F.val + (long)F.diag[i] * bb;
+  for (int c = b - 1; c >= 0; --c) {
+    if (a == c) acc = acc / D[(long)c * b + c];
+    const V vc = __shfl_sync(mask, acc, c, FV_LG);
+    if (live && a < c) acc -= D[(long)a * b + c] * vc;
+  }
+  if (live) x[(long)i * b + a] = acc;
+}
+
+template <class V>
+__global__ void k_ilu_upper_t_lg(IluView<V> F, const int* tptr, const int* tidx, const int* tblk,
+                                 const int* rows, int count, V* z) {
+  const int gid = (blockIdx.x * blockDim.x + threadIdx.x) / FV_LG;
+  const int a = threadIdx.x & (FV_LG - 1);
+  if (gid >= count) return;
+  const unsigned mask = lg_mask();
+  const int i = rows[gid], b = F.b;
+  const bool live = a < b;
+  const long bb = (long)b * b;
+  V acc = live ? z[(long)i * b + a] : V(0);
+  if (live)
+    for (int q = tptr[i]; q < tptr[i + 1]; ++q) {
+      const int j = tidx[q];
+      if (j >= i) continue;
+      const V* U = F.val + (long)tblk[q] * bb;  // block (j, i)
+      const V* zj = z + (long)j * b;
+      for (int c = 0; c < b; ++c) acc -= U[(long)c * b + a] * zj[c];
+    }
+  const V* D = F.val + (long)F.diag[i] * bb;
+  for (int c = 0; c < b; ++c) {
+    if (a == c) acc = acc / D[(long)c * b + c];
+    const V vc = __shfl_sync(mask, acc, c, FV_LG);
+    if (live && a > c) acc -= D[(long)c * b + a] * vc;
+  }
+  if (live) z[(long)i * b + a] = acc;
+}
+
+template <class V>
+__global__ void k_ilu_lower_t_lg(IluView<V> F, const int* tptr, const int* tidx, const int* tblk,
+                                 const int* rows, int count, V* x) {
+  const int gid = (blockIdx.x * blockDim.x + threadIdx.x) / FV_LG;
+  const int a = threadIdx.x & (FV_LG - 1);
+  if (gid >= count) return;
+  const unsigned mask = lg_mask();
+  const int i = rows[gid], b = F.b;
+  const bool live = a < b;
+  const long bb = (long)b * b;
+  V acc = live ? x[(long)i * b + a] : V(0);
+  if (live)
+    for (int q = tptr[i + 1] - 1; q >= tptr[i]; --q) {
+      const int k = tidx[q];
+      if (k <= i) continue;
+      const V* L = F.val + (long)tblk[q] * bb;  // block (k, i)
+      const V* xk = x + (long)k * b;
+      for (int c = b - 1; c >= 0; --c) acc -= L[(long)c * b + a] * xk[c];
+    }
+  const V* D = F.val + (long)F.diag[i] * bb;
+  for (int c = b - 1; c >= 0; --c) {
+    const V vc = __shfl_sync(mask, acc, c, FV_LG);
+    if (live && a < c) acc -= D[(long)c * b + a] * vc;
+  }
+  if (live) x[(long)i * b + a] = acc;
+}
+
 template <class V>
 __global__ void k_copy(long n, const V* a, V* b) {
   long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -312,6 +483,9 @@ struct FvIlu0 {
   int* rows_tfwd = nullptr;  // U^T order
   int* rows_tbwd = nullptr;  // L^T order
   std::vector<int> lv_fwd, lv_bwd, lv_tfwd, lv_tbwd;
+  void* work = nullptr;                      // (n * b) vector the captured sweeps run on
+  cudaGraphExec_t apply_exec[2] = {nullptr, nullptr};  // forward / transposed solve
+  cudaGraphExec_t factor_exec = nullptr;
 };
 
 namespace {
@@ -349,17 +523,89 @@ IluView<V> view(FvIlu0* f) {
   return IluView<V>{f->n, f->b, f->ptr, f->idx, f->diag, (V*)f->val};
 }
 
+// Launch the level sequence of the factorization / a solve on `s` (captured into a graph once).
+template <class V>
+void launch_factor_levels(FvIlu0* f, cudaStream_t s) {
+  IluView<V> F = view<V>(f);
+  for (size_t l = 0; l + 1 < f->lv_fwd.size(); ++l) {
+    const int cnt = f->lv_fwd[l + 1] - f->lv_fwd[l];
+    if (cnt == 0) continue;
+    if (f->b == 1)
+      k_ilu_factor_level<V><<<fv_blocks(cnt, 128), 128, 0, s>>>(F, f->rows_fwd + f->lv_fwd[l], cnt,
+                                                                f->zero_flag);
+    else
+      k_ilu_factor_lg<V><<<fv_blocks((long)cnt * FV_LG, 128), 128, 0, s>>>(
+          F, f->rows_fwd + f->lv_fwd[l], cnt, f->zero_flag);
+  }
+}
+
+template <class V>
+void launch_apply_levels(FvIlu0* f, int transpose, V* x, cudaStream_t s) {
+  IluView<V> F = view<V>(f);
+  const bool lg = f->b > 1;
+  auto grid = [&](int cnt) { return lg ? fv_blocks((long)cnt * FV_LG, 128) : fv_blocks(cnt, 128); };
+  if (!transpose) {
+    for (size_t l = 0; l + 1 < f->lv_fwd.size(); ++l) {
+      const int cnt = f->lv_fwd[l + 1] - f->lv_fwd[l];
+      if (!cnt) continue;
+      if (lg) k_ilu_lower_lg<V><<<grid(cnt), 128, 0, s>>>(F, f->rows_fwd + f->lv_fwd[l], cnt, x);
+      else k_ilu_lower<V><<<grid(cnt), 128, 0, s>>>(F, f->rows_fwd + f->lv_fwd[l], cnt, x);
+    }
+    for (size_t l = 0; l + 1 < f->lv_bwd.size(); ++l) {
+      const int cnt = f->lv_bwd[l + 1] - f->lv_bwd[l];
+      if (!cnt) continue;
+      if (lg) k_ilu_upper_lg<V><<<grid(cnt), 128, 0, s>>>(F, f->rows_bwd + f->lv_bwd[l], cnt, x);
+      else k_ilu_upper<V><<<grid(cnt), 128, 0, s>>>(F, f->rows_bwd + f->lv_bwd[l], cnt, x);
+    }
+  } else {
+    for (size_t l = 0; l + 1 < f->lv_tfwd.size(); ++l) {
+      const int cnt = f->lv_tfwd[l + 1] - f->lv_tfwd[l];
+      if (!cnt) continue;
+      const int* rows = f->rows_tfwd + f->lv_tfwd[l];
+      if (lg) k_ilu_upper_t_lg<V><<<grid(cnt), 128, 0, s>>>(F, f->tptr, f->tidx, f->tblk, rows, cnt, x);
+      else k_ilu_upper_t<V><<<grid(cnt), 128, 0, s>>>(F, f->tptr, f->tidx, f->tblk, rows, cnt, x);
+    }
+    for (size_t l = 0; l + 1 < f->lv_tbwd.size(); ++l) {
+      const int cnt = f->lv_tbwd[l + 1] - f->lv_tbwd[l];
+      if (!cnt) continue;
+      const int* rows = f->rows_tbwd + f->lv_tbwd[l];
+      if (lg) k_ilu_lower_t_lg<V><<<grid(cnt), 128, 0, s>>>(F, f->tptr, f->tidx, f->tblk, rows, cnt, x);
+      else k_ilu_lower_t<V><<<grid(cnt), 128, 0, s>>>(F, f->tptr, f->tidx, f->tblk, rows, cnt, x);
+    }
+  }
+}
+
+// Capture `body` (a sequence of launches on a stream) into an executable graph, on a private
+// stream in thread-local capture mode so that a caller's own capture is unaffected.
+template <class Body>
+int capture(Body body, cudaGraphExec_t* out) {
+  cudaStream_t cs;
+  FV_CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    body(cs);
+    e = cudaStreamEndCapture(cs, &g);
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(out, g, 0);
+  if (g) cudaGraphDestroy(g);
+  cudaStreamDestroy(cs);
+  if (e != cudaSuccess) {
+    fv_set_error("ILU(0) graph capture failed: %s", cudaGetErrorString(e));
+    return FV_ERR_CUDA;
+  }
+  return FV_OK;
+}
+
 template <class V>
 int ilu_factor(FvIlu0* f, cudaStream_t s) {
-  IluView<V> F = view<V>(f);
   unsigned long long init = ~0ull;
   FV_CUDA_TRY(cudaMemcpyAsync(f->zero_flag, &init, sizeof(init), cudaMemcpyHostToDevice, s));
-  for (size_t l = 0; l + 1 < f->lv_fwd.size(); ++l) {
-    int cnt = f->lv_fwd[l + 1] - f->lv_fwd[l];
-    if (cnt == 0) continue;
-    k_ilu_factor_level<V><<<fv_blocks(cnt, 128), 128, 0, s>>>(F, f->rows_fwd + f->lv_fwd[l], cnt,
-                                                              f->zero_flag);
+  if (!f->factor_exec) {
+    int rc = capture([&](cudaStream_t cs) { launch_factor_levels<V>(f, cs); }, &f->factor_exec);
+    if (rc != FV_OK) return rc;
   }
+  FV_CUDA_TRY(cudaGraphLaunch(f->factor_exec, s));
   FV_CUDA_TRY(cudaGetLastError());
   unsigned long long flag;
   FV_CUDA_TRY(cudaMemcpyAsync(&flag, f->zero_flag, sizeof(flag), cudaMemcpyDeviceToHost, s));
@@ -378,32 +624,17 @@ int ilu_factor(FvIlu0* f, cudaStream_t s) {
 
 template <class V>
 int ilu_apply(FvIlu0* f, const V* r, V* x, int transpose, cudaStream_t s) {
-  IluView<V> F = view<V>(f);
   const long n = (long)f->n * f->b;
-  if (r != x) k_copy<V><<<fv_blocks(n, kThreads), kThreads, 0, s>>>(n, r, x);
-  if (!transpose) {
-    for (size_t l = 0; l + 1 < f->lv_fwd.size(); ++l) {
-      int cnt = f->lv_fwd[l + 1] - f->lv_fwd[l];
-      if (cnt) k_ilu_lower<V><<<fv_blocks(cnt, 128), 128, 0, s>>>(F, f->rows_fwd + f->lv_fwd[l], cnt, x);
-    }
-    for (size_t l = 0; l + 1 < f->lv_bwd.size(); ++l) {
-      int cnt = f->lv_bwd[l + 1] - f->lv_bwd[l];
-      if (cnt) k_ilu_upper<V><<<fv_blocks(cnt, 128), 128, 0, s>>>(F, f->rows_bwd + f->lv_bwd[l], cnt, x);
-    }
-  } else {
-    for (size_t l = 0; l + 1 < f->lv_tfwd.size(); ++l) {
-      int cnt = f->lv_tfwd[l + 1] - f->lv_tfwd[l];
-      if (cnt)
-        k_ilu_upper_t<V><<<fv_blocks(cnt, 128), 128, 0, s>>>(F, f->tptr, f->tidx, f->tblk,
-                                                             f->rows_tfwd + f->lv_tfwd[l], cnt, x);
-    }
-    for (size_t l = 0; l + 1 < f->lv_tbwd.size(); ++l) {
-      int cnt = f->lv_tbwd[l + 1] - f->lv_tbwd[l];
-      if (cnt)
-        k_ilu_lower_t<V><<<fv_blocks(cnt, 128), 128, 0, s>>>(F, f->tptr, f->tidx, f->tblk,
-                                                             f->rows_tbwd + f->lv_tbwd[l], cnt, x);
-    }
+  V* w = (V*)f->work;
+  const int t = transpose ? 1 : 0;
+  if (!f->apply_exec[t]) {
+    int rc = capture([&](cudaStream_t cs) { launch_apply_levels<V>(f, t, w, cs); },
+                     &f->apply_exec[t]);
+    if (rc != FV_OK) return rc;
   }
+  FV_CUDA_TRY(cudaMemcpyAsync(w, r, sizeof(V) * n, cudaMemcpyDeviceToDevice, s));
+  FV_CUDA_TRY(cudaGraphLaunch(f->apply_exec[t], s));
+  FV_CUDA_TRY(cudaMemcpyAsync(x, w, sizeof(V) * n, cudaMemcpyDeviceToDevice, s));
   FV_CUDA_TRY(cudaGetLastError());
   return FV_OK;
 }
@@ -484,6 +715,7 @@ extern "C" int fv_ilu0_create(int n, int b, const int* indptr, const int* indice
   size_t vs = precision == 64 ? sizeof(double) : sizeof(float);
   FV_CUDA_TRY(cudaMalloc(&f->val, vs * (size_t)nnzb * b * b));
   FV_CUDA_TRY(cudaMalloc(&f->zero_flag, sizeof(unsigned long long)));
+  FV_CUDA_TRY(cudaMalloc(&f->work, vs * (size_t)n * b));
   FV_CUDA_TRY(cudaStreamSynchronize(s));
   *out = f;
   return FV_OK;
@@ -503,6 +735,10 @@ extern "C" int fv_ilu0_destroy(FvIlu0* f) {
   cudaFree(f->rows_bwd);
   cudaFree(f->rows_tfwd);
   cudaFree(f->rows_tbwd);
+  cudaFree(f->work);
+  for (cudaGraphExec_t e : f->apply_exec)
+    if (e) cudaGraphExecDestroy(e);
+  if (f->factor_exec) cudaGraphExecDestroy(f->factor_exec);
   delete f;
   return FV_OK;
 }

@@ -10,7 +10,7 @@ Restates, for the GPU, the reference's implicit solve:
   reduces the residual norm, else the shortest rung);
 * ``solve_linear`` (``aquaflux/solve/linear.py:199-298``): a right-preconditioned Krylov solve with
   the matrix-free JVP as the operator.  The GMRES itself is a third-party lineax routine in the
-  reference; here it is flexible GMRES(m) (right preconditioning, modified Gram-Schmidt) written
+  reference; here it is flexible GMRES(m) (right preconditioning, CGS2 orthogonalisation) written
   over torch device tensors, so only converged states -- not Krylov iterates -- are compared;
 * the preconditioner: ILU(0) of a materialised block Jacobian (``materialize_block_jacobian``,
   ``aquaflux/solve/sparse_jacobian.py:722-847``) in the cell-major interleaved order
@@ -117,7 +117,7 @@ class KrylovResult:
 
 def fgmres(matvec, b: torch.Tensor, precond=None, *, rtol: float = 1e-3, atol: float = 0.0,
            restart: int = 30, maxiter: int = 300) -> KrylovResult:
-    """Flexible GMRES(restart), right-preconditioned, modified Gram-Schmidt, fp64."""
+    """Flexible GMRES(restart), right-preconditioned, CGS2 orthogonalisation, fp64."""
     M = precond if precond is not None else (lambda v: v)
     x = torch.zeros_like(b)
     bnorm = float(torch.linalg.vector_norm(b))
@@ -140,12 +140,14 @@ def fgmres(matvec, b: torch.Tensor, precond=None, *, rtol: float = 1e-3, atol: f
         for j in range(m):
             Z[j] = M(V[j])
             w = matvec(Z[j])
-            h = torch.empty(j + 2, dtype=torch.float64, device=b.device)
-            for i in range(j + 1):
-                hij = torch.dot(w, V[i])
-                w = w - hij * V[i]
-                h[i] = hij
-            h[j + 1] = torch.linalg.vector_norm(w)
+            # classical Gram-Schmidt with one re-orthogonalisation (CGS2): two matrix-vector
+            # products against the basis instead of j + 1 dependent dot products
+            Vj = V[: j + 1]
+            h1 = Vj @ w
+            w = w - h1 @ Vj
+            h2 = Vj @ w
+            w = w - h2 @ Vj
+            h = torch.cat([h1 + h2, torch.linalg.vector_norm(w).reshape(1)])
             hh = h.cpu().numpy()
             H[: j + 2, j] = hh
             if hh[j + 1] > 0:
