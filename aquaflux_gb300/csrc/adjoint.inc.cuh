@@ -214,7 +214,8 @@ __device__ __forceinline__ void mn_adjoint(const MeshView& m, int f, double wgt,
 template <int DIM, bool TURB>
 __global__ void __launch_bounds__(128) a_flux(MeshView m, CaseView cv, Src<double> st, Par<double> par,
                                               const double* G, const double* cl, const double* dco,
-                                              const double* me, AdjWork aw) {
+                                              const double* me, const double* aux, AdjWork aw) {
+  using AX = Aux<DIM, TURB>;
   using L = Layout<DIM, TURB>;
   constexpr int NF = L::NFLD;
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -255,20 +256,12 @@ __global__ void __launch_bounds__(128) a_flux(MeshView m, CaseView cv, Src<doubl
       double FLb[NF];
 #pragma unroll
       for (int q = 0; q < NF; ++q) FLb[q] = aw.Wt[(long)q * nc + o] - aw.Wt[(long)q * nc + n];
-      // forward recomputation of the face
-      const double pn = st((long)L::P * nc + n);
-      double gd = 0.0;
-#pragma unroll
-      for (int j = 0; j < DIM; ++j)
-        gd += lerp(G[((long)L::P * DIM + j) * nc + o], G[((long)L::P * DIM + j) * nc + n], g) *
-              m.dvec[(long)j * nf + f];
+      // forward face intermediates kept by k_flux
+      const double mdot = aux[0L * nf + f];
+      const double damping = aux[1L * nf + f];
+      const double dhat = aux[2L * nf + f];
+      const double cmo = aux[3L * nf + f];
       const double inv_nd = m.inv_nd[f];
-      const double dhat = m.nn2[f] * lerp(dco[o], dco[n], g);
-      const double damping = ((pn - po) - gd) * inv_nd;
-      const double mdot = me[f] - (rho * A) * dhat * damping;
-      const double mnbv = TURB ? par.mu + rho * cl[2L * nc + n] : par.mu;
-      const double iden = 1.0 / (m.dpn[f] * mnbv - mo * m.dnn[f]);
-      const double cmo = mo * mnbv * A * iden;
       const bool out = mdot >= 0.0;
       // reverse
       double mdotb = FLb[L::P];
@@ -276,10 +269,7 @@ __global__ void __launch_bounds__(128) a_flux(MeshView m, CaseView cv, Src<doubl
 #pragma unroll
       for (int i = 0; i < DIM; ++i) {
         const double uo = st((long)i * nc + o), un = st((long)i * nc + n);
-        double cpn = un - uo;
-#pragma unroll
-        for (int j = 0; j < DIM; ++j)
-          cpn += G[((long)i * DIM + j) * nc + n] * tN[j] - G[((long)i * DIM + j) * nc + o] * tP[j];
+        const double cpn = aux[(long)(AX::CPN + i) * nf + f];
         const double fb = FLb[i];
         mdotb += fb * (out ? uo : un);
         const double k1 = fb * cmo;  // F_i = ... - c cpn
@@ -295,12 +285,7 @@ __global__ void __launch_bounds__(128) a_flux(MeshView m, CaseView cv, Src<doubl
         }
         pfb += fb * nrm[i] * A;
       }
-      if (TURB) {
-        // c = m_o m_n A / (dpn m_n - m_o dnn): dc/dm_o = c (1/m_o + dnn/den), dc/dm_n = c (1/m_n - dpn/den)
-        const double mXb = isnb ? cb * cmo * (1.0 / mnbv - m.dpn[f] * iden)
-                                : cb * cmo * (1.0 / mo + m.dnn[f] * iden);
-        ntb += mXb * rho;
-      }
+      if (TURB) ntb += cb * aux[(isnb ? 5L : 4L) * nf + f] * rho;
       // pf = lerp(p) + gpf . skew
       double gpfb[DIM];
 #pragma unroll
@@ -314,14 +299,10 @@ __global__ void __launch_bounds__(128) a_flux(MeshView m, CaseView cv, Src<doubl
         for (int s = 0; s < 2; ++s) {
           const int q = s == 0 ? L::K : L::W;
           const double in = s == 0 ? SIGMA_K1 : SIGMA_W1, ou = s == 0 ? SIGMA_K2 : SIGMA_W2;
-          const double go = cl[(4L + s) * nc + o], gn = cl[(4L + s) * nc + n];
+          const long b0 = AX::S0 + 4 * s;
+          const double cs_ = aux[b0 * nf + f];
+          const double cpn = aux[(b0 + 3) * nf + f];
           const double phio = st((long)q * nc + o), phin = st((long)q * nc + n);
-          double cpn = phin - phio;
-#pragma unroll
-          for (int j = 0; j < DIM; ++j)
-            cpn += G[((long)q * DIM + j) * nc + n] * tN[j] - G[((long)q * DIM + j) * nc + o] * tP[j];
-          const double idn = 1.0 / (m.dpn[f] * gn - go * m.dnn[f]);
-          const double cs_ = go * gn * A * idn;
           const double fb = FLb[q];
           mdotb += fb * (vout ? phio : phin) * irho;
           const double k1 = fb * cs_;
@@ -334,9 +315,7 @@ __global__ void __launch_bounds__(128) a_flux(MeshView m, CaseView cv, Src<doubl
 #pragma unroll
             for (int j = 0; j < DIM; ++j) Gb[q][j] -= k1 * tN[j];
           }
-          const double csb = -fb * cpn;
-          const double gXb = isnb ? csb * cs_ * (1.0 / gn - m.dpn[f] * idn)
-                                  : csb * cs_ * (1.0 / go + m.dnn[f] * idn);
+          const double gXb = -fb * cpn * aux[(b0 + (isnb ? 2 : 1)) * nf + f];
           // gamma_X = nu + (sig_out + F1 (sig_in - sig_out)) nu_t
           F1b += gXb * (in - ou) * ntX;
           ntb += gXb * (ou + F1X * (in - ou));

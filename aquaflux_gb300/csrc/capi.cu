@@ -6,6 +6,7 @@
 
 size_t fv_residual_work_bytes(int dim, int turb, long nc, long nf);
 size_t fv_adjoint_work_bytes(int dim, int turb, long nc);
+size_t fv_aux_bytes(int dim, int turb, long nf);
 extern "C" int fv_dot_f64(long n, const double* x, const double* y, double* out, void* stream);
 int fv_residual_init_constants();
 
@@ -128,6 +129,7 @@ extern "C" int fv_case_create(const FvMesh* mesh, const FvCaseDesc* desc,
   FV_CUDA_TRY(cudaMalloc(&c->tmp, sizeof(double) * (size_t)c->nfld * m->nc));
   FV_CUDA_TRY(cudaMalloc(&c->tmp2, sizeof(double) * (size_t)c->nfld * m->nc));
   FV_CUDA_TRY(cudaMalloc(&c->adj, fv_adjoint_work_bytes(m->dim, desc->turbulent, m->nc)));
+  FV_CUDA_TRY(cudaMalloc(&c->aux, fv_aux_bytes(m->dim, desc->turbulent, m->nf)));
   FV_CUDA_TRY(cudaMalloc(&c->dscalar, sizeof(double) * 4));
   CaseView& v = c->view;
   v.turb = desc->turbulent;
@@ -170,6 +172,7 @@ extern "C" int fv_case_destroy(FvCase* c) {
   cudaFree(c->tmp);
   cudaFree(c->tmp2);
   cudaFree(c->adj);
+  cudaFree(c->aux);
   cudaFree(c->dscalar);
   for (cudaEvent_t e : c->prof_events) cudaEventDestroy(e);
   delete c;

@@ -111,6 +111,7 @@ struct FvCase {
   double* tmp = nullptr;    // (n_unknowns) scratch vector
   double* tmp2 = nullptr;   // (n_unknowns) scratch vector
   double* adj = nullptr;    // adjoint workspace
+  double* aux = nullptr;    // face intermediates of the double forward pass (for the adjoint)
   double* dscalar = nullptr; // (4) device scalars
   CaseView view;
   // optional per-stage CUDA-event profiling (fv_case_profile_begin / _end)

@@ -21,6 +21,8 @@
 //               advection.py:99-187, turbulence/transport.py:581-718)
 //   k_sum       cell  conservative face-to-cell sums, pressure pin, SST sources and the omega
 //               wall-cell fixation (turbulence/sources.py:60-412, fixed_value.py:124-158)
+#include <type_traits>
+
 #include "internal.cuh"
 
 namespace {
@@ -411,10 +413,21 @@ __global__ void k_dcoeff(MeshView m, const T* ac_own, const T* ac_nb, T* dco) {
 }
 
 // ---------------------------------------------------------------- k_flux
+// Face intermediates kept for the adjoint (double forward pass only), (FV_AUX_N, nf):
+//   0 mdot, 1 damping, 2 dhat, 3 c (momentum conductance), 4 dc/dm_o, 5 dc/dm_n,
+//   6.. 6+DIM-1 diffusion numerators of the velocity components, then for k and omega:
+//   conductance, d/dgamma_o, d/dgamma_n, numerator.
+template <int DIM, bool TURB>
+struct Aux {
+  static constexpr int N = 6 + DIM + (TURB ? 8 : 0);
+  static constexpr int CPN = 6, S0 = 6 + DIM;
+};
+
 template <class T, int DIM, bool TURB>
 __global__ void __launch_bounds__(128) k_flux(MeshView m, CaseView cv, Src<T> st, Par<T> par,
                                               const T* G, const T* cl, const T* dco, const T* me,
-                                              bool recompute_me, T* FL) {
+                                              bool recompute_me, T* FL, double* aux) {
+  constexpr bool KEEP = std::is_same<T, double>::value;
   using L = Layout<DIM, TURB>;
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= m.nf) return;
@@ -448,9 +461,22 @@ __global__ void __launch_bounds__(128) k_flux(MeshView m, CaseView cv, Src<T> st
     const T damping = ((pn - po) - gd) * m.inv_nd[f];
     const T mdot = mest - (rho * A) * dhat * damping;
     const T pf = lerp(po, pn, g) + gs;
-    const T cmo = conductance(mo, mu_eff<T, TURB>(par, rho, cl, nc, n), A, m.dpn[f], m.dnn[f]);
+    const T mnb = mu_eff<T, TURB>(par, rho, cl, nc, n);
+    const T iden = 1.0 / (m.dpn[f] * mnb - mo * m.dnn[f]);
+    const T cmo = mo * mnb * A * iden;
     const bool out = val(mdot) >= 0.0;
     const T pA = pf * A;
+    using AX = Aux<DIM, TURB>;
+    if constexpr (KEEP) {
+      if (aux) {
+        aux[0L * nf + f] = mdot;
+        aux[1L * nf + f] = damping;
+        aux[2L * nf + f] = dhat;
+        aux[3L * nf + f] = cmo;
+        aux[4L * nf + f] = (mnb * A * iden) * (1.0 + mo * m.dnn[f] * iden);
+        aux[5L * nf + f] = (mo * A * iden) * (1.0 - mnb * m.dpn[f] * iden);
+      }
+    }
 #pragma unroll
     for (int i = 0; i < DIM; ++i) {
       const T uo = st((long)i * nc + o), un = st((long)i * nc + n);
@@ -459,6 +485,9 @@ __global__ void __launch_bounds__(128) k_flux(MeshView m, CaseView cv, Src<T> st
       for (int j = 0; j < DIM; ++j)
         cpn += G[((long)i * DIM + j) * nc + n] * tN[j] - G[((long)i * DIM + j) * nc + o] * tP[j];
       FL[(long)i * nf + f] = (pA * nrm[i] - cmo * cpn) + mdot * (out ? uo : un);
+      if constexpr (KEEP) {
+        if (aux) aux[(long)(AX::CPN + i) * nf + f] = cpn;
+      }
     }
     FL[(long)L::P * nf + f] = mdot;
     if (TURB) {
@@ -473,7 +502,18 @@ __global__ void __launch_bounds__(128) k_flux(MeshView m, CaseView cv, Src<T> st
 #pragma unroll
         for (int j = 0; j < DIM; ++j)
           cpn += G[((long)q * DIM + j) * nc + n] * tN[j] - G[((long)q * DIM + j) * nc + o] * tP[j];
-        FL[(long)q * nf + f] = vflux * (vout ? phio : phin) - conductance(go, gn, A, m.dpn[f], m.dnn[f]) * cpn;
+        const T idn = 1.0 / (m.dpn[f] * gn - go * m.dnn[f]);
+        const T cs_ = go * gn * A * idn;
+        FL[(long)q * nf + f] = vflux * (vout ? phio : phin) - cs_ * cpn;
+        if constexpr (KEEP) {
+          if (aux) {
+            const long b0 = AX::S0 + 4 * s;
+            aux[b0 * nf + f] = cs_;
+            aux[(b0 + 1) * nf + f] = (gn * A * idn) * (1.0 + go * m.dnn[f] * idn);
+            aux[(b0 + 2) * nf + f] = (go * A * idn) * (1.0 - gn * m.dpn[f] * idn);
+            aux[(b0 + 3) * nf + f] = cpn;
+          }
+        }
       }
     }
   } else {
@@ -616,7 +656,7 @@ void freeze<Dual>(Dual* x, long n, cudaStream_t s) {
 
 template <class T, int DIM, bool TURB>
 int run(FvCase* cs, Src<T> st, Par<T> par, double* R, double* JV, cudaStream_t s,
-        bool frozen = false, bool end_profile_run = true) {
+        bool frozen = false, bool end_profile_run = true, double* aux = nullptr) {
   const MeshView& m = cs->mesh->view;
   const CaseView& cv = cs->view;
   const long nc = m.nc, nf = m.nf;
@@ -633,7 +673,8 @@ int run(FvCase* cs, Src<T> st, Par<T> par, double* R, double* JV, cudaStream_t s
   k_dcoeff<T><<<bc, TB, 0, s>>>(m, w.acown, w.acnb, w.dco);
   if (frozen) freeze<T>(w.G, (long)(w.dco + nc - w.G), s);  // G, closure, Gwi, a_P, d
   fv_prof_mark(cs, 4, s);
-  k_flux<T, DIM, TURB><<<bf, TB, 0, s>>>(m, cv, st, par, w.G, w.cl, w.dco, w.me, frozen, w.FL);
+  k_flux<T, DIM, TURB><<<bf, TB, 0, s>>>(m, cv, st, par, w.G, w.cl, w.dco, w.me, frozen, w.FL,
+                                         aux);
   fv_prof_mark(cs, 5, s);
   k_sum<T, DIM, TURB><<<bc, TB, 0, s>>>(m, cv, st, par, w.FL, w.cl, w.G, w.Gwi, R, JV);
   fv_prof_mark(cs, 6, s);
@@ -668,7 +709,7 @@ int run_vjp(FvCase* cs, const double* state, const double* W, double* R, double*
   const long nc = m.nc, nf = m.nf;
   Src<double> st{state};
   Par<double> par{cs->mu, cs->inlet_scale, cs->mu / cs->desc.rho};
-  int rc = run<double, DIM, TURB>(cs, st, par, R ? R : cs->tmp, nullptr, s, false, false);
+  int rc = run<double, DIM, TURB>(cs, st, par, R ? R : cs->tmp, nullptr, s, false, false, cs->aux);
   if (rc != FV_OK) return rc;
   // forward workspace (double layout, as written by run<double>)
   Work<double> fw = work_layout<double, DIM, TURB>(cs->work, nc, nf);
@@ -688,7 +729,7 @@ int run_vjp(FvCase* cs, const double* state, const double* W, double* R, double*
   const int bc = fv_blocks(nc, TB);
   a_sum<DIM, TURB><<<bc, TB, 0, s>>>(m, cv, st, par, W, cl, G, Gwi, aw);
   fv_prof_mark(cs, 7, s);
-  a_flux<DIM, TURB><<<bc, TB, 0, s>>>(m, cv, st, par, G, cl, dco, fw.me, aw);
+  a_flux<DIM, TURB><<<bc, TB, 0, s>>>(m, cv, st, par, G, cl, dco, fw.me, cs->aux, aw);
   fv_prof_mark(cs, 8, s);
   a_apcoef<DIM, TURB><<<bc, TB, 0, s>>>(m, cv, st, par, G, cl, dco, fw.me, aw);
   fv_prof_mark(cs, 9, s);
@@ -708,6 +749,10 @@ bool g_const_ready = false;
 size_t fv_adjoint_work_bytes(int dim, int turb, long nc) {
   long nfld = dim + 1 + (turb ? 2 : 0);
   return sizeof(double) * (size_t)(2 * nfld * nc + nfld * dim * nc + nc + 4 * nc + dim * nc);
+}
+
+size_t fv_aux_bytes(int dim, int turb, long nf) {
+  return sizeof(double) * (size_t)(6 + dim + (turb ? 8 : 0)) * nf;
 }
 
 int fv_case_vjp_run(FvCase* cs, const double* state, const double* W, double* R, double* out,

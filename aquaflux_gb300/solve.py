@@ -247,3 +247,47 @@ def newton_solve(case, state0, *, rtol: float = 1e-10, atol: float = 1e-12, max_
             break
     torch.cuda.synchronize()
     return NewtonResult(s, converged, step, norms, its, time.perf_counter() - t_all, phases)
+
+
+class TransposedPreconditioner:
+    """``M^T``: the transposed ILU(0) solve of an :class:`IluPreconditioner` (exact transpose, as
+    the reference's ``TransposedPreconditioner`` / ``jax.linear_transpose``,
+    ``aquaflux/solve/implicit.py:709-730``)."""
+
+    def __init__(self, pc: IluPreconditioner):
+        self.pc = pc
+
+    def apply(self, r: torch.Tensor) -> torch.Tensor:
+        pc = self.pc
+        n, b = pc.jac.n, pc.jac.b
+        pc._cm.copy_(r.view(b, n).t().reshape(-1))
+        pc.ilu.solve(pc._cm, transpose=True, out=pc._x)
+        return pc._x.view(n, b).t().reshape(-1).to(torch.float64)
+
+
+@dataclasses.dataclass
+class AdjointResult:
+    lam: torch.Tensor           # adjoint state: J^T lam = g
+    dparams: torch.Tensor       # (d/dmu, d/d inlet_scale) of the objective
+    krylov_iterations: int
+    converged: bool
+
+
+def implicit_adjoint(case, state, g, *, rtol: float = 1e-10, precision: int = 64,
+                     restart: int = 30, max_krylov: int = 1000,
+                     preconditioner: IluPreconditioner | None = None) -> AdjointResult:
+    """Implicit-function-theorem gradient at a converged root (``_implicit_solve_bwd``,
+    ``aquaflux/solve/implicit.py:733-761``): solve ``J^T lam = g`` with FGMRES on the hand-written
+    VJP and the transposed ILU(0) preconditioner (the reference's tight 1e-10 adjoint solve,
+    ``aquaflux/solve/linear.py:40-42``), then ``dL/dtheta = -lam^T dR/dtheta`` for
+    ``theta = (mu, inlet_scale)``."""
+    s = torch.as_tensor(state, dtype=torch.float64, device="cuda")
+    gv = torch.as_tensor(g, dtype=torch.float64, device="cuda")
+    if preconditioner is None:
+        preconditioner = IluPreconditioner(BlockJacobian(case, reach=1, frozen=True), precision)
+    preconditioner.refresh(s)
+    mt = TransposedPreconditioner(preconditioner)
+    res = fgmres(lambda w: case.vjp(s, w), gv, mt.apply, rtol=rtol, restart=restart,
+                 maxiter=max_krylov)
+    dparams = -case.param_vjp(s, res.x)
+    return AdjointResult(res.x, dparams, res.iterations, res.converged)

@@ -85,3 +85,35 @@ def test_fp32_and_fp64_preconditioners_reach_the_same_root():
     assert a.converged and b.converged
     sa, sb = a.state.cpu().numpy(), b.state.cpu().numpy()
     assert np.abs(sa - sb).max() <= 1e-8 * np.abs(sa).max()
+
+
+def test_implicit_adjoint_matches_finite_differences_of_the_solve():
+    """d(mean |u|)/d mu through the converged cavity, against central differences of the solve
+    (the check of the reference's tests/integration/test_cavity.py:74-95)."""
+    from aquaflux_gb300.solve import implicit_adjoint, newton_solve
+
+    n = 12
+    m, case = _cavity(n)
+    z = np.zeros(case.n_unknowns)
+
+    def mean_speed(mu):
+        case.set_params(mu=mu)
+        res = newton_solve(case, z, precision=64, max_steps=40, reach=3, frozen=False, rtol=1e-14)
+        assert res.converged
+        u = res.state[: n * n]
+        return float(u.abs().mean()), res.state
+
+    mu0 = 0.01
+    f0, state = mean_speed(mu0)
+    u = state[: n * n]
+    g = torch.zeros_like(state)
+    g[: n * n] = torch.sign(u) / (n * n)
+    case.set_params(mu=mu0)
+    adj = implicit_adjoint(case, state, g)
+    assert adj.converged
+    h = 1e-5
+    fd = (mean_speed(mu0 + h)[0] - mean_speed(mu0 - h)[0]) / (2 * h)
+    case.set_params(mu=mu0)
+    grad = float(adj.dparams[0])
+    assert abs(fd) > 1e-3
+    assert abs(grad - fd) <= 1e-4 * abs(fd)
