@@ -90,7 +90,8 @@ __global__ void __launch_bounds__(128) a_sum(MeshView m, CaseView cv, Src<double
       const double kp = fmax(k, 0.0);
       const double num = PROD_RATIO * BETA_STAR * kp * w;
       const double den = fmax(nut, NUT_FLOOR);
-      const double cap = num / den;
+      const double iden = 1.0 / den;
+      const double cap = num * iden;
       const double S2 = S * S;
       const double mn = fmin(S2, cap);
       // R_w -= alpha * min(S^2, cap) * V
@@ -99,7 +100,7 @@ __global__ void __launch_bounds__(128) a_sum(MeshView m, CaseView cv, Src<double
       double S2b = 0.0, capb = 0.0;
       split_ext(S2, cap, mbar, true, &S2b, &capb);
       Sb += S2b * 2.0 * S;
-      double numb = capb / den, denb = -capb * num / (den * den);
+      double numb = capb * iden, denb = -capb * cap * iden;
       double nutb_f = 0.0, flb = 0.0;
       split_ext(nut, NUT_FLOOR, denb, false, &nutb_f, &flb);
       ntb += nutb_f;
@@ -118,16 +119,17 @@ __global__ void __launch_bounds__(128) a_sum(MeshView m, CaseView cv, Src<double
         gwi[j] = Gwi[(long)j * nc + c];
         dkw += gk[j] * gwi[j];
       }
-      const double cross = 2.0 * (1.0 - F1) * SIGMA_W2 * dkw / w;
+      const double iw = 1.0 / w;
+      const double cross = 2.0 * (1.0 - F1) * SIGMA_W2 * dkw * iw;
       const double crb = -Ww * V;
-      F1b += crb * (-2.0 * SIGMA_W2 * dkw / w);
-      const double dotb = crb * 2.0 * (1.0 - F1) * SIGMA_W2 / w;
+      F1b += crb * (-2.0 * SIGMA_W2 * dkw * iw);
+      const double dotb = crb * 2.0 * (1.0 - F1) * SIGMA_W2 * iw;
 #pragma unroll
       for (int j = 0; j < DIM; ++j) {
         gkb[j] += dotb * gwi[j];
         gwib[j] += dotb * gk[j];
       }
-      sb[L::W] += crb * (-cross / w);
+      sb[L::W] += crb * (-cross * iw);
     }
     // ---- k row: R_k -= lim * V;  R_k += beta* k weff V
     const double Wk = wr[L::K];
@@ -480,7 +482,7 @@ __global__ void __launch_bounds__(128) a_flux(MeshView m, CaseView cv, Src<doubl
 template <int DIM, bool TURB>
 __global__ void __launch_bounds__(128) a_apcoef(MeshView m, CaseView cv, Src<double> st, Par<double> par,
                                                 const double* G, const double* cl, const double* dco,
-                                                const double* me, AdjWork aw) {
+                                                const double* me, const double* aux, AdjWork aw) {
   using L = Layout<DIM, TURB>;
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= m.nc) return;
@@ -508,13 +510,8 @@ __global__ void __launch_bounds__(128) a_apcoef(MeshView m, CaseView cv, Src<dou
       const double abn = -aw.dcob[n] * dco[n] * dco[n] * m.inv_vol[n];
       meb = (abo * dpos(mdot) - abn * dpos(-mdot)) * (isnb ? g : 1.0 - g);
       if (TURB) {
-        const double mo = par.mu + rho * cl[2L * nc + o];
-        const double mnbv = par.mu + rho * cl[2L * nc + n];
-        const double iden = 1.0 / (m.dpn[f] * mnbv - mo * m.dnn[f]);
-        const double cv_ = mo * mnbv * A * iden;
-        const double viscb = abo + abn;
-        ntb += rho * viscb * cv_ * (isnb ? (1.0 / mnbv - m.dpn[f] * iden)
-                                          : (1.0 / mo + m.dnn[f] * iden));
+        // the viscous conductance is the flux stage's c(m_o, m_n): its derivatives were kept
+        ntb += rho * (abo + abn) * aux[(isnb ? 5L : 4L) * nf + f];
       }
     } else {
       const signed char kind = cv.fkind[f];
@@ -603,23 +600,26 @@ __global__ void __launch_bounds__(128) a_closure(MeshView m, CaseView cv, Src<do
   double dot_kw = gk[0] * gw[0];
 #pragma unroll
   for (int j = 1; j < DIM; ++j) dot_kw += gk[j] * gw[j];
-  const double cd0 = 2.0 * SIGMA_W2 * dot_kw / w;
+  const double iw = 1.0 / w, id = cv.inv_wd[c], id2 = cv.inv_wd2[c];
+  const double cd0 = (2.0 * SIGMA_W2) * dot_kw * iw;
   const double cd = fmax(cd0, CROSS_FLOOR);
+  const double icd = 1.0 / cd;
   const double sk = kp > 0.0 ? sqrt(kp) : 0.0;
-  const double vt = 500.0 * nu / ((d * d) * w);
-  const double c1 = sk / (BETA_STAR * w * d);
+  const double vt = (500.0 * id2) * nu * iw;
+  const double c1 = sk * iw * (id / BETA_STAR);
   const double inner = fmax(c1, vt);
-  const double c2 = 4.0 * SIGMA_W2 * kp / (cd * (d * d));
+  const double c2 = (4.0 * SIGMA_W2 * id2) * kp * icd;
   const double arg1 = fmin(inner, c2);
   const double a1sq = arg1 * arg1;
-  const double F1 = tanh(a1sq * a1sq);
-  const double a2 = 2.0 * sk / (BETA_STAR * w * d);
+  const double F1 = cl[(long)nc + c];   // tanh(arg1^4), kept by the forward closure
+  const double a2 = 2.0 * c1;
   const double arg2 = fmax(a2, vt);
-  const double F2 = tanh(arg2 * arg2);
+  const double F2 = cl[6L * nc + c];    // tanh(arg2^2)
   const double Mx = fmax(A1 * w, S * F2);
+  const double iMx = 1.0 / Mx;
   // reverse: nut = A1 kp / M
-  double kpb = ntb * A1 / Mx;
-  const double Mb = -ntb * A1 * kp / (Mx * Mx);
+  double kpb = ntb * A1 * iMx;
+  const double Mb = -ntb * A1 * kp * iMx * iMx;
   double awb = 0.0, sfb = 0.0;
   split_ext(A1 * w, S * F2, Mb, false, &awb, &sfb);
   double wb = awb * A1;
@@ -628,30 +628,29 @@ __global__ void __launch_bounds__(128) a_closure(MeshView m, CaseView cv, Src<do
   const double arg2b = F2b * (1.0 - F2 * F2) * 2.0 * arg2;
   double a2b = 0.0, vtb = 0.0;
   split_ext(a2, vt, arg2b, false, &a2b, &vtb);
-  double skb = a2b * 2.0 / (BETA_STAR * w * d);
-  wb += a2b * (-a2 / w);
+  // a2 = 2 c1
+  double c1b = 2.0 * a2b;
   // F1 = tanh(arg1^4)
   const double arg1b = F1b * (1.0 - F1 * F1) * 4.0 * a1sq * arg1;
   double innerb = 0.0, c2b = 0.0;
   split_ext(inner, c2, arg1b, true, &innerb, &c2b);
-  double c1b = 0.0;
   split_ext(c1, vt, innerb, false, &c1b, &vtb);
-  skb += c1b / (BETA_STAR * w * d);
-  wb += c1b * (-c1 / w);
-  wb += vtb * (-vt / w);
-  kpb += c2b * 4.0 * SIGMA_W2 / (cd * (d * d));
-  const double cdb = -c2b * c2 / cd;
+  // c1 = sk / (beta* w d), vt = 500 nu / (d^2 w)
+  double skb = c1b * iw * (id / BETA_STAR);
+  wb -= (c1b * c1 + vtb * vt) * iw;
+  kpb += c2b * (4.0 * SIGMA_W2 * id2) * icd;
+  const double cdb = -c2b * c2 * icd;
   double cd0b = 0.0, flb = 0.0;
   split_ext(cd0, CROSS_FLOOR, cdb, false, &cd0b, &flb);
-  const double dotb = cd0b * 2.0 * SIGMA_W2 / w;
-  wb += cd0b * (-cd0 / w);
+  const double dotb = cd0b * (2.0 * SIGMA_W2) * iw;
+  wb -= cd0b * cd0 * iw;
   double gkb[DIM], gwb[DIM];
 #pragma unroll
   for (int j = 0; j < DIM; ++j) {
     gkb[j] = dotb * gw[j];
     gwb[j] = dotb * gk[j] + aw.Gwib[(long)j * nc + c];
   }
-  kpb += skb * (kp > 0.0 ? 0.5 / sk : 0.0);
+  kpb += kp > 0.0 ? skb * 0.5 / sk : 0.0;
   double kb = kpb * dpos(k);
   double S0b = Sb;
   double ub[DIM];
@@ -704,7 +703,7 @@ __global__ void __launch_bounds__(128) a_closure(MeshView m, CaseView cv, Src<do
   }
   // S0 = safe_sqrt(2 sum s_ij^2)
   if (S0 > 0.0 && S0b != 0.0) {
-    const double sumb = S0b / S0;
+    const double sumb = S0b / S0;  // d sqrt(2 sum) / d sum = 1 / S0
 #pragma unroll
     for (int i = 0; i < DIM; ++i)
 #pragma unroll
@@ -726,8 +725,48 @@ __global__ void __launch_bounds__(128) a_closure(MeshView m, CaseView cv, Src<do
 }
 
 // ---------------------------------------------------------------- a_grad
+// G_c = (1/V_c) sum_f (+-) S_f phi_f  =>  phib_f = S_f . (Gb_o / V_o - Gb_n / V_n), then each side
+// takes its interpolation weight of phib_f.  The face pass forms phib once per face (into `pb`,
+// (NF, nf)); the cell pass gathers it.
 template <int DIM, bool TURB>
-__global__ void __launch_bounds__(128) a_grad(MeshView m, CaseView cv, AdjWork aw, double* out) {
+__global__ void __launch_bounds__(128) a_grad_face(MeshView m, CaseView cv, AdjWork aw, double* pb) {
+  using L = Layout<DIM, TURB>;
+  constexpr int NF = L::NFLD;
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= m.nf) return;
+  const int nc = m.nc, nf = m.nf;
+  const int o = m.owner[f];
+  const double A = m.area[f];
+  double S[DIM];
+#pragma unroll
+  for (int j = 0; j < DIM; ++j) S[j] = m.normal[(long)j * nf + f] * A;
+  const double ivo = m.inv_vol[o];
+  if (f < m.nfi) {
+    const int n = m.nb[f];
+    const double ivn = m.inv_vol[n];
+#pragma unroll
+    for (int q = 0; q < NF; ++q) {
+      double phib = 0.0;
+#pragma unroll
+      for (int j = 0; j < DIM; ++j)
+        phib += S[j] * (aw.Gb[((long)q * DIM + j) * nc + o] * ivo -
+                        aw.Gb[((long)q * DIM + j) * nc + n] * ivn);
+      pb[(long)q * nf + f] = phib;
+    }
+  } else {
+#pragma unroll
+    for (int q = 0; q < NF; ++q) {
+      double phib = 0.0;
+#pragma unroll
+      for (int j = 0; j < DIM; ++j) phib += S[j] * aw.Gb[((long)q * DIM + j) * nc + o];
+      pb[(long)q * nf + f] = phib * ivo;
+    }
+  }
+}
+
+template <int DIM, bool TURB>
+__global__ void __launch_bounds__(128) a_grad(MeshView m, CaseView cv, AdjWork aw, const double* pb,
+                                              double* out) {
   using L = Layout<DIM, TURB>;
   constexpr int NF = L::NFLD;
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -740,28 +779,14 @@ __global__ void __launch_bounds__(128) a_grad(MeshView m, CaseView cv, AdjWork a
   for (int it = b; it < e; ++it) {
     const unsigned ent = m.cf_face[it];
     const int f = (int)(ent & ~FV_NB_BIT);
-    const bool isnb = (ent & FV_NB_BIT) != 0;
-    const int o = m.owner[f];
-    const double A = m.area[f];
-    double S[DIM];
-#pragma unroll
-    for (int j = 0; j < DIM; ++j) S[j] = m.normal[(long)j * nf + f] * A;
-    const double ivo = 1.0 / m.vol[o];
     if (f < m.nfi) {
-      const int n = m.nb[f];
-      const double ivn = 1.0 / m.vol[n];
       const double g = m.g[f];
-      const double wgt = isnb ? g : 1.0 - g;
+      const double wgt = (ent & FV_NB_BIT) ? g : 1.0 - g;
 #pragma unroll
-      for (int q = 0; q < NF; ++q) {
-        double phib = 0.0;
-#pragma unroll
-        for (int j = 0; j < DIM; ++j)
-          phib += S[j] * (aw.Gb[((long)q * DIM + j) * nc + o] * ivo -
-                          aw.Gb[((long)q * DIM + j) * nc + n] * ivn);
-        acc[q] += wgt * phib;
-      }
+      for (int q = 0; q < NF; ++q) acc[q] += wgt * pb[(long)q * nf + f];
     } else {
+      // leading-order boundary values depend on the owner value: outlet velocity,
+      // wall / inlet pressure, zero-gradient k and omega
       const signed char kind = cv.fkind[f];
 #pragma unroll
       for (int q = 0; q < NF; ++q) {
@@ -770,11 +795,7 @@ __global__ void __launch_bounds__(128) a_grad(MeshView m, CaseView cv, AdjWork a
         else if (q == L::P) dep = kind >= 0 && kind <= 2;
         else if (q == L::K) dep = cv.kkind[f] == 1;
         else dep = cv.wkind[f] == 1;
-        if (!dep) continue;
-        double phib = 0.0;
-#pragma unroll
-        for (int j = 0; j < DIM; ++j) phib += S[j] * aw.Gb[((long)q * DIM + j) * nc + o] * ivo;
-        acc[q] += phib;
+        if (dep) acc[q] += pb[(long)q * nf + f];
       }
     }
   }

@@ -159,7 +159,7 @@ struct Layout {
 template <class T>
 struct Work {
   T* G;      // (NF, DIM, nc) gradients
-  T* cl;     // (6, nc) strain, F1, nu_t, wall shear rate, k diffusivity, omega diffusivity
+  T* cl;     // (7, nc) strain, F1, nu_t, wall shear rate, k diffusivity, omega diffusivity, F2
   T* Gwi;    // (DIM, nc) omega gradient with the wall-cell value imposed
   T* acown;  // (nf) momentum-diagonal coefficient, owner side
   T* acnb;   // (nf) neighbour side
@@ -173,7 +173,7 @@ Work<T> work_layout(void* base, long nc, long nf) {
   T* p = (T*)base;
   Work<T> w;
   w.G = p; p += (long)NF * DIM * nc;
-  w.cl = p; p += 6 * nc;
+  w.cl = p; p += 7 * nc;
   w.Gwi = p; p += DIM * nc;
   w.acown = p; p += nf;
   w.acnb = p; p += nf;
@@ -323,6 +323,7 @@ __global__ void __launch_bounds__(128) k_closure(MeshView m, CaseView cv, Src<T>
   cl[3L * nc + c] = shear;
   cl[4L * nc + c] = nu + (SIGMA_K2 + F1 * (SIGMA_K1 - SIGMA_K2)) * nut;
   cl[5L * nc + c] = nu + (SIGMA_W2 + F1 * (SIGMA_W1 - SIGMA_W2)) * nut;
+  cl[6L * nc + c] = F2;
 #pragma unroll
   for (int j = 0; j < DIM; ++j) Gwi[(long)j * nc + c] = gw[j];
 }
@@ -731,11 +732,12 @@ int run_vjp(FvCase* cs, const double* state, const double* W, double* R, double*
   fv_prof_mark(cs, 7, s);
   a_flux<DIM, TURB><<<bc, TB, 0, s>>>(m, cv, st, par, G, cl, dco, fw.me, cs->aux, aw);
   fv_prof_mark(cs, 8, s);
-  a_apcoef<DIM, TURB><<<bc, TB, 0, s>>>(m, cv, st, par, G, cl, dco, fw.me, aw);
+  a_apcoef<DIM, TURB><<<bc, TB, 0, s>>>(m, cv, st, par, G, cl, dco, fw.me, cs->aux, aw);
   fv_prof_mark(cs, 9, s);
   if (TURB) a_closure<DIM><<<bc, TB, 0, s>>>(m, cv, st, par, G, cl, aw);
   fv_prof_mark(cs, 10, s);
-  a_grad<DIM, TURB><<<bc, TB, 0, s>>>(m, cv, aw, out);
+  a_grad_face<DIM, TURB><<<fv_blocks(nf, TB), TB, 0, s>>>(m, cv, aw, fw.FL);
+  a_grad<DIM, TURB><<<bc, TB, 0, s>>>(m, cv, aw, fw.FL, out);
   fv_prof_mark(cs, 11, s);
   fv_prof_end_run(cs);
   FV_CUDA_TRY(cudaGetLastError());
@@ -766,7 +768,7 @@ int fv_case_vjp_run(FvCase* cs, const double* state, const double* W, double* R,
 
 size_t fv_residual_work_bytes(int dim, int turb, long nc, long nf) {
   long nfld = dim + 1 + (turb ? 2 : 0);
-  long n = nfld * dim * nc + 6 * nc + dim * nc + 3 * nf + nc + nfld * nf;
+  long n = nfld * dim * nc + 7 * nc + dim * nc + 3 * nf + nc + nfld * nf;
   return (size_t)n * sizeof(Dual);
 }
 
