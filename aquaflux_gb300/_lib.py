@@ -60,6 +60,10 @@ SIGNATURES = {
     "fv_ilu0_factor_values": (c_int, [P, P, P]),
     "fv_dot_f64": (c_int, [c_long, P, P, P, P]),
     "fv_saturation_colouring": (c_int, [c_int, P, P, P, P]),
+    "fv_aggregate": (c_int, [c_int, P, P, P, P]),
+    "fv_galerkin_f32": (c_int, [c_long, c_int, P, P, P, c_int, P, P]),
+    "fv_restrict_f32": (c_int, [c_int, c_int, P, P, P, P, P]),
+    "fv_prolong_add_f32": (c_int, [c_int, c_int, P, P, P, P]),
 }
 
 _lib = None

@@ -16,7 +16,7 @@ CSRC = os.path.join(HERE, "csrc")
 ROOT = os.path.dirname(HERE)
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 UNITS = {"mesh.cu": [], "residual.cu": [], "capi.cu": [], "sparse.cu": ["-fmad=false"],
-         "colour.cu": [], "noalloc.cu": []}
+         "colour.cu": [], "noalloc.cu": [], "amg.cu": []}
 
 
 def _nvcc() -> str:

@@ -1,0 +1,142 @@
+// Aggregation multigrid pieces: cell aggregation (host), Galerkin coarse operators, restriction
+// and prolongation (device).
+//
+// The hierarchy follows the reference's aggregation AMG for the coupled block operator
+// (aquaflux/solve/multigrid.py:1011-1245 _build_aggregation_hierarchy, :353 _mis_aggregate, used
+// by the ILU-smoothed V-cycle of aquaflux/solve/ilu_inverse.py:160-308): cells are aggregated on
+// the cell graph, every field of a cell rides its aggregate's coarse unknown (block-size aware),
+// and the coarse operator is the Galerkin product P^T A P.  Here P is the unsmoothed (piecewise
+// constant) tentative prolongation, so P^T A P is an aggregate-to-aggregate sum of fine blocks: the
+// GPU forms each coarse block as the ordered sum of its fine blocks (deterministic, no atomics).
+#include <vector>
+
+#include "internal.cuh"
+
+// Greedy aggregation of a symmetric cell graph (CSR, self loops ignored):
+//   pass 1 -- cells in index order whose whole neighbourhood is free become the root of an
+//             aggregate holding the cell and its neighbours;
+//   pass 2 -- a free cell joins the aggregate of its first aggregated neighbour;
+//   pass 3 -- cells still free group with their free neighbours (or alone).
+extern "C" int fv_aggregate(int n, const int* indptr, const int* indices, int* agg, int* n_agg) {
+  if (n <= 0 || !indptr || !indices || !agg || !n_agg) {
+    fv_set_error("fv_aggregate: bad arguments");
+    return FV_ERR_ARG;
+  }
+  for (int i = 0; i < n; ++i) agg[i] = -1;
+  int na = 0;
+  for (int i = 0; i < n; ++i) {
+    bool free_nb = true;
+    for (int q = indptr[i]; q < indptr[i + 1] && free_nb; ++q) {
+      const int j = indices[q];
+      if (j < 0 || j >= n) {
+        fv_set_error("fv_aggregate: neighbour index out of range");
+        return FV_ERR_ARG;
+      }
+      if (agg[j] >= 0) free_nb = false;
+    }
+    if (!free_nb || agg[i] >= 0) continue;
+    agg[i] = na;
+    for (int q = indptr[i]; q < indptr[i + 1]; ++q) agg[indices[q]] = na;
+    ++na;
+  }
+  std::vector<int> pass2(n, -1);
+  for (int i = 0; i < n; ++i) {
+    if (agg[i] >= 0) continue;
+    for (int q = indptr[i]; q < indptr[i + 1]; ++q) {
+      const int j = indices[q];
+      if (j != i && agg[j] >= 0) {
+        pass2[i] = agg[j];
+        break;
+      }
+    }
+  }
+  for (int i = 0; i < n; ++i)
+    if (agg[i] < 0 && pass2[i] >= 0) agg[i] = pass2[i];
+  for (int i = 0; i < n; ++i) {
+    if (agg[i] >= 0) continue;
+    agg[i] = na;
+    for (int q = indptr[i]; q < indptr[i + 1]; ++q)
+      if (agg[indices[q]] < 0) agg[indices[q]] = na;
+    ++na;
+  }
+  *n_agg = na;
+  return FV_OK;
+}
+
+namespace {
+
+// coarse[Q] = sum over the fine blocks listed for Q (gptr / glist), in list order.
+template <class In>
+__global__ void k_galerkin(long n_coarse_blocks, int b, const long* gptr, const long* glist,
+                           const In* fine, float* coarse) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long bb = (long)b * b;
+  if (t >= n_coarse_blocks * bb) return;
+  const long Q = t / bb, e = t % bb;
+  double acc = 0.0;
+  for (long p = gptr[Q]; p < gptr[Q + 1]; ++p) acc += (double)fine[glist[p] * bb + e];
+  coarse[t] = (float)acc;
+}
+
+// rc[I * b + a] = sum over the member cells i of aggregate I (mptr / mlist) of r[i * b + a]
+__global__ void k_restrict(int n_coarse, int b, const int* mptr, const int* mlist, const float* r,
+                           float* rc) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long)n_coarse * b) return;
+  const int I = (int)(t / b), a = (int)(t % b);
+  float acc = 0.0f;
+  for (int p = mptr[I]; p < mptr[I + 1]; ++p) acc += r[(long)mlist[p] * b + a];
+  rc[t] = acc;
+}
+
+// x[i * b + a] += xc[agg[i] * b + a]
+__global__ void k_prolong_add(int n_fine, int b, const int* agg, const float* xc, float* x) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long)n_fine * b) return;
+  const int i = (int)(t / b), a = (int)(t % b);
+  x[t] += xc[(long)agg[i] * b + a];
+}
+
+}  // namespace
+
+extern "C" int fv_galerkin_f32(long n_coarse_blocks, int b, const long* gptr, const long* glist,
+                               const void* fine, int fine_f64, float* coarse, void* stream) {
+  if (n_coarse_blocks <= 0 || b <= 0 || !gptr || !glist || !fine || !coarse) {
+    fv_set_error("fv_galerkin_f32: bad arguments");
+    return FV_ERR_ARG;
+  }
+  const long n = n_coarse_blocks * b * b;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (fine_f64)
+    k_galerkin<double><<<fv_blocks(n, 256), 256, 0, s>>>(n_coarse_blocks, b, gptr, glist,
+                                                         (const double*)fine, coarse);
+  else
+    k_galerkin<float><<<fv_blocks(n, 256), 256, 0, s>>>(n_coarse_blocks, b, gptr, glist,
+                                                        (const float*)fine, coarse);
+  FV_CUDA_TRY(cudaGetLastError());
+  return FV_OK;
+}
+
+extern "C" int fv_restrict_f32(int n_coarse, int b, const int* mptr, const int* mlist,
+                               const float* r, float* rc, void* stream) {
+  if (n_coarse <= 0 || b <= 0 || !mptr || !mlist || !r || !rc) {
+    fv_set_error("fv_restrict_f32: bad arguments");
+    return FV_ERR_ARG;
+  }
+  const long n = (long)n_coarse * b;
+  k_restrict<<<fv_blocks(n, 256), 256, 0, (cudaStream_t)stream>>>(n_coarse, b, mptr, mlist, r, rc);
+  FV_CUDA_TRY(cudaGetLastError());
+  return FV_OK;
+}
+
+extern "C" int fv_prolong_add_f32(int n_fine, int b, const int* agg, const float* xc, float* x,
+                                  void* stream) {
+  if (n_fine <= 0 || b <= 0 || !agg || !xc || !x) {
+    fv_set_error("fv_prolong_add_f32: bad arguments");
+    return FV_ERR_ARG;
+  }
+  const long n = (long)n_fine * b;
+  k_prolong_add<<<fv_blocks(n, 256), 256, 0, (cudaStream_t)stream>>>(n_fine, b, agg, xc, x);
+  FV_CUDA_TRY(cudaGetLastError());
+  return FV_OK;
+}

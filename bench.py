@@ -132,6 +132,23 @@ def flux_kernel_bytes(wl) -> float:
     return m.n_faces * per_face + m.n_cells * per_cell
 
 
+def aflux_kernel_bytes(wl) -> float:
+    """Compulsory bytes of one launch of the adjoint face-flux kernel (``a_flux``, fp64).
+
+    Per face: indices (8 B), the factors it reads (area, normal, tP, tN, skew, dvec, n (x) skew,
+    n.n, 1/nd, g: 4 + 5 dim + dim^2 doubles) and the forward intermediates kept by the flux stage
+    (6 + dim + 8 doubles for SST).  Per cell in: state, gradients, F1, nu_t, the two diffusivities,
+    d, the flux-sum cotangent; out: state, gradient, d, F1 and nu_t adjoints.
+    """
+    m = wl.mesh
+    dim, nf = m.dim, m.dim + (3 if wl.sst else 1)
+    aux = 6 + dim + (8 if wl.sst else 0)
+    per_face = 8 + (4 + 5 * dim + dim * dim + aux) * 8
+    per_cell = (nf + nf * dim + (4 if wl.sst else 0) + 1 + nf) * 8 + \
+        (nf + nf * dim + 1 + (2 if wl.sst else 0)) * 8
+    return m.n_faces * per_face + m.n_cells * per_cell
+
+
 def measured_peaks() -> dict:
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -273,15 +290,23 @@ def run_gpu(args, rank: int, world: int, local_rank: int) -> dict | None:
 
     peaks = measured_peaks()
     dom = max(stage_ms, key=stage_ms.get)
-    flux_avg_ms = stage_ms["flux"] / max(runs, 1)
-    flux_bytes = flux_kernel_bytes(wl)
-    achieved = flux_bytes / (flux_avg_ms * 1e-3) / 1e9
+    # roofline of the dominant kernel of this step: its algorithmic bytes per launch over its
+    # CUDA-event duration; DRAM traffic and FP64-pipe utilisation from the committed ncu capture
+    if args.step == "vjp":
+        kname, kstage, kbytes, tkey = "a_flux<3, SST> (adjoint face fluxes)", "a_flux", \
+            aflux_kernel_bytes(wl), "a_flux"
+    else:
+        kname, kstage, kbytes, tkey = "k_flux<Dual, 3, SST> (JVP face fluxes)", "flux", \
+            flux_kernel_bytes(wl), "k_flux_dual"
+    k_avg_ms = stage_ms[kstage] / max(runs, 1)
+    achieved = kbytes / (k_avg_ms * 1e-3) / 1e9
+    traffic, fp64 = None, None
     traffic_path = os.path.join(ROOT, "profiles", "flux_traffic.json")
-    traffic = None
-    if os.path.exists(traffic_path):
+    if os.path.exists(traffic_path) and args.size == 128:
         with open(traffic_path) as f:
-            tr = json.load(f)
-        traffic = tr.get("bytes_per_face", 0.0) * F if tr.get("size") else None
+            tr = json.load(f).get(tkey, {})
+        traffic = tr.get("bytes_128")
+        fp64 = tr.get("fp64_pipe_active_pct")
     bpf = step_bytes_per_face(wl)
     out = {
         "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world,
@@ -301,10 +326,14 @@ def run_gpu(args, rank: int, world: int, local_rank: int) -> dict | None:
         "stage_ms_per_step": {k: round(v / max(runs, 1), 4) for k, v in stage_ms.items()},
         "algorithmic_bytes_per_face": round(bpf, 2),
         "step_achieved_gbs": round(bpf * F / (ms / args.steps * 1e-3) / 1e9, 1),
-        "roofline": {"bound": "hbm", "kernel": "k_flux<Dual>", "dominant_stage": dom,
+        "roofline": {"bound": "hbm", "kernel": kname, "dominant_stage": dom,
                      "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                     "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": traffic,
-                     "peak_source": f"{peaks['source']} (MEASURED_PEAKS.json hbm_gbs)"},
+                     "frac": round(achieved / peaks["hbm_gbs"], 4),
+                     "traffic": round(traffic) if traffic else None,
+                     "algorithmic_bytes": round(kbytes), "kernel_ms": round(k_avg_ms, 4),
+                     "peak_source": f"{peaks['source']} (MEASURED_PEAKS.json hbm_gbs)",
+                     "fp64_pipe_active_pct_ncu": fp64,
+                     "binding_limit": "fp64 pipe (see profiles/flux_kernels_channel3d_64.md)"},
         "clocks": clk.summary(),
     }
     if not args.no_newton:

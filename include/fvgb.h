@@ -201,6 +201,23 @@ int fv_saturation_colouring(int n, const int* indptr, const int* indices, int* c
                             int* n_colours);
 
 /* ------------------------------------------------------------------------------------------
+ * Aggregation multigrid.  Replaces the aggregation hierarchy of aquaflux/solve/multigrid.py
+ * (_build_aggregation_hierarchy :1011, _mis_aggregate :353) as used by the ILU-smoothed V-cycle
+ * of aquaflux/solve/ilu_inverse.py:160-308, with unsmoothed (piecewise-constant) prolongation.
+ * ------------------------------------------------------------------------------------------ */
+/* Aggregate the cells of a symmetric cell graph (host CSR); agg[i] in [0, *n_agg). */
+int fv_aggregate(int n, const int* indptr, const int* indices, int* agg, int* n_agg);
+/* Galerkin coarse blocks: coarse[Q] = sum of the fine blocks glist[gptr[Q] .. gptr[Q+1]) in list
+ * order (device; fine fp64 when fine_f64 != 0, else fp32; coarse fp32; b x b row-major blocks). */
+int fv_galerkin_f32(long n_coarse_blocks, int b, const long* gptr, const long* glist,
+                    const void* fine, int fine_f64, float* coarse, void* stream);
+/* rc[I] = sum of r over the member cells mlist[mptr[I] .. mptr[I+1]) (b values per cell). */
+int fv_restrict_f32(int n_coarse, int b, const int* mptr, const int* mlist, const float* r,
+                    float* rc, void* stream);
+/* x[i] += xc[agg[i]] (b values per cell). */
+int fv_prolong_add_f32(int n_fine, int b, const int* agg, const float* xc, float* x, void* stream);
+
+/* ------------------------------------------------------------------------------------------
  * Deterministic reductions for the Krylov solver (fixed blocking, fixed order: run-to-run
  * bit-identical).  Device arrays; `out` is a device scalar.
  * ------------------------------------------------------------------------------------------ */

@@ -117,3 +117,30 @@ def test_implicit_adjoint_matches_finite_differences_of_the_solve():
     grad = float(adj.dparams[0])
     assert abs(fd) > 1e-3
     assert abs(grad - fd) <= 1e-4 * abs(fd)
+
+
+def test_amg_vcycle_is_a_fixed_linear_operator_and_converges_newton():
+    """The fp32 V-cycle is fixed-linear (tests/unit/test_host_vcycle.py:76) and, as the FGMRES
+    preconditioner, drives the SST channel's Newton solve to the same root as ILU(0)."""
+    from aquaflux_gb300 import workloads
+    from aquaflux_gb300.amg import AmgPreconditioner
+    from aquaflux_gb300.solve import BlockJacobian, newton_solve
+
+    wl = workloads.channel3d(16)
+    case = wl.device_case()
+    jac = BlockJacobian(case)
+    pc = AmgPreconditioner(jac, min_cells=200)
+    assert len(pc.h.levels) >= 2
+    s = torch.tensor(wl.initial_state(), device="cuda")
+    pc.refresh(s)
+    r1 = torch.randn(case.n_unknowns, dtype=torch.float64, device="cuda")
+    r2 = torch.randn_like(r1)
+    a = pc.apply(r1).clone()
+    b = pc.apply(r2).clone()
+    ab = pc.apply(2.0 * r1 - 3.0 * r2).clone()
+    assert float((ab - (2.0 * a - 3.0 * b)).abs().max()) <= 1e-4 * float(ab.abs().max())
+    res_amg = newton_solve(case, wl.initial_state(), kind="amg", max_steps=40)
+    res_ilu = newton_solve(case, wl.initial_state(), precision=64, max_steps=40)
+    assert res_amg.converged and res_ilu.converged
+    sa, si = res_amg.state.cpu().numpy(), res_ilu.state.cpu().numpy()
+    assert np.abs(sa - si).max() <= 1e-7 * np.abs(si).max()
