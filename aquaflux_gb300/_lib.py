@@ -47,6 +47,7 @@ SIGNATURES = {
     "fv_jvp_shift": (c_int, [P, P, P, P, P, P]),
     "fv_jvp_frozen": (c_int, [P, P, P, P, P]),
     "fv_probe_jacobian": (c_int, [P, P, c_int, P, c_int, P, P, P, P]),
+    "fv_assemble_jacobian": (c_int, [P, P, P, P, P, P]),
     "fv_param_jvp": (c_int, [P, P, P, P, P]),
     "fv_vjp": (c_int, [P, P, P, P, P, P]),
     "fv_param_vjp": (c_int, [P, P, P, P, P]),
@@ -60,6 +61,8 @@ SIGNATURES = {
     "fv_ilu0_factor_values": (c_int, [P, P, P]),
     "fv_dot_f64": (c_int, [c_long, P, P, P, P]),
     "fv_saturation_colouring": (c_int, [c_int, P, P, P, P]),
+    "fv_coarsen": (c_int, [c_int, P, P, P, c_int, P, P, P, P, P, P, P]),
+    "fv_cell_pattern": (c_int, [c_int, c_long, P, P, P, P]),
     "fv_aggregate": (c_int, [c_int, P, P, P, P]),
     "fv_galerkin_f32": (c_int, [c_long, c_int, P, P, P, c_int, P, P]),
     "fv_restrict_f32": (c_int, [c_int, c_int, P, P, P, P, P]),

@@ -8,7 +8,9 @@ pattern on the host (``fv_aggregate``), every level's operator is the Galerkin p
 unsmoothed aggregation (formed on the GPU by ordered block sums), and the smoothing, residuals,
 restriction and prolongation all run in fp32 on the device.  The coarsest level is smoothed by
 ILU(0) sweeps instead of the reference's dense inverse (the 2M-cell hierarchy's coarsest level is
-too large for a dense factor).  Vectors inside the hierarchy are cell-major.
+too large for a dense factor).  Coarse aggregates are numbered colour by colour, so that the coarse
+levels' ILU(0) sweeps run in a handful of level sets.  Vectors inside the hierarchy are
+cell-major.
 """
 from __future__ import annotations
 
@@ -39,6 +41,7 @@ class _Level:
         self.x = torch.zeros(n * b, dtype=torch.float32, device="cuda")
         self.r = torch.zeros_like(self.x)
         self.t = torch.zeros_like(self.x)
+        self.rhs = torch.zeros_like(self.x)  # right-hand side when this is a coarse level
         self.coarse = None  # transfer data to the next level
 
     def spmv(self, x, y):
@@ -46,43 +49,77 @@ class _Level:
                                     ptr(self.values), ptr(x), ptr(y), 0, _stream()))
 
 
+def plan_hierarchy(n, indptr, indices, *, min_cells: int = 4000, max_levels: int = 10,
+                   coarse_order: str = "colour") -> list[dict]:
+    """Host plan of the aggregation hierarchy over a cell graph (sorted CSR with self loops).
+
+    One entry per coarsening: ``agg`` (fine cell -> aggregate), ``mptr``/``mlist`` (members of
+    each aggregate), the coarse pattern ``indptr``/``indices`` and, per coarse block, the ordered
+    list of fine blocks summed into it (``gptr``/``glist``).  With ``coarse_order="colour"`` the
+    aggregates are numbered colour by colour (distance-1 colouring of the coarse graph): rows of
+    one colour are independent, so the coarse ILU(0) sweeps need as many level sets as there are
+    colours instead of hundreds.
+    """
+    ip = np.ascontiguousarray(indptr, dtype=np.int32)
+    ix = np.ascontiguousarray(indices, dtype=np.int32)
+    plan = []
+    while n > min_cells and len(plan) + 1 < max_levels:
+        agg = np.empty(n, dtype=np.int32)
+        na = ctypes.c_int(0)
+        check(lib().fv_aggregate(n, ptr(ip), ptr(ix), ptr(agg), ctypes.byref(na)))
+        na = int(na.value)
+        if na >= n * 0.9:  # aggregation stalled
+            break
+        if coarse_order == "colour":
+            step = _coarsen(n, ip, ix, agg, na, lists=False)
+            col = np.empty(na, dtype=np.int32)
+            nco = ctypes.c_int(0)
+            check(lib().fv_saturation_colouring(na, ptr(step["indptr"]), ptr(step["indices"]),
+                                                ptr(col), ctypes.byref(nco)))
+            order = np.argsort(col, kind="stable")
+            newid = np.empty(na, dtype=np.int32)
+            newid[order] = np.arange(na, dtype=np.int32)
+            agg = newid[agg]
+        step = _coarsen(n, ip, ix, agg, na)
+        plan.append(step)
+        cip, cix = step["indptr"], step["indices"]
+        n, ip, ix = na, cip, cix
+    return plan
+
+
+def _coarsen(n, ip, ix, agg, na, lists: bool = True) -> dict:
+    """One coarsening step (``fv_coarsen``): members, coarse pattern, ordered fine-block lists."""
+    nnz = int(ip[-1])
+    mptr = np.empty(na + 1, dtype=np.int32)
+    mlist = np.empty(n, dtype=np.int32)
+    cip = np.empty(na + 1, dtype=np.int32)
+    cix = np.empty(nnz, dtype=np.int32)
+    gptr = np.empty(nnz + 1, dtype=np.int64) if lists else None
+    glist = np.empty(nnz, dtype=np.int64) if lists else None
+    ncb = ctypes.c_long(0)
+    agg = np.ascontiguousarray(agg, dtype=np.int32)
+    check(lib().fv_coarsen(n, ptr(ip), ptr(ix), ptr(agg), na, ptr(mptr), ptr(mlist), ptr(cip),
+                           ptr(cix), ptr(gptr), ptr(glist), ctypes.byref(ncb)))
+    ncb = int(ncb.value)
+    return {"n_coarse": na, "agg": agg, "mptr": mptr, "mlist": mlist, "indptr": cip,
+            "indices": cix[:ncb].copy(), "gptr": gptr[:ncb + 1].copy() if lists else None,
+            "glist": glist}
+
+
 class AmgHierarchy:
     """Aggregation hierarchy on a fixed block pattern; ``refresh(values)`` re-forms every level."""
 
     def __init__(self, n, b, indptr, indices, *, min_cells: int = 4000, max_levels: int = 10,
-                 sweeps: int = 1, coarse_sweeps: int = 4):
+                 sweeps: int = 1, coarse_sweeps: int = 4, coarse_order: str = "colour"):
         self.b, self.sweeps, self.coarse_sweeps = b, sweeps, coarse_sweeps
         self.levels = [_Level(n, b, indptr, indices)]
-        while self.levels[-1].n > min_cells and len(self.levels) < max_levels:
+        for step in plan_hierarchy(n, indptr, indices, min_cells=min_cells,
+                                   max_levels=max_levels, coarse_order=coarse_order):
             fine = self.levels[-1]
-            agg = np.empty(fine.n, dtype=np.int32)
-            na = ctypes.c_int(0)
-            check(lib().fv_aggregate(fine.n, ptr(fine.indptr), ptr(fine.indices), ptr(agg),
-                                     ctypes.byref(na)))
-            na = int(na.value)
-            if na >= fine.n * 0.9:  # aggregation stalled
-                break
-            members = np.argsort(agg, kind="stable").astype(np.int32)
-            mptr = np.zeros(na + 1, dtype=np.int32)
-            np.cumsum(np.bincount(agg, minlength=na), out=mptr[1:])
-            rows = np.repeat(np.arange(fine.n, dtype=np.int64), np.diff(fine.indptr))
-            key = agg[rows].astype(np.int64) * na + agg[fine.indices]
-            ukey, qmap = np.unique(key, return_inverse=True)
-            cip = np.zeros(na + 1, dtype=np.int64)
-            np.cumsum(np.bincount((ukey // na).astype(np.int64), minlength=na), out=cip[1:])
-            cix = (ukey % na).astype(np.int32)
-            glist = np.argsort(qmap, kind="stable").astype(np.int64)
-            gptr = np.zeros(ukey.size + 1, dtype=np.int64)
-            np.cumsum(np.bincount(qmap, minlength=ukey.size), out=gptr[1:])
-            fine.coarse = {
-                "agg": torch.tensor(agg, device="cuda"),
-                "mptr": torch.tensor(mptr, device="cuda"),
-                "mlist": torch.tensor(members, device="cuda"),
-                "gptr": torch.tensor(gptr, device="cuda"),
-                "glist": torch.tensor(glist, device="cuda"),
-                "n_coarse_blocks": int(ukey.size),
-            }
-            self.levels.append(_Level(na, b, cip.astype(np.int32), cix))
+            fine.coarse = {k: torch.tensor(step[k], device="cuda")
+                           for k in ("agg", "mptr", "mlist", "gptr", "glist")}
+            fine.coarse["n_coarse_blocks"] = int(step["gptr"].size - 1)
+            self.levels.append(_Level(step["n_coarse"], b, step["indptr"], step["indices"]))
 
     @property
     def sizes(self):
@@ -121,7 +158,7 @@ class AmgHierarchy:
         torch.sub(b_vec, lv.t, out=lv.r)
         coarse = self.levels[level + 1]
         t = lv.coarse
-        bc = torch.empty(coarse.n * self.b, dtype=torch.float32, device="cuda")
+        bc = coarse.rhs
         check(lib().fv_restrict_f32(coarse.n, self.b, ptr(t["mptr"]), ptr(t["mlist"]), ptr(lv.r),
                                     ptr(bc), _stream()))
         xc = self.vcycle(level + 1, bc)

@@ -51,6 +51,17 @@ def stencil_pattern(owner, nb, n: int, reach: int) -> sp.csr_matrix:
     return pat
 
 
+def cell_pattern(owner, nb, n: int) -> tuple[np.ndarray, np.ndarray]:
+    """The reach-1 pattern (``stencil_pattern(.., 1)``) as sorted int32 CSR arrays, built by
+    ``fv_cell_pattern``."""
+    owner = np.ascontiguousarray(owner, dtype=np.int32)
+    nb = np.ascontiguousarray(nb, dtype=np.int32)
+    indptr = np.empty(n + 1, dtype=np.int32)
+    indices = np.empty(n + 2 * owner.size, dtype=np.int32)
+    check(lib().fv_cell_pattern(n, owner.size, ptr(owner), ptr(nb), ptr(indptr), ptr(indices)))
+    return indptr, indices[:int(indptr[-1])].copy()
+
+
 def saturation_colouring(conflict: sp.csr_matrix) -> np.ndarray:
     n = conflict.shape[0]
     ip = np.ascontiguousarray(conflict.indptr, dtype=np.int32)

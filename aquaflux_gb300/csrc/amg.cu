@@ -8,6 +8,7 @@
 // and the coarse operator is the Galerkin product P^T A P.  Here P is the unsmoothed (piecewise
 // constant) tentative prolongation, so P^T A P is an aggregate-to-aggregate sum of fine blocks: the
 // GPU forms each coarse block as the ordered sum of its fine blocks (deterministic, no atomics).
+#include <algorithm>
 #include <vector>
 
 #include "internal.cuh"
@@ -60,6 +61,78 @@ extern "C" int fv_aggregate(int n, const int* indptr, const int* indices, int* a
     ++na;
   }
   *n_agg = na;
+  return FV_OK;
+}
+
+// One coarsening step of a block pattern by an aggregation (host): members of every aggregate
+// (ascending fine index), the sorted coarse pattern, and for every coarse block the fine blocks
+// that sum into it (ascending fine block index), i.e. the Galerkin product of the piecewise-
+// constant prolongation expressed as ordered block lists.
+extern "C" int fv_coarsen(int n, const int* indptr, const int* indices, const int* agg, int na,
+                          int* mptr, int* mlist, int* cip, int* cix, long* gptr, long* glist,
+                          long* n_coarse_blocks) {
+  if (n <= 0 || na <= 0 || !indptr || !indices || !agg || !mptr || !mlist || !cip || !cix ||
+      !n_coarse_blocks || (!gptr) != (!glist)) {
+    fv_set_error("fv_coarsen: bad arguments");
+    return FV_ERR_ARG;
+  }
+  const long nnz = indptr[n];
+  for (int i = 0; i < n; ++i)
+    if (agg[i] < 0 || agg[i] >= na) {
+      fv_set_error("fv_coarsen: aggregate index out of range at cell %d", i);
+      return FV_ERR_ARG;
+    }
+  for (long q = 0; q < nnz; ++q)
+    if (indices[q] < 0 || indices[q] >= n) {
+      fv_set_error("fv_coarsen: column index out of range");
+      return FV_ERR_ARG;
+    }
+  // members (counting sort, stable)
+  std::vector<int> cnt(na + 1, 0);
+  for (int i = 0; i < n; ++i) ++cnt[agg[i] + 1];
+  for (int a = 0; a < na; ++a) cnt[a + 1] += cnt[a];
+  for (int a = 0; a <= na; ++a) mptr[a] = cnt[a];
+  for (int i = 0; i < n; ++i) mlist[cnt[agg[i]]++] = i;
+  // coarse rows: sorted unique aggregate columns (a marker per aggregate column avoids sorting the
+  // duplicates); qmap: fine block -> coarse block
+  const bool lists = gptr != nullptr;  // NULL gptr / glist: the coarse pattern only
+  std::vector<long> qmap(lists ? nnz : 0);
+  std::vector<int> cols, mark(na, -1), slot(na, 0);
+  long pos = 0;
+  cip[0] = 0;
+  for (int a = 0; a < na; ++a) {
+    cols.clear();
+    for (int m = mptr[a]; m < mptr[a + 1]; ++m) {
+      const int i = mlist[m];
+      for (int q = indptr[i]; q < indptr[i + 1]; ++q) {
+        const int col = agg[indices[q]];
+        if (mark[col] != a) {
+          mark[col] = a;
+          cols.push_back(col);
+        }
+      }
+    }
+    std::sort(cols.begin(), cols.end());
+    for (size_t k = 0; k < cols.size(); ++k) {
+      cix[pos + (long)k] = cols[k];
+      slot[cols[k]] = (int)k;
+    }
+    if (lists)
+      for (int m = mptr[a]; m < mptr[a + 1]; ++m) {
+        const int i = mlist[m];
+        for (int q = indptr[i]; q < indptr[i + 1]; ++q) qmap[q] = pos + slot[agg[indices[q]]];
+      }
+    pos += (long)cols.size();
+    cip[a + 1] = (int)pos;
+  }
+  *n_coarse_blocks = pos;
+  if (!lists) return FV_OK;
+  // ordered fine-block lists (counting sort of qmap, stable)
+  for (long b = 0; b <= pos; ++b) gptr[b] = 0;
+  for (long q = 0; q < nnz; ++q) ++gptr[qmap[q] + 1];
+  for (long b = 0; b < pos; ++b) gptr[b + 1] += gptr[b];
+  std::vector<long> fill(gptr, gptr + pos);
+  for (long q = 0; q < nnz; ++q) glist[fill[qmap[q]]++] = q;
   return FV_OK;
 }
 

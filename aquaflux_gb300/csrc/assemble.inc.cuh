@@ -1,0 +1,155 @@
+// Direct assembly of the frozen (reach-1) block Jacobian J_direct, the operator that
+// materialize_block_jacobian (aquaflux/solve/sparse_jacobian.py:722-847) recovers by coloured JVP
+// probes of the frozen JVP.  Included by residual.cu (shares its device helpers).
+//
+// With the gradients, the SST closure fields and a_P held at their values for `state`, a face's
+// fluxes depend on its owner's and neighbour's unknowns only and a cell's SST sources on its own k
+// and omega only, so the Jacobian needs no colouring:
+//   k_jac_face  face  forward-mode derivative of every flux of the face with respect to each of the
+//                     2 x NF unknowns of its two cells (the flux code of the residual, evaluated with
+//                     one seeded tangent per unknown), into D (2, NF, NF, nf);
+//   k_jac_cell  (cell, row field)  one row of every block of the cell's block row: the face
+//                     derivatives summed in the cell's face order with the residual's signs, then
+//                     the SST source rows, the omega wall-cell rows and the pressure-pin row.
+// Every entry is the tangent the coloured probe computes for it, by the same arithmetic in the
+// same order.
+
+// The state with a unit tangent on one unknown (index `seed` of the field-major state).
+struct SeedSrc {
+  const double* v;
+  long seed;
+  __device__ __forceinline__ Dual operator()(long i) const { return {v[i], i == seed ? 1.0 : 0.0}; }
+};
+
+// Keeps the tangent of flux q as D[((side * NF + q) * NF + r) * nf + f].
+struct DerivStore {
+  double* D;
+  long base;  // ((side * NF) * NF + r) * nf + f
+  long qstride;  // NF * nf
+  __device__ __forceinline__ void operator()(int q, const Dual& x) const {
+    D[base + q * qstride] = x.d;
+  }
+};
+
+template <int DIM, bool TURB>
+__global__ void __launch_bounds__(128) k_jac_face(MeshView m, CaseView cv, const double* state,
+                                                  Par<Dual> par, const Dual* G, const Dual* cl,
+                                                  const Dual* dco, double* D) {
+  constexpr int NF = Layout<DIM, TURB>::NFLD;
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= m.nf) return;
+  const int nc = m.nc, nf = m.nf;
+  const int nside = f < m.nfi ? 2 : 1;
+  for (int side = 0; side < nside; ++side) {
+    const int cell = side ? m.nb[f] : m.owner[f];
+#pragma unroll 1
+    for (int r = 0; r < NF; ++r) {
+      const SeedSrc st{state, (long)r * nc + cell};
+      const DerivStore wr{D, ((long)(side * NF) * NF + r) * nf + f, (long)NF * nf};
+      flux_face<Dual, DIM, TURB>(m, cv, st, par, G, cl, dco, (const Dual*)nullptr, true, f, wr,
+                                 nullptr);
+    }
+  }
+}
+
+template <int DIM, bool TURB>
+__global__ void __launch_bounds__(128) k_jac_cell(MeshView m, CaseView cv, const double* state,
+                                                  Par<Dual> par, const Dual* G, const Dual* cl,
+                                                  const Dual* Gwi, const double* D,
+                                                  const int* indptr, const int* indices,
+                                                  double* values) {
+  using L = Layout<DIM, TURB>;
+  constexpr int NF = L::NFLD;
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long)NF * m.nc) return;
+  const int nc = m.nc, nf = m.nf;
+  const int c = (int)(t % nc), q = (int)(t / nc);
+  const int bp = indptr[c], be = indptr[c + 1];
+  for (int p = bp; p < be; ++p)
+#pragma unroll
+    for (int r = 0; r < NF; ++r) values[((long)p * NF + q) * NF + r] = 0.0;
+  const bool pinned = c == cv.pin && q == L::P;
+  bool wall_omega = false;
+  if constexpr (TURB) wall_omega = q == L::W && cv.wcell[c] != 0;
+  double dg[NF];
+#pragma unroll
+  for (int r = 0; r < NF; ++r) dg[r] = 0.0;
+  const long rstride = nf;
+  if (!pinned && !wall_omega) {
+    const int b = m.cf_ptr[c], e = m.cf_ptr[c + 1];
+    for (int i = b; i < e; ++i) {
+      const unsigned ent = m.cf_face[i];
+      const int f = (int)(ent & ~FV_NB_BIT);
+      const bool isnb = (ent & FV_NB_BIT) != 0;
+      const double sg = isnb ? -1.0 : 1.0;
+      const long self = ((long)((isnb ? NF : 0) + q) * NF) * nf + f;
+#pragma unroll
+      for (int r = 0; r < NF; ++r) {
+        const double x = sg * D[self + r * rstride];
+        dg[r] = i == b ? x : dg[r] + x;
+      }
+      if (f < m.nfi) {
+        const int j = isnb ? m.owner[f] : m.nb[f];
+        int slot = -1;
+        for (int p = bp; p < be; ++p)
+          if (indices[p] == j) {
+            slot = p;
+            break;
+          }
+        if (slot >= 0) {
+          const long oth = ((long)((isnb ? 0 : NF) + q) * NF) * nf + f;
+          double* row = values + ((long)slot * NF + q) * NF;
+#pragma unroll
+          for (int r = 0; r < NF; ++r) row[r] += sg * D[oth + r * rstride];
+        }
+      }
+    }
+  }
+  if (pinned) {
+#pragma unroll
+    for (int r = 0; r < NF; ++r) dg[r] = r == L::P ? 1.0 : 0.0;
+  }
+  if constexpr (TURB) {
+    if (q == L::K || q == L::W) {
+      // only k and omega of the cell itself enter its source rows
+#pragma unroll
+      for (int r = L::K; r <= L::W; ++r) {
+        const SeedSrc st{state, (long)r * nc + c};
+        Dual rk{0.0, q == L::K ? dg[r] : 0.0}, rw{0.0, q == L::W ? dg[r] : 0.0};
+        sst_rows<Dual, DIM>(m, cv, st, par, cl, G, Gwi, c, rk, rw);
+        dg[r] = q == L::K ? rk.d : rw.d;
+      }
+    }
+  }
+  for (int p = bp; p < be; ++p)
+    if (indices[p] == c) {
+      double* row = values + ((long)p * NF + q) * NF;
+#pragma unroll
+      for (int r = 0; r < NF; ++r) row[r] = dg[r];
+      break;
+    }
+}
+
+template <int DIM, bool TURB>
+int assemble_frozen(FvCase* cs, const double* state, const int* indptr, const int* indices,
+                    double* values, double* D, cudaStream_t s) {
+  const MeshView& m = cs->mesh->view;
+  const CaseView& cv = cs->view;
+  const long nc = m.nc, nf = m.nf;
+  constexpr int NF = Layout<DIM, TURB>::NFLD;
+  Work<Dual> w = work_layout<Dual, DIM, TURB>(cs->work, nc, nf);
+  Src<Dual> st{state, nullptr};  // zero tangent: the forward stages give the frozen values
+  const double irho = 1.0 / cs->desc.rho;
+  Par<Dual> par{{cs->mu, 0.0}, {cs->inlet_scale, 0.0}, {cs->mu * irho, 0.0}};
+  constexpr int TB = 128;
+  const int bc = fv_blocks(nc, TB), bf = fv_blocks(nf, TB);
+  k_grad<Dual, DIM, TURB><<<bc, TB, 0, s>>>(m, cv, st, par, w.G);
+  if (TURB) k_closure<Dual, DIM><<<bc, TB, 0, s>>>(m, cv, st, par, w.G, w.cl, w.Gwi);
+  k_apcoef<Dual, DIM, TURB><<<bf, TB, 0, s>>>(m, cv, st, par, w.G, w.cl, w.acown, w.acnb, w.me);
+  k_dcoeff<Dual><<<bc, TB, 0, s>>>(m, w.acown, w.acnb, w.dco);
+  k_jac_face<DIM, TURB><<<bf, TB, 0, s>>>(m, cv, state, par, w.G, w.cl, w.dco, D);
+  k_jac_cell<DIM, TURB><<<fv_blocks((long)NF * nc, TB), TB, 0, s>>>(
+      m, cv, state, par, w.G, w.cl, w.Gwi, D, indptr, indices, values);
+  FV_CUDA_TRY(cudaGetLastError());
+  return FV_OK;
+}

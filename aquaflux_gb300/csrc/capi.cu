@@ -174,6 +174,7 @@ extern "C" int fv_case_destroy(FvCase* c) {
   cudaFree(c->adj);
   cudaFree(c->aux);
   cudaFree(c->dscalar);
+  cudaFree(c->jac_face);
   for (cudaEvent_t e : c->prof_events) cudaEventDestroy(e);
   delete c;
   return FV_OK;
@@ -278,6 +279,20 @@ extern "C" int fv_probe_jacobian(FvCase* c, const double* state, int frozen, con
   }
   FV_CUDA_TRY(cudaGetLastError());
   return FV_OK;
+}
+
+extern "C" int fv_assemble_jacobian(FvCase* c, const double* state, const int* indptr,
+                                    const int* indices, double* values, void* stream) {
+  if (!c || !state || !indptr || !indices || !values) {
+    fv_set_error("fv_assemble_jacobian: bad arguments");
+    return FV_ERR_ARG;
+  }
+  if (!c->jac_face) {
+    FV_CUDA_TRY(cudaMalloc(&c->jac_face,
+                           fv_jac_face_bytes(c->mesh->dim, c->desc.turbulent, c->mesh->nf)));
+  }
+  return fv_case_assemble_frozen(c, state, indptr, indices, values, c->jac_face,
+                                 (cudaStream_t)stream);
 }
 
 extern "C" int fv_jvp_shift(FvCase* c, const double* state, const double* v, const double* shift,

@@ -10,6 +10,7 @@
 //     taken by a coloured neighbour, then, for every still-uncoloured neighbour (in CSR order)
 //     seeing that colour for the first time, moves it to the head of its new (higher) bucket.
 // Runs in O(n + m) with a bitset of taken colours per vertex.
+#include <algorithm>
 #include <cstdint>
 #include <vector>
 
@@ -98,5 +99,48 @@ extern "C" int fv_saturation_colouring(int n, const int* indptr, const int* indi
     }
   }
   if (n_colours) *n_colours = ncol;
+  return FV_OK;
+}
+
+// Reach-1 cell pattern (host): row i holds i and the cells sharing a face with i, sorted and
+// unique.  Interior faces given as (owner, neighbour) pairs.  indptr (n + 1); indices receives
+// at most n + 2 * n_pairs entries.
+extern "C" int fv_cell_pattern(int n, long n_pairs, const int* owner, const int* neighbour,
+                               int* indptr, int* indices) {
+  if (n <= 0 || n_pairs < 0 || (n_pairs > 0 && (!owner || !neighbour)) || !indptr || !indices) {
+    fv_set_error("fv_cell_pattern: bad arguments");
+    return FV_ERR_ARG;
+  }
+  std::vector<long> cnt(n + 1, 0);
+  for (long f = 0; f < n_pairs; ++f) {
+    const int a = owner[f], b = neighbour[f];
+    if (a < 0 || a >= n || b < 0 || b >= n) {
+      fv_set_error("fv_cell_pattern: cell index out of range at pair %ld", f);
+      return FV_ERR_ARG;
+    }
+    ++cnt[a + 1];
+    ++cnt[b + 1];
+  }
+  for (int i = 0; i < n; ++i) cnt[i + 1] += cnt[i] + 1;  // + the diagonal
+  std::vector<int> tmp(cnt[n]);
+  std::vector<long> fill(cnt.begin(), cnt.end() - 1);
+  for (int i = 0; i < n; ++i) tmp[fill[i]++] = i;
+  for (long f = 0; f < n_pairs; ++f) {
+    tmp[fill[owner[f]]++] = neighbour[f];
+    tmp[fill[neighbour[f]]++] = owner[f];
+  }
+  long pos = 0;
+  indptr[0] = 0;
+  for (int i = 0; i < n; ++i) {
+    auto b = tmp.begin() + cnt[i], e = tmp.begin() + cnt[i + 1];
+    std::sort(b, e);
+    e = std::unique(b, e);
+    for (auto it = b; it != e; ++it) indices[pos++] = *it;
+    if (pos > 0x7fffffffL) {
+      fv_set_error("fv_cell_pattern: pattern exceeds int32 entries");
+      return FV_ERR_ARG;
+    }
+    indptr[i + 1] = (int)pos;
+  }
   return FV_OK;
 }

@@ -113,6 +113,7 @@ struct FvCase {
   double* adj = nullptr;    // adjoint workspace
   double* aux = nullptr;    // face intermediates of the double forward pass (for the adjoint)
   double* dscalar = nullptr; // (4) device scalars
+  double* jac_face = nullptr; // (2, nfld, nfld, nf) face flux derivatives of the Jacobian assembly
   CaseView view;
   // optional per-stage CUDA-event profiling (fv_case_profile_begin / _end)
   std::vector<cudaEvent_t> prof_events;  // max_runs * (FV_MAX_STAGES + 1)
@@ -130,6 +131,11 @@ int fv_case_run(FvCase* c, const double* state, const double* tangent, int tange
                 double* residual, double* jv, cudaStream_t s);
 int fv_case_vjp_run(FvCase* c, const double* state, const double* w, double* residual, double* out,
                     cudaStream_t s);
+// Frozen reach-1 Jacobian by per-face forward-mode derivatives (residual.cu); D holds
+// fv_jac_face_bytes.
+int fv_case_assemble_frozen(FvCase* c, const double* state, const int* indptr, const int* indices,
+                            double* values, double* D, cudaStream_t s);
+size_t fv_jac_face_bytes(int dim, int turb, long nf);
 enum { FV_TAN_NONE = 0, FV_TAN_STATE = 1, FV_TAN_MU = 2, FV_TAN_INLET = 3, FV_TAN_FROZEN = 4 };
 
 // Wall distance + gradient for a turbulent case (mesh.cu).

@@ -337,8 +337,8 @@ __device__ __forceinline__ T mu_eff(const Par<T>& par, double rho, const T* cl, 
 
 // lagged advective momentum flux (rho u)_f . n with the skew-corrected face value
 // (aquaflux/flow/rhie_chow.py:220-271): rho (sum_j n_j u_j,f + sum_jq n_j skew_q (grad u)_jq,f)
-template <class T, int DIM, bool TURB>
-__device__ __forceinline__ T mom_normal(const MeshView& m, const Src<T>& st, const T* G, double rho,
+template <class T, int DIM, bool TURB, class S>
+__device__ __forceinline__ T mom_normal(const MeshView& m, const S& st, const T* G, double rho,
                                         int f, int o, int n, double g) {
   const int nc = m.nc, nf = m.nf;
   T mn = cst(0.0, st(o));
@@ -424,14 +424,15 @@ struct Aux {
   static constexpr int CPN = 6, S0 = 6 + DIM;
 };
 
-template <class T, int DIM, bool TURB>
-__global__ void __launch_bounds__(128) k_flux(MeshView m, CaseView cv, Src<T> st, Par<T> par,
-                                              const T* G, const T* cl, const T* dco, const T* me,
-                                              bool recompute_me, T* FL, double* aux) {
+// The fluxes of face f, handed to wr(q, flux_q) for every field q.  `st` reads the state (Src, or
+// a seeded accessor in the Jacobian assembly); aux (double only) receives the face intermediates.
+template <class T, int DIM, bool TURB, class S, class Wr>
+__device__ __forceinline__ void flux_face(const MeshView& m, const CaseView& cv, const S& st,
+                                          const Par<T>& par, const T* G, const T* cl, const T* dco,
+                                          const T* me, bool recompute_me, int f, const Wr& wr,
+                                          double* aux) {
   constexpr bool KEEP = std::is_same<T, double>::value;
   using L = Layout<DIM, TURB>;
-  const int f = blockIdx.x * blockDim.x + threadIdx.x;
-  if (f >= m.nf) return;
   const int nc = m.nc, nf = m.nf;
   const int o = m.owner[f];
   const double A = m.area[f], rho = cv.rho, irho = 1.0 / cv.rho;
@@ -485,12 +486,12 @@ __global__ void __launch_bounds__(128) k_flux(MeshView m, CaseView cv, Src<T> st
 #pragma unroll
       for (int j = 0; j < DIM; ++j)
         cpn += G[((long)i * DIM + j) * nc + n] * tN[j] - G[((long)i * DIM + j) * nc + o] * tP[j];
-      FL[(long)i * nf + f] = (pA * nrm[i] - cmo * cpn) + mdot * (out ? uo : un);
+      wr(i, (pA * nrm[i] - cmo * cpn) + mdot * (out ? uo : un));
       if constexpr (KEEP) {
         if (aux) aux[(long)(AX::CPN + i) * nf + f] = cpn;
       }
     }
-    FL[(long)L::P * nf + f] = mdot;
+    wr(L::P, mdot);
     if (TURB) {
       const T vflux = mdot * irho;
       const bool vout = val(vflux) >= 0.0;
@@ -505,7 +506,7 @@ __global__ void __launch_bounds__(128) k_flux(MeshView m, CaseView cv, Src<T> st
           cpn += G[((long)q * DIM + j) * nc + n] * tN[j] - G[((long)q * DIM + j) * nc + o] * tP[j];
         const T idn = 1.0 / (m.dpn[f] * gn - go * m.dnn[f]);
         const T cs_ = go * gn * A * idn;
-        FL[(long)q * nf + f] = vflux * (vout ? phio : phin) - cs_ * cpn;
+        wr(q, vflux * (vout ? phio : phin) - cs_ * cpn);
         if constexpr (KEEP) {
           if (aux) {
             const long b0 = AX::S0 + 4 * s;
@@ -560,9 +561,9 @@ __global__ void __launch_bounds__(128) k_flux(MeshView m, CaseView cv, Src<T> st
       T cp = G[((long)i * DIM) * nc + o] * tP[0];
 #pragma unroll
       for (int j = 1; j < DIM; ++j) cp += G[((long)i * DIM + j) * nc + o] * tP[j];
-      FL[(long)i * nf + f] = (pA * nrm[i] - gA * (bu[i] - uo[i] - cp)) + mdot * (out ? uo[i] : bu[i]);
+      wr(i, (pA * nrm[i] - gA * (bu[i] - uo[i] - cp)) + mdot * (out ? uo[i] : bu[i]));
     }
-    FL[(long)L::P * nf + f] = mdot;
+    wr(L::P, mdot);
     if (TURB) {
       const T vflux = mdot * irho;
       const bool vout = val(vflux) >= 0.0;
@@ -578,13 +579,70 @@ __global__ void __launch_bounds__(128) k_flux(MeshView m, CaseView cv, Src<T> st
                               : bscalar(cv.wkind[f], cv.wval[f], phio, cp);
         T gface = go;
         if (s == 0 && cv.swall[f]) gface = (1.0 - wall_weight(par.nu, cv.wd[o], phio)) * go;
-        FL[(long)q * nf + f] = vflux * (vout ? phio : bphi) - gface * (A * m.inv_dpn[f]) * (bphi - phio - cp);
+        wr(q, vflux * (vout ? phio : bphi) - gface * (A * m.inv_dpn[f]) * (bphi - phio - cp));
       }
     }
   }
 }
 
+template <class T>
+struct FluxStore {
+  T* FL;
+  int nf, f;
+  __device__ __forceinline__ void operator()(int q, const T& x) const { FL[(long)q * nf + f] = x; }
+};
+
+template <class T, int DIM, bool TURB>
+__global__ void __launch_bounds__(128) k_flux(MeshView m, CaseView cv, Src<T> st, Par<T> par,
+                                              const T* G, const T* cl, const T* dco, const T* me,
+                                              bool recompute_me, T* FL, double* aux) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= m.nf) return;
+  flux_face<T, DIM, TURB>(m, cv, st, par, G, cl, dco, me, recompute_me, f,
+                          FluxStore<T>{FL, m.nf, f}, aux);
+}
+
 // ---------------------------------------------------------------- k_sum
+// SST rows of cell c: k and omega source terms added to the face sums rk / rw, and the omega
+// wall-cell fixation (aquaflux/turbulence/sources.py:60-412, fixed_value.py:124-158).
+template <class T, int DIM, class Acc>
+__device__ __forceinline__ void sst_rows(const MeshView& m, const CaseView& cv, const Acc& st,
+                                         const Par<T>& par, const T* cl, const T* G, const T* Gwi,
+                                         int c, T& rk, T& rw) {
+  using L = Layout<DIM, true>;
+  const int nc = m.nc;
+  const double V = m.vol[c];
+  const T k = st((long)L::K * nc + c), w = st((long)L::W * nc + c);
+  const T S = cl[c], F1 = cl[(long)nc + c], nut = cl[2L * nc + c];
+  const T nu = par.nu;
+  const double d = cv.wd[c];
+  const bool wall = cv.wcell[c] != 0;
+  const T kp = pos(k);
+  const T limit = (PROD_RATIO * BETA_STAR) * kp * w;
+  T lim = fv_min(nut * (S * S), limit);
+  T weff = w;
+  if (wall) {
+    const T lw = wall_weight(nu, d, k);
+    const T pw = (nu + nut_wall(nu, d, k)) * cl[3L * nc + c] * log_shear(d, k);
+    lim = (1.0 - lw) * lim + lw * pw;
+    weff = omega_wall(nu, d, k);
+  }
+  rk = rk - lim * V;
+  rk = rk + BETA_STAR * V * k * weff;
+  if (wall) {
+    rw = w - omega_wall(nu, d, k);
+  } else {
+    const T alpha = ALPHA_2 + F1 * (ALPHA_1 - ALPHA_2);
+    const T cap = limit / fv_max(nut, cst(NUT_FLOOR, nut));
+    const T beta = BETA_2 + F1 * (BETA_1 - BETA_2);
+    T dkw = G[((long)L::K * DIM) * nc + c] * Gwi[c];
+#pragma unroll
+    for (int j = 1; j < DIM; ++j) dkw += G[((long)L::K * DIM + j) * nc + c] * Gwi[(long)j * nc + c];
+    const T cross = (2.0 * SIGMA_W2) * (1.0 - F1) * dkw / w;
+    rw = rw + V * (beta * (w * w) - alpha * fv_min(S * S, cap) - cross);
+  }
+}
+
 template <class T, int DIM, bool TURB>
 __global__ void __launch_bounds__(128) k_sum(MeshView m, CaseView cv, Src<T> st, Par<T> par, const T* FL, const T* cl,
                                              const T* G, const T* Gwi, double* R, double* JV) {
@@ -607,38 +665,7 @@ __global__ void __launch_bounds__(128) k_sum(MeshView m, CaseView cv, Src<T> st,
     }
   }
   if (c == cv.pin) r[L::P] = st((long)L::P * nc + c) - cv.pin_value;
-  if (TURB) {
-    const double V = m.vol[c];
-    const T k = st((long)L::K * nc + c), w = st((long)L::W * nc + c);
-    const T S = cl[c], F1 = cl[(long)nc + c], nut = cl[2L * nc + c];
-    const T nu = par.nu;
-    const double d = cv.wd[c];
-    const bool wall = cv.wcell[c] != 0;
-    const T kp = pos(k);
-    const T limit = (PROD_RATIO * BETA_STAR) * kp * w;
-    T lim = fv_min(nut * (S * S), limit);
-    T weff = w;
-    if (wall) {
-      const T lw = wall_weight(nu, d, k);
-      const T pw = (nu + nut_wall(nu, d, k)) * cl[3L * nc + c] * log_shear(d, k);
-      lim = (1.0 - lw) * lim + lw * pw;
-      weff = omega_wall(nu, d, k);
-    }
-    r[L::K] = r[L::K] - lim * V;
-    r[L::K] = r[L::K] + BETA_STAR * V * k * weff;
-    if (wall) {
-      r[L::W] = w - omega_wall(nu, d, k);
-    } else {
-      const T alpha = ALPHA_2 + F1 * (ALPHA_1 - ALPHA_2);
-      const T cap = limit / fv_max(nut, cst(NUT_FLOOR, nut));
-      const T beta = BETA_2 + F1 * (BETA_1 - BETA_2);
-      T dkw = G[((long)L::K * DIM) * nc + c] * Gwi[c];
-#pragma unroll
-      for (int j = 1; j < DIM; ++j) dkw += G[((long)L::K * DIM + j) * nc + c] * Gwi[(long)j * nc + c];
-      const T cross = (2.0 * SIGMA_W2) * (1.0 - F1) * dkw / w;
-      r[L::W] = r[L::W] + V * (beta * (w * w) - alpha * fv_min(S * S, cap) - cross);
-    }
-  }
+  if constexpr (TURB) sst_rows<T, DIM>(m, cv, st, par, cl, G, Gwi, c, r[L::K], r[L::W]);
 #pragma unroll
   for (int q = 0; q < NF; ++q) put<T>(R, JV, (long)q * nc + c, r[q]);
 }
@@ -700,6 +727,7 @@ int dispatch_t(FvCase* cs, const double* state, const double* tangent, int kind,
 }
 
 #include "adjoint.inc.cuh"
+#include "assemble.inc.cuh"
 
 template <int DIM, bool TURB>
 int run_vjp(FvCase* cs, const double* state, const double* W, double* R, double* out,
@@ -770,6 +798,22 @@ size_t fv_residual_work_bytes(int dim, int turb, long nc, long nf) {
   long nfld = dim + 1 + (turb ? 2 : 0);
   long n = nfld * dim * nc + 7 * nc + dim * nc + 3 * nf + nc + nfld * nf;
   return (size_t)n * sizeof(Dual);
+}
+
+size_t fv_jac_face_bytes(int dim, int turb, long nf) {
+  long nfld = dim + 1 + (turb ? 2 : 0);
+  return sizeof(double) * (size_t)(2 * nfld * nfld) * nf;
+}
+
+int fv_case_assemble_frozen(FvCase* cs, const double* state, const int* indptr,
+                            const int* indices, double* values, double* D, cudaStream_t s) {
+  const int dim = cs->mesh->dim;
+  const bool turb = cs->desc.turbulent != 0;
+  if (dim == 2)
+    return turb ? assemble_frozen<2, true>(cs, state, indptr, indices, values, D, s)
+                : assemble_frozen<2, false>(cs, state, indptr, indices, values, D, s);
+  return turb ? assemble_frozen<3, true>(cs, state, indptr, indices, values, D, s)
+              : assemble_frozen<3, false>(cs, state, indptr, indices, values, D, s);
 }
 
 int fv_residual_init_constants() {

@@ -27,7 +27,7 @@ import numpy as np
 import torch
 
 from ._lib import check, lib, ptr
-from .colouring import block_stencil_colouring, stencil_pattern
+from .colouring import block_stencil_colouring, cell_pattern, stencil_pattern
 from .ilu0 import Ilu0
 
 
@@ -36,40 +36,62 @@ def _stream() -> int:
 
 
 class BlockJacobian:
-    """The block Jacobian on the reach-``reach`` cell pattern, materialised by coloured probes.
+    """The block Jacobian on the reach-``reach`` cell pattern.
 
-    ``frozen=True`` probes ``fv_jvp_frozen`` (gradients, SST closure and a_P held fixed), whose
-    operator is exactly reach 1, so reach 1 recovers it without contamination; ``frozen=False``
-    probes the full JVP (exact when ``reach`` covers the Jacobian's reach, 3 for these residuals).
-    Blocks are cell-major ``b x b`` with ``b`` the number of fields.
+    ``frozen=True`` is ``J_direct`` (gradients, SST closure and a_P held fixed), an operator of
+    exactly reach 1.  At reach 1 it is assembled directly (``fv_assemble_jacobian``: forward-mode
+    face-flux derivatives summed into the block rows, no colouring); ``method="probe"`` recovers
+    the same operator by coloured probes of ``fv_jvp_frozen`` as the reference does.
+    ``frozen=False`` probes the full JVP (exact when ``reach`` covers the Jacobian's reach, 3 for
+    these residuals).  Blocks are cell-major ``b x b`` with ``b`` the number of fields.
     """
 
-    def __init__(self, case, *, reach: int = 1, frozen: bool = True):
+    def __init__(self, case, *, reach: int = 1, frozen: bool = True, method: str | None = None):
         self.case = case
         mesh = case.dmesh.mesh
         self.n = mesh.n_cells
         self.b = case.n_unknowns // self.n
         interior = mesh.neighbour >= 0
-        own, nb = mesh.owner[interior], mesh.neighbour[interior]
-        self.colouring = block_stencil_colouring(own, nb, self.n, reach)
-        pat = stencil_pattern(own, nb, self.n, reach).tocsr()
-        pat.sort_indices()
-        self.indptr = np.ascontiguousarray(pat.indptr, dtype=np.int32)
-        self.indices = np.ascontiguousarray(pat.indices, dtype=np.int32)
+        self._own, self._nb = mesh.owner[interior], mesh.neighbour[interior]
+        self.reach = reach
+        if reach == 1:
+            self.indptr, self.indices = cell_pattern(self._own, self._nb, self.n)
+        else:
+            pat = stencil_pattern(self._own, self._nb, self.n, reach).tocsr()
+            pat.sort_indices()
+            self.indptr = np.ascontiguousarray(pat.indptr, dtype=np.int32)
+            self.indices = np.ascontiguousarray(pat.indices, dtype=np.int32)
         self.nnzb = int(self.indptr[-1])
         self.frozen = frozen
-        self.d_colour = torch.tensor(self.colouring.colour.astype(np.int32), device="cuda")
+        if method is None:
+            method = "assemble" if (frozen and reach == 1) else "probe"
+        if method == "assemble" and not (frozen and reach == 1):
+            raise ValueError("direct assembly builds the frozen reach-1 Jacobian only")
+        self.method = method
+        self._colouring = None
         self.d_indptr = torch.tensor(self.indptr, device="cuda")
         self.d_indices = torch.tensor(self.indices, device="cuda")
         self.values = torch.zeros(self.nnzb * self.b * self.b, dtype=torch.float64, device="cuda")
+
+    @property
+    def colouring(self):
+        if self._colouring is None:
+            self._colouring = block_stencil_colouring(self._own, self._nb, self.n, self.reach)
+            self.d_colour = torch.tensor(self._colouring.colour.astype(np.int32), device="cuda")
+        return self._colouring
 
     @property
     def n_probes(self) -> int:
         return self.colouring.n_colours * self.b
 
     def materialize(self, state: torch.Tensor) -> torch.Tensor:
+        if self.method == "assemble":
+            check(lib().fv_assemble_jacobian(self.case.handle, ptr(state), ptr(self.d_indptr),
+                                             ptr(self.d_indices), ptr(self.values), _stream()))
+            return self.values
+        n_colours = self.colouring.n_colours
         check(lib().fv_probe_jacobian(self.case.handle, ptr(state), int(self.frozen),
-                                      ptr(self.d_colour), self.colouring.n_colours,
+                                      ptr(self.d_colour), n_colours,
                                       ptr(self.d_indptr), ptr(self.d_indices), ptr(self.values),
                                       _stream()))
         return self.values

@@ -48,6 +48,8 @@ def _args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--step", default="vjp", choices=["vjp", "jvp"])
     ap.add_argument("--no-newton", action="store_true", help="skip the Newton-solve timing")
+    ap.add_argument("--newton-amg", action="store_true",
+                    help="also time Newton with the fp32 aggregation-AMG V-cycle preconditioner")
     ap.add_argument("--newton-oracle-check", action="store_true",
                     help="also evaluate the converged fp32-preconditioned state with the CPU oracle")
     return ap.parse_args()
@@ -358,6 +360,21 @@ def newton_block(args, wl, case) -> dict:
     from aquaflux_gb300 import solve
 
     out = {}
+    # one materialisation of the frozen block Jacobian: direct face assembly vs coloured probes
+    s0 = torch.tensor(wl.initial_state(), device="cuda")
+    jt = {}
+    for method in ("assemble", "probe"):
+        jac = solve.BlockJacobian(case, method=method)
+        jac.materialize(s0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        jac.materialize(s0)
+        torch.cuda.synchronize()
+        jt[method] = round((time.perf_counter() - t0) * 1e3, 2)
+        if method == "probe":
+            jt["n_probes"] = jac.n_probes
+        del jac
+    out["jacobian_ms"] = jt
     states = {}
     for prec in (64, 32):
         torch.cuda.synchronize()
@@ -368,6 +385,14 @@ def newton_block(args, wl, case) -> dict:
             "final_rel_residual": res.residual_norms[-1] / res.residual_norms[0],
             "phase_seconds": {k: round(v, 3) for k, v in res.phase_seconds.items()}}
         states[prec] = res.state
+    if args.newton_amg:
+        torch.cuda.synchronize()
+        res = solve.newton_solve(case, wl.initial_state(), kind="amg", max_steps=40)
+        out["fp32_amg"] = {
+            "seconds": round(res.seconds, 3), "converged": bool(res.converged),
+            "newton_steps": res.steps, "krylov_iterations": int(sum(res.krylov_iterations)),
+            "final_rel_residual": res.residual_norms[-1] / res.residual_norms[0],
+            "phase_seconds": {k: round(v, 3) for k, v in res.phase_seconds.items()}}
     a, b = states[64], states[32]
     out["fp32_vs_fp64_field_max_rel_diff"] = float((a - b).abs().max() / a.abs().max())
     out["speedup_fp32_vs_fp64"] = round(out["fp64"]["seconds"] / out["fp32"]["seconds"], 3)

@@ -120,6 +120,16 @@ int fv_jvp_frozen(FvCase* c, const double* state, const double* v, double* jv, v
 int fv_probe_jacobian(FvCase* c, const double* state, int frozen, const int* colour,
                       int n_colours, const int* indptr, const int* indices, double* values,
                       void* stream);
+/* The same frozen Jacobian (J_direct, reach 1) assembled directly: forward-mode derivatives of
+ * every face flux with respect to the unknowns of its two cells, summed into the block rows in
+ * the residual's face order, then the SST source, omega wall-cell and pressure-pin rows.  Needs
+ * no colouring (one face pass instead of n_colours * b probes); the pattern must hold every
+ * cell's diagonal block and the blocks of its face neighbours (blocks outside reach 1 are set to
+ * 0).  Fast path of materialize_block_jacobian (aquaflux/solve/sparse_jacobian.py:722-847) for
+ * the frozen operator.  Allocates a face-derivative buffer of 2 b^2 doubles per face on first
+ * use (kept with the case).  Device. */
+int fv_assemble_jacobian(FvCase* c, const double* state, const int* indptr, const int* indices,
+                         double* values, void* stream);
 /* jv = J v + shift * v (the pseudo-transient operator of aquaflux/solve/continuation.py:111-112);
  * `shift` is a device vector of the state's length. */
 int fv_jvp_shift(FvCase* c, const double* state, const double* v, const double* shift, double* jv,
@@ -199,6 +209,11 @@ int fv_ilu0_factor_values(const FvIlu0* f, void* out, void* stream);
  * ------------------------------------------------------------------------------------------ */
 int fv_saturation_colouring(int n, const int* indptr, const int* indices, int* colour,
                             int* n_colours);
+/* Reach-1 cell pattern (host): row i = {i} + the cells sharing an interior face with i, sorted
+ * and unique (the pattern of the frozen Jacobian; stencil_pattern with reach 1,
+ * aquaflux/solve/sparse_jacobian.py).  indptr (n + 1); indices capacity n + 2 * n_pairs. */
+int fv_cell_pattern(int n, long n_pairs, const int* owner, const int* neighbour, int* indptr,
+                    int* indices);
 
 /* ------------------------------------------------------------------------------------------
  * Aggregation multigrid.  Replaces the aggregation hierarchy of aquaflux/solve/multigrid.py
@@ -207,6 +222,15 @@ int fv_saturation_colouring(int n, const int* indptr, const int* indices, int* c
  * ------------------------------------------------------------------------------------------ */
 /* Aggregate the cells of a symmetric cell graph (host CSR); agg[i] in [0, *n_agg). */
 int fv_aggregate(int n, const int* indptr, const int* indices, int* agg, int* n_agg);
+/* One coarsening of a (block) pattern by an aggregation agg (host): mptr (na + 1) / mlist (n)
+ * the members of every aggregate in ascending order; cip (na + 1) / cix (capacity nnz) the sorted
+ * coarse pattern; gptr (capacity nnz + 1) / glist (nnz) for every coarse block the fine blocks
+ * summed into it, ascending (both NULL: the pattern only); n_coarse_blocks the coarse pattern's
+ * size.  No reference
+ * counterpart as an entry point: the Galerkin product of the piecewise-constant aggregation
+ * prolongation (aquaflux/solve/multigrid.py:1011-1245) as ordered block lists. */
+int fv_coarsen(int n, const int* indptr, const int* indices, const int* agg, int na, int* mptr,
+               int* mlist, int* cip, int* cix, long* gptr, long* glist, long* n_coarse_blocks);
 /* Galerkin coarse blocks: coarse[Q] = sum of the fine blocks glist[gptr[Q] .. gptr[Q+1]) in list
  * order (device; fine fp64 when fine_f64 != 0, else fp32; coarse fp32; b x b row-major blocks). */
 int fv_galerkin_f32(long n_coarse_blocks, int b, const long* gptr, const long* glist,

@@ -1,0 +1,82 @@
+"""Host plan of the aggregation hierarchy (no GPU): aggregates partition the cells, the ordered
+fine-block lists reproduce the Galerkin product P^T A P of the piecewise-constant prolongation,
+and colour-ordered coarse levels have shallow ILU(0) level schedules."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from aquaflux_gb300 import workloads
+from aquaflux_gb300.amg import plan_hierarchy
+
+
+def _cell_graph(n_ax):
+    m = workloads.channel3d(n_ax).mesh
+    o, nb = np.asarray(m.owner), np.asarray(m.neighbour)
+    keep = nb >= 0
+    n = m.n_cells
+    a = sp.coo_matrix((np.ones(int(keep.sum())), (o[keep], nb[keep])), shape=(n, n))
+    a = (a + a.T + sp.eye(n)).tocsr()
+    a.sort_indices()
+    return n, a.indptr.astype(np.int32), a.indices.astype(np.int32)
+
+
+def _lower_depth(ip, ix):
+    n = len(ip) - 1
+    lev = np.zeros(n, np.int64)
+    for i in range(n):
+        lo = ix[ip[i]:ip[i + 1]]
+        lo = lo[lo < i]
+        if lo.size:
+            lev[i] = lev[lo].max() + 1
+    return int(lev.max()) + 1
+
+
+@pytest.mark.parametrize("order", ["colour", "natural"])
+def test_plan_partitions_cells_and_forms_galerkin_blocks(order):
+    n, ip, ix = _cell_graph(12)
+    plan = plan_hierarchy(n, ip, ix, min_cells=50, coarse_order=order)
+    assert len(plan) >= 2
+    rng = np.random.default_rng(0)
+    b = 2
+    vals = rng.standard_normal((int(ip[-1]), b, b))
+    for step in plan:
+        na, agg = step["n_coarse"], step["agg"]
+        assert agg.min() == 0 and agg.max() == na - 1 and np.unique(agg).size == na
+        assert np.array_equal(np.sort(step["mlist"]), np.arange(len(agg)))
+        for i in range(na):
+            assert np.all(agg[step["mlist"][step["mptr"][i]:step["mptr"][i + 1]]] == i)
+        # coarse blocks from the ordered fine-block lists == P^T A P
+        gp, gl = step["gptr"], step["glist"]
+        coarse = np.stack([vals[gl[gp[q]:gp[q + 1]]].sum(axis=0) for q in range(len(gp) - 1)])
+        A = sp.bsr_matrix((vals, ix, ip), shape=(len(agg) * b, len(agg) * b)).toarray()
+        P = np.zeros((len(agg) * b, na * b))
+        for i, g in enumerate(agg):
+            P[i * b:(i + 1) * b, g * b:(g + 1) * b] = np.eye(b)
+        cip, cix = step["indptr"], step["indices"]
+        C = sp.bsr_matrix((coarse, cix, cip), shape=(na * b, na * b)).toarray()
+        np.testing.assert_allclose(C, P.T @ A @ P, rtol=1e-12, atol=1e-12)
+        for i in range(na):
+            row = cix[cip[i]:cip[i + 1]]
+            assert np.all(np.diff(row) > 0) and i in row
+        vals, ip, ix = coarse, cip, cix
+
+
+def test_colour_order_gives_shallow_coarse_level_sets():
+    n, ip, ix = _cell_graph(16)
+    nat = plan_hierarchy(n, ip, ix, min_cells=200, coarse_order="natural")
+    col = plan_hierarchy(n, ip, ix, min_cells=200, coarse_order="colour")
+    d_nat = _lower_depth(nat[0]["indptr"], nat[0]["indices"])
+    d_col = _lower_depth(col[0]["indptr"], col[0]["indices"])
+    assert d_col <= 16 < d_nat
+
+
+def test_cell_pattern_equals_the_reach_one_stencil():
+    from aquaflux_gb300.colouring import cell_pattern, stencil_pattern
+
+    m = workloads.channel3d(10).mesh
+    o, nb = np.asarray(m.owner), np.asarray(m.neighbour)
+    keep = nb >= 0
+    ip, ix = cell_pattern(o[keep], nb[keep], m.n_cells)
+    ref = stencil_pattern(o[keep], nb[keep], m.n_cells, 1).tocsr()
+    ref.sort_indices()
+    assert np.array_equal(ip, ref.indptr) and np.array_equal(ix, ref.indices)

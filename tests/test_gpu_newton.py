@@ -144,3 +144,41 @@ def test_amg_vcycle_is_a_fixed_linear_operator_and_converges_newton():
     assert res_amg.converged and res_ilu.converged
     sa, si = res_amg.state.cpu().numpy(), res_ilu.state.cpu().numpy()
     assert np.abs(sa - si).max() <= 1e-7 * np.abs(si).max()
+
+
+@pytest.mark.parametrize("name", ["cav8", "cavj", "lam3", "sst2", "sst3"])
+def test_assembled_jacobian_equals_the_coloured_probe(name):
+    """The direct face assembly of J_direct gives the blocks the coloured probes of the frozen JVP
+    give (materialize_block_jacobian, aquaflux/solve/sparse_jacobian.py:722-847), at the golden
+    states (negative-k cells, wall cells, the pressure pin) and at the zero state (mass-flux ties)."""
+    from tests.cases import device_case
+
+    from aquaflux_gb300.solve import BlockJacobian
+
+    fc, _, d, p = device_case(name)
+    ja = BlockJacobian(fc, method="assemble")
+    jp = BlockJacobian(fc, method="probe")
+    states = [np.asarray(x) for x in d[p + "states"]] + [np.zeros(fc.n_unknowns)]
+    for st in states:
+        s = torch.tensor(st, device="cuda")
+        a = ja.materialize(s).clone()
+        b = jp.materialize(s).clone()
+        # omega = 0 (the SST zero state) makes both operators non-finite at the same entries
+        assert torch.equal(torch.isfinite(a), torch.isfinite(b)), name
+        fin = torch.isfinite(b)
+        scale = float(b[fin].abs().max())
+        assert float((a[fin] - b[fin]).abs().max()) <= 1e-14 * scale, name
+
+
+def test_assembled_jacobian_overwrites_stale_values():
+    """Every block of the pattern is rewritten (no accumulation into what the buffer held)."""
+    from aquaflux_gb300.solve import BlockJacobian
+
+    m, case = _cavity(6)
+    jac = BlockJacobian(case)
+    s = torch.tensor(np.random.default_rng(3).standard_normal(case.n_unknowns) * 0.2,
+                     device="cuda")
+    a = jac.materialize(s).clone()
+    jac.values.fill_(7.0)
+    b = jac.materialize(s)
+    assert torch.equal(a, b)
