@@ -67,6 +67,13 @@ SIGNATURES = {
     "fv_galerkin_f32": (c_int, [c_long, c_int, P, P, P, c_int, P, P]),
     "fv_restrict_f32": (c_int, [c_int, c_int, P, P, P, P, P]),
     "fv_prolong_add_f32": (c_int, [c_int, c_int, P, P, P, P]),
+    "fv_galerkin_f64": (c_int, [c_long, c_int, P, P, P, c_int, P, P]),
+    "fv_permute_pattern": (c_int, [c_int, P, P, P, P, P, P]),
+    "fv_gather_blocks": (c_int, [c_long, c_int, P, P, c_int, P, c_int, P]),
+    "fv_to_cells": (c_int, [c_int, c_int, P, P, P, c_int, P]),
+    "fv_from_cells": (c_int, [c_int, c_int, P, P, c_int, P, P]),
+    "fv_restrict_f64": (c_int, [c_int, c_int, P, P, P, P, P]),
+    "fv_prolong_add_f64": (c_int, [c_int, c_int, P, P, P, P]),
 }
 
 _lib = None

@@ -6,7 +6,8 @@ coarse correction, prolongation ``P``) over an aggregation hierarchy
 (``aquaflux/solve/multigrid.py:1011-1245``), restated for the GPU: cells are aggregated once per
 pattern on the host (``fv_aggregate``), every level's operator is the Galerkin product of the
 unsmoothed aggregation (formed on the GPU by ordered block sums), and the smoothing, residuals,
-restriction and prolongation all run in fp32 on the device.  The coarsest level is smoothed by
+restriction and prolongation all run on the device, in fp32 (the mixed-precision preconditioner)
+or fp64.  The coarsest level is smoothed by
 ILU(0) sweeps instead of the reference's dense inverse (the 2M-cell hierarchy's coarsest level is
 too large for a dense factor).  Coarse aggregates are numbered colour by colour, so that the coarse
 levels' ILU(0) sweeps run in a handful of level sets.  Vectors inside the hierarchy are
@@ -28,25 +29,28 @@ def _stream() -> int:
 
 
 class _Level:
-    def __init__(self, n, b, indptr, indices):
+    def __init__(self, n, b, indptr, indices, precision):
         self.n, self.b = n, b
+        self.sfx = "f32" if precision == 32 else "f64"
+        dtype = torch.float32 if precision == 32 else torch.float64
         self.indptr = np.ascontiguousarray(indptr, dtype=np.int32)
         self.indices = np.ascontiguousarray(indices, dtype=np.int32)
         self.nnzb = int(self.indptr[-1])
         self.d_indptr = torch.tensor(self.indptr, device="cuda")
         self.d_indices = torch.tensor(self.indices, device="cuda")
-        self.values = torch.zeros(self.nnzb * b * b, dtype=torch.float32, device="cuda")
+        self.values = torch.zeros(self.nnzb * b * b, dtype=dtype, device="cuda")
         self.ilu = Ilu0.__new__(Ilu0)
-        self.ilu._setup(self.indptr, self.indices, b, 32)
-        self.x = torch.zeros(n * b, dtype=torch.float32, device="cuda")
+        self.ilu._setup(self.indptr, self.indices, b, precision)
+        self.x = torch.zeros(n * b, dtype=dtype, device="cuda")
         self.r = torch.zeros_like(self.x)
         self.t = torch.zeros_like(self.x)
         self.rhs = torch.zeros_like(self.x)  # right-hand side when this is a coarse level
         self.coarse = None  # transfer data to the next level
 
     def spmv(self, x, y):
-        check(lib().fv_bsr_spmv_f32(self.n, self.b, ptr(self.d_indptr), ptr(self.d_indices),
-                                    ptr(self.values), ptr(x), ptr(y), 0, _stream()))
+        check(getattr(lib(), "fv_bsr_spmv_" + self.sfx)(
+            self.n, self.b, ptr(self.d_indptr), ptr(self.d_indices), ptr(self.values), ptr(x),
+            ptr(y), 0, _stream()))
 
 
 def plan_hierarchy(n, indptr, indices, *, min_cells: int = 4000, max_levels: int = 10,
@@ -110,31 +114,46 @@ class AmgHierarchy:
     """Aggregation hierarchy on a fixed block pattern; ``refresh(values)`` re-forms every level."""
 
     def __init__(self, n, b, indptr, indices, *, min_cells: int = 4000, max_levels: int = 10,
-                 sweeps: int = 1, coarse_sweeps: int = 4, coarse_order: str = "colour"):
+                 sweeps: int = 1, coarse_sweeps: int = 4, coarse_order: str = "colour",
+                 precision: int = 32):
+        if precision not in (32, 64):
+            raise ValueError(f"precision must be 32 or 64, got {precision}")
         self.b, self.sweeps, self.coarse_sweeps = b, sweeps, coarse_sweeps
-        self.levels = [_Level(n, b, indptr, indices)]
+        self.precision = precision
+        self.sfx = "f32" if precision == 32 else "f64"
+        self.levels = [_Level(n, b, indptr, indices, precision)]
         for step in plan_hierarchy(n, indptr, indices, min_cells=min_cells,
                                    max_levels=max_levels, coarse_order=coarse_order):
             fine = self.levels[-1]
             fine.coarse = {k: torch.tensor(step[k], device="cuda")
                            for k in ("agg", "mptr", "mlist", "gptr", "glist")}
             fine.coarse["n_coarse_blocks"] = int(step["gptr"].size - 1)
-            self.levels.append(_Level(step["n_coarse"], b, step["indptr"], step["indices"]))
+            self.levels.append(_Level(step["n_coarse"], b, step["indptr"], step["indices"],
+                                      precision))
 
     @property
     def sizes(self):
         return [lv.n for lv in self.levels]
 
-    def refresh(self, fine_values: torch.Tensor) -> None:
-        """Re-form every level from the fine operator's block values (fp64 or fp32, device)."""
+    def refresh(self, fine_values: torch.Tensor, bmap: torch.Tensor | None = None) -> None:
+        """Re-form every level from the fine operator's block values (fp64 or fp32, device);
+        with ``bmap`` the hierarchy's fine block q is block ``bmap[q]`` of ``fine_values``."""
         lv0 = self.levels[0]
-        lv0.values.copy_(fine_values)
-        lv0.ilu.refactor(fine_values)
+        if bmap is not None:
+            check(lib().fv_gather_blocks(lv0.nnzb, self.b, ptr(bmap), ptr(fine_values),
+                                         int(fine_values.dtype == torch.float64),
+                                         ptr(lv0.values), int(self.precision == 64), _stream()))
+        elif self.precision == 64 and fine_values.dtype == torch.float64:
+            lv0.values = fine_values  # the fine operator itself (no copy)
+        else:
+            lv0.values.copy_(fine_values)
+        lv0.ilu.refactor(lv0.values)
+        galerkin = getattr(lib(), "fv_galerkin_" + self.sfx)
         for fine, coarse in zip(self.levels[:-1], self.levels[1:]):
             t = fine.coarse
-            check(lib().fv_galerkin_f32(t["n_coarse_blocks"], self.b, ptr(t["gptr"]),
-                                        ptr(t["glist"]), ptr(fine.values), 0,
-                                        ptr(coarse.values), _stream()))
+            check(galerkin(t["n_coarse_blocks"], self.b, ptr(t["gptr"]), ptr(t["glist"]),
+                           ptr(fine.values), int(fine.values.dtype == torch.float64),
+                           ptr(coarse.values), _stream()))
             coarse.ilu.refactor(coarse.values)
 
     def _smooth(self, lv, b_vec, x, sweeps, from_zero):
@@ -159,28 +178,59 @@ class AmgHierarchy:
         coarse = self.levels[level + 1]
         t = lv.coarse
         bc = coarse.rhs
-        check(lib().fv_restrict_f32(coarse.n, self.b, ptr(t["mptr"]), ptr(t["mlist"]), ptr(lv.r),
-                                    ptr(bc), _stream()))
+        check(getattr(lib(), "fv_restrict_" + self.sfx)(
+            coarse.n, self.b, ptr(t["mptr"]), ptr(t["mlist"]), ptr(lv.r), ptr(bc), _stream()))
         xc = self.vcycle(level + 1, bc)
-        check(lib().fv_prolong_add_f32(lv.n, self.b, ptr(t["agg"]), ptr(xc), ptr(x), _stream()))
+        check(getattr(lib(), "fv_prolong_add_" + self.sfx)(
+            lv.n, self.b, ptr(t["agg"]), ptr(xc), ptr(x), _stream()))
         self._smooth(lv, b_vec, x, self.sweeps, False)
         return x
 
 
 class AmgPreconditioner:
-    """``M ~= J^-1``: one fp32 aggregation V-cycle with ILU(0) smoothing of the materialised block
-    Jacobian (field-major fp64 vectors in and out)."""
+    """``M ~= J^-1``: one aggregation V-cycle with ILU(0) smoothing of the materialised block
+    Jacobian, fp32 (default) or fp64 throughout (field-major fp64 vectors in and out).
 
-    def __init__(self, jac, **kw):
+    ``fine_order="colour"`` numbers the fine cells colour by colour (a distance-1 colouring of the
+    cell graph; two colours on a hexahedral mesh), so that the fine ILU(0) sweeps run in a few
+    level sets of many rows each instead of hundreds of short ones; ``"natural"`` keeps the
+    operator's own cell order.
+    """
+
+    def __init__(self, jac, precision: int = 32, *, fine_order: str = "colour", **kw):
         self.jac = jac
-        self.h = AmgHierarchy(jac.n, jac.b, jac.indptr, jac.indices, **kw)
-        self._b = torch.empty(jac.n * jac.b, dtype=torch.float32, device="cuda")
+        n, b = jac.n, jac.b
+        self._perm = self._bmap = None
+        indptr, indices = jac.indptr, jac.indices
+        if fine_order == "colour":
+            col = np.empty(n, dtype=np.int32)
+            nco = ctypes.c_int(0)
+            check(lib().fv_saturation_colouring(n, ptr(indptr), ptr(indices), ptr(col),
+                                                ctypes.byref(nco)))
+            perm = np.argsort(col, kind="stable").astype(np.int32)
+            pip = np.empty(n + 1, dtype=np.int32)
+            pix = np.empty(int(indptr[-1]), dtype=np.int32)
+            bmap = np.empty(int(indptr[-1]), dtype=np.int64)
+            check(lib().fv_permute_pattern(n, ptr(indptr), ptr(indices), ptr(perm), ptr(pip),
+                                           ptr(pix), ptr(bmap)))
+            self.n_colours = int(nco.value)
+            self._perm = torch.tensor(perm, device="cuda")
+            self._bmap = torch.tensor(bmap, device="cuda")
+            indptr, indices = pip, pix
+        elif fine_order != "natural":
+            raise ValueError(f"fine_order must be 'colour' or 'natural', got {fine_order!r}")
+        self.h = AmgHierarchy(n, b, indptr, indices, precision=precision, **kw)
+        self._f64 = int(precision == 64)
+        self._b = torch.empty(n * b, dtype=self.h.levels[0].x.dtype, device="cuda")
 
     def refresh(self, state: torch.Tensor) -> None:
-        self.h.refresh(self.jac.materialize(state))
+        self.h.refresh(self.jac.materialize(state), self._bmap)
 
     def apply(self, r: torch.Tensor) -> torch.Tensor:
         n, b = self.jac.n, self.jac.b
-        self._b.copy_(r.view(b, n).t().reshape(-1))
+        check(lib().fv_to_cells(n, b, ptr(self._perm), ptr(r), ptr(self._b), self._f64,
+                                _stream()))
         x = self.h.vcycle(0, self._b)
-        return x.view(n, b).t().reshape(-1).to(torch.float64)
+        out = torch.empty(n * b, dtype=torch.float64, device="cuda")
+        check(lib().fv_from_cells(n, b, ptr(self._perm), ptr(x), self._f64, ptr(out), _stream()))
+        return out

@@ -136,80 +136,244 @@ extern "C" int fv_coarsen(int n, const int* indptr, const int* indices, const in
   return FV_OK;
 }
 
+// Symmetric block permutation of a pattern (host): new row r is old row perm[r]; the new pattern
+// (out_indptr (n + 1), out_indices (nnz)) is sorted per row, and bmap[q'] is the old block index of
+// new block q'.  iperm is perm's inverse.
+extern "C" int fv_permute_pattern(int n, const int* indptr, const int* indices, const int* perm,
+                                  int* out_indptr, int* out_indices, long* bmap) {
+  if (n <= 0 || !indptr || !indices || !perm || !out_indptr || !out_indices || !bmap) {
+    fv_set_error("fv_permute_pattern: bad arguments");
+    return FV_ERR_ARG;
+  }
+  std::vector<int> iperm(n, -1);
+  for (int r = 0; r < n; ++r) {
+    if (perm[r] < 0 || perm[r] >= n || iperm[perm[r]] >= 0) {
+      fv_set_error("fv_permute_pattern: perm is not a permutation");
+      return FV_ERR_ARG;
+    }
+    iperm[perm[r]] = r;
+  }
+  std::vector<std::pair<int, long>> row;
+  long pos = 0;
+  out_indptr[0] = 0;
+  for (int r = 0; r < n; ++r) {
+    const int i = perm[r];
+    row.clear();
+    for (int q = indptr[i]; q < indptr[i + 1]; ++q) {
+      const int j = indices[q];
+      if (j < 0 || j >= n) {
+        fv_set_error("fv_permute_pattern: column index out of range");
+        return FV_ERR_ARG;
+      }
+      row.emplace_back(iperm[j], (long)q);
+    }
+    std::sort(row.begin(), row.end());
+    for (const auto& e : row) {
+      out_indices[pos] = e.first;
+      bmap[pos] = e.second;
+      ++pos;
+    }
+    out_indptr[r + 1] = (int)pos;
+  }
+  return FV_OK;
+}
+
 namespace {
 
-// coarse[Q] = sum over the fine blocks listed for Q (gptr / glist), in list order.
+// dst block q = src block bmap[q] (b x b entries), converted to Out.
+template <class In, class Out>
+__global__ void k_gather_blocks(long nnzb, int bb, const long* bmap, const In* src, Out* dst) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nnzb * bb) return;
+  const long q = t / bb, e = t % bb;
+  dst[t] = (Out)src[bmap[q] * bb + e];
+}
+
+// Field-major fp64 vector -> cell-major Out vector in the permuted cell order:
+//   out[r * b + a] = in[a * n + perm[r]]   (perm NULL: identity)
+template <class Out>
+__global__ void k_to_cells(int n, int b, const int* perm, const double* in, Out* out) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long)n * b) return;
+  const int r = (int)(t / b), a = (int)(t % b);
+  const int i = perm ? perm[r] : r;
+  out[t] = (Out)in[(long)a * n + i];
+}
+
+// The inverse: out[a * n + perm[r]] = in[r * b + a], widened to fp64.
 template <class In>
+__global__ void k_from_cells(int n, int b, const int* perm, const In* in, double* out) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long)n * b) return;
+  const int r = (int)(t / b), a = (int)(t % b);
+  const int i = perm ? perm[r] : r;
+  out[(long)a * n + i] = (double)in[t];
+}
+
+}  // namespace
+
+extern "C" int fv_gather_blocks(long nnzb, int b, const long* bmap, const void* src, int src_f64,
+                                void* dst, int dst_f64, void* stream) {
+  if (nnzb <= 0 || b <= 0 || !bmap || !src || !dst) {
+    fv_set_error("fv_gather_blocks: bad arguments");
+    return FV_ERR_ARG;
+  }
+  const long n = nnzb * b * b;
+  const int bb = b * b;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int g = fv_blocks(n, 256);
+  if (src_f64 && dst_f64)
+    k_gather_blocks<double, double><<<g, 256, 0, s>>>(nnzb, bb, bmap, (const double*)src, (double*)dst);
+  else if (src_f64)
+    k_gather_blocks<double, float><<<g, 256, 0, s>>>(nnzb, bb, bmap, (const double*)src, (float*)dst);
+  else if (dst_f64)
+    k_gather_blocks<float, double><<<g, 256, 0, s>>>(nnzb, bb, bmap, (const float*)src, (double*)dst);
+  else
+    k_gather_blocks<float, float><<<g, 256, 0, s>>>(nnzb, bb, bmap, (const float*)src, (float*)dst);
+  FV_CUDA_TRY(cudaGetLastError());
+  return FV_OK;
+}
+
+extern "C" int fv_to_cells(int n, int b, const int* perm, const double* in, void* out, int out_f64,
+                           void* stream) {
+  if (n <= 0 || b <= 0 || !in || !out) {
+    fv_set_error("fv_to_cells: bad arguments");
+    return FV_ERR_ARG;
+  }
+  const long m = (long)n * b;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (out_f64)
+    k_to_cells<double><<<fv_blocks(m, 256), 256, 0, s>>>(n, b, perm, in, (double*)out);
+  else
+    k_to_cells<float><<<fv_blocks(m, 256), 256, 0, s>>>(n, b, perm, in, (float*)out);
+  FV_CUDA_TRY(cudaGetLastError());
+  return FV_OK;
+}
+
+extern "C" int fv_from_cells(int n, int b, const int* perm, const void* in, int in_f64,
+                             double* out, void* stream) {
+  if (n <= 0 || b <= 0 || !in || !out) {
+    fv_set_error("fv_from_cells: bad arguments");
+    return FV_ERR_ARG;
+  }
+  const long m = (long)n * b;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (in_f64)
+    k_from_cells<double><<<fv_blocks(m, 256), 256, 0, s>>>(n, b, perm, (const double*)in, out);
+  else
+    k_from_cells<float><<<fv_blocks(m, 256), 256, 0, s>>>(n, b, perm, (const float*)in, out);
+  FV_CUDA_TRY(cudaGetLastError());
+  return FV_OK;
+}
+
+namespace {
+
+// coarse[Q] = sum over the fine blocks listed for Q (gptr / glist), in list order, accumulated in
+// fp64 and stored in Out.
+template <class In, class Out>
 __global__ void k_galerkin(long n_coarse_blocks, int b, const long* gptr, const long* glist,
-                           const In* fine, float* coarse) {
+                           const In* fine, Out* coarse) {
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const long bb = (long)b * b;
   if (t >= n_coarse_blocks * bb) return;
   const long Q = t / bb, e = t % bb;
   double acc = 0.0;
   for (long p = gptr[Q]; p < gptr[Q + 1]; ++p) acc += (double)fine[glist[p] * bb + e];
-  coarse[t] = (float)acc;
+  coarse[t] = (Out)acc;
 }
 
 // rc[I * b + a] = sum over the member cells i of aggregate I (mptr / mlist) of r[i * b + a]
-__global__ void k_restrict(int n_coarse, int b, const int* mptr, const int* mlist, const float* r,
-                           float* rc) {
+template <class T>
+__global__ void k_restrict(int n_coarse, int b, const int* mptr, const int* mlist, const T* r,
+                           T* rc) {
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (long)n_coarse * b) return;
   const int I = (int)(t / b), a = (int)(t % b);
-  float acc = 0.0f;
+  T acc = 0;
   for (int p = mptr[I]; p < mptr[I + 1]; ++p) acc += r[(long)mlist[p] * b + a];
   rc[t] = acc;
 }
 
 // x[i * b + a] += xc[agg[i] * b + a]
-__global__ void k_prolong_add(int n_fine, int b, const int* agg, const float* xc, float* x) {
+template <class T>
+__global__ void k_prolong_add(int n_fine, int b, const int* agg, const T* xc, T* x) {
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (long)n_fine * b) return;
   const int i = (int)(t / b), a = (int)(t % b);
   x[t] += xc[(long)agg[i] * b + a];
 }
 
-}  // namespace
-
-extern "C" int fv_galerkin_f32(long n_coarse_blocks, int b, const long* gptr, const long* glist,
-                               const void* fine, int fine_f64, float* coarse, void* stream) {
+template <class Out>
+int galerkin(const char* name, long n_coarse_blocks, int b, const long* gptr, const long* glist,
+             const void* fine, int fine_f64, Out* coarse, void* stream) {
   if (n_coarse_blocks <= 0 || b <= 0 || !gptr || !glist || !fine || !coarse) {
-    fv_set_error("fv_galerkin_f32: bad arguments");
+    fv_set_error("%s: bad arguments", name);
     return FV_ERR_ARG;
   }
   const long n = n_coarse_blocks * b * b;
   cudaStream_t s = (cudaStream_t)stream;
   if (fine_f64)
-    k_galerkin<double><<<fv_blocks(n, 256), 256, 0, s>>>(n_coarse_blocks, b, gptr, glist,
-                                                         (const double*)fine, coarse);
+    k_galerkin<double, Out><<<fv_blocks(n, 256), 256, 0, s>>>(n_coarse_blocks, b, gptr, glist,
+                                                              (const double*)fine, coarse);
   else
-    k_galerkin<float><<<fv_blocks(n, 256), 256, 0, s>>>(n_coarse_blocks, b, gptr, glist,
-                                                        (const float*)fine, coarse);
+    k_galerkin<float, Out><<<fv_blocks(n, 256), 256, 0, s>>>(n_coarse_blocks, b, gptr, glist,
+                                                             (const float*)fine, coarse);
   FV_CUDA_TRY(cudaGetLastError());
   return FV_OK;
 }
 
-extern "C" int fv_restrict_f32(int n_coarse, int b, const int* mptr, const int* mlist,
-                               const float* r, float* rc, void* stream) {
+template <class T>
+int restrict_(const char* name, int n_coarse, int b, const int* mptr, const int* mlist,
+              const T* r, T* rc, void* stream) {
   if (n_coarse <= 0 || b <= 0 || !mptr || !mlist || !r || !rc) {
-    fv_set_error("fv_restrict_f32: bad arguments");
+    fv_set_error("%s: bad arguments", name);
     return FV_ERR_ARG;
   }
   const long n = (long)n_coarse * b;
-  k_restrict<<<fv_blocks(n, 256), 256, 0, (cudaStream_t)stream>>>(n_coarse, b, mptr, mlist, r, rc);
+  k_restrict<T><<<fv_blocks(n, 256), 256, 0, (cudaStream_t)stream>>>(n_coarse, b, mptr, mlist, r,
+                                                                     rc);
   FV_CUDA_TRY(cudaGetLastError());
   return FV_OK;
 }
 
-extern "C" int fv_prolong_add_f32(int n_fine, int b, const int* agg, const float* xc, float* x,
-                                  void* stream) {
+template <class T>
+int prolong_add(const char* name, int n_fine, int b, const int* agg, const T* xc, T* x,
+                void* stream) {
   if (n_fine <= 0 || b <= 0 || !agg || !xc || !x) {
-    fv_set_error("fv_prolong_add_f32: bad arguments");
+    fv_set_error("%s: bad arguments", name);
     return FV_ERR_ARG;
   }
   const long n = (long)n_fine * b;
-  k_prolong_add<<<fv_blocks(n, 256), 256, 0, (cudaStream_t)stream>>>(n_fine, b, agg, xc, x);
+  k_prolong_add<T><<<fv_blocks(n, 256), 256, 0, (cudaStream_t)stream>>>(n_fine, b, agg, xc, x);
   FV_CUDA_TRY(cudaGetLastError());
   return FV_OK;
+}
+
+}  // namespace
+
+extern "C" int fv_galerkin_f32(long n_coarse_blocks, int b, const long* gptr, const long* glist,
+                               const void* fine, int fine_f64, float* coarse, void* stream) {
+  return galerkin("fv_galerkin_f32", n_coarse_blocks, b, gptr, glist, fine, fine_f64, coarse,
+                  stream);
+}
+extern "C" int fv_galerkin_f64(long n_coarse_blocks, int b, const long* gptr, const long* glist,
+                               const void* fine, int fine_f64, double* coarse, void* stream) {
+  return galerkin("fv_galerkin_f64", n_coarse_blocks, b, gptr, glist, fine, fine_f64, coarse,
+                  stream);
+}
+extern "C" int fv_restrict_f32(int n_coarse, int b, const int* mptr, const int* mlist,
+                               const float* r, float* rc, void* stream) {
+  return restrict_("fv_restrict_f32", n_coarse, b, mptr, mlist, r, rc, stream);
+}
+extern "C" int fv_restrict_f64(int n_coarse, int b, const int* mptr, const int* mlist,
+                               const double* r, double* rc, void* stream) {
+  return restrict_("fv_restrict_f64", n_coarse, b, mptr, mlist, r, rc, stream);
+}
+extern "C" int fv_prolong_add_f32(int n_fine, int b, const int* agg, const float* xc, float* x,
+                                  void* stream) {
+  return prolong_add("fv_prolong_add_f32", n_fine, b, agg, xc, x, stream);
+}
+extern "C" int fv_prolong_add_f64(int n_fine, int b, const int* agg, const double* xc, double* x,
+                                  void* stream) {
+  return prolong_add("fv_prolong_add_f64", n_fine, b, agg, xc, x, stream);
 }

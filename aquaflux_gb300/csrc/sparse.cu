@@ -13,6 +13,7 @@
 // scalar CSR ILU(0).
 #include <algorithm>
 #include <cstdio>
+#include <type_traits>
 #include <vector>
 
 #include "internal.cuh"
@@ -22,6 +23,54 @@ void fv_set_error_index(long i);
 namespace {
 
 constexpr int kThreads = 256;
+
+// B contiguous values p[0 .. B) into registers with the widest vector loads the block size allows
+// (p is aligned to B values: every block row segment and every cell segment is).
+template <int B, class V>
+__device__ __forceinline__ void load_seg(const V* __restrict__ p, V (&o)[B]) {
+  if constexpr (std::is_same<V, double>::value && B % 2 == 0) {
+#pragma unroll
+    for (int k = 0; k < B / 2; ++k) {
+      const double2 t = reinterpret_cast<const double2*>(p)[k];
+      o[2 * k] = t.x;
+      o[2 * k + 1] = t.y;
+    }
+  } else if constexpr (std::is_same<V, float>::value && B % 4 == 0) {
+#pragma unroll
+    for (int k = 0; k < B / 4; ++k) {
+      const float4 t = reinterpret_cast<const float4*>(p)[k];
+      o[4 * k] = t.x;
+      o[4 * k + 1] = t.y;
+      o[4 * k + 2] = t.z;
+      o[4 * k + 3] = t.w;
+    }
+  } else if constexpr (std::is_same<V, float>::value && B % 2 == 0) {
+#pragma unroll
+    for (int k = 0; k < B / 2; ++k) {
+      const float2 t = reinterpret_cast<const float2*>(p)[k];
+      o[2 * k] = t.x;
+      o[2 * k + 1] = t.y;
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < B; ++k) o[k] = p[k];
+  }
+}
+
+// Calls fn(std::integral_constant<int, B>) for the runtime block size b in 2 .. 8.
+template <class Fn>
+void with_block_size(int b, Fn&& fn) {
+  switch (b) {
+    case 2: fn(std::integral_constant<int, 2>{}); break;
+    case 3: fn(std::integral_constant<int, 3>{}); break;
+    case 4: fn(std::integral_constant<int, 4>{}); break;
+    case 5: fn(std::integral_constant<int, 5>{}); break;
+    case 6: fn(std::integral_constant<int, 6>{}); break;
+    case 7: fn(std::integral_constant<int, 7>{}); break;
+    default: fn(std::integral_constant<int, 8>{}); break;
+  }
+}
+
 
 // ------------------------------------------------------------------------------ BSR SpMV
 template <class V>
@@ -37,6 +86,27 @@ __global__ void k_bsr_spmv(int nbr, int b, const int* __restrict__ ptr, const in
     const V* blk = val + (long)q * bb + (long)a * b;
     const V* xs = x + (long)idx[q] * b;
     for (int c = 0; c < b; ++c) acc += blk[c] * xs[c];
+  }
+  y[r] = acc;
+}
+
+// The same product with a compile-time block size and vector loads of each row segment (every
+// block row segment and x segment starts at a multiple of B values from 16-byte aligned bases).
+template <class V, int B>
+__global__ void k_bsr_spmv_b(int nbr, const int* __restrict__ ptr, const int* __restrict__ idx,
+                             const V* __restrict__ val, const V* __restrict__ x,
+                             V* __restrict__ y) {
+  const long r = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= (long)nbr * B) return;
+  const int i = (int)(r / B), a = (int)(r % B);
+  constexpr long BB = (long)B * B;
+  V acc = 0;
+  for (int q = ptr[i]; q < ptr[i + 1]; ++q) {
+    V m[B], xs[B];
+    load_seg<B>(val + (long)q * BB + (long)a * B, m);
+    load_seg<B>(x + (long)idx[q] * B, xs);
+#pragma unroll
+    for (int c = 0; c < B; ++c) acc += m[c] * xs[c];
   }
   y[r] = acc;
 }
@@ -324,53 +394,63 @@ __global__ void k_ilu_factor_lg(IluView<V> F, const int* rows, int count,
   }
 }
 
-template <class V>
+// Forward sweep of one level, a group of FV_LG lanes per block row (lane a = row a of the block).
+template <class V, int B>
 __global__ void k_ilu_lower_lg(IluView<V> F, const int* rows, int count, V* y) {
   const int gid = (blockIdx.x * blockDim.x + threadIdx.x) / FV_LG;
   const int a = threadIdx.x & (FV_LG - 1);
   if (gid >= count) return;
   const unsigned mask = lg_mask();
-  const int i = rows[gid], b = F.b;
-  const bool live = a < b;
-  const long bb = (long)b * b;
-  V acc = live ? y[(long)i * b + a] : V(0);
+  const int i = rows[gid];
+  const bool live = a < B;
+  constexpr long BB = (long)B * B;
+  V acc = live ? y[(long)i * B + a] : V(0);
   if (live)
     for (int q = F.ptr[i]; q < F.diag[i]; ++q) {
-      const V* L = F.val + (long)q * bb + (long)a * b;
-      const V* yj = y + (long)F.idx[q] * b;
-      for (int c = 0; c < b; ++c) acc -= L[c] * yj[c];
+      V L[B], yj[B];
+      load_seg<B>(F.val + (long)q * BB + (long)a * B, L);
+      load_seg<B>(y + (long)F.idx[q] * B, yj);
+#pragma unroll
+      for (int c = 0; c < B; ++c) acc -= L[c] * yj[c];
     }
-  const V* D = F.val + (long)F.diag[i] * bb;
-  for (int c = 0; c < b; ++c) {
+  V D[B];
+  if (live) load_seg<B>(F.val + (long)F.diag[i] * BB + (long)a * B, D);
+#pragma unroll
+  for (int c = 0; c < B; ++c) {
     const V vc = __shfl_sync(mask, acc, c, FV_LG);
-    if (live && a > c) acc -= D[(long)a * b + c] * vc;
+    if (live && a > c) acc -= D[c] * vc;
   }
-  if (live) y[(long)i * b + a] = acc;
+  if (live) y[(long)i * B + a] = acc;
 }
 
-template <class V>
+// Backward sweep of one level (U x = y).
+template <class V, int B>
 __global__ void k_ilu_upper_lg(IluView<V> F, const int* rows, int count, V* x) {
   const int gid = (blockIdx.x * blockDim.x + threadIdx.x) / FV_LG;
   const int a = threadIdx.x & (FV_LG - 1);
   if (gid >= count) return;
   const unsigned mask = lg_mask();
-  const int i = rows[gid], b = F.b;
-  const bool live = a < b;
-  const long bb = (long)b * b;
-  V acc = live ? x[(long)i * b + a] : V(0);
+  const int i = rows[gid];
+  const bool live = a < B;
+  constexpr long BB = (long)B * B;
+  V acc = live ? x[(long)i * B + a] : V(0);
   if (live)
     for (int q = F.diag[i] + 1; q < F.ptr[i + 1]; ++q) {
-      const V* U = F.val + (long)q * bb + (long)a * b;
-      const V* xk = x + (long)F.idx[q] * b;
-      for (int c = 0; c < b; ++c) acc -= U[c] * xk[c];
+      V U[B], xk[B];
+      load_seg<B>(F.val + (long)q * BB + (long)a * B, U);
+      load_seg<B>(x + (long)F.idx[q] * B, xk);
+#pragma unroll
+      for (int c = 0; c < B; ++c) acc -= U[c] * xk[c];
     }
-  const V* D = F.val + (long)F.diag[i] * bb;
-  for (int c = b - 1; c >= 0; --c) {
-    if (a == c) acc = acc / D[(long)c * b + c];
+  V D[B];
+  if (live) load_seg<B>(F.val + (long)F.diag[i] * BB + (long)a * B, D);
+#pragma unroll
+  for (int c = B - 1; c >= 0; --c) {
+    if (a == c) acc = acc / D[c];
     const V vc = __shfl_sync(mask, acc, c, FV_LG);
-    if (live && a < c) acc -= D[(long)a * b + c] * vc;
+    if (live && a < c) acc -= D[c] * vc;
   }
-  if (live) x[(long)i * b + a] = acc;
+  if (live) x[(long)i * B + a] = acc;
 }
 
 template <class V>
@@ -548,13 +628,19 @@ void launch_apply_levels(FvIlu0* f, int transpose, V* x, cudaStream_t s) {
     for (size_t l = 0; l + 1 < f->lv_fwd.size(); ++l) {
       const int cnt = f->lv_fwd[l + 1] - f->lv_fwd[l];
       if (!cnt) continue;
-      if (lg) k_ilu_lower_lg<V><<<grid(cnt), 128, 0, s>>>(F, f->rows_fwd + f->lv_fwd[l], cnt, x);
+      if (lg)
+        with_block_size(f->b, [&](auto B) {
+          k_ilu_lower_lg<V, B()><<<grid(cnt), 128, 0, s>>>(F, f->rows_fwd + f->lv_fwd[l], cnt, x);
+        });
       else k_ilu_lower<V><<<grid(cnt), 128, 0, s>>>(F, f->rows_fwd + f->lv_fwd[l], cnt, x);
     }
     for (size_t l = 0; l + 1 < f->lv_bwd.size(); ++l) {
       const int cnt = f->lv_bwd[l + 1] - f->lv_bwd[l];
       if (!cnt) continue;
-      if (lg) k_ilu_upper_lg<V><<<grid(cnt), 128, 0, s>>>(F, f->rows_bwd + f->lv_bwd[l], cnt, x);
+      if (lg)
+        with_block_size(f->b, [&](auto B) {
+          k_ilu_upper_lg<V, B()><<<grid(cnt), 128, 0, s>>>(F, f->rows_bwd + f->lv_bwd[l], cnt, x);
+        });
       else k_ilu_upper<V><<<grid(cnt), 128, 0, s>>>(F, f->rows_bwd + f->lv_bwd[l], cnt, x);
     }
   } else {
@@ -793,7 +879,15 @@ int spmv(int nbr, int b, const int* indptr, const int* indices, const V* values,
   }
   const long rows = (long)nbr * b;
   if (!transpose) {
-    k_bsr_spmv<V><<<fv_blocks(rows, kThreads), kThreads, 0, s>>>(nbr, b, indptr, indices, values, x, y);
+    const bool aligned = ((uintptr_t)values % 16 == 0) && ((uintptr_t)x % 16 == 0);
+    if (aligned && b >= 2 && b <= 8)
+      with_block_size(b, [&](auto B) {
+        k_bsr_spmv_b<V, B()><<<fv_blocks(rows, kThreads), kThreads, 0, s>>>(nbr, indptr, indices,
+                                                                           values, x, y);
+      });
+    else
+      k_bsr_spmv<V><<<fv_blocks(rows, kThreads), kThreads, 0, s>>>(nbr, b, indptr, indices,
+                                                                   values, x, y);
     FV_CUDA_TRY(cudaGetLastError());
     return FV_OK;
   }

@@ -214,9 +214,11 @@ def newton_solve(case, state0, *, rtol: float = 1e-10, atol: float = 1e-12, max_
                  linear_rtol: float = 1e-3, restart: int = 30,
                  max_krylov: int = 300, precision: int = 32, reach: int = 1, frozen: bool = True,
                  refresh_every: int = 1, line_search_steps: int = 10,
-                 preconditioner=None, kind: str = "ilu") -> NewtonResult:
-    """Newton's method with FGMRES, preconditioned by ILU(0) of the materialised Jacobian (fp32 or
-    fp64, ``kind="ilu"``) or by an fp32 ILU(0)-smoothed aggregation V-cycle (``kind="amg"``)."""
+                 preconditioner=None, kind: str = "ilu",
+                 precond_options: dict | None = None) -> NewtonResult:
+    """Newton's method with FGMRES, preconditioned by ILU(0) of the materialised Jacobian
+    (``kind="ilu"``) or by an ILU(0)-smoothed aggregation V-cycle (``kind="amg"``), in fp32 or
+    fp64 (``precision``)."""
     t_all = time.perf_counter()
     s = torch.as_tensor(state0, dtype=torch.float64, device="cuda").clone()
     if preconditioner is None:
@@ -224,7 +226,7 @@ def newton_solve(case, state0, *, rtol: float = 1e-10, atol: float = 1e-12, max_
         if kind == "amg":
             from .amg import AmgPreconditioner
 
-            preconditioner = AmgPreconditioner(jac)
+            preconditioner = AmgPreconditioner(jac, precision, **(precond_options or {}))
         else:
             preconditioner = IluPreconditioner(jac, precision)
     phases = {"residual": 0.0, "precond_setup": 0.0, "krylov": 0.0, "line_search": 0.0}

@@ -226,9 +226,9 @@ int fv_aggregate(int n, const int* indptr, const int* indices, int* agg, int* n_
  * the members of every aggregate in ascending order; cip (na + 1) / cix (capacity nnz) the sorted
  * coarse pattern; gptr (capacity nnz + 1) / glist (nnz) for every coarse block the fine blocks
  * summed into it, ascending (both NULL: the pattern only); n_coarse_blocks the coarse pattern's
- * size.  No reference
- * counterpart as an entry point: the Galerkin product of the piecewise-constant aggregation
- * prolongation (aquaflux/solve/multigrid.py:1011-1245) as ordered block lists. */
+ * size.  No reference counterpart as an entry point: the Galerkin product of the
+ * piecewise-constant aggregation prolongation (aquaflux/solve/multigrid.py:1011-1245) as ordered
+ * block lists. */
 int fv_coarsen(int n, const int* indptr, const int* indices, const int* agg, int na, int* mptr,
                int* mlist, int* cip, int* cix, long* gptr, long* glist, long* n_coarse_blocks);
 /* Galerkin coarse blocks: coarse[Q] = sum of the fine blocks glist[gptr[Q] .. gptr[Q+1]) in list
@@ -240,6 +240,26 @@ int fv_restrict_f32(int n_coarse, int b, const int* mptr, const int* mlist, cons
                     float* rc, void* stream);
 /* x[i] += xc[agg[i]] (b values per cell). */
 int fv_prolong_add_f32(int n_fine, int b, const int* agg, const float* xc, float* x, void* stream);
+/* Symmetric block permutation of a pattern (host): new row r = old row perm[r], rows sorted;
+ * bmap (nnz) the old block index of every new block. */
+int fv_permute_pattern(int n, const int* indptr, const int* indices, const int* perm,
+                       int* out_indptr, int* out_indices, long* bmap);
+/* dst block q = src block bmap[q] (device; b x b entries; fp64 when *_f64 != 0, else fp32). */
+int fv_gather_blocks(long nnzb, int b, const long* bmap, const void* src, int src_f64, void* dst,
+                     int dst_f64, void* stream);
+/* Field-major fp64 state-layout vector <-> cell-major vector in a permuted cell order
+ * (perm NULL: identity): out[r * b + a] = in[a * n + perm[r]] and its inverse (device). */
+int fv_to_cells(int n, int b, const int* perm, const double* in, void* out, int out_f64,
+                void* stream);
+int fv_from_cells(int n, int b, const int* perm, const void* in, int in_f64, double* out,
+                  void* stream);
+/* The same three in fp64 (the fp64 V-cycle of the all-fp64 Newton-Krylov solve). */
+int fv_galerkin_f64(long n_coarse_blocks, int b, const long* gptr, const long* glist,
+                    const void* fine, int fine_f64, double* coarse, void* stream);
+int fv_restrict_f64(int n_coarse, int b, const int* mptr, const int* mlist, const double* r,
+                    double* rc, void* stream);
+int fv_prolong_add_f64(int n_fine, int b, const int* agg, const double* xc, double* x,
+                       void* stream);
 
 /* ------------------------------------------------------------------------------------------
  * Deterministic reductions for the Krylov solver (fixed blocking, fixed order: run-to-run

@@ -80,3 +80,29 @@ def test_cell_pattern_equals_the_reach_one_stencil():
     ref = stencil_pattern(o[keep], nb[keep], m.n_cells, 1).tocsr()
     ref.sort_indices()
     assert np.array_equal(ip, ref.indptr) and np.array_equal(ix, ref.indices)
+
+
+def test_permuted_pattern_maps_every_block():
+    """fv_permute_pattern: new block (r, c) is old block (perm[r], perm[c])."""
+    import ctypes
+
+    from aquaflux_gb300._lib import check, lib, ptr
+
+    n, ip, ix = _cell_graph(6)
+    perm = np.random.default_rng(1).permutation(n).astype(np.int32)
+    pip = np.empty(n + 1, np.int32)
+    pix = np.empty(ip[-1], np.int32)
+    bmap = np.empty(ip[-1], np.int64)
+    check(lib().fv_permute_pattern(n, ptr(ip), ptr(ix), ptr(perm), ptr(pip), ptr(pix), ptr(bmap)))
+    rows_old = np.repeat(np.arange(n), np.diff(ip))
+    rows_new = np.repeat(np.arange(n), np.diff(pip))
+    assert np.array_equal(perm[rows_new], rows_old[bmap])
+    assert np.array_equal(perm[pix], ix[bmap])
+    assert np.array_equal(np.sort(bmap), np.arange(ip[-1]))
+    for r in range(n):
+        assert np.all(np.diff(pix[pip[r]:pip[r + 1]]) > 0)
+    bad = perm.copy()
+    bad[0] = bad[1]
+    with pytest.raises(Exception):
+        check(lib().fv_permute_pattern(n, ptr(ip), ptr(ix), ptr(bad), ptr(pip), ptr(pix),
+                                       ptr(bmap)))

@@ -119,8 +119,10 @@ def test_implicit_adjoint_matches_finite_differences_of_the_solve():
     assert abs(grad - fd) <= 1e-4 * abs(fd)
 
 
-def test_amg_vcycle_is_a_fixed_linear_operator_and_converges_newton():
-    """The fp32 V-cycle is fixed-linear (tests/unit/test_host_vcycle.py:76) and, as the FGMRES
+@pytest.mark.parametrize("precision,fine_order", [(32, "colour"), (64, "colour"),
+                                                  (32, "natural")])
+def test_amg_vcycle_is_a_fixed_linear_operator_and_converges_newton(precision, fine_order):
+    """The V-cycle is fixed-linear (tests/unit/test_host_vcycle.py:76) and, as the FGMRES
     preconditioner, drives the SST channel's Newton solve to the same root as ILU(0)."""
     from aquaflux_gb300 import workloads
     from aquaflux_gb300.amg import AmgPreconditioner
@@ -129,7 +131,7 @@ def test_amg_vcycle_is_a_fixed_linear_operator_and_converges_newton():
     wl = workloads.channel3d(16)
     case = wl.device_case()
     jac = BlockJacobian(case)
-    pc = AmgPreconditioner(jac, min_cells=200)
+    pc = AmgPreconditioner(jac, precision, fine_order=fine_order, min_cells=200)
     assert len(pc.h.levels) >= 2
     s = torch.tensor(wl.initial_state(), device="cuda")
     pc.refresh(s)
@@ -138,8 +140,10 @@ def test_amg_vcycle_is_a_fixed_linear_operator_and_converges_newton():
     a = pc.apply(r1).clone()
     b = pc.apply(r2).clone()
     ab = pc.apply(2.0 * r1 - 3.0 * r2).clone()
-    assert float((ab - (2.0 * a - 3.0 * b)).abs().max()) <= 1e-4 * float(ab.abs().max())
-    res_amg = newton_solve(case, wl.initial_state(), kind="amg", max_steps=40)
+    tol = 1e-4 if precision == 32 else 1e-11
+    assert float((ab - (2.0 * a - 3.0 * b)).abs().max()) <= tol * float(ab.abs().max())
+    res_amg = newton_solve(case, wl.initial_state(), kind="amg", precision=precision,
+                           precond_options={"fine_order": fine_order}, max_steps=40)
     res_ilu = newton_solve(case, wl.initial_state(), precision=64, max_steps=40)
     assert res_amg.converged and res_ilu.converged
     sa, si = res_amg.state.cpu().numpy(), res_ilu.state.cpu().numpy()
