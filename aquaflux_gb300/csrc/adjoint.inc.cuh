@@ -40,6 +40,8 @@ struct AdjWork {
   double* dcob;  // (nc) d-coefficient adjoint
   double* clb;   // (4, nc) strain, F1, nu_t, shear-rate adjoints
   double* Gwib;  // (D, nc) imposed omega-gradient adjoint
+  double* Gb2;   // (NF, D, nc) second iterate cotangent of the corrected-gradient sweeps
+  double* Bb;    // (NF, D, nc) cotangent of the corrected scheme's right-hand side B phi
 };
 
 // ---------------------------------------------------------------- a_sum
@@ -728,8 +730,97 @@ __global__ void __launch_bounds__(128) a_closure(MeshView m, CaseView cv, Src<do
 // G_c = (1/V_c) sum_f (+-) S_f phi_f  =>  phib_f = S_f . (Gb_o / V_o - Gb_n / V_n), then each side
 // takes its interpolation weight of phib_f.  The face pass forms phib once per face (into `pb`,
 // (NF, nf)); the cell pass gathers it.
+// ---------------------------------------------------------------- corrected-gradient sweeps
+// Adjoint of the swept corrected Green-Gauss solve (gradient.py:618-705, 1122-1337).  Forward:
+// X_0 = rel B phi / V, X_i = X_{i-1} + rel (B phi - V X_{i-1} + C X_{i-1}) / V.  Backward, with
+// y = rel Xb / V per cell: Bb += y and Xb <- Xb - V y + C^T y, where
+// (C^T y)_P += (1 - g) skew wb_f, (C^T y)_N += g skew wb_f, wb_f = S_f . (y_P - y_N).
+template <int DIM, int NQ>
+__global__ void __launch_bounds__(128) a_gg_skew(MeshView m, const double* Xb, double rel,
+                                                 double* wb) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= m.nfi) return;
+  const int nc = m.nc, nf = m.nf;
+  const int o = m.owner[f], n = m.nb[f];
+  const double A = m.area[f];
+  const double ro = rel * m.inv_vol[o], rn = rel * m.inv_vol[n];
+  double S[DIM];
+#pragma unroll
+  for (int j = 0; j < DIM; ++j) S[j] = m.normal[(long)j * nf + f] * A;
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) {
+    double acc = 0.0;
+#pragma unroll
+    for (int j = 0; j < DIM; ++j)
+      acc += S[j] * (Xb[((long)q * DIM + j) * nc + o] * ro - Xb[((long)q * DIM + j) * nc + n] * rn);
+    wb[(long)q * nf + f] = acc;
+  }
+}
+
+template <int DIM, int NQ>
+__global__ void __launch_bounds__(128) a_gg_sweep(MeshView m, const double* Xb, const double* wb,
+                                                  double rel, bool first, double* Bb, double* Xbn) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nc) return;
+  const int nc = m.nc, nf = m.nf;
+  const double V = m.vol[c], r = rel * m.inv_vol[c];
+  double acc[NQ][DIM];
+#pragma unroll
+  for (int q = 0; q < NQ; ++q)
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) {
+      const long k = ((long)q * DIM + j) * nc + c;
+      const double x = Xb[k];
+      const double y = x * r;
+      Bb[k] = first ? y : Bb[k] + y;
+      acc[q][j] = x - V * y;
+    }
+  const int b = m.cf_ptr[c], e = m.cf_ptr[c + 1];
+  for (int i = b; i < e; ++i) {
+    const unsigned ent = m.cf_face[i];
+    const int f = (int)(ent & ~FV_NB_BIT);
+    if (f >= m.nfi) continue;
+    const double g = m.g[f];
+    const double wgt = (ent & FV_NB_BIT) ? g : 1.0 - g;
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+      const double t = wgt * wb[(long)q * nf + f];
+#pragma unroll
+      for (int j = 0; j < DIM; ++j) acc[q][j] += t * m.skew[(long)j * nf + f];
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < NQ; ++q)
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) Xbn[((long)q * DIM + j) * nc + c] = acc[q][j];
+}
+
+// Runs the backward sweeps from aw.Gb; returns the cotangent of the first iterate (aw.Gb or
+// aw.Gb2).  With fewer than two sweeps there is nothing to run and aw.Bb stays unused.
+template <int DIM, int NQ>
+const double* gg_sweeps_adjoint(const MeshView& m, int sweeps, double rel, const AdjWork& aw,
+                                double* wface, cudaStream_t s) {
+  constexpr int TB = 128;
+  const int bc = fv_blocks(m.nc, TB), bfi = fv_blocks(m.nfi > 0 ? m.nfi : 1, TB);
+  double* cur = aw.Gb;
+  double* nxt = aw.Gb2;
+  for (int it = 1; it < sweeps; ++it) {
+    if (m.nfi > 0) a_gg_skew<DIM, NQ><<<bfi, TB, 0, s>>>(m, cur, rel, wface);
+    a_gg_sweep<DIM, NQ><<<bc, TB, 0, s>>>(m, cur, wface, rel, it == 1, aw.Bb, nxt);
+    double* t = cur;
+    cur = nxt;
+    nxt = t;
+  }
+  return cur;
+}
+
+// Face cotangents of the Green-Gauss face values: pb_f = S_f . (nb_P - nb_N) with nb the
+// cotangent of the Green-Gauss numerator B phi, nb = rel Gb0 / V (+ Bb when swept).  Gb0 is the
+// cotangent of the first gradient iterate (the gradient itself for the compact scheme).
 template <int DIM, bool TURB>
-__global__ void __launch_bounds__(128) a_grad_face(MeshView m, CaseView cv, AdjWork aw, double* pb) {
+__global__ void __launch_bounds__(128) a_grad_face(MeshView m, CaseView cv, AdjWork aw,
+                                                   const double* Gb0, const double* Bb, double rel,
+                                                   double* pb) {
   using L = Layout<DIM, TURB>;
   constexpr int NF = L::NFLD;
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
@@ -741,6 +832,31 @@ __global__ void __launch_bounds__(128) a_grad_face(MeshView m, CaseView cv, AdjW
 #pragma unroll
   for (int j = 0; j < DIM; ++j) S[j] = m.normal[(long)j * nf + f] * A;
   const double ivo = m.inv_vol[o];
+  if (Bb || rel != 1.0) {
+    const double ro = rel * ivo;
+    const int n = f < m.nfi ? m.nb[f] : o;
+    const double rn = rel * m.inv_vol[n];
+#pragma unroll
+    for (int q = 0; q < NF; ++q) {
+      double phib = 0.0;
+#pragma unroll
+      for (int j = 0; j < DIM; ++j) {
+        const long ko = ((long)q * DIM + j) * nc + o;
+        double nbo = Gb0[ko] * ro;
+        if (Bb) nbo += Bb[ko];
+        if (f < m.nfi) {
+          const long kn = ((long)q * DIM + j) * nc + n;
+          double nbn = Gb0[kn] * rn;
+          if (Bb) nbn += Bb[kn];
+          phib += S[j] * (nbo - nbn);
+        } else {
+          phib += S[j] * nbo;
+        }
+      }
+      pb[(long)q * nf + f] = phib;
+    }
+    return;
+  }
   if (f < m.nfi) {
     const int n = m.nb[f];
     const double ivn = m.inv_vol[n];
@@ -749,8 +865,8 @@ __global__ void __launch_bounds__(128) a_grad_face(MeshView m, CaseView cv, AdjW
       double phib = 0.0;
 #pragma unroll
       for (int j = 0; j < DIM; ++j)
-        phib += S[j] * (aw.Gb[((long)q * DIM + j) * nc + o] * ivo -
-                        aw.Gb[((long)q * DIM + j) * nc + n] * ivn);
+        phib += S[j] * (Gb0[((long)q * DIM + j) * nc + o] * ivo -
+                        Gb0[((long)q * DIM + j) * nc + n] * ivn);
       pb[(long)q * nf + f] = phib;
     }
   } else {
@@ -758,7 +874,7 @@ __global__ void __launch_bounds__(128) a_grad_face(MeshView m, CaseView cv, AdjW
     for (int q = 0; q < NF; ++q) {
       double phib = 0.0;
 #pragma unroll
-      for (int j = 0; j < DIM; ++j) phib += S[j] * aw.Gb[((long)q * DIM + j) * nc + o];
+      for (int j = 0; j < DIM; ++j) phib += S[j] * Gb0[((long)q * DIM + j) * nc + o];
       pb[(long)q * nf + f] = phib * ivo;
     }
   }

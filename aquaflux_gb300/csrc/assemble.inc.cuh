@@ -143,7 +143,7 @@ int assemble_frozen(FvCase* cs, const double* state, const int* indptr, const in
   Par<Dual> par{{cs->mu, 0.0}, {cs->inlet_scale, 0.0}, {cs->mu * irho, 0.0}};
   constexpr int TB = 128;
   const int bc = fv_blocks(nc, TB), bf = fv_blocks(nf, TB);
-  k_grad<Dual, DIM, TURB><<<bc, TB, 0, s>>>(m, cv, st, par, w.G);
+  gradient_stage<Dual, DIM, TURB>(cs, st, par, w, s);
   if (TURB) k_closure<Dual, DIM><<<bc, TB, 0, s>>>(m, cv, st, par, w.G, w.cl, w.Gwi);
   k_apcoef<Dual, DIM, TURB><<<bf, TB, 0, s>>>(m, cv, st, par, w.G, w.cl, w.acown, w.acnb, w.me);
   k_dcoeff<Dual><<<bc, TB, 0, s>>>(m, w.acown, w.acnb, w.dco);

@@ -140,4 +140,10 @@ enum { FV_TAN_NONE = 0, FV_TAN_STATE = 1, FV_TAN_MU = 2, FV_TAN_INLET = 3, FV_TA
 
 // Wall distance + gradient for a turbulent case (mesh.cu).
 int fv_wall_distance_compute(FvMesh* m, const unsigned char* swall_dev, int n_wall_faces,
-                             double* wd, double* wdg, cudaStream_t s);
+                             double* wd, double* wdg, int gradient_sweeps,
+                             double gradient_relaxation, cudaStream_t s);
+// Corrected Green-Gauss sweeps of one scalar field's gradient (residual.cu): on entry x0 holds
+// rel * B phi / V and num holds B phi; the last iterate lands in x0 or x1 by the sweep count's
+// parity (x0 when sweeps - 1 is even).
+int fv_gg_sweeps_scalar(const MeshView& m, int sweeps, double rel, const double* num, double* x0,
+                        double* x1, double* wface, cudaStream_t s);

@@ -249,9 +249,10 @@ __global__ void k_gather_wall_xf(int nf, int dim, const unsigned char* swall, co
 
 // Compact Green-Gauss gradient of the wall distance with Dirichlet 0 on the SST walls and zero
 // gradient (owner value) elsewhere: aquaflux/turbulence/transport.py:86-111.
+// With num non-null (corrected scheme) num receives the numerator B d and wdg rel * B d / V.
 template <int DIM>
 __global__ void k_wall_distance_gradient(MeshView m, const unsigned char* swall, const double* wd,
-                                         double* wdg) {
+                                         double* wdg, double* num, double rel) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= m.nc) return;
   double acc[DIM];
@@ -273,7 +274,15 @@ __global__ void k_wall_distance_gradient(MeshView m, const unsigned char* swall,
     for (int j = 0; j < DIM; ++j) acc[j] += (m.normal[j * m.nf + f] * m.area[f]) * s;
   }
   double inv = 1.0 / m.vol[c];
-  for (int j = 0; j < DIM; ++j) wdg[j * m.nc + c] = acc[j] * inv;
+  if (num || rel != 1.0) {
+    const double iv = m.inv_vol[c];
+    for (int j = 0; j < DIM; ++j) {
+      if (num) num[j * m.nc + c] = acc[j];
+      wdg[j * m.nc + c] = rel * (acc[j] * iv);
+    }
+  } else {
+    for (int j = 0; j < DIM; ++j) wdg[j * m.nc + c] = acc[j] * inv;
+  }
 }
 
 thread_local char g_err[1024] = "";
@@ -329,7 +338,7 @@ int fv_mesh_compute_geometry(FvMesh* m, cudaStream_t s) {
 }
 
 int fv_wall_distance_compute(FvMesh* m, const unsigned char* swall_dev, int n_wall, double* wd,
-                             double* wdg, cudaStream_t s) {
+                             double* wdg, int sweeps, double rel, cudaStream_t s) {
   if (n_wall <= 0) {
     fv_set_error("a turbulent case needs at least one SST wall face");
     return FV_ERR_ARG;
@@ -349,18 +358,34 @@ int fv_wall_distance_compute(FvMesh* m, const unsigned char* swall_dev, int n_wa
   FV_CUDA_TRY(cudaMemcpyAsync(d_slot, slot.data(), sizeof(int) * m->nf, cudaMemcpyHostToDevice, s));
   int bf = fv_blocks(m->nf, kThreads), bc = fv_blocks(m->nc, kThreads);
   k_gather_wall_xf<<<bf, kThreads, 0, s>>>(m->nf, m->dim, swall_dev, d_slot, m->view.xf, d_wxf, k);
+  // corrected scheme: B d, the other sweep iterate and the face scratch
+  double *num = nullptr, *galt = nullptr, *wface = nullptr;
+  double* x0 = wdg;
+  if (sweeps >= 2) {
+    FV_CUDA_TRY(cudaMalloc(&num, sizeof(double) * (size_t)m->dim * m->nc));
+    FV_CUDA_TRY(cudaMalloc(&galt, sizeof(double) * (size_t)m->dim * m->nc));
+    FV_CUDA_TRY(cudaMalloc(&wface, sizeof(double) * (size_t)m->nf));
+    if ((sweeps - 1) % 2 != 0) x0 = galt;
+  }
+  const double r0 = sweeps >= 1 ? rel : 1.0;
   if (m->dim == 2) {
     k_wall_distance<2><<<bc, 256, 0, s>>>(m->view, d_wxf, k, wd);
-    k_wall_distance_gradient<2><<<bc, kThreads, 0, s>>>(m->view, swall_dev, wd, wdg);
+    k_wall_distance_gradient<2><<<bc, kThreads, 0, s>>>(m->view, swall_dev, wd, x0, num, r0);
   } else {
     k_wall_distance<3><<<bc, 256, 0, s>>>(m->view, d_wxf, k, wd);
-    k_wall_distance_gradient<3><<<bc, kThreads, 0, s>>>(m->view, swall_dev, wd, wdg);
+    k_wall_distance_gradient<3><<<bc, kThreads, 0, s>>>(m->view, swall_dev, wd, x0, num, r0);
   }
+  int rc = FV_OK;
+  if (sweeps >= 2)
+    rc = fv_gg_sweeps_scalar(m->view, sweeps, rel, num, x0, x0 == wdg ? galt : wdg, wface, s);
   FV_CUDA_TRY(cudaGetLastError());
   FV_CUDA_TRY(cudaStreamSynchronize(s));
   cudaFree(d_slot);
   cudaFree(d_wxf);
-  return FV_OK;
+  cudaFree(num);
+  cudaFree(galt);
+  cudaFree(wface);
+  return rc;
 }
 
 extern "C" int fv_mesh_create(int dim, int n_cells, int n_faces, int n_nodes, const double* nodes,

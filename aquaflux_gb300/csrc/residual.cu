@@ -165,7 +165,9 @@ struct Work {
   T* acnb;   // (nf) neighbour side
   T* dco;    // (nc) d = V / a_P
   T* me;     // (nf) lagged mass-flux estimate (rho u)_f . n A
-  T* FL;     // (NF, nf) face fluxes
+  T* FL;     // (NF, nf) face fluxes (also the face scratch of the gradient sweeps)
+  T* Bg;     // (NF, DIM, nc) corrected Green-Gauss right-hand side B phi (swept cases only)
+  T* Galt;   // (NF, DIM, nc) second iterate buffer of the sweeps (swept cases only)
 };
 template <class T, int DIM, bool TURB>
 Work<T> work_layout(void* base, long nc, long nf) {
@@ -179,13 +181,19 @@ Work<T> work_layout(void* base, long nc, long nf) {
   w.acnb = p; p += nf;
   w.dco = p; p += nc;
   w.me = p; p += nf;
-  w.FL = p;
+  w.FL = p; p += (long)NF * nf;
+  w.Bg = p; p += (long)NF * DIM * nc;
+  w.Galt = p;
   return w;
 }
 
 // ---------------------------------------------------------------- k_grad
+// G = rel * (B phi / V) with B phi the compact Green-Gauss numerator; Bg (may be null) receives
+// B phi itself (the right-hand side of the corrected scheme's sweeps).  rel = 1 and Bg = null is
+// the compact scheme.
 template <class T, int DIM, bool TURB>
-__global__ void __launch_bounds__(128) k_grad(MeshView m, CaseView cv, Src<T> st, Par<T> par, T* G) {
+__global__ void __launch_bounds__(128) k_grad(MeshView m, CaseView cv, Src<T> st, Par<T> par, T* G,
+                                              T* Bg, double rel) {
   using L = Layout<DIM, TURB>;
   constexpr int NF = L::NFLD;
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -234,10 +242,112 @@ __global__ void __launch_bounds__(128) k_grad(MeshView m, CaseView cv, Src<T> st
       for (int j = 0; j < DIM; ++j) acc[q][j] += S[j] * phif[q];
   }
   const double inv = m.inv_vol[c];
+  if (Bg) {
 #pragma unroll
-  for (int q = 0; q < NF; ++q)
+    for (int q = 0; q < NF; ++q)
 #pragma unroll
-    for (int j = 0; j < DIM; ++j) G[((long)q * DIM + j) * nc + c] = acc[q][j] * inv;
+      for (int j = 0; j < DIM; ++j) {
+        Bg[((long)q * DIM + j) * nc + c] = acc[q][j];
+        G[((long)q * DIM + j) * nc + c] = rel * (acc[q][j] * inv);
+      }
+  } else if (rel != 1.0) {
+#pragma unroll
+    for (int q = 0; q < NF; ++q)
+#pragma unroll
+      for (int j = 0; j < DIM; ++j) G[((long)q * DIM + j) * nc + c] = rel * (acc[q][j] * inv);
+  } else {
+#pragma unroll
+    for (int q = 0; q < NF; ++q)
+#pragma unroll
+      for (int j = 0; j < DIM; ++j) G[((long)q * DIM + j) * nc + c] = acc[q][j] * inv;
+  }
+}
+
+// ---------------------------------------------------------------- corrected Green-Gauss sweeps
+// CorrectedGreenGauss (aquaflux/schemes/gradient.py:1122-1337) by SweptGradientSolve
+// (gradient.py:618-705): A_g G = V G - C(G), C(G)_c = sum over the interior faces of c of
+// +-S_f w_f, w_f = (1 - g) skew . G_P + g skew . G_N; every sweep after the peeled first one is
+// X <- X + rel (B phi - A_g X) / V.  Gradients are field-major (NQ, DIM, nc).
+//
+// w_f for every field (face pass, interior faces).
+template <class T, int DIM, int NQ>
+__global__ void __launch_bounds__(128) k_gg_skew(MeshView m, const T* X, T* w) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= m.nfi) return;
+  const int nc = m.nc, nf = m.nf;
+  const int o = m.owner[f], n = m.nb[f];
+  const double g = m.g[f];
+  double sk[DIM];
+#pragma unroll
+  for (int j = 0; j < DIM; ++j) sk[j] = m.skew[(long)j * nf + f];
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) {
+    T so = sk[0] * X[((long)q * DIM) * nc + o];
+    T sn = sk[0] * X[((long)q * DIM) * nc + n];
+#pragma unroll
+    for (int j = 1; j < DIM; ++j) {
+      so = so + sk[j] * X[((long)q * DIM + j) * nc + o];
+      sn = sn + sk[j] * X[((long)q * DIM + j) * nc + n];
+    }
+    w[(long)q * nf + f] = (1.0 - g) * so + g * sn;
+  }
+}
+
+// One sweep (cell pass): Xn = X + rel (Bg - (V X - C(X))) / V.
+template <class T, int DIM, int NQ>
+__global__ void __launch_bounds__(128) k_gg_sweep(MeshView m, const T* Bg, const T* X, const T* w,
+                                                  double rel, T* Xn) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nc) return;
+  const int nc = m.nc, nf = m.nf;
+  T corr[NQ][DIM];
+  bool first = true;
+  const int b = m.cf_ptr[c], e = m.cf_ptr[c + 1];
+  for (int i = b; i < e; ++i) {
+    const unsigned ent = m.cf_face[i];
+    const int f = (int)(ent & ~FV_NB_BIT);
+    if (f >= m.nfi) continue;  // the correction vanishes on boundary faces
+    const double A = (ent & FV_NB_BIT) ? -m.area[f] : m.area[f];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+      const T wq = w[(long)q * nf + f];
+#pragma unroll
+      for (int j = 0; j < DIM; ++j) {
+        const T x = (m.normal[(long)j * nf + f] * A) * wq;
+        corr[q][j] = first ? x : corr[q][j] + x;
+      }
+    }
+    first = false;
+  }
+  const double V = m.vol[c], inv = m.inv_vol[c];
+#pragma unroll
+  for (int q = 0; q < NQ; ++q)
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) {
+      const long k = ((long)q * DIM + j) * nc + c;
+      const T x = X[k];
+      const T ax = first ? x * V : x * V - corr[q][j];
+      Xn[k] = x + rel * ((Bg[k] - ax) * inv);
+    }
+}
+
+// The swept gradients of NQ fields: on entry G0 holds rel * B phi / V and Bg holds B phi; the
+// iterates alternate between G0 and Galt so that the last one lands in G (= G0 or Galt, chosen by
+// the caller from the parity of the sweep count).
+template <class T, int DIM, int NQ>
+void gg_sweeps(const MeshView& m, int sweeps, double rel, const T* Bg, T* G0, T* Galt, T* wface,
+               cudaStream_t s) {
+  constexpr int TB = 128;
+  const int bc = fv_blocks(m.nc, TB), bfi = fv_blocks(m.nfi > 0 ? m.nfi : 1, TB);
+  T* cur = G0;
+  T* nxt = Galt;
+  for (int it = 1; it < sweeps; ++it) {
+    if (m.nfi > 0) k_gg_skew<T, DIM, NQ><<<bfi, TB, 0, s>>>(m, cur, wface);
+    k_gg_sweep<T, DIM, NQ><<<bc, TB, 0, s>>>(m, Bg, cur, wface, rel, nxt);
+    T* t = cur;
+    cur = nxt;
+    nxt = t;
+  }
 }
 
 // ---------------------------------------------------------------- k_closure (SST)
@@ -682,6 +792,26 @@ void freeze<Dual>(Dual* x, long n, cudaStream_t s) {
   k_freeze<<<fv_blocks(n, 256), 256, 0, s>>>(n, x);
 }
 
+// Every field's gradient with the case's scheme, into w.G.
+template <class T, int DIM, bool TURB>
+void gradient_stage(FvCase* cs, Src<T> st, Par<T> par, const Work<T>& w, cudaStream_t s) {
+  const MeshView& m = cs->mesh->view;
+  const CaseView& cv = cs->view;
+  constexpr int NF = Layout<DIM, TURB>::NFLD;
+  constexpr int TB = 128;
+  const int bc = fv_blocks(m.nc, TB);
+  const int sweeps = cs->desc.gradient_sweeps;
+  const double rel = sweeps >= 1 ? cs->desc.gradient_relaxation : 1.0;
+  if (sweeps <= 1) {
+    k_grad<T, DIM, TURB><<<bc, TB, 0, s>>>(m, cv, st, par, w.G, nullptr, rel);
+    return;
+  }
+  T* x0 = ((sweeps - 1) % 2 == 0) ? w.G : w.Galt;
+  T* x1 = x0 == w.G ? w.Galt : w.G;
+  k_grad<T, DIM, TURB><<<bc, TB, 0, s>>>(m, cv, st, par, x0, w.Bg, rel);
+  gg_sweeps<T, DIM, NF>(m, sweeps, rel, w.Bg, x0, x1, w.FL, s);
+}
+
 template <class T, int DIM, bool TURB>
 int run(FvCase* cs, Src<T> st, Par<T> par, double* R, double* JV, cudaStream_t s,
         bool frozen = false, bool end_profile_run = true, double* aux = nullptr) {
@@ -692,7 +822,7 @@ int run(FvCase* cs, Src<T> st, Par<T> par, double* R, double* JV, cudaStream_t s
   constexpr int TB = 128;
   const int bc = fv_blocks(nc, TB), bf = fv_blocks(nf, TB);
   fv_prof_mark(cs, 0, s);
-  k_grad<T, DIM, TURB><<<bc, TB, 0, s>>>(m, cv, st, par, w.G);
+  gradient_stage<T, DIM, TURB>(cs, st, par, w, s);
   fv_prof_mark(cs, 1, s);
   if (TURB) k_closure<T, DIM><<<bc, TB, 0, s>>>(m, cv, st, par, w.G, w.cl, w.Gwi);
   fv_prof_mark(cs, 2, s);
@@ -754,6 +884,8 @@ int run_vjp(FvCase* cs, const double* state, const double* W, double* R, double*
   aw.dcob = p; p += nc;
   aw.clb = p; p += 4 * nc;
   aw.Gwib = p; p += DIM * nc;
+  aw.Gb2 = p; p += L::NFLD * DIM * nc;  // present when the case is swept
+  aw.Bb = p;
   constexpr int TB = 128;
   const int bc = fv_blocks(nc, TB);
   a_sum<DIM, TURB><<<bc, TB, 0, s>>>(m, cv, st, par, W, cl, G, Gwi, aw);
@@ -764,7 +896,13 @@ int run_vjp(FvCase* cs, const double* state, const double* W, double* R, double*
   fv_prof_mark(cs, 9, s);
   if (TURB) a_closure<DIM><<<bc, TB, 0, s>>>(m, cv, st, par, G, cl, aw);
   fv_prof_mark(cs, 10, s);
-  a_grad_face<DIM, TURB><<<fv_blocks(nf, TB), TB, 0, s>>>(m, cv, aw, fw.FL);
+  const int sweeps = cs->desc.gradient_sweeps;
+  const double rel = sweeps >= 1 ? cs->desc.gradient_relaxation : 1.0;
+  const double* gb0 = aw.Gb;
+  if (sweeps >= 2) gb0 = gg_sweeps_adjoint<DIM, L::NFLD>(m, sweeps, rel, aw, fw.FL, s);
+  a_grad_face<DIM, TURB><<<fv_blocks(nf, TB), TB, 0, s>>>(m, cv, aw, gb0,
+                                                         sweeps >= 2 ? aw.Bb : nullptr, rel,
+                                                         fw.FL);
   a_grad<DIM, TURB><<<bc, TB, 0, s>>>(m, cv, aw, fw.FL, out);
   fv_prof_mark(cs, 11, s);
   fv_prof_end_run(cs);
@@ -776,9 +914,11 @@ bool g_const_ready = false;
 
 }  // namespace
 
-size_t fv_adjoint_work_bytes(int dim, int turb, long nc) {
+size_t fv_adjoint_work_bytes(int dim, int turb, long nc, int sweeps) {
   long nfld = dim + 1 + (turb ? 2 : 0);
-  return sizeof(double) * (size_t)(2 * nfld * nc + nfld * dim * nc + nc + 4 * nc + dim * nc);
+  long n = 2 * nfld * nc + nfld * dim * nc + nc + 4 * nc + dim * nc;
+  if (sweeps >= 1) n += 2 * nfld * dim * nc;  // the sweeps' second iterate cotangent and B phi's
+  return sizeof(double) * (size_t)n;
 }
 
 size_t fv_aux_bytes(int dim, int turb, long nf) {
@@ -794,9 +934,10 @@ int fv_case_vjp_run(FvCase* cs, const double* state, const double* W, double* R,
   return turb ? run_vjp<3, true>(cs, state, W, R, out, s) : run_vjp<3, false>(cs, state, W, R, out, s);
 }
 
-size_t fv_residual_work_bytes(int dim, int turb, long nc, long nf) {
+size_t fv_residual_work_bytes(int dim, int turb, long nc, long nf, int sweeps) {
   long nfld = dim + 1 + (turb ? 2 : 0);
   long n = nfld * dim * nc + 7 * nc + dim * nc + 3 * nf + nc + nfld * nf;
+  if (sweeps >= 2) n += 2 * nfld * dim * nc;  // B phi and the second sweep iterate
   return (size_t)n * sizeof(Dual);
 }
 
@@ -814,6 +955,16 @@ int fv_case_assemble_frozen(FvCase* cs, const double* state, const int* indptr,
                 : assemble_frozen<2, false>(cs, state, indptr, indices, values, D, s);
   return turb ? assemble_frozen<3, true>(cs, state, indptr, indices, values, D, s)
               : assemble_frozen<3, false>(cs, state, indptr, indices, values, D, s);
+}
+
+int fv_gg_sweeps_scalar(const MeshView& m, int sweeps, double rel, const double* num, double* x0,
+                        double* x1, double* wface, cudaStream_t s) {
+  if (m.dim == 2)
+    gg_sweeps<double, 2, 1>(m, sweeps, rel, num, x0, x1, wface, s);
+  else
+    gg_sweeps<double, 3, 1>(m, sweeps, rel, num, x0, x1, wface, s);
+  FV_CUDA_TRY(cudaGetLastError());
+  return FV_OK;
 }
 
 int fv_residual_init_constants() {

@@ -115,21 +115,26 @@ def case_tables(mesh: MeshData, flow_bc: dict, sst: dict | None):
 class FlowCase:
     """``MomentumContinuity`` (laminar) or ``CoupledRANS`` (k-omega SST) on the GPU.
 
-    Compact Green-Gauss gradients and first-order upwind advection; constant viscosity ``mu`` and
-    density ``rho``; optional pressure pin (``FixedValueCells`` on the continuity row).
+    First-order upwind advection; compact Green-Gauss gradients (``gradient=None``) or corrected
+    Green-Gauss by ``SweptGradientSolve`` (``gradient={"sweeps": s, "relaxation": r}``,
+    ``aquaflux/schemes/gradient.py:547-705, 1122-1337``); constant viscosity ``mu`` and density
+    ``rho``; optional pressure pin (``FixedValueCells`` on the continuity row).
     """
 
     def __init__(self, dmesh: DeviceMesh, *, mu: float, rho: float, flow_bc: dict,
                  pressure_pin: int | None = None, pressure_pin_value: float = 0.0,
-                 sst: dict | None = None):
+                 sst: dict | None = None, gradient: dict | None = None):
         self.dmesh = dmesh
         mesh = dmesh.mesh
         self.dim, self.n_cells = mesh.dim, mesh.n_cells
         self.turbulent = sst is not None
         t = case_tables(mesh, flow_bc, sst)
+        sweeps = 0 if gradient is None else int(gradient["sweeps"])
+        relax = 1.0 if gradient is None else float(gradient.get("relaxation", 1.0))
+        self.gradient = gradient
         desc = FvCaseDesc(1 if sst is not None else 0, float(mu), float(rho),
                           -1 if pressure_pin is None else int(pressure_pin),
-                          float(pressure_pin_value))
+                          float(pressure_pin_value), sweeps, relax)
         h = ctypes.c_void_p()
         arrs = [np.ascontiguousarray(t.get(k)) if t.get(k) is not None else None
                 for k in ("flow_kind", "flow_vel", "flow_p", "k_kind", "k_val", "omega_kind",

@@ -69,7 +69,8 @@ int fv_mesh_sizes(const FvMesh* mesh, int* dim, int* n_cells, int* n_faces, int*
 /* ------------------------------------------------------------------------------------------
  * Case.  Replaces MomentumContinuity.build (aquaflux/flow/momentum.py:233-293) and, with
  * turbulent = 1, SSTTurbulence.build + CoupledRANS.build (aquaflux/turbulence/transport.py:198-243,
- * coupled.py:311-340).  Schemes: compact Green-Gauss gradients, first-order upwind advection.
+ * coupled.py:311-340).  Schemes: compact or corrected (swept) Green-Gauss gradients, first-order
+ * upwind advection.
  * Boundary tables are per face in reference face order (entries of interior faces ignored):
  *   flow_kind: -1 none, 0 NoSlipWall, 1 MovingWall, 2 VelocityInlet, 3 PressureOutlet
  *   flow_vel (F, dim): the MovingWall / VelocityInlet velocity;  flow_p (F): outlet pressure
@@ -84,6 +85,12 @@ typedef struct FvCaseDesc {
   double rho;                /* density (Constant) */
   int pressure_pin;          /* cell index whose pressure row is fixed, -1 for none */
   double pressure_pin_value;
+  /* Gradient scheme: 0 = CompactGreenGauss (aquaflux/schemes/gradient.py:129-153); s >= 1 =
+   * CorrectedGreenGauss solved by SweptGradientSolve with s sweeps and the given relaxation in
+   * (0, 1] (gradient.py:547-705, 1122-1337; preconditioner InverseCellVolume).  Applies to every
+   * reconstructed gradient, the wall-distance gradient included. */
+  int gradient_sweeps;
+  double gradient_relaxation;
 } FvCaseDesc;
 
 int fv_case_create(const FvMesh* mesh, const FvCaseDesc* desc,

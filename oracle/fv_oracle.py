@@ -200,12 +200,30 @@ class Metrics:
         self.area_vector = n * geo["area"][:, None]
 
 
-def gg_gradient(m: Metrics, phi, bvals):
-    """Compact Green-Gauss, ``aquaflux/schemes/gradient.py:129-153``."""
+def gg_gradient(m: Metrics, phi, bvals, scheme=None):
+    """Compact Green-Gauss, ``aquaflux/schemes/gradient.py:129-153``; with ``scheme =
+    {"sweeps": s, "relaxation": r}`` the corrected Green-Gauss reconstruction of
+    ``CorrectedGreenGauss`` (``gradient.py:1122-1337``: operator ``A_g G = V G - C(G)`` with the
+    skewness coupling ``C``, right-hand side ``B phi`` = the compact numerator) solved by
+    ``SweptGradientSolve`` (``gradient.py:618-705``: the peeled first sweep ``x = r P^-1 B phi``,
+    then ``s - 1`` sweeps ``x += r P^-1 (B phi - A_g x)``, ``P^-1 = 1 / V``)."""
     topo = m.topo
     phi_face = topo.combine(topo.blend(phi, phi, m.g), bvals)
     gsum = topo.scatter_conservative(m.area_vector * phi_face[:, None])
-    return gsum * (1.0 / m.geo["volume"])[:, None]
+    inv_v = (1.0 / m.geo["volume"])[:, None]
+    if scheme is None or scheme["sweeps"] <= 1 and scheme.get("relaxation", 1.0) == 1.0:
+        return gsum * inv_v
+    rel = scheme.get("relaxation", 1.0)
+    vol = m.geo["volume"][:, None]
+    x = rel * (gsum * inv_v)
+    o, nb = topo.owner, topo.safe_nb
+    for _ in range(scheme["sweeps"] - 1):
+        w = (1.0 - m.g) * _dot(m.skew, x[o]) + m.g * _dot(m.skew, x[nb])
+        face = torch.where(topo.interior[:, None], m.area_vector * w[:, None],
+                           torch.zeros_like(m.area_vector))
+        ax = x * vol - topo.scatter_conservative(face)
+        x = x + rel * ((gsum - ax) * inv_v)
+    return x
 
 
 def interpolate_to_face(m: Metrics, field, grad):
@@ -247,13 +265,16 @@ def upwind_flux(m: Metrics, phi, mass_flux, bvals):
 
 
 # ----------------------------------------------------------------------------- the case
-def make_case(mesh, *, mu, rho, flow_bc, pressure_pin=None, pressure_pin_value=0.0, sst=None):
+def make_case(mesh, *, mu, rho, flow_bc, pressure_pin=None, pressure_pin_value=0.0, sst=None,
+              gradient=None):
     """Flatten a case description into per-face tables.
 
     ``mesh``: object with ``nodes, fn_offsets, fn_indices, owner, neighbour, n_cells, patches``.
     ``flow_bc``: ``{patch: ("wall",) | ("moving", U) | ("inlet", U) | ("outlet", p)}``.
     ``sst``: ``None`` or ``{"nu": float, "walls": [patches], "k": {patch: ("dirichlet", v) |
     ("zerograd",)}, "omega": {...}}``.
+    ``gradient``: ``None`` (compact Green-Gauss) or ``{"sweeps": s, "relaxation": r}`` (corrected
+    Green-Gauss by ``s`` swept sweeps).
     """
     nf = len(mesh.owner)
     dim = mesh.nodes.shape[1]
@@ -270,7 +291,7 @@ def make_case(mesh, *, mu, rho, flow_bc, pressure_pin=None, pressure_pin_value=0
             pb[faces] = float(spec[1])
     case = {"mesh": mesh, "dim": dim, "mu": float(mu), "rho": float(rho), "bc_kind": kind,
             "bc_vel": vel, "bc_p": pb, "pin": pressure_pin, "pin_value": float(pressure_pin_value),
-            "sst": None}
+            "sst": None, "gradient": gradient}
     if sst is not None:
         sc = {"nu": float(sst["nu"])}
         for fld in ("k", "omega"):
@@ -313,7 +334,7 @@ def wall_distance(case, geo) -> tuple[torch.Tensor, torch.Tensor]:
     is_wall[sc["wall_faces"]] = True
     bvals = torch.where(torch.as_tensor(is_wall), torch.zeros(topo.n_faces, dtype=T),
                         dist[topo.owner])
-    return dist, gg_gradient(m, dist, bvals)
+    return dist, gg_gradient(m, dist, bvals, case.get("gradient"))
 
 
 # ----------------------------------------------------------------------------- SST pieces
@@ -493,8 +514,9 @@ class Oracle:
         # boundary values (leading order) and gradients, momentum.py:445-529, 822-857
         bvel = self._boundary_velocity(u)
         bp = self._boundary_pressure(p)
-        grad_u = torch.stack([gg_gradient(m, u[:, i], bvel[:, i]) for i in range(dim)], dim=1)
-        grad_p = gg_gradient(m, p, bp)
+        gs = case.get("gradient")
+        grad_u = torch.stack([gg_gradient(m, u[:, i], bvel[:, i], gs) for i in range(dim)], dim=1)
+        grad_p = gg_gradient(m, p, bp, gs)
 
         visc = mu_c
         boundary_visc = None
@@ -512,9 +534,9 @@ class Oracle:
             strain = strain.index_copy(0, wc, (1.0 - wgt) * strain[wc]
                                        + wgt * log_layer_shear_rate(dist[wc], k[wc]))
             kb0 = self._scalar_bvals(k, None, sst["k_kind"], sst["k_val"], geo)
-            grad_k = gg_gradient(m, k, kb0)
+            grad_k = gg_gradient(m, k, kb0, gs)
             wb0 = self._scalar_bvals(w, None, sst["omega_kind"], sst["omega_val"], geo)
-            grad_w_rec = gg_gradient(m, w, wb0)
+            grad_w_rec = gg_gradient(m, w, wb0, gs)
             imposed = _omega_wall_gradient_live(nu[wc], dist[wc], k[wc], dgrad[wc], grad_k[wc])
             grad_w = grad_w_rec.index_copy(0, wc, imposed)
             f1 = sst_f1(k, w, nu, dist, grad_k, grad_w)

@@ -42,14 +42,21 @@ def sst_spec(dim, nu, k_in, w_in, walls):
 
 
 # (fixture file, prefix, description) of every residual case pinned by the reference.
+# Cases with a ``gradient`` entry use corrected Green-Gauss by swept sweeps (fixture "corrected").
 LAMINAR = {
     "cav8": dict(prefix="cav8_", mu=0.01, bc=CAVITY_BC, pin=0),
     "cavj": dict(prefix="cavj_", mu=0.01, bc=CAVITY_BC, pin=0),
     "lam3": dict(prefix="lam3_", mu=0.02, bc=DUCT3_BC, pin=None),
+    "ccavj": dict(prefix="ccavj_", mu=0.01, bc=CAVITY_BC, pin=0, file="corrected",
+                  gradient={"sweeps": 4, "relaxation": 1.0}),
 }
 SST = {
     "sst2": dict(prefix="sst2_", dim=2, nu=2e-5, walls=["bottom", "top"]),
     "sst3": dict(prefix="sst3_", dim=3, nu=1e-3, walls=["bottom", "top", "back", "front"]),
+    "csst2": dict(prefix="csst2_", dim=2, nu=2e-5, walls=["bottom", "top"], file="corrected",
+                  gradient={"sweeps": 4, "relaxation": 1.0}),
+    "csst3": dict(prefix="csst3_", dim=3, nu=1e-3, walls=["bottom", "top", "back", "front"],
+                  file="corrected", gradient={"sweeps": 3, "relaxation": 0.8}),
 }
 
 
@@ -59,17 +66,18 @@ def oracle_case(name: str):
 
     if name in LAMINAR:
         spec = LAMINAR[name]
-        d = golden("laminar")
+        d = golden(spec.get("file", "laminar"))
         mesh = mesh_from(d, spec["prefix"])
         case = fo.make_case(mesh, mu=spec["mu"], rho=1.0, flow_bc=spec["bc"],
-                            pressure_pin=spec["pin"])
+                            pressure_pin=spec["pin"], gradient=spec.get("gradient"))
         return case, d, spec["prefix"]
     spec = SST[name]
-    d = golden("sst")
+    d = golden(spec.get("file", "sst"))
     mesh = mesh_from(d, spec["prefix"])
     k_in, w_in = d[spec["prefix"] + "inlet"]
     fb, sst = sst_spec(spec["dim"], spec["nu"], float(k_in), float(w_in), spec["walls"])
-    case = fo.make_case(mesh, mu=spec["nu"], rho=1.0, flow_bc=fb, sst=sst)
+    case = fo.make_case(mesh, mu=spec["nu"], rho=1.0, flow_bc=fb, sst=sst,
+                        gradient=spec.get("gradient"))
     return case, d, spec["prefix"]
 
 
@@ -93,10 +101,12 @@ def device_case(name: str):
     dm = fv.DeviceMesh(m)
     if name in LAMINAR:
         spec = LAMINAR[name]
-        fc = fv.FlowCase(dm, mu=spec["mu"], rho=1.0, flow_bc=spec["bc"], pressure_pin=spec["pin"])
+        fc = fv.FlowCase(dm, mu=spec["mu"], rho=1.0, flow_bc=spec["bc"], pressure_pin=spec["pin"],
+                         gradient=spec.get("gradient"))
     else:
         spec = SST[name]
         k_in, w_in = d[p + "inlet"]
         fb, sst = sst_spec(spec["dim"], spec["nu"], float(k_in), float(w_in), spec["walls"])
-        fc = fv.FlowCase(dm, mu=spec["nu"], rho=1.0, flow_bc=fb, sst=sst)
+        fc = fv.FlowCase(dm, mu=spec["nu"], rho=1.0, flow_bc=fb, sst=sst,
+                         gradient=spec.get("gradient"))
     return fc, case, d, p

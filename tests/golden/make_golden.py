@@ -50,7 +50,8 @@ from aquaflux.flow import (  # noqa: E402
 )
 from aquaflux.mesh import graded_nodes, structured_grid_2d, structured_grid_3d  # noqa: E402
 from aquaflux.properties import Constant, PropertyModel  # noqa: E402
-from aquaflux.schemes import CompactGreenGauss  # noqa: E402
+from aquaflux.schemes import CompactGreenGauss, CorrectedGreenGauss  # noqa: E402
+from aquaflux.schemes.gradient import SweptGradientSolve  # noqa: E402
 from aquaflux.solve import ilu0 as ref_ilu0  # noqa: E402
 from aquaflux.turbulence import SSTModel, SSTTurbulence, inlet_k, inlet_omega  # noqa: E402
 from aquaflux.turbulence.coupled import CoupledRANS  # noqa: E402
@@ -111,7 +112,7 @@ def mesh_cases():
 
 
 # --------------------------------------------------------------------------- laminar flow
-def _cavity(n, perturb=0.0, seed=0, mu=0.01):
+def _cavity(n, perturb=0.0, seed=0, mu=0.01, scheme=None):
     mesh = structured_grid_2d(n, n, lx=1.0, ly=1.0, named_boundaries=True)
     if perturb:
         mesh = _with_nodes(mesh, jitter_interior_nodes(np.asarray(mesh.node_coords), (n, n),
@@ -119,7 +120,7 @@ def _cavity(n, perturb=0.0, seed=0, mu=0.01):
     geom = mesh.geometry()
     asm = MomentumContinuity.build(
         mesh, geom, PropertyModel({"viscosity": Constant(mu), "density": Constant(1.0)}),
-        CompactGreenGauss(),
+        scheme or CompactGreenGauss(),
         BoundaryConditions({"top": MovingWall(velocity=(1.0, 0.0)), "bottom": NoSlipWall(),
                             "left": NoSlipWall(), "right": NoSlipWall()}),
         advection_scheme=FirstOrderUpwind(), pressure_pin=0)
@@ -200,7 +201,8 @@ def laminar_cases():
 
 # --------------------------------------------------------------------------- k-omega SST
 def _rans(mesh, geom, dim, nu, u_in, walls, inlet="left", outlet="right", intensity=0.05,
-          length_scale=0.07):
+          length_scale=0.07, scheme=None):
+    scheme = scheme or CompactGreenGauss()
     rho = 1.0
     model = SSTModel()
     k_in = float(inlet_k(jnp.array(u_in), intensity))
@@ -214,9 +216,9 @@ def _rans(mesh, geom, dim, nu, u_in, walls, inlet="left", outlet="right", intens
     w_bc.update({w: ZeroGradient() for w in walls})
     momentum = MomentumContinuity.build(
         mesh, geom, PropertyModel({"viscosity": Constant(rho * nu), "density": Constant(rho)}),
-        CompactGreenGauss(), BoundaryConditions(flow_bc), advection_scheme=FirstOrderUpwind())
+        scheme, BoundaryConditions(flow_bc), advection_scheme=FirstOrderUpwind())
     turb = SSTTurbulence.build(
-        model, mesh, geom, CompactGreenGauss(), FirstOrderUpwind(), density=rho,
+        model, mesh, geom, scheme, FirstOrderUpwind(), density=rho,
         molecular_viscosity=jnp.full(mesh.n_cells, nu), wall_patches=list(walls),
         k_boundary=BoundaryConditions(k_bc), omega_boundary=BoundaryConditions(w_bc))
     return CoupledRANS.build(momentum, turb), turb, k_in, omega_in
@@ -282,6 +284,90 @@ def sst_cases():
     return out
 
 
+# --------------------------------------------------------------------------- corrected gradients
+def _swept(sweeps, relaxation=1.0):
+    """CorrectedGreenGauss with a fixed sweep count (``aquaflux/schemes/gradient.py:547-705,
+    1122-1337``); the convergence diagnostic is off (it only warns)."""
+    return CorrectedGreenGauss(solver=SweptGradientSolve(sweeps=sweeps, warn_tol=None,
+                                                         relaxation=relaxation))
+
+
+def corrected_cases():
+    out = {}
+    rng = np.random.default_rng(31)
+    # the standalone scheme on a jittered 2D mesh: a linear field (exact at convergence) and a
+    # random field with random boundary values, at 4 and 24 sweeps
+    m = structured_grid_2d(9, 7, lx=1.5, ly=1.0, named_boundaries=True)
+    m = _with_nodes(m, jitter_interior_nodes(np.asarray(m.node_coords), (9, 7), (1.5, 1.0),
+                                             0.2, 6))
+    geom = m.geometry()
+    out.update(_mesh_arrays("g2_", m, geom))
+    cc = np.asarray(geom.cell.centroid)
+    xf = np.asarray(geom.face.centroid)
+    lin = 0.7 + 1.3 * cc[:, 0] - 2.1 * cc[:, 1]
+    lin_b = 0.7 + 1.3 * xf[:, 0] - 2.1 * xf[:, 1]
+    phi = rng.standard_normal(m.n_cells)
+    phi_b = rng.standard_normal(len(xf))
+    out["g2_fields"] = np.stack([lin, phi])
+    out["g2_bvals"] = np.stack([lin_b, phi_b])
+    for sw, rel in ((4, 1.0), (24, 1.0), (6, 0.8)):
+        sch = _swept(sw, rel)
+        out[f"g2_grad_s{sw}"] = np.stack([
+            np.asarray(sch.gradients(jnp.asarray(f), m, geom, jnp.asarray(b)))
+            for f, b in zip(out["g2_fields"], out["g2_bvals"])])
+    # jittered cavity, 4 sweeps
+    mesh, geom, asm = _cavity(10, perturb=0.15, seed=0, scheme=_swept(4))
+    out.update(_mesh_arrays("ccavj_", mesh, geom))
+    states = [rng.standard_normal(300) * 0.3, rng.standard_normal(300)]
+    out["ccavj_states"] = np.stack(states)
+    out["ccavj_residuals"] = np.stack([np.asarray(asm.residual(jnp.asarray(s))) for s in states])
+    out.update(_flow_fields("ccavj_s0_", asm, states[0]))
+    v = rng.standard_normal(300)
+    out["ccavj_jvp_dir"] = v
+    out["ccavj_jvp_fd"] = _fd_jvp(asm.residual, states[0], v, 1e-6)
+    # 2D graded jittered SST channel, 4 sweeps (the corrected form of the backward-step physics)
+    nx, ny = 12, 8
+    yn = graded_nodes(ny, 1.0, 1.2)
+    mesh = structured_grid_2d(nx, ny, lx=4.0, ly=1.0, named_boundaries=True, y_nodes=yn)
+    mesh = _with_nodes(mesh, jitter_interior_nodes(np.asarray(mesh.node_coords), (nx, ny),
+                                                   (4.0, 1.0), 0.15, 4))
+    geom = mesh.geometry()
+    coupled, turb, k_in, omega_in = _rans(mesh, geom, 2, 2e-5, 1.0, ["bottom", "top"],
+                                          scheme=_swept(4))
+    out.update(_mesh_arrays("csst2_", mesh, geom))
+    out["csst2_y_nodes"] = np.asarray(yn)
+    out["csst2_wall_distance"] = np.asarray(turb.wall_distance)
+    out["csst2_wall_distance_gradient"] = np.asarray(turb.wall_distance_gradient)
+    out["csst2_inlet"] = np.array([k_in, omega_in])
+    n = mesh.n_cells
+    states = _rans_states(rng, n, 2, k_in, omega_in, 2, negative_k=True)
+    out["csst2_states"] = np.stack(states)
+    out["csst2_residuals"] = np.stack([np.asarray(coupled.residual(jnp.asarray(s)))
+                                       for s in states])
+    v = rng.standard_normal(5 * n)
+    scale = np.abs(states[0]) + 1e-3
+    out["csst2_jvp_dir"] = v * scale
+    out["csst2_jvp_fd"] = _fd_jvp(coupled.residual, states[0], v * scale, 1e-7)
+    # 3D duct with a bump, 3 under-relaxed sweeps
+    shape = (5, 4, 3)
+    mesh = structured_grid_3d(*shape, lx=2.0, ly=1.0, lz=1.0, named_boundaries=True)
+    mesh = _with_nodes(mesh, bump_channel_nodes_3d(shape, (2.0, 1.0, 1.0), 0.1, 0.1, 9))
+    geom = mesh.geometry()
+    walls = ["bottom", "top", "back", "front"]
+    coupled, turb, k_in, omega_in = _rans(mesh, geom, 3, 1e-3, 1.0, walls,
+                                          scheme=_swept(3, 0.8))
+    out.update(_mesh_arrays("csst3_", mesh, geom))
+    out["csst3_wall_distance"] = np.asarray(turb.wall_distance)
+    out["csst3_wall_distance_gradient"] = np.asarray(turb.wall_distance_gradient)
+    out["csst3_inlet"] = np.array([k_in, omega_in])
+    n = mesh.n_cells
+    states = _rans_states(rng, n, 3, k_in, omega_in, 2)
+    out["csst3_states"] = np.stack(states)
+    out["csst3_residuals"] = np.stack([np.asarray(coupled.residual(jnp.asarray(s)))
+                                       for s in states])
+    return out
+
+
 # --------------------------------------------------------------------------- ILU(0)
 def ilu_cases():
     import test_ilu0  # the reference's own unit test module (its fixture operator)
@@ -330,13 +416,16 @@ def colouring_cases():
     return out
 
 
+FILES = {"colouring": lambda: colouring_cases(), "meshes": lambda: mesh_cases(),
+         "laminar": lambda: laminar_cases(), "sst": lambda: sst_cases(),
+         "ilu0": lambda: ilu_cases(), "corrected": lambda: corrected_cases()}
+
+
 def main():
-    np.savez_compressed(os.path.join(HERE, "colouring.npz"), **colouring_cases())
-    np.savez_compressed(os.path.join(HERE, "meshes.npz"), **mesh_cases())
-    np.savez_compressed(os.path.join(HERE, "laminar.npz"), **laminar_cases())
-    np.savez_compressed(os.path.join(HERE, "sst.npz"), **sst_cases())
-    np.savez_compressed(os.path.join(HERE, "ilu0.npz"), **ilu_cases())
-    for f in ("colouring", "meshes", "laminar", "sst", "ilu0"):
+    """``make_golden.py REF [name ...]``: regenerate the named fixture files (default: all)."""
+    names = sys.argv[2:] or list(FILES)
+    for f in names:
+        np.savez_compressed(os.path.join(HERE, f + ".npz"), **FILES[f]())
         print(f, os.path.getsize(os.path.join(HERE, f + ".npz")))
 
 

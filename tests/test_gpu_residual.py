@@ -6,7 +6,7 @@ import pytest
 import torch
 
 from oracle import fv_oracle as fo
-from tests.cases import LAMINAR, SST, device_case, golden, mesh_data
+from tests.cases import LAMINAR, SST, device_case, golden, mesh_data, oracle_case
 
 pytestmark = pytest.mark.gpu
 ALL = list(LAMINAR) + list(SST)
@@ -61,7 +61,7 @@ def test_jvp_matches_oracle(name):
     assert _rel(r, orc.residual(torch.as_tensor(s)).numpy()) <= 1e-12
 
 
-@pytest.mark.parametrize("name", ["cav8", "lam3", "sst2", "sst3"])
+@pytest.mark.parametrize("name", ["cav8", "lam3", "sst2", "sst3", "ccavj", "csst2"])
 def test_jvp_matches_reference_finite_differences(name):
     fc, case, d, p = device_case(name)
     s = d[p + "states"][1 if name == "cav8" else 0]
@@ -69,7 +69,7 @@ def test_jvp_matches_reference_finite_differences(name):
     assert _rel(jv, d[p + "jvp_fd"]) <= 1e-7
 
 
-@pytest.mark.parametrize("name", ["cavj", "lam3", "sst2"])
+@pytest.mark.parametrize("name", ["cavj", "lam3", "sst2", "ccavj", "csst3"])
 def test_parameter_jvp_matches_oracle(name):
     fc, case, d, p = device_case(name)
     orc = fo.Oracle(case)
@@ -99,7 +99,7 @@ def test_zero_state_jvp_uses_the_tie_rule():
     assert np.abs(jv - central).max() <= 1e-6 * np.abs(central).max()
 
 
-@pytest.mark.parametrize("name", ["cav8", "sst3"])
+@pytest.mark.parametrize("name", ["cav8", "sst3", "csst3"])
 def test_run_to_run_bitwise_identical(name):
     fc, case, d, p = device_case(name)
     s = d[p + "states"][0]
@@ -163,7 +163,7 @@ def test_vjp_is_the_transpose_of_jvp_on_gpu(name):
     assert abs(lhs - rhs) <= 1e-12 * scale
 
 
-@pytest.mark.parametrize("name", ["cavj", "lam3", "sst2", "sst3"])
+@pytest.mark.parametrize("name", ["cavj", "lam3", "sst2", "sst3", "ccavj", "csst2", "csst3"])
 def test_param_vjp_matches_oracle(name):
     fc, case, d, p = device_case(name)
     orc = fo.Oracle(case)
@@ -193,3 +193,37 @@ def test_vjp_at_negative_k_and_zero_state():
     lhs = float(np.dot(w, fc0.jvp(z, v).cpu().numpy()))
     rhs = float(np.dot(fc0.vjp(z, w).cpu().numpy(), v))
     assert abs(lhs - rhs) <= 1e-12 * max(1.0, abs(lhs))
+
+
+@pytest.mark.parametrize("sweeps,relax", [(1, 1.0), (1, 0.7), (2, 1.0), (5, 0.8), (24, 1.0)])
+def test_corrected_gradient_sweep_counts(sweeps, relax):
+    """Odd and even sweep counts, the peel alone and under-relaxation: residual, JVP and VJP against
+    the oracle on the jittered cavity (the ping-pong of the sweep iterates ends in the right
+    buffer for every count)."""
+    from aquaflux_gb300 import fv
+
+    case, d, p = oracle_case("cavj")
+    case = dict(case, gradient={"sweeps": sweeps, "relaxation": relax})
+    fc = fv.FlowCase(fv.DeviceMesh(mesh_data(d, p)), mu=0.01, rho=1.0,
+                     flow_bc=LAMINAR["cavj"]["bc"], pressure_pin=0,
+                     gradient={"sweeps": sweeps, "relaxation": relax})
+    orc = fo.Oracle(case)
+    s = d[p + "states"][1]
+    assert _rel(fc.residual(s), orc.residual(torch.as_tensor(s)).numpy()) <= 1e-12
+    rng = np.random.default_rng(sweeps)
+    v = rng.standard_normal(s.size)
+    assert _rel(fc.jvp(s, v), orc.jvp(s, v).numpy()) <= 1e-11
+    w = rng.standard_normal(s.size)
+    assert _rel(fc.vjp(s, w), orc.vjp(s, w).numpy()) <= 1e-11
+
+
+def test_corrected_scheme_rejects_bad_relaxation():
+    from aquaflux_gb300 import fv
+    from aquaflux_gb300._lib import FvError
+
+    case, d, p = oracle_case("cavj")
+    dm = fv.DeviceMesh(mesh_data(d, p))
+    for bad in ({"sweeps": 3, "relaxation": 0.0}, {"sweeps": 3, "relaxation": 1.5},
+                {"sweeps": -1, "relaxation": 1.0}):
+        with pytest.raises(FvError):
+            fv.FlowCase(dm, mu=0.01, rho=1.0, flow_bc=LAMINAR["cavj"]["bc"], gradient=bad)

@@ -34,7 +34,7 @@ def test_residual_matches_reference(name):
         assert np.abs(r - ref).max() <= 1e-13 * np.abs(ref).max()
 
 
-@pytest.mark.parametrize("name", ["cav8", "cavj", "lam3", "sst2", "sst3"])
+@pytest.mark.parametrize("name", ["cav8", "cavj", "lam3", "sst2", "sst3", "ccavj", "csst2"])
 def test_jvp_matches_reference_finite_differences(name):
     case, d, p = oracle_case(name)
     orc = fo.Oracle(case)
@@ -75,3 +75,30 @@ def test_vjp_is_the_transpose_of_jvp():
     lhs = float(np.dot(w, orc.jvp(state, v).numpy()))
     rhs = float(np.dot(orc.vjp(state, w).numpy(), v))
     assert abs(lhs - rhs) <= 1e-10 * abs(lhs)
+
+
+@pytest.mark.parametrize("sweeps,relax", [(4, 1.0), (24, 1.0), (6, 0.8)])
+def test_corrected_gradient_matches_reference(sweeps, relax):
+    """CorrectedGreenGauss + SweptGradientSolve on a jittered mesh, for a linear field (exact at
+    convergence: 24 sweeps) and a random field with random boundary values."""
+    d = golden("corrected")
+    mesh = mesh_from(d, "g2_")
+    topo = fo.Topology(mesh.owner, mesh.neighbour, mesh.n_cells, mesh.fn_offsets, mesh.fn_indices)
+    m = fo.Metrics(topo, fo.geometry(topo, torch.as_tensor(mesh.nodes)))
+    for f, b, ref in zip(d["g2_fields"], d["g2_bvals"], d[f"g2_grad_s{sweeps}"]):
+        g = fo.gg_gradient(m, torch.as_tensor(f), torch.as_tensor(b),
+                           {"sweeps": sweeps, "relaxation": relax}).numpy()
+        assert np.abs(g - ref).max() <= 1e-13 * np.abs(ref).max()
+    if sweeps == 24:
+        np.testing.assert_allclose(d["g2_grad_s24"][0], np.tile([1.3, -2.1], (mesh.n_cells, 1)),
+                                   rtol=0, atol=1e-13)
+
+
+def test_corrected_intermediate_fields_match_reference():
+    case, d, p = oracle_case("ccavj")
+    orc = fo.Oracle(case)
+    _, f = orc.residual(torch.as_tensor(d[p + "states"][0]), return_fields=True)
+    for key in ("grad_u", "grad_p", "mdot", "a_p", "bvel", "bp"):
+        ref = d["ccavj_s0_" + key]
+        np.testing.assert_allclose(f[key].numpy(), ref, rtol=0,
+                                   atol=1e-13 * max(1.0, np.abs(ref).max()))
