@@ -269,3 +269,104 @@ def cell_adjacency_csr(mesh: MeshData) -> tuple[np.ndarray, np.ndarray]:
     indptr = np.zeros(mesh.n_cells + 1, dtype=np.int64)
     np.add.at(indptr, rows + 1, 1)
     return np.cumsum(indptr).astype(np.int32), cols.astype(np.int32)
+
+
+def remove_cells(mesh: MeshData, keep: np.ndarray, patch: str) -> MeshData:
+    """The sub-mesh of the cells with ``keep[c]``; kept cells are renumbered in order, faces keep
+    their order.  Interior faces between a kept and a removed cell become boundary faces of the
+    kept cell in the new patch ``patch``; faces touching no kept cell are dropped, and so are the
+    nodes no remaining face references."""
+    keep = np.asarray(keep, dtype=bool)
+    new_id = np.full(mesh.n_cells, -1, dtype=np.int64)
+    new_id[keep] = np.arange(int(keep.sum()))
+    o = mesh.owner.astype(np.int64)
+    nb = mesh.neighbour.astype(np.int64)
+    ko = keep[o]
+    kn = np.where(nb >= 0, keep[np.clip(nb, 0, None)], False)
+    live = ko | kn
+    owner = np.where(ko, new_id[o], new_id[np.clip(nb, 0, None)])
+    neighbour = np.where(ko & kn, new_id[np.clip(nb, 0, None)], -1)
+    exposed = (nb >= 0) & (ko ^ kn)
+    face_ids = np.flatnonzero(live)
+    remap = np.full(mesh.n_faces, -1, dtype=np.int64)
+    remap[face_ids] = np.arange(face_ids.size)
+    counts = np.diff(mesh.fn_offsets)
+    rows = np.repeat(np.arange(mesh.n_faces), counts)
+    fn = mesh.fn_indices[live[rows]]
+    used = np.zeros(mesh.n_nodes, dtype=bool)
+    used[fn] = True
+    node_id = np.cumsum(used) - 1
+    patches = {}
+    for name, faces in mesh.patches.items():
+        faces = np.asarray(faces, dtype=np.int64)
+        kept = faces[live[faces]]
+        patches[name] = remap[kept].astype(np.int32)
+    patches[patch] = remap[np.flatnonzero(exposed)].astype(np.int32)
+    return MeshData(
+        nodes=np.ascontiguousarray(mesh.nodes[used]),
+        fn_offsets=np.concatenate([[0], np.cumsum(counts[live])]).astype(np.int32),
+        fn_indices=node_id[fn].astype(np.int32),
+        owner=owner[live].astype(np.int32),
+        neighbour=neighbour[live].astype(np.int32),
+        n_cells=int(keep.sum()),
+        patches=patches,
+    ).validate()
+
+
+def backward_step_2d(*, n_step: int = 48, n_channel: int = 96, n_upstream: int = 120,
+                     n_downstream: int = 1300, step: float = 0.5, height: float = 1.5,
+                     upstream: float = 5.0, downstream: float = 25.0, ratio_y: float = 8.0,
+                     ratio_upstream: float = 5.0, ratio_downstream: float = 20.0,
+                     jitter: float = 0.15, seed: int = 0) -> MeshData:
+    """Two-block quad mesh of a backward-facing step (the reference ships no generator for it).
+
+    The inlet channel ``[-upstream, 0] x [step, height]`` opens at ``x = 0`` into the channel
+    ``[0, downstream] x [0, height]``; with ``height = 1.5`` and ``step = 0.5`` the inlet height is
+    1 (the length unit ``h``) and the expansion ratio ``height / (height - step)`` is 1.5 on a
+    ``30h x 1.5h`` domain.  Node lines are graded (:func:`graded_nodes`, geometric ``growth``)
+    toward the walls, the step corner line ``y = step`` and the step face ``x = 0``, each block's
+largest to smallest spacing being the given ``ratio_*``.  Every node
+    strictly inside the fluid is displaced by a seeded uniform ``+-jitter`` of its local spacing
+    per axis (the smaller of the two adjacent spacings).  Patches: ``inlet``, ``outlet``, ``top``,
+    ``bottom`` (the lower wall downstream of the step) and ``step`` (the step face and the inlet
+    channel's lower wall).
+    """
+    def growth(ratio, n_cells):  # geometric growth reaching `ratio` over n_cells cells
+        return float(ratio) ** (1.0 / max(n_cells - 1, 1))
+
+    y = np.concatenate([graded_nodes(n_step, step, growth(ratio_y, (n_step + 1) // 2)),
+                        step + graded_nodes(n_channel, height - step,
+                                            growth(ratio_y, (n_channel + 1) // 2))[1:]])
+    # cells shrink toward the step face x = 0 on both sides of it
+    x_up = -graded_nodes(n_upstream, upstream, growth(ratio_upstream, n_upstream),
+                         both_sides=False)[::-1]
+    x_down = graded_nodes(n_downstream, downstream, growth(ratio_downstream, n_downstream),
+                          both_sides=False)
+    x = np.concatenate([x_up, x_down[1:]])
+    nx, ny = x.size - 1, y.size - 1
+    full = structured_grid_2d(nx, ny, x_nodes=x, y_nodes=y)
+    # jitter the strictly interior nodes of the full lattice by the local spacing
+    rng = np.random.default_rng(seed)
+    jj, ii = np.meshgrid(np.arange(ny + 1), np.arange(nx + 1), indexing="ij")
+    dx, dy = np.diff(x), np.diff(y)
+    hx = np.minimum(np.concatenate([[dx[0]], dx]), np.concatenate([dx, [dx[-1]]]))
+    hy = np.minimum(np.concatenate([[dy[0]], dy]), np.concatenate([dy, [dy[-1]]]))
+    ux = rng.uniform(-jitter, jitter, jj.shape)
+    uy = rng.uniform(-jitter, jitter, jj.shape)
+    xn, yn = x[ii], y[jj]
+    inside = (ii > 0) & (ii < nx) & (jj > 0) & (jj < ny)
+    on_step = (xn <= 0.0) & (yn <= step)  # the step's faces and the removed block
+    free = inside & ~on_step
+    nodes = full.nodes.copy()
+    nodes[:, 0] += (free * ux * hx[ii]).ravel()
+    nodes[:, 1] += (free * uy * hy[jj]).ravel()
+    full = full.with_nodes(nodes)
+    ci, cj = np.meshgrid(np.arange(nx), np.arange(ny), indexing="ij")
+    cell = (cj * nx + ci).ravel()
+    keep = np.ones(nx * ny, dtype=bool)
+    in_step = (x[ci + 1] <= 0.0) & (y[cj + 1] <= step)
+    keep[cell[in_step.ravel()]] = False
+    mesh = remove_cells(full, keep, "step")
+    mesh.patches["inlet"] = mesh.patches.pop("left")
+    mesh.patches["outlet"] = mesh.patches.pop("right")
+    return mesh

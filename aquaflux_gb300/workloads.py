@@ -11,6 +11,11 @@ perturbations and a case description, built the same way on every machine.
   Cuthill-McKee; coupled (u, v, w, p) + k-omega SST, velocity inlet (u = 1, turbulence intensity
   5 %, length scale 0.07), pressure outlet, four no-slip walls.  128^3 is the 2,097,152-cell case
   (6,340,608 faces).
+* :func:`backward_step` -- 2D backward-facing step (:func:`aquaflux_gb300.mesh.backward_step_2d`:
+  inlet height h = 1, step 0.5 h, expansion ratio 1.5, a 30h x 1.5h domain, ~200k quads graded to
+  the walls, interior nodes jittered +-0.15 of the local spacing), coupled (u, v, p) + k-omega SST
+  at Re_h = 5e4 (nu = 2e-5, inlet u = 1, intensity 5 %), corrected Green-Gauss gradients by four
+  swept sweeps.
 """
 from __future__ import annotations
 
@@ -44,6 +49,7 @@ class Workload:
     sst: dict | None
     k_in: float = 0.0
     omega_in: float = 0.0
+    gradient: dict | None = None
 
     @property
     def n_unknowns(self) -> int:
@@ -70,7 +76,7 @@ class Workload:
 
         dm = fv.DeviceMesh(self.mesh)
         return fv.FlowCase(dm, mu=self.mu, rho=self.rho, flow_bc=self.flow_bc,
-                           pressure_pin=self.pressure_pin, sst=self.sst)
+                           pressure_pin=self.pressure_pin, sst=self.sst, gradient=self.gradient)
 
 
 def cavity(n: int = 64, mu: float = 0.01, lid: float = 1.0) -> Workload:
@@ -112,3 +118,22 @@ def channel3d(nx: int = 128, ny: int | None = None, nz: int | None = None, *, nu
     wb.update({w: ("zerograd",) for w in walls})
     sst = {"walls": walls, "k": kb, "omega": wb}
     return Workload(f"channel3d_{nx}x{ny}x{nz}_sst", m, nu, 1.0, flow_bc, None, sst, k_in, w_in)
+
+
+def backward_step(*, n_step: int = 48, n_channel: int = 96, n_upstream: int = 120,
+                  n_downstream: int = 1300, nu: float = 2e-5, seed: int = 0,
+                  sweeps: int = 4) -> Workload:
+    m = fm.backward_step_2d(n_step=n_step, n_channel=n_channel, n_upstream=n_upstream,
+                            n_downstream=n_downstream, seed=seed)
+    k_in = inlet_k(1.0, 0.05)
+    w_in = inlet_omega(k_in, 0.07)
+    walls = ["bottom", "top", "step"]
+    flow_bc = {"inlet": ("inlet", (1.0, 0.0)), "outlet": ("outlet", 0.0)}
+    flow_bc.update({w: ("wall",) for w in walls})
+    kb = {"inlet": ("dirichlet", k_in), "outlet": ("zerograd",)}
+    kb.update({w: ("dirichlet", 0.0) for w in walls})
+    wb = {"inlet": ("dirichlet", w_in), "outlet": ("zerograd",)}
+    wb.update({w: ("zerograd",) for w in walls})
+    sst = {"walls": walls, "k": kb, "omega": wb}
+    return Workload(f"backward_step_{m.n_cells}_sst", m, nu, 1.0, flow_bc, None, sst, k_in, w_in,
+                    gradient={"sweeps": sweeps, "relaxation": 1.0} if sweeps else None)

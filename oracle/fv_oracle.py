@@ -323,11 +323,17 @@ def wall_distance(case, geo) -> tuple[torch.Tensor, torch.Tensor]:
     topo = Topology(mesh.owner, mesh.neighbour, mesh.n_cells, mesh.fn_offsets, mesh.fn_indices)
     cc = geo["cell_centroid"].detach().numpy()
     tgt = geo["face_centroid"].detach().numpy()[sc["wall_faces"]]
-    best = np.full(cc.shape[0], np.inf)
-    for start in range(0, tgt.shape[0], 256):
-        blk = tgt[start:start + 256]
-        d2 = ((cc[:, None, :] - blk[None, :, :]) ** 2).sum(-1)
-        best = np.minimum(best, d2.min(axis=1))
+    if cc.shape[0] * tgt.shape[0] <= 5e7:
+        best = np.full(cc.shape[0], np.inf)
+        for start in range(0, tgt.shape[0], 256):
+            blk = tgt[start:start + 256]
+            d2 = ((cc[:, None, :] - blk[None, :, :]) ** 2).sum(-1)
+            best = np.minimum(best, d2.min(axis=1))
+    else:  # large meshes: the nearest wall face by a k-d tree, the distance recomputed as above
+        from scipy.spatial import cKDTree
+
+        _, idx = cKDTree(tgt).query(cc, k=1)
+        best = ((cc - tgt[idx]) ** 2).sum(-1)
     dist = torch.as_tensor(np.sqrt(best), dtype=T)
     m = Metrics(topo, {k: v.detach() for k, v in geo.items()})
     is_wall = np.zeros(topo.n_faces, dtype=bool)

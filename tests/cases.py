@@ -110,3 +110,15 @@ def device_case(name: str):
         fc = fv.FlowCase(dm, mu=spec["nu"], rho=1.0, flow_bc=fb, sst=sst,
                          gradient=spec.get("gradient"))
     return fc, case, d, p
+
+
+def workload_oracle_case(wl):
+    """The oracle's case dict for a :class:`aquaflux_gb300.workloads.Workload`."""
+    from oracle import fv_oracle as fo
+
+    sst = None
+    if wl.sst is not None:
+        sst = {"nu": wl.mu / wl.rho, "walls": wl.sst["walls"], "k": wl.sst["k"],
+               "omega": wl.sst["omega"]}
+    return fo.make_case(wl.mesh, mu=wl.mu, rho=wl.rho, flow_bc=wl.flow_bc,
+                        pressure_pin=wl.pressure_pin, sst=sst, gradient=wl.gradient)

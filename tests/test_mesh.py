@@ -79,3 +79,36 @@ def test_validate_rejects_bad_topology():
     bad.owner[0] = m.n_cells
     with pytest.raises(ValueError):
         bad.validate()
+
+
+def test_backward_step_mesh():
+    """The two-block backward-facing-step generator: closed cells of positive volume filling the
+    30h x 1.5h domain less the step, every boundary face in exactly one patch, seeded jitter."""
+    import torch
+
+    from aquaflux_gb300.mesh import backward_step_2d
+    from oracle import fv_oracle as fo
+
+    m = backward_step_2d(n_step=6, n_channel=8, n_upstream=6, n_downstream=20)
+    assert m.n_cells == 8 * 26 + 6 * 20
+    topo = fo.Topology(m.owner, m.neighbour, m.n_cells, m.fn_offsets, m.fn_indices)
+    geo = fo.geometry(topo, torch.as_tensor(m.nodes))
+    vol = geo["volume"].numpy()
+    assert vol.min() > 0 and abs(vol.sum() - (30.0 * 1.5 - 5.0 * 0.5)) <= 1e-12
+    bnd = np.flatnonzero(m.neighbour < 0)
+    allp = np.concatenate([m.patches[k] for k in ("inlet", "outlet", "top", "bottom", "step")])
+    assert np.array_equal(np.sort(allp), bnd)
+    assert len(m.patches["step"]) == 6 + 6 and len(m.patches["inlet"]) == 8
+    # closed cells: the area vectors of each cell's faces sum to zero
+    s = (geo["normal"] * geo["area"][:, None]).numpy()
+    tot = np.zeros((m.n_cells, 2))
+    np.add.at(tot, m.owner, s)
+    inner = m.neighbour >= 0
+    np.add.at(tot, m.neighbour[inner], -s[inner])
+    assert np.abs(tot).max() <= 1e-13
+    again = backward_step_2d(n_step=6, n_channel=8, n_upstream=6, n_downstream=20)
+    assert np.array_equal(again.nodes, m.nodes)
+    other = backward_step_2d(n_step=6, n_channel=8, n_upstream=6, n_downstream=20, seed=1)
+    assert not np.array_equal(other.nodes, m.nodes)
+    full = backward_step_2d()
+    assert 190_000 <= full.n_cells <= 210_000
