@@ -48,6 +48,7 @@ SIGNATURES = {
     "fv_jvp_shift": (c_int, [P, P, P, P, P, P]),
     "fv_jvp_frozen": (c_int, [P, P, P, P, P]),
     "fv_probe_jacobian": (c_int, [P, P, c_int, P, c_int, P, P, P, P]),
+    "fv_jvp_batch": (c_int, [P, P, P, c_int, P, P]),
     "fv_assemble_jacobian": (c_int, [P, P, P, P, P, P]),
     "fv_param_jvp": (c_int, [P, P, P, P, P]),
     "fv_vjp": (c_int, [P, P, P, P, P, P]),
@@ -71,8 +72,11 @@ SIGNATURES = {
     "fv_galerkin_f64": (c_int, [c_long, c_int, P, P, P, c_int, P, P]),
     "fv_permute_pattern": (c_int, [c_int, P, P, P, P, P, P]),
     "fv_gather_blocks": (c_int, [c_long, c_int, P, P, c_int, P, c_int, P]),
-    "fv_to_cells": (c_int, [c_int, c_int, P, P, P, c_int, P]),
-    "fv_from_cells": (c_int, [c_int, c_int, P, P, c_int, P, P]),
+    "fv_to_cells": (c_int, [c_int, c_int, P, P, P, P, c_int, P]),
+    "fv_from_cells": (c_int, [c_int, c_int, P, P, P, c_int, P, P]),
+    "fv_bsr_transpose_map": (c_int, [c_int, P, P, P, P, P]),
+    "fv_bsr_spmv_t_mapped": (c_int, [c_int, c_int, P, P, P, P, P, P, c_int, P]),
+    "fv_bsr_shift_equilibrate": (c_int, [c_int, c_int, P, P, P, P, c_int, P, P, P, c_int, P]),
     "fv_restrict_f64": (c_int, [c_int, c_int, P, P, P, P, P]),
     "fv_prolong_add_f64": (c_int, [c_int, c_int, P, P, P, P]),
 }

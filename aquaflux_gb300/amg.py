@@ -46,11 +46,25 @@ class _Level:
         self.t = torch.zeros_like(self.x)
         self.rhs = torch.zeros_like(self.x)  # right-hand side when this is a coarse level
         self.coarse = None  # transfer data to the next level
+        self._tmap = None  # transpose map, built on the first transposed product
 
-    def spmv(self, x, y):
-        check(getattr(lib(), "fv_bsr_spmv_" + self.sfx)(
-            self.n, self.b, ptr(self.d_indptr), ptr(self.d_indices), ptr(self.values), ptr(x),
-            ptr(y), 0, _stream()))
+    def spmv(self, x, y, transpose: bool = False):
+        if not transpose:
+            check(getattr(lib(), "fv_bsr_spmv_" + self.sfx)(
+                self.n, self.b, ptr(self.d_indptr), ptr(self.d_indices), ptr(self.values), ptr(x),
+                ptr(y), 0, _stream()))
+            return
+        if self._tmap is None:
+            tp = np.empty(self.n + 1, dtype=np.int32)
+            ti = np.empty(self.nnzb, dtype=np.int32)
+            tb = np.empty(self.nnzb, dtype=np.int32)
+            check(lib().fv_bsr_transpose_map(self.n, ptr(self.indptr), ptr(self.indices), ptr(tp),
+                                             ptr(ti), ptr(tb)))
+            self._tmap = [torch.tensor(a, device="cuda") for a in (tp, ti, tb)]
+        tp, ti, tb = self._tmap
+        check(lib().fv_bsr_spmv_t_mapped(self.n, self.b, ptr(tp), ptr(ti), ptr(tb),
+                                         ptr(self.values), ptr(x), ptr(y),
+                                         int(self.sfx == "f64"), _stream()))
 
 
 def plan_hierarchy(n, indptr, indices, *, min_cells: int = 4000, max_levels: int = 10,
@@ -156,34 +170,37 @@ class AmgHierarchy:
                            ptr(coarse.values), _stream()))
             coarse.ilu.refactor(coarse.values)
 
-    def _smooth(self, lv, b_vec, x, sweeps, from_zero):
+    def _smooth(self, lv, b_vec, x, sweeps, from_zero, transpose=False):
         if from_zero:
-            lv.ilu.solve(b_vec, out=x)
+            lv.ilu.solve(b_vec, transpose=transpose, out=x)
             sweeps -= 1
         for _ in range(sweeps):
-            lv.spmv(x, lv.t)
+            lv.spmv(x, lv.t, transpose)
             torch.sub(b_vec, lv.t, out=lv.r)
-            lv.ilu.solve(lv.r, out=lv.t)
+            lv.ilu.solve(lv.r, transpose=transpose, out=lv.t)
             x.add_(lv.t)
 
-    def vcycle(self, level: int, b_vec: torch.Tensor) -> torch.Tensor:
+    def vcycle(self, level: int, b_vec: torch.Tensor, transpose: bool = False) -> torch.Tensor:
+        """One V-cycle from a zero guess; ``transpose`` gives its exact transpose, the same cycle
+        on ``A^T`` with transposed ILU(0) smoothers (the pre- and post-smoother coincide and
+        ``R = P^T``), as the reference's V-cycle transpose (``ilu_inverse.py:275-308``)."""
         lv = self.levels[level]
         x = lv.x
         if level == len(self.levels) - 1:
-            self._smooth(lv, b_vec, x, self.coarse_sweeps, True)
+            self._smooth(lv, b_vec, x, self.coarse_sweeps, True, transpose)
             return x
-        self._smooth(lv, b_vec, x, self.sweeps, True)
-        lv.spmv(x, lv.t)
+        self._smooth(lv, b_vec, x, self.sweeps, True, transpose)
+        lv.spmv(x, lv.t, transpose)
         torch.sub(b_vec, lv.t, out=lv.r)
         coarse = self.levels[level + 1]
         t = lv.coarse
         bc = coarse.rhs
         check(getattr(lib(), "fv_restrict_" + self.sfx)(
             coarse.n, self.b, ptr(t["mptr"]), ptr(t["mlist"]), ptr(lv.r), ptr(bc), _stream()))
-        xc = self.vcycle(level + 1, bc)
+        xc = self.vcycle(level + 1, bc, transpose)
         check(getattr(lib(), "fv_prolong_add_" + self.sfx)(
             lv.n, self.b, ptr(t["agg"]), ptr(xc), ptr(x), _stream()))
-        self._smooth(lv, b_vec, x, self.sweeps, False)
+        self._smooth(lv, b_vec, x, self.sweeps, False, transpose)
         return x
 
 
@@ -197,7 +214,10 @@ class AmgPreconditioner:
     operator's own cell order.
     """
 
-    def __init__(self, jac, precision: int = 32, *, fine_order: str = "colour", **kw):
+    def __init__(self, jac, precision: int = 32, *, fine_order: str = "colour", shift=None,
+                 equilibrate: bool = False, **kw):
+        from .solve import ShiftedCellMajorOperator
+
         self.jac = jac
         n, b = jac.n, jac.b
         self._perm = self._bmap = None
@@ -219,18 +239,46 @@ class AmgPreconditioner:
             indptr, indices = pip, pix
         elif fine_order != "natural":
             raise ValueError(f"fine_order must be 'colour' or 'natural', got {fine_order!r}")
+        self.precision = precision
+        self.shift = None if shift is None else torch.as_tensor(shift, dtype=torch.float64,
+                                                                device="cuda")
+        self.op = (ShiftedCellMajorOperator(jac, equilibrate=equilibrate, precision=64)
+                   if (shift is not None or equilibrate) else None)
         self.h = AmgHierarchy(n, b, indptr, indices, precision=precision, **kw)
         self._f64 = int(precision == 64)
         self._b = torch.empty(n * b, dtype=self.h.levels[0].x.dtype, device="cuda")
 
-    def refresh(self, state: torch.Tensor) -> None:
-        self.h.refresh(self.jac.materialize(state), self._bmap)
+    def _form(self, values):
+        if self.op is not None:
+            values, _ = self.op.assemble(values, self.shift)
+        self.h.refresh(values, self._bmap)
 
-    def apply(self, r: torch.Tensor) -> torch.Tensor:
+    def refresh(self, state: torch.Tensor) -> None:
+        self._form(self.jac.materialize(state))
+
+    def reshift(self, shift) -> None:
+        """New shift on the last materialised Jacobian: re-form the hierarchy without
+        re-materialising (the beta-only refresh of ``amg_preconditioner.py:909-948``)."""
+        from .solve import ShiftedCellMajorOperator
+
+        if self.op is None:
+            self.op = ShiftedCellMajorOperator(self.jac, equilibrate=False, precision=64)
+        self.shift = None if shift is None else torch.as_tensor(shift, dtype=torch.float64,
+                                                                device="cuda")
+        self._form(self.jac.values)
+
+    def apply(self, r: torch.Tensor, transpose: bool = False) -> torch.Tensor:
         n, b = self.jac.n, self.jac.b
-        check(lib().fv_to_cells(n, b, ptr(self._perm), ptr(r), ptr(self._b), self._f64,
-                                _stream()))
-        x = self.h.vcycle(0, self._b)
+        scale = None if self.op is None else self.op.scale
+        check(lib().fv_to_cells(n, b, ptr(self._perm), ptr(scale), ptr(r), ptr(self._b),
+                                self._f64, _stream()))
+        x = self.h.vcycle(0, self._b, transpose)
         out = torch.empty(n * b, dtype=torch.float64, device="cuda")
-        check(lib().fv_from_cells(n, b, ptr(self._perm), ptr(x), self._f64, ptr(out), _stream()))
+        check(lib().fv_from_cells(n, b, ptr(self._perm), ptr(scale), ptr(x), self._f64, ptr(out),
+                                  _stream()))
         return out
+
+    def apply_transpose(self, r: torch.Tensor) -> torch.Tensor:
+        """``M^T r``: the transposed V-cycle between the same (diagonal) scalings and the same
+        (orthogonal) cell permutation."""
+        return self.apply(r, transpose=True)

@@ -189,25 +189,27 @@ __global__ void k_gather_blocks(long nnzb, int bb, const long* bmap, const In* s
   dst[t] = (Out)src[bmap[q] * bb + e];
 }
 
-// Field-major fp64 vector -> cell-major Out vector in the permuted cell order:
-//   out[r * b + a] = in[a * n + perm[r]]   (perm NULL: identity)
+// Field-major fp64 vector -> cell-major Out vector in the permuted cell order, scaled:
+//   out[r * b + a] = in[a * n + perm[r]] * scale[a * n + perm[r]]   (perm / scale NULL: none)
 template <class Out>
-__global__ void k_to_cells(int n, int b, const int* perm, const double* in, Out* out) {
+__global__ void k_to_cells(int n, int b, const int* perm, const double* scale, const double* in,
+                           Out* out) {
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (long)n * b) return;
   const int r = (int)(t / b), a = (int)(t % b);
-  const int i = perm ? perm[r] : r;
-  out[t] = (Out)in[(long)a * n + i];
+  const long k = (long)a * n + (perm ? perm[r] : r);
+  out[t] = (Out)(scale ? in[k] * scale[k] : in[k]);
 }
 
-// The inverse: out[a * n + perm[r]] = in[r * b + a], widened to fp64.
+// The inverse: out[a * n + perm[r]] = in[r * b + a] * scale[a * n + perm[r]], widened to fp64.
 template <class In>
-__global__ void k_from_cells(int n, int b, const int* perm, const In* in, double* out) {
+__global__ void k_from_cells(int n, int b, const int* perm, const double* scale, const In* in,
+                             double* out) {
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (long)n * b) return;
   const int r = (int)(t / b), a = (int)(t % b);
-  const int i = perm ? perm[r] : r;
-  out[(long)a * n + i] = (double)in[t];
+  const long k = (long)a * n + (perm ? perm[r] : r);
+  out[k] = scale ? (double)in[t] * scale[k] : (double)in[t];
 }
 
 }  // namespace
@@ -234,8 +236,8 @@ extern "C" int fv_gather_blocks(long nnzb, int b, const long* bmap, const void* 
   return FV_OK;
 }
 
-extern "C" int fv_to_cells(int n, int b, const int* perm, const double* in, void* out, int out_f64,
-                           void* stream) {
+extern "C" int fv_to_cells(int n, int b, const int* perm, const double* scale, const double* in,
+                           void* out, int out_f64, void* stream) {
   if (n <= 0 || b <= 0 || !in || !out) {
     fv_set_error("fv_to_cells: bad arguments");
     return FV_ERR_ARG;
@@ -243,15 +245,15 @@ extern "C" int fv_to_cells(int n, int b, const int* perm, const double* in, void
   const long m = (long)n * b;
   cudaStream_t s = (cudaStream_t)stream;
   if (out_f64)
-    k_to_cells<double><<<fv_blocks(m, 256), 256, 0, s>>>(n, b, perm, in, (double*)out);
+    k_to_cells<double><<<fv_blocks(m, 256), 256, 0, s>>>(n, b, perm, scale, in, (double*)out);
   else
-    k_to_cells<float><<<fv_blocks(m, 256), 256, 0, s>>>(n, b, perm, in, (float*)out);
+    k_to_cells<float><<<fv_blocks(m, 256), 256, 0, s>>>(n, b, perm, scale, in, (float*)out);
   FV_CUDA_TRY(cudaGetLastError());
   return FV_OK;
 }
 
-extern "C" int fv_from_cells(int n, int b, const int* perm, const void* in, int in_f64,
-                             double* out, void* stream) {
+extern "C" int fv_from_cells(int n, int b, const int* perm, const double* scale, const void* in,
+                             int in_f64, double* out, void* stream) {
   if (n <= 0 || b <= 0 || !in || !out) {
     fv_set_error("fv_from_cells: bad arguments");
     return FV_ERR_ARG;
@@ -259,9 +261,9 @@ extern "C" int fv_from_cells(int n, int b, const int* perm, const void* in, int 
   const long m = (long)n * b;
   cudaStream_t s = (cudaStream_t)stream;
   if (in_f64)
-    k_from_cells<double><<<fv_blocks(m, 256), 256, 0, s>>>(n, b, perm, (const double*)in, out);
+    k_from_cells<double><<<fv_blocks(m, 256), 256, 0, s>>>(n, b, perm, scale, (const double*)in, out);
   else
-    k_from_cells<float><<<fv_blocks(m, 256), 256, 0, s>>>(n, b, perm, (const float*)in, out);
+    k_from_cells<float><<<fv_blocks(m, 256), 256, 0, s>>>(n, b, perm, scale, (const float*)in, out);
   FV_CUDA_TRY(cudaGetLastError());
   return FV_OK;
 }

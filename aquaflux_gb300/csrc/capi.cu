@@ -304,6 +304,21 @@ extern "C" int fv_assemble_jacobian(FvCase* c, const double* state, const int* i
                                  (cudaStream_t)stream);
 }
 
+extern "C" int fv_jvp_batch(FvCase* c, const double* state, const double* v, int k, double* jv,
+                            void* stream) {
+  if (!c || !state || !v || !jv || k < 0) {
+    fv_set_error("fv_jvp_batch: bad arguments");
+    return FV_ERR_ARG;
+  }
+  const long n = fv_case_n_unknowns(c);
+  for (int i = 0; i < k; ++i) {
+    int rc = fv_case_run(c, state, v + (long)i * n, FV_TAN_STATE, nullptr, jv + (long)i * n,
+                         (cudaStream_t)stream);
+    if (rc != FV_OK) return rc;
+  }
+  return FV_OK;
+}
+
 extern "C" int fv_jvp_shift(FvCase* c, const double* state, const double* v, const double* shift,
                             double* jv, void* stream) {
   if (!c || !state || !v || !shift || !jv) {

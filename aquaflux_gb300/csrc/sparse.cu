@@ -868,6 +868,97 @@ extern "C" int fv_ilu0_factor_values(const FvIlu0* f, void* out, void* stream) {
   return FV_OK;
 }
 
+// ------------------------------------------------------------------------------ shifted operator
+namespace {
+// Diagonal of every dof (cell i, field a) after the shift, and its equilibration factor.
+__global__ void k_shift_diag(int n, int b, const int* __restrict__ ptr, const int* __restrict__ idx,
+                             const double* __restrict__ val, const double* __restrict__ shift,
+                             double* diag_cm, double* scale_cm, double* scale_fm, int* missing) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long)n * b) return;
+  const int i = (int)(t / b), a = (int)(t % b);
+  int dq = -1;
+  for (int q = ptr[i]; q < ptr[i + 1]; ++q)
+    if (idx[q] == i) {
+      dq = q;
+      break;
+    }
+  if (dq < 0) {
+    atomicMin(missing, i);
+    return;
+  }
+  double d = val[((long)dq * b + a) * b + a];
+  if (shift) d = d + shift[(long)a * n + i];
+  diag_cm[t] = d;
+  if (scale_cm) {
+    double m = fabs(d);
+    if (m == 0.0) m = 1.0;
+    const double sc = 1.0 / sqrt(m);
+    scale_cm[t] = sc;
+    if (scale_fm) scale_fm[(long)a * n + i] = sc;
+  }
+}
+
+// out[q][a][c] = ((v + shift on the diagonal) * s_row) * s_col, one thread per scalar row (i, a).
+template <class Out>
+__global__ void k_shift_scale(int n, int b, const int* __restrict__ ptr, const int* __restrict__ idx,
+                              const double* __restrict__ val, const double* __restrict__ diag_cm,
+                              const double* __restrict__ scale_cm, Out* __restrict__ out) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long)n * b) return;
+  const int i = (int)(t / b), a = (int)(t % b);
+  const double sr = scale_cm ? scale_cm[t] : 1.0;
+  for (int q = ptr[i]; q < ptr[i + 1]; ++q) {
+    const int j = idx[q];
+    const long base = ((long)q * b + a) * b;
+    for (int c = 0; c < b; ++c) {
+      double v = (j == i && c == a) ? diag_cm[t] : val[base + c];
+      if (scale_cm) {
+        v = v * sr;
+        v = v * scale_cm[(long)j * b + c];
+      }
+      out[base + c] = (Out)v;
+    }
+  }
+}
+}  // namespace
+
+extern "C" int fv_bsr_shift_equilibrate(int n, int b, const int* indptr, const int* indices,
+                                        const double* values, const double* shift, int equilibrate,
+                                        double* scale_fm, double* work, void* out, int out_f64,
+                                        void* stream) {
+  if (n <= 0 || b <= 0 || !indptr || !indices || !values || !work || !out) {
+    fv_set_error("fv_bsr_shift_equilibrate: bad arguments");
+    return FV_ERR_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  const long m = (long)n * b;
+  double* diag_cm = work;
+  double* scale_cm = equilibrate ? work + m : nullptr;
+  int* missing = reinterpret_cast<int*>(work + 2 * m);
+  const int init = 0x7fffffff;
+  FV_CUDA_TRY(cudaMemcpyAsync(missing, &init, sizeof(int), cudaMemcpyHostToDevice, s));
+  k_shift_diag<<<fv_blocks(m, kThreads), kThreads, 0, s>>>(n, b, indptr, indices, values, shift,
+                                                           diag_cm, scale_cm, scale_fm, missing);
+  if (out_f64)
+    k_shift_scale<double><<<fv_blocks(m, kThreads), kThreads, 0, s>>>(
+        n, b, indptr, indices, values, diag_cm, scale_cm, (double*)out);
+  else
+    k_shift_scale<float><<<fv_blocks(m, kThreads), kThreads, 0, s>>>(
+        n, b, indptr, indices, values, diag_cm, scale_cm, (float*)out);
+  FV_CUDA_TRY(cudaGetLastError());
+  int miss = 0;
+  FV_CUDA_TRY(cudaMemcpyAsync(&miss, missing, sizeof(int), cudaMemcpyDeviceToHost, s));
+  FV_CUDA_TRY(cudaStreamSynchronize(s));
+  if (miss != init) {
+    fv_set_error_index(miss);
+    fv_set_error("fv_bsr_shift_equilibrate: block row %d stores no diagonal block; the shift has "
+                 "nowhere to go", miss);
+    return FV_ERR_NO_DIAG;
+  }
+  return FV_OK;
+}
+
 // ------------------------------------------------------------------------------ SpMV entry points
 namespace {
 template <class V>
@@ -910,6 +1001,47 @@ int spmv(int nbr, int b, const int* indptr, const int* indices, const V* values,
   return FV_OK;
 }
 }  // namespace
+
+// Transpose map of a square BSR pattern (host): for block row j of A^T the rows i of A with a
+// block (i, j) (tptr / tidx) and that block's index in A (tblk).  tptr n + 1; tidx, tblk nnzb.
+extern "C" int fv_bsr_transpose_map(int n, const int* indptr, const int* indices, int* tptr,
+                                    int* tidx, int* tblk) {
+  if (n <= 0 || !indptr || !indices || !tptr || !tidx || !tblk) {
+    fv_set_error("fv_bsr_transpose_map: bad arguments");
+    return FV_ERR_ARG;
+  }
+  for (int q = 0; q < indptr[n]; ++q)
+    if (indices[q] < 0 || indices[q] >= n) {
+      fv_set_error("fv_bsr_transpose_map: column index out of range");
+      return FV_ERR_ARG;
+    }
+  Transpose T;
+  build_transpose(n, n, indptr, indices, &T);
+  std::copy(T.ptr.begin(), T.ptr.end(), tptr);
+  std::copy(T.idx.begin(), T.idx.end(), tidx);
+  std::copy(T.blk.begin(), T.blk.end(), tblk);
+  return FV_OK;
+}
+
+// y = A^T x through a transpose map from fv_bsr_transpose_map (device arrays; no allocation).
+extern "C" int fv_bsr_spmv_t_mapped(int n, int b, const int* tptr, const int* tidx,
+                                    const int* tblk, const void* values, const void* x, void* y,
+                                    int f64, void* stream) {
+  if (n <= 0 || b <= 0 || !tptr || !tidx || !tblk || !values || !x || !y) {
+    fv_set_error("fv_bsr_spmv_t_mapped: bad arguments");
+    return FV_ERR_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  const long rows = (long)n * b;
+  if (f64)
+    k_bsr_spmv_t<double><<<fv_blocks(rows, kThreads), kThreads, 0, s>>>(
+        n, b, tptr, tidx, tblk, (const double*)values, (const double*)x, (double*)y);
+  else
+    k_bsr_spmv_t<float><<<fv_blocks(rows, kThreads), kThreads, 0, s>>>(
+        n, b, tptr, tidx, tblk, (const float*)values, (const float*)x, (float*)y);
+  FV_CUDA_TRY(cudaGetLastError());
+  return FV_OK;
+}
 
 extern "C" int fv_bsr_spmv_f64(int nbr, int b, const int* indptr, const int* indices,
                                const double* values, const double* x, double* y, int transpose,

@@ -176,6 +176,16 @@ class FlowCase:
         check(lib().fv_jvp(self._h, ptr(s), ptr(vv), ptr(r), ptr(jv), _stream()))
         return (r, jv) if return_residual else jv
 
+    def jvp_batch(self, state, vs) -> torch.Tensor:
+        """``J(state) v_i`` for every row of the ``(k, n)`` seed block ``vs``."""
+        s = self._vec(state)
+        v = torch.as_tensor(vs, dtype=torch.float64, device="cuda").contiguous()
+        if v.dim() != 2 or v.shape[1] != self.n_unknowns:
+            raise ValueError(f"expected seeds of shape (k, {self.n_unknowns}), got {tuple(v.shape)}")
+        out = torch.empty_like(v)
+        check(lib().fv_jvp_batch(self._h, ptr(s), ptr(v), int(v.shape[0]), ptr(out), _stream()))
+        return out
+
     def jvp_shift(self, state, v, shift) -> torch.Tensor:
         s, vv, sh = self._vec(state), self._vec(v), self._vec(shift)
         jv = torch.empty_like(s)

@@ -104,29 +104,93 @@ class BlockJacobian:
         return sp.bsr_matrix((v, self.indices, self.indptr), shape=(n, n))
 
 
-class IluPreconditioner:
-    """``M ~= J^-1``: ILU(0) of the materialised block Jacobian, fp32 or fp64, on the GPU.
+class ShiftedCellMajorOperator:
+    """``D (J + diag(shift)) D`` of a :class:`BlockJacobian` on the GPU, pattern fixed.
 
-    Vectors arrive field-major (the state layout) and are interleaved cell-major for the factor.
+    ``ShiftedCellMajorOperator.assemble`` (``aquaflux/solve/amg_preconditioner.py:545-658``): the
+    pseudo-transient shift (field-major, may be None) on the diagonal, then (``equilibrate``) the
+    symmetric square-root-diagonal scale, in the cell-major block layout the Jacobian already has.
+    ``assemble`` returns ``(values, scale)``, ``scale`` field-major (None without equilibration);
+    the values buffer is reused by the next call.
     """
 
-    def __init__(self, jac: BlockJacobian, precision: int = 32):
+    def __init__(self, jac: BlockJacobian, *, equilibrate: bool = True, precision: int = 64):
+        self.jac = jac
+        n, b = jac.n, jac.b
+        self.equilibrate = bool(equilibrate)
+        self.dtype = torch.float64 if precision == 64 else torch.float32
+        self._work = torch.empty(2 * n * b + 1, dtype=torch.float64, device="cuda")
+        self.scale = (torch.empty(n * b, dtype=torch.float64, device="cuda")
+                      if self.equilibrate else None)
+        self.values = torch.empty(jac.nnzb * b * b, dtype=self.dtype, device="cuda")
+
+    def assemble(self, values: torch.Tensor, shift: torch.Tensor | None = None):
+        jac = self.jac
+        check(lib().fv_bsr_shift_equilibrate(
+            jac.n, jac.b, ptr(jac.d_indptr), ptr(jac.d_indices), ptr(values), ptr(shift),
+            int(self.equilibrate), ptr(self.scale), ptr(self._work), ptr(self.values),
+            int(self.dtype == torch.float64), _stream()))
+        return self.values, self.scale
+
+
+class IluPreconditioner:
+    """``M ~= (J + diag(shift))^-1``: ILU(0) of the materialised block Jacobian, fp32 or fp64, on
+    the GPU; optionally of the shifted and symmetrically equilibrated operator
+    (:class:`ShiftedCellMajorOperator`), ``M = D (D (J + shift) D)_ILU^-1 D``.
+
+    Vectors arrive field-major (the state layout) and are interleaved cell-major (and scaled) for
+    the factor by one kernel each way.  ``reshift(shift)`` re-factors for a new shift without
+    re-materialising the Jacobian (the beta-only refresh of ``amg_preconditioner.py:909-948``).
+    """
+
+    def __init__(self, jac: BlockJacobian, precision: int = 32, *, shift=None,
+                 equilibrate: bool = False):
         self.jac = jac
         self.precision = precision
         self.dtype = torch.float32 if precision == 32 else torch.float64
         self.ilu = Ilu0.__new__(Ilu0)
         self.ilu._setup(jac.indptr, jac.indices, jac.b, precision)
+        self.shift = None if shift is None else torch.as_tensor(shift, dtype=torch.float64,
+                                                                device="cuda")
+        self.op = (ShiftedCellMajorOperator(jac, equilibrate=equilibrate, precision=precision)
+                   if (shift is not None or equilibrate) else None)
         self._cm = torch.empty(jac.n * jac.b, dtype=self.dtype, device="cuda")
         self._x = torch.empty_like(self._cm)
+        self._f64 = int(precision == 64)
+
+    def _factor(self, values):
+        if self.op is None:
+            self.ilu.refactor(values)
+        else:
+            vals, _ = self.op.assemble(values, self.shift)
+            self.ilu.refactor(vals)
 
     def refresh(self, state: torch.Tensor) -> None:
-        self.ilu.refactor(self.jac.materialize(state))
+        self._factor(self.jac.materialize(state))
 
-    def apply(self, r: torch.Tensor) -> torch.Tensor:
+    def reshift(self, shift) -> None:
+        """New shift on the last materialised Jacobian: re-assemble and re-factor only."""
+        if self.op is None:
+            self.op = ShiftedCellMajorOperator(self.jac, equilibrate=False,
+                                               precision=self.precision)
+        self.shift = None if shift is None else torch.as_tensor(shift, dtype=torch.float64,
+                                                                device="cuda")
+        self._factor(self.jac.values)
+
+    def apply(self, r: torch.Tensor, transpose: bool = False) -> torch.Tensor:
         n, b = self.jac.n, self.jac.b
-        self._cm.copy_(r.view(b, n).t().reshape(-1))
-        self.ilu.solve(self._cm, out=self._x)
-        return self._x.view(n, b).t().reshape(-1).to(torch.float64)
+        scale = None if self.op is None else self.op.scale
+        check(lib().fv_to_cells(n, b, 0, ptr(scale), ptr(r), ptr(self._cm), self._f64,
+                                _stream()))
+        self.ilu.solve(self._cm, transpose=transpose, out=self._x)
+        out = torch.empty(n * b, dtype=torch.float64, device="cuda")
+        check(lib().fv_from_cells(n, b, 0, ptr(scale), ptr(self._x), self._f64, ptr(out),
+                                  _stream()))
+        return out
+
+    def apply_transpose(self, r: torch.Tensor) -> torch.Tensor:
+        """``M^T r`` (``D`` is diagonal, so only the factor's solve is transposed)."""
+        return self.apply(r, transpose=True)
 
 
 @dataclasses.dataclass
@@ -280,19 +344,15 @@ def newton_solve(case, state0, *, rtol: float = 1e-10, atol: float = 1e-12, max_
 
 
 class TransposedPreconditioner:
-    """``M^T``: the transposed ILU(0) solve of an :class:`IluPreconditioner` (exact transpose, as
-    the reference's ``TransposedPreconditioner`` / ``jax.linear_transpose``,
-    ``aquaflux/solve/implicit.py:709-730``)."""
+    """``M^T`` of a preconditioner with an exact transposed application (``apply_transpose``: the
+    transposed ILU(0) solve, or the transposed V-cycle), as the reference's
+    ``TransposedPreconditioner`` / ``jax.linear_transpose`` (``aquaflux/solve/implicit.py:709-730``)."""
 
-    def __init__(self, pc: IluPreconditioner):
+    def __init__(self, pc):
         self.pc = pc
 
     def apply(self, r: torch.Tensor) -> torch.Tensor:
-        pc = self.pc
-        n, b = pc.jac.n, pc.jac.b
-        pc._cm.copy_(r.view(b, n).t().reshape(-1))
-        pc.ilu.solve(pc._cm, transpose=True, out=pc._x)
-        return pc._x.view(n, b).t().reshape(-1).to(torch.float64)
+        return self.pc.apply_transpose(r)
 
 
 @dataclasses.dataclass
@@ -305,12 +365,13 @@ class AdjointResult:
 
 def implicit_adjoint(case, state, g, *, rtol: float = 1e-10, precision: int = 64,
                      restart: int = 30, max_krylov: int = 1000,
-                     preconditioner: IluPreconditioner | None = None) -> AdjointResult:
+                     preconditioner=None) -> AdjointResult:
     """Implicit-function-theorem gradient at a converged root (``_implicit_solve_bwd``,
     ``aquaflux/solve/implicit.py:733-761``): solve ``J^T lam = g`` with FGMRES on the hand-written
     VJP and the transposed ILU(0) preconditioner (the reference's tight 1e-10 adjoint solve,
     ``aquaflux/solve/linear.py:40-42``), then ``dL/dtheta = -lam^T dR/dtheta`` for
-    ``theta = (mu, inlet_scale)``."""
+    ``theta = (mu, inlet_scale)``.  ``preconditioner``: any with ``refresh`` and
+    ``apply_transpose`` (ILU(0) by default; the AMG V-cycle has an exact transpose too)."""
     s = torch.as_tensor(state, dtype=torch.float64, device="cuda")
     gv = torch.as_tensor(g, dtype=torch.float64, device="cuda")
     if preconditioner is None:

@@ -119,6 +119,10 @@ int fv_jvp(FvCase* c, const double* state, const double* v, double* residual, do
  * preconditioner is built from).  No reference counterpart as an entry point; it is the
  * linearisation a Picard / SIMPLE-type preconditioner uses.  Device. */
 int fv_jvp_frozen(FvCase* c, const double* state, const double* v, double* jv, void* stream);
+/* k directional derivatives at one state: jv[i] = J(state) v[i] for the row-major (k, n) seed
+ * block v, the vmapped JVP of aquaflux/turbulence/coupled.py:741-752 (_batched_jacobian_matvec).
+ * Device. */
+int fv_jvp_batch(FvCase* c, const double* state, const double* v, int k, double* jv, void* stream);
 /* Materialise the Jacobian (frozen = 1: J_direct; 0: the full J, exact on the pattern only when
  * the colouring's reach covers J's) into a cell-major BSR matrix with b = number of fields, by
  * coloured JVP probes: materialize_block_jacobian (aquaflux/solve/sparse_jacobian.py:722-847).
@@ -185,6 +189,14 @@ int fv_bsr_spmv_t_f64_noalloc(int n_block_rows, long nnzb, int b, const int* ind
 /* fp32 values and vectors. */
 int fv_bsr_spmv_f32(int n_block_rows, int b, const int* indptr, const int* indices,
                     const float* values, const float* x, float* y, int transpose, void* stream);
+/* Transpose map of a square BSR pattern (host): tptr (n + 1) / tidx (nnzb) list, for block row j
+ * of A^T, the rows i of A holding a block (i, j); tblk (nnzb) that block's index in A. */
+int fv_bsr_transpose_map(int n, const int* indptr, const int* indices, int* tptr, int* tidx,
+                         int* tblk);
+/* y = A^T x through that map (device; fp64 when f64 != 0, else fp32; allocates nothing): the
+ * transposed products of the exact V-cycle transpose. */
+int fv_bsr_spmv_t_mapped(int n, int b, const int* tptr, const int* tidx, const int* tblk,
+                         const void* values, const void* x, void* y, int f64, void* stream);
 
 /* ------------------------------------------------------------------------------------------
  * Zero-fill ILU(0) over a BSR pattern.  Replaces Ilu0 (aquaflux/solve/ilu0.py:153-255) and the
@@ -207,6 +219,21 @@ int fv_ilu0_factor(FvIlu0* f, const void* values, int values_f64, void* stream);
 int fv_ilu0_apply(FvIlu0* f, const void* r, void* x, int transpose, void* stream);
 /* Copy the factor (device, nnzb * b * b, `precision`) -- combined L (unit diagonal) and U. */
 int fv_ilu0_factor_values(const FvIlu0* f, void* out, void* stream);
+
+/* ------------------------------------------------------------------------------------------
+ * The shifted, equilibrated cell-major operator D (J + diag(shift)) D of
+ * ShiftedCellMajorOperator.assemble (aquaflux/solve/amg_preconditioner.py:545-658), with
+ * shifted_jacobian (sparse_jacobian.py:893-927) and the equilibration of
+ * frozen_operator.py:72-143.  The matrix is cell-major BSR (b x b row-major blocks, the reference's
+ * cell-major CSR with every block entry stored).  shift (field-major, n * b) may be NULL; with
+ * equilibrate != 0 every entry is scaled by s[row] then s[column], s = 1 / sqrt(|shifted diagonal|)
+ * (|0| read as 1), and scale_fm (may be NULL) receives s in field-major order.  work: device scratch
+ * of 2 n b + 1 doubles.  out: nnzb b^2 values, fp64 (out_f64 != 0) or fp32.  A block row without a
+ * diagonal block returns FV_ERR_NO_DIAG.  Synchronizes the stream (to report that error).
+ * ------------------------------------------------------------------------------------------ */
+int fv_bsr_shift_equilibrate(int n, int b, const int* indptr, const int* indices,
+                             const double* values, const double* shift, int equilibrate,
+                             double* scale_fm, double* work, void* out, int out_f64, void* stream);
 
 /* ------------------------------------------------------------------------------------------
  * Graph colouring for compressed Jacobian probing.  Replaces _saturation_colouring
@@ -255,11 +282,12 @@ int fv_permute_pattern(int n, const int* indptr, const int* indices, const int* 
 int fv_gather_blocks(long nnzb, int b, const long* bmap, const void* src, int src_f64, void* dst,
                      int dst_f64, void* stream);
 /* Field-major fp64 state-layout vector <-> cell-major vector in a permuted cell order
- * (perm NULL: identity): out[r * b + a] = in[a * n + perm[r]] and its inverse (device). */
-int fv_to_cells(int n, int b, const int* perm, const double* in, void* out, int out_f64,
-                void* stream);
-int fv_from_cells(int n, int b, const int* perm, const void* in, int in_f64, double* out,
-                  void* stream);
+ * (perm NULL: identity), each entry multiplied by scale_fm (field-major, may be NULL):
+ * out[r * b + a] = in[a * n + perm[r]] * scale_fm[a * n + perm[r]] and its inverse (device). */
+int fv_to_cells(int n, int b, const int* perm, const double* scale_fm, const double* in, void* out,
+                int out_f64, void* stream);
+int fv_from_cells(int n, int b, const int* perm, const double* scale_fm, const void* in,
+                  int in_f64, double* out, void* stream);
 /* The same three in fp64 (the fp64 V-cycle of the all-fp64 Newton-Krylov solve). */
 int fv_galerkin_f64(long n_coarse_blocks, int b, const long* gptr, const long* glist,
                     const void* fine, int fine_f64, double* coarse, void* stream);

@@ -368,6 +368,64 @@ def corrected_cases():
     return out
 
 
+# --------------------------------------------------------------------------- shifted operators
+def operator_cases():
+    """``ShiftedCellMajorOperator.assemble`` (``aquaflux/solve/amg_preconditioner.py:545-658``),
+    ``shifted_jacobian`` (``sparse_jacobian.py:893-927``) and ``equilibrate_cell_major``
+    (``frozen_operator.py:382-435``) on a block-stencil matrix in the field-major layout."""
+    import scipy.sparse as sp
+
+    from aquaflux.solve.amg_preconditioner import ShiftedCellMajorOperator
+    from aquaflux.solve.frozen_operator import equilibrate_cell_major
+    from aquaflux.solve.sparse_jacobian import shifted_jacobian
+
+    out = {}
+    rng = np.random.default_rng(41)
+    mesh = structured_grid_2d(7, 5, named_boundaries=True)
+    n, b = mesh.n_cells, 3
+    own = np.asarray(mesh.face_cells.owner)
+    nb = np.asarray(mesh.face_cells.neighbour)
+    inner = nb >= 0
+    rows = np.concatenate([own[inner], nb[inner], np.arange(n)])
+    cols = np.concatenate([nb[inner], own[inner], np.arange(n)])
+    pat = sp.csr_matrix((np.ones(rows.size), (rows, cols)), shape=(n, n))
+    pat.sort_indices()
+    nnzb = pat.nnz
+    blocks = rng.standard_normal((nnzb, b, b))
+    blocks[rng.random((nnzb, b, b)) < 0.1] = 0.0  # explicit zeros stay in the pattern
+    dq = pat.indptr[:-1] + np.array([np.searchsorted(pat.indices[pat.indptr[i]:pat.indptr[i + 1]], i)
+                                     for i in range(n)])
+    blocks[dq, 2, 2] = 0.0  # zero pressure diagonal: the scale treats |0| as 1
+    # field-major CSR with every block entry stored
+    brow = np.repeat(np.arange(n), np.diff(pat.indptr))
+    r = (np.arange(b)[None, :, None] * n + brow[:, None, None]) * np.ones((1, 1, b), dtype=np.int64)
+    c = (np.arange(b)[None, None, :] * n + pat.indices[:, None, None]) * np.ones((1, b, 1), dtype=np.int64)
+    coo = sp.coo_matrix((np.ones(r.size), (r.ravel(), c.ravel())), shape=(n * b, n * b)).tocsr()
+    coo.sort_indices()
+    # place the values into the sorted field-major pattern
+    key = r.ravel() * (n * b) + c.ravel()
+    order = np.argsort(key)
+    fm_values = blocks.ravel()[order]
+    shift = np.concatenate([rng.random(n) * 2.0, rng.random(n) * 2.0, np.zeros(n)])
+    op = ShiftedCellMajorOperator(coo.indptr, coo.indices, b)
+    mat, scale, perm = op.assemble(fm_values, shift)
+    out["op_bsr_indptr"] = pat.indptr.astype(np.int32)
+    out["op_bsr_indices"] = pat.indices.astype(np.int32)
+    out["op_blocks"] = blocks
+    out["op_shift"] = shift
+    out["op_cm_indptr"] = np.asarray(mat.indptr)
+    out["op_cm_indices"] = np.asarray(mat.indices)
+    out["op_cm_data"] = np.asarray(mat.data).copy()
+    out["op_scale"] = np.asarray(scale)
+    out["op_perm"] = np.asarray(perm)
+    fm = sp.csr_matrix((fm_values, coo.indices, coo.indptr), shape=coo.shape)
+    out["op_shifted_fm_data"] = np.asarray(shifted_jacobian(fm, shift).data)
+    eq, eq_scale, _ = equilibrate_cell_major(fm, b)
+    out["op_eq_cm_data"] = np.asarray(eq.data)
+    out["op_eq_scale"] = np.asarray(eq_scale)
+    return out
+
+
 # --------------------------------------------------------------------------- ILU(0)
 def ilu_cases():
     import test_ilu0  # the reference's own unit test module (its fixture operator)
@@ -418,7 +476,8 @@ def colouring_cases():
 
 FILES = {"colouring": lambda: colouring_cases(), "meshes": lambda: mesh_cases(),
          "laminar": lambda: laminar_cases(), "sst": lambda: sst_cases(),
-         "ilu0": lambda: ilu_cases(), "corrected": lambda: corrected_cases()}
+         "ilu0": lambda: ilu_cases(), "corrected": lambda: corrected_cases(),
+         "operator": lambda: operator_cases()}
 
 
 def main():

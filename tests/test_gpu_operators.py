@@ -1,0 +1,135 @@
+"""Shifted / equilibrated cell-major operators, exact preconditioner transposes and batched JVPs on
+the GPU."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import operator_oracle as oo
+from tests.cases import golden
+
+pytestmark = pytest.mark.gpu
+
+
+def _stream():
+    return torch.cuda.current_stream().cuda_stream
+
+
+def _run_shift_equilibrate(d, shift, equilibrate, out_f64=True):
+    from aquaflux_gb300._lib import check, lib, ptr
+
+    ip = torch.tensor(d["op_bsr_indptr"], device="cuda")
+    ix = torch.tensor(d["op_bsr_indices"], device="cuda")
+    blocks = torch.tensor(d["op_blocks"].reshape(-1), device="cuda")
+    n, b = len(d["op_bsr_indptr"]) - 1, d["op_blocks"].shape[1]
+    sh = None if shift is None else torch.tensor(shift, device="cuda")
+    scale = torch.empty(n * b, dtype=torch.float64, device="cuda")
+    work = torch.empty(2 * n * b + 1, dtype=torch.float64, device="cuda")
+    out = torch.empty(blocks.numel(), dtype=torch.float64 if out_f64 else torch.float32,
+                      device="cuda")
+    check(lib().fv_bsr_shift_equilibrate(n, b, ptr(ip), ptr(ix), ptr(blocks), ptr(sh),
+                                         int(equilibrate), ptr(scale), ptr(work), ptr(out),
+                                         int(out_f64), _stream()))
+    return out.cpu().numpy().reshape(-1, b, b), scale.cpu().numpy()
+
+
+@pytest.mark.parametrize("shifted,equilibrate", [(True, True), (False, True), (True, False)])
+def test_shift_equilibrate_matches_reference_bitwise(shifted, equilibrate):
+    d = golden("operator")
+    shift = d["op_shift"] if shifted else None
+    got, scale = _run_shift_equilibrate(d, shift, equilibrate)
+    ref, ref_scale = oo.shift_equilibrate(d["op_blocks"], d["op_bsr_indptr"], d["op_bsr_indices"],
+                                          shift, equilibrate)
+    assert np.array_equal(got, ref)
+    if equilibrate:
+        assert np.array_equal(scale, ref_scale)
+        key = "op_cm_data" if shifted else "op_eq_cm_data"
+        data = oo.bsr_to_cell_major_csr_data(got, d["op_bsr_indptr"], d["op_bsr_indices"])
+        assert np.array_equal(data, d[key])
+
+
+def test_shift_equilibrate_fp32_output_is_the_rounded_fp64():
+    d = golden("operator")
+    got32, _ = _run_shift_equilibrate(d, d["op_shift"], True, out_f64=False)
+    got64, _ = _run_shift_equilibrate(d, d["op_shift"], True)
+    assert np.array_equal(got32, got64.astype(np.float32))
+
+
+def _cavity_pc(kind, precision, **kw):
+    from aquaflux_gb300 import workloads
+    from aquaflux_gb300.amg import AmgPreconditioner
+    from aquaflux_gb300.solve import BlockJacobian, IluPreconditioner
+
+    wl = workloads.channel3d(12)
+    case = wl.device_case()
+    jac = BlockJacobian(case)
+    if kind == "ilu":
+        pc = IluPreconditioner(jac, precision, **kw)
+    else:
+        pc = AmgPreconditioner(jac, precision, min_cells=150, **kw)
+    s = torch.tensor(wl.initial_state(noise=0.02), device="cuda")
+    return wl, case, pc, s
+
+
+@pytest.mark.parametrize("kind,opts", [
+    ("ilu", {}), ("ilu", {"equilibrate": True}), ("amg", {}),
+    ("amg", {"fine_order": "natural"}), ("amg", {"equilibrate": True})])
+def test_preconditioner_transpose_is_exact(kind, opts):
+    """<M x, y> = <x, M^T y> for the fp64 ILU(0) solve and the fp64 V-cycle (the adjoint
+    preconditioner of aquaflux/solve/implicit.py:709-730)."""
+    wl, case, pc, s = _cavity_pc(kind, 64, **opts)
+    shift = torch.rand(case.n_unknowns, dtype=torch.float64, device="cuda")
+    pc.shift = shift if kind == "ilu" and opts else pc.shift
+    pc.refresh(s)
+    g = torch.Generator(device="cuda").manual_seed(0)
+    x = torch.randn(case.n_unknowns, dtype=torch.float64, device="cuda", generator=g)
+    y = torch.randn(case.n_unknowns, dtype=torch.float64, device="cuda", generator=g)
+    lhs = float(torch.dot(pc.apply(x), y))
+    rhs = float(torch.dot(x, pc.apply_transpose(y)))
+    assert abs(lhs - rhs) <= 1e-11 * max(abs(lhs), 1.0)
+
+
+@pytest.mark.parametrize("kind", ["ilu", "amg"])
+def test_reshift_equals_a_fresh_shifted_preconditioner(kind):
+    """The beta-only refresh (new shift, same materialised Jacobian) gives the preconditioner a
+    fresh build with that shift gives."""
+    wl, case, pc, s = _cavity_pc(kind, 64)
+    pc.refresh(s)
+    shift = 0.5 + torch.rand(case.n_unknowns, dtype=torch.float64, device="cuda")
+    pc.reshift(shift)
+    _, _, fresh, _ = _cavity_pc(kind, 64, shift=shift)
+    fresh.refresh(s)
+    r = torch.randn(case.n_unknowns, dtype=torch.float64, device="cuda")
+    assert torch.equal(pc.apply(r), fresh.apply(r))
+
+
+def test_implicit_adjoint_with_amg_equals_ilu():
+    from aquaflux_gb300.amg import AmgPreconditioner
+    from aquaflux_gb300.solve import BlockJacobian, implicit_adjoint, newton_solve
+
+    from aquaflux_gb300 import workloads
+
+    wl = workloads.channel3d(10)
+    case = wl.device_case()
+    res = newton_solve(case, wl.initial_state(), precision=64, max_steps=40, rtol=1e-12)
+    assert res.converged
+    g = torch.randn(case.n_unknowns, dtype=torch.float64, device="cuda")
+    a = implicit_adjoint(case, res.state, g, rtol=1e-12)
+    b = implicit_adjoint(case, res.state, g, rtol=1e-12,
+                         preconditioner=AmgPreconditioner(BlockJacobian(case), 64, min_cells=100))
+    assert a.converged and b.converged
+    assert float((a.lam - b.lam).abs().max()) <= 1e-8 * float(a.lam.abs().max())
+    assert float((a.dparams - b.dparams).abs().max()) <= 1e-8 * float(a.dparams.abs().max())
+
+
+def test_batched_jvp_equals_single_jvps():
+    from aquaflux_gb300 import workloads
+
+    wl = workloads.channel3d(8)
+    case = wl.device_case()
+    s = wl.initial_state(noise=0.05)
+    vs = torch.randn(3, case.n_unknowns, dtype=torch.float64, device="cuda")
+    out = case.jvp_batch(s, vs)
+    for i in range(3):
+        assert torch.equal(out[i], case.jvp(s, vs[i]))
