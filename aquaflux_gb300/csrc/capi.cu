@@ -123,8 +123,9 @@ extern "C" int fv_case_create(const FvMesh* mesh, const FvCaseDesc* desc,
   FV_CUDA_TRY(cudaMalloc(&c->inv_wd, sizeof(double) * 2 * m->nc));
   FV_CUDA_TRY(cudaMemsetAsync(c->inv_wd, 0, sizeof(double) * 2 * m->nc, s));
   if (desc->turbulent) {
+    FV_CUDA_TRY(cudaMalloc(&c->wnear, sizeof(int) * m->nc));
     rc = fv_wall_distance_compute(m, c->swall, n_wall, c->wd, c->wdg, desc->gradient_sweeps,
-                                  desc->gradient_relaxation, s);
+                                  desc->gradient_relaxation, c->wnear, s);
     if (rc != FV_OK) {
       fv_case_destroy(c);
       return rc;
@@ -184,6 +185,8 @@ extern "C" int fv_case_destroy(FvCase* c) {
   cudaFree(c->aux);
   cudaFree(c->dscalar);
   cudaFree(c->jac_face);
+  cudaFree(c->wnear);
+  fv_node_adjoint_free(c);
   for (cudaEvent_t e : c->prof_events) cudaEventDestroy(e);
   delete c;
   return FV_OK;
@@ -359,6 +362,15 @@ extern "C" int fv_vjp(FvCase* c, const double* state, const double* w, double* r
     return FV_ERR_ARG;
   }
   return fv_case_vjp_run(c, state, w, residual, vjp, (cudaStream_t)stream);
+}
+
+extern "C" int fv_node_vjp(FvCase* c, const double* state, const double* w, double* dnodes,
+                           void* stream) {
+  if (!c || !state || !w || !dnodes) {
+    fv_set_error("fv_node_vjp: bad arguments");
+    return FV_ERR_ARG;
+  }
+  return fv_case_node_vjp(c, state, w, dnodes, (cudaStream_t)stream);
 }
 
 extern "C" int fv_param_vjp(FvCase* c, const double* state, const double* w, double* out,

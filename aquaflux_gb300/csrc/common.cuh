@@ -59,6 +59,9 @@ FV_HD Dual& operator-=(Dual& a, Dual b) { a = a - b; return a; }
 // a + g (b - a): the linear owner / neighbour blend (1 - g) a + g b with one multiply-add.
 FV_HD double lerp(double a, double b, double g) { return fma(g, b - a, a); }
 FV_HD Dual lerp(Dual a, Dual b, double g) { return {fma(g, b.v - a.v, a.v), fma(g, b.d - a.d, a.d)}; }
+FV_HD Dual lerp(Dual a, Dual b, Dual g) {
+  return {fma(g.v, b.v - a.v, a.v), fma(g.v, b.d - a.d, a.d) + g.d * (b.v - a.v)};
+}
 
 // Scalar-generic elementary functions.
 FV_HD double cst(double x, double) { return x; }

@@ -88,6 +88,16 @@ struct CaseView {
   const double* inv_wd2;      // (nc) 1 / wall distance^2
 };
 
+// Workspace of the mesh-coordinate adjoint (residual.cu), allocated on its first use.
+struct NodeAdjoint {
+  void* dual_work = nullptr;  // forward workspace as dual numbers with zero tangents
+  double* buf = nullptr;
+  int* node_ptr = nullptr;    // node -> face-node entries (CSR over fn_idx positions)
+  int* node_ent = nullptr;
+  int* wall_ptr = nullptr;    // face -> cells whose nearest wall face it is
+  int* wall_cell = nullptr;
+};
+
 struct FvCase {
   FvMesh* mesh = nullptr;
   FvCaseDesc desc{};
@@ -114,6 +124,8 @@ struct FvCase {
   double* aux = nullptr;    // face intermediates of the double forward pass (for the adjoint)
   double* dscalar = nullptr; // (4) device scalars
   double* jac_face = nullptr; // (2, nfld, nfld, nf) face flux derivatives of the Jacobian assembly
+  int* wnear = nullptr;       // (nc) nearest SST wall face (internal index), turbulent cases
+  NodeAdjoint* nadj = nullptr;  // mesh-coordinate adjoint workspace, allocated on first use
   CaseView view;
   // optional per-stage CUDA-event profiling (fv_case_profile_begin / _end)
   std::vector<cudaEvent_t> prof_events;  // max_runs * (FV_MAX_STAGES + 1)
@@ -133,6 +145,10 @@ int fv_case_vjp_run(FvCase* c, const double* state, const double* w, double* res
                     cudaStream_t s);
 // Frozen reach-1 Jacobian by per-face forward-mode derivatives (residual.cu); D holds
 // fv_jac_face_bytes.
+// Mesh-coordinate adjoint dL/dnodes of L = w . R(state, nodes) (residual.cu).
+int fv_case_node_vjp(FvCase* c, const double* state, const double* w, double* dnodes,
+                     cudaStream_t s);
+void fv_node_adjoint_free(FvCase* c);
 int fv_case_assemble_frozen(FvCase* c, const double* state, const int* indptr, const int* indices,
                             double* values, double* D, cudaStream_t s);
 size_t fv_jac_face_bytes(int dim, int turb, long nf);
@@ -141,7 +157,7 @@ enum { FV_TAN_NONE = 0, FV_TAN_STATE = 1, FV_TAN_MU = 2, FV_TAN_INLET = 3, FV_TA
 // Wall distance + gradient for a turbulent case (mesh.cu).
 int fv_wall_distance_compute(FvMesh* m, const unsigned char* swall_dev, int n_wall_faces,
                              double* wd, double* wdg, int gradient_sweeps,
-                             double gradient_relaxation, cudaStream_t s);
+                             double gradient_relaxation, int* nearest_face, cudaStream_t s);
 // Corrected Green-Gauss sweeps of one scalar field's gradient (residual.cu): on entry x0 holds
 // rel * B phi / V and num holds B phi; the last iterate lands in x0 or x1 by the sweep count's
 // parity (x0 when sweeps - 1 is even).

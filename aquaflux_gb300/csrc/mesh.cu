@@ -12,6 +12,7 @@
 #include <cstring>
 #include <numeric>
 
+#include "geom.cuh"
 #include "internal.cuh"
 
 namespace {
@@ -23,70 +24,14 @@ __global__ void k_face_geometry(MeshView m, double* area, double* normal, double
   int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= m.nf) return;
   const int nf = m.nf;
-  int b = m.fn_ptr[f], e = m.fn_ptr[f + 1];
-  if (DIM == 2) {
-    const double* p0 = m.nodes + 2 * (long)m.fn_idx[b];
-    const double* p1 = m.nodes + 2 * (long)m.fn_idx[b + 1];
-    double dx = p1[0] - p0[0], dy = p1[1] - p0[1];
-    double sq = dx * dx + dy * dy;
-    double a = sq > 0.0 ? sqrt(sq) : 0.0;
-    area[f] = a;
-    xf[f] = 0.5 * (p0[0] + p1[0]);
-    xf[nf + f] = 0.5 * (p0[1] + p1[1]);
-    // normal = unit(d_y, -d_x)
-    normal[f] = sq > 0.0 ? dy / a : 0.0;
-    normal[nf + f] = sq > 0.0 ? -dx / a : 0.0;
-  } else {
-    int k = e - b;
-    double pa[3] = {0.0, 0.0, 0.0};
-    for (int i = b; i < e; ++i) {
-      const double* p = m.nodes + 3 * (long)m.fn_idx[i];
-      pa[0] += p[0];
-      pa[1] += p[1];
-      pa[2] += p[2];
-    }
-    double inv = 1.0 / (double)k;
-    pa[0] *= inv;
-    pa[1] *= inv;
-    pa[2] *= inv;
-    double S[3] = {0.0, 0.0, 0.0};
-    for (int i = 0; i < k; ++i) {
-      const double* pb = m.nodes + 3 * (long)m.fn_idx[b + i];
-      const double* pc = m.nodes + 3 * (long)m.fn_idx[b + (i + 1) % k];
-      double u0 = pb[0] - pa[0], u1 = pb[1] - pa[1], u2 = pb[2] - pa[2];
-      double v0 = pc[0] - pa[0], v1 = pc[1] - pa[1], v2 = pc[2] - pa[2];
-      S[0] += 0.5 * (u1 * v2 - u2 * v1);
-      S[1] += 0.5 * (u2 * v0 - u0 * v2);
-      S[2] += 0.5 * (u0 * v1 - u1 * v0);
-    }
-    double sq = S[0] * S[0] + S[1] * S[1] + S[2] * S[2];
-    double a = sq > 0.0 ? sqrt(sq) : 0.0;
-    double n[3] = {0.0, 0.0, 0.0};
-    if (sq > 0.0) {
-      n[0] = S[0] / a;
-      n[1] = S[1] / a;
-      n[2] = S[2] / a;
-    }
-    double c[3] = {0.0, 0.0, 0.0};
-    for (int i = 0; i < k; ++i) {
-      const double* pb = m.nodes + 3 * (long)m.fn_idx[b + i];
-      const double* pc = m.nodes + 3 * (long)m.fn_idx[b + (i + 1) % k];
-      double u0 = pb[0] - pa[0], u1 = pb[1] - pa[1], u2 = pb[2] - pa[2];
-      double v0 = pc[0] - pa[0], v1 = pc[1] - pa[1], v2 = pc[2] - pa[2];
-      double d0 = 0.5 * (u1 * v2 - u2 * v1);
-      double d1 = 0.5 * (u2 * v0 - u0 * v2);
-      double d2 = 0.5 * (u0 * v1 - u1 * v0);
-      double w = d0 * n[0] + d1 * n[1] + d2 * n[2];
-      c[0] += w * ((pa[0] + pb[0] + pc[0]) / 3.0);
-      c[1] += w * ((pa[1] + pb[1] + pc[1]) / 3.0);
-      c[2] += w * ((pa[2] + pb[2] + pc[2]) / 3.0);
-    }
-    double sa = a > 0.0 ? a : 1.0;
-    area[f] = a;
-    for (int j = 0; j < 3; ++j) {
-      normal[j * nf + f] = n[j];
-      xf[j * nf + f] = c[j] / sa;
-    }
+  const int b = m.fn_ptr[f], e = m.fn_ptr[f + 1];
+  auto P = [&](int i, int j) -> double { return m.nodes[(long)DIM * m.fn_idx[b + i] + j]; };
+  double a, n[DIM], x[DIM];
+  face_geom<double, DIM>(e - b, P, a, n, x);
+  area[f] = a;
+  for (int j = 0; j < DIM; ++j) {
+    normal[j * nf + f] = n[j];
+    xf[j * nf + f] = x[j];
   }
 }
 
@@ -119,35 +64,25 @@ __global__ void k_orient(MeshView m, const double* xf, const double* approx, dou
 
 template <int DIM>
 __global__ void k_cell_geometry(MeshView m, const double* area, const double* normal,
-                                const double* xf, const double* approx, double* vol, double* xc,
-                                double* inv_vol) {
+                                const double* xf, double* vol, double* xc, double* inv_vol) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= m.nc) return;
-  double a[DIM], cs[DIM];
-  for (int j = 0; j < DIM; ++j) {
-    a[j] = approx[j * m.nc + c];
-    cs[j] = 0.0;
-  }
-  double v = 0.0;
-  int b = m.cf_ptr[c], e = m.cf_ptr[c + 1];
-  for (int i = b; i < e; ++i) {
-    unsigned ent = m.cf_face[i];
-    int f = (int)(ent & ~FV_NB_BIT);
-    double loc[DIM], dn = 0.0;
+  const int b = m.cf_ptr[c], e = m.cf_ptr[c + 1];
+  auto F = [&](int i, double& A, double* n, double* x, bool& isnb) {
+    const unsigned ent = m.cf_face[b + i];
+    const int f = (int)(ent & ~FV_NB_BIT);
+    A = area[f];
     for (int j = 0; j < DIM; ++j) {
-      loc[j] = xf[j * m.nf + f] - a[j];
-      dn += loc[j] * normal[j * m.nf + f];
+      n[j] = normal[j * m.nf + f];
+      x[j] = xf[j * m.nf + f];
     }
-    double fl = dn * area[f];
-    if (ent & FV_NB_BIT) fl = -fl;
-    v += fl;
-    for (int j = 0; j < DIM; ++j) cs[j] += fl * loc[j];
-  }
-  double volume = v / (double)DIM;
+    isnb = (ent & FV_NB_BIT) != 0;
+  };
+  double volume, x[DIM];
+  cell_geom<double, DIM>(e - b, F, volume, x);
   vol[c] = volume;
   inv_vol[c] = 1.0 / volume;
-  double inv = 1.0 / ((double)(DIM + 1) * volume);
-  for (int j = 0; j < DIM; ++j) xc[j * m.nc + c] = cs[j] * inv + a[j];
+  for (int j = 0; j < DIM; ++j) xc[j * m.nc + c] = x[j];
 }
 
 template <int DIM>
@@ -157,44 +92,32 @@ __global__ void k_face_factors(MeshView m, double* g, double* nd, double* dpn, d
   int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= m.nf) return;
   const int nf = m.nf, nc = m.nc;
-  int o = m.owner[f];
-  bool interior = f < m.nfi;
-  int n = interior ? m.nb[f] : o;
-  double n_[DIM], d[DIM], dp[DIM], dn[DIM];
-  double dd = 0.0, fd = 0.0, vpn = 0.0, vnn = 0.0, s2 = 0.0;
+  const int o = m.owner[f];
+  const bool interior = f < m.nfi;
+  const int n = interior ? m.nb[f] : o;
+  double n_[DIM], x[DIM], xo[DIM], xn[DIM];
   for (int j = 0; j < DIM; ++j) {
     n_[j] = m.normal[j * nf + f];
-    double xp = m.xc[j * nc + o], xn = m.xc[j * nc + n], x = m.xf[j * nf + f];
-    d[j] = xn - xp;
-    dp[j] = x - xp;
-    dn[j] = x - xn;
-    dd += d[j] * d[j];
-    fd += dp[j] * d[j];
-    vpn += dp[j] * n_[j];
-    vnn += dn[j] * n_[j];
-    s2 += n_[j] * n_[j];
+    x[j] = m.xf[j * nf + f];
+    xo[j] = m.xc[j * nc + o];
+    xn[j] = m.xc[j * nc + n];
   }
-  double gg = interior ? fd / dd : 0.0;
-  double dn_ = 0.0;
-  for (int j = 0; j < DIM; ++j) dn_ += d[j] * n_[j];
-  g[f] = gg;
-  const double ndv = interior ? dn_ : vpn;
-  nd[f] = ndv;
-  dpn[f] = vpn;
-  dnn[f] = vnn;
-  nn2[f] = s2;
-  inv_nd[f] = 1.0 / ndv;
-  inv_dpn[f] = 1.0 / vpn;
-  double sk[DIM];
+  FaceFactors<double, DIM> F;
+  face_factors<double, DIM>(n_, x, xo, xn, interior, F);
+  g[f] = F.g;
+  nd[f] = F.nd;
+  dpn[f] = F.dpn;
+  dnn[f] = F.dnn;
+  nn2[f] = F.nn2;
+  inv_nd[f] = F.inv_nd;
+  inv_dpn[f] = F.inv_dpn;
   for (int j = 0; j < DIM; ++j) {
-    dvec[j * nf + f] = d[j];
-    sk[j] = m.xf[j * nf + f] - (m.xc[j * nc + o] + d[j] * gg);
-    skew[j * nf + f] = sk[j];
-    tP[j * nf + f] = dp[j] - n_[j] * vpn;
-    tN[j * nf + f] = dn[j] - n_[j] * vnn;
+    dvec[j * nf + f] = F.dvec[j];
+    skew[j * nf + f] = F.skew[j];
+    tP[j * nf + f] = F.tP[j];
+    tN[j * nf + f] = F.tN[j];
   }
-  for (int j = 0; j < DIM; ++j)
-    for (int q = 0; q < DIM; ++q) ns[(long)(j * DIM + q) * nf + f] = n_[j] * sk[q];
+  for (int j = 0; j < DIM * DIM; ++j) ns[(long)j * nf + f] = F.ns[j];
 }
 
 // Scatter an internal-order face array (dim, nf) SoA to reference order (nf, dim) row-major.
@@ -214,13 +137,15 @@ __global__ void k_cell_out(int nc, int dim, const double* in, double* out) {
 // Nearest SST-wall face centroid per cell (aquaflux/mesh/distance.py:52-84: exact nearest
 // neighbour), by a brute-force search over the wall-face centroids staged through shared memory.
 template <int DIM>
-__global__ void k_wall_distance(MeshView m, const double* wall_xf, int n_wall, double* wd) {
+__global__ void k_wall_distance(MeshView m, const double* wall_xf, int n_wall, double* wd,
+                                const int* slot_face, int* nearest) {
   __shared__ double tile[DIM][256];
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   double x[DIM];
   bool live = c < m.nc;
   for (int j = 0; j < DIM; ++j) x[j] = live ? m.xc[j * m.nc + c] : 0.0;
   double best = 1.0 / 0.0;
+  int arg = 0;
   for (int base = 0; base < n_wall; base += 256) {
     int cnt = min(256, n_wall - base);
     __syncthreads();
@@ -233,10 +158,16 @@ __global__ void k_wall_distance(MeshView m, const double* wall_xf, int n_wall, d
         double dd = x[j] - tile[j][t];
         s += dd * dd;
       }
-      best = s < best ? s : best;
+      if (s < best) {
+        best = s;
+        arg = base + t;
+      }
     }
   }
-  if (live) wd[c] = sqrt(best);
+  if (live) {
+    wd[c] = sqrt(best);
+    if (nearest) nearest[c] = slot_face[arg];
+  }
 }
 
 __global__ void k_gather_wall_xf(int nf, int dim, const unsigned char* swall, const int* slot,
@@ -314,7 +245,7 @@ int fv_mesh_compute_geometry(FvMesh* m, cudaStream_t s) {
     k_face_geometry<2><<<bf, kThreads, 0, s>>>(v, area, normal, xf);
     k_approx_centroid<2><<<bc, kThreads, 0, s>>>(v, xf, m->approx);
     k_orient<2><<<bf, kThreads, 0, s>>>(v, xf, m->approx, normal);
-    k_cell_geometry<2><<<bc, kThreads, 0, s>>>(v, area, normal, xf, m->approx, vol, xc,
+    k_cell_geometry<2><<<bc, kThreads, 0, s>>>(v, area, normal, xf, vol, xc,
                                                  const_cast<double*>(v.inv_vol));
     k_face_factors<2><<<bf, kThreads, 0, s>>>(
         v, const_cast<double*>(v.g), const_cast<double*>(v.nd), const_cast<double*>(v.dpn),
@@ -325,7 +256,7 @@ int fv_mesh_compute_geometry(FvMesh* m, cudaStream_t s) {
     k_face_geometry<3><<<bf, kThreads, 0, s>>>(v, area, normal, xf);
     k_approx_centroid<3><<<bc, kThreads, 0, s>>>(v, xf, m->approx);
     k_orient<3><<<bf, kThreads, 0, s>>>(v, xf, m->approx, normal);
-    k_cell_geometry<3><<<bc, kThreads, 0, s>>>(v, area, normal, xf, m->approx, vol, xc,
+    k_cell_geometry<3><<<bc, kThreads, 0, s>>>(v, area, normal, xf, vol, xc,
                                                  const_cast<double*>(v.inv_vol));
     k_face_factors<3><<<bf, kThreads, 0, s>>>(
         v, const_cast<double*>(v.g), const_cast<double*>(v.nd), const_cast<double*>(v.dpn),
@@ -338,7 +269,7 @@ int fv_mesh_compute_geometry(FvMesh* m, cudaStream_t s) {
 }
 
 int fv_wall_distance_compute(FvMesh* m, const unsigned char* swall_dev, int n_wall, double* wd,
-                             double* wdg, int sweeps, double rel, cudaStream_t s) {
+                             double* wdg, int sweeps, double rel, int* nearest, cudaStream_t s) {
   if (n_wall <= 0) {
     fv_set_error("a turbulent case needs at least one SST wall face");
     return FV_ERR_ARG;
@@ -347,15 +278,22 @@ int fv_wall_distance_compute(FvMesh* m, const unsigned char* swall_dev, int n_wa
   std::vector<unsigned char> h_sw(m->nf);
   FV_CUDA_TRY(cudaMemcpyAsync(h_sw.data(), swall_dev, m->nf, cudaMemcpyDeviceToHost, s));
   FV_CUDA_TRY(cudaStreamSynchronize(s));
-  std::vector<int> slot(m->nf, -1);
+  std::vector<int> slot(m->nf, -1), slot_face;
   int k = 0;
   for (int f = 0; f < m->nf; ++f)
-    if (h_sw[f]) slot[f] = k++;
+    if (h_sw[f]) {
+      slot[f] = k++;
+      slot_face.push_back(f);
+    }
   int* d_slot = nullptr;
+  int* d_slot_face = nullptr;
   double* d_wxf = nullptr;
   FV_CUDA_TRY(cudaMalloc(&d_slot, sizeof(int) * m->nf));
+  FV_CUDA_TRY(cudaMalloc(&d_slot_face, sizeof(int) * std::max(k, 1)));
   FV_CUDA_TRY(cudaMalloc(&d_wxf, sizeof(double) * (size_t)k * m->dim));
   FV_CUDA_TRY(cudaMemcpyAsync(d_slot, slot.data(), sizeof(int) * m->nf, cudaMemcpyHostToDevice, s));
+  FV_CUDA_TRY(cudaMemcpyAsync(d_slot_face, slot_face.data(), sizeof(int) * k,
+                              cudaMemcpyHostToDevice, s));
   int bf = fv_blocks(m->nf, kThreads), bc = fv_blocks(m->nc, kThreads);
   k_gather_wall_xf<<<bf, kThreads, 0, s>>>(m->nf, m->dim, swall_dev, d_slot, m->view.xf, d_wxf, k);
   // corrected scheme: B d, the other sweep iterate and the face scratch
@@ -369,10 +307,10 @@ int fv_wall_distance_compute(FvMesh* m, const unsigned char* swall_dev, int n_wa
   }
   const double r0 = sweeps >= 1 ? rel : 1.0;
   if (m->dim == 2) {
-    k_wall_distance<2><<<bc, 256, 0, s>>>(m->view, d_wxf, k, wd);
+    k_wall_distance<2><<<bc, 256, 0, s>>>(m->view, d_wxf, k, wd, d_slot_face, nearest);
     k_wall_distance_gradient<2><<<bc, kThreads, 0, s>>>(m->view, swall_dev, wd, x0, num, r0);
   } else {
-    k_wall_distance<3><<<bc, 256, 0, s>>>(m->view, d_wxf, k, wd);
+    k_wall_distance<3><<<bc, 256, 0, s>>>(m->view, d_wxf, k, wd, d_slot_face, nearest);
     k_wall_distance_gradient<3><<<bc, kThreads, 0, s>>>(m->view, swall_dev, wd, x0, num, r0);
   }
   int rc = FV_OK;
@@ -381,6 +319,7 @@ int fv_wall_distance_compute(FvMesh* m, const unsigned char* swall_dev, int n_wa
   FV_CUDA_TRY(cudaGetLastError());
   FV_CUDA_TRY(cudaStreamSynchronize(s));
   cudaFree(d_slot);
+  cudaFree(d_slot_face);
   cudaFree(d_wxf);
   cudaFree(num);
   cudaFree(galt);

@@ -1,0 +1,673 @@
+// Mesh-coordinate adjoint: dL/dnodes of L = w . R(state, nodes), the node-coordinate part of
+// theta_bar = -(dR/dtheta)^T lambda in _implicit_solve_bwd (aquaflux/solve/implicit.py:733-761).
+// Included by residual.cu after the state adjoint (it reuses that adjoint's cotangents).
+//
+// Reverse mode over the stages, each stage's geometry cotangent formed by local forward mode: a
+// stage's formula is evaluated once more with a dual number on one geometric input (GeoSeed) and
+// the tangent contracted with the stage's output cotangent, which the state adjoint has left:
+//   face fluxes           FL_bar = Wt_P - Wt_N                                 (k_nadj_flux)
+//   a_P face coefficients a_bar = -d_bar d^2 / V of the owner / neighbour      (k_nadj_apcoef)
+//   Green-Gauss gradients G_bar (linear in S_f, g, 1/V: written out)          (k_nadj_grad_*)
+//   SST closure           (S, F1, nu_t, shear, imposed omega gradient)_bar     (k_nadj_closure)
+//   SST sources           w on the k and omega rows                           (k_nadj_src)
+//   d = V / a_P           d_bar d / V                                          (k_nadj_dcoeff)
+// then back through the geometry, again by dual numbers on the same formulas as the forward
+// pipeline (geom.cuh): the per-face factors (normal, face and cell centroids), the wall distance
+// (nearest wall-face centroid) and its Green-Gauss gradient, the cell volumes / centroids (face
+// areas, normals, centroids) and the face geometry (node coordinates; the owner-outward flip is a
+// constant sign).  Every scatter is a gather over a precomputed incidence list: deterministic.
+// Supports the compact gradient scheme.
+
+
+namespace {
+
+__global__ void k_lift(long n, const double* src, Dual* dst) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = Dual{src[i], 0.0};
+}
+
+struct Contract {
+  const double* w;
+  double* acc;
+  __device__ __forceinline__ void operator()(int q, const Dual& x) const { *acc += w[q] * x.d; }
+};
+
+template <int DIM, bool TURB>
+__global__ void __launch_bounds__(128) k_nadj_flux(MeshView m, CaseView cv, const double* state,
+                                                   Par<Dual> par, const Dual* G, const Dual* cl,
+                                                   const Dual* dco, const double* Wt, double* Fb,
+                                                   double* wdf) {
+  constexpr int NF = Layout<DIM, TURB>::NFLD;
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= m.nf) return;
+  const int nc = m.nc, nf = m.nf;
+  const int o = m.owner[f];
+  const bool interior = f < m.nfi;
+  double FLb[NF];
+#pragma unroll
+  for (int q = 0; q < NF; ++q)
+    FLb[q] = Wt[(long)q * nc + o] - (interior ? Wt[(long)q * nc + m.nb[f]] : 0.0);
+  const Src<Dual> st{state, nullptr};
+#pragma unroll 1
+  for (int comp = 0; comp < GF_COUNT; ++comp) {
+    double acc = 0.0;
+    flux_face<Dual, DIM, TURB>(m, cv, st, par, G, cl, dco, (const Dual*)nullptr, true, f,
+                               Contract{FLb, &acc}, nullptr, GeoSeed{comp, -1, f, -1});
+    Fb[(long)comp * nf + f] += acc;
+  }
+  double acc = 0.0;
+  if (TURB && !interior)
+    flux_face<Dual, DIM, TURB>(m, cv, st, par, G, cl, dco, (const Dual*)nullptr, true, f,
+                               Contract{FLb, &acc}, nullptr, GeoSeed{-1, GC_WD, -1, o});
+  wdf[f] = acc;
+}
+
+template <int DIM, bool TURB>
+__global__ void __launch_bounds__(128) k_nadj_apcoef(MeshView m, CaseView cv, const double* state,
+                                                     Par<Dual> par, const Dual* G, const Dual* cl,
+                                                     const double* dco, const double* dcob,
+                                                     double* Fb, double* wdf) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= m.nf) return;
+  const int nf = m.nf;
+  const int o = m.owner[f];
+  const bool interior = f < m.nfi;
+  const double abo = -dcob[o] * dco[o] * dco[o] * m.inv_vol[o];
+  double abn = 0.0;
+  if (interior) {
+    const int n = m.nb[f];
+    abn = -dcob[n] * dco[n] * dco[n] * m.inv_vol[n];
+  }
+  const Src<Dual> st{state, nullptr};
+#pragma unroll 1
+  for (int comp = 0; comp < GF_COUNT; ++comp) {
+    Dual ao, an, mf;
+    apcoef_face<Dual, DIM, TURB>(m, cv, st, par, G, cl, f, GeoSeed{comp, -1, f, -1}, ao, an, mf);
+    Fb[(long)comp * nf + f] += abo * ao.d + abn * an.d;
+  }
+  if (TURB && !interior) {
+    Dual ao, an, mf;
+    apcoef_face<Dual, DIM, TURB>(m, cv, st, par, G, cl, f, GeoSeed{-1, GC_WD, -1, o}, ao, an, mf);
+    wdf[f] += abo * ao.d;
+  }
+}
+
+// Green-Gauss: G_c = (1/V_c) sum_f +-S_f phi_f, S_f = n_f A_f, phi_f = lerp(phi_P, phi_N, g_f) or
+// the leading-order boundary value.
+template <int DIM, bool TURB>
+__global__ void __launch_bounds__(128) k_nadj_grad_face(MeshView m, CaseView cv,
+                                                        const double* state, Par<double> par,
+                                                        const double* Gb, double* Fb) {
+  using L = Layout<DIM, TURB>;
+  constexpr int NF = L::NFLD;
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= m.nf) return;
+  const int nc = m.nc, nf = m.nf;
+  const int o = m.owner[f];
+  const double A = m.area[f];
+  double nrm[DIM], Sb[DIM];
+#pragma unroll
+  for (int j = 0; j < DIM; ++j) {
+    nrm[j] = m.normal[(long)j * nf + f];
+    Sb[j] = 0.0;
+  }
+  const double ivo = m.inv_vol[o];
+  if (f < m.nfi) {
+    const int n = m.nb[f];
+    const double g = m.g[f], ivn = m.inv_vol[n];
+    double gb = 0.0;
+#pragma unroll
+    for (int q = 0; q < NF; ++q) {
+      const double po = state[(long)q * nc + o], pn = state[(long)q * nc + n];
+      const double pf = lerp(po, pn, g);
+      double pbar = 0.0;
+#pragma unroll
+      for (int j = 0; j < DIM; ++j) {
+        const double y = Gb[((long)q * DIM + j) * nc + o] * ivo - Gb[((long)q * DIM + j) * nc + n] * ivn;
+        Sb[j] += pf * y;
+        pbar += nrm[j] * A * y;
+      }
+      gb += pbar * (pn - po);
+    }
+    Fb[(long)GF_G * nf + f] += gb;
+  } else {
+    const signed char kind = cv.fkind[f];
+#pragma unroll
+    for (int q = 0; q < NF; ++q) {
+      const double po = state[(long)q * nc + o];
+      double pb;
+      if (q < DIM) pb = bvel(cv, nf, f, q, kind, po, par);
+      else if (q == L::P) pb = bpress(cv, f, kind, po);
+      else if (q == L::K) pb = bscalar(cv.kkind[f], cv.kval[f], po, 0.0);
+      else pb = bscalar(cv.wkind[f], cv.wval[f], po, 0.0);
+#pragma unroll
+      for (int j = 0; j < DIM; ++j) Sb[j] += pb * Gb[((long)q * DIM + j) * nc + o] * ivo;
+    }
+  }
+  double ab = 0.0;
+#pragma unroll
+  for (int j = 0; j < DIM; ++j) {
+    ab += Sb[j] * nrm[j];
+    Fb[(long)(GF_NORMAL + j) * nf + f] += Sb[j] * A;
+  }
+  Fb[(long)GF_AREA * nf + f] += ab;
+}
+
+// 1/V part of the gradients (numerator = G V) and d = V / a_P.
+template <int DIM, bool TURB>
+__global__ void k_nadj_grad_cell(MeshView m, const double* Gb, const double* G, const double* dco,
+                                 const double* dcob, double* ivb, double* Cb) {
+  constexpr int NF = Layout<DIM, TURB>::NFLD;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nc) return;
+  const int nc = m.nc;
+  double acc = 0.0;
+  for (int k = 0; k < NF * DIM; ++k) acc += Gb[(long)k * nc + c] * G[(long)k * nc + c];
+  ivb[c] += acc * m.vol[c];
+  Cb[(long)GC_VOL * nc + c] += dcob[c] * dco[c] / m.vol[c];
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(128) k_nadj_closure(MeshView m, CaseView cv, const double* state,
+                                                      Par<Dual> par, const Dual* G,
+                                                      const double* clb, const double* Gwib,
+                                                      double* Cb, double* Fb) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nc) return;
+  const int nc = m.nc, nf = m.nf;
+  const Src<Dual> st{state, nullptr};
+  auto contract = [&](const GeoSeed& gs) {
+    Dual out[7], gw[DIM];
+    closure_cell<Dual, DIM>(m, cv, st, par, G, c, gs, out, gw);
+    double acc = 0.0;
+    for (int i = 0; i < 4; ++i) acc += clb[(long)i * nc + c] * out[i].d;
+    for (int j = 0; j < DIM; ++j) acc += Gwib[(long)j * nc + c] * gw[j].d;
+    return acc;
+  };
+#pragma unroll 1
+  for (int comp = GC_WD; comp < GC_WDG + DIM; ++comp)
+    Cb[(long)comp * nc + c] += contract(GeoSeed{-1, comp, -1, c});
+  if (cv.wcell[c]) {
+    const int b = m.cf_ptr[c], e = m.cf_ptr[c + 1];
+    for (int i = b; i < e; ++i) {
+      const int f = (int)(m.cf_face[i] & ~FV_NB_BIT);
+      if (f < m.nfi || !cv.swall[f]) continue;
+      Fb[(long)GF_AREA * nf + f] += contract(GeoSeed{GF_AREA, -1, f, -1});
+    }
+  }
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(128) k_nadj_src(MeshView m, CaseView cv, const double* state,
+                                                  Par<Dual> par, const Dual* cl, const Dual* G,
+                                                  const Dual* Gwi, const double* W, double* Cb) {
+  using L = Layout<DIM, true>;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nc) return;
+  const int nc = m.nc;
+  const Src<Dual> st{state, nullptr};
+  const double wk = W[(long)L::K * nc + c], ww = W[(long)L::W * nc + c];
+  for (int comp = GC_VOL; comp <= GC_WD; ++comp) {
+    Dual rk{0.0, 0.0}, rw{0.0, 0.0};
+    sst_rows<Dual, DIM>(m, cv, st, par, cl, G, Gwi, c, rk, rw, GeoSeed{-1, comp, -1, c});
+    Cb[(long)comp * nc + c] += wk * rk.d + ww * rw.d;
+  }
+}
+
+// Wall-distance gradient (compact Green-Gauss of d: Dirichlet 0 on SST walls, the owner value on
+// other boundaries): face part.
+template <int DIM>
+__global__ void k_nadj_wdg_face(MeshView m, CaseView cv, const double* Cb, double* Fb,
+                                double* dpart) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= m.nf) return;
+  const int nc = m.nc, nf = m.nf;
+  const int o = m.owner[f];
+  const double A = m.area[f];
+  const double* yb = Cb + (long)GC_WDG * nc;
+  double nrm[DIM], Sb[DIM];
+  for (int j = 0; j < DIM; ++j) {
+    nrm[j] = m.normal[(long)j * nf + f];
+    Sb[j] = 0.0;
+  }
+  const double ivo = 1.0 / m.vol[o];
+  double pbar = 0.0, d_o = 0.0, d_n = 0.0, po = 0.0, pn = 0.0;
+  if (f < m.nfi) {
+    const int n = m.nb[f];
+    const double g = m.g[f], ivn = 1.0 / m.vol[n];
+    d_o = cv.wd[o];
+    d_n = cv.wd[n];
+    const double df = (1.0 - g) * d_o + g * d_n;
+    for (int j = 0; j < DIM; ++j) {
+      const double y = yb[(long)j * nc + o] * ivo - yb[(long)j * nc + n] * ivn;
+      Sb[j] += df * y;
+      pbar += nrm[j] * A * y;
+    }
+    Fb[(long)GF_G * nf + f] += pbar * (d_n - d_o);
+    po = (1.0 - g) * pbar;
+    pn = g * pbar;
+  } else {
+    const double df = cv.swall[f] ? 0.0 : cv.wd[o];
+    for (int j = 0; j < DIM; ++j) {
+      const double y = yb[(long)j * nc + o] * ivo;
+      Sb[j] += df * y;
+      pbar += nrm[j] * A * y;
+    }
+    po = cv.swall[f] ? 0.0 : pbar;
+  }
+  double ab = 0.0;
+  for (int j = 0; j < DIM; ++j) {
+    ab += Sb[j] * nrm[j];
+    Fb[(long)(GF_NORMAL + j) * nf + f] += Sb[j] * A;
+  }
+  Fb[(long)GF_AREA * nf + f] += ab;
+  dpart[f] = po;
+  dpart[(long)nf + f] = pn;
+}
+
+// ... cell part: d cotangent from the faces, and the 1/V of the wall-distance gradient.
+template <int DIM>
+__global__ void k_nadj_wdg_cell(MeshView m, CaseView cv, const double* dpart, double* Cb,
+                                double* Vb) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nc) return;
+  const int nc = m.nc, nf = m.nf;
+  double db = 0.0;
+  const int b = m.cf_ptr[c], e = m.cf_ptr[c + 1];
+  for (int i = b; i < e; ++i) {
+    const unsigned ent = m.cf_face[i];
+    const int f = (int)(ent & ~FV_NB_BIT);
+    db += (ent & FV_NB_BIT) ? dpart[(long)nf + f] : dpart[f];
+  }
+  Cb[(long)GC_WD * nc + c] += db;
+  // wdg = num / V: d wdg / dV = -wdg / V
+  double acc = 0.0;
+  for (int j = 0; j < DIM; ++j) acc += Cb[(long)(GC_WDG + j) * nc + c] * cv.wdg[(long)j * nc + c];
+  Vb[c] += -acc / m.vol[c];
+}
+
+// Cell scalars: V_bar (with the 1/V cotangent) and the wall-distance cotangent; the nearest wall
+// face's centroid and the cell centroid take d_bar (x_c - x_w) / d.
+template <int DIM, bool TURB>
+__global__ void k_nadj_cell_chain(MeshView m, CaseView cv, const double* Cb, const double* ivb,
+                                  const double* wdf, const int* wnear, double* Vb, double* xcb,
+                                  double* wcon) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nc) return;
+  const int nc = m.nc, nf = m.nf;
+  const double iv = m.inv_vol[c];
+  Vb[c] += Cb[(long)GC_VOL * nc + c] - ivb[c] * iv * iv;
+  for (int j = 0; j < DIM; ++j) xcb[(long)j * nc + c] = 0.0;
+  if (!TURB) return;
+  double db = Cb[(long)GC_WD * nc + c];
+  const double i1 = cv.inv_wd[c], i2 = cv.inv_wd2[c];
+  db += -Cb[(long)GC_INV_WD * nc + c] * i1 * i1 - 2.0 * Cb[(long)GC_INV_WD2 * nc + c] * i1 * i2;
+  const int b = m.cf_ptr[c], e = m.cf_ptr[c + 1];
+  for (int i = b; i < e; ++i) {
+    const int f = (int)(m.cf_face[i] & ~FV_NB_BIT);
+    if (f >= m.nfi && m.owner[f] == c) db += wdf[f];
+  }
+  const int w = wnear[c];
+  const double d = cv.wd[c];
+  for (int j = 0; j < DIM; ++j) {
+    const double t = d > 0.0 ? db * (m.xc[(long)j * nc + c] - m.xf[(long)j * nf + w]) / d : 0.0;
+    xcb[(long)j * nc + c] = t;
+    wcon[(long)j * nc + c] = t;
+  }
+}
+
+template <int DIM>
+__global__ void k_nadj_wall_face(MeshView m, const int* wall_ptr, const int* wall_cell,
+                                 const double* wcon, double* xfb) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= m.nf) return;
+  const int nc = m.nc, nf = m.nf;
+  for (int i = wall_ptr[f]; i < wall_ptr[f + 1]; ++i) {
+    const int c = wall_cell[i];
+    for (int j = 0; j < DIM; ++j) xfb[(long)j * nf + f] -= wcon[(long)j * nc + c];
+  }
+}
+
+// Per-face factors -> normal, face centroid and the two cell centroids.
+template <int DIM>
+__global__ void __launch_bounds__(128) k_nadj_factors(MeshView m, const double* Fb, double* nbt,
+                                                      double* xfb, double* xcpart) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= m.nf) return;
+  const int nc = m.nc, nf = m.nf;
+  const int o = m.owner[f];
+  const bool interior = f < m.nfi;
+  const int n = interior ? m.nb[f] : o;
+  double nv[DIM], xv[DIM], ov[DIM], wv[DIM];
+  for (int j = 0; j < DIM; ++j) {
+    nv[j] = m.normal[(long)j * nf + f];
+    xv[j] = m.xf[(long)j * nf + f];
+    ov[j] = m.xc[(long)j * nc + o];
+    wv[j] = m.xc[(long)j * nc + n];
+  }
+  const int groups = interior ? 4 : 3;
+#pragma unroll 1
+  for (int sdx = 0; sdx < groups * DIM; ++sdx) {
+    const int grp = sdx / DIM, sj = sdx % DIM;
+    Dual nd[DIM], xd[DIM], od[DIM], wd[DIM];
+    for (int j = 0; j < DIM; ++j) {
+      nd[j] = {nv[j], (grp == 0 && j == sj) ? 1.0 : 0.0};
+      xd[j] = {xv[j], (grp == 1 && j == sj) ? 1.0 : 0.0};
+      od[j] = {ov[j], (grp == 2 && j == sj) ? 1.0 : 0.0};
+      wd[j] = {wv[j], (grp == 3 && j == sj) ? 1.0 : 0.0};
+    }
+    FaceFactors<Dual, DIM> F;
+    face_factors<Dual, DIM>(nd, xd, od, interior ? wd : od, interior, F);
+    auto fb = [&](int comp) { return Fb[(long)comp * nf + f]; };
+    double acc = fb(GF_G) * F.g.d + fb(GF_DPN) * F.dpn.d + fb(GF_DNN) * F.dnn.d +
+                 fb(GF_NN2) * F.nn2.d + fb(GF_INV_ND) * F.inv_nd.d + fb(GF_INV_DPN) * F.inv_dpn.d;
+    for (int j = 0; j < DIM; ++j)
+      acc += fb(GF_DVEC + j) * F.dvec[j].d + fb(GF_SKEW + j) * F.skew[j].d +
+             fb(GF_TP + j) * F.tP[j].d + fb(GF_TN + j) * F.tN[j].d;
+    for (int k = 0; k < DIM * DIM; ++k) acc += fb(GF_NS + k) * F.ns[k].d;
+    if (grp == 0) nbt[(long)sj * nf + f] = fb(GF_NORMAL + sj) + acc;
+    else if (grp == 1) xfb[(long)sj * nf + f] += acc;
+    else if (grp == 2) xcpart[(long)sj * nf + f] = acc;
+    else xcpart[(long)(DIM + sj) * nf + f] = acc;
+  }
+  if (!interior)
+    for (int j = 0; j < DIM; ++j) xcpart[(long)(DIM + j) * nf + f] = 0.0;
+}
+
+template <int DIM>
+__global__ void k_nadj_xc_gather(MeshView m, const double* xcpart, double* xcb) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nc) return;
+  const int nc = m.nc, nf = m.nf;
+  const int b = m.cf_ptr[c], e = m.cf_ptr[c + 1];
+  for (int i = b; i < e; ++i) {
+    const unsigned ent = m.cf_face[i];
+    const int f = (int)(ent & ~FV_NB_BIT);
+    const long base = (ent & FV_NB_BIT) ? (long)DIM * nf : 0;
+    for (int j = 0; j < DIM; ++j) xcb[(long)j * nc + c] += xcpart[base + (long)j * nf + f];
+  }
+}
+
+// Cell volume and centroid -> the areas, normals and centroids of the cell's faces.
+template <int DIM>
+__global__ void __launch_bounds__(128) k_nadj_cell_geom(MeshView m, const double* Vb,
+                                                        const double* xcb, double* cfA,
+                                                        double* cfN, double* cfX, long ncf) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nc) return;
+  const int nc = m.nc, nf = m.nf;
+  const int b = m.cf_ptr[c], e = m.cf_ptr[c + 1];
+  const int k = e - b;
+  const double vb = Vb[c];
+  double xb[DIM];
+  for (int j = 0; j < DIM; ++j) xb[j] = xcb[(long)j * nc + c];
+#pragma unroll 1
+  for (int sdx = 0; sdx < k * (1 + 2 * DIM); ++sdx) {
+    const int slot = sdx / (1 + 2 * DIM), comp = sdx % (1 + 2 * DIM);
+    auto F = [&](int i, Dual& A, Dual* n, Dual* x, bool& isnb) {
+      const unsigned ent = m.cf_face[b + i];
+      const int f = (int)(ent & ~FV_NB_BIT);
+      const bool hit = i == slot;
+      A = {m.area[f], (hit && comp == 0) ? 1.0 : 0.0};
+      for (int j = 0; j < DIM; ++j) {
+        n[j] = {m.normal[(long)j * nf + f], (hit && comp == 1 + j) ? 1.0 : 0.0};
+        x[j] = {m.xf[(long)j * nf + f], (hit && comp == 1 + DIM + j) ? 1.0 : 0.0};
+      }
+      isnb = (ent & FV_NB_BIT) != 0;
+    };
+    Dual vol, xc[DIM];
+    cell_geom<Dual, DIM>(k, F, vol, xc);
+    double acc = vb * vol.d;
+    for (int j = 0; j < DIM; ++j) acc += xb[j] * xc[j].d;
+    const long ent = b + slot;
+    if (comp == 0) cfA[ent] = acc;
+    else if (comp <= DIM) cfN[(long)(comp - 1) * ncf + ent] = acc;
+    else cfX[(long)(comp - 1 - DIM) * ncf + ent] = acc;
+  }
+}
+
+__device__ __forceinline__ int cf_entry(const MeshView& m, int c, int f, bool nb) {
+  const unsigned want = (unsigned)f | (nb ? FV_NB_BIT : 0u);
+  for (int i = m.cf_ptr[c]; i < m.cf_ptr[c + 1]; ++i)
+    if (m.cf_face[i] == want) return i;
+  return -1;
+}
+
+// Totals of the face primitives' cotangents (residual stages + factors + cell geometry).
+template <int DIM>
+__global__ void k_nadj_cf_gather(MeshView m, const double* Fb, const double* cfA, const double* cfN,
+                                 const double* cfX, long ncf, double* Ab, double* nbt,
+                                 double* xfb) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= m.nf) return;
+  const int nf = m.nf;
+  const int eo = cf_entry(m, m.owner[f], f, false);
+  const int en = f < m.nfi ? cf_entry(m, m.nb[f], f, true) : -1;
+  double a = Fb[(long)GF_AREA * nf + f];
+  if (eo >= 0) a += cfA[eo];
+  if (en >= 0) a += cfA[en];
+  Ab[f] = a;
+  for (int j = 0; j < DIM; ++j) {
+    double nb = 0.0, xb = 0.0;
+    if (eo >= 0) {
+      nb += cfN[(long)j * ncf + eo];
+      xb += cfX[(long)j * ncf + eo];
+    }
+    if (en >= 0) {
+      nb += cfN[(long)j * ncf + en];
+      xb += cfX[(long)j * ncf + en];
+    }
+    nbt[(long)j * nf + f] += nb;
+    xfb[(long)j * nf + f] += xb;
+  }
+}
+
+// Face area / normal / centroid -> the face's node coordinates.
+template <int DIM>
+__global__ void __launch_bounds__(128) k_nadj_face_geom(MeshView m, const double* Ab,
+                                                        const double* nbt, const double* xfb,
+                                                        double* nodepart) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= m.nf) return;
+  const int nf = m.nf;
+  const int b = m.fn_ptr[f], e = m.fn_ptr[f + 1];
+  const int k = e - b;
+  double ns_[DIM], nbf[DIM], xbf[DIM];
+  for (int j = 0; j < DIM; ++j) {
+    ns_[j] = m.normal[(long)j * nf + f];
+    nbf[j] = nbt[(long)j * nf + f];
+    xbf[j] = xfb[(long)j * nf + f];
+  }
+  const double ab = Ab[f];
+#pragma unroll 1
+  for (int sdx = 0; sdx < k * DIM; ++sdx) {
+    const int si = sdx / DIM, sj = sdx % DIM;
+    auto P = [&](int i, int j) -> Dual {
+      return {m.nodes[(long)DIM * m.fn_idx[b + i] + j], (i == si && j == sj) ? 1.0 : 0.0};
+    };
+    Dual A, n[DIM], x[DIM];
+    face_geom<Dual, DIM>(k, P, A, n, x);
+    double dot = 0.0;
+    for (int j = 0; j < DIM; ++j) dot += n[j].v * ns_[j];
+    const double sgn = dot < 0.0 ? -1.0 : 1.0;  // the owner-outward flip
+    double acc = ab * A.d;
+    for (int j = 0; j < DIM; ++j) acc += nbf[j] * sgn * n[j].d + xbf[j] * x[j].d;
+    nodepart[(long)(b + si) * DIM + sj] = acc;
+  }
+}
+
+__global__ void k_nadj_nodes(int nn, int dim, const int* node_ptr, const int* node_ent,
+                             const double* nodepart, double* dnodes) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nn) return;
+  for (int j = 0; j < dim; ++j) {
+    double acc = 0.0;
+    for (int i = node_ptr[v]; i < node_ptr[v + 1]; ++i)
+      acc += nodepart[(long)node_ent[i] * dim + j];
+    dnodes[(long)v * dim + j] = acc;
+  }
+}
+
+struct NadjBuffers {
+  double *Fb, *Cb, *ivb, *wdf, *dpart, *Vb, *Ab, *nbt, *xfb, *xcpart, *xcb, *wcon, *cfA, *cfN,
+      *cfX, *nodepart;
+};
+
+NadjBuffers nadj_layout(double* p, int dim, long nc, long nf, long ncf, long nfn) {
+  NadjBuffers B;
+  B.Fb = p; p += (long)GF_COUNT * nf;
+  B.Cb = p; p += (long)GC_COUNT * nc;
+  B.ivb = p; p += nc;
+  B.wdf = p; p += nf;
+  B.dpart = p; p += 2 * nf;
+  B.Vb = p; p += nc;
+  B.Ab = p; p += nf;
+  B.nbt = p; p += (long)dim * nf;
+  B.xfb = p; p += (long)dim * nf;
+  B.xcpart = p; p += 2L * dim * nf;
+  B.xcb = p; p += (long)dim * nc;
+  B.wcon = p; p += (long)dim * nc;
+  B.cfA = p; p += ncf;
+  B.cfN = p; p += (long)dim * ncf;
+  B.cfX = p; p += (long)dim * ncf;
+  B.nodepart = p;
+  return B;
+}
+
+size_t nadj_doubles(int dim, long nc, long nf, long ncf, long nfn) {
+  return (size_t)GF_COUNT * nf + (size_t)GC_COUNT * nc + 2 * nc + 4 * nf + 2 * dim * nf +
+         2 * dim * nf + 2 * dim * nc + ncf * (1 + 2 * dim) + (size_t)dim * nfn;
+}
+
+int nadj_setup(FvCase* cs, cudaStream_t s) {
+  if (cs->nadj) return FV_OK;
+  FvMesh* M = cs->mesh;
+  const int dim = M->dim;
+  const long nc = M->nc, nf = M->nf;
+  const long ncf = M->h_cf_ptr[nc];
+  std::vector<int> fp(nf + 1);
+  FV_CUDA_TRY(cudaMemcpyAsync(fp.data(), M->fn_ptr, sizeof(int) * (nf + 1), cudaMemcpyDeviceToHost, s));
+  FV_CUDA_TRY(cudaStreamSynchronize(s));
+  const long nfn = fp[nf];
+  std::vector<int> fi(nfn);
+  FV_CUDA_TRY(cudaMemcpy(fi.data(), M->fn_idx, sizeof(int) * nfn, cudaMemcpyDeviceToHost));
+  // node -> entries of fn_idx (ascending)
+  std::vector<int> np(M->nn + 1, 0), ne(nfn);
+  for (long i = 0; i < nfn; ++i) np[fi[i] + 1]++;
+  for (int v = 0; v < M->nn; ++v) np[v + 1] += np[v];
+  std::vector<int> fill(np.begin(), np.end() - 1);
+  for (long i = 0; i < nfn; ++i) ne[fill[fi[i]]++] = (int)i;
+  // face -> cells whose nearest wall face it is
+  std::vector<int> wp(nf + 1, 0), wc;
+  if (cs->desc.turbulent) {
+    std::vector<int> near(nc);
+    FV_CUDA_TRY(cudaMemcpy(near.data(), cs->wnear, sizeof(int) * nc, cudaMemcpyDeviceToHost));
+    for (long c = 0; c < nc; ++c) wp[near[c] + 1]++;
+    for (long f = 0; f < nf; ++f) wp[f + 1] += wp[f];
+    wc.assign(nc, 0);
+    std::vector<int> wf(wp.begin(), wp.end() - 1);
+    for (long c = 0; c < nc; ++c) wc[wf[near[c]]++] = (int)c;
+  }
+  NodeAdjoint* na = new NodeAdjoint();
+  cs->nadj = na;
+  FV_CUDA_TRY(cudaMalloc(&na->dual_work, cs->work_bytes));
+  FV_CUDA_TRY(cudaMalloc(&na->buf, sizeof(double) * nadj_doubles(dim, nc, nf, ncf, nfn)));
+  FV_CUDA_TRY(cudaMalloc(&na->node_ptr, sizeof(int) * np.size()));
+  FV_CUDA_TRY(cudaMalloc(&na->node_ent, sizeof(int) * std::max<long>(nfn, 1)));
+  FV_CUDA_TRY(cudaMalloc(&na->wall_ptr, sizeof(int) * wp.size()));
+  FV_CUDA_TRY(cudaMalloc(&na->wall_cell, sizeof(int) * std::max<size_t>(wc.size(), 1)));
+  FV_CUDA_TRY(cudaMemcpyAsync(na->node_ptr, np.data(), sizeof(int) * np.size(), cudaMemcpyHostToDevice, s));
+  FV_CUDA_TRY(cudaMemcpyAsync(na->node_ent, ne.data(), sizeof(int) * nfn, cudaMemcpyHostToDevice, s));
+  FV_CUDA_TRY(cudaMemcpyAsync(na->wall_ptr, wp.data(), sizeof(int) * wp.size(), cudaMemcpyHostToDevice, s));
+  if (!wc.empty())
+    FV_CUDA_TRY(cudaMemcpyAsync(na->wall_cell, wc.data(), sizeof(int) * wc.size(), cudaMemcpyHostToDevice, s));
+  FV_CUDA_TRY(cudaStreamSynchronize(s));
+  return FV_OK;
+}
+
+template <int DIM, bool TURB>
+int node_vjp(FvCase* cs, const double* state, const double* W, double* dnodes, cudaStream_t s) {
+  using L = Layout<DIM, TURB>;
+  constexpr int NF = L::NFLD;
+  int rc = run_vjp<DIM, TURB>(cs, state, W, nullptr, cs->tmp2, s);  // cotangents of every stage
+  if (rc != FV_OK) return rc;
+  FvMesh* M = cs->mesh;
+  const MeshView& m = M->view;
+  const CaseView& cv = cs->view;
+  const long nc = m.nc, nf = m.nf;
+  const long ncf = M->h_cf_ptr[nc];
+  NodeAdjoint* na = cs->nadj;
+  Work<double> fw = work_layout<double, DIM, TURB>(cs->work, nc, nf);
+  Work<Dual> dw = work_layout<Dual, DIM, TURB>(na->dual_work, nc, nf);
+  AdjWork aw = adj_layout<DIM, TURB>(cs);
+  NadjBuffers B = nadj_layout(na->buf, DIM, nc, nf, ncf, 0);
+  constexpr int TB = 128;
+  const int bc = fv_blocks(nc, TB), bf = fv_blocks(nf, TB);
+  auto lift = [&](const double* src, Dual* dst, long n) {
+    k_lift<<<fv_blocks(n, 256), 256, 0, s>>>(n, src, dst);
+  };
+  lift(fw.G, dw.G, (long)NF * DIM * nc);
+  lift(fw.cl, dw.cl, 7 * nc);
+  lift(fw.Gwi, dw.Gwi, (long)DIM * nc);
+  lift(fw.dco, dw.dco, nc);
+  FV_CUDA_TRY(cudaMemsetAsync(B.Fb, 0, sizeof(double) * ((size_t)GF_COUNT * nf + (size_t)GC_COUNT * nc + nc), s));
+  FV_CUDA_TRY(cudaMemsetAsync(B.Vb, 0, sizeof(double) * nc, s));
+  FV_CUDA_TRY(cudaMemsetAsync(B.xfb, 0, sizeof(double) * DIM * nf, s));
+  const double irho = 1.0 / cs->desc.rho;
+  const Par<Dual> pd{{cs->mu, 0.0}, {cs->inlet_scale, 0.0}, {cs->mu * irho, 0.0}};
+  const Par<double> pdd{cs->mu, cs->inlet_scale, cs->mu * irho};
+  k_nadj_flux<DIM, TURB><<<bf, TB, 0, s>>>(m, cv, state, pd, dw.G, dw.cl, dw.dco, aw.Wt, B.Fb, B.wdf);
+  k_nadj_apcoef<DIM, TURB><<<bf, TB, 0, s>>>(m, cv, state, pd, dw.G, dw.cl, fw.dco, aw.dcob, B.Fb, B.wdf);
+  k_nadj_grad_face<DIM, TURB><<<bf, TB, 0, s>>>(m, cv, state, pdd, aw.Gb, B.Fb);
+  k_nadj_grad_cell<DIM, TURB><<<bc, TB, 0, s>>>(m, aw.Gb, fw.G, fw.dco, aw.dcob, B.ivb, B.Cb);
+  if constexpr (TURB) {
+    k_nadj_closure<DIM><<<bc, TB, 0, s>>>(m, cv, state, pd, dw.G, aw.clb, aw.Gwib, B.Cb, B.Fb);
+    k_nadj_src<DIM><<<bc, TB, 0, s>>>(m, cv, state, pd, dw.cl, dw.G, dw.Gwi, W, B.Cb);
+    k_nadj_wdg_face<DIM><<<bf, TB, 0, s>>>(m, cv, B.Cb, B.Fb, B.dpart);
+    k_nadj_wdg_cell<DIM><<<bc, TB, 0, s>>>(m, cv, B.dpart, B.Cb, B.Vb);
+  }
+  k_nadj_cell_chain<DIM, TURB><<<bc, TB, 0, s>>>(m, cv, B.Cb, B.ivb, B.wdf, cs->wnear, B.Vb, B.xcb,
+                                                 B.wcon);
+  if constexpr (TURB)
+    k_nadj_wall_face<DIM><<<bf, TB, 0, s>>>(m, na->wall_ptr, na->wall_cell, B.wcon, B.xfb);
+  k_nadj_factors<DIM><<<bf, TB, 0, s>>>(m, B.Fb, B.nbt, B.xfb, B.xcpart);
+  k_nadj_xc_gather<DIM><<<bc, TB, 0, s>>>(m, B.xcpart, B.xcb);
+  k_nadj_cell_geom<DIM><<<bc, TB, 0, s>>>(m, B.Vb, B.xcb, B.cfA, B.cfN, B.cfX, ncf);
+  k_nadj_cf_gather<DIM><<<bf, TB, 0, s>>>(m, B.Fb, B.cfA, B.cfN, B.cfX, ncf, B.Ab, B.nbt, B.xfb);
+  k_nadj_face_geom<DIM><<<bf, TB, 0, s>>>(m, B.Ab, B.nbt, B.xfb, B.nodepart);
+  k_nadj_nodes<<<fv_blocks(M->nn, 256), 256, 0, s>>>(M->nn, DIM, na->node_ptr, na->node_ent,
+                                                    B.nodepart, dnodes);
+  FV_CUDA_TRY(cudaGetLastError());
+  return FV_OK;
+}
+
+}  // namespace
+
+int fv_case_node_vjp(FvCase* cs, const double* state, const double* w, double* dnodes,
+                     cudaStream_t s) {
+  if (cs->desc.gradient_sweeps != 0) {
+    fv_set_error("fv_node_vjp: the mesh-coordinate adjoint supports the compact gradient scheme "
+                 "(gradient_sweeps = 0)");
+    return FV_ERR_ARG;
+  }
+  int rc = nadj_setup(cs, s);
+  if (rc != FV_OK) return rc;
+  const int dim = cs->mesh->dim;
+  const bool turb = cs->desc.turbulent != 0;
+  if (dim == 2)
+    return turb ? node_vjp<2, true>(cs, state, w, dnodes, s) : node_vjp<2, false>(cs, state, w, dnodes, s);
+  return turb ? node_vjp<3, true>(cs, state, w, dnodes, s) : node_vjp<3, false>(cs, state, w, dnodes, s);
+}
+
+void fv_node_adjoint_free(FvCase* cs) {
+  NodeAdjoint* na = cs->nadj;
+  if (!na) return;
+  cudaFree(na->dual_work);
+  cudaFree(na->buf);
+  cudaFree(na->node_ptr);
+  cudaFree(na->node_ent);
+  cudaFree(na->wall_ptr);
+  cudaFree(na->wall_cell);
+  delete na;
+  cs->nadj = nullptr;
+}

@@ -23,6 +23,7 @@
 //               wall-cell fixation (turbulence/sources.py:60-412, fixed_value.py:124-158)
 #include <type_traits>
 
+#include "geom.cuh"
 #include "internal.cuh"
 
 namespace {
@@ -74,22 +75,22 @@ __device__ __forceinline__ void put<Dual>(double* r, double* t, long i, const Du
 
 // ---------------------------------------------------------------- SST wall functions
 // aquaflux/turbulence/boundary.py:45-589.
-template <class T>
-__device__ __forceinline__ T y_star(T nu, double d, T k) {
+template <class T, class D>
+__device__ __forceinline__ T y_star(T nu, D d, T k) {
   return c_sst.bs4 * safe_sqrt(pos(k)) * d / nu;
 }
-template <class T>
-__device__ __forceinline__ T wall_weight(T nu, double d, T k) {
+template <class T, class D>
+__device__ __forceinline__ T wall_weight(T nu, D d, T k) {
   T r = y_star(nu, d, k) / c_sst.ylam;
   T r2 = r * r;
   return fv_tanh(r2 * r2);
 }
-template <class T>
-__device__ __forceinline__ T log_shear(double d, T k) {
+template <class T, class D>
+__device__ __forceinline__ T log_shear(D d, T k) {
   return c_sst.bs4 * safe_sqrt(pos(k)) / (KAPPA * d);
 }
-template <class T>
-__device__ __forceinline__ T omega_wall(T nu, double d, T k) {
+template <class T, class D>
+__device__ __forceinline__ T omega_wall(T nu, D d, T k) {
   T vis = 6.0 * nu / (BETA_1 * (d * d));
   T lg = safe_sqrt(pos(k)) / (c_sst.bs4 * KAPPA * d);
   T m = fv_max(vis, lg);
@@ -97,8 +98,8 @@ __device__ __forceinline__ T omega_wall(T nu, double d, T k) {
   T bt = val(rb) > 0.0 ? rb * rb : cst(0.0, rb);
   return m * fv_sqrt(ra * ra + bt);
 }
-template <class T>
-__device__ __forceinline__ T nut_wall(T nu, double d, T k) {
+template <class T, class D>
+__device__ __forceinline__ T nut_wall(T nu, D d, T k) {
   T ys = y_star(nu, d, k);
   T arg = E_WALL * fv_max(ys, cst(c_sst.ylam, ys));
   T ratio = ys * KAPPA / fv_log(arg) - 1.0;
@@ -106,8 +107,8 @@ __device__ __forceinline__ T nut_wall(T nu, double d, T k) {
 }
 // d omega_wall / d d and d omega_wall / d k in closed form (the reference obtains them with
 // jax.grad, boundary.py:585-589); written in T so the JVP differentiates them once more.
-template <class T>
-__device__ __forceinline__ void omega_wall_partials(T nu, double d, T k, T* dwdd, T* dwdk) {
+template <class T, class D>
+__device__ __forceinline__ void omega_wall_partials(T nu, D d, T k, T* dwdd, T* dwdk) {
   T vis = 6.0 * nu / (BETA_1 * (d * d));
   T kp = pos(k);
   T sk = safe_sqrt(kp);
@@ -147,6 +148,124 @@ __device__ __forceinline__ T bscalar(signed char kind, double value, T phi_owner
   if (kind == 1) return phi_owner + corr;
   return cst(0.0, phi_owner);
 }
+
+// ---------------------------------------------------------------- geometry accessors
+// The face and cell formulas read the mesh geometry through an accessor: GeoPlain returns the
+// stored doubles; GeoSeed returns dual numbers whose tangent is 1 on one geometric input (one
+// component, on every face / cell or on one of them), which lets the mesh-coordinate adjoint
+// differentiate the same formulas with respect to the geometry by local forward mode.
+enum GeoFace {
+  GF_AREA = 0, GF_NORMAL = 1, GF_TP = 4, GF_TN = 7, GF_G = 10, GF_DVEC = 11, GF_SKEW = 14,
+  GF_NN2 = 17, GF_INV_ND = 18, GF_INV_DPN = 19, GF_DPN = 20, GF_DNN = 21, GF_NS = 22,
+  GF_COUNT = 31
+};
+enum GeoCell { GC_VOL = 0, GC_WD = 1, GC_INV_WD = 2, GC_INV_WD2 = 3, GC_WDG = 4, GC_COUNT = 7 };
+
+struct GeoPlain {
+  __device__ __forceinline__ double area(const MeshView& m, int f) const { return m.area[f]; }
+  __device__ __forceinline__ double normal(const MeshView& m, int j, int f) const {
+    return m.normal[(long)j * m.nf + f];
+  }
+  __device__ __forceinline__ double tP(const MeshView& m, int j, int f) const {
+    return m.tP[(long)j * m.nf + f];
+  }
+  __device__ __forceinline__ double tN(const MeshView& m, int j, int f) const {
+    return m.tN[(long)j * m.nf + f];
+  }
+  __device__ __forceinline__ double g(const MeshView& m, int f) const { return m.g[f]; }
+  __device__ __forceinline__ double dvec(const MeshView& m, int j, int f) const {
+    return m.dvec[(long)j * m.nf + f];
+  }
+  __device__ __forceinline__ double skew(const MeshView& m, int j, int f) const {
+    return m.skew[(long)j * m.nf + f];
+  }
+  __device__ __forceinline__ double nn2(const MeshView& m, int f) const { return m.nn2[f]; }
+  __device__ __forceinline__ double inv_nd(const MeshView& m, int f) const { return m.inv_nd[f]; }
+  __device__ __forceinline__ double inv_dpn(const MeshView& m, int f) const {
+    return m.inv_dpn[f];
+  }
+  __device__ __forceinline__ double dpn(const MeshView& m, int f) const { return m.dpn[f]; }
+  __device__ __forceinline__ double dnn(const MeshView& m, int f) const { return m.dnn[f]; }
+  __device__ __forceinline__ double ns(const MeshView& m, int jq, int f) const {
+    return m.ns[(long)jq * m.nf + f];
+  }
+  __device__ __forceinline__ double vol(const MeshView& m, int c) const { return m.vol[c]; }
+  __device__ __forceinline__ double wd(const CaseView& cv, int c) const { return cv.wd[c]; }
+  __device__ __forceinline__ double inv_wd(const CaseView& cv, int c) const {
+    return cv.inv_wd[c];
+  }
+  __device__ __forceinline__ double inv_wd2(const CaseView& cv, int c) const {
+    return cv.inv_wd2[c];
+  }
+  __device__ __forceinline__ double wdg(const CaseView& cv, int nc, int j, int c) const {
+    return cv.wdg[(long)j * nc + c];
+  }
+};
+
+struct GeoSeed {
+  int fcomp;  // seeded face component (GeoFace), -1 for none
+  int ccomp;  // seeded cell component (GeoCell), -1 for none
+  int face;   // the one seeded face, -1 for every face
+  int cell;   // the one seeded cell, -1 for every cell
+  __device__ __forceinline__ double hf(int id, int f) const {
+    return (fcomp == id && (face < 0 || face == f)) ? 1.0 : 0.0;
+  }
+  __device__ __forceinline__ double hc(int id, int c) const {
+    return (ccomp == id && (cell < 0 || cell == c)) ? 1.0 : 0.0;
+  }
+  __device__ __forceinline__ Dual area(const MeshView& m, int f) const {
+    return {m.area[f], hf(GF_AREA, f)};
+  }
+  __device__ __forceinline__ Dual normal(const MeshView& m, int j, int f) const {
+    return {m.normal[(long)j * m.nf + f], hf(GF_NORMAL + j, f)};
+  }
+  __device__ __forceinline__ Dual tP(const MeshView& m, int j, int f) const {
+    return {m.tP[(long)j * m.nf + f], hf(GF_TP + j, f)};
+  }
+  __device__ __forceinline__ Dual tN(const MeshView& m, int j, int f) const {
+    return {m.tN[(long)j * m.nf + f], hf(GF_TN + j, f)};
+  }
+  __device__ __forceinline__ Dual g(const MeshView& m, int f) const { return {m.g[f], hf(GF_G, f)}; }
+  __device__ __forceinline__ Dual dvec(const MeshView& m, int j, int f) const {
+    return {m.dvec[(long)j * m.nf + f], hf(GF_DVEC + j, f)};
+  }
+  __device__ __forceinline__ Dual skew(const MeshView& m, int j, int f) const {
+    return {m.skew[(long)j * m.nf + f], hf(GF_SKEW + j, f)};
+  }
+  __device__ __forceinline__ Dual nn2(const MeshView& m, int f) const {
+    return {m.nn2[f], hf(GF_NN2, f)};
+  }
+  __device__ __forceinline__ Dual inv_nd(const MeshView& m, int f) const {
+    return {m.inv_nd[f], hf(GF_INV_ND, f)};
+  }
+  __device__ __forceinline__ Dual inv_dpn(const MeshView& m, int f) const {
+    return {m.inv_dpn[f], hf(GF_INV_DPN, f)};
+  }
+  __device__ __forceinline__ Dual dpn(const MeshView& m, int f) const {
+    return {m.dpn[f], hf(GF_DPN, f)};
+  }
+  __device__ __forceinline__ Dual dnn(const MeshView& m, int f) const {
+    return {m.dnn[f], hf(GF_DNN, f)};
+  }
+  __device__ __forceinline__ Dual ns(const MeshView& m, int jq, int f) const {
+    return {m.ns[(long)jq * m.nf + f], hf(GF_NS + jq, f)};
+  }
+  __device__ __forceinline__ Dual vol(const MeshView& m, int c) const {
+    return {m.vol[c], hc(GC_VOL, c)};
+  }
+  __device__ __forceinline__ Dual wd(const CaseView& cv, int c) const {
+    return {cv.wd[c], hc(GC_WD, c)};
+  }
+  __device__ __forceinline__ Dual inv_wd(const CaseView& cv, int c) const {
+    return {cv.inv_wd[c], hc(GC_INV_WD, c)};
+  }
+  __device__ __forceinline__ Dual inv_wd2(const CaseView& cv, int c) const {
+    return {cv.inv_wd2[c], hc(GC_INV_WD2, c)};
+  }
+  __device__ __forceinline__ Dual wdg(const CaseView& cv, int nc, int j, int c) const {
+    return {cv.wdg[(long)j * nc + c], hc(GC_WDG + j, c)};
+  }
+};
 
 template <int DIM, bool TURB>
 struct Layout {
@@ -351,12 +470,14 @@ void gg_sweeps(const MeshView& m, int sweeps, double rel, const T* Bg, T* G0, T*
 }
 
 // ---------------------------------------------------------------- k_closure (SST)
-template <class T, int DIM>
-__global__ void __launch_bounds__(128) k_closure(MeshView m, CaseView cv, Src<T> st, Par<T> par,
-                                                 const T* G, T* cl, T* Gwi) {
+// The closure of cell c: out = (S, F1, nu_t, wall shear rate, k diffusivity, omega diffusivity,
+// F2), gw = the omega gradient with the wall-cell value imposed.
+template <class T, int DIM, class S_, class GV>
+__device__ __forceinline__ void closure_cell(const MeshView& m, const CaseView& cv, const S_& st,
+                                             const Par<T>& par, const T* G, int c, const GV& gv,
+                                             T* out, T* gw) {
   using L = Layout<DIM, true>;
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= m.nc) return;
+  using GT = decltype(gv.area(m, 0));
   const int nc = m.nc, nf = m.nf;
   T gu[DIM][DIM];
 #pragma unroll
@@ -375,8 +496,8 @@ __global__ void __launch_bounds__(128) k_closure(MeshView m, CaseView cv, Src<T>
   const T k = st((long)L::K * nc + c);
   const T w = st((long)L::W * nc + c);
   const T nu = par.nu;
-  const double d = cv.wd[c], id = cv.inv_wd[c], id2 = cv.inv_wd2[c];
-  T gk[DIM], gw[DIM];
+  const GT d = gv.wd(cv, c), id = gv.inv_wd(cv, c), id2 = gv.inv_wd2(cv, c);
+  T gk[DIM];
 #pragma unroll
   for (int j = 0; j < DIM; ++j) {
     gk[j] = G[((long)L::K * DIM + j) * nc + c];
@@ -389,9 +510,9 @@ __global__ void __launch_bounds__(128) k_closure(MeshView m, CaseView cv, Src<T>
     T dwdd, dwdk;
     omega_wall_partials(nu, d, k, &dwdd, &dwdk);
 #pragma unroll
-    for (int j = 0; j < DIM; ++j) gw[j] = cv.wdg[(long)j * nc + c] * dwdd + gk[j] * dwdk;
+    for (int j = 0; j < DIM; ++j) gw[j] = gv.wdg(cv, nc, j, c) * dwdd + gk[j] * dwdk;
     T num = cst(0.0, k);
-    double den = 0.0;
+    GT den{};
     T u[DIM];
 #pragma unroll
     for (int j = 0; j < DIM; ++j) u[j] = st((long)j * nc + c);
@@ -406,8 +527,9 @@ __global__ void __launch_bounds__(128) k_closure(MeshView m, CaseView cv, Src<T>
         T sl = u[j] - bvel(cv, nf, f, j, kind, u[j], par);
         s2 += sl * sl;
       }
-      num += safe_sqrt(s2) * m.area[f];
-      den += m.area[f];
+      const GT af = gv.area(m, f);
+      num += safe_sqrt(s2) * af;
+      den += af;
     }
     shear = num * (id / den);
   }
@@ -427,13 +549,25 @@ __global__ void __launch_bounds__(128) k_closure(MeshView m, CaseView cv, Src<T>
   const T arg2 = fv_max(2.0 * c1, vt);
   const T F2 = fv_tanh(arg2 * arg2);
   const T nut = A1 * kp / fv_max(A1 * w, S * F2);
-  cl[c] = S;
-  cl[(long)nc + c] = F1;
-  cl[2L * nc + c] = nut;
-  cl[3L * nc + c] = shear;
-  cl[4L * nc + c] = nu + (SIGMA_K2 + F1 * (SIGMA_K1 - SIGMA_K2)) * nut;
-  cl[5L * nc + c] = nu + (SIGMA_W2 + F1 * (SIGMA_W1 - SIGMA_W2)) * nut;
-  cl[6L * nc + c] = F2;
+  out[0] = S;
+  out[1] = F1;
+  out[2] = nut;
+  out[3] = shear;
+  out[4] = nu + (SIGMA_K2 + F1 * (SIGMA_K1 - SIGMA_K2)) * nut;
+  out[5] = nu + (SIGMA_W2 + F1 * (SIGMA_W1 - SIGMA_W2)) * nut;
+  out[6] = F2;
+}
+
+template <class T, int DIM>
+__global__ void __launch_bounds__(128) k_closure(MeshView m, CaseView cv, Src<T> st, Par<T> par,
+                                                 const T* G, T* cl, T* Gwi) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nc) return;
+  const int nc = m.nc;
+  T out[7], gw[DIM];
+  closure_cell<T, DIM>(m, cv, st, par, G, c, GeoPlain{}, out, gw);
+#pragma unroll
+  for (int i = 0; i < 7; ++i) cl[(long)i * nc + c] = out[i];
 #pragma unroll
   for (int j = 0; j < DIM; ++j) Gwi[(long)j * nc + c] = gw[j];
 }
@@ -447,17 +581,17 @@ __device__ __forceinline__ T mu_eff(const Par<T>& par, double rho, const T* cl, 
 
 // lagged advective momentum flux (rho u)_f . n with the skew-corrected face value
 // (aquaflux/flow/rhie_chow.py:220-271): rho (sum_j n_j u_j,f + sum_jq n_j skew_q (grad u)_jq,f)
-template <class T, int DIM, bool TURB, class S>
+template <class T, int DIM, bool TURB, class S, class GV, class GT>
 __device__ __forceinline__ T mom_normal(const MeshView& m, const S& st, const T* G, double rho,
-                                        int f, int o, int n, double g) {
-  const int nc = m.nc, nf = m.nf;
+                                        int f, int o, int n, GT g, const GV& gv) {
+  const int nc = m.nc;
   T mn = cst(0.0, st(o));
 #pragma unroll
   for (int j = 0; j < DIM; ++j) {
-    mn += m.normal[(long)j * nf + f] * lerp(st((long)j * nc + o), st((long)j * nc + n), g);
+    mn += gv.normal(m, j, f) * lerp(st((long)j * nc + o), st((long)j * nc + n), g);
 #pragma unroll
     for (int q = 0; q < DIM; ++q)
-      mn += m.ns[(long)(j * DIM + q) * nf + f] *
+      mn += gv.ns(m, j * DIM + q, f) *
             lerp(G[((long)j * DIM + q) * nc + o], G[((long)j * DIM + q) * nc + n], g);
   }
   return rho * mn;
@@ -465,46 +599,60 @@ __device__ __forceinline__ T mom_normal(const MeshView& m, const S& st, const T*
 
 // flux-continuous conductance g_o A / (dpn - g_o / g_n dnn), one division
 // (aquaflux/discretization/diffusion.py:85-134)
-template <class T>
-__device__ __forceinline__ T conductance(T go, T gn, double A, double dpn, double dnn) {
+template <class T, class GT>
+__device__ __forceinline__ T conductance(T go, T gn, GT A, GT dpn, GT dnn) {
   return go * gn * A / (dpn * gn - go * dnn);
 }
 
 // ---------------------------------------------------------------- k_apcoef
-template <class T, int DIM, bool TURB>
-__global__ void __launch_bounds__(128) k_apcoef(MeshView m, CaseView cv, Src<T> st, Par<T> par,
-                                                const T* G, const T* cl, T* ac_own, T* ac_nb,
-                                                T* me) {
+// The momentum-diagonal face coefficients of face f (owner side, neighbour side) and the lagged
+// mass-flux estimate me.
+template <class T, int DIM, bool TURB, class S_, class GV>
+__device__ __forceinline__ void apcoef_face(const MeshView& m, const CaseView& cv, const S_& st,
+                                            const Par<T>& par, const T* G, const T* cl, int f,
+                                            const GV& gv, T& ac_own, T& ac_nb, T& me) {
   using L = Layout<DIM, TURB>;
-  const int f = blockIdx.x * blockDim.x + threadIdx.x;
-  if (f >= m.nf) return;
+  using GT = decltype(gv.area(m, 0));
   const int nc = m.nc;
   const int o = m.owner[f];
   const bool interior = f < m.nfi;
   const int n = interior ? m.nb[f] : o;
-  const double g = m.g[f], A = m.area[f];
+  const GT g = gv.g(m, f), A = gv.area(m, f);
   const double rho = cv.rho;
-  const T mdot = mom_normal<T, DIM, TURB>(m, st, G, rho, f, o, n, g) * A;
-  me[f] = mdot;
+  const T mdot = mom_normal<T, DIM, TURB>(m, st, G, rho, f, o, n, g, gv) * A;
+  me = mdot;
   const T mo = mu_eff<T, TURB>(par, rho, cl, nc, o);
   if (interior) {
     const T mnb = mu_eff<T, TURB>(par, rho, cl, nc, n);
-    const T visc = conductance(mo, mnb, A, m.dpn[f], m.dnn[f]);
-    ac_own[f] = visc + pos(mdot);
-    ac_nb[f] = visc + pos(-mdot);
+    const T visc = conductance(mo, mnb, A, gv.dpn(m, f), gv.dnn(m, f));
+    ac_own = visc + pos(mdot);
+    ac_nb = visc + pos(-mdot);
   } else {
     const signed char kind = cv.fkind[f];
     T bv = mo;
     if (TURB && (kind == 0 || kind == 1)) {
       T nutw = cst(0.0, mo);
-      if (cv.swall[f]) nutw = nut_wall(par.nu, cv.wd[o], st((long)L::K * nc + o));
+      if (cv.swall[f]) nutw = nut_wall(par.nu, gv.wd(cv, o), st((long)L::K * nc + o));
       bv = par.mu + rho * nutw;
     }
-    const T vo = bv * (A * m.inv_nd[f]);
+    const T vo = bv * (A * gv.inv_nd(m, f));
     const T conv = pos(mdot);
-    ac_own[f] = kind == 0 || kind == 1 ? vo : (kind == 2 ? vo + conv : (kind == 3 ? conv : cst(0.0, vo)));
-    ac_nb[f] = cst(0.0, vo);
+    ac_own = kind == 0 || kind == 1 ? vo : (kind == 2 ? vo + conv : (kind == 3 ? conv : cst(0.0, vo)));
+    ac_nb = cst(0.0, vo);
   }
+}
+
+template <class T, int DIM, bool TURB>
+__global__ void __launch_bounds__(128) k_apcoef(MeshView m, CaseView cv, Src<T> st, Par<T> par,
+                                                const T* G, const T* cl, T* ac_own, T* ac_nb,
+                                                T* me) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= m.nf) return;
+  T ao, an, mf;
+  apcoef_face<T, DIM, TURB>(m, cv, st, par, G, cl, f, GeoPlain{}, ao, an, mf);
+  ac_own[f] = ao;
+  ac_nb[f] = an;
+  me[f] = mf;
 }
 
 // ---------------------------------------------------------------- k_dcoeff
@@ -536,45 +684,47 @@ struct Aux {
 
 // The fluxes of face f, handed to wr(q, flux_q) for every field q.  `st` reads the state (Src, or
 // a seeded accessor in the Jacobian assembly); aux (double only) receives the face intermediates.
-template <class T, int DIM, bool TURB, class S, class Wr>
+template <class T, int DIM, bool TURB, class S, class Wr, class GV = GeoPlain>
 __device__ __forceinline__ void flux_face(const MeshView& m, const CaseView& cv, const S& st,
                                           const Par<T>& par, const T* G, const T* cl, const T* dco,
                                           const T* me, bool recompute_me, int f, const Wr& wr,
-                                          double* aux) {
-  constexpr bool KEEP = std::is_same<T, double>::value;
+                                          double* aux, const GV& gv = GV{}) {
+  using GT = decltype(gv.area(m, 0));
+  constexpr bool KEEP = std::is_same<T, double>::value && std::is_same<GT, double>::value;
   using L = Layout<DIM, TURB>;
   const int nc = m.nc, nf = m.nf;
   const int o = m.owner[f];
-  const double A = m.area[f], rho = cv.rho, irho = 1.0 / cv.rho;
-  double nrm[DIM], tP[DIM];
+  const GT A = gv.area(m, f);
+  const double rho = cv.rho, irho = 1.0 / cv.rho;
+  GT nrm[DIM], tP[DIM];
 #pragma unroll
   for (int j = 0; j < DIM; ++j) {
-    nrm[j] = m.normal[(long)j * nf + f];
-    tP[j] = m.tP[(long)j * nf + f];
+    nrm[j] = gv.normal(m, j, f);
+    tP[j] = gv.tP(m, j, f);
   }
   const T po = st((long)L::P * nc + o);
   const T mo = mu_eff<T, TURB>(par, rho, cl, nc, o);
   if (f < m.nfi) {
     const int n = m.nb[f];
-    const double g = m.g[f];
-    double tN[DIM];
+    const GT g = gv.g(m, f);
+    GT tN[DIM];
 #pragma unroll
-    for (int j = 0; j < DIM; ++j) tN[j] = m.tN[(long)j * nf + f];
+    for (int j = 0; j < DIM; ++j) tN[j] = gv.tN(m, j, f);
     const T pn = st((long)L::P * nc + n);
-    const T mest = recompute_me ? mom_normal<T, DIM, TURB>(m, st, G, rho, f, o, n, g) * A : me[f];
+    const T mest = recompute_me ? mom_normal<T, DIM, TURB>(m, st, G, rho, f, o, n, g, gv) * A : me[f];
     T gd = cst(0.0, po), gs = cst(0.0, po);
 #pragma unroll
     for (int j = 0; j < DIM; ++j) {
       const T gpf = lerp(G[((long)L::P * DIM + j) * nc + o], G[((long)L::P * DIM + j) * nc + n], g);
-      gd += gpf * m.dvec[(long)j * nf + f];
-      gs += gpf * m.skew[(long)j * nf + f];
+      gd += gpf * gv.dvec(m, j, f);
+      gs += gpf * gv.skew(m, j, f);
     }
-    const T dhat = m.nn2[f] * lerp(dco[o], dco[n], g);
-    const T damping = ((pn - po) - gd) * m.inv_nd[f];
+    const T dhat = gv.nn2(m, f) * lerp(dco[o], dco[n], g);
+    const T damping = ((pn - po) - gd) * gv.inv_nd(m, f);
     const T mdot = mest - (rho * A) * dhat * damping;
     const T pf = lerp(po, pn, g) + gs;
     const T mnb = mu_eff<T, TURB>(par, rho, cl, nc, n);
-    const T iden = 1.0 / (m.dpn[f] * mnb - mo * m.dnn[f]);
+    const T iden = 1.0 / (gv.dpn(m, f) * mnb - mo * gv.dnn(m, f));
     const T cmo = mo * mnb * A * iden;
     const bool out = val(mdot) >= 0.0;
     const T pA = pf * A;
@@ -614,7 +764,7 @@ __device__ __forceinline__ void flux_face(const MeshView& m, const CaseView& cv,
 #pragma unroll
         for (int j = 0; j < DIM; ++j)
           cpn += G[((long)q * DIM + j) * nc + n] * tN[j] - G[((long)q * DIM + j) * nc + o] * tP[j];
-        const T idn = 1.0 / (m.dpn[f] * gn - go * m.dnn[f]);
+        const T idn = 1.0 / (gv.dpn(m, f) * gn - go * gv.dnn(m, f));
         const T cs_ = go * gn * A * idn;
         wr(q, vflux * (vout ? phio : phin) - cs_ * cpn);
         if constexpr (KEEP) {
@@ -650,8 +800,8 @@ __device__ __forceinline__ void flux_face(const MeshView& m, const CaseView& cv,
         un += uo[j] * nrm[j];
         interp += G[((long)L::P * DIM + j) * nc + o] * nrm[j];
       }
-      const T dh = m.nn2[f] * dco[o];
-      const T compact = (cv.fp[f] - po) * m.inv_nd[f];
+      const T dh = gv.nn2(m, f) * dco[o];
+      const T compact = (cv.fp[f] - po) * gv.inv_nd(m, f);
       mdot = (rho * A) * (un - dh * (compact - interp));
     } else {
       mdot = cst(0.0, po);
@@ -660,10 +810,10 @@ __device__ __forceinline__ void flux_face(const MeshView& m, const CaseView& cv,
     T gb = mo;
     if (TURB && (kind == 0 || kind == 1)) {
       T nutw = cst(0.0, mo);
-      if (cv.swall[f]) nutw = nut_wall(par.nu, cv.wd[o], st((long)L::K * nc + o));
+      if (cv.swall[f]) nutw = nut_wall(par.nu, gv.wd(cv, o), st((long)L::K * nc + o));
       gb = par.mu + rho * nutw;
     }
-    const T gA = gb * (A * m.inv_dpn[f]);
+    const T gA = gb * (A * gv.inv_dpn(m, f));
     const bool out = val(mdot) >= 0.0;
     const T pA = pf * A;
 #pragma unroll
@@ -688,8 +838,8 @@ __device__ __forceinline__ void flux_face(const MeshView& m, const CaseView& cv,
         const T bphi = s == 0 ? bscalar(cv.kkind[f], cv.kval[f], phio, cp)
                               : bscalar(cv.wkind[f], cv.wval[f], phio, cp);
         T gface = go;
-        if (s == 0 && cv.swall[f]) gface = (1.0 - wall_weight(par.nu, cv.wd[o], phio)) * go;
-        wr(q, vflux * (vout ? phio : bphi) - gface * (A * m.inv_dpn[f]) * (bphi - phio - cp));
+        if (s == 0 && cv.swall[f]) gface = (1.0 - wall_weight(par.nu, gv.wd(cv, o), phio)) * go;
+        wr(q, vflux * (vout ? phio : bphi) - gface * (A * gv.inv_dpn(m, f)) * (bphi - phio - cp));
       }
     }
   }
@@ -715,17 +865,18 @@ __global__ void __launch_bounds__(128) k_flux(MeshView m, CaseView cv, Src<T> st
 // ---------------------------------------------------------------- k_sum
 // SST rows of cell c: k and omega source terms added to the face sums rk / rw, and the omega
 // wall-cell fixation (aquaflux/turbulence/sources.py:60-412, fixed_value.py:124-158).
-template <class T, int DIM, class Acc>
+template <class T, int DIM, class Acc, class GV = GeoPlain>
 __device__ __forceinline__ void sst_rows(const MeshView& m, const CaseView& cv, const Acc& st,
                                          const Par<T>& par, const T* cl, const T* G, const T* Gwi,
-                                         int c, T& rk, T& rw) {
+                                         int c, T& rk, T& rw, const GV& gv = GV{}) {
   using L = Layout<DIM, true>;
+  using GT = decltype(gv.area(m, 0));
   const int nc = m.nc;
-  const double V = m.vol[c];
+  const GT V = gv.vol(m, c);
   const T k = st((long)L::K * nc + c), w = st((long)L::W * nc + c);
   const T S = cl[c], F1 = cl[(long)nc + c], nut = cl[2L * nc + c];
   const T nu = par.nu;
-  const double d = cv.wd[c];
+  const GT d = gv.wd(cv, c);
   const bool wall = cv.wcell[c] != 0;
   const T kp = pos(k);
   const T limit = (PROD_RATIO * BETA_STAR) * kp * w;
@@ -860,6 +1011,23 @@ int dispatch_t(FvCase* cs, const double* state, const double* tangent, int kind,
 #include "assemble.inc.cuh"
 
 template <int DIM, bool TURB>
+AdjWork adj_layout(FvCase* cs) {
+  using L = Layout<DIM, TURB>;
+  const long nc = cs->mesh->view.nc;
+  AdjWork aw;
+  double* p = cs->adj;
+  aw.Wt = p; p += L::NFLD * nc;
+  aw.sb = p; p += L::NFLD * nc;
+  aw.Gb = p; p += L::NFLD * DIM * nc;
+  aw.dcob = p; p += nc;
+  aw.clb = p; p += 4 * nc;
+  aw.Gwib = p; p += DIM * nc;
+  aw.Gb2 = p; p += L::NFLD * DIM * nc;  // present when the case is swept
+  aw.Bb = p;
+  return aw;
+}
+
+template <int DIM, bool TURB>
 int run_vjp(FvCase* cs, const double* state, const double* W, double* R, double* out,
             cudaStream_t s) {
   using L = Layout<DIM, TURB>;
@@ -876,16 +1044,7 @@ int run_vjp(FvCase* cs, const double* state, const double* W, double* R, double*
   double* cl = fw.cl;
   double* Gwi = fw.Gwi;
   double* dco = fw.dco;
-  AdjWork aw;
-  double* p = cs->adj;
-  aw.Wt = p; p += L::NFLD * nc;
-  aw.sb = p; p += L::NFLD * nc;
-  aw.Gb = p; p += L::NFLD * DIM * nc;
-  aw.dcob = p; p += nc;
-  aw.clb = p; p += 4 * nc;
-  aw.Gwib = p; p += DIM * nc;
-  aw.Gb2 = p; p += L::NFLD * DIM * nc;  // present when the case is swept
-  aw.Bb = p;
+  AdjWork aw = adj_layout<DIM, TURB>(cs);
   constexpr int TB = 128;
   const int bc = fv_blocks(nc, TB);
   a_sum<DIM, TURB><<<bc, TB, 0, s>>>(m, cv, st, par, W, cl, G, Gwi, aw);
@@ -913,6 +1072,8 @@ int run_vjp(FvCase* cs, const double* state, const double* W, double* R, double*
 bool g_const_ready = false;
 
 }  // namespace
+
+#include "node_adjoint.inc.cuh"
 
 size_t fv_adjoint_work_bytes(int dim, int turb, long nc, int sweeps) {
   long nfld = dim + 1 + (turb ? 2 : 0);

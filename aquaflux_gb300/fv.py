@@ -176,6 +176,15 @@ class FlowCase:
         check(lib().fv_jvp(self._h, ptr(s), ptr(vv), ptr(r), ptr(jv), _stream()))
         return (r, jv) if return_residual else jv
 
+    def node_vjp(self, state, w) -> torch.Tensor:
+        """``d/dnodes (w . R(state, nodes))``, shape ``(n_nodes, dim)`` (the mesh-coordinate
+        adjoint; compact gradient scheme)."""
+        s, ww = self._vec(state), self._vec(w)
+        mesh = self.dmesh.mesh
+        out = torch.empty(mesh.n_nodes, mesh.dim, dtype=torch.float64, device="cuda")
+        check(lib().fv_node_vjp(self._h, ptr(s), ptr(ww), ptr(out), _stream()))
+        return out
+
     def jvp_batch(self, state, vs) -> torch.Tensor:
         """``J(state) v_i`` for every row of the ``(k, n)`` seed block ``vs``."""
         s = self._vec(state)

@@ -157,6 +157,14 @@ int fv_vjp(FvCase* c, const double* state, const double* w, double* residual, do
 /* Parameter cotangents w^T dR/dtheta for theta = (mu, inlet_scale): the vjp_theta of
  * aquaflux/solve/implicit.py:759-760.  `out` is a device array of 2 doubles. */
 int fv_param_vjp(FvCase* c, const double* state, const double* w, double* out, void* stream);
+/* dnodes = d/dnodes (w . R(state, nodes)): the mesh-coordinate adjoint (the node-coordinate part
+ * of theta_bar in _implicit_solve_bwd, aquaflux/solve/implicit.py:733-761), through the face
+ * areas, normals and centroids, the cell volumes and centroids, every factor derived from them and
+ * (turbulent cases) the wall distance to the nearest wall face and its gradient; the owner-outward
+ * normal flip is a constant sign.  Device (n_nodes, dim) row-major output in the caller's node
+ * order.  Compact gradient scheme only (FV_ERR_ARG otherwise).  Allocates a workspace with the
+ * case on first use. */
+int fv_node_vjp(FvCase* c, const double* state, const double* w, double* dnodes, void* stream);
 
 /* Per-stage CUDA-event timing of the next `max_runs` pipeline runs on this case (diagnostics;
  * no reference counterpart).  profile_end synchronizes, writes the summed milliseconds of each

@@ -343,6 +343,39 @@ def wall_distance(case, geo) -> tuple[torch.Tensor, torch.Tensor]:
     return dist, gg_gradient(m, dist, bvals, case.get("gradient"))
 
 
+def nearest_wall_face(case, geo) -> np.ndarray:
+    """Index (into the face arrays) of every cell's nearest SST wall-face centroid, first minimum."""
+    sc = case["sst"]
+    cc = geo["cell_centroid"].detach().numpy()
+    wf = np.asarray(sc["wall_faces"])
+    tgt = geo["face_centroid"].detach().numpy()[wf]
+    best = np.full(cc.shape[0], np.inf)
+    arg = np.zeros(cc.shape[0], dtype=np.int64)
+    for start in range(0, tgt.shape[0], 256):
+        blk = tgt[start:start + 256]
+        d2 = ((cc[:, None, :] - blk[None, :, :]) ** 2).sum(-1)
+        k = d2.argmin(axis=1)
+        v = d2[np.arange(cc.shape[0]), k]
+        better = v < best
+        best = np.where(better, v, best)
+        arg = np.where(better, start + k, arg)
+    return wf[arg]
+
+
+def wall_distance_live(case, geo, m, nearest):
+    """The wall distance and its gradient as differentiable functions of the geometry, the nearest
+    wall face held fixed (the mesh-coordinate derivative of ``distance_to_patches``)."""
+    sc = case["sst"]
+    topo = m.topo
+    dv = geo["cell_centroid"] - geo["face_centroid"][torch.as_tensor(nearest)]
+    dist = torch.sqrt((dv * dv).sum(-1))
+    is_wall = np.zeros(topo.n_faces, dtype=bool)
+    is_wall[sc["wall_faces"]] = True
+    bvals = torch.where(torch.as_tensor(is_wall), torch.zeros(topo.n_faces, dtype=T),
+                        dist[topo.owner])
+    return dist, gg_gradient(m, dist, bvals, case.get("gradient"))
+
+
 # ----------------------------------------------------------------------------- SST pieces
 def safe_sqrt(x):
     pos = x > 0.0
@@ -446,6 +479,7 @@ class Oracle:
 
     def __init__(self, case, nodes=None):
         self.case = case
+        self._live_geometry = False
         mesh = case["mesh"]
         self.topo = Topology(mesh.owner, mesh.neighbour, mesh.n_cells, mesh.fn_offsets,
                              mesh.fn_indices)
@@ -457,6 +491,7 @@ class Oracle:
         if case["sst"] is not None:
             geo0 = geometry(self.topo, _t(mesh.nodes))
             self.wall_d, self.wall_dgrad = wall_distance(case, geo0)
+            self._nearest = None
 
     # --- boundary tables ----------------------------------------------------------------------
     def _boundary_velocity(self, u):
@@ -490,6 +525,8 @@ class Oracle:
         """
         case, topo, dim = self.case, self.topo, self.dim
         nc = topo.n_cells
+        # with node coordinates given, the SST wall distance follows the geometry too
+        self._live_geometry = nodes is not None
         nodes = self.nodes if nodes is None else nodes
         geo = geometry(topo, nodes)
         m = Metrics(topo, geo)
@@ -532,6 +569,10 @@ class Oracle:
             w = state[n_flow + nc:]
             nu = (mu / rho) * torch.ones(nc, dtype=T)
             dist, dgrad = self.wall_d, self.wall_dgrad
+            if self._live_geometry:
+                if self._nearest is None:
+                    self._nearest = nearest_wall_face(case, geometry(topo, self.nodes))
+                dist, dgrad = wall_distance_live(case, geo, m, self._nearest)
             wc = torch.as_tensor(sst["wall_cells"])
             wf = torch.as_tensor(sst["wall_faces"])
             # closure_fields, transport.py:548-579
