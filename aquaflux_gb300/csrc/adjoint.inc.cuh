@@ -42,6 +42,7 @@ struct AdjWork {
   double* Gwib;  // (D, nc) imposed omega-gradient adjoint
   double* Gb2;   // (NF, D, nc) second iterate cotangent of the corrected-gradient sweeps
   double* Bb;    // (NF, D, nc) cotangent of the corrected scheme's right-hand side B phi
+  const double* FLx;  // (NF, nf) extra face-flux cotangent (a face-flux functional), or null
 };
 
 // ---------------------------------------------------------------- a_sum
@@ -259,7 +260,9 @@ __global__ void __launch_bounds__(128) a_flux(MeshView m, CaseView cv, Src<doubl
       for (int j = 0; j < DIM; ++j) tN[j] = m.tN[(long)j * nf + f];
       double FLb[NF];
 #pragma unroll
-      for (int q = 0; q < NF; ++q) FLb[q] = aw.Wt[(long)q * nc + o] - aw.Wt[(long)q * nc + n];
+      for (int q = 0; q < NF; ++q)
+        FLb[q] = aw.Wt[(long)q * nc + o] - aw.Wt[(long)q * nc + n] +
+                 (aw.FLx ? aw.FLx[(long)q * nf + f] : 0.0);
       // forward face intermediates kept by k_flux
       const double mdot = aux[0L * nf + f];
       const double damping = aux[1L * nf + f];
@@ -347,7 +350,8 @@ __global__ void __launch_bounds__(128) a_flux(MeshView m, CaseView cv, Src<doubl
       const signed char kind = cv.fkind[f];
       double FLb[NF];
 #pragma unroll
-      for (int q = 0; q < NF; ++q) FLb[q] = aw.Wt[(long)q * nc + o];
+      for (int q = 0; q < NF; ++q)
+        FLb[q] = aw.Wt[(long)q * nc + o] + (aw.FLx ? aw.FLx[(long)q * nf + f] : 0.0);
       double uo[DIM], bu[DIM];
 #pragma unroll
       for (int j = 0; j < DIM; ++j) {

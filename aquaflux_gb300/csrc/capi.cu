@@ -187,6 +187,8 @@ extern "C" int fv_case_destroy(FvCase* c) {
   cudaFree(c->jac_face);
   cudaFree(c->wnear);
   fv_node_adjoint_free(c);
+  cudaFree(c->flx);
+  cudaFree(c->red);
   for (cudaEvent_t e : c->prof_events) cudaEventDestroy(e);
   delete c;
   return FV_OK;
@@ -371,6 +373,17 @@ extern "C" int fv_node_vjp(FvCase* c, const double* state, const double* w, doub
     return FV_ERR_ARG;
   }
   return fv_case_node_vjp(c, state, w, dnodes, (cudaStream_t)stream);
+}
+
+extern "C" int fv_face_functional(FvCase* c, const double* state, const double* weights,
+                                  int viscous_only, double* value, double* dstate,
+                                  double* dparams, double* dnodes, void* stream) {
+  if (!c || !state || !weights || !value || !dstate) {
+    fv_set_error("fv_face_functional: bad arguments");
+    return FV_ERR_ARG;
+  }
+  return fv_case_face_functional(c, state, weights, viscous_only, value, dstate, dparams, dnodes,
+                                 (cudaStream_t)stream);
 }
 
 extern "C" int fv_param_vjp(FvCase* c, const double* state, const double* w, double* out,

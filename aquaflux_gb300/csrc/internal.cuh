@@ -126,6 +126,10 @@ struct FvCase {
   double* jac_face = nullptr; // (2, nfld, nfld, nf) face flux derivatives of the Jacobian assembly
   int* wnear = nullptr;       // (nc) nearest SST wall face (internal index), turbulent cases
   NodeAdjoint* nadj = nullptr;  // mesh-coordinate adjoint workspace, allocated on first use
+  double* flx = nullptr;        // (nfld, nf) weights of a face-flux functional (internal order)
+  bool flx_active = false;      // the adjoints add flx to their face-flux cotangents
+  bool flx_viscous = false;     // ... with the pressure part p_f A n_i taken out
+  double* red = nullptr;        // reduction partials of the functional
   CaseView view;
   // optional per-stage CUDA-event profiling (fv_case_profile_begin / _end)
   std::vector<cudaEvent_t> prof_events;  // max_runs * (FV_MAX_STAGES + 1)
@@ -149,6 +153,11 @@ int fv_case_vjp_run(FvCase* c, const double* state, const double* w, double* res
 int fv_case_node_vjp(FvCase* c, const double* state, const double* w, double* dnodes,
                      cudaStream_t s);
 void fv_node_adjoint_free(FvCase* c);
+// Face-flux functional J = sum_f sum_q w_qf FL_q(f) (- the pressure part), its value and partial
+// derivatives (residual.cu).
+int fv_case_face_functional(FvCase* c, const double* state, const double* weights_ref,
+                            int viscous_only, double* value, double* dstate, double* dparams,
+                            double* dnodes, cudaStream_t s);
 int fv_case_assemble_frozen(FvCase* c, const double* state, const int* indptr, const int* indices,
                             double* values, double* D, cudaStream_t s);
 size_t fv_jac_face_bytes(int dim, int turb, long nf);

@@ -35,8 +35,8 @@ struct Contract {
 template <int DIM, bool TURB>
 __global__ void __launch_bounds__(128) k_nadj_flux(MeshView m, CaseView cv, const double* state,
                                                    Par<Dual> par, const Dual* G, const Dual* cl,
-                                                   const Dual* dco, const double* Wt, double* Fb,
-                                                   double* wdf) {
+                                                   const Dual* dco, const double* Wt,
+                                                   const double* FLx, double* Fb, double* wdf) {
   constexpr int NF = Layout<DIM, TURB>::NFLD;
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= m.nf) return;
@@ -46,7 +46,8 @@ __global__ void __launch_bounds__(128) k_nadj_flux(MeshView m, CaseView cv, cons
   double FLb[NF];
 #pragma unroll
   for (int q = 0; q < NF; ++q)
-    FLb[q] = Wt[(long)q * nc + o] - (interior ? Wt[(long)q * nc + m.nb[f]] : 0.0);
+    FLb[q] = Wt[(long)q * nc + o] - (interior ? Wt[(long)q * nc + m.nb[f]] : 0.0) +
+             (FLx ? FLx[(long)q * nf + f] : 0.0);
   const Src<Dual> st{state, nullptr};
 #pragma unroll 1
   for (int comp = 0; comp < GF_COUNT; ++comp) {
@@ -508,6 +509,27 @@ __global__ void k_nadj_nodes(int nn, int dim, const int* node_ptr, const int* no
   }
 }
 
+// The pressure part sum_i w_i p_f A n_i of a viscous-only functional on boundary faces: its
+// geometry cotangents are subtracted (p_f = the owner pressure, or the outlet value).
+template <int DIM, bool TURB>
+__global__ void k_nadj_pressure_term(MeshView m, CaseView cv, const double* state,
+                                     const double* FLx, double* Fb) {
+  using L = Layout<DIM, TURB>;
+  const int f = m.nfi + blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= m.nf) return;
+  const int nf = m.nf;
+  const int o = m.owner[f];
+  const double pf = bpress(cv, f, cv.fkind[f], state[(long)L::P * m.nc + o]);
+  const double A = m.area[f];
+  double ab = 0.0;
+  for (int i = 0; i < DIM; ++i) {
+    const double wi = FLx[(long)i * nf + f];
+    ab += wi * pf * m.normal[(long)i * nf + f];
+    Fb[(long)(GF_NORMAL + i) * nf + f] -= wi * pf * A;
+  }
+  Fb[(long)GF_AREA * nf + f] -= ab;
+}
+
 struct NadjBuffers {
   double *Fb, *Cb, *ivb, *wdf, *dpart, *Vb, *Ab, *nbt, *xfb, *xcpart, *xcb, *wcon, *cfA, *cfN,
       *cfX, *nodepart;
@@ -616,7 +638,10 @@ int node_vjp(FvCase* cs, const double* state, const double* W, double* dnodes, c
   const double irho = 1.0 / cs->desc.rho;
   const Par<Dual> pd{{cs->mu, 0.0}, {cs->inlet_scale, 0.0}, {cs->mu * irho, 0.0}};
   const Par<double> pdd{cs->mu, cs->inlet_scale, cs->mu * irho};
-  k_nadj_flux<DIM, TURB><<<bf, TB, 0, s>>>(m, cv, state, pd, dw.G, dw.cl, dw.dco, aw.Wt, B.Fb, B.wdf);
+  k_nadj_flux<DIM, TURB><<<bf, TB, 0, s>>>(m, cv, state, pd, dw.G, dw.cl, dw.dco, aw.Wt, aw.FLx,
+                                           B.Fb, B.wdf);
+  if (aw.FLx && cs->flx_viscous)
+    k_nadj_pressure_term<DIM, TURB><<<bf, TB, 0, s>>>(m, cv, state, aw.FLx, B.Fb);
   k_nadj_apcoef<DIM, TURB><<<bf, TB, 0, s>>>(m, cv, state, pd, dw.G, dw.cl, fw.dco, aw.dcob, B.Fb, B.wdf);
   k_nadj_grad_face<DIM, TURB><<<bf, TB, 0, s>>>(m, cv, state, pdd, aw.Gb, B.Fb);
   k_nadj_grad_cell<DIM, TURB><<<bc, TB, 0, s>>>(m, aw.Gb, fw.G, fw.dco, aw.dcob, B.ivb, B.Cb);
@@ -670,4 +695,153 @@ void fv_node_adjoint_free(FvCase* cs) {
   cudaFree(na->wall_cell);
   delete na;
   cs->nadj = nullptr;
+}
+
+// ------------------------------------------------------------------------ face-flux functionals
+// J = sum_f sum_q w_qf FL_q(f), optionally less the pressure part sum_i w_if p_f A_f n_if on
+// boundary faces (the viscous, "wall shear" force): the outlet mass flux (w = 1 on the
+// continuity flux of the outlet faces) and the wall shear force (w = 1 on a momentum component of
+// the wall faces) of the 3D channel's adjoint objectives.  Value, dJ/dstate (the state adjoint
+// with w as an extra face-flux cotangent), the parameter partials (forward tangents of the face
+// fluxes) and dJ/dnodes (the mesh-coordinate adjoint with the same extra cotangent).
+namespace {
+
+constexpr int kFnBlocks = 304;
+
+__global__ void k_face_in(int nf, int nfld, const int* face_old, const double* w_ref,
+                          double* w_int) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nf) return;
+  const int r = face_old[f];
+  for (int q = 0; q < nfld; ++q) w_int[(long)q * nf + f] = w_ref[(long)q * nf + r];
+}
+
+template <class T>
+__device__ __forceinline__ double part_of(const T& x, bool tangent);
+template <>
+__device__ __forceinline__ double part_of<double>(const double& x, bool) { return x; }
+template <>
+__device__ __forceinline__ double part_of<Dual>(const Dual& x, bool tangent) {
+  return tangent ? x.d : x.v;
+}
+
+template <int DIM, bool TURB, class T>
+__global__ void __launch_bounds__(256) k_functional_partial(MeshView m, CaseView cv,
+                                                            const double* state, const double* w,
+                                                            const T* FL, int viscous, int tangent,
+                                                            double* part) {
+  using L = Layout<DIM, TURB>;
+  constexpr int NF = L::NFLD;
+  __shared__ double red[256];
+  const int nf = m.nf;
+  double acc = 0.0;
+  for (long f = (long)blockIdx.x * blockDim.x + threadIdx.x; f < nf; f += (long)gridDim.x * blockDim.x) {
+    double a = 0.0;
+    for (int q = 0; q < NF; ++q) {
+      const double wq = w[(long)q * nf + f];
+      if (wq != 0.0) a += wq * part_of(FL[(long)q * nf + f], tangent != 0);
+    }
+    if (viscous && !tangent && f >= m.nfi) {
+      const int o = m.owner[f];
+      const double pf = bpress(cv, (int)f, cv.fkind[f], state[(long)L::P * m.nc + o]);
+      for (int i = 0; i < DIM; ++i)
+        a -= w[(long)i * nf + f] * pf * m.area[f] * m.normal[(long)i * nf + f];
+    }
+    acc += a;
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int h = 128; h > 0; h >>= 1) {
+    if (threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+__global__ void k_functional_final(int nparts, const double* part, double* out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double acc = 0.0;
+  for (int i = 0; i < nparts; ++i) acc += part[i];
+  *out = acc;
+}
+
+// d(pressure part)/d(owner pressure) on boundary faces whose pressure is the owner's.
+template <int DIM, bool TURB>
+__global__ void k_functional_pressure_state(MeshView m, CaseView cv, const double* w,
+                                            double* dstate) {
+  using L = Layout<DIM, TURB>;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nc) return;
+  const int nf = m.nf;
+  double acc = 0.0;
+  for (int i = m.cf_ptr[c]; i < m.cf_ptr[c + 1]; ++i) {
+    const int f = (int)(m.cf_face[i] & ~FV_NB_BIT);
+    const signed char kind = cv.fkind[f];
+    if (f < m.nfi || kind < 0 || kind > 2) continue;
+    for (int j = 0; j < DIM; ++j) acc += w[(long)j * nf + f] * m.area[f] * m.normal[(long)j * nf + f];
+  }
+  dstate[(long)L::P * m.nc + c] -= acc;
+}
+
+template <int DIM, bool TURB>
+int face_functional(FvCase* cs, const double* state, const double* wref, int viscous,
+                    double* value, double* dstate, double* dparams, double* dnodes,
+                    cudaStream_t s) {
+  using L = Layout<DIM, TURB>;
+  constexpr int NF = L::NFLD;
+  const MeshView& m = cs->mesh->view;
+  const CaseView& cv = cs->view;
+  const long nc = m.nc, nf = m.nf, n = (long)NF * nc;
+  if (!cs->flx) FV_CUDA_TRY(cudaMalloc(&cs->flx, sizeof(double) * ((size_t)NF * nf + n)));
+  if (!cs->red) FV_CUDA_TRY(cudaMalloc(&cs->red, sizeof(double) * kFnBlocks));
+  double* zeros = cs->flx + (long)NF * nf;
+  FV_CUDA_TRY(cudaMemsetAsync(zeros, 0, sizeof(double) * n, s));
+  k_face_in<<<fv_blocks(nf, 256), 256, 0, s>>>((int)nf, NF, cs->mesh->face_old, wref, cs->flx);
+  // value
+  int rc = fv_case_run(cs, state, nullptr, FV_TAN_NONE, cs->tmp, nullptr, s);
+  if (rc != FV_OK) return rc;
+  {
+    Work<double> fw = work_layout<double, DIM, TURB>(cs->work, nc, nf);
+    k_functional_partial<DIM, TURB, double><<<kFnBlocks, 256, 0, s>>>(m, cv, state, cs->flx, fw.FL,
+                                                                      viscous, 0, cs->red);
+    k_functional_final<<<1, 32, 0, s>>>(kFnBlocks, cs->red, value);
+  }
+  // parameter partials at fixed state
+  if (dparams) {
+    const int kinds[2] = {FV_TAN_MU, FV_TAN_INLET};
+    for (int i = 0; i < 2; ++i) {
+      rc = fv_case_run(cs, state, nullptr, kinds[i], nullptr, cs->tmp2, s);
+      if (rc != FV_OK) return rc;
+      Work<Dual> dw = work_layout<Dual, DIM, TURB>(cs->work, nc, nf);
+      k_functional_partial<DIM, TURB, Dual><<<kFnBlocks, 256, 0, s>>>(m, cv, state, cs->flx, dw.FL,
+                                                                      0, 1, cs->red);
+      k_functional_final<<<1, 32, 0, s>>>(kFnBlocks, cs->red, dparams + i);
+    }
+  }
+  // state partial: the adjoint with no residual cotangent and w on the face fluxes
+  cs->flx_active = true;
+  cs->flx_viscous = viscous != 0;
+  rc = run_vjp<DIM, TURB>(cs, state, zeros, nullptr, dstate, s);
+  if (rc == FV_OK && viscous)
+    k_functional_pressure_state<DIM, TURB><<<fv_blocks(nc, 128), 128, 0, s>>>(m, cv, cs->flx, dstate);
+  if (rc == FV_OK && dnodes) rc = fv_case_node_vjp(cs, state, zeros, dnodes, s);
+  cs->flx_active = false;
+  cs->flx_viscous = false;
+  if (rc != FV_OK) return rc;
+  FV_CUDA_TRY(cudaGetLastError());
+  return FV_OK;
+}
+
+}  // namespace
+
+int fv_case_face_functional(FvCase* cs, const double* state, const double* weights_ref,
+                            int viscous_only, double* value, double* dstate, double* dparams,
+                            double* dnodes, cudaStream_t s) {
+  const int dim = cs->mesh->dim;
+  const bool turb = cs->desc.turbulent != 0;
+  if (dim == 2)
+    return turb ? face_functional<2, true>(cs, state, weights_ref, viscous_only, value, dstate, dparams, dnodes, s)
+                : face_functional<2, false>(cs, state, weights_ref, viscous_only, value, dstate, dparams, dnodes, s);
+  return turb ? face_functional<3, true>(cs, state, weights_ref, viscous_only, value, dstate, dparams, dnodes, s)
+              : face_functional<3, false>(cs, state, weights_ref, viscous_only, value, dstate, dparams, dnodes, s);
 }

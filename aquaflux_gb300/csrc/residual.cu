@@ -1024,6 +1024,7 @@ AdjWork adj_layout(FvCase* cs) {
   aw.Gwib = p; p += DIM * nc;
   aw.Gb2 = p; p += L::NFLD * DIM * nc;  // present when the case is swept
   aw.Bb = p;
+  aw.FLx = cs->flx_active ? cs->flx : nullptr;
   return aw;
 }
 

@@ -185,6 +185,35 @@ class FlowCase:
         check(lib().fv_node_vjp(self._h, ptr(s), ptr(ww), ptr(out), _stream()))
         return out
 
+    def functional_weights(self, spec: dict) -> torch.Tensor:
+        """Weights of a face-flux functional: ``spec = {patch: {field: weight}}`` puts ``weight``
+        on the ``field`` flux of every face of ``patch`` (fields: 0..dim-1 momentum, dim
+        continuity, dim+1 / dim+2 k / omega)."""
+        mesh = self.dmesh.mesh
+        nfld = self.n_unknowns // self.n_cells
+        w = np.zeros((nfld, mesh.n_faces))
+        for patch, fields in spec.items():
+            faces = np.asarray(mesh.patches[patch], dtype=np.int64)
+            for q, val in fields.items():
+                w[int(q), faces] = float(val)
+        return torch.tensor(w, device="cuda")
+
+    def face_functional(self, state, weights, *, viscous_only: bool = False, params: bool = True,
+                        nodes: bool = True) -> dict:
+        """``J = sum w . FL`` (less the boundary pressure part with ``viscous_only``): its value,
+        ``dJ/dstate``, ``dJ/d(mu, inlet_scale)`` and ``dJ/dnodes`` at fixed state."""
+        s = self._vec(state)
+        w = torch.as_tensor(weights, dtype=torch.float64, device="cuda").contiguous()
+        mesh = self.dmesh.mesh
+        value = torch.empty(1, dtype=torch.float64, device="cuda")
+        dstate = torch.empty_like(s)
+        dparams = torch.empty(2, dtype=torch.float64, device="cuda") if params else None
+        dnodes = (torch.empty(mesh.n_nodes, mesh.dim, dtype=torch.float64, device="cuda")
+                  if nodes else None)
+        check(lib().fv_face_functional(self._h, ptr(s), ptr(w), int(viscous_only), ptr(value),
+                                       ptr(dstate), ptr(dparams), ptr(dnodes), _stream()))
+        return {"value": float(value), "dstate": dstate, "dparams": dparams, "dnodes": dnodes}
+
     def jvp_batch(self, state, vs) -> torch.Tensor:
         """``J(state) v_i`` for every row of the ``(k, n)`` seed block ``vs``."""
         s = self._vec(state)

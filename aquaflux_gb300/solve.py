@@ -382,3 +382,26 @@ def implicit_adjoint(case, state, g, *, rtol: float = 1e-10, precision: int = 64
                  maxiter=max_krylov)
     dparams = -case.param_vjp(s, res.x)
     return AdjointResult(res.x, dparams, res.iterations, res.converged)
+
+
+@dataclasses.dataclass
+class FunctionalGradient:
+    value: float
+    dparams: torch.Tensor   # total dJ/d(mu, inlet_scale)
+    dnodes: torch.Tensor | None  # total dJ/dnodes, (n_nodes, dim)
+    adjoint: AdjointResult
+
+
+def functional_gradient(case, state, weights, *, viscous_only: bool = False, nodes: bool = True,
+                        rtol: float = 1e-10, preconditioner=None) -> FunctionalGradient:
+    """Total derivative of a face-flux functional ``J(state(theta), theta)`` at a converged state
+    by the implicit function theorem (``_implicit_solve_bwd``, ``aquaflux/solve/implicit.py:
+    733-761``): ``J^T lam = dJ/dstate``, then ``dJ/dtheta = dJ/dtheta|_state - lam^T dR/dtheta``
+    for ``theta`` = (mu, inlet_scale) and every node coordinate."""
+    f = case.face_functional(state, weights, viscous_only=viscous_only, nodes=nodes)
+    adj = implicit_adjoint(case, state, f["dstate"], rtol=rtol, preconditioner=preconditioner)
+    dparams = f["dparams"] + adj.dparams
+    dnodes = None
+    if nodes:
+        dnodes = f["dnodes"] - case.node_vjp(state, adj.lam)
+    return FunctionalGradient(f["value"], dparams, dnodes, adj)

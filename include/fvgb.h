@@ -165,6 +165,19 @@ int fv_param_vjp(FvCase* c, const double* state, const double* w, double* out, v
  * order.  Compact gradient scheme only (FV_ERR_ARG otherwise).  Allocates a workspace with the
  * case on first use. */
 int fv_node_vjp(FvCase* c, const double* state, const double* w, double* dnodes, void* stream);
+/* A face-flux functional J = sum_f sum_q weights[q, f] FL_q(f) of the residual's face fluxes
+ * (weights device (nfld, F) field-major, reference face order; FL_q(f) the flux of field q
+ * through face f, owner-outward: mass flux for the continuity field, momentum / k / omega fluxes
+ * otherwise), with viscous_only != 0 taking the pressure part sum_i w_i p_f A n_i out on boundary
+ * faces (the wall shear force).  The outlet mass flux and the wall shear of the adjoint objectives
+ * are such functionals.  value: device scalar J; dstate (device, n_unknowns): dJ/dstate; dparams
+ * (device (2), may be NULL): the partials dJ/d(mu, inlet_scale) at fixed state; dnodes (device
+ * (n_nodes, dim), may be NULL): dJ/dnodes at fixed state (compact gradient scheme).  The total
+ * derivative at a converged state is dJ/dtheta - lambda^T dR/dtheta with J^T lambda = dJ/dstate
+ * (fv_vjp / fv_param_vjp / fv_node_vjp). */
+int fv_face_functional(FvCase* c, const double* state, const double* weights, int viscous_only,
+                       double* value, double* dstate, double* dparams, double* dnodes,
+                       void* stream);
 
 /* Per-stage CUDA-event timing of the next `max_runs` pipeline runs on this case (diagnostics;
  * no reference counterpart).  profile_end synchronizes, writes the summed milliseconds of each
