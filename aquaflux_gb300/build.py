@@ -61,8 +61,7 @@ def build_library(verbose: bool = False) -> str:
 
 
 def build_oracle() -> None:
-    """Compile the oracle's C restatement (and, where the reference source is present, the
-    reference's own ILU(0) kernel) -- test infrastructure, see ``oracle/build_ref.py``."""
+    """Compile the oracle's C restatement of the ILU(0) kernel -- test infrastructure."""
     script = os.path.join(ROOT, "oracle", "build_oracle.py")
     if os.path.exists(script):
         subprocess.run(["python3", script], check=True, stdout=subprocess.DEVNULL)

@@ -216,7 +216,7 @@ __device__ __forceinline__ void mn_adjoint(const MeshView& m, int f, double wgt,
 //   F_i = pf n_i A - c (u_n - u_o + G_n . tN - G_o . tP) + mdot upwind(u),  c = m_o m_n A / den,
 //   den = dpn m_n - m_o dnn  (m = mu + rho nu_t);  F_p = mdot;
 //   F_s = (mdot / rho) upwind(phi) - c_s (phi_n - phi_o + ...), c_s from the cell diffusivities.
-template <int DIM, bool TURB>
+template <int DIM, bool TURB, bool FLX = false>
 __global__ void __launch_bounds__(128) a_flux(MeshView m, CaseView cv, Src<double> st, Par<double> par,
                                               const double* G, const double* cl, const double* dco,
                                               const double* me, const double* aux, AdjWork aw) {
@@ -260,9 +260,10 @@ __global__ void __launch_bounds__(128) a_flux(MeshView m, CaseView cv, Src<doubl
       for (int j = 0; j < DIM; ++j) tN[j] = m.tN[(long)j * nf + f];
       double FLb[NF];
 #pragma unroll
-      for (int q = 0; q < NF; ++q)
-        FLb[q] = aw.Wt[(long)q * nc + o] - aw.Wt[(long)q * nc + n] +
-                 (aw.FLx ? aw.FLx[(long)q * nf + f] : 0.0);
+      for (int q = 0; q < NF; ++q) {
+        FLb[q] = aw.Wt[(long)q * nc + o] - aw.Wt[(long)q * nc + n];
+        if constexpr (FLX) FLb[q] += aw.FLx[(long)q * nf + f];
+      }
       // forward face intermediates kept by k_flux
       const double mdot = aux[0L * nf + f];
       const double damping = aux[1L * nf + f];
@@ -350,8 +351,10 @@ __global__ void __launch_bounds__(128) a_flux(MeshView m, CaseView cv, Src<doubl
       const signed char kind = cv.fkind[f];
       double FLb[NF];
 #pragma unroll
-      for (int q = 0; q < NF; ++q)
-        FLb[q] = aw.Wt[(long)q * nc + o] + (aw.FLx ? aw.FLx[(long)q * nf + f] : 0.0);
+      for (int q = 0; q < NF; ++q) {
+        FLb[q] = aw.Wt[(long)q * nc + o];
+        if constexpr (FLX) FLb[q] += aw.FLx[(long)q * nf + f];
+      }
       double uo[DIM], bu[DIM];
 #pragma unroll
       for (int j = 0; j < DIM; ++j) {

@@ -1050,7 +1050,10 @@ int run_vjp(FvCase* cs, const double* state, const double* W, double* R, double*
   const int bc = fv_blocks(nc, TB);
   a_sum<DIM, TURB><<<bc, TB, 0, s>>>(m, cv, st, par, W, cl, G, Gwi, aw);
   fv_prof_mark(cs, 7, s);
-  a_flux<DIM, TURB><<<bc, TB, 0, s>>>(m, cv, st, par, G, cl, dco, fw.me, cs->aux, aw);
+  if (aw.FLx)
+    a_flux<DIM, TURB, true><<<bc, TB, 0, s>>>(m, cv, st, par, G, cl, dco, fw.me, cs->aux, aw);
+  else
+    a_flux<DIM, TURB><<<bc, TB, 0, s>>>(m, cv, st, par, G, cl, dco, fw.me, cs->aux, aw);
   fv_prof_mark(cs, 8, s);
   a_apcoef<DIM, TURB><<<bc, TB, 0, s>>>(m, cv, st, par, G, cl, dco, fw.me, cs->aux, aw);
   fv_prof_mark(cs, 9, s);

@@ -51,6 +51,8 @@ def _args():
     ap.add_argument("--newton-kinds", default="amg,ilu",
                     help="preconditioners timed in the Newton block (comma list of amg, "
                          "amg-natural, ilu)")
+    ap.add_argument("--no-adjoint", action="store_true",
+                    help="skip the adjoint objectives' gradients after the Newton solves")
     ap.add_argument("--newton-oracle-check", action="store_true",
                     help="also evaluate the converged fp32-preconditioned state with the CPU oracle")
     return ap.parse_args()
@@ -379,6 +381,18 @@ def newton_block(args, wl, case) -> dict:
             jt["n_probes"] = jac.n_probes
         del jac
     out["jacobian_ms"] = jt
+    # untimed warm-up of every solver path on a small channel (library initialisation, graph
+    # captures), so that the timed solves below measure steady-state work
+    from aquaflux_gb300 import workloads
+
+    warm = workloads.channel3d(16)
+    warm_case = warm.device_case()
+    for kind in args.newton_kinds.split(","):
+        for prec in (64, 32):
+            solve.newton_solve(warm_case, warm.initial_state(), precision=prec,
+                               kind="amg" if kind.startswith("amg") else kind, max_steps=40)
+    del warm_case
+    torch.cuda.synchronize()
     states = {}
     for kind in args.newton_kinds.split(","):
         for prec in (64, 32):
@@ -399,6 +413,8 @@ def newton_block(args, wl, case) -> dict:
                                                                a.abs().max())
         out[f"{kind}_speedup_fp32_vs_fp64"] = round(
             out[f"{kind}_fp64"]["seconds"] / out[f"{kind}_fp32"]["seconds"], 3)
+    if not args.no_adjoint:
+        out["adjoint"] = adjoint_block(case, states[(args.newton_kinds.split(",")[0], 32)])
     if args.newton_oracle_check:
         from oracle import fv_oracle as fo
 
@@ -411,6 +427,43 @@ def newton_block(args, wl, case) -> dict:
         kind = args.newton_kinds.split(",")[0]
         r32 = float(np.linalg.norm(orc.residual(states[(kind, 32)].cpu()).numpy()))
         out["fp32_oracle_rel_residual"] = r32 / r0
+    return out
+
+
+def adjoint_block(case, state) -> dict:
+    """The 3D channel's adjoint objectives at the converged fp32-preconditioned state: the outlet
+    mass flux and the wall shear force, each differentiated with respect to viscosity, inlet
+    velocity and every node coordinate by the implicit function theorem (the transposed fp32
+    V-cycle preconditioning FGMRES on the hand-written VJP, 1e-10)."""
+    import torch
+
+    from aquaflux_gb300 import solve
+    from aquaflux_gb300.amg import AmgPreconditioner
+
+    dim = case.dim
+    out = {}
+    pc = AmgPreconditioner(solve.BlockJacobian(case), 32)
+    for name, spec, visc in (("outlet_mass_flux", {"right": {dim: 1.0}}, False),
+                             ("wall_shear_x", {w: {0: 1.0} for w in
+                                               ("bottom", "top", "back", "front")}, True)):
+        w = case.functional_weights(spec)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        g = solve.functional_gradient(case, state, w, viscous_only=visc, preconditioner=pc)
+        torch.cuda.synchronize()
+        out[name] = {"seconds": round(time.perf_counter() - t0, 3), "value": g.value,
+                     "dJ_dmu": float(g.dparams[0]), "dJ_dinlet_scale": float(g.dparams[1]),
+                     "dJ_dnodes_norm": float(torch.linalg.vector_norm(g.dnodes)),
+                     "krylov_iterations": g.adjoint.krylov_iterations,
+                     "converged": bool(g.adjoint.converged)}
+    # the mesh-coordinate VJP alone
+    lam = torch.randn(case.n_unknowns, dtype=torch.float64, device="cuda")
+    case.node_vjp(state, lam)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    case.node_vjp(state, lam)
+    torch.cuda.synchronize()
+    out["node_vjp_ms"] = round((time.perf_counter() - t0) * 1e3, 2)
     return out
 
 

@@ -1,1 +1,1 @@
-"""CPU oracle package -- test infrastructure only (see ``fv_oracle`` and ``ilu0_ref``)."""
+"""CPU oracle package -- test infrastructure only (``fv_oracle``, ``operator_oracle``, ``ilu0_oracle.c``)."""

@@ -1,9 +1,7 @@
-"""ctypes access to the CPU ILU(0) checkers (C restatement, and the reference's own kernel)."""
+"""ctypes access to the CPU ILU(0) checker (the C restatement of the reference's kernel)."""
 from __future__ import annotations
 
 import ctypes
-import glob
-import importlib.util
 import os
 
 import numpy as np
@@ -19,17 +17,6 @@ def c_oracle():
 
         subprocess.run([sys.executable, os.path.join(ROOT, "oracle", "build_oracle.py")], check=True)
     return ctypes.CDLL(path)
-
-
-def reference_kernel():
-    """The reference's compiled ``_ilu0`` module built into ``oracle/_ref``, or None."""
-    hits = glob.glob(os.path.join(ROOT, "oracle", "_ref", "_ilu0*.so"))
-    if not hits:
-        return None
-    spec = importlib.util.spec_from_file_location("_ilu0", hits[0])
-    mod = importlib.util.module_from_spec(spec)
-    spec.loader.exec_module(mod)
-    return mod
 
 
 def _p(a):
