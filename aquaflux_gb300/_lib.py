@@ -50,6 +50,10 @@ SIGNATURES = {
     "fv_probe_jacobian": (c_int, [P, P, c_int, P, c_int, P, P, P, P]),
     "fv_jvp_batch": (c_int, [P, P, P, c_int, P, P]),
     "fv_node_vjp": (c_int, [P, P, P, P, P]),
+    "fv_case_set_viscosity_field": (c_int, [P, P, P]),
+    "fv_case_set_block_size": (c_int, [P, c_int]),
+    "fv_case_autotune": (c_int, [P, P, P, P, P, P]),
+    "fv_segment_dot": (c_int, [c_int, P, c_int, c_int, P, P, P, P]),
     "fv_face_functional": (c_int, [P, P, P, c_int, P, P, P, P, P]),
     "fv_assemble_jacobian": (c_int, [P, P, P, P, P, P]),
     "fv_param_jvp": (c_int, [P, P, P, P, P]),

@@ -249,7 +249,7 @@ __global__ void __launch_bounds__(128) a_flux(MeshView m, CaseView cv, Src<doubl
       nrm[j] = m.normal[(long)j * nf + f];
       tP[j] = m.tP[(long)j * nf + f];
     }
-    const double mo = TURB ? par.mu + rho * cl[2L * nc + o] : par.mu;
+    const double mo = TURB ? par.mu + rho * cl[2L * nc + o] : (cv.mu_cell ? cv.mu_cell[o] : par.mu);
     const double po = st((long)L::P * nc + o);
     if (f < m.nfi) {
       const int n = m.nb[f];
@@ -389,7 +389,7 @@ __global__ void __launch_bounds__(128) a_flux(MeshView m, CaseView cv, Src<doubl
           gbv = par.mu + rho * nw.v;
           dgb_dk = rho * nw.d;
         } else {
-          gbv = par.mu;
+          gbv = cv.mu_cell ? cv.mu_cell[o] : par.mu;
         }
       }
       const double Ad = A * m.inv_dpn[f];

@@ -159,6 +159,7 @@ extern "C" int fv_case_create(const FvMesh* mesh, const FvCaseDesc* desc,
   v.wdg = c->wdg;
   v.inv_wd = c->inv_wd;
   v.inv_wd2 = c->inv_wd + m->nc;
+  v.mu_cell = nullptr;
   FV_CUDA_TRY(cudaStreamSynchronize(s));
   *out = c;
   return FV_OK;
@@ -188,6 +189,7 @@ extern "C" int fv_case_destroy(FvCase* c) {
   cudaFree(c->wnear);
   fv_node_adjoint_free(c);
   cudaFree(c->flx);
+  cudaFree(c->mu_cell);
   cudaFree(c->red);
   for (cudaEvent_t e : c->prof_events) cudaEventDestroy(e);
   delete c;
@@ -201,6 +203,73 @@ extern "C" int fv_case_set_params(FvCase* c, double mu, double inlet_scale) {
   }
   c->mu = mu;
   c->inlet_scale = inlet_scale;
+  return FV_OK;
+}
+
+extern "C" int fv_case_set_viscosity_field(FvCase* c, const double* mu_cell, void* stream) {
+  if (!c) {
+    fv_set_error("fv_case_set_viscosity_field: null case");
+    return FV_ERR_ARG;
+  }
+  if (!mu_cell) {
+    c->view.mu_cell = nullptr;
+    return FV_OK;
+  }
+  if (c->desc.turbulent) {
+    fv_set_error("fv_case_set_viscosity_field: a per-cell viscosity applies to laminar cases");
+    return FV_ERR_ARG;
+  }
+  if (!c->mu_cell) FV_CUDA_TRY(cudaMalloc(&c->mu_cell, sizeof(double) * c->mesh->nc));
+  FV_CUDA_TRY(cudaMemcpyAsync(c->mu_cell, mu_cell, sizeof(double) * c->mesh->nc,
+                              cudaMemcpyDefault, (cudaStream_t)stream));
+  c->view.mu_cell = c->mu_cell;
+  return FV_OK;
+}
+
+extern "C" int fv_case_autotune(FvCase* c, const double* state, const double* w, double* out,
+                                void* stream, int* best) {
+  if (!c || !state || !w || !out) {
+    fv_set_error("fv_case_autotune: bad arguments");
+    return FV_ERR_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  const int cand[4] = {32, 64, 96, 128};
+  cudaEvent_t e0, e1;
+  FV_CUDA_TRY(cudaEventCreate(&e0));
+  FV_CUDA_TRY(cudaEventCreate(&e1));
+  float best_ms = 1e30f;
+  int best_tb = c->tb;
+  for (int k = 0; k < 4; ++k) {
+    c->tb = cand[k];
+    int rc = fv_case_vjp_run(c, state, w, nullptr, out, s);  // warm-up
+    if (rc != FV_OK) return rc;
+    cudaEventRecord(e0, s);
+    for (int r = 0; r < 3; ++r) {
+      rc = fv_case_vjp_run(c, state, w, nullptr, out, s);
+      if (rc != FV_OK) return rc;
+    }
+    cudaEventRecord(e1, s);
+    FV_CUDA_TRY(cudaEventSynchronize(e1));
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best_ms) {
+      best_ms = ms;
+      best_tb = cand[k];
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  c->tb = best_tb;
+  if (best) *best = best_tb;
+  return FV_OK;
+}
+
+extern "C" int fv_case_set_block_size(FvCase* c, int threads) {
+  if (!c || threads < 32 || threads > 128 || threads % 32 != 0) {
+    fv_set_error("fv_case_set_block_size: threads must be a multiple of 32 in [32, 128]");
+    return FV_ERR_ARG;
+  }
+  c->tb = threads;
   return FV_OK;
 }
 

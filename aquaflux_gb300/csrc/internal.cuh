@@ -86,6 +86,7 @@ struct CaseView {
   const double* wdg;          // (dim, nc) wall-distance gradient
   const double* inv_wd;       // (nc) 1 / wall distance
   const double* inv_wd2;      // (nc) 1 / wall distance^2
+  const double* mu_cell;      // (nc) per-cell molecular viscosity (laminar), or null
 };
 
 // Workspace of the mesh-coordinate adjoint (residual.cu), allocated on its first use.
@@ -126,6 +127,8 @@ struct FvCase {
   double* jac_face = nullptr; // (2, nfld, nfld, nf) face flux derivatives of the Jacobian assembly
   int* wnear = nullptr;       // (nc) nearest SST wall face (internal index), turbulent cases
   NodeAdjoint* nadj = nullptr;  // mesh-coordinate adjoint workspace, allocated on first use
+  int tb = 128;                 // threads per block of the residual / JVP / VJP stages (autotuned)
+  double* mu_cell = nullptr;    // (nc) per-cell viscosity field (laminar batched instances)
   double* flx = nullptr;        // (nfld, nf) weights of a face-flux functional (internal order)
   bool flx_active = false;      // the adjoints add flx to their face-flux cotangents
   bool flx_viscous = false;     // ... with the pressure part p_f A n_i taken out

@@ -573,10 +573,19 @@ __global__ void __launch_bounds__(128) k_closure(MeshView m, CaseView cv, Src<T>
 }
 
 // effective dynamic viscosity mu + rho nu_t (aquaflux/flow/momentum.py:357-368)
+// molecular viscosity of cell c: the case constant, or a per-cell field (laminar batched
+// instances) whose tangent under the viscosity seed is the constant's
+__device__ __forceinline__ double mu_at(const Par<double>& par, const CaseView& cv, int c) {
+  return cv.mu_cell ? cv.mu_cell[c] : par.mu;
+}
+__device__ __forceinline__ Dual mu_at(const Par<Dual>& par, const CaseView& cv, int c) {
+  return cv.mu_cell ? Dual{cv.mu_cell[c], par.mu.d} : par.mu;
+}
 template <class T, bool TURB>
-__device__ __forceinline__ T mu_eff(const Par<T>& par, double rho, const T* cl, int nc, int c) {
+__device__ __forceinline__ T mu_eff(const Par<T>& par, const CaseView& cv, double rho, const T* cl,
+                                    int nc, int c) {
   if (TURB) return par.mu + rho * cl[2L * nc + c];
-  return par.mu;
+  return mu_at(par, cv, c);
 }
 
 // lagged advective momentum flux (rho u)_f . n with the skew-corrected face value
@@ -621,9 +630,9 @@ __device__ __forceinline__ void apcoef_face(const MeshView& m, const CaseView& c
   const double rho = cv.rho;
   const T mdot = mom_normal<T, DIM, TURB>(m, st, G, rho, f, o, n, g, gv) * A;
   me = mdot;
-  const T mo = mu_eff<T, TURB>(par, rho, cl, nc, o);
+  const T mo = mu_eff<T, TURB>(par, cv, rho, cl, nc, o);
   if (interior) {
-    const T mnb = mu_eff<T, TURB>(par, rho, cl, nc, n);
+    const T mnb = mu_eff<T, TURB>(par, cv, rho, cl, nc, n);
     const T visc = conductance(mo, mnb, A, gv.dpn(m, f), gv.dnn(m, f));
     ac_own = visc + pos(mdot);
     ac_nb = visc + pos(-mdot);
@@ -703,7 +712,7 @@ __device__ __forceinline__ void flux_face(const MeshView& m, const CaseView& cv,
     tP[j] = gv.tP(m, j, f);
   }
   const T po = st((long)L::P * nc + o);
-  const T mo = mu_eff<T, TURB>(par, rho, cl, nc, o);
+  const T mo = mu_eff<T, TURB>(par, cv, rho, cl, nc, o);
   if (f < m.nfi) {
     const int n = m.nb[f];
     const GT g = gv.g(m, f);
@@ -723,7 +732,7 @@ __device__ __forceinline__ void flux_face(const MeshView& m, const CaseView& cv,
     const T damping = ((pn - po) - gd) * gv.inv_nd(m, f);
     const T mdot = mest - (rho * A) * dhat * damping;
     const T pf = lerp(po, pn, g) + gs;
-    const T mnb = mu_eff<T, TURB>(par, rho, cl, nc, n);
+    const T mnb = mu_eff<T, TURB>(par, cv, rho, cl, nc, n);
     const T iden = 1.0 / (gv.dpn(m, f) * mnb - mo * gv.dnn(m, f));
     const T cmo = mo * mnb * A * iden;
     const bool out = val(mdot) >= 0.0;
@@ -949,7 +958,7 @@ void gradient_stage(FvCase* cs, Src<T> st, Par<T> par, const Work<T>& w, cudaStr
   const MeshView& m = cs->mesh->view;
   const CaseView& cv = cs->view;
   constexpr int NF = Layout<DIM, TURB>::NFLD;
-  constexpr int TB = 128;
+  const int TB = cs->tb;
   const int bc = fv_blocks(m.nc, TB);
   const int sweeps = cs->desc.gradient_sweeps;
   const double rel = sweeps >= 1 ? cs->desc.gradient_relaxation : 1.0;
@@ -970,7 +979,7 @@ int run(FvCase* cs, Src<T> st, Par<T> par, double* R, double* JV, cudaStream_t s
   const CaseView& cv = cs->view;
   const long nc = m.nc, nf = m.nf;
   Work<T> w = work_layout<T, DIM, TURB>(cs->work, nc, nf);
-  constexpr int TB = 128;
+  const int TB = cs->tb;
   const int bc = fv_blocks(nc, TB), bf = fv_blocks(nf, TB);
   fv_prof_mark(cs, 0, s);
   gradient_stage<T, DIM, TURB>(cs, st, par, w, s);
@@ -1046,7 +1055,7 @@ int run_vjp(FvCase* cs, const double* state, const double* W, double* R, double*
   double* Gwi = fw.Gwi;
   double* dco = fw.dco;
   AdjWork aw = adj_layout<DIM, TURB>(cs);
-  constexpr int TB = 128;
+  const int TB = cs->tb;
   const int bc = fv_blocks(nc, TB);
   a_sum<DIM, TURB><<<bc, TB, 0, s>>>(m, cv, st, par, W, cl, G, Gwi, aw);
   fv_prof_mark(cs, 7, s);

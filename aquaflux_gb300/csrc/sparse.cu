@@ -1054,6 +1054,37 @@ extern "C" int fv_bsr_spmv_f32(int nbr, int b, const int* indptr, const int* ind
   return spmv<float>(nbr, b, indptr, indices, values, x, y, transpose, (cudaStream_t)stream);
 }
 
+// out[i] = sum over fields q and cells c in [seg[i], seg[i + 1]) of a[q nc + c] b[q nc + c]: one
+// block per segment, fixed summation order.
+__global__ void k_segment_dot(const int* seg, int nfld, int nc, const double* a, const double* b,
+                              double* out) {
+  __shared__ double red[256];
+  const int i = blockIdx.x;
+  const int lo = seg[i], hi = seg[i + 1];
+  double acc = 0.0;
+  for (int q = 0; q < nfld; ++q)
+    for (int c = lo + threadIdx.x; c < hi; c += blockDim.x)
+      acc += a[(long)q * nc + c] * b[(long)q * nc + c];
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int h = 128; h > 0; h >>= 1) {
+    if (threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[i] = red[0];
+}
+
+extern "C" int fv_segment_dot(int n_seg, const int* seg, int nfld, int nc, const double* a,
+                              const double* b, double* out, void* stream) {
+  if (n_seg <= 0 || nfld <= 0 || nc <= 0 || !seg || !a || !b || !out) {
+    fv_set_error("fv_segment_dot: bad arguments");
+    return FV_ERR_ARG;
+  }
+  k_segment_dot<<<n_seg, 256, 0, (cudaStream_t)stream>>>(seg, nfld, nc, a, b, out);
+  FV_CUDA_TRY(cudaGetLastError());
+  return FV_OK;
+}
+
 extern "C" int fv_dot_f64(long n, const double* x, const double* y, double* out, void* stream) {
   if (n < 0 || !x || !y || !out) {
     fv_set_error("fv_dot_f64: bad arguments");

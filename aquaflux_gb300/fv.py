@@ -129,10 +129,19 @@ class FlowCase:
         self.dim, self.n_cells = mesh.dim, mesh.n_cells
         self.turbulent = sst is not None
         t = case_tables(mesh, flow_bc, sst)
+        mu_arr = np.asarray(mu, dtype=np.float64)
+        mu_field = None
+        if mu_arr.ndim == 1:  # a per-cell viscosity field (laminar instances side by side)
+            if mu_arr.shape != (mesh.n_cells,):
+                raise ValueError(f"a viscosity field needs {mesh.n_cells} values")
+            mu_field = mu_arr
+            mu_const = float(mu_arr.mean())
+        else:
+            mu_const = float(mu_arr)
         sweeps = 0 if gradient is None else int(gradient["sweeps"])
         relax = 1.0 if gradient is None else float(gradient.get("relaxation", 1.0))
         self.gradient = gradient
-        desc = FvCaseDesc(1 if sst is not None else 0, float(mu), float(rho),
+        desc = FvCaseDesc(1 if sst is not None else 0, mu_const, float(rho),
                           -1 if pressure_pin is None else int(pressure_pin),
                           float(pressure_pin_value), sweeps, relax)
         h = ctypes.c_void_p()
@@ -144,7 +153,11 @@ class FlowCase:
         self._h = h
         self._keep = arrs
         self.n_unknowns = int(lib().fv_case_n_unknowns(h))
-        self.mu, self.rho, self.inlet_scale = float(mu), float(rho), 1.0
+        self.mu, self.rho, self.inlet_scale = float(mu_const), float(rho), 1.0
+        self.mu_field = None
+        if mu_field is not None:
+            self.mu_field = torch.as_tensor(mu_field, dtype=torch.float64, device="cuda")
+            check(lib().fv_case_set_viscosity_field(h, ptr(self.mu_field), _stream()))
 
     @property
     def handle(self):
@@ -184,6 +197,18 @@ class FlowCase:
         out = torch.empty(mesh.n_nodes, mesh.dim, dtype=torch.float64, device="cuda")
         check(lib().fv_node_vjp(self._h, ptr(s), ptr(ww), ptr(out), _stream()))
         return out
+
+    def autotune(self, state, w) -> int:
+        """Pick the stage kernels' block size by timing the residual + VJP step (``fv_case_autotune``)."""
+        s, ww = self._vec(state), self._vec(w)
+        out = torch.empty_like(s)
+        best = ctypes.c_int(0)
+        check(lib().fv_case_autotune(self._h, ptr(s), ptr(ww), ptr(out), _stream(),
+                                     ctypes.byref(best)))
+        return int(best.value)
+
+    def set_block_size(self, threads: int) -> None:
+        check(lib().fv_case_set_block_size(self._h, int(threads)))
 
     def functional_weights(self, spec: dict) -> torch.Tensor:
         """Weights of a face-flux functional: ``spec = {patch: {field: weight}}`` puts ``weight``

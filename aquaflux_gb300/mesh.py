@@ -370,3 +370,35 @@ largest to smallest spacing being the given ``ratio_*``.  Every node
     mesh.patches["inlet"] = mesh.patches.pop("left")
     mesh.patches["outlet"] = mesh.patches.pop("right")
     return mesh
+
+
+def disjoint_union(meshes) -> tuple[MeshData, np.ndarray]:
+    """One mesh holding independent meshes side by side: cells, faces and nodes of mesh ``i`` follow
+    those of mesh ``i - 1``; patch ``name`` of mesh ``i`` becomes ``"i:name"``.  Returns the mesh and
+    the cell offsets (``len(meshes) + 1``) delimiting each instance."""
+    nodes, fo, fi, own, nb, patches = [], [], [], [], [], {}
+    cell0 = node0 = face0 = inc0 = 0
+    offsets = [0]
+    for i, m in enumerate(meshes):
+        nodes.append(m.nodes)
+        fo.append(np.asarray(m.fn_offsets[1:], dtype=np.int64) + inc0)
+        fi.append(np.asarray(m.fn_indices, dtype=np.int64) + node0)
+        own.append(np.asarray(m.owner, dtype=np.int64) + cell0)
+        nb.append(np.where(m.neighbour >= 0, np.asarray(m.neighbour, dtype=np.int64) + cell0, -1))
+        for name, faces in m.patches.items():
+            patches[f"{i}:{name}"] = (np.asarray(faces, dtype=np.int64) + face0).astype(np.int32)
+        cell0 += m.n_cells
+        node0 += m.n_nodes
+        face0 += m.n_faces
+        inc0 += int(m.fn_offsets[-1])
+        offsets.append(cell0)
+    union = MeshData(
+        nodes=np.ascontiguousarray(np.concatenate(nodes), dtype=np.float64),
+        fn_offsets=np.concatenate([np.zeros(1, dtype=np.int64)] + fo).astype(np.int32),
+        fn_indices=np.concatenate(fi).astype(np.int32),
+        owner=np.concatenate(own).astype(np.int32),
+        neighbour=np.concatenate(nb).astype(np.int32),
+        n_cells=int(cell0),
+        patches=patches,
+    ).validate()
+    return union, np.asarray(offsets, dtype=np.int32)

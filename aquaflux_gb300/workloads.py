@@ -16,6 +16,10 @@ perturbations and a case description, built the same way on every machine.
   the walls, interior nodes jittered +-0.15 of the local spacing), coupled (u, v, p) + k-omega SST
   at Re_h = 5e4 (nu = 2e-5, inlet u = 1, intensity 5 %), corrected Green-Gauss gradients by four
   swept sweeps.
+* :func:`batched_channels` -- the batched calibration sweep: 64 independent 2D laminar channels
+  (2 x 1, inlet / outlet / two walls) of uneven size n x n, n log-uniform in [32, 256], viscosity
+  log-uniform in [1e-3, 1e-1], inlet velocity uniform in [0.5, 2], held side by side in one
+  disjoint-union mesh (one launch per stage for all instances) with a per-cell viscosity field.
 """
 from __future__ import annotations
 
@@ -137,3 +141,56 @@ def backward_step(*, n_step: int = 48, n_channel: int = 96, n_upstream: int = 12
     sst = {"walls": walls, "k": kb, "omega": wb}
     return Workload(f"backward_step_{m.n_cells}_sst", m, nu, 1.0, flow_bc, None, sst, k_in, w_in,
                     gradient={"sweeps": sweeps, "relaxation": 1.0} if sweeps else None)
+
+
+@dataclasses.dataclass
+class BatchedWorkload:
+    workload: Workload      # the disjoint union (laminar, per-cell viscosity)
+    offsets: np.ndarray     # (n_instances + 1) cell offsets of the instances
+    mu: np.ndarray          # per instance
+    velocity: np.ndarray    # per-instance inlet velocity
+    sizes: np.ndarray       # cells per axis of each instance
+
+    @property
+    def n_instances(self) -> int:
+        return int(self.mu.size)
+
+    def initial_state(self) -> np.ndarray:
+        """Plug flow at each instance's inlet velocity, zero pressure."""
+        m = self.workload.mesh
+        n = m.n_cells
+        u = np.zeros((m.dim + 1, n))
+        u[0] = np.repeat(self.velocity, np.diff(self.offsets))
+        return u.reshape(-1)
+
+    def outlet_weights(self, areas: np.ndarray) -> np.ndarray:
+        """``g`` with ``g . state`` restricted to instance i equal to its mean outlet velocity
+        ``sum_f A_f u_P(f) / sum_f A_f`` over the outlet faces (the outlet boundary value is the
+        owner's velocity)."""
+        m = self.workload.mesh
+        g = np.zeros((m.dim + 1) * m.n_cells)
+        for i in range(self.n_instances):
+            faces = np.asarray(m.patches[f"{i}:right"], dtype=np.int64)
+            a = areas[faces]
+            np.add.at(g, m.owner[faces], a / a.sum())
+        return g
+
+
+def batched_channels(n_instances: int = 64, *, n_min: int = 32, n_max: int = 256,
+                     seed: int = 0) -> BatchedWorkload:
+    rng = np.random.default_rng(seed)
+    sizes = np.rint(np.exp(rng.uniform(np.log(n_min), np.log(n_max), n_instances))).astype(int)
+    mu = np.exp(rng.uniform(np.log(1e-3), np.log(1e-1), n_instances))
+    vel = rng.uniform(0.5, 2.0, n_instances)
+    meshes = [fm.structured_grid_2d(int(n), int(n), 2.0, 1.0) for n in sizes]
+    union, offsets = fm.disjoint_union(meshes)
+    flow_bc = {}
+    for i in range(n_instances):
+        flow_bc[f"{i}:left"] = ("inlet", (float(vel[i]), 0.0))
+        flow_bc[f"{i}:right"] = ("outlet", 0.0)
+        flow_bc[f"{i}:bottom"] = ("wall",)
+        flow_bc[f"{i}:top"] = ("wall",)
+    mu_cell = np.repeat(mu, np.diff(offsets))
+    wl = Workload(f"batched_channels_{n_instances}_{union.n_cells}", union, mu_cell, 1.0,
+                  flow_bc, None, None)
+    return BatchedWorkload(wl, offsets, mu, vel, sizes)

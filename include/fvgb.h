@@ -102,6 +102,18 @@ int fv_case_destroy(FvCase* c);
 /* Change the differentiable physical parameters: molecular viscosity and a factor applied to
  * every prescribed inlet velocity.  Takes effect for later calls on `stream`. */
 int fv_case_set_params(FvCase* c, double mu, double inlet_scale);
+/* Per-cell molecular viscosity (host or device, n_cells; NULL restores the constant): the
+ * viscosity of independent instances held in one disjoint-union mesh (the batched calibration
+ * sweep).  Laminar cases only.  The viscosity tangent (fv_param_jvp / fv_param_vjp) seeds every
+ * cell's viscosity with 1; its dot product with an adjoint restricted to one instance's unknowns
+ * (fv_segment_dot) is that instance's derivative. */
+int fv_case_set_viscosity_field(FvCase* c, const double* mu_cell, void* stream);
+/* Threads per block of the residual / JVP / VJP stage kernels (a multiple of 32 in [32, 128];
+ * results do not depend on it).  fv_case_autotune times the residual + VJP step at state / w for
+ * 32, 64, 96 and 128 and keeps the fastest (best receives it; out: n_unknowns scratch). */
+int fv_case_set_block_size(FvCase* c, int threads);
+int fv_case_autotune(FvCase* c, const double* state, const double* w, double* out, void* stream,
+                     int* best);
 /* Device copies (C) and (C, dim) of the SST wall distance and its gradient (turbulent cases). */
 int fv_case_wall_distance(const FvCase* c, double* distance, double* gradient, void* stream);
 /* Number of unknowns: (dim + 1) * C, or (dim + 3) * C when turbulent. */
@@ -322,6 +334,12 @@ int fv_prolong_add_f64(int n_fine, int b, const int* agg, const double* xc, doub
  * bit-identical).  Device arrays; `out` is a device scalar.
  * ------------------------------------------------------------------------------------------ */
 int fv_dot_f64(long n, const double* x, const double* y, double* out, void* stream);
+/* Per-segment dot products over field-major vectors: out[i] = sum over fields q and cells
+ * c in [seg[i], seg[i + 1]) of a[q nc + c] b[q nc + c] (device; fixed order).  The per-instance
+ * reductions of the batched calibration sweep (independent instances as cell ranges of one
+ * disjoint-union mesh). */
+int fv_segment_dot(int n_seg, const int* seg, int nfld, int nc, const double* a, const double* b,
+                   double* out, void* stream);
 
 #ifdef __cplusplus
 }
