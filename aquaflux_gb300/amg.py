@@ -208,13 +208,15 @@ class AmgPreconditioner:
     """``M ~= J^-1``: one aggregation V-cycle with ILU(0) smoothing of the materialised block
     Jacobian, fp32 (default) or fp64 throughout (field-major fp64 vectors in and out).
 
-    ``fine_order="colour"`` numbers the fine cells colour by colour (a distance-1 colouring of the
-    cell graph; two colours on a hexahedral mesh), so that the fine ILU(0) sweeps run in a few
-    level sets of many rows each instead of hundreds of short ones; ``"natural"`` keeps the
-    operator's own cell order.
+    ``fine_order="natural"`` (default) keeps the operator's own cell order for the fine ILU(0)
+    smoother; ``"colour"`` numbers the fine cells colour by colour (a distance-1 colouring of the
+    cell graph; two colours on a hexahedral mesh), so that the fine sweeps run in a few wide level
+    sets -- cheaper per cycle, but a red-black ILU(0) is a weaker smoother: on the 3D SST channel
+    the two orders give the same Newton time, on 2D laminar saddle-point systems the coloured
+    smoother stalls.  Coarse levels are always colour-numbered.
     """
 
-    def __init__(self, jac, precision: int = 32, *, fine_order: str = "colour", shift=None,
+    def __init__(self, jac, precision: int = 32, *, fine_order: str = "natural", shift=None,
                  equilibrate: bool = False, **kw):
         from .solve import ShiftedCellMajorOperator
 

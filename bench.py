@@ -50,7 +50,7 @@ def _args():
     ap.add_argument("--no-newton", action="store_true", help="skip the Newton-solve timing")
     ap.add_argument("--newton-kinds", default="amg,ilu",
                     help="preconditioners timed in the Newton block (comma list of amg, "
-                         "amg-natural, ilu)")
+                         "amg-colour, ilu)")
     ap.add_argument("--workload", default="channel3d", choices=["channel3d", "batched"],
                     help="channel3d: the 128^3 SST channel (the headline); batched: the 64-instance "
                          "calibration sweep (its own JSON line)")
@@ -400,7 +400,7 @@ def newton_block(args, wl, case) -> dict:
     for kind in args.newton_kinds.split(","):
         for prec in (64, 32):
             torch.cuda.synchronize()
-            opts = {"fine_order": "natural"} if kind == "amg-natural" else None
+            opts = {"fine_order": "colour"} if kind == "amg-colour" else None
             res = solve.newton_solve(case, wl.initial_state(), precision=prec,
                                      kind="amg" if kind.startswith("amg") else kind,
                                      precond_options=opts, max_steps=40)

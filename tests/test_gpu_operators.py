@@ -74,7 +74,7 @@ def _cavity_pc(kind, precision, **kw):
 
 @pytest.mark.parametrize("kind,opts", [
     ("ilu", {}), ("ilu", {"equilibrate": True}), ("amg", {}),
-    ("amg", {"fine_order": "natural"}), ("amg", {"equilibrate": True})])
+    ("amg", {"fine_order": "colour"}), ("amg", {"equilibrate": True})])
 def test_preconditioner_transpose_is_exact(kind, opts):
     """<M x, y> = <x, M^T y> for the fp64 ILU(0) solve and the fp64 V-cycle (the adjoint
     preconditioner of aquaflux/solve/implicit.py:709-730)."""
