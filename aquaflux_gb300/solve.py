@@ -441,3 +441,100 @@ def batched_gradients(case, state, bw, *, rtol: float = 1e-10,
     dmu = -seg_dot(adj.lam, dmu_vec)
     dvel = -seg_dot(adj.lam, dsc_vec) / torch.tensor(bw.velocity, device="cuda")
     return BatchedGradients(value, dmu, dvel, adj)
+
+
+@dataclasses.dataclass
+class ContinuationResult:
+    state: torch.Tensor
+    converged: bool
+    steps: int
+    residual_norms: list
+    betas: list
+    escalations: int
+    krylov_iterations: list
+    seconds: float
+
+
+def shift_basis(jac: BlockJacobian, velocity_only: bool = False) -> torch.Tensor:
+    """The base pseudo-time shift ``d`` (field-major): the magnitude of the frozen Jacobian's
+    diagonal on the momentum rows (the momentum diagonal ``a_P``, ``LocalCourantBasis`` with weight
+    1, ``aquaflux/solve/shift_basis.py:62-91``) and, unless ``velocity_only``, on the k / omega rows;
+    zero on the continuity rows (``MomentumShiftPolicy``, ``aquaflux/flow/continuation.py:111-186``).
+    Uses the values the Jacobian last materialised."""
+    n, b = jac.n, jac.b
+    if not hasattr(jac, "_diag_blocks"):
+        rows = np.repeat(np.arange(n), np.diff(jac.indptr))
+        jac._diag_blocks = torch.tensor(np.flatnonzero(rows == jac.indices), device="cuda")
+    blocks = jac.values.view(-1, b, b)[jac._diag_blocks]  # (n, b, b)
+    d = torch.diagonal(blocks, dim1=1, dim2=2).abs().t().contiguous()  # (b, n)
+    dim = b - 1 if b in (3, 4) else b - 3
+    d[dim] = 0.0  # continuity
+    if velocity_only:
+        d[dim + 1:] = 0.0
+    return d.reshape(-1)
+
+
+def pseudo_transient_solve(case, state0, *, beta0: float = 2.0, exponent: float = 1.0,
+                           beta_floor: float = 0.0, max_escalations: int = 6,
+                           escalation_factor: float = 2.0, divergence_cap: float = 10.0,
+                           rtol: float = 1e-10, atol: float = 1e-12, max_steps: int = 200,
+                           linear_rtol: float = 1e-3, restart: int = 30, max_krylov: int = 300,
+                           kind: str = "amg", precision: int = 32,
+                           velocity_only: bool = False) -> ContinuationResult:
+    """Pseudo-transient continuation (``PseudoTransientStep``, ``aquaflux/solve/continuation.py:
+    333-735``): each step solves ``(J + beta d) delta = -R`` (the true JVP plus the shift,
+    ``fv_jvp_shift``; right-preconditioned FGMRES with the preconditioner built at the same shifted
+    diagonal), with the switched-evolution-relaxation schedule ``beta = max(beta_floor,
+    beta0 (||R|| / ||R0||)^exponent)`` (``relaxation.py:53-95``) and the divergence guard: a
+    candidate is accepted unless it is non-finite or ``||R|| > divergence_cap ||R0||``; otherwise
+    ``beta`` grows by ``escalation_factor`` and the step is re-solved (re-factoring the
+    preconditioner at the new shift without re-materialising the Jacobian), up to
+    ``max_escalations`` times.  ``beta -> 0`` at the root recovers Newton's step."""
+    from .amg import AmgPreconditioner
+
+    t_all = time.perf_counter()
+    s = torch.as_tensor(state0, dtype=torch.float64, device="cuda").clone()
+    jac = BlockJacobian(case)
+    zero = torch.zeros(case.n_unknowns, dtype=torch.float64, device="cuda")
+    if kind == "amg":
+        pc = AmgPreconditioner(jac, precision, shift=zero)
+    else:
+        pc = IluPreconditioner(jac, precision, shift=zero)
+    r = case.residual(s)
+    norms = [float(torch.linalg.vector_norm(r))]
+    r0 = norms[0]
+    target = atol + rtol * r0
+    betas, its = [], []
+    escalations = 0
+    step = 0
+    converged = norms[0] <= target
+    while not converged and step < max_steps:
+        beta = max(beta_floor, beta0 * (norms[-1] / r0) ** exponent)
+        pc.shift = zero
+        pc.refresh(s)  # materialise J at s (its diagonal also gives the shift basis)
+        d = shift_basis(jac, velocity_only)
+        accepted = False
+        for attempt in range(max_escalations + 1):
+            shift = beta * d
+            pc.reshift(shift)
+            res = fgmres(lambda v: case.jvp_shift(s, v, shift), -r, pc.apply, rtol=linear_rtol,
+                         restart=restart, maxiter=max_krylov)
+            cand = s + res.x
+            rc = case.residual(cand)
+            nc = float(torch.linalg.vector_norm(rc))
+            its.append(res.iterations)
+            if math.isfinite(nc) and nc <= divergence_cap * r0:
+                accepted = True
+                break
+            beta *= escalation_factor
+            escalations += 1
+        if not accepted:
+            break
+        s, r = cand, rc
+        norms.append(nc)
+        betas.append(beta)
+        step += 1
+        converged = nc <= target
+    torch.cuda.synchronize()
+    return ContinuationResult(s, converged, step, norms, betas, escalations, its,
+                              time.perf_counter() - t_all)
