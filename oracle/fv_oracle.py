@@ -264,9 +264,70 @@ def upwind_flux(m: Metrics, phi, mass_flux, bvals):
     return mass_flux * torch.where(topo.interior, interior_value, boundary_value)
 
 
+def venkatakrishnan(m: Metrics, phi, grad, k):
+    """``VenkatakrishnanLimiter.limit`` (``aquaflux/schemes/limiter.py:78-117``): per-cell
+    ``psi = clip(min over faces of psi_face, 0, 1)`` with the stencil extrema over the interior
+    neighbours and ``eps^2 = V K^3``."""
+    topo = m.topo
+    o, nb, inter = topo.owner, topo.safe_nb, topo.interior
+    geo = m.geo
+    nc = topo.n_cells
+    io, inb = o[inter], nb[inter]
+    idx = torch.cat([io, inb])
+    src = torch.cat([phi[inb], phi[io]])
+    pmax = phi.scatter_reduce(0, idx, src, reduce="amax", include_self=True)
+    pmin = phi.scatter_reduce(0, idx, src, reduce="amin", include_self=True)
+    eps2 = geo["volume"] * k ** 3
+    xf, xc = geo["face_centroid"], geo["cell_centroid"]
+
+    def face_limiter(cell):
+        dm = _dot(grad[cell], xf - xc[cell])
+        sign = torch.where(dm >= 0.0, torch.ones_like(dm), -torch.ones_like(dm))
+        dm = sign * (torch.abs(dm) + 1e-12)
+        head = torch.where(dm > 0.0, pmax[cell] - phi[cell], pmin[cell] - phi[cell])
+        e2 = eps2[cell]
+        num = (head ** 2 + e2) * dm + 2.0 * dm ** 2 * head
+        den = (head ** 2 + 2.0 * dm ** 2 + head * dm + e2) * dm
+        return num / den
+
+    lo, ln = face_limiter(o), face_limiter(nb)
+    big = torch.full((nc,), float("inf"), dtype=T)
+    psi = big.scatter_reduce(0, torch.cat([o, inb]), torch.cat([lo, ln[inter]]), reduce="amin",
+                             include_self=True)
+    return torch.clamp(psi, 0.0, 1.0)
+
+
+def advected_face_value(m: Metrics, phi, grad, mass_flux, bvals, scheme):
+    """The advected face value: ``FirstOrderUpwind`` (``scheme`` None) or ``LimitedUpwind``
+    (``aquaflux/discretization/advection.py:117-157``: ``phi_C + psi_C grad phi_C . (x_f - x_C)``
+    from the upwind cell, ``psi`` Venkatakrishnan with ``K = scheme["k"]`` or 1 when ``k`` is
+    None); boundary inflow takes the weak boundary value."""
+    topo = m.topo
+    out = mass_flux >= 0.0
+    if scheme is None:
+        interior_value = torch.where(out, phi[topo.owner], phi[topo.safe_nb])
+        boundary_value = torch.where(out, phi[topo.owner], bvals)
+        return torch.where(topo.interior, interior_value, boundary_value)
+    psi = (torch.ones_like(phi) if scheme.get("k") is None
+           else venkatakrishnan(m, phi, grad, scheme["k"]))
+    o, nb = topo.owner, topo.safe_nb
+    xc, xf = m.geo["cell_centroid"], m.geo["face_centroid"]
+    phi_up = torch.where(out, phi[o], phi[nb])
+    psi_up = torch.where(out, psi[o], psi[nb])
+    grad_up = torch.where(out[:, None], grad[o], grad[nb])
+    x_up = torch.where(out[:, None], xc[o], xc[nb])
+    rec = phi_up + psi_up * _dot(grad_up, xf - x_up)
+    return torch.where(topo.interior | out, rec, bvals)
+
+
+def advection_flux(m: Metrics, phi, grad, mass_flux, bvals, scheme):
+    """``AdvectionFlux.face_flux``: ``mdot_f phi_f``."""
+    return mass_flux * advected_face_value(m, phi, grad, mass_flux, bvals, scheme)
+
+
 # ----------------------------------------------------------------------------- the case
 def make_case(mesh, *, mu, rho, flow_bc, pressure_pin=None, pressure_pin_value=0.0, sst=None,
-              gradient=None):
+              gradient=None, advection=None):
     """Flatten a case description into per-face tables.
 
     ``mesh``: object with ``nodes, fn_offsets, fn_indices, owner, neighbour, n_cells, patches``.
@@ -275,6 +336,8 @@ def make_case(mesh, *, mu, rho, flow_bc, pressure_pin=None, pressure_pin_value=0
     ("zerograd",)}, "omega": {...}}``.
     ``gradient``: ``None`` (compact Green-Gauss) or ``{"sweeps": s, "relaxation": r}`` (corrected
     Green-Gauss by ``s`` swept sweeps).
+    ``advection``: ``None`` (first-order upwind) or ``{"k": K}`` (limited linear upwind with the
+    Venkatakrishnan limiter, ``K`` None for the unlimited reconstruction).
     """
     nf = len(mesh.owner)
     dim = mesh.nodes.shape[1]
@@ -291,7 +354,7 @@ def make_case(mesh, *, mu, rho, flow_bc, pressure_pin=None, pressure_pin_value=0
             pb[faces] = float(spec[1])
     case = {"mesh": mesh, "dim": dim, "mu": float(mu), "rho": float(rho), "bc_kind": kind,
             "bc_vel": vel, "bc_p": pb, "pin": pressure_pin, "pin_value": float(pressure_pin_value),
-            "sst": None, "gradient": gradient}
+            "sst": None, "gradient": gradient, "advection": advection}
     if sst is not None:
         sc = {"nu": float(sst["nu"])}
         for fld in ("k", "omega"):
@@ -648,7 +711,8 @@ class Oracle:
         for i in range(dim):
             diff = diffusion_flux(m, u[:, i], grad_u[:, i], visc, bvel[:, i], boundary_visc)
             press = p_face * normal[:, i] * area
-            adv = upwind_flux(m, u[:, i], mdot, bvel[:, i])
+            adv = advection_flux(m, u[:, i], grad_u[:, i], mdot, bvel[:, i],
+                                 case.get("advection"))
             flux = ((torch.zeros_like(area) + diff) + press) + adv
             cols.append(topo.scatter_conservative(flux) - 0.0 * vol)
         r_cont = topo.scatter_conservative(mdot)
@@ -670,7 +734,8 @@ class Oracle:
         face_gamma = gam_k[o]
         wfw = wall_function_weight(nu[ow], dist[ow], k[ow])
         face_gamma = face_gamma.index_copy(0, wf, (1.0 - wfw) * face_gamma[wf])
-        kflux = (torch.zeros_like(area) + upwind_flux(m, k, vflux, kb)) + \
+        kflux = (torch.zeros_like(area) + advection_flux(m, k, grad_k, vflux, kb,
+                                                         case.get("advection"))) + \
             diffusion_flux(m, k, grad_k, gam_k, kb, face_gamma)
         r_k = topo.scatter_conservative(kflux)
         prod = nut * strain ** 2
@@ -688,7 +753,8 @@ class Oracle:
         # omega equation, transport.py:655-718
         gam_w = nu + blend(f1, SIGMA_W1, SIGMA_W2) * nut
         wb = self._scalar_bvals(w, grad_w_rec, sst["omega_kind"], sst["omega_val"], geo)
-        wflux = (torch.zeros_like(area) + upwind_flux(m, w, vflux, wb)) + \
+        wflux = (torch.zeros_like(area) + advection_flux(m, w, grad_w_rec, vflux, wb,
+                                                         case.get("advection"))) + \
             diffusion_flux(m, w, grad_w_rec, gam_w, wb)
         r_w = topo.scatter_conservative(wflux)
         alpha = blend(f1, ALPHA_1, ALPHA_2)

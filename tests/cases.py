@@ -49,6 +49,10 @@ LAMINAR = {
     "lam3": dict(prefix="lam3_", mu=0.02, bc=DUCT3_BC, pin=None),
     "ccavj": dict(prefix="ccavj_", mu=0.01, bc=CAVITY_BC, pin=0, file="corrected",
                   gradient={"sweeps": 4, "relaxation": 1.0}),
+    "lcavj": dict(prefix="lcavj_", mu=0.01, bc=CAVITY_BC, pin=0, file="limited",
+                  advection={"k": 5.0}),
+    "ucavj": dict(prefix="ucavj_", mu=0.01, bc=CAVITY_BC, pin=0, file="limited",
+                  advection={"k": None}),
 }
 SST = {
     "sst2": dict(prefix="sst2_", dim=2, nu=2e-5, walls=["bottom", "top"]),
@@ -57,6 +61,8 @@ SST = {
                   gradient={"sweeps": 4, "relaxation": 1.0}),
     "csst3": dict(prefix="csst3_", dim=3, nu=1e-3, walls=["bottom", "top", "back", "front"],
                   file="corrected", gradient={"sweeps": 3, "relaxation": 0.8}),
+    "lsst2": dict(prefix="lsst2_", dim=2, nu=2e-5, walls=["bottom", "top"], file="limited",
+                  advection={"k": 5.0}),
 }
 
 
@@ -69,7 +75,8 @@ def oracle_case(name: str):
         d = golden(spec.get("file", "laminar"))
         mesh = mesh_from(d, spec["prefix"])
         case = fo.make_case(mesh, mu=spec["mu"], rho=1.0, flow_bc=spec["bc"],
-                            pressure_pin=spec["pin"], gradient=spec.get("gradient"))
+                            pressure_pin=spec["pin"], gradient=spec.get("gradient"),
+                            advection=spec.get("advection"))
         return case, d, spec["prefix"]
     spec = SST[name]
     d = golden(spec.get("file", "sst"))
@@ -77,7 +84,7 @@ def oracle_case(name: str):
     k_in, w_in = d[spec["prefix"] + "inlet"]
     fb, sst = sst_spec(spec["dim"], spec["nu"], float(k_in), float(w_in), spec["walls"])
     case = fo.make_case(mesh, mu=spec["nu"], rho=1.0, flow_bc=fb, sst=sst,
-                        gradient=spec.get("gradient"))
+                        gradient=spec.get("gradient"), advection=spec.get("advection"))
     return case, d, spec["prefix"]
 
 
@@ -102,13 +109,13 @@ def device_case(name: str):
     if name in LAMINAR:
         spec = LAMINAR[name]
         fc = fv.FlowCase(dm, mu=spec["mu"], rho=1.0, flow_bc=spec["bc"], pressure_pin=spec["pin"],
-                         gradient=spec.get("gradient"))
+                         gradient=spec.get("gradient"), advection=spec.get("advection"))
     else:
         spec = SST[name]
         k_in, w_in = d[p + "inlet"]
         fb, sst = sst_spec(spec["dim"], spec["nu"], float(k_in), float(w_in), spec["walls"])
         fc = fv.FlowCase(dm, mu=spec["nu"], rho=1.0, flow_bc=fb, sst=sst,
-                         gradient=spec.get("gradient"))
+                         gradient=spec.get("gradient"), advection=spec.get("advection"))
     return fc, case, d, p
 
 

@@ -40,7 +40,8 @@ sys.path.insert(0, os.path.join(REF, "tests"))
 
 import jax.numpy as jnp  # noqa: E402  (the shim)
 from aquaflux.boundary import BoundaryConditions, Dirichlet, ZeroGradient  # noqa: E402
-from aquaflux.discretization import FirstOrderUpwind  # noqa: E402
+from aquaflux.discretization import FirstOrderUpwind, LimitedUpwind  # noqa: E402
+from aquaflux.schemes.limiter import VenkatakrishnanLimiter  # noqa: E402
 from aquaflux.flow import (  # noqa: E402
     MomentumContinuity,
     MovingWall,
@@ -112,7 +113,7 @@ def mesh_cases():
 
 
 # --------------------------------------------------------------------------- laminar flow
-def _cavity(n, perturb=0.0, seed=0, mu=0.01, scheme=None):
+def _cavity(n, perturb=0.0, seed=0, mu=0.01, scheme=None, advection=None):
     mesh = structured_grid_2d(n, n, lx=1.0, ly=1.0, named_boundaries=True)
     if perturb:
         mesh = _with_nodes(mesh, jitter_interior_nodes(np.asarray(mesh.node_coords), (n, n),
@@ -123,7 +124,7 @@ def _cavity(n, perturb=0.0, seed=0, mu=0.01, scheme=None):
         scheme or CompactGreenGauss(),
         BoundaryConditions({"top": MovingWall(velocity=(1.0, 0.0)), "bottom": NoSlipWall(),
                             "left": NoSlipWall(), "right": NoSlipWall()}),
-        advection_scheme=FirstOrderUpwind(), pressure_pin=0)
+        advection_scheme=advection or FirstOrderUpwind(), pressure_pin=0)
     return mesh, geom, asm
 
 
@@ -201,8 +202,9 @@ def laminar_cases():
 
 # --------------------------------------------------------------------------- k-omega SST
 def _rans(mesh, geom, dim, nu, u_in, walls, inlet="left", outlet="right", intensity=0.05,
-          length_scale=0.07, scheme=None):
+          length_scale=0.07, scheme=None, advection=None):
     scheme = scheme or CompactGreenGauss()
+    advection = advection or FirstOrderUpwind()
     rho = 1.0
     model = SSTModel()
     k_in = float(inlet_k(jnp.array(u_in), intensity))
@@ -216,9 +218,9 @@ def _rans(mesh, geom, dim, nu, u_in, walls, inlet="left", outlet="right", intens
     w_bc.update({w: ZeroGradient() for w in walls})
     momentum = MomentumContinuity.build(
         mesh, geom, PropertyModel({"viscosity": Constant(rho * nu), "density": Constant(rho)}),
-        scheme, BoundaryConditions(flow_bc), advection_scheme=FirstOrderUpwind())
+        scheme, BoundaryConditions(flow_bc), advection_scheme=advection)
     turb = SSTTurbulence.build(
-        model, mesh, geom, scheme, FirstOrderUpwind(), density=rho,
+        model, mesh, geom, scheme, advection, density=rho,
         molecular_viscosity=jnp.full(mesh.n_cells, nu), wall_patches=list(walls),
         k_boundary=BoundaryConditions(k_bc), omega_boundary=BoundaryConditions(w_bc))
     return CoupledRANS.build(momentum, turb), turb, k_in, omega_in
@@ -368,6 +370,46 @@ def corrected_cases():
     return out
 
 
+# --------------------------------------------------------------------------- limited advection
+def limited_cases():
+    """``LimitedUpwind`` (``aquaflux/discretization/advection.py:117-157``) with the
+    ``VenkatakrishnanLimiter`` (``aquaflux/schemes/limiter.py:78-117``, K = 5) and unlimited."""
+    out = {}
+    rng = np.random.default_rng(47)
+    for prefix, adv in (("lcavj_", LimitedUpwind(limiter=VenkatakrishnanLimiter(k=5.0))),
+                        ("ucavj_", LimitedUpwind(limiter=None))):
+        mesh, geom, asm = _cavity(10, perturb=0.15, seed=0, advection=adv)
+        out.update(_mesh_arrays(prefix, mesh, geom))
+        states = [rng.standard_normal(300) * 0.3, rng.standard_normal(300)]
+        out[prefix + "states"] = np.stack(states)
+        out[prefix + "residuals"] = np.stack([np.asarray(asm.residual(jnp.asarray(x)))
+                                              for x in states])
+        v = rng.standard_normal(300)
+        out[prefix + "jvp_dir"] = v
+        out[prefix + "jvp_fd"] = _fd_jvp(asm.residual, states[0], v, 1e-6)
+    nx, ny = 12, 8
+    yn = graded_nodes(ny, 1.0, 1.2)
+    mesh = structured_grid_2d(nx, ny, lx=4.0, ly=1.0, named_boundaries=True, y_nodes=yn)
+    mesh = _with_nodes(mesh, jitter_interior_nodes(np.asarray(mesh.node_coords), (nx, ny),
+                                                   (4.0, 1.0), 0.1, 4))
+    geom = mesh.geometry()
+    coupled, turb, k_in, omega_in = _rans(mesh, geom, 2, 2e-5, 1.0, ["bottom", "top"],
+                                          advection=LimitedUpwind(
+                                              limiter=VenkatakrishnanLimiter(k=5.0)))
+    out.update(_mesh_arrays("lsst2_", mesh, geom))
+    out["lsst2_inlet"] = np.array([k_in, omega_in])
+    n = mesh.n_cells
+    states = _rans_states(rng, n, 2, k_in, omega_in, 2)
+    out["lsst2_states"] = np.stack(states)
+    out["lsst2_residuals"] = np.stack([np.asarray(coupled.residual(jnp.asarray(x)))
+                                       for x in states])
+    v = rng.standard_normal(5 * n)
+    scale = np.abs(states[0]) + 1e-3
+    out["lsst2_jvp_dir"] = v * scale
+    out["lsst2_jvp_fd"] = _fd_jvp(coupled.residual, states[0], v * scale, 1e-7)
+    return out
+
+
 # --------------------------------------------------------------------------- shifted operators
 def operator_cases():
     """``ShiftedCellMajorOperator.assemble`` (``aquaflux/solve/amg_preconditioner.py:545-658``),
@@ -477,7 +519,7 @@ def colouring_cases():
 FILES = {"colouring": lambda: colouring_cases(), "meshes": lambda: mesh_cases(),
          "laminar": lambda: laminar_cases(), "sst": lambda: sst_cases(),
          "ilu0": lambda: ilu_cases(), "corrected": lambda: corrected_cases(),
-         "operator": lambda: operator_cases()}
+         "operator": lambda: operator_cases(), "limited": lambda: limited_cases()}
 
 
 def main():

@@ -110,7 +110,7 @@ def test_run_to_run_bitwise_identical(name):
     assert np.array_equal(fc.jvp(s, v).cpu().numpy(), fc.jvp(s, v).cpu().numpy())
 
 
-@pytest.mark.parametrize("name", list(SST))
+@pytest.mark.parametrize("name", [n for n in SST if n != "lsst2"])
 def test_wall_distance_matches_reference(name):
     fc, case, d, p = device_case(name)
     wd, wdg = fc.wall_distance()

@@ -34,7 +34,8 @@ def test_residual_matches_reference(name):
         assert np.abs(r - ref).max() <= 1e-13 * np.abs(ref).max()
 
 
-@pytest.mark.parametrize("name", ["cav8", "cavj", "lam3", "sst2", "sst3", "ccavj", "csst2"])
+@pytest.mark.parametrize("name", ["cav8", "cavj", "lam3", "sst2", "sst3", "ccavj", "csst2", "lcavj",
+                                  "ucavj", "lsst2"])
 def test_jvp_matches_reference_finite_differences(name):
     case, d, p = oracle_case(name)
     orc = fo.Oracle(case)
@@ -47,6 +48,8 @@ def test_jvp_matches_reference_finite_differences(name):
 def test_sst_wall_distance_matches_reference():
     for name in SST:
         case, d, p = oracle_case(name)
+        if p + "wall_distance" not in d:
+            continue
         orc = fo.Oracle(case)
         np.testing.assert_allclose(orc.wall_d.numpy(), d[p + "wall_distance"], rtol=1e-14)
         np.testing.assert_allclose(orc.wall_dgrad.numpy(), d[p + "wall_distance_gradient"],
