@@ -23,7 +23,8 @@ FV_ERR_NONFINITE, FV_ERR_NOT_CONVERGED, FV_ERR_TIMEOUT = 5, 6, 7
 class FvCaseDesc(ctypes.Structure):
     _fields_ = [("turbulent", c_int), ("mu", c_double), ("rho", c_double),
                 ("pressure_pin", c_int), ("pressure_pin_value", c_double),
-                ("gradient_sweeps", c_int), ("gradient_relaxation", c_double)]
+                ("gradient_sweeps", c_int), ("gradient_relaxation", c_double),
+                ("advection", c_int), ("limiter_k", c_double)]
 
 
 # name -> (restype, argtypes); this table is the binding a ctypes user of the C ABI adds.

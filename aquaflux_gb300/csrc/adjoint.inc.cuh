@@ -43,7 +43,22 @@ struct AdjWork {
   double* Gb2;   // (NF, D, nc) second iterate cotangent of the corrected-gradient sweeps
   double* Bb;    // (NF, D, nc) cotangent of the corrected scheme's right-hand side B phi
   const double* FLx;  // (NF, nf) extra face-flux cotangent (a face-flux functional), or null
+  const double* psi;  // (NA, nc) forward slope limiters (limited upwind), or null
+  double* psib;       // (NA, nc) their cotangents
+  double* lnb;        // (2, NA, nf) limiter cotangent to the other cell of each face
 };
+
+// Gradient of advected field q at cell cu dotted with (x_f - x_cu): the limited reconstruction's
+// increment (the forward pass's upwind_rec without psi).
+template <int DIM>
+__device__ __forceinline__ double rec_dot(const MeshView& m, const double* G, int q, int f, int cu) {
+  const int nc = m.nc, nf = m.nf;
+  double d = G[((long)q * DIM) * nc + cu] * (m.xf[f] - m.xc[cu]);
+#pragma unroll
+  for (int j = 1; j < DIM; ++j)
+    d = d + G[((long)q * DIM + j) * nc + cu] * (m.xf[(long)j * nf + f] - m.xc[(long)j * nc + cu]);
+  return d;
+}
 
 // ---------------------------------------------------------------- a_sum
 template <int DIM, bool TURB>
@@ -216,7 +231,7 @@ __device__ __forceinline__ void mn_adjoint(const MeshView& m, int f, double wgt,
 //   F_i = pf n_i A - c (u_n - u_o + G_n . tN - G_o . tP) + mdot upwind(u),  c = m_o m_n A / den,
 //   den = dpn m_n - m_o dnn  (m = mu + rho nu_t);  F_p = mdot;
 //   F_s = (mdot / rho) upwind(phi) - c_s (phi_n - phi_o + ...), c_s from the cell diffusivities.
-template <int DIM, bool TURB, bool FLX = false>
+template <int DIM, bool TURB, bool FLX = false, bool LIM = false>
 __global__ void __launch_bounds__(128) a_flux(MeshView m, CaseView cv, Src<double> st, Par<double> par,
                                               const double* G, const double* cl, const double* dco,
                                               const double* me, const double* aux, AdjWork aw) {
@@ -236,6 +251,21 @@ __global__ void __launch_bounds__(128) a_flux(MeshView m, CaseView cv, Src<doubl
     for (int j = 0; j < DIM; ++j) Gb[q][j] = 0.0;
   }
   double dcb = 0.0, F1b = 0.0, ntb = 0.0;
+  constexpr int NA = DIM + (TURB ? 2 : 0);
+  double psb[NA];
+#pragma unroll
+  for (int a = 0; a < NA; ++a) psb[a] = 0.0;
+  // this cell's share of a limited reconstruction it is the upwind cell of: t = the cotangent of
+  // the reconstructed face value
+  auto rec_adj = [&](int a, int q, int f, double t) {
+    const double ps = aw.psi[(long)a * nc + c];
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) {
+      const double dx = m.xf[(long)j * nf + f] - m.xc[(long)j * nc + c];
+      Gb[q][j] += t * ps * dx;
+    }
+    psb[a] += t * rec_dot<DIM>(m, G, q, f, c);
+  };
   const int b = m.cf_ptr[c], e = m.cf_ptr[c + 1];
   for (int it = b; it < e; ++it) {
     const unsigned ent = m.cf_face[it];
@@ -279,7 +309,13 @@ __global__ void __launch_bounds__(128) a_flux(MeshView m, CaseView cv, Src<doubl
         const double uo = st((long)i * nc + o), un = st((long)i * nc + n);
         const double cpn = aux[(long)(AX::CPN + i) * nf + f];
         const double fb = FLb[i];
-        mdotb += fb * (out ? uo : un);
+        double up = out ? uo : un;
+        if constexpr (LIM) {
+          const int cu = out ? o : n;
+          up += aw.psi[(long)i * nc + cu] * rec_dot<DIM>(m, G, i, f, cu);
+          if (out != isnb) rec_adj(i, i, f, fb * mdot);
+        }
+        mdotb += fb * up;
         const double k1 = fb * cmo;  // F_i = ... - c cpn
         cb -= fb * cpn;
         if (!isnb) {
@@ -312,7 +348,13 @@ __global__ void __launch_bounds__(128) a_flux(MeshView m, CaseView cv, Src<doubl
           const double cpn = aux[(b0 + 3) * nf + f];
           const double phio = st((long)q * nc + o), phin = st((long)q * nc + n);
           const double fb = FLb[q];
-          mdotb += fb * (vout ? phio : phin) * irho;
+          double up = vout ? phio : phin;
+          if constexpr (LIM) {
+            const int cu = vout ? o : n;
+            up += aw.psi[(long)(DIM + s) * nc + cu] * rec_dot<DIM>(m, G, q, f, cu);
+            if (vout != isnb) rec_adj(DIM + s, q, f, fb * vflux);
+          }
+          mdotb += fb * up * irho;
           const double k1 = fb * cs_;
           if (!isnb) {
             sb[q] += k1 + (vout ? fb * vflux : 0.0);
@@ -402,7 +444,14 @@ __global__ void __launch_bounds__(128) a_flux(MeshView m, CaseView cv, Src<doubl
         for (int j = 0; j < DIM; ++j) cp += G[((long)i * DIM + j) * nc + o] * tP[j];
         const double num = bu[i] - uo[i] - cp;
         const double fb = FLb[i];
-        mdotb += fb * (out ? uo[i] : bu[i]);
+        double up = out ? uo[i] : bu[i];
+        if constexpr (LIM) {
+          if (out) {
+            up += aw.psi[(long)i * nc + o] * rec_dot<DIM>(m, G, i, f, o);
+            rec_adj(i, i, f, fb * mdot);
+          }
+        }
+        mdotb += fb * up;
         const double numb = -fb * gbv * Ad;
         gbb -= fb * num * Ad;
         const double bub = numb + (!out ? fb * mdot : 0.0);
@@ -441,7 +490,14 @@ __global__ void __launch_bounds__(128) a_flux(MeshView m, CaseView cv, Src<doubl
           }
           const double num = bphi - phio - cp;
           const double fb = FLb[q];
-          mdotb += fb * (vout ? phio : bphi) * irho;
+          double up = vout ? phio : bphi;
+          if constexpr (LIM) {
+            if (vout) {
+              up += aw.psi[(long)(DIM + s) * nc + o] * rec_dot<DIM>(m, G, q, f, o);
+              rec_adj(DIM + s, q, f, fb * vflux);
+            }
+          }
+          mdotb += fb * up * irho;
           const double numb = -fb * gface * Ad;
           const double gfb = -fb * num * Ad;
           const double bphib = numb + (!vout ? fb * vflux : 0.0);
@@ -484,6 +540,75 @@ __global__ void __launch_bounds__(128) a_flux(MeshView m, CaseView cv, Src<doubl
     aw.clb[(long)nc + c] += F1b;
     aw.clb[2L * nc + c] += ntb;
   }
+  if constexpr (LIM) {
+#pragma unroll
+    for (int a = 0; a < NA; ++a) aw.psib[(long)a * nc + c] = psb[a];
+  }
+}
+
+// ---------------------------------------------------------------- a_limiter
+// Adjoint of the Venkatakrishnan limiters: psi of cell c depends on its own value and gradient and
+// on its face neighbours' values (the stencil extrema); d psi / d(input) by dual numbers seeded on
+// one input at a time (the forward formula, limiter_cell).  Own contributions go to the state and
+// gradient cotangents; a neighbour's to lnb (per face and side), gathered by a_limiter_gather.
+template <int DIM, bool TURB>
+__global__ void __launch_bounds__(128) a_limiter(MeshView m, Src<double> st, const double* G,
+                                                 double K, AdjWork aw) {
+  constexpr int NA = DIM + (TURB ? 2 : 0);
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nc) return;
+  const int nc = m.nc, nf = m.nf;
+  const int b = m.cf_ptr[c], e = m.cf_ptr[c + 1];
+#pragma unroll 1
+  for (int a = 0; a < NA; ++a) {
+    const int q = advected_field<DIM, TURB>(a);
+    const double pb = aw.psib[(long)a * nc + c];
+    // seeds: -1 = phi_c, 0..DIM-1 = grad_j, then the cell's faces (their other cell's phi)
+    auto eval = [&](int seed_grad, int seed_cell) {
+      auto phi = [&](int cell) {
+        return Dual{st((long)q * nc + cell), cell == seed_cell ? 1.0 : 0.0};
+      };
+      auto grad = [&](int j) {
+        return Dual{G[((long)q * DIM + j) * nc + c], j == seed_grad ? 1.0 : 0.0};
+      };
+      return limiter_cell<Dual, DIM>(m, c, K, phi, grad).d;
+    };
+    aw.sb[(long)q * nc + c] += pb * eval(-1, c);
+#pragma unroll 1
+    for (int j = 0; j < DIM; ++j) aw.Gb[((long)q * DIM + j) * nc + c] += pb * eval(j, -1);
+    for (int i = b; i < e; ++i) {
+      const unsigned ent = m.cf_face[i];
+      const int f = (int)(ent & ~FV_NB_BIT);
+      if (f >= m.nfi) continue;
+      const bool isnb = (ent & FV_NB_BIT) != 0;
+      const int other = isnb ? m.owner[f] : m.nb[f];
+      // slot 0: the owner's limiter to the neighbour's value; slot 1: the neighbour's to the owner's
+      aw.lnb[((long)(isnb ? NA : 0) + a) * nf + f] = pb * eval(-1, other);
+    }
+  }
+}
+
+template <int DIM, bool TURB>
+__global__ void a_limiter_gather(MeshView m, AdjWork aw) {
+  constexpr int NA = DIM + (TURB ? 2 : 0);
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nc) return;
+  const int nc = m.nc, nf = m.nf;
+  double acc[NA];
+#pragma unroll
+  for (int a = 0; a < NA; ++a) acc[a] = 0.0;
+  for (int i = m.cf_ptr[c]; i < m.cf_ptr[c + 1]; ++i) {
+    const unsigned ent = m.cf_face[i];
+    const int f = (int)(ent & ~FV_NB_BIT);
+    if (f >= m.nfi) continue;
+    // this cell is the neighbour: the owner's limiter wrote slot 0; the owner: slot 1
+    const long slot = (ent & FV_NB_BIT) ? 0 : NA;
+#pragma unroll
+    for (int a = 0; a < NA; ++a) acc[a] += aw.lnb[(slot + a) * nf + f];
+  }
+#pragma unroll
+  for (int a = 0; a < NA; ++a)
+    aw.sb[(long)advected_field<DIM, TURB>(a) * nc + c] += acc[a];
 }
 
 // ---------------------------------------------------------------- a_apcoef

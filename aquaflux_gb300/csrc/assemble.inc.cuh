@@ -34,7 +34,7 @@ struct DerivStore {
 template <int DIM, bool TURB>
 __global__ void __launch_bounds__(128) k_jac_face(MeshView m, CaseView cv, const double* state,
                                                   Par<Dual> par, const Dual* G, const Dual* cl,
-                                                  const Dual* dco, double* D) {
+                                                  const Dual* dco, const Dual* psi, double* D) {
   constexpr int NF = Layout<DIM, TURB>::NFLD;
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= m.nf) return;
@@ -46,8 +46,8 @@ __global__ void __launch_bounds__(128) k_jac_face(MeshView m, CaseView cv, const
     for (int r = 0; r < NF; ++r) {
       const SeedSrc st{state, (long)r * nc + cell};
       const DerivStore wr{D, ((long)(side * NF) * NF + r) * nf + f, (long)NF * nf};
-      flux_face<Dual, DIM, TURB>(m, cv, st, par, G, cl, dco, (const Dual*)nullptr, true, f, wr,
-                                 nullptr);
+      flux_face<Dual, DIM, TURB>(m, cv, st, par, G, cl, dco, (const Dual*)nullptr, psi, true, f,
+                                 wr, nullptr);
     }
   }
 }
@@ -137,7 +137,7 @@ int assemble_frozen(FvCase* cs, const double* state, const int* indptr, const in
   const CaseView& cv = cs->view;
   const long nc = m.nc, nf = m.nf;
   constexpr int NF = Layout<DIM, TURB>::NFLD;
-  Work<Dual> w = work_layout<Dual, DIM, TURB>(cs->work, nc, nf);
+  Work<Dual> w = work_layout<Dual, DIM, TURB>(cs->work, nc, nf, psi_count<DIM, TURB>(cs));
   Src<Dual> st{state, nullptr};  // zero tangent: the forward stages give the frozen values
   const double irho = 1.0 / cs->desc.rho;
   Par<Dual> par{{cs->mu, 0.0}, {cs->inlet_scale, 0.0}, {cs->mu * irho, 0.0}};
@@ -147,7 +147,12 @@ int assemble_frozen(FvCase* cs, const double* state, const int* indptr, const in
   if (TURB) k_closure<Dual, DIM><<<bc, TB, 0, s>>>(m, cv, st, par, w.G, w.cl, w.Gwi);
   k_apcoef<Dual, DIM, TURB><<<bf, TB, 0, s>>>(m, cv, st, par, w.G, w.cl, w.acown, w.acnb, w.me);
   k_dcoeff<Dual><<<bc, TB, 0, s>>>(m, w.acown, w.acnb, w.dco);
-  k_jac_face<DIM, TURB><<<bf, TB, 0, s>>>(m, cv, state, par, w.G, w.cl, w.dco, D);
+  const long npsi = psi_count<DIM, TURB>(cs);
+  if (npsi)
+    k_limiter<Dual, DIM, TURB><<<bc, TB, 0, s>>>(m, st, w.G, cs->desc.advection == 2 ?
+                                                 cs->desc.limiter_k : 0.0, w.psi);
+  k_jac_face<DIM, TURB><<<bf, TB, 0, s>>>(m, cv, state, par, w.G, w.cl, w.dco,
+                                          npsi ? w.psi : nullptr, D);
   k_jac_cell<DIM, TURB><<<fv_blocks((long)NF * nc, TB), TB, 0, s>>>(
       m, cv, state, par, w.G, w.cl, w.Gwi, D, indptr, indices, values);
   FV_CUDA_TRY(cudaGetLastError());

@@ -4,8 +4,8 @@
 
 #include "internal.cuh"
 
-size_t fv_residual_work_bytes(int dim, int turb, long nc, long nf, int sweeps);
-size_t fv_adjoint_work_bytes(int dim, int turb, long nc, int sweeps);
+size_t fv_residual_work_bytes(int dim, int turb, long nc, long nf, int sweeps, int advection);
+size_t fv_adjoint_work_bytes(int dim, int turb, long nc, long nf, int sweeps, int advection);
 size_t fv_aux_bytes(int dim, int turb, long nf);
 extern "C" int fv_dot_f64(long n, const double* x, const double* y, double* out, void* stream);
 int fv_residual_init_constants();
@@ -71,6 +71,12 @@ extern "C" int fv_case_create(const FvMesh* mesh, const FvCaseDesc* desc,
     fv_set_error("fv_case_create: gradient sweeps must be >= 0 and the relaxation in (0, 1]");
     return FV_ERR_ARG;
   }
+  if (desc->advection < 0 || desc->advection > 2 ||
+      (desc->advection == 2 && !(desc->limiter_k > 0.0))) {
+    fv_set_error("fv_case_create: advection must be 0 (upwind), 1 (linear upwind) or 2 "
+                 "(Venkatakrishnan-limited, limiter_k > 0)");
+    return FV_ERR_ARG;
+  }
   if (desc->turbulent && (!k_kind || !omega_kind || !sst_wall)) {
     fv_set_error("fv_case_create: a turbulent case needs k / omega boundary tables and SST walls");
     return FV_ERR_ARG;
@@ -133,12 +139,12 @@ extern "C" int fv_case_create(const FvMesh* mesh, const FvCaseDesc* desc,
     k_inv_distance<<<fv_blocks(m->nc, 256), 256, 0, s>>>(m->nc, c->wd, c->inv_wd);
   }
   c->work_bytes = fv_residual_work_bytes(m->dim, desc->turbulent, m->nc, m->nf,
-                                        desc->gradient_sweeps);
+                                        desc->gradient_sweeps, desc->advection);
   FV_CUDA_TRY(cudaMalloc(&c->work, c->work_bytes));
   FV_CUDA_TRY(cudaMalloc(&c->tmp, sizeof(double) * (size_t)c->nfld * m->nc));
   FV_CUDA_TRY(cudaMalloc(&c->tmp2, sizeof(double) * (size_t)c->nfld * m->nc));
-  FV_CUDA_TRY(cudaMalloc(&c->adj, fv_adjoint_work_bytes(m->dim, desc->turbulent, m->nc,
-                                                        desc->gradient_sweeps)));
+  FV_CUDA_TRY(cudaMalloc(&c->adj, fv_adjoint_work_bytes(m->dim, desc->turbulent, m->nc, m->nf,
+                                                        desc->gradient_sweeps, desc->advection)));
   FV_CUDA_TRY(cudaMalloc(&c->aux, fv_aux_bytes(m->dim, desc->turbulent, m->nf)));
   FV_CUDA_TRY(cudaMalloc(&c->dscalar, sizeof(double) * 4));
   CaseView& v = c->view;

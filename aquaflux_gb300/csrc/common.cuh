@@ -82,6 +82,8 @@ FV_HD Dual fv_min(Dual a, Dual b) {
 FV_HD Dual fv_max(Dual a, double b) { return fv_max(a, Dual{b, 0.0}); }
 FV_HD Dual fv_min(Dual a, double b) { return fv_min(a, Dual{b, 0.0}); }
 
+FV_HD double fv_abs(double x) { return fabs(x); }
+FV_HD Dual fv_abs(Dual x) { return {fabs(x.v), x.v > 0.0 ? x.d : (x.v < 0.0 ? -x.d : 0.0)}; }
 FV_HD double fv_sqrt(double x) { return sqrt(x); }
 FV_HD Dual fv_sqrt(Dual x) {
   double s = sqrt(x.v);

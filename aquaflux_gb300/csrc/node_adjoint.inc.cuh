@@ -52,14 +52,16 @@ __global__ void __launch_bounds__(128) k_nadj_flux(MeshView m, CaseView cv, cons
 #pragma unroll 1
   for (int comp = 0; comp < GF_COUNT; ++comp) {
     double acc = 0.0;
-    flux_face<Dual, DIM, TURB>(m, cv, st, par, G, cl, dco, (const Dual*)nullptr, true, f,
-                               Contract{FLb, &acc}, nullptr, GeoSeed{comp, -1, f, -1});
+    flux_face<Dual, DIM, TURB>(m, cv, st, par, G, cl, dco, (const Dual*)nullptr,
+                               (const Dual*)nullptr, true, f, Contract{FLb, &acc}, nullptr,
+                               GeoSeed{comp, -1, f, -1});
     Fb[(long)comp * nf + f] += acc;
   }
   double acc = 0.0;
   if (TURB && !interior)
-    flux_face<Dual, DIM, TURB>(m, cv, st, par, G, cl, dco, (const Dual*)nullptr, true, f,
-                               Contract{FLb, &acc}, nullptr, GeoSeed{-1, GC_WD, -1, o});
+    flux_face<Dual, DIM, TURB>(m, cv, st, par, G, cl, dco, (const Dual*)nullptr,
+                               (const Dual*)nullptr, true, f, Contract{FLb, &acc}, nullptr,
+                               GeoSeed{-1, GC_WD, -1, o});
   wdf[f] = acc;
 }
 
@@ -619,8 +621,8 @@ int node_vjp(FvCase* cs, const double* state, const double* W, double* dnodes, c
   const long nc = m.nc, nf = m.nf;
   const long ncf = M->h_cf_ptr[nc];
   NodeAdjoint* na = cs->nadj;
-  Work<double> fw = work_layout<double, DIM, TURB>(cs->work, nc, nf);
-  Work<Dual> dw = work_layout<Dual, DIM, TURB>(na->dual_work, nc, nf);
+  Work<double> fw = work_layout<double, DIM, TURB>(cs->work, nc, nf, psi_count<DIM, TURB>(cs));
+  Work<Dual> dw = work_layout<Dual, DIM, TURB>(na->dual_work, nc, nf, psi_count<DIM, TURB>(cs));
   AdjWork aw = adj_layout<DIM, TURB>(cs);
   NadjBuffers B = nadj_layout(na->buf, DIM, nc, nf, ncf, 0);
   constexpr int TB = 128;
@@ -670,9 +672,9 @@ int node_vjp(FvCase* cs, const double* state, const double* W, double* dnodes, c
 
 int fv_case_node_vjp(FvCase* cs, const double* state, const double* w, double* dnodes,
                      cudaStream_t s) {
-  if (cs->desc.gradient_sweeps != 0) {
+  if (cs->desc.gradient_sweeps != 0 || cs->desc.advection != 0) {
     fv_set_error("fv_node_vjp: the mesh-coordinate adjoint supports the compact gradient scheme "
-                 "(gradient_sweeps = 0)");
+                 "and first-order upwind advection (gradient_sweeps = 0, advection = 0)");
     return FV_ERR_ARG;
   }
   int rc = nadj_setup(cs, s);
@@ -801,7 +803,7 @@ int face_functional(FvCase* cs, const double* state, const double* wref, int vis
   int rc = fv_case_run(cs, state, nullptr, FV_TAN_NONE, cs->tmp, nullptr, s);
   if (rc != FV_OK) return rc;
   {
-    Work<double> fw = work_layout<double, DIM, TURB>(cs->work, nc, nf);
+    Work<double> fw = work_layout<double, DIM, TURB>(cs->work, nc, nf, psi_count<DIM, TURB>(cs));
     k_functional_partial<DIM, TURB, double><<<kFnBlocks, 256, 0, s>>>(m, cv, state, cs->flx, fw.FL,
                                                                       viscous, 0, cs->red);
     k_functional_final<<<1, 32, 0, s>>>(kFnBlocks, cs->red, value);
@@ -812,7 +814,7 @@ int face_functional(FvCase* cs, const double* state, const double* wref, int vis
     for (int i = 0; i < 2; ++i) {
       rc = fv_case_run(cs, state, nullptr, kinds[i], nullptr, cs->tmp2, s);
       if (rc != FV_OK) return rc;
-      Work<Dual> dw = work_layout<Dual, DIM, TURB>(cs->work, nc, nf);
+      Work<Dual> dw = work_layout<Dual, DIM, TURB>(cs->work, nc, nf, psi_count<DIM, TURB>(cs));
       k_functional_partial<DIM, TURB, Dual><<<kFnBlocks, 256, 0, s>>>(m, cv, state, cs->flx, dw.FL,
                                                                       0, 1, cs->red);
       k_functional_final<<<1, 32, 0, s>>>(kFnBlocks, cs->red, dparams + i);

@@ -283,13 +283,25 @@ struct Work {
   T* acown;  // (nf) momentum-diagonal coefficient, owner side
   T* acnb;   // (nf) neighbour side
   T* dco;    // (nc) d = V / a_P
+  T* psi;    // (NA, nc) slope limiter of each advected field (limited upwind only)
   T* me;     // (nf) lagged mass-flux estimate (rho u)_f . n A
   T* FL;     // (NF, nf) face fluxes (also the face scratch of the gradient sweeps)
   T* Bg;     // (NF, DIM, nc) corrected Green-Gauss right-hand side B phi (swept cases only)
   T* Galt;   // (NF, DIM, nc) second iterate buffer of the sweeps (swept cases only)
 };
+// Number of advected fields (the momentum components, and k and omega) and the limiter storage a
+// case needs (limited linear upwind only).
+template <int DIM, bool TURB>
+__host__ __device__ constexpr int n_advected() {
+  return DIM + (TURB ? 2 : 0);
+}
+template <int DIM, bool TURB>
+long psi_count(const FvCase* cs) {
+  return cs->desc.advection >= 1 ? (long)n_advected<DIM, TURB>() * cs->mesh->nc : 0;
+}
+
 template <class T, int DIM, bool TURB>
-Work<T> work_layout(void* base, long nc, long nf) {
+Work<T> work_layout(void* base, long nc, long nf, long npsi = 0) {
   constexpr int NF = Layout<DIM, TURB>::NFLD;
   T* p = (T*)base;
   Work<T> w;
@@ -299,6 +311,7 @@ Work<T> work_layout(void* base, long nc, long nf) {
   w.acown = p; p += nf;
   w.acnb = p; p += nf;
   w.dco = p; p += nc;
+  w.psi = p; p += npsi;
   w.me = p; p += nf;
   w.FL = p; p += (long)NF * nf;
   w.Bg = p; p += (long)NF * DIM * nc;
@@ -613,6 +626,87 @@ __device__ __forceinline__ T conductance(T go, T gn, GT A, GT dpn, GT dnn) {
   return go * gn * A / (dpn * gn - go * dnn);
 }
 
+// ---------------------------------------------------------------- slope limiter
+// VenkatakrishnanLimiter.limit (aquaflux/schemes/limiter.py:78-117) of one field at cell c:
+// psi = clip(min over the cell's faces of psi_face, 0, 1), psi_face from the unlimited increment
+// dm = grad . (x_f - x_c) (regularised away from 0) and the headroom to the extrema over the cell
+// and its face neighbours, eps^2 = V K^3.  phi(cell) and grad(j) read the field (either may carry
+// a tangent).
+template <class T, int DIM, class PhiFn, class GradFn>
+__device__ __forceinline__ T limiter_cell(const MeshView& m, int c, double K, const PhiFn& phi,
+                                          const GradFn& grad) {
+  const int nc = m.nc, nf = m.nf;
+  const T pc = phi(c);
+  T pmax = pc, pmin = pc;
+  const int b = m.cf_ptr[c], e = m.cf_ptr[c + 1];
+  for (int i = b; i < e; ++i) {
+    const unsigned ent = m.cf_face[i];
+    const int f = (int)(ent & ~FV_NB_BIT);
+    if (f >= m.nfi) continue;
+    const T po = phi((ent & FV_NB_BIT) ? m.owner[f] : m.nb[f]);
+    pmax = fv_max(pmax, po);
+    pmin = fv_min(pmin, po);
+  }
+  const double e2 = m.vol[c] * (K * K * K);
+  T psi = cst(1.0, pc);
+  for (int i = b; i < e; ++i) {
+    const int f = (int)(m.cf_face[i] & ~FV_NB_BIT);
+    T dm = grad(0) * (m.xf[f] - m.xc[c]);
+#pragma unroll
+    for (int j = 1; j < DIM; ++j) dm = dm + grad(j) * (m.xf[(long)j * nf + f] - m.xc[(long)j * nc + c]);
+    const double sign = val(dm) >= 0.0 ? 1.0 : -1.0;
+    dm = sign * (fv_abs(dm) + 1e-12);
+    const T head = val(dm) > 0.0 ? pmax - pc : pmin - pc;
+    const T num = (head * head + e2) * dm + 2.0 * (dm * dm) * head;
+    const T den = (head * head + 2.0 * (dm * dm) + head * dm + e2) * dm;
+    const T pf = num / den;
+    psi = i == b ? pf : fv_min(psi, pf);
+  }
+  return fv_min(fv_max(psi, cst(0.0, psi)), cst(1.0, psi));
+}
+
+// Field index of advected field a: the momentum components, then k and omega.
+template <int DIM, bool TURB>
+__device__ __forceinline__ int advected_field(int a) {
+  return a < DIM ? a : (a == DIM ? Layout<DIM, TURB>::K : Layout<DIM, TURB>::W);
+}
+
+template <class T, int DIM, bool TURB>
+__global__ void __launch_bounds__(128) k_limiter(MeshView m, Src<T> st, const T* G, double K,
+                                                 T* psi) {
+  constexpr int NA = n_advected<DIM, TURB>();
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nc) return;
+  const int nc = m.nc;
+#pragma unroll 1
+  for (int a = 0; a < NA; ++a) {
+    const int q = advected_field<DIM, TURB>(a);
+    T v;
+    if (K > 0.0) {
+      auto phi = [&](int cell) { return st((long)q * nc + cell); };
+      auto grad = [&](int j) { return G[((long)q * DIM + j) * nc + c]; };
+      v = limiter_cell<T, DIM>(m, c, K, phi, grad);
+    } else {
+      v = cst(1.0, st((long)q * nc + c));
+    }
+    psi[(long)a * nc + c] = v;
+  }
+}
+
+// The advected face value of field q through face f from the upwind cell cu (upwind_value, the
+// cell value; with a limiter, plus psi grad . (x_f - x_cu)).
+template <class T, int DIM>
+__device__ __forceinline__ T upwind_rec(const MeshView& m, const T* G, const T* psi, int a, int q,
+                                        int f, int cu, const T& value) {
+  if (!psi) return value;
+  const int nc = m.nc, nf = m.nf;
+  T d = G[((long)q * DIM) * nc + cu] * (m.xf[f] - m.xc[cu]);
+#pragma unroll
+  for (int j = 1; j < DIM; ++j)
+    d = d + G[((long)q * DIM + j) * nc + cu] * (m.xf[(long)j * nf + f] - m.xc[(long)j * nc + cu]);
+  return value + psi[(long)a * nc + cu] * d;
+}
+
 // ---------------------------------------------------------------- k_apcoef
 // The momentum-diagonal face coefficients of face f (owner side, neighbour side) and the lagged
 // mass-flux estimate me.
@@ -696,8 +790,8 @@ struct Aux {
 template <class T, int DIM, bool TURB, class S, class Wr, class GV = GeoPlain>
 __device__ __forceinline__ void flux_face(const MeshView& m, const CaseView& cv, const S& st,
                                           const Par<T>& par, const T* G, const T* cl, const T* dco,
-                                          const T* me, bool recompute_me, int f, const Wr& wr,
-                                          double* aux, const GV& gv = GV{}) {
+                                          const T* me, const T* psi, bool recompute_me, int f,
+                                          const Wr& wr, double* aux, const GV& gv = GV{}) {
   using GT = decltype(gv.area(m, 0));
   constexpr bool KEEP = std::is_same<T, double>::value && std::is_same<GT, double>::value;
   using L = Layout<DIM, TURB>;
@@ -755,7 +849,9 @@ __device__ __forceinline__ void flux_face(const MeshView& m, const CaseView& cv,
 #pragma unroll
       for (int j = 0; j < DIM; ++j)
         cpn += G[((long)i * DIM + j) * nc + n] * tN[j] - G[((long)i * DIM + j) * nc + o] * tP[j];
-      wr(i, (pA * nrm[i] - cmo * cpn) + mdot * (out ? uo : un));
+      const T up = out ? upwind_rec<T, DIM>(m, G, psi, i, i, f, o, uo)
+                       : upwind_rec<T, DIM>(m, G, psi, i, i, f, n, un);
+      wr(i, (pA * nrm[i] - cmo * cpn) + mdot * up);
       if constexpr (KEEP) {
         if (aux) aux[(long)(AX::CPN + i) * nf + f] = cpn;
       }
@@ -775,7 +871,9 @@ __device__ __forceinline__ void flux_face(const MeshView& m, const CaseView& cv,
           cpn += G[((long)q * DIM + j) * nc + n] * tN[j] - G[((long)q * DIM + j) * nc + o] * tP[j];
         const T idn = 1.0 / (gv.dpn(m, f) * gn - go * gv.dnn(m, f));
         const T cs_ = go * gn * A * idn;
-        wr(q, vflux * (vout ? phio : phin) - cs_ * cpn);
+        const T up = vout ? upwind_rec<T, DIM>(m, G, psi, DIM + s, q, f, o, phio)
+                          : upwind_rec<T, DIM>(m, G, psi, DIM + s, q, f, n, phin);
+        wr(q, vflux * up - cs_ * cpn);
         if constexpr (KEEP) {
           if (aux) {
             const long b0 = AX::S0 + 4 * s;
@@ -830,7 +928,8 @@ __device__ __forceinline__ void flux_face(const MeshView& m, const CaseView& cv,
       T cp = G[((long)i * DIM) * nc + o] * tP[0];
 #pragma unroll
       for (int j = 1; j < DIM; ++j) cp += G[((long)i * DIM + j) * nc + o] * tP[j];
-      wr(i, (pA * nrm[i] - gA * (bu[i] - uo[i] - cp)) + mdot * (out ? uo[i] : bu[i]));
+      const T up = out ? upwind_rec<T, DIM>(m, G, psi, i, i, f, o, uo[i]) : bu[i];
+      wr(i, (pA * nrm[i] - gA * (bu[i] - uo[i] - cp)) + mdot * up);
     }
     wr(L::P, mdot);
     if (TURB) {
@@ -848,7 +947,8 @@ __device__ __forceinline__ void flux_face(const MeshView& m, const CaseView& cv,
                               : bscalar(cv.wkind[f], cv.wval[f], phio, cp);
         T gface = go;
         if (s == 0 && cv.swall[f]) gface = (1.0 - wall_weight(par.nu, gv.wd(cv, o), phio)) * go;
-        wr(q, vflux * (vout ? phio : bphi) - gface * (A * gv.inv_dpn(m, f)) * (bphi - phio - cp));
+        const T up = vout ? upwind_rec<T, DIM>(m, G, psi, DIM + s, q, f, o, phio) : bphi;
+        wr(q, vflux * up - gface * (A * gv.inv_dpn(m, f)) * (bphi - phio - cp));
       }
     }
   }
@@ -864,10 +964,10 @@ struct FluxStore {
 template <class T, int DIM, bool TURB>
 __global__ void __launch_bounds__(128) k_flux(MeshView m, CaseView cv, Src<T> st, Par<T> par,
                                               const T* G, const T* cl, const T* dco, const T* me,
-                                              bool recompute_me, T* FL, double* aux) {
+                                              const T* psi, bool recompute_me, T* FL, double* aux) {
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= m.nf) return;
-  flux_face<T, DIM, TURB>(m, cv, st, par, G, cl, dco, me, recompute_me, f,
+  flux_face<T, DIM, TURB>(m, cv, st, par, G, cl, dco, me, psi, recompute_me, f,
                           FluxStore<T>{FL, m.nf, f}, aux);
 }
 
@@ -978,7 +1078,7 @@ int run(FvCase* cs, Src<T> st, Par<T> par, double* R, double* JV, cudaStream_t s
   const MeshView& m = cs->mesh->view;
   const CaseView& cv = cs->view;
   const long nc = m.nc, nf = m.nf;
-  Work<T> w = work_layout<T, DIM, TURB>(cs->work, nc, nf);
+  Work<T> w = work_layout<T, DIM, TURB>(cs->work, nc, nf, psi_count<DIM, TURB>(cs));
   const int TB = cs->tb;
   const int bc = fv_blocks(nc, TB), bf = fv_blocks(nf, TB);
   fv_prof_mark(cs, 0, s);
@@ -989,10 +1089,15 @@ int run(FvCase* cs, Src<T> st, Par<T> par, double* R, double* JV, cudaStream_t s
   k_apcoef<T, DIM, TURB><<<bf, TB, 0, s>>>(m, cv, st, par, w.G, w.cl, w.acown, w.acnb, w.me);
   fv_prof_mark(cs, 3, s);
   k_dcoeff<T><<<bc, TB, 0, s>>>(m, w.acown, w.acnb, w.dco);
-  if (frozen) freeze<T>(w.G, (long)(w.dco + nc - w.G), s);  // G, closure, Gwi, a_P, d
+  const long npsi = psi_count<DIM, TURB>(cs);
+  if (npsi)
+    k_limiter<T, DIM, TURB><<<bc, TB, 0, s>>>(m, st, w.G, cs->desc.advection == 2 ?
+                                              cs->desc.limiter_k : 0.0, w.psi);
+  // G, closure, Gwi, a_P, d and the slope limiters
+  if (frozen) freeze<T>(w.G, (long)(w.psi + npsi - w.G), s);
   fv_prof_mark(cs, 4, s);
-  k_flux<T, DIM, TURB><<<bf, TB, 0, s>>>(m, cv, st, par, w.G, w.cl, w.dco, w.me, frozen, w.FL,
-                                         aux);
+  k_flux<T, DIM, TURB><<<bf, TB, 0, s>>>(m, cv, st, par, w.G, w.cl, w.dco, w.me,
+                                         npsi ? w.psi : nullptr, frozen, w.FL, aux);
   fv_prof_mark(cs, 5, s);
   k_sum<T, DIM, TURB><<<bc, TB, 0, s>>>(m, cv, st, par, w.FL, w.cl, w.G, w.Gwi, R, JV);
   fv_prof_mark(cs, 6, s);
@@ -1034,6 +1139,11 @@ AdjWork adj_layout(FvCase* cs) {
   aw.Gb2 = p; p += L::NFLD * DIM * nc;  // present when the case is swept
   aw.Bb = p;
   aw.FLx = cs->flx_active ? cs->flx : nullptr;
+  p += L::NFLD * DIM * nc;  // Bb
+  constexpr int NA = n_advected<DIM, TURB>();
+  aw.psi = nullptr;
+  aw.psib = p; p += (long)NA * nc;
+  aw.lnb = p;
   return aw;
 }
 
@@ -1049,7 +1159,7 @@ int run_vjp(FvCase* cs, const double* state, const double* W, double* R, double*
   int rc = run<double, DIM, TURB>(cs, st, par, R ? R : cs->tmp, nullptr, s, false, false, cs->aux);
   if (rc != FV_OK) return rc;
   // forward workspace (double layout, as written by run<double>)
-  Work<double> fw = work_layout<double, DIM, TURB>(cs->work, nc, nf);
+  Work<double> fw = work_layout<double, DIM, TURB>(cs->work, nc, nf, psi_count<DIM, TURB>(cs));
   double* G = fw.G;
   double* cl = fw.cl;
   double* Gwi = fw.Gwi;
@@ -1059,10 +1169,20 @@ int run_vjp(FvCase* cs, const double* state, const double* W, double* R, double*
   const int bc = fv_blocks(nc, TB);
   a_sum<DIM, TURB><<<bc, TB, 0, s>>>(m, cv, st, par, W, cl, G, Gwi, aw);
   fv_prof_mark(cs, 7, s);
-  if (aw.FLx)
+  const bool lim = psi_count<DIM, TURB>(cs) > 0;
+  if (lim) aw.psi = fw.psi;
+  if (aw.FLx && lim)
+    a_flux<DIM, TURB, true, true><<<bc, TB, 0, s>>>(m, cv, st, par, G, cl, dco, fw.me, cs->aux, aw);
+  else if (aw.FLx)
     a_flux<DIM, TURB, true><<<bc, TB, 0, s>>>(m, cv, st, par, G, cl, dco, fw.me, cs->aux, aw);
+  else if (lim)
+    a_flux<DIM, TURB, false, true><<<bc, TB, 0, s>>>(m, cv, st, par, G, cl, dco, fw.me, cs->aux, aw);
   else
     a_flux<DIM, TURB><<<bc, TB, 0, s>>>(m, cv, st, par, G, cl, dco, fw.me, cs->aux, aw);
+  if (lim && cs->desc.advection == 2) {
+    a_limiter<DIM, TURB><<<bc, TB, 0, s>>>(m, st, G, cs->desc.limiter_k, aw);
+    a_limiter_gather<DIM, TURB><<<bc, TB, 0, s>>>(m, aw);
+  }
   fv_prof_mark(cs, 8, s);
   a_apcoef<DIM, TURB><<<bc, TB, 0, s>>>(m, cv, st, par, G, cl, dco, fw.me, cs->aux, aw);
   fv_prof_mark(cs, 9, s);
@@ -1088,10 +1208,12 @@ bool g_const_ready = false;
 
 #include "node_adjoint.inc.cuh"
 
-size_t fv_adjoint_work_bytes(int dim, int turb, long nc, int sweeps) {
+size_t fv_adjoint_work_bytes(int dim, int turb, long nc, long nf, int sweeps, int advection) {
   long nfld = dim + 1 + (turb ? 2 : 0);
   long n = 2 * nfld * nc + nfld * dim * nc + nc + 4 * nc + dim * nc;
-  if (sweeps >= 1) n += 2 * nfld * dim * nc;  // the sweeps' second iterate cotangent and B phi's
+  // the sweeps' second iterate cotangent and B phi's (the limiter buffers follow them)
+  if (sweeps >= 1 || advection >= 1) n += 2 * nfld * dim * nc;
+  if (advection >= 1) n += (long)(dim + (turb ? 2 : 0)) * (nc + 2 * nf);
   return sizeof(double) * (size_t)n;
 }
 
@@ -1108,9 +1230,10 @@ int fv_case_vjp_run(FvCase* cs, const double* state, const double* W, double* R,
   return turb ? run_vjp<3, true>(cs, state, W, R, out, s) : run_vjp<3, false>(cs, state, W, R, out, s);
 }
 
-size_t fv_residual_work_bytes(int dim, int turb, long nc, long nf, int sweeps) {
+size_t fv_residual_work_bytes(int dim, int turb, long nc, long nf, int sweeps, int advection) {
   long nfld = dim + 1 + (turb ? 2 : 0);
   long n = nfld * dim * nc + 7 * nc + dim * nc + 3 * nf + nc + nfld * nf;
+  if (advection >= 1) n += (long)(dim + (turb ? 2 : 0)) * nc;  // slope limiters
   if (sweeps >= 2) n += 2 * nfld * dim * nc;  // B phi and the second sweep iterate
   return (size_t)n * sizeof(Dual);
 }

@@ -115,7 +115,9 @@ def case_tables(mesh: MeshData, flow_bc: dict, sst: dict | None):
 class FlowCase:
     """``MomentumContinuity`` (laminar) or ``CoupledRANS`` (k-omega SST) on the GPU.
 
-    First-order upwind advection; compact Green-Gauss gradients (``gradient=None``) or corrected
+    First-order upwind advection (``advection=None``) or limited linear upwind
+    (``advection={"k": K}``: ``LimitedUpwind(VenkatakrishnanLimiter(k=K))``, ``K`` None for the
+    unlimited reconstruction); compact Green-Gauss gradients (``gradient=None``) or corrected
     Green-Gauss by ``SweptGradientSolve`` (``gradient={"sweeps": s, "relaxation": r}``,
     ``aquaflux/schemes/gradient.py:547-705, 1122-1337``); constant viscosity ``mu`` and density
     ``rho``; optional pressure pin (``FixedValueCells`` on the continuity row).
@@ -123,7 +125,8 @@ class FlowCase:
 
     def __init__(self, dmesh: DeviceMesh, *, mu: float, rho: float, flow_bc: dict,
                  pressure_pin: int | None = None, pressure_pin_value: float = 0.0,
-                 sst: dict | None = None, gradient: dict | None = None):
+                 sst: dict | None = None, gradient: dict | None = None,
+                 advection: dict | None = None):
         self.dmesh = dmesh
         mesh = dmesh.mesh
         self.dim, self.n_cells = mesh.dim, mesh.n_cells
@@ -138,12 +141,17 @@ class FlowCase:
             mu_const = float(mu_arr.mean())
         else:
             mu_const = float(mu_arr)
+        adv_kind, adv_k = 0, 0.0
+        if advection is not None:
+            adv_kind = 1 if advection.get("k") is None else 2
+            adv_k = 0.0 if advection.get("k") is None else float(advection["k"])
+        self.advection = advection
         sweeps = 0 if gradient is None else int(gradient["sweeps"])
         relax = 1.0 if gradient is None else float(gradient.get("relaxation", 1.0))
         self.gradient = gradient
         desc = FvCaseDesc(1 if sst is not None else 0, mu_const, float(rho),
                           -1 if pressure_pin is None else int(pressure_pin),
-                          float(pressure_pin_value), sweeps, relax)
+                          float(pressure_pin_value), sweeps, relax, adv_kind, adv_k)
         h = ctypes.c_void_p()
         arrs = [np.ascontiguousarray(t.get(k)) if t.get(k) is not None else None
                 for k in ("flow_kind", "flow_vel", "flow_p", "k_kind", "k_val", "omega_kind",

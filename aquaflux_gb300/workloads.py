@@ -54,6 +54,7 @@ class Workload:
     k_in: float = 0.0
     omega_in: float = 0.0
     gradient: dict | None = None
+    advection: dict | None = None
 
     @property
     def n_unknowns(self) -> int:
@@ -80,7 +81,8 @@ class Workload:
 
         dm = fv.DeviceMesh(self.mesh)
         return fv.FlowCase(dm, mu=self.mu, rho=self.rho, flow_bc=self.flow_bc,
-                           pressure_pin=self.pressure_pin, sst=self.sst, gradient=self.gradient)
+                           pressure_pin=self.pressure_pin, sst=self.sst, gradient=self.gradient,
+                           advection=self.advection)
 
 
 def cavity(n: int = 64, mu: float = 0.01, lid: float = 1.0) -> Workload:

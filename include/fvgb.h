@@ -91,6 +91,11 @@ typedef struct FvCaseDesc {
    * reconstructed gradient, the wall-distance gradient included. */
   int gradient_sweeps;
   double gradient_relaxation;
+  /* Advection scheme of the momentum (and k, omega) face values: 0 FirstOrderUpwind; 1
+   * LimitedUpwind without a limiter; 2 LimitedUpwind with VenkatakrishnanLimiter(k = limiter_k)
+   * (aquaflux/discretization/advection.py:99-157, aquaflux/schemes/limiter.py:78-117). */
+  int advection;
+  double limiter_k;
 } FvCaseDesc;
 
 int fv_case_create(const FvMesh* mesh, const FvCaseDesc* desc,

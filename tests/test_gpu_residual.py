@@ -61,7 +61,8 @@ def test_jvp_matches_oracle(name):
     assert _rel(r, orc.residual(torch.as_tensor(s)).numpy()) <= 1e-12
 
 
-@pytest.mark.parametrize("name", ["cav8", "lam3", "sst2", "sst3", "ccavj", "csst2"])
+@pytest.mark.parametrize("name", ["cav8", "lam3", "sst2", "sst3", "ccavj", "csst2", "lcavj", "ucavj",
+                                  "lsst2"])
 def test_jvp_matches_reference_finite_differences(name):
     fc, case, d, p = device_case(name)
     s = d[p + "states"][1 if name == "cav8" else 0]
