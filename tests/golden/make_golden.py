@@ -516,10 +516,55 @@ def colouring_cases():
     return out
 
 
+# polyMesh directories read by the reference's importer: its own unit-test fixtures and the
+# validation cases that ship a mesh (paths relative to the reference checkout).
+POLYMESH_DIRS = {
+    "slab2d": "tests/fixtures/polymesh_2d_slab",
+    "slab2d_fb": "tests/fixtures/polymesh_2d_slab_frontandback",
+    "cubes3d": "tests/fixtures/polymesh_3d_two_cubes",
+    "pitzdaily": "validation/pitzdaily_openfoam/of_case",
+    "bfs3d": "validation/bfs3d_species/of_case",
+}
+
+
+def _digest(a, dtype):
+    import hashlib
+    return hashlib.sha256(np.ascontiguousarray(np.asarray(a), dtype=dtype).tobytes()).hexdigest()
+
+
+def openfoam_cases():
+    """``read_openfoam`` (``aquaflux/io/openfoam/reader.py:133``) on the reference's polyMesh
+    directories.  The meshes themselves stay in the reference checkout: only SHA-256 digests of the
+    imported arrays (node coordinates as float64, connectivity as int64, each patch's face indices)
+    and the geometry totals are kept, so the import tests compare against them wherever the
+    reference checkout is present."""
+    from aquaflux.io import read_openfoam
+    out = {}
+    for key, rel in POLYMESH_DIRS.items():
+        m = read_openfoam(os.path.join(REF, rel))
+        fc, fn = m.face_cells, m.face_nodes
+        geom = m.geometry()
+        out[f"{key}_counts"] = np.array([m.dim, m.n_cells, m.n_faces,
+                                         np.asarray(m.node_coords).shape[0]], dtype=np.int64)
+        out[f"{key}_digest"] = np.array([
+            _digest(m.node_coords, np.float64), _digest(fn.offsets, np.int64),
+            _digest(fn.face_node_indices, np.int64), _digest(fc.owner, np.int64),
+            _digest(fc.neighbour, np.int64)])
+        names = [n for n in m.face_patches.names if n not in ("interior", "boundary")]
+        out[f"{key}_patch_names"] = np.array(names)
+        out[f"{key}_patch_digest"] = np.array(
+            [_digest(m.face_patches.indices(n), np.int64) for n in names])
+        vol = np.asarray(geom.cell.volume)
+        out[f"{key}_geometry"] = np.array([vol.sum(), np.abs(np.asarray(geom.face.area)).sum(),
+                                           *(vol[:, None] * np.asarray(geom.cell.centroid)).sum(0)])
+    return out
+
+
 FILES = {"colouring": lambda: colouring_cases(), "meshes": lambda: mesh_cases(),
          "laminar": lambda: laminar_cases(), "sst": lambda: sst_cases(),
          "ilu0": lambda: ilu_cases(), "corrected": lambda: corrected_cases(),
-         "operator": lambda: operator_cases(), "limited": lambda: limited_cases()}
+         "operator": lambda: operator_cases(), "limited": lambda: limited_cases(),
+         "openfoam": lambda: openfoam_cases()}
 
 
 def main():
