@@ -24,7 +24,8 @@ class FvCaseDesc(ctypes.Structure):
     _fields_ = [("turbulent", c_int), ("mu", c_double), ("rho", c_double),
                 ("pressure_pin", c_int), ("pressure_pin_value", c_double),
                 ("gradient_sweeps", c_int), ("gradient_relaxation", c_double),
-                ("advection", c_int), ("limiter_k", c_double)]
+                ("advection", c_int), ("limiter_k", c_double),
+                ("scalar_transform", c_int)]
 
 
 # name -> (restype, argtypes); this table is the binding a ctypes user of the C ABI adds.

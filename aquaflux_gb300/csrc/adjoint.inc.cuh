@@ -96,10 +96,16 @@ __global__ void __launch_bounds__(128) a_sum(MeshView m, CaseView cv, Src<double
     // ---- omega row
     double Ww = wr[L::W];
     if (wall) {
-      // R_w = w - omega_wall(nu, d, k): the flux sum and the sources are overwritten
+      // R_w = w - omega_wall(nu, d, k), or log(w / omega_wall) for a log-solved omega: the
+      // flux sum and the sources are overwritten
       Dual ow = omega_wall(nud, d, kd);
-      sb[L::W] += Ww;
-      sb[L::K] += -Ww * ow.d;
+      if (cv.log_w) {
+        sb[L::W] += Ww / w;
+        sb[L::K] += -Ww * ow.d / ow.v;
+      } else {
+        sb[L::W] += Ww;
+        sb[L::K] += -Ww * ow.d;
+      }
       Ww = 0.0;
       wr[L::W] = 0.0;
     }

@@ -27,6 +27,50 @@ int upload_face_table(const FvMesh* m, const X* host, int width, X fill, X** dev
   return FV_OK;
 }
 
+// ---- log-solved turbulence scalars (LogScalars, aquaflux/turbulence/coupled.py:178-207)
+// The kernels run in the physical fields; the entry points below map the solved state to them
+// (phi = exp(w) on the transformed blocks, the tangent by the chain factor phi) and scale the
+// state cotangents and Jacobian columns they return by the same chain factor d(phi)/d(w) = phi.
+__device__ __forceinline__ bool log_field(int f, int kf, int tr) {
+  return (f == kf && (tr & 1)) || (f == kf + 1 && (tr & 2));
+}
+
+__global__ void k_to_physical(long nc, int nfld, int kf, int tr, const double* s, double* p) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (long)nfld * nc) return;
+  p[i] = log_field((int)(i / nc), kf, tr) ? exp(s[i]) : s[i];
+}
+
+__global__ void k_tangent_to_physical(long nc, int nfld, int kf, int tr, const double* p,
+                                      const double* t, double* pt) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (long)nfld * nc) return;
+  pt[i] = log_field((int)(i / nc), kf, tr) ? p[i] * t[i] : t[i];
+}
+
+// v *= phi on the transformed blocks (a state cotangent / partial derivative)
+__global__ void k_chain_state(long nc, int kf, int tr, const double* p, double* v) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 2 * nc) return;
+  const long j = (long)kf * nc + i;
+  if (log_field((int)(j / nc), kf, tr)) v[j] *= p[j];
+}
+
+// Jacobian columns of the transformed fields times phi of the column cell (BSR, nfld x nfld
+// row-major blocks, one thread per block row of cell c and field q).
+__global__ void k_chain_bsr(int nc, int nfld, int kf, int tr, const int* indptr, const int* indices,
+                            const double* p, double* values) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long)nfld * nc) return;
+  const int c = (int)(t % nc), q = (int)(t / nc);
+  for (int b = indptr[c]; b < indptr[c + 1]; ++b) {
+    const int j = indices[b];
+    double* row = values + ((long)b * nfld + q) * nfld;
+    for (int r = kf; r <= kf + 1; ++r)
+      if (log_field(r, kf, tr)) row[r] *= p[(long)r * nc + j];
+  }
+}
+
 __global__ void k_axpy_shift(long n, const double* shift, const double* v, double* out) {
   long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) out[i] += shift[i] * v[i];
@@ -47,6 +91,32 @@ __global__ void k_cell_to_rowmajor(int nc, int dim, const double* in, double* ou
 }
 
 }  // namespace
+
+// The physical state of a log-transformed case (written into c->phys), or `state` itself.
+static const double* physical_state(FvCase* c, const double* state, cudaStream_t s) {
+  if (!c->desc.scalar_transform) return state;
+  const long nc = c->mesh->nc;
+  k_to_physical<<<fv_blocks((long)c->nfld * nc, 256), 256, 0, s>>>(
+      nc, c->nfld, c->mesh->dim + 1, c->desc.scalar_transform, state, c->phys);
+  return c->phys;
+}
+
+// The physical tangent of `t` at the state last mapped by physical_state (into c->tphys).
+static const double* physical_tangent(FvCase* c, const double* t, cudaStream_t s) {
+  if (!c->desc.scalar_transform || !t) return t;
+  const long nc = c->mesh->nc;
+  k_tangent_to_physical<<<fv_blocks((long)c->nfld * nc, 256), 256, 0, s>>>(
+      nc, c->nfld, c->mesh->dim + 1, c->desc.scalar_transform, c->phys, t, c->tphys);
+  return c->tphys;
+}
+
+static void chain_state(FvCase* c, double* v, cudaStream_t s) {
+  if (!c->desc.scalar_transform || !v) return;
+  const long nc = c->mesh->nc;
+  k_chain_state<<<fv_blocks(2 * nc, 256), 256, 0, s>>>(nc, c->mesh->dim + 1,
+                                                        c->desc.scalar_transform, c->phys, v);
+}
+
 
 extern "C" int fv_case_create(const FvMesh* mesh, const FvCaseDesc* desc,
                               const signed char* flow_kind, const double* flow_vel,
@@ -75,6 +145,12 @@ extern "C" int fv_case_create(const FvMesh* mesh, const FvCaseDesc* desc,
       (desc->advection == 2 && !(desc->limiter_k > 0.0))) {
     fv_set_error("fv_case_create: advection must be 0 (upwind), 1 (linear upwind) or 2 "
                  "(Venkatakrishnan-limited, limiter_k > 0)");
+    return FV_ERR_ARG;
+  }
+  if (desc->scalar_transform < 0 || desc->scalar_transform > 3 ||
+      (desc->scalar_transform != 0 && !desc->turbulent)) {
+    fv_set_error("fv_case_create: scalar_transform must be a bit set in [0, 3] (bit 0 log k, "
+                 "bit 1 log omega), for turbulent cases only");
     return FV_ERR_ARG;
   }
   if (desc->turbulent && (!k_kind || !omega_kind || !sst_wall)) {
@@ -147,7 +223,12 @@ extern "C" int fv_case_create(const FvMesh* mesh, const FvCaseDesc* desc,
                                                         desc->gradient_sweeps, desc->advection)));
   FV_CUDA_TRY(cudaMalloc(&c->aux, fv_aux_bytes(m->dim, desc->turbulent, m->nf)));
   FV_CUDA_TRY(cudaMalloc(&c->dscalar, sizeof(double) * 4));
+  if (desc->scalar_transform) {
+    FV_CUDA_TRY(cudaMalloc(&c->phys, sizeof(double) * (size_t)c->nfld * m->nc));
+    FV_CUDA_TRY(cudaMalloc(&c->tphys, sizeof(double) * (size_t)c->nfld * m->nc));
+  }
   CaseView& v = c->view;
+  v.log_w = (desc->scalar_transform & 2) != 0;
   v.turb = desc->turbulent;
   v.rho = desc->rho;
   v.pin = desc->pressure_pin;
@@ -197,6 +278,8 @@ extern "C" int fv_case_destroy(FvCase* c) {
   cudaFree(c->flx);
   cudaFree(c->mu_cell);
   cudaFree(c->red);
+  cudaFree(c->phys);
+  cudaFree(c->tphys);
   for (cudaEvent_t e : c->prof_events) cudaEventDestroy(e);
   delete c;
   return FV_OK;
@@ -239,6 +322,7 @@ extern "C" int fv_case_autotune(FvCase* c, const double* state, const double* w,
     return FV_ERR_ARG;
   }
   cudaStream_t s = (cudaStream_t)stream;
+  state = physical_state(c, state, s);
   const int cand[4] = {32, 64, 96, 128};
   cudaEvent_t e0, e1;
   FV_CUDA_TRY(cudaEventCreate(&e0));
@@ -302,7 +386,8 @@ extern "C" int fv_residual(FvCase* c, const double* state, double* residual, voi
     fv_set_error("fv_residual: bad arguments");
     return FV_ERR_ARG;
   }
-  return fv_case_run(c, state, nullptr, FV_TAN_NONE, residual, nullptr, (cudaStream_t)stream);
+  cudaStream_t s = (cudaStream_t)stream;
+  return fv_case_run(c, physical_state(c, state, s), nullptr, FV_TAN_NONE, residual, nullptr, s);
 }
 
 extern "C" int fv_jvp(FvCase* c, const double* state, const double* v, double* residual,
@@ -311,7 +396,9 @@ extern "C" int fv_jvp(FvCase* c, const double* state, const double* v, double* r
     fv_set_error("fv_jvp: bad arguments");
     return FV_ERR_ARG;
   }
-  return fv_case_run(c, state, v, FV_TAN_STATE, residual, jv, (cudaStream_t)stream);
+  cudaStream_t s = (cudaStream_t)stream;
+  state = physical_state(c, state, s);
+  return fv_case_run(c, state, physical_tangent(c, v, s), FV_TAN_STATE, residual, jv, s);
 }
 
 extern "C" int fv_jvp_frozen(FvCase* c, const double* state, const double* v, double* jv,
@@ -320,7 +407,9 @@ extern "C" int fv_jvp_frozen(FvCase* c, const double* state, const double* v, do
     fv_set_error("fv_jvp_frozen: bad arguments");
     return FV_ERR_ARG;
   }
-  return fv_case_run(c, state, v, FV_TAN_FROZEN, nullptr, jv, (cudaStream_t)stream);
+  cudaStream_t s = (cudaStream_t)stream;
+  state = physical_state(c, state, s);
+  return fv_case_run(c, state, physical_tangent(c, v, s), FV_TAN_FROZEN, nullptr, jv, s);
 }
 
 namespace {
@@ -356,11 +445,12 @@ extern "C" int fv_probe_jacobian(FvCase* c, const double* state, int frozen, con
   cudaStream_t s = (cudaStream_t)stream;
   const int n = c->mesh->nc, b = c->nfld;
   const long len = (long)n * b;
+  state = physical_state(c, state, s);
   for (int field = 0; field < b; ++field) {
     for (int col = 0; col < n_colours; ++col) {
       k_probe_seed<<<fv_blocks(len, 256), 256, 0, s>>>(n, b, colour, col, field, c->tmp);
-      int rc = fv_case_run(c, state, c->tmp, frozen ? FV_TAN_FROZEN : FV_TAN_STATE, nullptr,
-                           c->tmp2, s);
+      int rc = fv_case_run(c, state, physical_tangent(c, c->tmp, s),
+                           frozen ? FV_TAN_FROZEN : FV_TAN_STATE, nullptr, c->tmp2, s);
       if (rc != FV_OK) return rc;
       k_probe_scatter<<<fv_blocks(n, 256), 256, 0, s>>>(n, b, indptr, indices, colour, col, field,
                                                           c->tmp2, values);
@@ -380,8 +470,16 @@ extern "C" int fv_assemble_jacobian(FvCase* c, const double* state, const int* i
     FV_CUDA_TRY(cudaMalloc(&c->jac_face,
                            fv_jac_face_bytes(c->mesh->dim, c->desc.turbulent, c->mesh->nf)));
   }
-  return fv_case_assemble_frozen(c, state, indptr, indices, values, c->jac_face,
-                                 (cudaStream_t)stream);
+  cudaStream_t s = (cudaStream_t)stream;
+  int rc = fv_case_assemble_frozen(c, physical_state(c, state, s), indptr, indices, values,
+                                   c->jac_face, s);
+  if (rc == FV_OK && c->desc.scalar_transform) {
+    k_chain_bsr<<<fv_blocks((long)c->nfld * c->mesh->nc, 128), 128, 0, s>>>(
+        c->mesh->nc, c->nfld, c->mesh->dim + 1, c->desc.scalar_transform, indptr, indices,
+        c->phys, values);
+    FV_CUDA_TRY(cudaGetLastError());
+  }
+  return rc;
 }
 
 extern "C" int fv_jvp_batch(FvCase* c, const double* state, const double* v, int k, double* jv,
@@ -391,9 +489,11 @@ extern "C" int fv_jvp_batch(FvCase* c, const double* state, const double* v, int
     return FV_ERR_ARG;
   }
   const long n = fv_case_n_unknowns(c);
+  cudaStream_t s = (cudaStream_t)stream;
+  state = physical_state(c, state, s);
   for (int i = 0; i < k; ++i) {
-    int rc = fv_case_run(c, state, v + (long)i * n, FV_TAN_STATE, nullptr, jv + (long)i * n,
-                         (cudaStream_t)stream);
+    int rc = fv_case_run(c, state, physical_tangent(c, v + (long)i * n, s), FV_TAN_STATE, nullptr,
+                         jv + (long)i * n, s);
     if (rc != FV_OK) return rc;
   }
   return FV_OK;
@@ -406,7 +506,8 @@ extern "C" int fv_jvp_shift(FvCase* c, const double* state, const double* v, con
     return FV_ERR_ARG;
   }
   cudaStream_t s = (cudaStream_t)stream;
-  int rc = fv_case_run(c, state, v, FV_TAN_STATE, nullptr, jv, s);
+  state = physical_state(c, state, s);
+  int rc = fv_case_run(c, state, physical_tangent(c, v, s), FV_TAN_STATE, nullptr, jv, s);
   if (rc != FV_OK) return rc;
   long n = fv_case_n_unknowns(c);
   k_axpy_shift<<<fv_blocks(n, 256), 256, 0, s>>>(n, shift, v, jv);
@@ -421,6 +522,7 @@ extern "C" int fv_param_jvp(FvCase* c, const double* state, double* out_mu, doub
     return FV_ERR_ARG;
   }
   cudaStream_t s = (cudaStream_t)stream;
+  state = physical_state(c, state, s);
   if (out_mu) {
     int rc = fv_case_run(c, state, nullptr, FV_TAN_MU, nullptr, out_mu, s);
     if (rc != FV_OK) return rc;
@@ -438,7 +540,10 @@ extern "C" int fv_vjp(FvCase* c, const double* state, const double* w, double* r
     fv_set_error("fv_vjp: bad arguments");
     return FV_ERR_ARG;
   }
-  return fv_case_vjp_run(c, state, w, residual, vjp, (cudaStream_t)stream);
+  cudaStream_t s = (cudaStream_t)stream;
+  int rc = fv_case_vjp_run(c, physical_state(c, state, s), w, residual, vjp, s);
+  if (rc == FV_OK) chain_state(c, vjp, s);
+  return rc;
 }
 
 extern "C" int fv_node_vjp(FvCase* c, const double* state, const double* w, double* dnodes,
@@ -447,7 +552,8 @@ extern "C" int fv_node_vjp(FvCase* c, const double* state, const double* w, doub
     fv_set_error("fv_node_vjp: bad arguments");
     return FV_ERR_ARG;
   }
-  return fv_case_node_vjp(c, state, w, dnodes, (cudaStream_t)stream);
+  cudaStream_t s = (cudaStream_t)stream;
+  return fv_case_node_vjp(c, physical_state(c, state, s), w, dnodes, s);
 }
 
 extern "C" int fv_face_functional(FvCase* c, const double* state, const double* weights,
@@ -457,8 +563,11 @@ extern "C" int fv_face_functional(FvCase* c, const double* state, const double* 
     fv_set_error("fv_face_functional: bad arguments");
     return FV_ERR_ARG;
   }
-  return fv_case_face_functional(c, state, weights, viscous_only, value, dstate, dparams, dnodes,
-                                 (cudaStream_t)stream);
+  cudaStream_t s = (cudaStream_t)stream;
+  int rc = fv_case_face_functional(c, physical_state(c, state, s), weights, viscous_only, value,
+                                   dstate, dparams, dnodes, s);
+  if (rc == FV_OK) chain_state(c, dstate, s);
+  return rc;
 }
 
 extern "C" int fv_param_vjp(FvCase* c, const double* state, const double* w, double* out,
@@ -469,6 +578,7 @@ extern "C" int fv_param_vjp(FvCase* c, const double* state, const double* w, dou
   }
   cudaStream_t s = (cudaStream_t)stream;
   long n = fv_case_n_unknowns(c);
+  state = physical_state(c, state, s);
   int rc = fv_case_run(c, state, nullptr, FV_TAN_MU, nullptr, c->tmp2, s);
   if (rc == FV_OK) rc = fv_dot_f64(n, w, c->tmp2, out, stream);
   if (rc == FV_OK) rc = fv_case_run(c, state, nullptr, FV_TAN_INLET, nullptr, c->tmp2, s);

@@ -87,6 +87,7 @@ struct CaseView {
   const double* inv_wd;       // (nc) 1 / wall distance
   const double* inv_wd2;      // (nc) 1 / wall distance^2
   const double* mu_cell;      // (nc) per-cell molecular viscosity (laminar), or null
+  int log_w;                  // the omega fixation row is the log ratio (log-solved omega)
 };
 
 // Workspace of the mesh-coordinate adjoint (residual.cu), allocated on its first use.
@@ -133,6 +134,8 @@ struct FvCase {
   bool flx_active = false;      // the adjoints add flx to their face-flux cotangents
   bool flx_viscous = false;     // ... with the pressure part p_f A n_i taken out
   double* red = nullptr;        // reduction partials of the functional
+  double* phys = nullptr;       // (n_unknowns) physical state of a log-transformed case
+  double* tphys = nullptr;      // (n_unknowns) physical tangent of a log-transformed case
   CaseView view;
   // optional per-stage CUDA-event profiling (fv_case_profile_begin / _end)
   std::vector<cudaEvent_t> prof_events;  // max_runs * (FV_MAX_STAGES + 1)

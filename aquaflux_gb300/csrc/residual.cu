@@ -1000,7 +1000,9 @@ __device__ __forceinline__ void sst_rows(const MeshView& m, const CaseView& cv, 
   rk = rk - lim * V;
   rk = rk + BETA_STAR * V * k * weff;
   if (wall) {
-    rw = w - omega_wall(nu, d, k);
+    // DifferenceRow w - omega_wall, or LogRatioRow log(w / omega_wall) for a log-solved omega
+    // (aquaflux/discretization/fixed_value.py:80-120)
+    rw = cv.log_w ? fv_log(w / omega_wall(nu, d, k)) : w - omega_wall(nu, d, k);
   } else {
     const T alpha = ALPHA_2 + F1 * (ALPHA_1 - ALPHA_2);
     const T cap = limit / fv_max(nut, cst(NUT_FLOOR, nut));

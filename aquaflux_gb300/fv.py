@@ -126,7 +126,8 @@ class FlowCase:
     def __init__(self, dmesh: DeviceMesh, *, mu: float, rho: float, flow_bc: dict,
                  pressure_pin: int | None = None, pressure_pin_value: float = 0.0,
                  sst: dict | None = None, gradient: dict | None = None,
-                 advection: dict | None = None):
+                 advection: dict | None = None, k_transform: str = "direct",
+                 omega_transform: str = "direct"):
         self.dmesh = dmesh
         mesh = dmesh.mesh
         self.dim, self.n_cells = mesh.dim, mesh.n_cells
@@ -149,9 +150,16 @@ class FlowCase:
         sweeps = 0 if gradient is None else int(gradient["sweeps"])
         relax = 1.0 if gradient is None else float(gradient.get("relaxation", 1.0))
         self.gradient = gradient
+        for name, tr in (("k_transform", k_transform), ("omega_transform", omega_transform)):
+            if tr not in ("direct", "log"):
+                raise ValueError(f"{name} must be 'direct' or 'log', got {tr!r}")
+        self.k_transform, self.omega_transform = k_transform, omega_transform
+        transform = (k_transform == "log") | ((omega_transform == "log") << 1)
+        if transform and sst is None:
+            raise ValueError("the log transforms apply to the k and omega of a turbulent case")
         desc = FvCaseDesc(1 if sst is not None else 0, mu_const, float(rho),
                           -1 if pressure_pin is None else int(pressure_pin),
-                          float(pressure_pin_value), sweeps, relax, adv_kind, adv_k)
+                          float(pressure_pin_value), sweeps, relax, adv_kind, adv_k, transform)
         h = ctypes.c_void_p()
         arrs = [np.ascontiguousarray(t.get(k)) if t.get(k) is not None else None
                 for k in ("flow_kind", "flow_vel", "flow_p", "k_kind", "k_val", "omega_kind",
@@ -177,6 +185,28 @@ class FlowCase:
         if inlet_scale is not None:
             self.inlet_scale = float(inlet_scale)
         check(lib().fv_case_set_params(self._h, self.mu, self.inlet_scale))
+
+    def _log_blocks(self):
+        n, d = self.n_cells, self.dim
+        return [slice((d + 1 + i) * n, (d + 2 + i) * n)
+                for i, tr in enumerate((self.k_transform, self.omega_transform)) if tr == "log"]
+
+    def to_solved(self, state):
+        """Physical ``[u.., p, k, omega]`` -> the solved variables of this case (``log`` on the
+        log-transformed blocks, ``CoupledRANS.solved_state``,
+        ``aquaflux/turbulence/coupled.py:383-392``)."""
+        out = state.clone() if torch.is_tensor(state) else np.array(state, dtype=np.float64)
+        for sl in self._log_blocks():
+            out[sl] = torch.log(out[sl]) if torch.is_tensor(out) else np.log(out[sl])
+        return out
+
+    def to_physical(self, state):
+        """Solved variables -> physical ``[u.., p, k, omega]`` (``exp`` on the log blocks,
+        ``CoupledRANS.physical_fields``, ``coupled.py:366-381``)."""
+        out = state.clone() if torch.is_tensor(state) else np.array(state, dtype=np.float64)
+        for sl in self._log_blocks():
+            out[sl] = torch.exp(out[sl]) if torch.is_tensor(out) else np.exp(out[sl])
+        return out
 
     def _vec(self, x) -> torch.Tensor:
         x = torch.as_tensor(x, dtype=torch.float64, device="cuda").contiguous()

@@ -55,6 +55,8 @@ class Workload:
     omega_in: float = 0.0
     gradient: dict | None = None
     advection: dict | None = None
+    k_transform: str = "direct"      # solved variable of k: "direct" or "log" (k = exp(w_k))
+    omega_transform: str = "direct"  # ... of omega (LogScalars, omega = exp(w))
 
     @property
     def n_unknowns(self) -> int:
@@ -82,7 +84,8 @@ class Workload:
         dm = fv.DeviceMesh(self.mesh)
         return fv.FlowCase(dm, mu=self.mu, rho=self.rho, flow_bc=self.flow_bc,
                            pressure_pin=self.pressure_pin, sst=self.sst, gradient=self.gradient,
-                           advection=self.advection)
+                           advection=self.advection, k_transform=self.k_transform,
+                           omega_transform=self.omega_transform)
 
 
 def cavity(n: int = 64, mu: float = 0.01, lid: float = 1.0) -> Workload:

@@ -96,6 +96,14 @@ typedef struct FvCaseDesc {
    * (aquaflux/discretization/advection.py:99-157, aquaflux/schemes/limiter.py:78-117). */
   int advection;
   double limiter_k;
+  /* Solved variable of the turbulence scalars (CoupledRANS k_transform / omega_transform,
+   * aquaflux/turbulence/coupled.py:111-207): bit 0 set = k is solved as w_k with k = exp(w_k),
+   * bit 1 set = omega as w with omega = exp(w) (LogScalars); clear = the field itself
+   * (DirectScalars).  The state vectors of every call hold the solved variables; the residual
+   * rows stay the physical transport residuals, except the near-wall omega fixation, which under a
+   * log omega is the log ratio log(omega / omega_wall) (LogRatioRow,
+   * aquaflux/discretization/fixed_value.py:96-120).  Turbulent cases only. */
+  int scalar_transform;
 } FvCaseDesc;
 
 int fv_case_create(const FvMesh* mesh, const FvCaseDesc* desc,

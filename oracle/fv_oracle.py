@@ -327,7 +327,7 @@ def advection_flux(m: Metrics, phi, grad, mass_flux, bvals, scheme):
 
 # ----------------------------------------------------------------------------- the case
 def make_case(mesh, *, mu, rho, flow_bc, pressure_pin=None, pressure_pin_value=0.0, sst=None,
-              gradient=None, advection=None):
+              gradient=None, advection=None, transforms=("direct", "direct")):
     """Flatten a case description into per-face tables.
 
     ``mesh``: object with ``nodes, fn_offsets, fn_indices, owner, neighbour, n_cells, patches``.
@@ -338,6 +338,8 @@ def make_case(mesh, *, mu, rho, flow_bc, pressure_pin=None, pressure_pin_value=0
     Green-Gauss by ``s`` swept sweeps).
     ``advection``: ``None`` (first-order upwind) or ``{"k": K}`` (limited linear upwind with the
     Venkatakrishnan limiter, ``K`` None for the unlimited reconstruction).
+    ``transforms``: the solved variables of k and omega, ``"direct"`` or ``"log"`` (``DirectScalars``
+    / ``LogScalars``, ``aquaflux/turbulence/coupled.py:111-207``).
     """
     nf = len(mesh.owner)
     dim = mesh.nodes.shape[1]
@@ -354,7 +356,8 @@ def make_case(mesh, *, mu, rho, flow_bc, pressure_pin=None, pressure_pin_value=0
             pb[faces] = float(spec[1])
     case = {"mesh": mesh, "dim": dim, "mu": float(mu), "rho": float(rho), "bc_kind": kind,
             "bc_vel": vel, "bc_p": pb, "pin": pressure_pin, "pin_value": float(pressure_pin_value),
-            "sst": None, "gradient": gradient, "advection": advection}
+            "sst": None, "gradient": gradient, "advection": advection,
+            "transforms": tuple(transforms)}
     if sst is not None:
         sc = {"nu": float(sst["nu"])}
         for fld in ("k", "omega"):
@@ -627,9 +630,13 @@ class Oracle:
         visc = mu_c
         boundary_visc = None
         fields = {}
+        log_k, log_w = (t == "log" for t in case.get("transforms", ("direct", "direct")))
         if sst is not None:
+            # CoupledRANS.physical_fields (coupled.py:366-381): exp of a log-solved block
             k = state[n_flow:n_flow + nc]
             w = state[n_flow + nc:]
+            k = torch.exp(k) if log_k else k
+            w = torch.exp(w) if log_w else w
             nu = (mu / rho) * torch.ones(nc, dtype=T)
             dist, dgrad = self.wall_d, self.wall_dgrad
             if self._live_geometry:
@@ -765,7 +772,11 @@ class Oracle:
         r_w = r_w - (-beta * w ** 2 * vol)
         cross = 2.0 * (1.0 - f1) * SIGMA_W2 * _dot(grad_k, grad_w) / w
         r_w = r_w - cross * vol
-        r_w = r_w.index_copy(0, wc, w[wc] - omega_wall(nu[wc], dist[wc], k[wc]))
+        # FixedValueCells with the transform's fixation row (fixed_value.py:80-158): the plain
+        # difference, or the log ratio for a log-solved omega
+        target = omega_wall(nu[wc], dist[wc], k[wc])
+        fix = torch.log(w[wc] / target) if log_w else w[wc] - target
+        r_w = r_w.index_copy(0, wc, fix)
         r = torch.cat(out + [r_k, r_w])
         if return_fields:
             fields.update(strain=strain, f1=f1, nut=nut, grad_k=grad_k, grad_w=grad_w, shear=shear)

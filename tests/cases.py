@@ -63,6 +63,11 @@ SST = {
                   file="corrected", gradient={"sweeps": 3, "relaxation": 0.8}),
     "lsst2": dict(prefix="lsst2_", dim=2, nu=2e-5, walls=["bottom", "top"], file="limited",
                   advection={"k": 5.0}),
+    # LogScalars: log omega (2D), log k and log omega (3D); states hold the solved variables
+    "wsst2": dict(prefix="wsst2_", dim=2, nu=2e-5, walls=["bottom", "top"], file="logscalars",
+                  transforms=("direct", "log")),
+    "bsst3": dict(prefix="bsst3_", dim=3, nu=1e-3, walls=["bottom", "top", "back", "front"],
+                  file="logscalars", transforms=("log", "log")),
 }
 
 
@@ -84,7 +89,8 @@ def oracle_case(name: str):
     k_in, w_in = d[spec["prefix"] + "inlet"]
     fb, sst = sst_spec(spec["dim"], spec["nu"], float(k_in), float(w_in), spec["walls"])
     case = fo.make_case(mesh, mu=spec["nu"], rho=1.0, flow_bc=fb, sst=sst,
-                        gradient=spec.get("gradient"), advection=spec.get("advection"))
+                        gradient=spec.get("gradient"), advection=spec.get("advection"),
+                        transforms=spec.get("transforms", ("direct", "direct")))
     return case, d, spec["prefix"]
 
 
@@ -114,8 +120,10 @@ def device_case(name: str):
         spec = SST[name]
         k_in, w_in = d[p + "inlet"]
         fb, sst = sst_spec(spec["dim"], spec["nu"], float(k_in), float(w_in), spec["walls"])
+        k_tr, w_tr = spec.get("transforms", ("direct", "direct"))
         fc = fv.FlowCase(dm, mu=spec["nu"], rho=1.0, flow_bc=fb, sst=sst,
-                         gradient=spec.get("gradient"), advection=spec.get("advection"))
+                         gradient=spec.get("gradient"), advection=spec.get("advection"),
+                         k_transform=k_tr, omega_transform=w_tr)
     return fc, case, d, p
 
 
@@ -128,4 +136,6 @@ def workload_oracle_case(wl):
         sst = {"nu": wl.mu / wl.rho, "walls": wl.sst["walls"], "k": wl.sst["k"],
                "omega": wl.sst["omega"]}
     return fo.make_case(wl.mesh, mu=wl.mu, rho=wl.rho, flow_bc=wl.flow_bc,
-                        pressure_pin=wl.pressure_pin, sst=sst, gradient=wl.gradient)
+                        pressure_pin=wl.pressure_pin, sst=sst, gradient=wl.gradient,
+                        advection=wl.advection,
+                        transforms=(wl.k_transform, wl.omega_transform))

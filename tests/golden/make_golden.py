@@ -55,7 +55,7 @@ from aquaflux.schemes import CompactGreenGauss, CorrectedGreenGauss  # noqa: E40
 from aquaflux.schemes.gradient import SweptGradientSolve  # noqa: E402
 from aquaflux.solve import ilu0 as ref_ilu0  # noqa: E402
 from aquaflux.turbulence import SSTModel, SSTTurbulence, inlet_k, inlet_omega  # noqa: E402
-from aquaflux.turbulence.coupled import CoupledRANS  # noqa: E402
+from aquaflux.turbulence.coupled import CoupledRANS, LogScalars  # noqa: E402
 
 sys.path.insert(0, os.path.join(REF, "tests", "unit"))
 
@@ -202,7 +202,7 @@ def laminar_cases():
 
 # --------------------------------------------------------------------------- k-omega SST
 def _rans(mesh, geom, dim, nu, u_in, walls, inlet="left", outlet="right", intensity=0.05,
-          length_scale=0.07, scheme=None, advection=None):
+          length_scale=0.07, scheme=None, advection=None, k_transform=None, omega_transform=None):
     scheme = scheme or CompactGreenGauss()
     advection = advection or FirstOrderUpwind()
     rho = 1.0
@@ -223,7 +223,8 @@ def _rans(mesh, geom, dim, nu, u_in, walls, inlet="left", outlet="right", intens
         model, mesh, geom, scheme, advection, density=rho,
         molecular_viscosity=jnp.full(mesh.n_cells, nu), wall_patches=list(walls),
         k_boundary=BoundaryConditions(k_bc), omega_boundary=BoundaryConditions(w_bc))
-    return CoupledRANS.build(momentum, turb), turb, k_in, omega_in
+    return (CoupledRANS.build(momentum, turb, k_transform=k_transform,
+                              omega_transform=omega_transform), turb, k_in, omega_in)
 
 
 def _rans_states(rng, n, dim, k_in, omega_in, count, negative_k=False):
@@ -283,6 +284,51 @@ def sst_cases():
     scale = np.abs(states[0]) + 1e-3
     out["sst3_jvp_dir"] = v * scale
     out["sst3_jvp_fd"] = _fd_jvp(coupled.residual, states[0], v * scale, 1e-7)
+    return out
+
+
+# --------------------------------------------------------------------------- log-solved scalars
+def logscalar_cases():
+    """``CoupledRANS`` with ``LogScalars`` (``aquaflux/turbulence/coupled.py:178-207``): the state
+    holds ``log omega`` (and ``log k`` in the 3D case); the near-wall omega rows are the log ratio
+    (``LogRatioRow``, ``aquaflux/discretization/fixed_value.py:96-120``).  Same meshes and inlet
+    conditions as the direct cases ``sst2_`` / ``sst3_``."""
+    out = {}
+    rng = np.random.default_rng(41)
+    nx, ny = 12, 8
+    yn = graded_nodes(ny, 1.0, 1.2)
+    mesh = structured_grid_2d(nx, ny, lx=4.0, ly=1.0, named_boundaries=True, y_nodes=yn)
+    mesh = _with_nodes(mesh, jitter_interior_nodes(np.asarray(mesh.node_coords), (nx, ny),
+                                                   (4.0, 1.0), 0.1, 4))
+    shape = (5, 4, 3)
+    mesh3 = structured_grid_3d(*shape, lx=2.0, ly=1.0, lz=1.0, named_boundaries=True)
+    mesh3 = _with_nodes(mesh3, bump_channel_nodes_3d(shape, (2.0, 1.0, 1.0), 0.1, 0.1, 9))
+    for prefix, m, dim, nu, walls, log_k in (
+            ("wsst2_", mesh, 2, 2e-5, ["bottom", "top"], False),
+            ("bsst3_", mesh3, 3, 1e-3, ["bottom", "top", "back", "front"], True)):
+        geom = m.geometry()
+        coupled, turb, k_in, omega_in = _rans(
+            m, geom, dim, nu, 1.0, walls, k_transform=LogScalars() if log_k else None,
+            omega_transform=LogScalars())
+        out.update(_mesh_arrays(prefix, m, geom))
+        out[prefix + "wall_distance"] = np.asarray(turb.wall_distance)
+        out[prefix + "wall_distance_gradient"] = np.asarray(turb.wall_distance_gradient)
+        out[prefix + "inlet"] = np.array([k_in, omega_in])
+        n = m.n_cells
+        states = []
+        for phys in _rans_states(rng, n, dim, k_in, omega_in, 2):
+            solved = phys.copy()
+            solved[(dim + 2) * n:] = np.log(phys[(dim + 2) * n:])
+            if log_k:
+                solved[(dim + 1) * n:(dim + 2) * n] = np.log(phys[(dim + 1) * n:(dim + 2) * n])
+            states.append(solved)
+        out[prefix + "states"] = np.stack(states)
+        out[prefix + "residuals"] = np.stack([np.asarray(coupled.residual(jnp.asarray(s)))
+                                              for s in states])
+        v = rng.standard_normal((dim + 3) * n)
+        scale = np.abs(states[0]) + 1e-3
+        out[prefix + "jvp_dir"] = v * scale
+        out[prefix + "jvp_fd"] = _fd_jvp(coupled.residual, states[0], v * scale, 1e-7)
     return out
 
 
@@ -564,7 +610,7 @@ FILES = {"colouring": lambda: colouring_cases(), "meshes": lambda: mesh_cases(),
          "laminar": lambda: laminar_cases(), "sst": lambda: sst_cases(),
          "ilu0": lambda: ilu_cases(), "corrected": lambda: corrected_cases(),
          "operator": lambda: operator_cases(), "limited": lambda: limited_cases(),
-         "openfoam": lambda: openfoam_cases()}
+         "openfoam": lambda: openfoam_cases(), "logscalars": lambda: logscalar_cases()}
 
 
 def main():

@@ -62,7 +62,7 @@ def test_jvp_matches_oracle(name):
 
 
 @pytest.mark.parametrize("name", ["cav8", "lam3", "sst2", "sst3", "ccavj", "csst2", "lcavj", "ucavj",
-                                  "lsst2"])
+                                  "lsst2", "wsst2", "bsst3"])
 def test_jvp_matches_reference_finite_differences(name):
     fc, case, d, p = device_case(name)
     s = d[p + "states"][1 if name == "cav8" else 0]
@@ -70,7 +70,7 @@ def test_jvp_matches_reference_finite_differences(name):
     assert _rel(jv, d[p + "jvp_fd"]) <= 1e-7
 
 
-@pytest.mark.parametrize("name", ["cavj", "lam3", "sst2", "ccavj", "csst3"])
+@pytest.mark.parametrize("name", ["cavj", "lam3", "sst2", "ccavj", "csst3", "wsst2", "bsst3"])
 def test_parameter_jvp_matches_oracle(name):
     fc, case, d, p = device_case(name)
     orc = fo.Oracle(case)
@@ -164,7 +164,8 @@ def test_vjp_is_the_transpose_of_jvp_on_gpu(name):
     assert abs(lhs - rhs) <= 1e-12 * scale
 
 
-@pytest.mark.parametrize("name", ["cavj", "lam3", "sst2", "sst3", "ccavj", "csst2", "csst3"])
+@pytest.mark.parametrize("name", ["cavj", "lam3", "sst2", "sst3", "ccavj", "csst2", "csst3", "wsst2",
+                                  "bsst3"])
 def test_param_vjp_matches_oracle(name):
     fc, case, d, p = device_case(name)
     orc = fo.Oracle(case)
