@@ -25,7 +25,8 @@ class FvCaseDesc(ctypes.Structure):
                 ("pressure_pin", c_int), ("pressure_pin_value", c_double),
                 ("gradient_sweeps", c_int), ("gradient_relaxation", c_double),
                 ("advection", c_int), ("limiter_k", c_double),
-                ("scalar_transform", c_int)]
+                ("scalar_transform", c_int), ("scalar_advection", c_int),
+                ("scalar_limiter_k", c_double)]
 
 
 # name -> (restype, argtypes); this table is the binding a ctypes user of the C ABI adds.

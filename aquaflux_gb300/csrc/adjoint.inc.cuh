@@ -317,9 +317,11 @@ __global__ void __launch_bounds__(128) a_flux(MeshView m, CaseView cv, Src<doubl
         const double fb = FLb[i];
         double up = out ? uo : un;
         if constexpr (LIM) {
-          const int cu = out ? o : n;
-          up += aw.psi[(long)i * nc + cu] * rec_dot<DIM>(m, G, i, f, cu);
-          if (out != isnb) rec_adj(i, i, f, fb * mdot);
+          if (cv.rec_mom) {
+            const int cu = out ? o : n;
+            up += aw.psi[(long)i * nc + cu] * rec_dot<DIM>(m, G, i, f, cu);
+            if (out != isnb) rec_adj(i, i, f, fb * mdot);
+          }
         }
         mdotb += fb * up;
         const double k1 = fb * cmo;  // F_i = ... - c cpn
@@ -356,9 +358,11 @@ __global__ void __launch_bounds__(128) a_flux(MeshView m, CaseView cv, Src<doubl
           const double fb = FLb[q];
           double up = vout ? phio : phin;
           if constexpr (LIM) {
-            const int cu = vout ? o : n;
-            up += aw.psi[(long)(DIM + s) * nc + cu] * rec_dot<DIM>(m, G, q, f, cu);
-            if (vout != isnb) rec_adj(DIM + s, q, f, fb * vflux);
+            if (cv.rec_sca) {
+              const int cu = vout ? o : n;
+              up += aw.psi[(long)(DIM + s) * nc + cu] * rec_dot<DIM>(m, G, q, f, cu);
+              if (vout != isnb) rec_adj(DIM + s, q, f, fb * vflux);
+            }
           }
           mdotb += fb * up * irho;
           const double k1 = fb * cs_;
@@ -452,7 +456,7 @@ __global__ void __launch_bounds__(128) a_flux(MeshView m, CaseView cv, Src<doubl
         const double fb = FLb[i];
         double up = out ? uo[i] : bu[i];
         if constexpr (LIM) {
-          if (out) {
+          if (out && cv.rec_mom) {
             up += aw.psi[(long)i * nc + o] * rec_dot<DIM>(m, G, i, f, o);
             rec_adj(i, i, f, fb * mdot);
           }
@@ -498,7 +502,7 @@ __global__ void __launch_bounds__(128) a_flux(MeshView m, CaseView cv, Src<doubl
           const double fb = FLb[q];
           double up = vout ? phio : bphi;
           if constexpr (LIM) {
-            if (vout) {
+            if (vout && cv.rec_sca) {
               up += aw.psi[(long)(DIM + s) * nc + o] * rec_dot<DIM>(m, G, q, f, o);
               rec_adj(DIM + s, q, f, fb * vflux);
             }
@@ -559,7 +563,7 @@ __global__ void __launch_bounds__(128) a_flux(MeshView m, CaseView cv, Src<doubl
 // gradient cotangents; a neighbour's to lnb (per face and side), gathered by a_limiter_gather.
 template <int DIM, bool TURB>
 __global__ void __launch_bounds__(128) a_limiter(MeshView m, Src<double> st, const double* G,
-                                                 double K, AdjWork aw) {
+                                                 double Km, double Ks, AdjWork aw) {
   constexpr int NA = DIM + (TURB ? 2 : 0);
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= m.nc) return;
@@ -568,7 +572,16 @@ __global__ void __launch_bounds__(128) a_limiter(MeshView m, Src<double> st, con
 #pragma unroll 1
   for (int a = 0; a < NA; ++a) {
     const int q = advected_field<DIM, TURB>(a);
+    const double K = a < DIM ? Km : Ks;
     const double pb = aw.psib[(long)a * nc + c];
+    if (!(K > 0.0)) {  // psi = 1: no dependence (the neighbour slots still need writing)
+      for (int i = b; i < e; ++i) {
+        const unsigned ent = m.cf_face[i];
+        const int f = (int)(ent & ~FV_NB_BIT);
+        if (f < m.nfi) aw.lnb[((long)((ent & FV_NB_BIT) ? NA : 0) + a) * nf + f] = 0.0;
+      }
+      continue;
+    }
     // seeds: -1 = phi_c, 0..DIM-1 = grad_j, then the cell's faces (their other cell's phi)
     auto eval = [&](int seed_grad, int seed_cell) {
       auto phi = [&](int cell) {

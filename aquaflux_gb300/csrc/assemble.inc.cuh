@@ -149,8 +149,7 @@ int assemble_frozen(FvCase* cs, const double* state, const int* indptr, const in
   k_dcoeff<Dual><<<bc, TB, 0, s>>>(m, w.acown, w.acnb, w.dco);
   const long npsi = psi_count<DIM, TURB>(cs);
   if (npsi)
-    k_limiter<Dual, DIM, TURB><<<bc, TB, 0, s>>>(m, st, w.G, cs->desc.advection == 2 ?
-                                                 cs->desc.limiter_k : 0.0, w.psi);
+    k_limiter<Dual, DIM, TURB><<<bc, TB, 0, s>>>(m, st, w.G, cv.lim_km, cv.lim_ks, w.psi);
   k_jac_face<DIM, TURB><<<bf, TB, 0, s>>>(m, cv, state, par, w.G, w.cl, w.dco,
                                           npsi ? w.psi : nullptr, D);
   k_jac_cell<DIM, TURB><<<fv_blocks((long)NF * nc, TB), TB, 0, s>>>(

@@ -147,6 +147,14 @@ extern "C" int fv_case_create(const FvMesh* mesh, const FvCaseDesc* desc,
                  "(Venkatakrishnan-limited, limiter_k > 0)");
     return FV_ERR_ARG;
   }
+  if (desc->scalar_advection < 0 || desc->scalar_advection > 3 ||
+      (desc->scalar_advection != 0 && !desc->turbulent) ||
+      (desc->scalar_advection == 3 && !(desc->scalar_limiter_k > 0.0))) {
+    fv_set_error("fv_case_create: scalar_advection must be 0 (the momentum scheme), 1 (upwind), 2 "
+                 "(linear upwind) or 3 (Venkatakrishnan-limited, scalar_limiter_k > 0), for "
+                 "turbulent cases only");
+    return FV_ERR_ARG;
+  }
   if (desc->scalar_transform < 0 || desc->scalar_transform > 3 ||
       (desc->scalar_transform != 0 && !desc->turbulent)) {
     fv_set_error("fv_case_create: scalar_transform must be a bit set in [0, 3] (bit 0 log k, "
@@ -214,13 +222,17 @@ extern "C" int fv_case_create(const FvMesh* mesh, const FvCaseDesc* desc,
     }
     k_inv_distance<<<fv_blocks(m->nc, 256), 256, 0, s>>>(m->nc, c->wd, c->inv_wd);
   }
+  // effective schemes: momentum (0 upwind, 1 linear, 2 limited) and k, omega likewise
+  const int sadv = desc->scalar_advection == 0 ? desc->advection : desc->scalar_advection - 1;
+  const double sK = desc->scalar_advection == 0 ? desc->limiter_k : desc->scalar_limiter_k;
+  const int rec_any = (desc->advection >= 1 || (desc->turbulent && sadv >= 1)) ? 1 : 0;
   c->work_bytes = fv_residual_work_bytes(m->dim, desc->turbulent, m->nc, m->nf,
-                                        desc->gradient_sweeps, desc->advection);
+                                        desc->gradient_sweeps, rec_any);
   FV_CUDA_TRY(cudaMalloc(&c->work, c->work_bytes));
   FV_CUDA_TRY(cudaMalloc(&c->tmp, sizeof(double) * (size_t)c->nfld * m->nc));
   FV_CUDA_TRY(cudaMalloc(&c->tmp2, sizeof(double) * (size_t)c->nfld * m->nc));
   FV_CUDA_TRY(cudaMalloc(&c->adj, fv_adjoint_work_bytes(m->dim, desc->turbulent, m->nc, m->nf,
-                                                        desc->gradient_sweeps, desc->advection)));
+                                                        desc->gradient_sweeps, rec_any)));
   FV_CUDA_TRY(cudaMalloc(&c->aux, fv_aux_bytes(m->dim, desc->turbulent, m->nf)));
   FV_CUDA_TRY(cudaMalloc(&c->dscalar, sizeof(double) * 4));
   if (desc->scalar_transform) {
@@ -229,6 +241,10 @@ extern "C" int fv_case_create(const FvMesh* mesh, const FvCaseDesc* desc,
   }
   CaseView& v = c->view;
   v.log_w = (desc->scalar_transform & 2) != 0;
+  v.rec_mom = desc->advection >= 1;
+  v.rec_sca = desc->turbulent && sadv >= 1;
+  v.lim_km = desc->advection == 2 ? desc->limiter_k : 0.0;
+  v.lim_ks = (desc->turbulent && sadv == 2) ? sK : 0.0;
   v.turb = desc->turbulent;
   v.rho = desc->rho;
   v.pin = desc->pressure_pin;

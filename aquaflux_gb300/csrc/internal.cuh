@@ -88,6 +88,8 @@ struct CaseView {
   const double* inv_wd2;      // (nc) 1 / wall distance^2
   const double* mu_cell;      // (nc) per-cell molecular viscosity (laminar), or null
   int log_w;                  // the omega fixation row is the log ratio (log-solved omega)
+  int rec_mom, rec_sca;       // linear-upwind reconstruction of the momentum / the k, omega faces
+  double lim_km, lim_ks;      // their Venkatakrishnan constants (0: unlimited, psi = 1)
 };
 
 // Workspace of the mesh-coordinate adjoint (residual.cu), allocated on its first use.

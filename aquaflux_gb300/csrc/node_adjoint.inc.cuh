@@ -672,7 +672,7 @@ int node_vjp(FvCase* cs, const double* state, const double* W, double* dnodes, c
 
 int fv_case_node_vjp(FvCase* cs, const double* state, const double* w, double* dnodes,
                      cudaStream_t s) {
-  if (cs->desc.gradient_sweeps != 0 || cs->desc.advection != 0) {
+  if (cs->desc.gradient_sweeps != 0 || cs->view.rec_mom || cs->view.rec_sca) {
     fv_set_error("fv_node_vjp: the mesh-coordinate adjoint supports the compact gradient scheme "
                  "and first-order upwind advection (gradient_sweeps = 0, advection = 0)");
     return FV_ERR_ARG;

@@ -297,7 +297,7 @@ __host__ __device__ constexpr int n_advected() {
 }
 template <int DIM, bool TURB>
 long psi_count(const FvCase* cs) {
-  return cs->desc.advection >= 1 ? (long)n_advected<DIM, TURB>() * cs->mesh->nc : 0;
+  return (cs->view.rec_mom || cs->view.rec_sca) ? (long)n_advected<DIM, TURB>() * cs->mesh->nc : 0;
 }
 
 template <class T, int DIM, bool TURB>
@@ -671,9 +671,10 @@ __device__ __forceinline__ int advected_field(int a) {
   return a < DIM ? a : (a == DIM ? Layout<DIM, TURB>::K : Layout<DIM, TURB>::W);
 }
 
+// Km / Ks: the limiter constants of the momentum components / of k and omega (0: psi = 1).
 template <class T, int DIM, bool TURB>
-__global__ void __launch_bounds__(128) k_limiter(MeshView m, Src<T> st, const T* G, double K,
-                                                 T* psi) {
+__global__ void __launch_bounds__(128) k_limiter(MeshView m, Src<T> st, const T* G, double Km,
+                                                 double Ks, T* psi) {
   constexpr int NA = n_advected<DIM, TURB>();
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= m.nc) return;
@@ -681,6 +682,7 @@ __global__ void __launch_bounds__(128) k_limiter(MeshView m, Src<T> st, const T*
 #pragma unroll 1
   for (int a = 0; a < NA; ++a) {
     const int q = advected_field<DIM, TURB>(a);
+    const double K = a < DIM ? Km : Ks;
     T v;
     if (K > 0.0) {
       auto phi = [&](int cell) { return st((long)q * nc + cell); };
@@ -849,8 +851,9 @@ __device__ __forceinline__ void flux_face(const MeshView& m, const CaseView& cv,
 #pragma unroll
       for (int j = 0; j < DIM; ++j)
         cpn += G[((long)i * DIM + j) * nc + n] * tN[j] - G[((long)i * DIM + j) * nc + o] * tP[j];
-      const T up = out ? upwind_rec<T, DIM>(m, G, psi, i, i, f, o, uo)
-                       : upwind_rec<T, DIM>(m, G, psi, i, i, f, n, un);
+      const T* pm = cv.rec_mom ? psi : nullptr;
+      const T up = out ? upwind_rec<T, DIM>(m, G, pm, i, i, f, o, uo)
+                       : upwind_rec<T, DIM>(m, G, pm, i, i, f, n, un);
       wr(i, (pA * nrm[i] - cmo * cpn) + mdot * up);
       if constexpr (KEEP) {
         if (aux) aux[(long)(AX::CPN + i) * nf + f] = cpn;
@@ -871,8 +874,9 @@ __device__ __forceinline__ void flux_face(const MeshView& m, const CaseView& cv,
           cpn += G[((long)q * DIM + j) * nc + n] * tN[j] - G[((long)q * DIM + j) * nc + o] * tP[j];
         const T idn = 1.0 / (gv.dpn(m, f) * gn - go * gv.dnn(m, f));
         const T cs_ = go * gn * A * idn;
-        const T up = vout ? upwind_rec<T, DIM>(m, G, psi, DIM + s, q, f, o, phio)
-                          : upwind_rec<T, DIM>(m, G, psi, DIM + s, q, f, n, phin);
+        const T* ps = cv.rec_sca ? psi : nullptr;
+        const T up = vout ? upwind_rec<T, DIM>(m, G, ps, DIM + s, q, f, o, phio)
+                          : upwind_rec<T, DIM>(m, G, ps, DIM + s, q, f, n, phin);
         wr(q, vflux * up - cs_ * cpn);
         if constexpr (KEEP) {
           if (aux) {
@@ -928,7 +932,8 @@ __device__ __forceinline__ void flux_face(const MeshView& m, const CaseView& cv,
       T cp = G[((long)i * DIM) * nc + o] * tP[0];
 #pragma unroll
       for (int j = 1; j < DIM; ++j) cp += G[((long)i * DIM + j) * nc + o] * tP[j];
-      const T up = out ? upwind_rec<T, DIM>(m, G, psi, i, i, f, o, uo[i]) : bu[i];
+      const T up = out ? upwind_rec<T, DIM>(m, G, cv.rec_mom ? psi : nullptr, i, i, f, o, uo[i])
+                       : bu[i];
       wr(i, (pA * nrm[i] - gA * (bu[i] - uo[i] - cp)) + mdot * up);
     }
     wr(L::P, mdot);
@@ -947,7 +952,9 @@ __device__ __forceinline__ void flux_face(const MeshView& m, const CaseView& cv,
                               : bscalar(cv.wkind[f], cv.wval[f], phio, cp);
         T gface = go;
         if (s == 0 && cv.swall[f]) gface = (1.0 - wall_weight(par.nu, gv.wd(cv, o), phio)) * go;
-        const T up = vout ? upwind_rec<T, DIM>(m, G, psi, DIM + s, q, f, o, phio) : bphi;
+        const T up = vout ? upwind_rec<T, DIM>(m, G, cv.rec_sca ? psi : nullptr, DIM + s, q, f, o,
+                                               phio)
+                          : bphi;
         wr(q, vflux * up - gface * (A * gv.inv_dpn(m, f)) * (bphi - phio - cp));
       }
     }
@@ -1093,8 +1100,7 @@ int run(FvCase* cs, Src<T> st, Par<T> par, double* R, double* JV, cudaStream_t s
   k_dcoeff<T><<<bc, TB, 0, s>>>(m, w.acown, w.acnb, w.dco);
   const long npsi = psi_count<DIM, TURB>(cs);
   if (npsi)
-    k_limiter<T, DIM, TURB><<<bc, TB, 0, s>>>(m, st, w.G, cs->desc.advection == 2 ?
-                                              cs->desc.limiter_k : 0.0, w.psi);
+    k_limiter<T, DIM, TURB><<<bc, TB, 0, s>>>(m, st, w.G, cv.lim_km, cv.lim_ks, w.psi);
   // G, closure, Gwi, a_P, d and the slope limiters
   if (frozen) freeze<T>(w.G, (long)(w.psi + npsi - w.G), s);
   fv_prof_mark(cs, 4, s);
@@ -1181,8 +1187,8 @@ int run_vjp(FvCase* cs, const double* state, const double* W, double* R, double*
     a_flux<DIM, TURB, false, true><<<bc, TB, 0, s>>>(m, cv, st, par, G, cl, dco, fw.me, cs->aux, aw);
   else
     a_flux<DIM, TURB><<<bc, TB, 0, s>>>(m, cv, st, par, G, cl, dco, fw.me, cs->aux, aw);
-  if (lim && cs->desc.advection == 2) {
-    a_limiter<DIM, TURB><<<bc, TB, 0, s>>>(m, st, G, cs->desc.limiter_k, aw);
+  if (lim && (cv.lim_km > 0.0 || cv.lim_ks > 0.0)) {
+    a_limiter<DIM, TURB><<<bc, TB, 0, s>>>(m, st, G, cv.lim_km, cv.lim_ks, aw);
     a_limiter_gather<DIM, TURB><<<bc, TB, 0, s>>>(m, aw);
   }
   fv_prof_mark(cs, 8, s);

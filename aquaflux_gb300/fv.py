@@ -127,7 +127,7 @@ class FlowCase:
                  pressure_pin: int | None = None, pressure_pin_value: float = 0.0,
                  sst: dict | None = None, gradient: dict | None = None,
                  advection: dict | None = None, k_transform: str = "direct",
-                 omega_transform: str = "direct"):
+                 omega_transform: str = "direct", scalar_advection=None):
         self.dmesh = dmesh
         mesh = dmesh.mesh
         self.dim, self.n_cells = mesh.dim, mesh.n_cells
@@ -157,9 +157,21 @@ class FlowCase:
         transform = (k_transform == "log") | ((omega_transform == "log") << 1)
         if transform and sst is None:
             raise ValueError("the log transforms apply to the k and omega of a turbulent case")
+        # k / omega advection: None = the momentum scheme, "upwind", or a dict like `advection`
+        s_kind, s_k = 0, 0.0
+        if scalar_advection is not None:
+            if sst is None:
+                raise ValueError("scalar_advection applies to the k and omega of a turbulent case")
+            if scalar_advection == "upwind":
+                s_kind = 1
+            else:
+                s_kind = 2 if scalar_advection.get("k") is None else 3
+                s_k = 0.0 if scalar_advection.get("k") is None else float(scalar_advection["k"])
+        self.scalar_advection = scalar_advection
         desc = FvCaseDesc(1 if sst is not None else 0, mu_const, float(rho),
                           -1 if pressure_pin is None else int(pressure_pin),
-                          float(pressure_pin_value), sweeps, relax, adv_kind, adv_k, transform)
+                          float(pressure_pin_value), sweeps, relax, adv_kind, adv_k, transform,
+                          s_kind, s_k)
         h = ctypes.c_void_p()
         arrs = [np.ascontiguousarray(t.get(k)) if t.get(k) is not None else None
                 for k in ("flow_kind", "flow_vel", "flow_p", "k_kind", "k_val", "omega_kind",

@@ -57,6 +57,7 @@ class Workload:
     advection: dict | None = None
     k_transform: str = "direct"      # solved variable of k: "direct" or "log" (k = exp(w_k))
     omega_transform: str = "direct"  # ... of omega (LogScalars, omega = exp(w))
+    scalar_advection: object = None  # k / omega advection when not the momentum scheme
 
     @property
     def n_unknowns(self) -> int:
@@ -85,7 +86,8 @@ class Workload:
         return fv.FlowCase(dm, mu=self.mu, rho=self.rho, flow_bc=self.flow_bc,
                            pressure_pin=self.pressure_pin, sst=self.sst, gradient=self.gradient,
                            advection=self.advection, k_transform=self.k_transform,
-                           omega_transform=self.omega_transform)
+                           omega_transform=self.omega_transform,
+                           scalar_advection=self.scalar_advection)
 
 
 def cavity(n: int = 64, mu: float = 0.01, lid: float = 1.0) -> Workload:

@@ -104,6 +104,12 @@ typedef struct FvCaseDesc {
    * log omega is the log ratio log(omega / omega_wall) (LogRatioRow,
    * aquaflux/discretization/fixed_value.py:96-120).  Turbulent cases only. */
   int scalar_transform;
+  /* Advection scheme of k and omega when it differs from the momentum's (the reference builds
+   * SSTTurbulence with its own scheme, aquaflux/turbulence/transport.py:266-312): 0 = the momentum
+   * scheme above; 1 FirstOrderUpwind; 2 LimitedUpwind without a limiter; 3 LimitedUpwind with
+   * VenkatakrishnanLimiter(k = scalar_limiter_k).  Turbulent cases only. */
+  int scalar_advection;
+  double scalar_limiter_k;
 } FvCaseDesc;
 
 int fv_case_create(const FvMesh* mesh, const FvCaseDesc* desc,

@@ -327,7 +327,8 @@ def advection_flux(m: Metrics, phi, grad, mass_flux, bvals, scheme):
 
 # ----------------------------------------------------------------------------- the case
 def make_case(mesh, *, mu, rho, flow_bc, pressure_pin=None, pressure_pin_value=0.0, sst=None,
-              gradient=None, advection=None, transforms=("direct", "direct")):
+              gradient=None, advection=None, transforms=("direct", "direct"),
+              scalar_advection=None):
     """Flatten a case description into per-face tables.
 
     ``mesh``: object with ``nodes, fn_offsets, fn_indices, owner, neighbour, n_cells, patches``.
@@ -340,6 +341,9 @@ def make_case(mesh, *, mu, rho, flow_bc, pressure_pin=None, pressure_pin_value=0
     Venkatakrishnan limiter, ``K`` None for the unlimited reconstruction).
     ``transforms``: the solved variables of k and omega, ``"direct"`` or ``"log"`` (``DirectScalars``
     / ``LogScalars``, ``aquaflux/turbulence/coupled.py:111-207``).
+    ``scalar_advection``: the k / omega advection scheme when it is not the momentum's (the
+    reference builds ``SSTTurbulence`` with its own scheme): ``"upwind"`` or a dict like
+    ``advection``.
     """
     nf = len(mesh.owner)
     dim = mesh.nodes.shape[1]
@@ -357,7 +361,9 @@ def make_case(mesh, *, mu, rho, flow_bc, pressure_pin=None, pressure_pin_value=0
     case = {"mesh": mesh, "dim": dim, "mu": float(mu), "rho": float(rho), "bc_kind": kind,
             "bc_vel": vel, "bc_p": pb, "pin": pressure_pin, "pin_value": float(pressure_pin_value),
             "sst": None, "gradient": gradient, "advection": advection,
-            "transforms": tuple(transforms)}
+            "transforms": tuple(transforms),
+            "scalar_advection": advection if scalar_advection is None else
+            (None if scalar_advection == "upwind" else scalar_advection)}
     if sst is not None:
         sc = {"nu": float(sst["nu"])}
         for fld in ("k", "omega"):
@@ -741,8 +747,8 @@ class Oracle:
         face_gamma = gam_k[o]
         wfw = wall_function_weight(nu[ow], dist[ow], k[ow])
         face_gamma = face_gamma.index_copy(0, wf, (1.0 - wfw) * face_gamma[wf])
-        kflux = (torch.zeros_like(area) + advection_flux(m, k, grad_k, vflux, kb,
-                                                         case.get("advection"))) + \
+        sadv = case.get("scalar_advection", case.get("advection"))
+        kflux = (torch.zeros_like(area) + advection_flux(m, k, grad_k, vflux, kb, sadv)) + \
             diffusion_flux(m, k, grad_k, gam_k, kb, face_gamma)
         r_k = topo.scatter_conservative(kflux)
         prod = nut * strain ** 2
@@ -760,8 +766,7 @@ class Oracle:
         # omega equation, transport.py:655-718
         gam_w = nu + blend(f1, SIGMA_W1, SIGMA_W2) * nut
         wb = self._scalar_bvals(w, grad_w_rec, sst["omega_kind"], sst["omega_val"], geo)
-        wflux = (torch.zeros_like(area) + advection_flux(m, w, grad_w_rec, vflux, wb,
-                                                         case.get("advection"))) + \
+        wflux = (torch.zeros_like(area) + advection_flux(m, w, grad_w_rec, vflux, wb, sadv)) + \
             diffusion_flux(m, w, grad_w_rec, gam_w, wb)
         r_w = topo.scatter_conservative(wflux)
         alpha = blend(f1, ALPHA_1, ALPHA_2)

@@ -31,11 +31,11 @@ DUCT3_BC = {"left": ("inlet", (1.0, 0.0, 0.0)), "right": ("outlet", 0.0), "botto
             "top": ("wall",), "back": ("wall",), "front": ("wall",)}
 
 
-def sst_spec(dim, nu, k_in, w_in, walls):
+def sst_spec(dim, nu, k_in, w_in, walls, k_wall=("dirichlet", 0.0)):
     fb = {"left": ("inlet", (1.0,) + (0.0,) * (dim - 1)), "right": ("outlet", 0.0)}
     fb.update({w: ("wall",) for w in walls})
     kb = {"left": ("dirichlet", k_in), "right": ("zerograd",)}
-    kb.update({w: ("dirichlet", 0.0) for w in walls})
+    kb.update({w: tuple(k_wall) for w in walls})
     wb = {"left": ("dirichlet", w_in), "right": ("zerograd",)}
     wb.update({w: ("zerograd",) for w in walls})
     return fb, {"nu": nu, "walls": list(walls), "k": kb, "omega": wb}
@@ -68,6 +68,14 @@ SST = {
                   transforms=("direct", "log")),
     "bsst3": dict(prefix="bsst3_", dim=3, nu=1e-3, walls=["bottom", "top", "back", "front"],
                   file="logscalars", transforms=("log", "log")),
+    # the backward-step validation configuration: limited momentum, upwind k / omega, corrected
+    # gradients, zero-gradient k walls, log omega; and the reverse advection split
+    "psst2": dict(prefix="psst2_", dim=2, nu=2e-5, walls=["bottom", "top"], file="mixed",
+                  advection={"k": 5.0}, scalar_advection="upwind",
+                  gradient={"sweeps": 4, "relaxation": 1.0}, k_wall=("zerograd",),
+                  transforms=("direct", "log")),
+    "msst2": dict(prefix="msst2_", dim=2, nu=2e-5, walls=["bottom", "top"], file="mixed",
+                  scalar_advection={"k": 5.0}),
 }
 
 
@@ -87,9 +95,11 @@ def oracle_case(name: str):
     d = golden(spec.get("file", "sst"))
     mesh = mesh_from(d, spec["prefix"])
     k_in, w_in = d[spec["prefix"] + "inlet"]
-    fb, sst = sst_spec(spec["dim"], spec["nu"], float(k_in), float(w_in), spec["walls"])
+    fb, sst = sst_spec(spec["dim"], spec["nu"], float(k_in), float(w_in), spec["walls"],
+                       spec.get("k_wall", ("dirichlet", 0.0)))
     case = fo.make_case(mesh, mu=spec["nu"], rho=1.0, flow_bc=fb, sst=sst,
                         gradient=spec.get("gradient"), advection=spec.get("advection"),
+                        scalar_advection=spec.get("scalar_advection"),
                         transforms=spec.get("transforms", ("direct", "direct")))
     return case, d, spec["prefix"]
 
@@ -119,11 +129,13 @@ def device_case(name: str):
     else:
         spec = SST[name]
         k_in, w_in = d[p + "inlet"]
-        fb, sst = sst_spec(spec["dim"], spec["nu"], float(k_in), float(w_in), spec["walls"])
+        fb, sst = sst_spec(spec["dim"], spec["nu"], float(k_in), float(w_in), spec["walls"],
+                           spec.get("k_wall", ("dirichlet", 0.0)))
         k_tr, w_tr = spec.get("transforms", ("direct", "direct"))
         fc = fv.FlowCase(dm, mu=spec["nu"], rho=1.0, flow_bc=fb, sst=sst,
                          gradient=spec.get("gradient"), advection=spec.get("advection"),
-                         k_transform=k_tr, omega_transform=w_tr)
+                         k_transform=k_tr, omega_transform=w_tr,
+                         scalar_advection=spec.get("scalar_advection"))
     return fc, case, d, p
 
 
@@ -137,5 +149,5 @@ def workload_oracle_case(wl):
                "omega": wl.sst["omega"]}
     return fo.make_case(wl.mesh, mu=wl.mu, rho=wl.rho, flow_bc=wl.flow_bc,
                         pressure_pin=wl.pressure_pin, sst=sst, gradient=wl.gradient,
-                        advection=wl.advection,
+                        advection=wl.advection, scalar_advection=wl.scalar_advection,
                         transforms=(wl.k_transform, wl.omega_transform))

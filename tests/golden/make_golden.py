@@ -202,7 +202,8 @@ def laminar_cases():
 
 # --------------------------------------------------------------------------- k-omega SST
 def _rans(mesh, geom, dim, nu, u_in, walls, inlet="left", outlet="right", intensity=0.05,
-          length_scale=0.07, scheme=None, advection=None, k_transform=None, omega_transform=None):
+          length_scale=0.07, scheme=None, advection=None, k_transform=None, omega_transform=None,
+          scalar_advection=None, k_wall=None):
     scheme = scheme or CompactGreenGauss()
     advection = advection or FirstOrderUpwind()
     rho = 1.0
@@ -213,14 +214,14 @@ def _rans(mesh, geom, dim, nu, u_in, walls, inlet="left", outlet="right", intens
     flow_bc = {inlet: VelocityInlet(velocity=vel), outlet: PressureOutlet(pressure=0.0)}
     flow_bc.update({w: NoSlipWall() for w in walls})
     k_bc = {inlet: Dirichlet(k_in), outlet: ZeroGradient()}
-    k_bc.update({w: Dirichlet(0.0) for w in walls})
+    k_bc.update({w: (k_wall or Dirichlet(0.0)) for w in walls})
     w_bc = {inlet: Dirichlet(omega_in), outlet: ZeroGradient()}
     w_bc.update({w: ZeroGradient() for w in walls})
     momentum = MomentumContinuity.build(
         mesh, geom, PropertyModel({"viscosity": Constant(rho * nu), "density": Constant(rho)}),
         scheme, BoundaryConditions(flow_bc), advection_scheme=advection)
     turb = SSTTurbulence.build(
-        model, mesh, geom, scheme, advection, density=rho,
+        model, mesh, geom, scheme, scalar_advection or advection, density=rho,
         molecular_viscosity=jnp.full(mesh.n_cells, nu), wall_patches=list(walls),
         k_boundary=BoundaryConditions(k_bc), omega_boundary=BoundaryConditions(w_bc))
     return (CoupledRANS.build(momentum, turb, k_transform=k_transform,
@@ -326,6 +327,49 @@ def logscalar_cases():
         out[prefix + "residuals"] = np.stack([np.asarray(coupled.residual(jnp.asarray(s)))
                                               for s in states])
         v = rng.standard_normal((dim + 3) * n)
+        scale = np.abs(states[0]) + 1e-3
+        out[prefix + "jvp_dir"] = v * scale
+        out[prefix + "jvp_fd"] = _fd_jvp(coupled.residual, states[0], v * scale, 1e-7)
+    return out
+
+
+# --------------------------------------------------------------------------- mixed schemes
+def mixed_cases():
+    """Momentum and k / omega on different advection schemes (``SSTTurbulence.build`` takes its
+    own, ``aquaflux/turbulence/transport.py:266-312``): ``psst2_`` is the reference's backward-step
+    validation configuration (``validation/pitzdaily_openfoam/compare.py:483-600``) at fixture
+    size -- Venkatakrishnan-limited linear upwind momentum, first-order upwind k / omega, corrected
+    Green-Gauss (4 sweeps), zero-gradient k on the walls, log omega; ``msst2_`` the reverse
+    split (upwind momentum, limited scalars)."""
+    out = {}
+    rng = np.random.default_rng(53)
+    nx, ny = 12, 8
+    yn = graded_nodes(ny, 1.0, 1.2)
+    mesh = structured_grid_2d(nx, ny, lx=4.0, ly=1.0, named_boundaries=True, y_nodes=yn)
+    mesh = _with_nodes(mesh, jitter_interior_nodes(np.asarray(mesh.node_coords), (nx, ny),
+                                                   (4.0, 1.0), 0.1, 4))
+    geom = mesh.geometry()
+    lim = LimitedUpwind(limiter=VenkatakrishnanLimiter(k=5.0))
+    for prefix, kw, log_w in (
+            ("psst2_", dict(advection=lim, scalar_advection=FirstOrderUpwind(),
+                            scheme=_swept(4), k_wall=ZeroGradient()), True),
+            ("msst2_", dict(advection=FirstOrderUpwind(), scalar_advection=lim), False)):
+        coupled, turb, k_in, omega_in = _rans(mesh, geom, 2, 2e-5, 1.0, ["bottom", "top"],
+                                              omega_transform=LogScalars() if log_w else None,
+                                              **kw)
+        out.update(_mesh_arrays(prefix, mesh, geom))
+        out[prefix + "wall_distance"] = np.asarray(turb.wall_distance)
+        out[prefix + "wall_distance_gradient"] = np.asarray(turb.wall_distance_gradient)
+        out[prefix + "inlet"] = np.array([k_in, omega_in])
+        n = mesh.n_cells
+        states = _rans_states(rng, n, 2, k_in, omega_in, 2)
+        if log_w:
+            for x in states:
+                x[4 * n:] = np.log(x[4 * n:])
+        out[prefix + "states"] = np.stack(states)
+        out[prefix + "residuals"] = np.stack([np.asarray(coupled.residual(jnp.asarray(x)))
+                                              for x in states])
+        v = rng.standard_normal(5 * n)
         scale = np.abs(states[0]) + 1e-3
         out[prefix + "jvp_dir"] = v * scale
         out[prefix + "jvp_fd"] = _fd_jvp(coupled.residual, states[0], v * scale, 1e-7)
@@ -610,7 +654,8 @@ FILES = {"colouring": lambda: colouring_cases(), "meshes": lambda: mesh_cases(),
          "laminar": lambda: laminar_cases(), "sst": lambda: sst_cases(),
          "ilu0": lambda: ilu_cases(), "corrected": lambda: corrected_cases(),
          "operator": lambda: operator_cases(), "limited": lambda: limited_cases(),
-         "openfoam": lambda: openfoam_cases(), "logscalars": lambda: logscalar_cases()}
+         "openfoam": lambda: openfoam_cases(), "logscalars": lambda: logscalar_cases(),
+         "mixed": lambda: mixed_cases()}
 
 
 def main():

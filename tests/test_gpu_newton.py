@@ -151,7 +151,7 @@ def test_amg_vcycle_is_a_fixed_linear_operator_and_converges_newton(precision, f
 
 
 @pytest.mark.parametrize("name", ["cav8", "cavj", "lam3", "sst2", "sst3", "ccavj", "csst3", "lcavj",
-                                  "lsst2", "wsst2", "bsst3"])
+                                  "lsst2", "wsst2", "bsst3", "psst2", "msst2"])
 def test_assembled_jacobian_equals_the_coloured_probe(name):
     """The direct face assembly of J_direct gives the blocks the coloured probes of the frozen JVP
     give (materialize_block_jacobian, aquaflux/solve/sparse_jacobian.py:722-847), at the golden

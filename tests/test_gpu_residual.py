@@ -62,7 +62,7 @@ def test_jvp_matches_oracle(name):
 
 
 @pytest.mark.parametrize("name", ["cav8", "lam3", "sst2", "sst3", "ccavj", "csst2", "lcavj", "ucavj",
-                                  "lsst2", "wsst2", "bsst3"])
+                                  "lsst2", "wsst2", "bsst3", "psst2", "msst2"])
 def test_jvp_matches_reference_finite_differences(name):
     fc, case, d, p = device_case(name)
     s = d[p + "states"][1 if name == "cav8" else 0]
