@@ -133,6 +133,9 @@ class FlowCase:
         self.dim, self.n_cells = mesh.dim, mesh.n_cells
         self.turbulent = sst is not None
         t = case_tables(mesh, flow_bc, sst)
+        # SST wall cells: owners of the SST wall faces, whose omega rows are the fixation
+        self.wall_cells = (np.unique(mesh.owner[t["sst_wall"] != 0]).astype(np.int64)
+                           if sst is not None else np.zeros(0, dtype=np.int64))
         mu_arr = np.asarray(mu, dtype=np.float64)
         mu_field = None
         if mu_arr.ndim == 1:  # a per-cell viscosity field (laminar instances side by side)

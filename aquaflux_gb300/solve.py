@@ -455,7 +455,8 @@ class ContinuationResult:
     seconds: float
 
 
-def shift_basis(jac: BlockJacobian, velocity_only: bool = False) -> torch.Tensor:
+def shift_basis(jac: BlockJacobian, velocity_only: bool = False,
+                fixed_rows: torch.Tensor | None = None) -> torch.Tensor:
     """The base pseudo-time shift ``d`` (field-major): the magnitude of the frozen Jacobian's
     diagonal on the momentum rows (the momentum diagonal ``a_P``, ``LocalCourantBasis`` with weight
     1, ``aquaflux/solve/shift_basis.py:62-91``) and, unless ``velocity_only``, on the k / omega rows;
@@ -471,7 +472,68 @@ def shift_basis(jac: BlockJacobian, velocity_only: bool = False) -> torch.Tensor
     d[dim] = 0.0  # continuity
     if velocity_only:
         d[dim + 1:] = 0.0
-    return d.reshape(-1)
+    d = d.reshape(-1)
+    if fixed_rows is not None:  # algebraic rows (the near-wall omega fixation) take no shift
+        d[fixed_rows] = 0.0
+    return d
+
+
+def jacobian_diagonal(jac: BlockJacobian) -> torch.Tensor:
+    """The scalar diagonal of the last materialised Jacobian, field-major ``(b * n,)``."""
+    n, b = jac.n, jac.b
+    if not hasattr(jac, "_diag_blocks"):
+        rows = np.repeat(np.arange(n), np.diff(jac.indptr))
+        jac._diag_blocks = torch.tensor(np.flatnonzero(rows == jac.indices), device="cuda")
+    blocks = jac.values.view(-1, b, b)[jac._diag_blocks]
+    return torch.diagonal(blocks, dim1=1, dim2=2).t().reshape(-1)
+
+
+class RowScaledMeasure:
+    """The row-equilibrated, field-normalised progress measure of a coupled residual
+    (``RowScaledNorm`` / ``coupled_scaled_norm``, ``aquaflux/solve/norm.py:90-200``,
+    ``aquaflux/turbulence/coupled.py:1073-1168``), frozen at one state:
+    ``m(R) = || [ mean_c(|R_bc| / a_bc) / s_b ]_b ||_2`` over the field blocks ``b``.
+
+    Row scales ``a``: the row's own diagonal of the (solved-variable) Jacobian, so a near-wall
+    omega row written as a log ratio passes through with its unit derivative.  Field scales ``s``:
+    ``mean|u|`` for the velocity blocks, ``mean(phi / (dphi/dw))`` for k and omega (``mean|phi|``
+    when solved directly, exactly 1 for a log-solved field).  Continuity differs from the
+    reference, which divides the mass imbalance by the cell's mass throughput: here the row is
+    divided by its pressure diagonal and the block by the mean dynamic-plus-static pressure
+    magnitude ``mean|p| + rho mean|u|^2 / 2``, making it a fractional pressure change."""
+
+    def __init__(self, case, jac: BlockJacobian, state: torch.Tensor):
+        n, b, d = jac.n, jac.b, case.dim
+        tiny = 1e-300
+        self.n, self.b = n, b
+        self.row = jacobian_diagonal(jac).abs() + tiny
+        phys = case.to_physical(state) if case.turbulent else state
+        u = phys[: d * n]
+        umean = float(u.abs().mean())
+        p = phys[d * n:(d + 1) * n]
+        scales = [umean] * d + [float(p.abs().mean()) + 0.5 * case.rho * umean ** 2]
+        if case.turbulent:
+            for i, tr in enumerate((case.k_transform, case.omega_transform)):
+                blk = phys[(d + 1 + i) * n:(d + 2 + i) * n]
+                scales.append(1.0 if tr == "log" else float(blk.abs().mean()))
+        self.field = torch.tensor([max(x, tiny) for x in scales], dtype=torch.float64,
+                                  device="cuda")
+
+    def per_block(self, r: torch.Tensor) -> torch.Tensor:
+        return (r.abs() / self.row).view(self.b, self.n).mean(dim=1) / self.field
+
+    def __call__(self, r: torch.Tensor) -> float:
+        return float(torch.linalg.vector_norm(self.per_block(r)))
+
+
+def positive_projection(state: torch.Tensor, delta: torch.Tensor, start: int, stop: int,
+                        tau: float = 0.99, floor: float = 0.0) -> torch.Tensor:
+    """Clip each entry's own correction so ``state[start:stop]`` stays positive:
+    ``delta_i <- max(delta_i, -tau (phi_i + floor))`` (``positive_block_projection``,
+    ``aquaflux/solve/implicit.py:197-300``).  Inactive at a root (``delta = 0``)."""
+    out = delta.clone()
+    out[start:stop] = torch.maximum(delta[start:stop], -tau * (state[start:stop] + floor))
+    return out
 
 
 def pseudo_transient_solve(case, state0, *, beta0: float = 2.0, exponent: float = 1.0,
@@ -480,7 +542,10 @@ def pseudo_transient_solve(case, state0, *, beta0: float = 2.0, exponent: float 
                            rtol: float = 1e-10, atol: float = 1e-12, max_steps: int = 200,
                            linear_rtol: float = 1e-3, restart: int = 30, max_krylov: int = 300,
                            kind: str = "amg", precision: int = 32,
-                           velocity_only: bool = False) -> ContinuationResult:
+                           velocity_only: bool = False, measure: str = "euclidean",
+                           scaled_tol: float | None = None, k_positive: bool = False,
+                           k_floor: float = 0.0, backtrack: int = 0,
+                           log=None) -> ContinuationResult:
     """Pseudo-transient continuation (``PseudoTransientStep``, ``aquaflux/solve/continuation.py:
     333-735``): each step solves ``(J + beta d) delta = -R`` (the true JVP plus the shift,
     ``fv_jvp_shift``; right-preconditioned FGMRES with the preconditioner built at the same shifted
@@ -489,7 +554,17 @@ def pseudo_transient_solve(case, state0, *, beta0: float = 2.0, exponent: float 
     candidate is accepted unless it is non-finite or ``||R|| > divergence_cap ||R0||``; otherwise
     ``beta`` grows by ``escalation_factor`` and the step is re-solved (re-factoring the
     preconditioner at the new shift without re-materialising the Jacobian), up to
-    ``max_escalations`` times.  ``beta -> 0`` at the root recovers Newton's step."""
+    ``max_escalations`` times.  ``beta -> 0`` at the root recovers Newton's step.
+
+    ``measure="row_scaled"`` steers the schedule and the guard by :class:`RowScaledMeasure`
+    (rebuilt at every outer step from the Jacobian materialised there, held fixed across its
+    escalations), and stops when that measure falls to ``scaled_tol`` (or the Euclidean test
+    passes).  ``k_positive`` clips each k correction of a directly-solved k so k stays positive
+    (:func:`positive_projection` with ``k_floor``).  ``backtrack`` > 0 first halves a rejected step
+    up to that many times (a backtracking line search along the shifted Newton direction, as
+    ``backtracking_line_search`` does for the plain Newton step) before the shift escalates: on
+    a saddle-point system a larger momentum shift leaves continuity to the pressure alone and can
+    lengthen the step rather than damp it.  ``log`` receives one dict per attempt."""
     from .amg import AmgPreconditioner
 
     t_all = time.perf_counter()
@@ -504,26 +579,64 @@ def pseudo_transient_solve(case, state0, *, beta0: float = 2.0, exponent: float 
     norms = [float(torch.linalg.vector_norm(r))]
     r0 = norms[0]
     target = atol + rtol * r0
+    scaled = measure == "row_scaled"
+    if measure not in ("euclidean", "row_scaled"):
+        raise ValueError(f"measure must be 'euclidean' or 'row_scaled', got {measure!r}")
+    kpos = k_positive and case.turbulent and case.k_transform == "direct"
+    n, dim = case.n_cells, case.dim
+    fixed = None
+    if case.turbulent:  # the near-wall omega rows (FixedValueCells) are not shifted
+        fixed = torch.as_tensor((dim + 2) * n + case.wall_cells, device="cuda")
     betas, its = [], []
     escalations = 0
     step = 0
     converged = norms[0] <= target
+    m0 = m_cur = None
     while not converged and step < max_steps:
-        beta = max(beta_floor, beta0 * (norms[-1] / r0) ** exponent)
         pc.shift = zero
         pc.refresh(s)  # materialise J at s (its diagonal also gives the shift basis)
-        d = shift_basis(jac, velocity_only)
+        if scaled:
+            meas = RowScaledMeasure(case, jac, s)
+            m_cur = meas(r)
+            if m0 is None:
+                m0 = m_cur
+            ratio, cap_ref = m_cur / m0, m0
+        else:
+            meas = None
+            ratio, cap_ref = norms[-1] / r0, r0
+        if scaled and scaled_tol is not None and m_cur <= scaled_tol:
+            converged = True
+            break
+        beta = max(beta_floor, beta0 * ratio ** exponent)
+        d = shift_basis(jac, velocity_only, fixed)
         accepted = False
         for attempt in range(max_escalations + 1):
             shift = beta * d
             pc.reshift(shift)
             res = fgmres(lambda v: case.jvp_shift(s, v, shift), -r, pc.apply, rtol=linear_rtol,
                          restart=restart, maxiter=max_krylov)
-            cand = s + res.x
-            rc = case.residual(cand)
-            nc = float(torch.linalg.vector_norm(rc))
+            dx = res.x
+            if kpos:
+                dx = positive_projection(s, dx, (dim + 1) * n, (dim + 2) * n, floor=k_floor)
             its.append(res.iterations)
-            if math.isfinite(nc) and nc <= divergence_cap * r0:
+            alpha = 1.0
+            for _ in range(backtrack + 1):
+                cand = s + alpha * dx
+                rc = case.residual(cand)
+                nc = float(torch.linalg.vector_norm(rc))
+                mc = meas(rc) if scaled else nc
+                ok = math.isfinite(nc) and math.isfinite(mc) and mc <= divergence_cap * cap_ref
+                if backtrack:  # a line search asks for decrease, not only for no divergence
+                    ok = ok and mc < (m_cur if scaled else norms[-1])
+                if ok:
+                    break
+                alpha *= 0.5
+            if log is not None:
+                log({"step": step, "attempt": attempt, "beta": beta, "alpha": alpha, "norm": nc,
+                     "measure": mc if scaled else None, "accepted": ok,
+                     "krylov": res.iterations, "krylov_converged": res.converged,
+                     "blocks": meas.per_block(rc).tolist() if scaled else None})
+            if ok:
                 accepted = True
                 break
             beta *= escalation_factor

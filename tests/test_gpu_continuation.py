@@ -47,3 +47,55 @@ def test_pseudo_transient_converges_high_reynolds_cavity(kind):
         s = res.state
     a, b = ptc.state.cpu().numpy(), s.cpu().numpy()
     assert np.abs(a - b).max() <= 1e-7 * np.abs(b).max()
+
+
+def test_fixation_rows_take_no_shift_and_the_row_scaled_measure():
+    """The near-wall omega rows (FixedValueCells) are algebraic: no pseudo-time shift there
+    (coupled.py:1098-1110); the row-scaled measure passes a log-ratio row through with its unit
+    derivative and a log-solved field with field scale 1 (coupled_scaled_norm, coupled.py:1073)."""
+    import dataclasses
+
+    from aquaflux_gb300 import workloads
+    from aquaflux_gb300.solve import BlockJacobian, RowScaledMeasure, shift_basis
+
+    wl = dataclasses.replace(workloads.channel3d(6, nu=1e-2), omega_transform="log")
+    case = wl.device_case()
+    jac = BlockJacobian(case)
+    s = torch.tensor(case.to_solved(wl.initial_state(noise=0.02)), device="cuda")
+    jac.materialize(s)
+    n = jac.n
+    fixed = torch.as_tensor(5 * n + case.wall_cells, device="cuda")
+    d = shift_basis(jac, fixed_rows=fixed)
+    assert float(d[fixed].abs().max()) == 0.0
+    free = torch.ones(6 * n, dtype=torch.bool, device="cuda")
+    free[fixed] = False
+    free[3 * n:4 * n] = False  # continuity
+    assert float(d[free].min()) > 0.0
+    meas = RowScaledMeasure(case, jac, s)
+    assert torch.allclose(meas.row[fixed], torch.ones_like(meas.row[fixed]), rtol=1e-12)
+    assert float(meas.field[5]) == 1.0  # log omega: a change of log omega is already relative
+    r = case.residual(s)
+    blocks = meas.per_block(r)
+    assert abs(float(torch.linalg.vector_norm(blocks)) - meas(r)) <= 1e-12 * meas(r)
+    manual = (r.abs() / meas.row).view(6, n).mean(dim=1) / meas.field
+    assert torch.allclose(blocks, manual)
+
+
+def test_row_scaled_march_with_backtracking_reaches_the_newton_root():
+    """The SST channel from a cold start, steered by the row-scaled measure with k kept positive
+    and backtracking before escalation, lands on the root plain Newton finds."""
+    import dataclasses
+
+    from aquaflux_gb300 import workloads
+    from aquaflux_gb300.solve import newton_solve, pseudo_transient_solve
+
+    wl = dataclasses.replace(workloads.channel3d(8, nu=2e-3), omega_transform="log")
+    case = wl.device_case()
+    s0 = case.to_solved(wl.initial_state())
+    ptc = pseudo_transient_solve(case, s0, kind="amg", precision=64, max_steps=120,
+                                 measure="row_scaled", k_positive=True, backtrack=4)
+    assert ptc.converged
+    ref = newton_solve(case, s0, precision=64, max_steps=60)
+    assert ref.converged
+    a, b = ptc.state.cpu().numpy(), ref.state.cpu().numpy()
+    assert np.abs(a - b).max() <= 1e-7 * np.abs(b).max()
