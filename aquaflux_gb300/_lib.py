@@ -59,6 +59,8 @@ SIGNATURES = {
     "fv_segment_dot": (c_int, [c_int, P, c_int, c_int, P, P, P, P]),
     "fv_face_functional": (c_int, [P, P, P, c_int, P, P, P, P, P]),
     "fv_assemble_jacobian": (c_int, [P, P, P, P, P, P]),
+    "fv_assemble_jacobian_f32": (c_int, [P, P, P, P, P, P]),
+    "fv_jvp_f32": (c_int, [P, P, P, P, P]),
     "fv_param_jvp": (c_int, [P, P, P, P, P]),
     "fv_vjp": (c_int, [P, P, P, P, P, P]),
     "fv_param_vjp": (c_int, [P, P, P, P, P]),

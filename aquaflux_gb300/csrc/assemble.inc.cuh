@@ -14,27 +14,32 @@
 // Every entry is the tangent the coloured probe computes for it, by the same arithmetic in the
 // same order.
 
-// The state with a unit tangent on one unknown (index `seed` of the field-major state).
+// The state with a unit tangent on one unknown (index `seed` of the field-major state); T = Dual,
+// or DualF for the fp32 assembly of an fp32 preconditioner.
+template <class T>
 struct SeedSrc {
   const double* v;
   long seed;
-  __device__ __forceinline__ Dual operator()(long i) const { return {v[i], i == seed ? 1.0 : 0.0}; }
+  __device__ __forceinline__ T operator()(long i) const {
+    return T{(decltype(T::v))v[i], (decltype(T::v))(i == seed ? 1 : 0)};
+  }
 };
 
 // Keeps the tangent of flux q as D[((side * NF + q) * NF + r) * nf + f].
+template <class T>
 struct DerivStore {
   double* D;
   long base;  // ((side * NF) * NF + r) * nf + f
   long qstride;  // NF * nf
-  __device__ __forceinline__ void operator()(int q, const Dual& x) const {
+  __device__ __forceinline__ void operator()(int q, const T& x) const {
     D[base + q * qstride] = x.d;
   }
 };
 
-template <int DIM, bool TURB>
+template <class T, int DIM, bool TURB>
 __global__ void __launch_bounds__(128) k_jac_face(MeshView m, CaseView cv, const double* state,
-                                                  Par<Dual> par, const Dual* G, const Dual* cl,
-                                                  const Dual* dco, const Dual* psi, double* D) {
+                                                  Par<T> par, const T* G, const T* cl,
+                                                  const T* dco, const T* psi, double* D) {
   constexpr int NF = Layout<DIM, TURB>::NFLD;
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= m.nf) return;
@@ -44,18 +49,18 @@ __global__ void __launch_bounds__(128) k_jac_face(MeshView m, CaseView cv, const
     const int cell = side ? m.nb[f] : m.owner[f];
 #pragma unroll 1
     for (int r = 0; r < NF; ++r) {
-      const SeedSrc st{state, (long)r * nc + cell};
-      const DerivStore wr{D, ((long)(side * NF) * NF + r) * nf + f, (long)NF * nf};
-      flux_face<Dual, DIM, TURB>(m, cv, st, par, G, cl, dco, (const Dual*)nullptr, psi, true, f,
-                                 wr, nullptr);
+      const SeedSrc<T> st{state, (long)r * nc + cell};
+      const DerivStore<T> wr{D, ((long)(side * NF) * NF + r) * nf + f, (long)NF * nf};
+      flux_face<T, DIM, TURB>(m, cv, st, par, G, cl, dco, (const T*)nullptr, psi, true, f, wr,
+                              nullptr);
     }
   }
 }
 
-template <int DIM, bool TURB>
+template <class T, int DIM, bool TURB>
 __global__ void __launch_bounds__(128) k_jac_cell(MeshView m, CaseView cv, const double* state,
-                                                  Par<Dual> par, const Dual* G, const Dual* cl,
-                                                  const Dual* Gwi, const double* D,
+                                                  Par<T> par, const T* G, const T* cl,
+                                                  const T* Gwi, const double* D,
                                                   const int* indptr, const int* indices,
                                                   double* values) {
   using L = Layout<DIM, TURB>;
@@ -114,9 +119,10 @@ __global__ void __launch_bounds__(128) k_jac_cell(MeshView m, CaseView cv, const
       // only k and omega of the cell itself enter its source rows
 #pragma unroll
       for (int r = L::K; r <= L::W; ++r) {
-        const SeedSrc st{state, (long)r * nc + c};
-        Dual rk{0.0, q == L::K ? dg[r] : 0.0}, rw{0.0, q == L::W ? dg[r] : 0.0};
-        sst_rows<Dual, DIM>(m, cv, st, par, cl, G, Gwi, c, rk, rw);
+        using S = decltype(T::v);
+        const SeedSrc<T> st{state, (long)r * nc + c};
+        T rk{S(0), S(q == L::K ? dg[r] : 0.0)}, rw{S(0), S(q == L::W ? dg[r] : 0.0)};
+        sst_rows<T, DIM>(m, cv, st, par, cl, G, Gwi, c, rk, rw);
         dg[r] = q == L::K ? rk.d : rw.d;
       }
     }
@@ -130,29 +136,30 @@ __global__ void __launch_bounds__(128) k_jac_cell(MeshView m, CaseView cv, const
     }
 }
 
-template <int DIM, bool TURB>
+template <class T, int DIM, bool TURB>
 int assemble_frozen(FvCase* cs, const double* state, const int* indptr, const int* indices,
                     double* values, double* D, cudaStream_t s) {
+  using S = decltype(T::v);
   const MeshView& m = cs->mesh->view;
   const CaseView& cv = cs->view;
   const long nc = m.nc, nf = m.nf;
   constexpr int NF = Layout<DIM, TURB>::NFLD;
-  Work<Dual> w = work_layout<Dual, DIM, TURB>(cs->work, nc, nf, psi_count<DIM, TURB>(cs));
-  Src<Dual> st{state, nullptr};  // zero tangent: the forward stages give the frozen values
+  Work<T> w = work_layout<T, DIM, TURB>(cs->work, nc, nf, psi_count<DIM, TURB>(cs));
+  Src<T> st{state, nullptr};  // zero tangent: the forward stages give the frozen values
   const double irho = 1.0 / cs->desc.rho;
-  Par<Dual> par{{cs->mu, 0.0}, {cs->inlet_scale, 0.0}, {cs->mu * irho, 0.0}};
+  Par<T> par{{S(cs->mu), S(0)}, {S(cs->inlet_scale), S(0)}, {S(cs->mu * irho), S(0)}};
   constexpr int TB = 128;
   const int bc = fv_blocks(nc, TB), bf = fv_blocks(nf, TB);
-  gradient_stage<Dual, DIM, TURB>(cs, st, par, w, s);
-  if (TURB) k_closure<Dual, DIM><<<bc, TB, 0, s>>>(m, cv, st, par, w.G, w.cl, w.Gwi);
-  k_apcoef<Dual, DIM, TURB><<<bf, TB, 0, s>>>(m, cv, st, par, w.G, w.cl, w.acown, w.acnb, w.me);
-  k_dcoeff<Dual><<<bc, TB, 0, s>>>(m, w.acown, w.acnb, w.dco);
+  gradient_stage<T, DIM, TURB>(cs, st, par, w, s);
+  if (TURB) k_closure<T, DIM><<<bc, TB, 0, s>>>(m, cv, st, par, w.G, w.cl, w.Gwi);
+  k_apcoef<T, DIM, TURB><<<bf, TB, 0, s>>>(m, cv, st, par, w.G, w.cl, w.acown, w.acnb, w.me);
+  k_dcoeff<T><<<bc, TB, 0, s>>>(m, w.acown, w.acnb, w.dco);
   const long npsi = psi_count<DIM, TURB>(cs);
   if (npsi)
-    k_limiter<Dual, DIM, TURB><<<bc, TB, 0, s>>>(m, st, w.G, cv.lim_km, cv.lim_ks, w.psi);
-  k_jac_face<DIM, TURB><<<bf, TB, 0, s>>>(m, cv, state, par, w.G, w.cl, w.dco,
-                                          npsi ? w.psi : nullptr, D);
-  k_jac_cell<DIM, TURB><<<fv_blocks((long)NF * nc, TB), TB, 0, s>>>(
+    k_limiter<T, DIM, TURB><<<bc, TB, 0, s>>>(m, st, w.G, cv.lim_km, cv.lim_ks, w.psi);
+  k_jac_face<T, DIM, TURB><<<bf, TB, 0, s>>>(m, cv, state, par, w.G, w.cl, w.dco,
+                                             npsi ? w.psi : nullptr, D);
+  k_jac_cell<T, DIM, TURB><<<fv_blocks((long)NF * nc, TB), TB, 0, s>>>(
       m, cv, state, par, w.G, w.cl, w.Gwi, D, indptr, indices, values);
   FV_CUDA_TRY(cudaGetLastError());
   return FV_OK;

@@ -476,8 +476,9 @@ extern "C" int fv_probe_jacobian(FvCase* c, const double* state, int frozen, con
   return FV_OK;
 }
 
-extern "C" int fv_assemble_jacobian(FvCase* c, const double* state, const int* indptr,
-                                    const int* indices, double* values, void* stream) {
+namespace {
+int assemble_jacobian(FvCase* c, const double* state, const int* indptr, const int* indices,
+                      double* values, int fp32, void* stream) {
   if (!c || !state || !indptr || !indices || !values) {
     fv_set_error("fv_assemble_jacobian: bad arguments");
     return FV_ERR_ARG;
@@ -488,7 +489,7 @@ extern "C" int fv_assemble_jacobian(FvCase* c, const double* state, const int* i
   }
   cudaStream_t s = (cudaStream_t)stream;
   int rc = fv_case_assemble_frozen(c, physical_state(c, state, s), indptr, indices, values,
-                                   c->jac_face, s);
+                                   c->jac_face, fp32, s);
   if (rc == FV_OK && c->desc.scalar_transform) {
     k_chain_bsr<<<fv_blocks((long)c->nfld * c->mesh->nc, 128), 128, 0, s>>>(
         c->mesh->nc, c->nfld, c->mesh->dim + 1, c->desc.scalar_transform, indptr, indices,
@@ -496,6 +497,28 @@ extern "C" int fv_assemble_jacobian(FvCase* c, const double* state, const int* i
     FV_CUDA_TRY(cudaGetLastError());
   }
   return rc;
+}
+}  // namespace
+
+extern "C" int fv_assemble_jacobian(FvCase* c, const double* state, const int* indptr,
+                                    const int* indices, double* values, void* stream) {
+  return assemble_jacobian(c, state, indptr, indices, values, 0, stream);
+}
+
+extern "C" int fv_assemble_jacobian_f32(FvCase* c, const double* state, const int* indptr,
+                                        const int* indices, double* values, void* stream) {
+  return assemble_jacobian(c, state, indptr, indices, values, 1, stream);
+}
+
+extern "C" int fv_jvp_f32(FvCase* c, const double* state, const double* v, double* jv,
+                          void* stream) {
+  if (!c || !state || !v || !jv) {
+    fv_set_error("fv_jvp_f32: bad arguments");
+    return FV_ERR_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  state = physical_state(c, state, s);
+  return fv_case_run(c, state, physical_tangent(c, v, s), FV_TAN_STATE32, nullptr, jv, s);
 }
 
 extern "C" int fv_jvp_batch(FvCase* c, const double* state, const double* v, int k, double* jv,

@@ -97,6 +97,75 @@ FV_HD Dual fv_tanh(Dual x) {
 FV_HD double fv_log(double x) { return log(x); }
 FV_HD Dual fv_log(Dual x) { return {log(x.v), x.d / x.v}; }
 
+// ------------------------------------------------------------------------------------------------
+// Single-precision dual number.  The same templates evaluated with ``DualF`` give the residual's
+// directional derivative in fp32 arithmetic: GB300 has ~64x the fp32 throughput of its fp64 pipe,
+// and the preconditioner's Jacobian (and the Krylov operator of a mixed-precision Newton, whose
+// defect stays fp64) needs no more than fp32 accuracy.  Double operands are rounded to float at
+// the operation; the JAX tie rule of max / min is kept.
+// ------------------------------------------------------------------------------------------------
+struct DualF {
+  float v, d;
+};
+
+FV_HD float val(const DualF& x) { return x.v; }
+FV_HD DualF operator+(DualF a, DualF b) { return {a.v + b.v, a.d + b.d}; }
+FV_HD DualF operator-(DualF a, DualF b) { return {a.v - b.v, a.d - b.d}; }
+FV_HD DualF operator*(DualF a, DualF b) { return {a.v * b.v, a.d * b.v + a.v * b.d}; }
+FV_HD DualF operator/(DualF a, DualF b) {
+  const float r = 1.0f / b.v;
+  const float q = a.v * r;
+  return {q, (a.d - q * b.d) * r};
+}
+FV_HD DualF operator-(DualF a) { return {-a.v, -a.d}; }
+FV_HD DualF operator+(DualF a, double b) { return {a.v + (float)b, a.d}; }
+FV_HD DualF operator+(double a, DualF b) { return {(float)a + b.v, b.d}; }
+FV_HD DualF operator-(DualF a, double b) { return {a.v - (float)b, a.d}; }
+FV_HD DualF operator-(double a, DualF b) { return {(float)a - b.v, -b.d}; }
+FV_HD DualF operator*(DualF a, double b) { return {a.v * (float)b, a.d * (float)b}; }
+FV_HD DualF operator*(double a, DualF b) { return {(float)a * b.v, (float)a * b.d}; }
+FV_HD DualF operator/(DualF a, double b) {
+  const float r = 1.0f / (float)b;
+  return {a.v * r, a.d * r};
+}
+FV_HD DualF operator/(double a, DualF b) {
+  const float r = 1.0f / b.v;
+  const float q = (float)a * r;
+  return {q, -q * b.d * r};
+}
+FV_HD DualF& operator+=(DualF& a, DualF b) { a = a + b; return a; }
+FV_HD DualF& operator-=(DualF& a, DualF b) { a = a - b; return a; }
+FV_HD DualF lerp(DualF a, DualF b, double g) {
+  const float gf = (float)g;
+  return {fmaf(gf, b.v - a.v, a.v), fmaf(gf, b.d - a.d, a.d)};
+}
+FV_HD DualF lerp(DualF a, DualF b, DualF g) {
+  return {fmaf(g.v, b.v - a.v, a.v), fmaf(g.v, b.d - a.d, a.d) + g.d * (b.v - a.v)};
+}
+FV_HD DualF cst(double x, DualF) { return {(float)x, 0.0f}; }
+FV_HD DualF fv_max(DualF a, DualF b) {
+  if (a.v > b.v) return a;
+  if (a.v < b.v) return b;
+  return {a.v, 0.5f * (a.d + b.d)};
+}
+FV_HD DualF fv_min(DualF a, DualF b) {
+  if (a.v < b.v) return a;
+  if (a.v > b.v) return b;
+  return {a.v, 0.5f * (a.d + b.d)};
+}
+FV_HD DualF fv_max(DualF a, double b) { return fv_max(a, DualF{(float)b, 0.0f}); }
+FV_HD DualF fv_min(DualF a, double b) { return fv_min(a, DualF{(float)b, 0.0f}); }
+FV_HD DualF fv_abs(DualF x) { return {fabsf(x.v), x.v > 0.0f ? x.d : (x.v < 0.0f ? -x.d : 0.0f)}; }
+FV_HD DualF fv_sqrt(DualF x) {
+  const float s = sqrtf(x.v);
+  return {s, 0.5f * x.d / s};
+}
+FV_HD DualF fv_tanh(DualF x) {
+  const float t = tanhf(x.v);
+  return {t, (1.0f - t * t) * x.d};
+}
+FV_HD DualF fv_log(DualF x) { return {logf(x.v), x.d / x.v}; }
+
 // sqrt with the reference's guard (``aquaflux/turbulence/strain.py:32-43``): 0 (and a zero
 // tangent) for a non-positive argument.
 template <class T>

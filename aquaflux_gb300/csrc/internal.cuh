@@ -167,9 +167,10 @@ int fv_case_face_functional(FvCase* c, const double* state, const double* weight
                             int viscous_only, double* value, double* dstate, double* dparams,
                             double* dnodes, cudaStream_t s);
 int fv_case_assemble_frozen(FvCase* c, const double* state, const int* indptr, const int* indices,
-                            double* values, double* D, cudaStream_t s);
+                            double* values, double* D, int fp32, cudaStream_t s);
 size_t fv_jac_face_bytes(int dim, int turb, long nf);
-enum { FV_TAN_NONE = 0, FV_TAN_STATE = 1, FV_TAN_MU = 2, FV_TAN_INLET = 3, FV_TAN_FROZEN = 4 };
+enum { FV_TAN_NONE = 0, FV_TAN_STATE = 1, FV_TAN_MU = 2, FV_TAN_INLET = 3, FV_TAN_FROZEN = 4,
+       FV_TAN_STATE32 = 5, FV_TAN_FROZEN32 = 6 };  // 32: the tangent pass in fp32 (DualF)
 
 // Wall distance + gradient for a turbulent case (mesh.cu).
 int fv_wall_distance_compute(FvMesh* m, const unsigned char* swall_dev, int n_wall_faces,

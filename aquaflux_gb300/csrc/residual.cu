@@ -53,6 +53,14 @@ struct Src<Dual> {
   const double* t;  // may be null: zero tangent
   __device__ __forceinline__ Dual operator()(long i) const { return {v[i], t ? t[i] : 0.0}; }
 };
+template <>
+struct Src<DualF> {
+  const double* v;
+  const double* t;  // may be null: zero tangent
+  __device__ __forceinline__ DualF operator()(long i) const {
+    return {(float)v[i], t ? (float)t[i] : 0.0f};
+  }
+};
 
 template <class T>
 struct Par {
@@ -69,6 +77,11 @@ __device__ __forceinline__ void put<double>(double* r, double*, long i, const do
 }
 template <>
 __device__ __forceinline__ void put<Dual>(double* r, double* t, long i, const Dual& x) {
+  if (r) r[i] = x.v;
+  t[i] = x.d;
+}
+template <>
+__device__ __forceinline__ void put<DualF>(double* r, double* t, long i, const DualF& x) {
   if (r) r[i] = x.v;
   t[i] = x.d;
 }
@@ -594,6 +607,9 @@ __device__ __forceinline__ double mu_at(const Par<double>& par, const CaseView& 
 __device__ __forceinline__ Dual mu_at(const Par<Dual>& par, const CaseView& cv, int c) {
   return cv.mu_cell ? Dual{cv.mu_cell[c], par.mu.d} : par.mu;
 }
+__device__ __forceinline__ DualF mu_at(const Par<DualF>& par, const CaseView& cv, int c) {
+  return cv.mu_cell ? DualF{(float)cv.mu_cell[c], par.mu.d} : par.mu;
+}
 template <class T, bool TURB>
 __device__ __forceinline__ T mu_eff(const Par<T>& par, const CaseView& cv, double rho, const T* cl,
                                     int nc, int c) {
@@ -1060,6 +1076,14 @@ template <>
 void freeze<Dual>(Dual* x, long n, cudaStream_t s) {
   k_freeze<<<fv_blocks(n, 256), 256, 0, s>>>(n, x);
 }
+__global__ void k_freeze_f(long n, DualF* x) {
+  long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) x[i].d = 0.0f;
+}
+template <>
+void freeze<DualF>(DualF* x, long n, cudaStream_t s) {
+  k_freeze_f<<<fv_blocks(n, 256), 256, 0, s>>>(n, x);
+}
 
 // Every field's gradient with the case's scheme, into w.G.
 template <class T, int DIM, bool TURB>
@@ -1121,6 +1145,12 @@ int dispatch_t(FvCase* cs, const double* state, const double* tangent, int kind,
   if (kind == FV_TAN_NONE) {
     return run<double, DIM, TURB>(
         cs, Src<double>{state}, Par<double>{cs->mu, cs->inlet_scale, cs->mu * irho}, R, nullptr, s);
+  }
+  if (kind == FV_TAN_STATE32 || kind == FV_TAN_FROZEN32) {
+    Par<DualF> pf{{(float)cs->mu, 0.0f}, {(float)cs->inlet_scale, 0.0f},
+                  {(float)(cs->mu * irho), 0.0f}};
+    return run<DualF, DIM, TURB>(cs, Src<DualF>{state, tangent}, pf, R, JV, s,
+                                 kind == FV_TAN_FROZEN32);
   }
   const double dmu = kind == FV_TAN_MU ? 1.0 : 0.0;
   Par<Dual> par{{cs->mu, dmu}, {cs->inlet_scale, kind == FV_TAN_INLET ? 1.0 : 0.0},
@@ -1252,14 +1282,19 @@ size_t fv_jac_face_bytes(int dim, int turb, long nf) {
 }
 
 int fv_case_assemble_frozen(FvCase* cs, const double* state, const int* indptr,
-                            const int* indices, double* values, double* D, cudaStream_t s) {
+                            const int* indices, double* values, double* D, int fp32,
+                            cudaStream_t s) {
   const int dim = cs->mesh->dim;
   const bool turb = cs->desc.turbulent != 0;
-  if (dim == 2)
-    return turb ? assemble_frozen<2, true>(cs, state, indptr, indices, values, D, s)
-                : assemble_frozen<2, false>(cs, state, indptr, indices, values, D, s);
-  return turb ? assemble_frozen<3, true>(cs, state, indptr, indices, values, D, s)
-              : assemble_frozen<3, false>(cs, state, indptr, indices, values, D, s);
+  auto go = [&](auto t) {
+    using T = decltype(t);
+    if (dim == 2)
+      return turb ? assemble_frozen<T, 2, true>(cs, state, indptr, indices, values, D, s)
+                  : assemble_frozen<T, 2, false>(cs, state, indptr, indices, values, D, s);
+    return turb ? assemble_frozen<T, 3, true>(cs, state, indptr, indices, values, D, s)
+                : assemble_frozen<T, 3, false>(cs, state, indptr, indices, values, D, s);
+  };
+  return fp32 ? go(DualF{}) : go(Dual{});
 }
 
 int fv_gg_sweeps_scalar(const MeshView& m, int sweeps, double rel, const double* num, double* x0,

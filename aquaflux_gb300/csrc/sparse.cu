@@ -566,6 +566,8 @@ struct FvIlu0 {
   void* work = nullptr;                      // (n * b) vector the captured sweeps run on
   cudaGraphExec_t apply_exec[2] = {nullptr, nullptr};  // forward / transposed solve
   cudaGraphExec_t factor_exec = nullptr;
+  // host copy of the pattern: the transposed-solve structures are built on first use
+  std::vector<int> h_ptr, h_idx, h_diag;
 };
 
 namespace {
@@ -708,11 +710,41 @@ int ilu_factor(FvIlu0* f, cudaStream_t s) {
   return FV_OK;
 }
 
+int upload(const std::vector<int>& h, int** d, cudaStream_t s);
+
+// The transposed-solve structures (the pattern's transpose and the level sets of U^T and L^T),
+// built the first time a transposed solve is asked for.
+int ensure_transpose(FvIlu0* f, cudaStream_t s) {
+  if (f->tptr) return FV_OK;
+  const int n = f->n;
+  Transpose T;
+  build_transpose(n, n, f->h_ptr.data(), f->h_idx.data(), &T);
+  std::vector<int> rows;
+  levels(n, true, [&](int i, auto&& use) {  // U^T: column i depends on rows j < i with (j, i)
+    for (int q = T.ptr[i]; q < T.ptr[i + 1]; ++q)
+      if (T.idx[q] < i) use(T.idx[q]);
+  }, &rows, &f->lv_tfwd);
+  if (upload(rows, &f->rows_tfwd, s)) return FV_ERR_CUDA;
+  levels(n, false, [&](int i, auto&& use) {  // L^T: column i depends on rows k > i with (k, i)
+    for (int q = T.ptr[i]; q < T.ptr[i + 1]; ++q)
+      if (T.idx[q] > i) use(T.idx[q]);
+  }, &rows, &f->lv_tbwd);
+  if (upload(rows, &f->rows_tbwd, s)) return FV_ERR_CUDA;
+  if (upload(T.ptr, &f->tptr, s) || upload(T.idx, &f->tidx, s) || upload(T.blk, &f->tblk, s))
+    return FV_ERR_CUDA;
+  FV_CUDA_TRY(cudaStreamSynchronize(s));
+  return FV_OK;
+}
+
 template <class V>
 int ilu_apply(FvIlu0* f, const V* r, V* x, int transpose, cudaStream_t s) {
   const long n = (long)f->n * f->b;
   V* w = (V*)f->work;
   const int t = transpose ? 1 : 0;
+  if (t) {
+    int rc = ensure_transpose(f, s);
+    if (rc != FV_OK) return rc;
+  }
   if (!f->apply_exec[t]) {
     int rc = capture([&](cudaStream_t cs) { launch_apply_levels<V>(f, t, w, cs); },
                      &f->apply_exec[t]);
@@ -773,8 +805,6 @@ extern "C" int fv_ilu0_create(int n, int b, const int* indptr, const int* indice
   f->b = b;
   f->nnzb = nnzb;
   f->precision = precision;
-  Transpose T;
-  build_transpose(n, n, indptr, indices, &T);
   std::vector<int> rows;
   levels(n, true, [&](int i, auto&& use) {
     for (int q = indptr[i]; q < diag[i]; ++q) use(indices[q]);
@@ -784,19 +814,10 @@ extern "C" int fv_ilu0_create(int n, int b, const int* indptr, const int* indice
     for (int q = diag[i] + 1; q < indptr[i + 1]; ++q) use(indices[q]);
   }, &rows, &f->lv_bwd);
   if (upload(rows, &f->rows_bwd, s)) return FV_ERR_CUDA;
-  levels(n, true, [&](int i, auto&& use) {  // U^T: column i depends on rows j < i with (j, i)
-    for (int q = T.ptr[i]; q < T.ptr[i + 1]; ++q)
-      if (T.idx[q] < i) use(T.idx[q]);
-  }, &rows, &f->lv_tfwd);
-  if (upload(rows, &f->rows_tfwd, s)) return FV_ERR_CUDA;
-  levels(n, false, [&](int i, auto&& use) {  // L^T: column i depends on rows k > i with (k, i)
-    for (int q = T.ptr[i]; q < T.ptr[i + 1]; ++q)
-      if (T.idx[q] > i) use(T.idx[q]);
-  }, &rows, &f->lv_tbwd);
-  if (upload(rows, &f->rows_tbwd, s)) return FV_ERR_CUDA;
-  std::vector<int> hp(indptr, indptr + n + 1), hi(indices, indices + nnzb);
-  if (upload(hp, &f->ptr, s) || upload(hi, &f->idx, s) || upload(diag, &f->diag, s) ||
-      upload(T.ptr, &f->tptr, s) || upload(T.idx, &f->tidx, s) || upload(T.blk, &f->tblk, s))
+  f->h_ptr.assign(indptr, indptr + n + 1);
+  f->h_idx.assign(indices, indices + nnzb);
+  f->h_diag = diag;
+  if (upload(f->h_ptr, &f->ptr, s) || upload(f->h_idx, &f->idx, s) || upload(diag, &f->diag, s))
     return FV_ERR_CUDA;
   size_t vs = precision == 64 ? sizeof(double) : sizeof(float);
   FV_CUDA_TRY(cudaMalloc(&f->val, vs * (size_t)nnzb * b * b));

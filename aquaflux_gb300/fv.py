@@ -235,9 +235,18 @@ class FlowCase:
         check(lib().fv_residual(self._h, ptr(s), ptr(r), _stream()))
         return r
 
-    def jvp(self, state, v, *, return_residual: bool = False):
+    def jvp(self, state, v, *, return_residual: bool = False, precision: int = 64):
+        """``J v``; ``precision=32`` evaluates the tangent pass in fp32 arithmetic
+        (``fv_jvp_f32``: ~1e-6 relative, for the Krylov operator of a mixed-precision Newton)."""
         s, vv = self._vec(state), self._vec(v)
         jv = torch.empty_like(s)
+        if precision == 32:
+            if return_residual:
+                raise ValueError("the fp32 JVP returns no residual")
+            check(lib().fv_jvp_f32(self._h, ptr(s), ptr(vv), ptr(jv), _stream()))
+            return jv
+        if precision != 64:
+            raise ValueError(f"precision must be 64 or 32, got {precision}")
         r = torch.empty_like(s) if return_residual else None
         check(lib().fv_jvp(self._h, ptr(s), ptr(vv), ptr(r), ptr(jv), _stream()))
         return (r, jv) if return_residual else jv

@@ -172,6 +172,13 @@ int fv_probe_jacobian(FvCase* c, const double* state, int frozen, const int* col
  * use (kept with the case).  Device. */
 int fv_assemble_jacobian(FvCase* c, const double* state, const int* indptr, const int* indices,
                          double* values, void* stream);
+/* The same assembly, and the same JVP as fv_jvp, evaluated in fp32 arithmetic (single-precision
+ * dual numbers; fp64 state in, fp64 values out): the Jacobian of an fp32 preconditioner and the
+ * Krylov operator of a mixed-precision Newton, whose defect R stays fp64.  Agree with the fp64
+ * forms to fp32 rounding (~1e-6 relative). */
+int fv_assemble_jacobian_f32(FvCase* c, const double* state, const int* indptr, const int* indices,
+                             double* values, void* stream);
+int fv_jvp_f32(FvCase* c, const double* state, const double* v, double* jv, void* stream);
 /* jv = J v + shift * v (the pseudo-transient operator of aquaflux/solve/continuation.py:111-112);
  * `shift` is a device vector of the state's length. */
 int fv_jvp_shift(FvCase* c, const double* state, const double* v, const double* shift, double* jv,
