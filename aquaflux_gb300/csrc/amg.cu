@@ -11,6 +11,7 @@
 #include <algorithm>
 #include <vector>
 
+#include "host_par.h"
 #include "internal.cuh"
 
 // Greedy aggregation of a symmetric cell graph (CSR, self loops ignored):
@@ -94,45 +95,78 @@ extern "C" int fv_coarsen(int n, const int* indptr, const int* indices, const in
   for (int a = 0; a <= na; ++a) mptr[a] = cnt[a];
   for (int i = 0; i < n; ++i) mlist[cnt[agg[i]]++] = i;
   // coarse rows: sorted unique aggregate columns (a marker per aggregate column avoids sorting the
-  // duplicates); qmap: fine block -> coarse block
+  // duplicates), computed per aggregate in parallel into a scratch buffer bounded by the
+  // aggregate's fine block count; then the row offsets, then the copy.  With lists, the fine
+  // blocks of each coarse block are listed in ascending fine block order, aggregate by aggregate:
+  // members ascend within an aggregate and blocks ascend within a row, so a per-aggregate
+  // counting pass places them without a global sort.
   const bool lists = gptr != nullptr;  // NULL gptr / glist: the coarse pattern only
-  std::vector<long> qmap(lists ? nnz : 0);
-  std::vector<int> cols, mark(na, -1), slot(na, 0);
-  long pos = 0;
-  cip[0] = 0;
+  std::vector<long> fb(na + 1, 0);     // fine blocks of each aggregate (prefix)
   for (int a = 0; a < na; ++a) {
-    cols.clear();
-    for (int m = mptr[a]; m < mptr[a + 1]; ++m) {
-      const int i = mlist[m];
-      for (int q = indptr[i]; q < indptr[i + 1]; ++q) {
-        const int col = agg[indices[q]];
-        if (mark[col] != a) {
-          mark[col] = a;
-          cols.push_back(col);
-        }
-      }
-    }
-    std::sort(cols.begin(), cols.end());
-    for (size_t k = 0; k < cols.size(); ++k) {
-      cix[pos + (long)k] = cols[k];
-      slot[cols[k]] = (int)k;
-    }
-    if (lists)
+    long c = 0;
+    for (int m = mptr[a]; m < mptr[a + 1]; ++m) c += indptr[mlist[m] + 1] - indptr[mlist[m]];
+    fb[a + 1] = fb[a] + c;
+  }
+  std::vector<int> scratch(fb[na]);
+  std::vector<int> width(na);
+  const int nth = host_threads();
+  std::vector<std::vector<int>> marks(nth), slots(nth);
+  host_parallel_for(na, 4096, [&](long b, long e, int t) {
+    std::vector<int>& mark = marks[t];
+    mark.assign(na, -1);
+    for (long a = b; a < e; ++a) {
+      int* cols = scratch.data() + fb[a];
+      int k = 0;
       for (int m = mptr[a]; m < mptr[a + 1]; ++m) {
         const int i = mlist[m];
-        for (int q = indptr[i]; q < indptr[i + 1]; ++q) qmap[q] = pos + slot[agg[indices[q]]];
+        for (int q = indptr[i]; q < indptr[i + 1]; ++q) {
+          const int col = agg[indices[q]];
+          if (mark[col] != (int)a) {
+            mark[col] = (int)a;
+            cols[k++] = col;
+          }
+        }
       }
-    pos += (long)cols.size();
-    cip[a + 1] = (int)pos;
-  }
+      std::sort(cols, cols + k);
+      width[a] = k;
+    }
+  });
+  cip[0] = 0;
+  for (int a = 0; a < na; ++a) cip[a + 1] = cip[a] + width[a];
+  const long pos = cip[na];
   *n_coarse_blocks = pos;
-  if (!lists) return FV_OK;
-  // ordered fine-block lists (counting sort of qmap, stable)
-  for (long b = 0; b <= pos; ++b) gptr[b] = 0;
-  for (long q = 0; q < nnz; ++q) ++gptr[qmap[q] + 1];
-  for (long b = 0; b < pos; ++b) gptr[b + 1] += gptr[b];
-  std::vector<long> fill(gptr, gptr + pos);
-  for (long q = 0; q < nnz; ++q) glist[fill[qmap[q]]++] = q;
+  if (lists) {
+    // coarse block c of aggregate a holds the fine blocks of its members whose column aggregate
+    // is cix[c]: their count, then their offsets
+    gptr[0] = 0;
+  }
+  host_parallel_for(na, 4096, [&](long b, long e, int t) {
+    std::vector<int>& slot = slots[t];
+    if (lists) slot.assign(na, 0);
+    std::vector<long> fill;
+    for (long a = b; a < e; ++a) {
+      const int k = width[a];
+      const int* cols = scratch.data() + fb[a];
+      for (int c = 0; c < k; ++c) cix[cip[a] + c] = cols[c];
+      if (!lists) continue;
+      for (int c = 0; c < k; ++c) slot[cols[c]] = c;
+      fill.assign(k + 1, 0);
+      for (int m = mptr[a]; m < mptr[a + 1]; ++m) {
+        const int i = mlist[m];
+        for (int q = indptr[i]; q < indptr[i + 1]; ++q) ++fill[slot[agg[indices[q]]] + 1];
+      }
+      // this aggregate's fine blocks occupy glist[fb[a], fb[a + 1])
+      for (int c = 0; c < k; ++c) {
+        fill[c + 1] += fill[c];
+        gptr[cip[a] + c + 1] = fb[a] + fill[c + 1];
+      }
+      for (int m = mptr[a]; m < mptr[a + 1]; ++m) {
+        const int i = mlist[m];
+        for (int q = indptr[i]; q < indptr[i + 1]; ++q)
+          glist[fb[a] + fill[slot[agg[indices[q]]]]++] = q;
+      }
+    }
+  });
   return FV_OK;
 }
 

@@ -14,6 +14,7 @@
 #include <cstdint>
 #include <vector>
 
+#include "host_par.h"
 #include "internal.cuh"
 
 extern "C" int fv_saturation_colouring(int n, const int* indptr, const int* indices, int* colour,
@@ -123,24 +124,35 @@ extern "C" int fv_cell_pattern(int n, long n_pairs, const int* owner, const int*
   }
   for (int i = 0; i < n; ++i) cnt[i + 1] += cnt[i] + 1;  // + the diagonal
   std::vector<int> tmp(cnt[n]);
-  std::vector<long> fill(cnt.begin(), cnt.end() - 1);
-  for (int i = 0; i < n; ++i) tmp[fill[i]++] = i;
-  for (long f = 0; f < n_pairs; ++f) {
-    tmp[fill[owner[f]]++] = neighbour[f];
-    tmp[fill[neighbour[f]]++] = owner[f];
-  }
+  std::vector<int> width(n);
+  // each thread fills, sorts and de-duplicates the rows of its own range (scanning every pair)
+  host_parallel_for(n, 1 << 16, [&](long r0, long r1, int) {
+    std::vector<long> fill(cnt.begin() + r0, cnt.begin() + r1);
+    for (long i = r0; i < r1; ++i) tmp[fill[i - r0]++] = (int)i;
+    for (long f = 0; f < n_pairs; ++f) {
+      const int a = owner[f], b = neighbour[f];
+      if (a >= r0 && a < r1) tmp[fill[a - r0]++] = b;
+      if (b >= r0 && b < r1) tmp[fill[b - r0]++] = a;
+    }
+    for (long i = r0; i < r1; ++i) {
+      auto b = tmp.begin() + cnt[i], e = tmp.begin() + cnt[i + 1];
+      std::sort(b, e);
+      width[i] = (int)(std::unique(b, e) - b);
+    }
+  });
   long pos = 0;
   indptr[0] = 0;
   for (int i = 0; i < n; ++i) {
-    auto b = tmp.begin() + cnt[i], e = tmp.begin() + cnt[i + 1];
-    std::sort(b, e);
-    e = std::unique(b, e);
-    for (auto it = b; it != e; ++it) indices[pos++] = *it;
+    pos += width[i];
     if (pos > 0x7fffffffL) {
       fv_set_error("fv_cell_pattern: pattern exceeds int32 entries");
       return FV_ERR_ARG;
     }
     indptr[i + 1] = (int)pos;
   }
+  host_parallel_for(n, 1 << 16, [&](long r0, long r1, int) {
+    for (long i = r0; i < r1; ++i)
+      std::copy(tmp.begin() + cnt[i], tmp.begin() + cnt[i] + width[i], indices + indptr[i]);
+  });
   return FV_OK;
 }
