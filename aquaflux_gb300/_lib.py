@@ -74,6 +74,7 @@ SIGNATURES = {
     "fv_ilu0_factor_values": (c_int, [P, P, P]),
     "fv_dot_f64": (c_int, [c_long, P, P, P, P]),
     "fv_saturation_colouring": (c_int, [c_int, P, P, P, P]),
+    "fv_greedy_colouring": (c_int, [c_int, P, P, P, P]),
     "fv_coarsen": (c_int, [c_int, P, P, P, c_int, P, P, P, P, P, P, P]),
     "fv_cell_pattern": (c_int, [c_int, c_long, P, P, P, P]),
     "fv_aggregate": (c_int, [c_int, P, P, P, P]),

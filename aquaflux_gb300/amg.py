@@ -208,15 +208,16 @@ class AmgPreconditioner:
     """``M ~= J^-1``: one aggregation V-cycle with ILU(0) smoothing of the materialised block
     Jacobian, fp32 (default) or fp64 throughout (field-major fp64 vectors in and out).
 
-    ``fine_order="natural"`` (default) keeps the operator's own cell order for the fine ILU(0)
-    smoother; ``"colour"`` numbers the fine cells colour by colour (a distance-1 colouring of the
-    cell graph; two colours on a hexahedral mesh), so that the fine sweeps run in a few wide level
-    sets -- cheaper per cycle, but a red-black ILU(0) is a weaker smoother: on the 3D SST channel
-    the two orders give the same Newton time, on 2D laminar saddle-point systems the coloured
-    smoother stalls.  Coarse levels are always colour-numbered.
+    ``fine_order="natural"`` keeps the operator's own cell order for the fine ILU(0) smoother;
+    ``"colour"`` numbers the fine cells colour by colour (a first-fit colouring of the cell graph:
+    a few colours on a hexahedral mesh), so that the fine sweeps run in a few wide level sets
+    instead of ~3N narrow ones -- much cheaper per cycle, a weaker smoother.  ``"auto"`` (default)
+    takes the coloured order in 3D, where it wins (128^3 SST channel: 95 instead of 72 Krylov
+    iterations, each V-cycle ~4x cheaper), and the natural order in 2D, where the coloured smoother
+    stalls on laminar saddle-point systems.  Coarse levels are always colour-numbered.
     """
 
-    def __init__(self, jac, precision: int = 32, *, fine_order: str = "natural", shift=None,
+    def __init__(self, jac, precision: int = 32, *, fine_order: str = "auto", shift=None,
                  equilibrate: bool = False, **kw):
         from .solve import ShiftedCellMajorOperator
 
@@ -224,11 +225,14 @@ class AmgPreconditioner:
         n, b = jac.n, jac.b
         self._perm = self._bmap = None
         indptr, indices = jac.indptr, jac.indices
+        if fine_order == "auto":
+            fine_order = "colour" if jac.case.dim == 3 else "natural"
+        self.fine_order = fine_order
         if fine_order == "colour":
             col = np.empty(n, dtype=np.int32)
             nco = ctypes.c_int(0)
-            check(lib().fv_saturation_colouring(n, ptr(indptr), ptr(indices), ptr(col),
-                                                ctypes.byref(nco)))
+            check(lib().fv_greedy_colouring(n, ptr(indptr), ptr(indices), ptr(col),
+                                            ctypes.byref(nco)))
             perm = np.argsort(col, kind="stable").astype(np.int32)
             pip = np.empty(n + 1, dtype=np.int32)
             pix = np.empty(int(indptr[-1]), dtype=np.int32)

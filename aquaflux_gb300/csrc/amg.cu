@@ -187,28 +187,29 @@ extern "C" int fv_permute_pattern(int n, const int* indptr, const int* indices, 
     }
     iperm[perm[r]] = r;
   }
-  std::vector<std::pair<int, long>> row;
-  long pos = 0;
+  // rows keep their widths: offsets first, then the rows in parallel
   out_indptr[0] = 0;
-  for (int r = 0; r < n; ++r) {
-    const int i = perm[r];
-    row.clear();
-    for (int q = indptr[i]; q < indptr[i + 1]; ++q) {
-      const int j = indices[q];
-      if (j < 0 || j >= n) {
-        fv_set_error("fv_permute_pattern: column index out of range");
-        return FV_ERR_ARG;
+  for (int r = 0; r < n; ++r) out_indptr[r + 1] = out_indptr[r] + (indptr[perm[r] + 1] - indptr[perm[r]]);
+  for (long q = 0; q < indptr[n]; ++q)
+    if (indices[q] < 0 || indices[q] >= n) {
+      fv_set_error("fv_permute_pattern: column index out of range");
+      return FV_ERR_ARG;
+    }
+  host_parallel_for(n, 1 << 15, [&](long r0, long r1, int) {
+    std::vector<std::pair<int, long>> row;
+    for (long r = r0; r < r1; ++r) {
+      const int i = perm[r];
+      row.clear();
+      for (int q = indptr[i]; q < indptr[i + 1]; ++q) row.emplace_back(iperm[indices[q]], (long)q);
+      std::sort(row.begin(), row.end());
+      long pos = out_indptr[r];
+      for (const auto& e : row) {
+        out_indices[pos] = e.first;
+        bmap[pos] = e.second;
+        ++pos;
       }
-      row.emplace_back(iperm[j], (long)q);
     }
-    std::sort(row.begin(), row.end());
-    for (const auto& e : row) {
-      out_indices[pos] = e.first;
-      bmap[pos] = e.second;
-      ++pos;
-    }
-    out_indptr[r + 1] = (int)pos;
-  }
+  });
   return FV_OK;
 }
 

@@ -106,6 +106,40 @@ extern "C" int fv_saturation_colouring(int n, const int* indptr, const int* indi
 // Reach-1 cell pattern (host): row i holds i and the cells sharing a face with i, sorted and
 // unique.  Interior faces given as (owner, neighbour) pairs.  indptr (n + 1); indices receives
 // at most n + 2 * n_pairs entries.
+// First-fit greedy colouring in index order (every vertex takes the smallest colour none of its
+// already coloured neighbours has): O(edges), for orderings where the colour count matters more
+// than its minimality (the AMG fine smoother's red-black-like sweeps).
+extern "C" int fv_greedy_colouring(int n, const int* indptr, const int* indices, int* colour,
+                                   int* n_colours) {
+  if (n < 0 || (n > 0 && (!indptr || !indices || !colour))) {
+    fv_set_error("fv_greedy_colouring: bad arguments");
+    return FV_ERR_ARG;
+  }
+  int ncol = 0;
+  std::vector<int> seen(64, -1);
+  for (int v = 0; v < n; ++v) colour[v] = -1;
+  for (int v = 0; v < n; ++v) {
+    for (int q = indptr[v]; q < indptr[v + 1]; ++q) {
+      const int u = indices[q];
+      if (u < 0 || u >= n) {
+        fv_set_error("fv_greedy_colouring: neighbour index out of range");
+        return FV_ERR_ARG;
+      }
+      const int c = colour[u];
+      if (c >= 0) {
+        if (c >= (int)seen.size()) seen.resize(2 * c + 2, -1);
+        seen[c] = v;
+      }
+    }
+    int c = 0;
+    while (c < (int)seen.size() && seen[c] == v) ++c;
+    colour[v] = c;
+    if (c + 1 > ncol) ncol = c + 1;
+  }
+  if (n_colours) *n_colours = ncol;
+  return FV_OK;
+}
+
 extern "C" int fv_cell_pattern(int n, long n_pairs, const int* owner, const int* neighbour,
                                int* indptr, int* indices) {
   if (n <= 0 || n_pairs < 0 || (n_pairs > 0 && (!owner || !neighbour)) || !indptr || !indices) {

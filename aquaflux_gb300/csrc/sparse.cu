@@ -335,62 +335,113 @@ __global__ void k_ilu_lower_t(IluView<V> F, const int* tptr, const int* tidx, co
 #define FV_LG 8
 __device__ __forceinline__ unsigned lg_mask() { return 0xffu << ((threadIdx.x & 31) & ~(FV_LG - 1)); }
 
-template <class V>
-__global__ void k_ilu_factor_lg(IluView<V> F, const int* rows, int count,
-                                unsigned long long* zero_flag) {
+// Factor the block rows of one level, a group of FV_LG lanes per block row (lane a = row a of the
+// block), with a compile-time block size: the row's lower block, the pivot row's diagonal block and
+// each upper block it updates with are held in registers (vector loads), the diagonal block's pivot
+// rows are shuffled from the lane that owns them.  Every entry sees the scalar elimination of
+// k_ilu_factor_level in the same order, so the factors are bitwise the same.
+template <class V, int B>
+__global__ void k_ilu_factor_lgb(IluView<V> F, const int* rows, int count,
+                                 unsigned long long* zero_flag) {
   const int gid = (blockIdx.x * blockDim.x + threadIdx.x) / FV_LG;
   const int a = threadIdx.x & (FV_LG - 1);
   if (gid >= count) return;  // whole groups exit together
   const unsigned mask = lg_mask();
   const int i = rows[gid];
-  const int b = F.b;
-  const bool live = a < b;
-  const long bb = (long)b * b;
+  const bool live = a < B;
+  const int ar = live ? a : 0;  // row index of the lane's (possibly unused) loads
+  constexpr long BB = (long)B * B;
   const int re = F.ptr[i + 1], di = F.diag[i];
   for (int q = F.ptr[i]; q < di; ++q) {
     const int j = F.idx[q];
-    V* Lij = F.val + (long)q * bb;
-    const V* Ujj = F.val + (long)F.diag[j] * bb;
+    V* Lij = F.val + (long)q * BB;
+    const V* Ujj = F.val + (long)F.diag[j] * BB;
+    V L[B], U[B * B];
+    load_seg<B>(Lij + (long)ar * B, L);
+#pragma unroll
+    for (int r = 0; r < B; ++r) {
+      V row[B];
+      load_seg<B>(Ujj + (long)r * B, row);
+#pragma unroll
+      for (int c = 0; c < B; ++c) U[r * B + c] = row[c];
+    }
+#pragma unroll
+    for (int cb = 0; cb < B; ++cb) {
+      const V piv = U[cb * B + cb];
+      if (piv == V(0) && a == 0) note_zero_pivot(zero_flag, i * B, j * B + cb);
+      const V l = L[cb] / piv;
+      L[cb] = l;
+#pragma unroll
+      for (int c2 = cb + 1; c2 < B; ++c2) L[c2] -= l * U[cb * B + c2];
+    }
     if (live) {
-      for (int cb = 0; cb < b; ++cb) {
-        const V piv = Ujj[(long)cb * b + cb];
-        if (piv == V(0) && a == 0) note_zero_pivot(zero_flag, i * b, j * b + cb);
-        const V l = Lij[(long)a * b + cb] / piv;
-        Lij[(long)a * b + cb] = l;
-        for (int c2 = cb + 1; c2 < b; ++c2) Lij[(long)a * b + c2] -= l * Ujj[(long)cb * b + c2];
+#pragma unroll
+      for (int c = 0; c < B; ++c) Lij[(long)a * B + c] = L[c];
+    }
+    // A_ik -= L_ij A_jk for k > j present in both rows (merge of sorted column lists)
+    int p = q + 1;
+    for (int s2 = F.diag[j] + 1; s2 < F.ptr[j + 1]; ++s2) {
+      const int k = F.idx[s2];
+      while (p < re && F.idx[p] < k) ++p;
+      if (p >= re) break;
+      if (F.idx[p] != k) continue;
+      V* Aik = F.val + (long)p * BB + (long)ar * B;
+      const V* Ajk = F.val + (long)s2 * BB;
+      V A[B], M[B * B];
+      load_seg<B>(Aik, A);
+#pragma unroll
+      for (int r = 0; r < B; ++r) {
+        V row[B];
+        load_seg<B>(Ajk + (long)r * B, row);
+#pragma unroll
+        for (int c = 0; c < B; ++c) M[r * B + c] = row[c];
       }
-      int p = q + 1;
-      for (int s2 = F.diag[j] + 1; s2 < F.ptr[j + 1]; ++s2) {
-        const int k = F.idx[s2];
-        while (p < re && F.idx[p] < k) ++p;
-        if (p >= re) break;
-        if (F.idx[p] != k) continue;
-        V* Aik = F.val + (long)p * bb + (long)a * b;
-        const V* Ajk = F.val + (long)s2 * bb;
-        for (int c = 0; c < b; ++c) {
-          V acc = Aik[c];
-          for (int mm = 0; mm < b; ++mm) acc -= Lij[(long)a * b + mm] * Ajk[(long)mm * b + c];
-          Aik[c] = acc;
-        }
+#pragma unroll
+      for (int c = 0; c < B; ++c) {
+        V acc = A[c];
+#pragma unroll
+        for (int mm = 0; mm < B; ++mm) acc -= L[mm] * M[mm * B + c];
+        A[c] = acc;
+      }
+      if (live) {
+#pragma unroll
+        for (int c = 0; c < B; ++c) Aik[c] = A[c];
       }
     }
   }
   __syncwarp(mask);
-  V* D = F.val + (long)di * bb;
-  for (int cb = 0; cb < b; ++cb) {
-    // row cb of the diagonal block (and of the upper blocks) is final here
+  V* D = F.val + (long)di * BB;
+  V Drow[B];
+  load_seg<B>(D + (long)ar * B, Drow);
+#pragma unroll
+  for (int cb = 0; cb < B; ++cb) {
+    // row cb of the diagonal block is final: lane cb's registers; of the upper blocks: in memory
+    V prow[B];
+#pragma unroll
+    for (int c = 0; c < B; ++c) prow[c] = __shfl_sync(mask, Drow[c], cb, FV_LG);
     if (live && a > cb) {
-      const V piv = D[(long)cb * b + cb];
-      if (piv == V(0)) note_zero_pivot(zero_flag, i * b + a, i * b + cb);
-      const V l = D[(long)a * b + cb] / piv;
-      D[(long)a * b + cb] = l;
-      for (int c = cb + 1; c < b; ++c) D[(long)a * b + c] -= l * D[(long)cb * b + c];
+      const V piv = prow[cb];
+      if (piv == V(0)) note_zero_pivot(zero_flag, i * B + a, i * B + cb);
+      const V l = Drow[cb] / piv;
+      Drow[cb] = l;
+#pragma unroll
+      for (int c = cb + 1; c < B; ++c) Drow[c] -= l * prow[c];
       for (int q = di + 1; q < re; ++q) {
-        V* U = F.val + (long)q * bb;
-        for (int c = 0; c < b; ++c) U[(long)a * b + c] -= l * U[(long)cb * b + c];
+        V* Ub = F.val + (long)q * BB;
+        V ua[B], uc[B];
+        load_seg<B>(Ub + (long)a * B, ua);
+        load_seg<B>(Ub + (long)cb * B, uc);
+#pragma unroll
+        for (int c = 0; c < B; ++c) ua[c] -= l * uc[c];
+#pragma unroll
+        for (int c = 0; c < B; ++c) Ub[(long)a * B + c] = ua[c];
       }
     }
     __syncwarp(mask);
+  }
+  if (live) {
+#pragma unroll
+    for (int c = 0; c < B; ++c) D[(long)a * B + c] = Drow[c];
   }
 }
 
@@ -616,8 +667,10 @@ void launch_factor_levels(FvIlu0* f, cudaStream_t s) {
       k_ilu_factor_level<V><<<fv_blocks(cnt, 128), 128, 0, s>>>(F, f->rows_fwd + f->lv_fwd[l], cnt,
                                                                 f->zero_flag);
     else
-      k_ilu_factor_lg<V><<<fv_blocks((long)cnt * FV_LG, 128), 128, 0, s>>>(
-          F, f->rows_fwd + f->lv_fwd[l], cnt, f->zero_flag);
+      with_block_size(f->b, [&](auto B) {
+        k_ilu_factor_lgb<V, B()><<<fv_blocks((long)cnt * FV_LG, 128), 128, 0, s>>>(
+            F, f->rows_fwd + f->lv_fwd[l], cnt, f->zero_flag);
+      });
   }
 }
 

@@ -48,9 +48,9 @@ def _args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--step", default="vjp", choices=["vjp", "jvp"])
     ap.add_argument("--no-newton", action="store_true", help="skip the Newton-solve timing")
-    ap.add_argument("--newton-kinds", default="amg,ilu",
-                    help="preconditioners timed in the Newton block (comma list of amg, "
-                         "amg-colour, ilu)")
+    ap.add_argument("--newton-kinds", default="amg,amg-natural,ilu",
+                    help="preconditioners timed in the Newton block (comma list of amg (fine "
+                         "order by dimension: coloured in 3D), amg-natural, amg-colour, ilu)")
     ap.add_argument("--workload", default="channel3d", choices=["channel3d", "batched"],
                     help="channel3d: the 128^3 SST channel (the headline); batched: the 64-instance "
                          "calibration sweep (its own JSON line)")
@@ -354,14 +354,14 @@ def run_gpu(args, rank: int, world: int, local_rank: int) -> dict | None:
 
 
 def newton_block(args, wl, case) -> dict:
-    """Newton-solve seconds, fp64-preconditioned (plain) vs fp32-preconditioned (mixed) form, for
-    each preconditioner kind (aggregation-AMG V-cycle, ILU(0)).
+    """Newton-solve seconds for each preconditioner kind (aggregation-AMG V-cycle, ILU(0)) in three
+    forms: fp64 throughout; an fp32 preconditioner; an fp32 preconditioner with the dual-number
+    passes (the Krylov operator J v and the preconditioner's Jacobian assembly) in fp32.
 
-    Every form: fp64 residual, fp64 JVP operator, fp64 FGMRES(30) with Krylov orthogonalisation,
-    fp64 Newton update and line search; fp32 and fp64 forms differ only in the precision of the
-    preconditioner built from the materialised reach-1 Jacobian.  Each solve is timed whole, from
-    the initial state and including the preconditioner's setup (pattern, hierarchy, factors).
-    Stops at ||R|| <= 1e-12 + 1e-10 ||R0||.
+    Every form: fp64 residual, fp64 FGMRES(30) with Krylov orthogonalisation, fp64 Newton update
+    and line search, so every form converges to the fp64 root.  Each solve is timed whole, from
+    the initial state and including the preconditioner's setup (pattern, hierarchy, factors; the
+    "setup" phase).  Stops at ||R|| <= 1e-12 + 1e-10 ||R0||.
     """
     import numpy as np
     import torch
@@ -390,40 +390,43 @@ def newton_block(args, wl, case) -> dict:
 
     warm = workloads.channel3d(16)
     warm_case = warm.device_case()
+    forms = ((64, 64), (32, 64), (32, 32))  # (preconditioner precision, tangent precision)
     for kind in args.newton_kinds.split(","):
-        for prec in (64, 32):
-            solve.newton_solve(warm_case, warm.initial_state(), precision=prec,
+        for prec, tan in forms:
+            solve.newton_solve(warm_case, warm.initial_state(), precision=prec, tangents=tan,
                                kind="amg" if kind.startswith("amg") else kind, max_steps=40)
     del warm_case
-    # the allocator's pool at full size: FGMRES(30)'s two bases (the largest buffers of a solve),
-    # so that no timed solve pays a first cudaMalloc the other forms do not
-    n = case.n_unknowns
-    pool = [torch.empty(31, n, dtype=torch.float64, device="cuda"),
-            torch.empty(30, n, dtype=torch.float64, device="cuda")]
-    del pool
+    # one untimed two-step solve at full size: the first full-size Krylov iterations of a process
+    # pay one-off costs (allocator growth to FGMRES(30)'s bases, first large-shape library calls)
+    # that no timed form should carry alone
+    solve.newton_solve(case, wl.initial_state(), precision=64, kind="amg", max_steps=2)
     torch.cuda.synchronize()
     states = {}
     for kind in args.newton_kinds.split(","):
-        for prec in (64, 32):
+        for prec, tan in forms:
             torch.cuda.synchronize()
-            opts = {"fine_order": "colour"} if kind == "amg-colour" else None
-            res = solve.newton_solve(case, wl.initial_state(), precision=prec,
+            opts = ({"fine_order": "colour"} if kind == "amg-colour" else
+                    {"fine_order": "natural"} if kind == "amg-natural" else None)
+            res = solve.newton_solve(case, wl.initial_state(), precision=prec, tangents=tan,
                                      kind="amg" if kind.startswith("amg") else kind,
                                      precond_options=opts, max_steps=40)
-            out[f"{kind}_fp{prec}"] = {
+            key = f"{kind}_fp{prec}" + ("_fp32_tangents" if tan == 32 else "")
+            out[key] = {
                 "seconds": round(res.seconds, 3), "converged": bool(res.converged),
                 "newton_steps": res.steps, "krylov_iterations": int(sum(res.krylov_iterations)),
                 "final_rel_residual": res.residual_norms[-1] / res.residual_norms[0],
                 "phase_seconds": {k: round(v, 3) for k, v in res.phase_seconds.items()}}
-            states[(kind, prec)] = res.state
+            states[(kind, prec, tan)] = res.state
             del res
-        a, b = states[(kind, 64)], states[(kind, 32)]
-        out[f"{kind}_fp32_vs_fp64_field_max_rel_diff"] = float((a - b).abs().max() /
-                                                               a.abs().max())
-        out[f"{kind}_speedup_fp32_vs_fp64"] = round(
-            out[f"{kind}_fp64"]["seconds"] / out[f"{kind}_fp32"]["seconds"], 3)
+        a = states[(kind, 64, 64)]
+        for prec, tan in forms[1:]:
+            key = f"{kind}_fp{prec}" + ("_fp32_tangents" if tan == 32 else "")
+            b = states[(kind, prec, tan)]
+            out[f"{key}_vs_fp64_field_max_rel_diff"] = float((a - b).abs().max() / a.abs().max())
+            out[f"{key}_speedup_vs_fp64"] = round(
+                out[f"{kind}_fp64"]["seconds"] / out[key]["seconds"], 3)
     if not args.no_adjoint:
-        out["adjoint"] = adjoint_block(case, states[(args.newton_kinds.split(",")[0], 32)])
+        out["adjoint"] = adjoint_block(case, states[(args.newton_kinds.split(",")[0], 32, 64)])
     if args.newton_oracle_check:
         from oracle import fv_oracle as fo
 
@@ -434,7 +437,7 @@ def newton_block(args, wl, case) -> dict:
         orc = fo.Oracle(c)
         r0 = float(np.linalg.norm(orc.residual(torch.as_tensor(wl.initial_state())).numpy()))
         kind = args.newton_kinds.split(",")[0]
-        r32 = float(np.linalg.norm(orc.residual(states[(kind, 32)].cpu()).numpy()))
+        r32 = float(np.linalg.norm(orc.residual(states[(kind, 32, 64)].cpu()).numpy()))
         out["fp32_oracle_rel_residual"] = r32 / r0
     return out
 

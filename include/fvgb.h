@@ -302,6 +302,9 @@ int fv_bsr_shift_equilibrate(int n, int b, const int* indptr, const int* indices
  * ------------------------------------------------------------------------------------------ */
 int fv_saturation_colouring(int n, const int* indptr, const int* indices, int* colour,
                             int* n_colours);
+/* First-fit greedy colouring in index order (O(edges); not the reference's): the AMG fine-level
+ * ordering of 3D operators, where only a small colour count matters. */
+int fv_greedy_colouring(int n, const int* indptr, const int* indices, int* colour, int* n_colours);
 /* Reach-1 cell pattern (host): row i = {i} + the cells sharing an interior face with i, sorted
  * and unique (the pattern of the frozen Jacobian; stencil_pattern with reach 1,
  * aquaflux/solve/sparse_jacobian.py).  indptr (n + 1); indices capacity n + 2 * n_pairs. */
