@@ -7,10 +7,11 @@
 // and omega only, so the Jacobian needs no colouring:
 //   k_jac_face  face  forward-mode derivative of every flux of the face with respect to each of the
 //                     2 x NF unknowns of its two cells (the flux code of the residual, evaluated with
-//                     one seeded tangent per unknown), into D (2, NF, NF, nf);
-//   k_jac_cell  (cell, row field)  one row of every block of the cell's block row: the face
-//                     derivatives summed in the cell's face order with the residual's signs, then
-//                     the SST source rows, the omega wall-cell rows and the pressure-pin row.
+//                     one seeded tangent per unknown), into D (nf, 2, NF, NF): each face's 2 NF^2
+//                     derivatives contiguous, so the cell gather reads whole rows;
+//   k_jac_cell  cell  the cell's block row: the face derivatives summed in the cell's face order
+//                     with the residual's signs (whole face blocks, contiguous), then the SST
+//                     source rows, the omega wall-cell rows and the pressure-pin row.
 // Every entry is the tangent the coloured probe computes for it, by the same arithmetic in the
 // same order.
 
@@ -25,12 +26,12 @@ struct SeedSrc {
   }
 };
 
-// Keeps the tangent of flux q as D[((side * NF + q) * NF + r) * nf + f].
+// Keeps the tangent of flux q as D[((f * 2 + side) * NF + q) * NF + r].
 template <class T>
 struct DerivStore {
   double* D;
-  long base;  // ((side * NF) * NF + r) * nf + f
-  long qstride;  // NF * nf
+  long base;  // ((f * 2 + side) * NF) * NF + r
+  long qstride;  // NF
   __device__ __forceinline__ void operator()(int q, const T& x) const {
     D[base + q * qstride] = x.d;
   }
@@ -50,7 +51,7 @@ __global__ void __launch_bounds__(128) k_jac_face(MeshView m, CaseView cv, const
 #pragma unroll 1
     for (int r = 0; r < NF; ++r) {
       const SeedSrc<T> st{state, (long)r * nc + cell};
-      const DerivStore<T> wr{D, ((long)(side * NF) * NF + r) * nf + f, (long)NF * nf};
+      const DerivStore<T> wr{D, ((long)f * 2 + side) * NF * NF + r, (long)NF};
       flux_face<T, DIM, TURB>(m, cv, st, par, G, cl, dco, (const T*)nullptr, psi, true, f, wr,
                               nullptr);
     }
@@ -65,73 +66,84 @@ __global__ void __launch_bounds__(128) k_jac_cell(MeshView m, CaseView cv, const
                                                   double* values) {
   using L = Layout<DIM, TURB>;
   constexpr int NF = L::NFLD;
-  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long)NF * m.nc) return;
-  const int nc = m.nc, nf = m.nf;
-  const int c = (int)(t % nc), q = (int)(t / nc);
-  const int bp = indptr[c], be = indptr[c + 1];
-  for (int p = bp; p < be; ++p)
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nc) return;
+  const int nc = m.nc;
+  const int bp = indptr[c], be = indptr[c + 1];  // (the block rows were zeroed before the launch)
+  // rows without the face sum: the pinned pressure row, the omega wall-cell row
+  bool skip[NF];
 #pragma unroll
-    for (int r = 0; r < NF; ++r) values[((long)p * NF + q) * NF + r] = 0.0;
-  const bool pinned = c == cv.pin && q == L::P;
-  bool wall_omega = false;
-  if constexpr (TURB) wall_omega = q == L::W && cv.wcell[c] != 0;
-  double dg[NF];
+  for (int q = 0; q < NF; ++q) skip[q] = false;
+  if (c == cv.pin) skip[L::P] = true;
+  if constexpr (TURB) skip[L::W] = cv.wcell[c] != 0;
+  double dg[NF][NF];
 #pragma unroll
-  for (int r = 0; r < NF; ++r) dg[r] = 0.0;
-  const long rstride = nf;
-  if (!pinned && !wall_omega) {
-    const int b = m.cf_ptr[c], e = m.cf_ptr[c + 1];
-    for (int i = b; i < e; ++i) {
-      const unsigned ent = m.cf_face[i];
-      const int f = (int)(ent & ~FV_NB_BIT);
-      const bool isnb = (ent & FV_NB_BIT) != 0;
-      const double sg = isnb ? -1.0 : 1.0;
-      const long self = ((long)((isnb ? NF : 0) + q) * NF) * nf + f;
+  for (int q = 0; q < NF; ++q)
+#pragma unroll
+    for (int r = 0; r < NF; ++r) dg[q][r] = 0.0;
+  const int b = m.cf_ptr[c], e = m.cf_ptr[c + 1];
+  for (int i = b; i < e; ++i) {
+    const unsigned ent = m.cf_face[i];
+    const int f = (int)(ent & ~FV_NB_BIT);
+    const bool isnb = (ent & FV_NB_BIT) != 0;
+    const double sg = isnb ? -1.0 : 1.0;
+    const double* self = D + ((long)f * 2 + (isnb ? 1 : 0)) * NF * NF;
+#pragma unroll
+    for (int q = 0; q < NF; ++q)
 #pragma unroll
       for (int r = 0; r < NF; ++r) {
-        const double x = sg * D[self + r * rstride];
-        dg[r] = i == b ? x : dg[r] + x;
+        const double x = sg * self[q * NF + r];
+        dg[q][r] = i == b ? x : dg[q][r] + x;
       }
-      if (f < m.nfi) {
-        const int j = isnb ? m.owner[f] : m.nb[f];
-        int slot = -1;
-        for (int p = bp; p < be; ++p)
-          if (indices[p] == j) {
-            slot = p;
-            break;
-          }
-        if (slot >= 0) {
-          const long oth = ((long)((isnb ? 0 : NF) + q) * NF) * nf + f;
-          double* row = values + ((long)slot * NF + q) * NF;
+    if (f < m.nfi) {
+      const int j = isnb ? m.owner[f] : m.nb[f];
+      int slot = -1;
+      for (int p = bp; p < be; ++p)
+        if (indices[p] == j) {
+          slot = p;
+          break;
+        }
+      if (slot >= 0) {
+        const double* oth = D + ((long)f * 2 + (isnb ? 0 : 1)) * NF * NF;
+        double* blk = values + (long)slot * NF * NF;
 #pragma unroll
-          for (int r = 0; r < NF; ++r) row[r] += sg * D[oth + r * rstride];
+        for (int q = 0; q < NF; ++q) {
+          if (skip[q]) continue;
+#pragma unroll
+          for (int r = 0; r < NF; ++r) blk[q * NF + r] += sg * oth[q * NF + r];
         }
       }
     }
   }
-  if (pinned) {
 #pragma unroll
-    for (int r = 0; r < NF; ++r) dg[r] = r == L::P ? 1.0 : 0.0;
+  for (int q = 0; q < NF; ++q)
+    if (skip[q])
+#pragma unroll
+      for (int r = 0; r < NF; ++r) dg[q][r] = 0.0;
+  if (c == cv.pin) {
+#pragma unroll
+    for (int r = 0; r < NF; ++r) dg[L::P][r] = r == L::P ? 1.0 : 0.0;
   }
   if constexpr (TURB) {
-    if (q == L::K || q == L::W) {
-      // only k and omega of the cell itself enter its source rows
+    // only k and omega of the cell itself enter its source rows: one seeded evaluation per
+    // column gives both rows (each row's tangent starts from its own face sum)
 #pragma unroll
-      for (int r = L::K; r <= L::W; ++r) {
-        using S = decltype(T::v);
-        const SeedSrc<T> st{state, (long)r * nc + c};
-        T rk{S(0), S(q == L::K ? dg[r] : 0.0)}, rw{S(0), S(q == L::W ? dg[r] : 0.0)};
-        sst_rows<T, DIM>(m, cv, st, par, cl, G, Gwi, c, rk, rw);
-        dg[r] = q == L::K ? rk.d : rw.d;
-      }
+    for (int r = L::K; r <= L::W; ++r) {
+      using S = decltype(T::v);
+      const SeedSrc<T> st{state, (long)r * nc + c};
+      T rk{S(0), S(dg[L::K][r])}, rw{S(0), S(dg[L::W][r])};
+      sst_rows<T, DIM>(m, cv, st, par, cl, G, Gwi, c, rk, rw);
+      dg[L::K][r] = rk.d;
+      dg[L::W][r] = rw.d;
     }
   }
   for (int p = bp; p < be; ++p)
     if (indices[p] == c) {
-      double* row = values + ((long)p * NF + q) * NF;
+      double* blk = values + (long)p * NF * NF;
 #pragma unroll
-      for (int r = 0; r < NF; ++r) row[r] = dg[r];
+      for (int q = 0; q < NF; ++q)
+#pragma unroll
+        for (int r = 0; r < NF; ++r) blk[q * NF + r] = dg[q][r];
       break;
     }
 }
@@ -159,7 +171,16 @@ int assemble_frozen(FvCase* cs, const double* state, const int* indptr, const in
     k_limiter<T, DIM, TURB><<<bc, TB, 0, s>>>(m, st, w.G, cv.lim_km, cv.lim_ks, w.psi);
   k_jac_face<T, DIM, TURB><<<bf, TB, 0, s>>>(m, cv, state, par, w.G, w.cl, w.dco,
                                              npsi ? w.psi : nullptr, D);
-  k_jac_cell<T, DIM, TURB><<<fv_blocks((long)NF * nc, TB), TB, 0, s>>>(
+  if (cs->jac_indptr != indptr) {  // the pattern's block count, read once per pattern
+    int nnzb = 0;
+    FV_CUDA_TRY(cudaMemcpyAsync(&nnzb, indptr + nc, sizeof(int), cudaMemcpyDeviceToHost, s));
+    FV_CUDA_TRY(cudaStreamSynchronize(s));
+    cs->jac_indptr = indptr;
+    cs->jac_nnzb = nnzb;
+  }
+  FV_CUDA_TRY(cudaMemsetAsync(values, 0, sizeof(double) * (size_t)NF * NF * (size_t)cs->jac_nnzb,
+                              s));
+  k_jac_cell<T, DIM, TURB><<<fv_blocks(nc, TB), TB, 0, s>>>(
       m, cv, state, par, w.G, w.cl, w.Gwi, D, indptr, indices, values);
   FV_CUDA_TRY(cudaGetLastError());
   return FV_OK;

@@ -127,7 +127,9 @@ struct FvCase {
   double* adj = nullptr;    // adjoint workspace
   double* aux = nullptr;    // face intermediates of the double forward pass (for the adjoint)
   double* dscalar = nullptr; // (4) device scalars
-  double* jac_face = nullptr; // (2, nfld, nfld, nf) face flux derivatives of the Jacobian assembly
+  double* jac_face = nullptr; // (nf, 2, nfld, nfld) face flux derivatives of the Jacobian assembly
+  const int* jac_indptr = nullptr;  // the block pattern last assembled into, and its block count
+  long jac_nnzb = 0;
   int* wnear = nullptr;       // (nc) nearest SST wall face (internal index), turbulent cases
   NodeAdjoint* nadj = nullptr;  // mesh-coordinate adjoint workspace, allocated on first use
   int tb = 128;                 // threads per block of the residual / JVP / VJP stages (autotuned)

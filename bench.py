@@ -58,7 +58,34 @@ def _args():
                     help="skip the adjoint objectives' gradients after the Newton solves")
     ap.add_argument("--newton-oracle-check", action="store_true",
                     help="also evaluate the converged fp32-preconditioned state with the CPU oracle")
+    ap.add_argument("--newton-only", default=None, metavar="KIND:PREC:TANGENTS",
+                    help="run one Newton solve of that form (e.g. amg:32:32) on the channel and "
+                         "print its timings only (for profiling the solve's kernels)")
     return ap.parse_args()
+
+
+def run_newton_only(args) -> dict:
+    """One Newton solve of the given form on the --size channel after one warm-up solve on a 16^3
+    channel (library initialisation), with no other GPU work in the process."""
+    import torch
+
+    from aquaflux_gb300 import solve, workloads
+
+    kind, prec, tan = args.newton_only.split(":")
+    warm = workloads.channel3d(16)
+    solve.newton_solve(warm.device_case(), warm.initial_state(), kind=kind, precision=int(prec),
+                       tangents=int(tan))
+    wl = workloads.channel3d(args.size)
+    case = wl.device_case()
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_push("newton")  # the profiled region (ncu --nvtx-include "newton/")
+    res = solve.newton_solve(case, wl.initial_state(), kind=kind, precision=int(prec),
+                             tangents=int(tan))
+    torch.cuda.nvtx.range_pop()
+    return {"newton_only": args.newton_only, "cells": wl.mesh.n_cells, "seconds": res.seconds,
+            "converged": res.converged, "newton_steps": res.steps,
+            "krylov_iterations": res.krylov_iterations,
+            "phase_seconds": {k: round(v, 4) for k, v in res.phase_seconds.items()}}
 
 
 # ----------------------------------------------------------------------------- clocks
@@ -598,6 +625,10 @@ def main():
     if args.workload == "batched":
         if rank == 0:
             print(json.dumps(run_batched(args)))
+        return
+    if args.newton_only:
+        if rank == 0:
+            print(json.dumps(run_newton_only(args)))
         return
     out = run_gpu(args, rank, world, local_rank)
     if out is not None:
