@@ -236,6 +236,19 @@ def cpu_residual_jvp_rate(size: int, min_seconds: float = 8.0, step: str = "vjp"
 
 
 # ----------------------------------------------------------------------------- GPU arm
+def replica_throughput(ms: float, faces: int, steps: int, world: int, dist, device) -> tuple:
+    """The replicas' timing contract: the slowest rank's time (max over ranks) and the whole job's
+    throughput in Gfaces/s, every rank having processed `faces` faces per step (weak scaling, no
+    data-path collective)."""
+    import torch
+
+    t = torch.tensor([ms], device=device, dtype=torch.float64)
+    if dist is not None and world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms = float(t)
+    return ms, world * faces * steps / (ms * 1e-3) / 1e9
+
+
 def run_gpu(args, rank: int, world: int, local_rank: int) -> dict | None:
     import numpy as np
     import torch
@@ -285,11 +298,7 @@ def run_gpu(args, rank: int, world: int, local_rank: int) -> dict | None:
     stage_ms, runs = case.profile_end()
     if not torch.isfinite(jv).all() or not torch.isfinite(r).all():
         raise RuntimeError("non-finite residual / derivative in the benchmark step")
-    t = torch.tensor([ms], device="cuda", dtype=torch.float64)
-    if dist is not None:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms = float(t)
-    value = world * F * args.steps / (ms * 1e-3) / 1e9
+    ms, value = replica_throughput(ms, F, args.steps, world, dist, "cuda")
 
     # end to end through the C ABI with pinned host buffers (copies inside the timed region)
     h_state = state.cpu().pin_memory()
@@ -314,12 +323,9 @@ def run_gpu(args, rank: int, world: int, local_rank: int) -> dict | None:
         e2e_step()
     e1.record(stream)
     torch.cuda.synchronize()
-    e2e_ms = e0.elapsed_time(e1)
-    te = torch.tensor([e2e_ms], device="cuda", dtype=torch.float64)
+    e2e_ms, _ = replica_throughput(e0.elapsed_time(e1), F, args.steps, world, dist, "cuda")
     if dist is not None:
-        dist.all_reduce(te, op=dist.ReduceOp.MAX)
         dist.barrier()
-    e2e_ms = float(te)
     if rank != 0:
         return None
 

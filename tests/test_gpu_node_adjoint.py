@@ -21,7 +21,7 @@ def _oracle_node_grad(case, d, p, s, w):
     return g.numpy()
 
 
-@pytest.mark.parametrize("name", ["cav8", "cavj", "lam3", "sst2", "sst3"])
+@pytest.mark.parametrize("name", ["cav8", "cavj", "lam3", "sst2", "sst3", "wsst2", "bsst3"])
 def test_node_vjp_matches_oracle_autograd(name):
     fc, case, d, p = device_case(name)
     s = d[p + "states"][0 if name != "cav8" else 1]
