@@ -19,17 +19,17 @@
 // or DualF for the fp32 assembly of an fp32 preconditioner.
 template <class T>
 struct SeedSrc {
-  const double* v;
+  const decltype(T::v)* v;  // the state in the pass's precision
   long seed;
   __device__ __forceinline__ T operator()(long i) const {
-    return T{(decltype(T::v))v[i], (decltype(T::v))(i == seed ? 1 : 0)};
+    return T{v[i], (decltype(T::v))(i == seed ? 1 : 0)};
   }
 };
 
 // Keeps the tangent of flux q as D[((f * 2 + side) * NF + q) * NF + r].
 template <class T>
 struct DerivStore {
-  double* D;
+  GS<T>* D;  // fp32 for an fp32 pass
   long base;  // ((f * 2 + side) * NF) * NF + r
   long qstride;  // NF
   __device__ __forceinline__ void operator()(int q, const T& x) const {
@@ -38,9 +38,10 @@ struct DerivStore {
 };
 
 template <class T, int DIM, bool TURB>
-__global__ void __launch_bounds__(128) k_jac_face(MeshView m, CaseView cv, const double* state,
+__global__ void __launch_bounds__(128) k_jac_face(MeshView m, CaseView cv,
+                                                  const decltype(T::v)* state,
                                                   Par<T> par, const T* G, const T* cl,
-                                                  const T* dco, const T* psi, double* D) {
+                                                  const T* dco, const T* psi, GS<T>* D) {
   constexpr int NF = Layout<DIM, TURB>::NFLD;
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= m.nf) return;
@@ -59,11 +60,13 @@ __global__ void __launch_bounds__(128) k_jac_face(MeshView m, CaseView cv, const
 }
 
 template <class T, int DIM, bool TURB>
-__global__ void __launch_bounds__(128) k_jac_cell(MeshView m, CaseView cv, const double* state,
+__global__ void __launch_bounds__(128) k_jac_cell(MeshView m, CaseView cv,
+                                                  const decltype(T::v)* state,
                                                   Par<T> par, const T* G, const T* cl,
-                                                  const T* Gwi, const double* D,
+                                                  const T* Gwi, const GS<T>* __restrict__ D,
                                                   const int* indptr, const int* indices,
-                                                  double* values) {
+                                                  GS<T>* __restrict__ values) {
+  using V = GS<T>;  // the pass's precision: the sums and the stored blocks
   using L = Layout<DIM, TURB>;
   constexpr int NF = L::NFLD;
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -76,23 +79,23 @@ __global__ void __launch_bounds__(128) k_jac_cell(MeshView m, CaseView cv, const
   for (int q = 0; q < NF; ++q) skip[q] = false;
   if (c == cv.pin) skip[L::P] = true;
   if constexpr (TURB) skip[L::W] = cv.wcell[c] != 0;
-  double dg[NF][NF];
+  V dg[NF][NF];
 #pragma unroll
   for (int q = 0; q < NF; ++q)
 #pragma unroll
-    for (int r = 0; r < NF; ++r) dg[q][r] = 0.0;
+    for (int r = 0; r < NF; ++r) dg[q][r] = V(0);
   const int b = m.cf_ptr[c], e = m.cf_ptr[c + 1];
   for (int i = b; i < e; ++i) {
     const unsigned ent = m.cf_face[i];
     const int f = (int)(ent & ~FV_NB_BIT);
     const bool isnb = (ent & FV_NB_BIT) != 0;
-    const double sg = isnb ? -1.0 : 1.0;
-    const double* self = D + ((long)f * 2 + (isnb ? 1 : 0)) * NF * NF;
+    const V sg = isnb ? V(-1) : V(1);
+    const V* self = D + ((long)f * 2 + (isnb ? 1 : 0)) * NF * NF;
 #pragma unroll
     for (int q = 0; q < NF; ++q)
 #pragma unroll
       for (int r = 0; r < NF; ++r) {
-        const double x = sg * self[q * NF + r];
+        const V x = sg * self[q * NF + r];
         dg[q][r] = i == b ? x : dg[q][r] + x;
       }
     if (f < m.nfi) {
@@ -104,13 +107,19 @@ __global__ void __launch_bounds__(128) k_jac_cell(MeshView m, CaseView cv, const
           break;
         }
       if (slot >= 0) {
-        const double* oth = D + ((long)f * 2 + (isnb ? 0 : 1)) * NF * NF;
-        double* blk = values + (long)slot * NF * NF;
+        const V* oth = D + ((long)f * 2 + (isnb ? 0 : 1)) * NF * NF;
+        V* blk = values + (long)slot * NF * NF;
 #pragma unroll
         for (int q = 0; q < NF; ++q) {
           if (skip[q]) continue;
+          V o[NF], b0[NF];
 #pragma unroll
-          for (int r = 0; r < NF; ++r) blk[q * NF + r] += sg * oth[q * NF + r];
+          for (int r = 0; r < NF; ++r) {
+            o[r] = oth[q * NF + r];
+            b0[r] = blk[q * NF + r];
+          }
+#pragma unroll
+          for (int r = 0; r < NF; ++r) blk[q * NF + r] = b0[r] + sg * o[r];
         }
       }
     }
@@ -119,10 +128,10 @@ __global__ void __launch_bounds__(128) k_jac_cell(MeshView m, CaseView cv, const
   for (int q = 0; q < NF; ++q)
     if (skip[q])
 #pragma unroll
-      for (int r = 0; r < NF; ++r) dg[q][r] = 0.0;
+      for (int r = 0; r < NF; ++r) dg[q][r] = V(0);
   if (c == cv.pin) {
 #pragma unroll
-    for (int r = 0; r < NF; ++r) dg[L::P][r] = r == L::P ? 1.0 : 0.0;
+    for (int r = 0; r < NF; ++r) dg[L::P][r] = r == L::P ? V(1) : V(0);
   }
   if constexpr (TURB) {
     // only k and omega of the cell itself enter its source rows: one seeded evaluation per
@@ -139,7 +148,7 @@ __global__ void __launch_bounds__(128) k_jac_cell(MeshView m, CaseView cv, const
   }
   for (int p = bp; p < be; ++p)
     if (indices[p] == c) {
-      double* blk = values + (long)p * NF * NF;
+      V* blk = values + (long)p * NF * NF;
 #pragma unroll
       for (int q = 0; q < NF; ++q)
 #pragma unroll
@@ -150,14 +159,24 @@ __global__ void __launch_bounds__(128) k_jac_cell(MeshView m, CaseView cv, const
 
 template <class T, int DIM, bool TURB>
 int assemble_frozen(FvCase* cs, const double* state, const int* indptr, const int* indices,
-                    double* values, double* D, cudaStream_t s) {
+                    GS<T>* values, GS<T>* D, cudaStream_t s) {
   using S = decltype(T::v);
   const MeshView& m = cs->mesh->view;
   const CaseView& cv = cs->view;
   const long nc = m.nc, nf = m.nf;
   constexpr int NF = Layout<DIM, TURB>::NFLD;
   Work<T> w = work_layout<T, DIM, TURB>(cs->work, nc, nf, psi_count<DIM, TURB>(cs));
-  Src<T> st{state, nullptr};  // zero tangent: the forward stages give the frozen values
+  const S* sv;  // the state in the pass's precision
+  if constexpr (std::is_same<S, float>::value) {
+    int rc = fv_case_ensure_f32(cs, s);
+    if (rc != FV_OK) return rc;
+    rc = fv_d2f((long)NF * nc, state, cs->f_state, s);
+    if (rc != FV_OK) return rc;
+    sv = cs->f_state;
+  } else {
+    sv = state;
+  }
+  Src<T> st{sv, nullptr};  // zero tangent: the forward stages give the frozen values
   const double irho = 1.0 / cs->desc.rho;
   Par<T> par{{S(cs->mu), S(0)}, {S(cs->inlet_scale), S(0)}, {S(cs->mu * irho), S(0)}};
   constexpr int TB = 128;
@@ -169,7 +188,7 @@ int assemble_frozen(FvCase* cs, const double* state, const int* indptr, const in
   const long npsi = psi_count<DIM, TURB>(cs);
   if (npsi)
     k_limiter<T, DIM, TURB><<<bc, TB, 0, s>>>(m, st, w.G, cv.lim_km, cv.lim_ks, w.psi);
-  k_jac_face<T, DIM, TURB><<<bf, TB, 0, s>>>(m, cv, state, par, w.G, w.cl, w.dco,
+  k_jac_face<T, DIM, TURB><<<bf, TB, 0, s>>>(m, cv, sv, par, w.G, w.cl, w.dco,
                                              npsi ? w.psi : nullptr, D);
   if (cs->jac_indptr != indptr) {  // the pattern's block count, read once per pattern
     int nnzb = 0;
@@ -178,10 +197,10 @@ int assemble_frozen(FvCase* cs, const double* state, const int* indptr, const in
     cs->jac_indptr = indptr;
     cs->jac_nnzb = nnzb;
   }
-  FV_CUDA_TRY(cudaMemsetAsync(values, 0, sizeof(double) * (size_t)NF * NF * (size_t)cs->jac_nnzb,
+  FV_CUDA_TRY(cudaMemsetAsync(values, 0, sizeof(GS<T>) * (size_t)NF * NF * (size_t)cs->jac_nnzb,
                               s));
   k_jac_cell<T, DIM, TURB><<<fv_blocks(nc, TB), TB, 0, s>>>(
-      m, cv, state, par, w.G, w.cl, w.Gwi, D, indptr, indices, values);
+      m, cv, sv, par, w.G, w.cl, w.Gwi, D, indptr, indices, values);
   FV_CUDA_TRY(cudaGetLastError());
   return FV_OK;
 }

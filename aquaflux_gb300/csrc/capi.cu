@@ -58,16 +58,17 @@ __global__ void k_chain_state(long nc, int kf, int tr, const double* p, double* 
 
 // Jacobian columns of the transformed fields times phi of the column cell (BSR, nfld x nfld
 // row-major blocks, one thread per block row of cell c and field q).
+template <class V>
 __global__ void k_chain_bsr(int nc, int nfld, int kf, int tr, const int* indptr, const int* indices,
-                            const double* p, double* values) {
+                            const double* p, V* values) {
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (long)nfld * nc) return;
   const int c = (int)(t % nc), q = (int)(t / nc);
   for (int b = indptr[c]; b < indptr[c + 1]; ++b) {
     const int j = indices[b];
-    double* row = values + ((long)b * nfld + q) * nfld;
+    V* row = values + ((long)b * nfld + q) * nfld;
     for (int r = kf; r <= kf + 1; ++r)
-      if (log_field(r, kf, tr)) row[r] *= p[(long)r * nc + j];
+      if (log_field(r, kf, tr)) row[r] = (V)(row[r] * p[(long)r * nc + j]);
   }
 }
 
@@ -296,6 +297,9 @@ extern "C" int fv_case_destroy(FvCase* c) {
   cudaFree(c->red);
   cudaFree(c->phys);
   cudaFree(c->tphys);
+  cudaFree(c->f32);
+  cudaFree(c->f_state);
+  cudaFree(c->f_tangent);
   for (cudaEvent_t e : c->prof_events) cudaEventDestroy(e);
   delete c;
   return FV_OK;
@@ -478,7 +482,7 @@ extern "C" int fv_probe_jacobian(FvCase* c, const double* state, int frozen, con
 
 namespace {
 int assemble_jacobian(FvCase* c, const double* state, const int* indptr, const int* indices,
-                      double* values, int fp32, void* stream) {
+                      void* values, int fp32, void* stream) {
   if (!c || !state || !indptr || !indices || !values) {
     fv_set_error("fv_assemble_jacobian: bad arguments");
     return FV_ERR_ARG;
@@ -491,9 +495,14 @@ int assemble_jacobian(FvCase* c, const double* state, const int* indptr, const i
   int rc = fv_case_assemble_frozen(c, physical_state(c, state, s), indptr, indices, values,
                                    c->jac_face, fp32, s);
   if (rc == FV_OK && c->desc.scalar_transform) {
-    k_chain_bsr<<<fv_blocks((long)c->nfld * c->mesh->nc, 128), 128, 0, s>>>(
-        c->mesh->nc, c->nfld, c->mesh->dim + 1, c->desc.scalar_transform, indptr, indices,
-        c->phys, values);
+    if (fp32)
+      k_chain_bsr<float><<<fv_blocks((long)c->nfld * c->mesh->nc, 128), 128, 0, s>>>(
+          c->mesh->nc, c->nfld, c->mesh->dim + 1, c->desc.scalar_transform, indptr, indices,
+          c->phys, (float*)values);
+    else
+      k_chain_bsr<double><<<fv_blocks((long)c->nfld * c->mesh->nc, 128), 128, 0, s>>>(
+          c->mesh->nc, c->nfld, c->mesh->dim + 1, c->desc.scalar_transform, indptr, indices,
+          c->phys, (double*)values);
     FV_CUDA_TRY(cudaGetLastError());
   }
   return rc;
@@ -506,7 +515,7 @@ extern "C" int fv_assemble_jacobian(FvCase* c, const double* state, const int* i
 }
 
 extern "C" int fv_assemble_jacobian_f32(FvCase* c, const double* state, const int* indptr,
-                                        const int* indices, double* values, void* stream) {
+                                        const int* indices, float* values, void* stream) {
   return assemble_jacobian(c, state, indptr, indices, values, 1, stream);
 }
 

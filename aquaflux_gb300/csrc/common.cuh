@@ -133,11 +133,29 @@ FV_HD DualF operator/(double a, DualF b) {
   const float q = (float)a * r;
   return {q, -q * b.d * r};
 }
+FV_HD DualF operator+(DualF a, float b) { return {a.v + b, a.d}; }
+FV_HD DualF operator+(float a, DualF b) { return {a + b.v, b.d}; }
+FV_HD DualF operator-(DualF a, float b) { return {a.v - b, a.d}; }
+FV_HD DualF operator-(float a, DualF b) { return {a - b.v, -b.d}; }
+FV_HD DualF operator*(DualF a, float b) { return {a.v * b, a.d * b}; }
+FV_HD DualF operator*(float a, DualF b) { return {a * b.v, a * b.d}; }
+FV_HD DualF operator/(DualF a, float b) {
+  const float r = 1.0f / b;
+  return {a.v * r, a.d * r};
+}
+FV_HD DualF operator/(float a, DualF b) {
+  const float r = 1.0f / b.v;
+  const float q = a * r;
+  return {q, -q * b.d * r};
+}
 FV_HD DualF& operator+=(DualF& a, DualF b) { a = a + b; return a; }
 FV_HD DualF& operator-=(DualF& a, DualF b) { a = a - b; return a; }
 FV_HD DualF lerp(DualF a, DualF b, double g) {
   const float gf = (float)g;
   return {fmaf(gf, b.v - a.v, a.v), fmaf(gf, b.d - a.d, a.d)};
+}
+FV_HD DualF lerp(DualF a, DualF b, float g) {
+  return {fmaf(g, b.v - a.v, a.v), fmaf(g, b.d - a.d, a.d)};
 }
 FV_HD DualF lerp(DualF a, DualF b, DualF g) {
   return {fmaf(g.v, b.v - a.v, a.v), fmaf(g.v, b.d - a.d, a.d) + g.d * (b.v - a.v)};

@@ -42,6 +42,10 @@ struct MeshView {
   const double* inv_dpn;       // (nf) 1 / dpn
   const double* ns;            // (dim * dim, nf) n_j skew_q at [(j * dim + q) * nf + f]
   const double* inv_vol;       // (nc) 1 / V
+  // fp32 mirror of the geometry (same layout), for the fp32 dual-number passes; null until
+  // fv_mesh_ensure_f32 makes it
+  const float *f_area, *f_normal, *f_xf, *f_vol, *f_xc, *f_g, *f_nd, *f_dpn, *f_dnn, *f_dvec,
+      *f_skew, *f_tP, *f_tN, *f_nn2, *f_inv_nd, *f_inv_dpn, *f_ns, *f_inv_vol;
 };
 
 struct FvMesh {
@@ -60,6 +64,8 @@ struct FvMesh {
   int* face_old = nullptr;  // device copy of h_face_old
   double* nodes = nullptr;
   double* geo = nullptr;  // one allocation holding every geometry / factor array
+  size_t geo_n = 0;
+  float* geo_f = nullptr;  // its fp32 mirror (fp32 passes), kept in step with the geometry
   double* approx = nullptr;  // (dim, nc) approximate centroids (work)
   MeshView view;
 };
@@ -88,6 +94,9 @@ struct CaseView {
   const double* inv_wd2;      // (nc) 1 / wall distance^2
   const double* mu_cell;      // (nc) per-cell molecular viscosity (laminar), or null
   int log_w;                  // the omega fixation row is the log ratio (log-solved omega)
+  // fp32 copies for the fp32 dual-number passes (null until made)
+  const float *f_wd, *f_wdg, *f_inv_wd, *f_inv_wd2, *f_mu_cell;
+  float f_rho;
   int rec_mom, rec_sca;       // linear-upwind reconstruction of the momentum / the k, omega faces
   double lim_km, lim_ks;      // their Venkatakrishnan constants (0: unlimited, psi = 1)
 };
@@ -138,6 +147,9 @@ struct FvCase {
   bool flx_active = false;      // the adjoints add flx to their face-flux cotangents
   bool flx_viscous = false;     // ... with the pressure part p_f A n_i taken out
   double* red = nullptr;        // reduction partials of the functional
+  float* f32 = nullptr;         // fp32 copies: wd, wdg, 1/wd, 1/wd^2, per-cell viscosity
+  float* f_state = nullptr;     // (n_unknowns) fp32 state of an fp32 pass
+  float* f_tangent = nullptr;   // (n_unknowns) fp32 tangent of an fp32 pass
   double* phys = nullptr;       // (n_unknowns) physical state of a log-transformed case
   double* tphys = nullptr;      // (n_unknowns) physical tangent of a log-transformed case
   CaseView view;
@@ -153,6 +165,10 @@ struct FvCase {
 void fv_prof_mark(FvCase* c, int k, cudaStream_t s);
 void fv_prof_end_run(FvCase* c);
 
+// fp32 mirrors for the fp32 dual-number passes (made on first use)
+int fv_d2f(long n, const double* in, float* out, cudaStream_t s);
+int fv_mesh_ensure_f32(FvMesh* m, cudaStream_t s);
+int fv_case_ensure_f32(FvCase* c, cudaStream_t s);
 int fv_case_run(FvCase* c, const double* state, const double* tangent, int tangent_kind,
                 double* residual, double* jv, cudaStream_t s);
 int fv_case_vjp_run(FvCase* c, const double* state, const double* w, double* residual, double* out,
@@ -169,7 +185,7 @@ int fv_case_face_functional(FvCase* c, const double* state, const double* weight
                             int viscous_only, double* value, double* dstate, double* dparams,
                             double* dnodes, cudaStream_t s);
 int fv_case_assemble_frozen(FvCase* c, const double* state, const int* indptr, const int* indices,
-                            double* values, double* D, int fp32, cudaStream_t s);
+                            void* values, void* D, int fp32, cudaStream_t s);
 size_t fv_jac_face_bytes(int dim, int turb, long nf);
 enum { FV_TAN_NONE = 0, FV_TAN_STATE = 1, FV_TAN_MU = 2, FV_TAN_INLET = 3, FV_TAN_FROZEN = 4,
        FV_TAN_STATE32 = 5, FV_TAN_FROZEN32 = 6 };  // 32: the tangent pass in fp32 (DualF)

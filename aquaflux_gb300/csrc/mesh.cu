@@ -426,6 +426,7 @@ extern "C" int fv_mesh_create(int dim, int n_cells, int n_faces, int n_nodes, co
   // + vol (nc) + xc (dim nc)
   size_t geo_n = 8 * nf + 6 * (size_t)dim * nf + (size_t)dim * dim * nf + 2 * nc +
                  (size_t)dim * nc;
+  m->geo_n = geo_n;
   FV_CUDA_TRY(cudaMalloc(&m->geo, sizeof(double) * geo_n));
   FV_CUDA_TRY(cudaMemcpyAsync(m->owner, m->h_owner.data(), sizeof(int) * nf, cudaMemcpyHostToDevice, s));
   FV_CUDA_TRY(cudaMemcpyAsync(m->nb, m->h_nb.data(), sizeof(int) * nf, cudaMemcpyHostToDevice, s));
@@ -488,9 +489,50 @@ extern "C" int fv_mesh_destroy(FvMesh* m) {
   cudaFree(m->face_old);
   cudaFree(m->nodes);
   cudaFree(m->geo);
+  cudaFree(m->geo_f);
   cudaFree(m->approx);
   delete m;
   return FV_OK;
+}
+
+__global__ void k_to_f32(long n, const double* in, float* out) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (float)in[i];
+}
+
+int fv_d2f(long n, const double* in, float* out, cudaStream_t s) {
+  if (n <= 0) return FV_OK;
+  k_to_f32<<<fv_blocks(n, kThreads), kThreads, 0, s>>>(n, in, out);
+  FV_CUDA_TRY(cudaGetLastError());
+  return FV_OK;
+}
+
+// The fp32 mirror of the geometry block (same layout), made on first use and refreshed whenever
+// the geometry is recomputed.
+int fv_mesh_ensure_f32(FvMesh* m, cudaStream_t s) {
+  if (m->geo_f) return FV_OK;
+  FV_CUDA_TRY(cudaMalloc(&m->geo_f, sizeof(float) * m->geo_n));
+  MeshView& v = m->view;
+  auto mirror = [&](const double* p) { return (const float*)(m->geo_f + (p - m->geo)); };
+  v.f_area = mirror(v.area);
+  v.f_normal = mirror(v.normal);
+  v.f_xf = mirror(v.xf);
+  v.f_vol = mirror(v.vol);
+  v.f_xc = mirror(v.xc);
+  v.f_g = mirror(v.g);
+  v.f_nd = mirror(v.nd);
+  v.f_dpn = mirror(v.dpn);
+  v.f_dnn = mirror(v.dnn);
+  v.f_dvec = mirror(v.dvec);
+  v.f_skew = mirror(v.skew);
+  v.f_tP = mirror(v.tP);
+  v.f_tN = mirror(v.tN);
+  v.f_nn2 = mirror(v.nn2);
+  v.f_inv_nd = mirror(v.inv_nd);
+  v.f_inv_dpn = mirror(v.inv_dpn);
+  v.f_ns = mirror(v.ns);
+  v.f_inv_vol = mirror(v.inv_vol);
+  return fv_d2f((long)m->geo_n, m->geo, m->geo_f, s);
 }
 
 extern "C" int fv_mesh_set_nodes(FvMesh* m, const double* nodes_device, void* stream) {
@@ -501,7 +543,9 @@ extern "C" int fv_mesh_set_nodes(FvMesh* m, const double* nodes_device, void* st
   cudaStream_t s = (cudaStream_t)stream;
   FV_CUDA_TRY(cudaMemcpyAsync(m->nodes, nodes_device, sizeof(double) * (size_t)m->nn * m->dim,
                               cudaMemcpyDeviceToDevice, s));
-  return fv_mesh_compute_geometry(m, s);
+  int rc = fv_mesh_compute_geometry(m, s);
+  if (rc == FV_OK && m->geo_f) rc = fv_d2f((long)m->geo_n, m->geo, m->geo_f, s);
+  return rc;
 }
 
 extern "C" int fv_mesh_geometry(const FvMesh* m, double* area, double* normal,

@@ -40,6 +40,25 @@ struct SstConst {
 };
 __constant__ SstConst c_sst;
 
+// fp32 passes (T = DualF) read the fp32 mirrors of the geometry and of the state, so that their
+// arithmetic stays off the fp64 pipe; GS<T> is the scalar type of the geometry a pass reads.
+template <class T>
+struct IsF32 : std::false_type {};
+template <>
+struct IsF32<DualF> : std::true_type {};
+template <class T>
+using GS = typename std::conditional<IsF32<T>::value, float, double>::type;
+template <class T>
+__device__ __forceinline__ GS<T> gx(const double* d, const float* f, long i) {
+  if constexpr (IsF32<T>::value) return f[i];
+  else return d[i];
+}
+template <class T>
+__device__ __forceinline__ GS<T> rho_of(const CaseView& cv) {
+  if constexpr (IsF32<T>::value) return cv.f_rho;
+  else return cv.rho;
+}
+
 template <class T>
 struct Src;
 template <>
@@ -55,11 +74,9 @@ struct Src<Dual> {
 };
 template <>
 struct Src<DualF> {
-  const double* v;
-  const double* t;  // may be null: zero tangent
-  __device__ __forceinline__ DualF operator()(long i) const {
-    return {(float)v[i], t ? (float)t[i] : 0.0f};
-  }
+  const float* v;  // the fp32 copy of the state
+  const float* t;  // of the tangent; may be null: zero tangent
+  __device__ __forceinline__ DualF operator()(long i) const { return {v[i], t ? t[i] : 0.0f}; }
 };
 
 template <class T>
@@ -215,6 +232,58 @@ struct GeoPlain {
   }
 };
 
+// The fp32 mirror (fp32 passes).
+struct GeoPlainF {
+  __device__ __forceinline__ float area(const MeshView& m, int f) const { return m.f_area[f]; }
+  __device__ __forceinline__ float normal(const MeshView& m, int j, int f) const {
+    return m.f_normal[(long)j * m.nf + f];
+  }
+  __device__ __forceinline__ float tP(const MeshView& m, int j, int f) const {
+    return m.f_tP[(long)j * m.nf + f];
+  }
+  __device__ __forceinline__ float tN(const MeshView& m, int j, int f) const {
+    return m.f_tN[(long)j * m.nf + f];
+  }
+  __device__ __forceinline__ float g(const MeshView& m, int f) const { return m.f_g[f]; }
+  __device__ __forceinline__ float dvec(const MeshView& m, int j, int f) const {
+    return m.f_dvec[(long)j * m.nf + f];
+  }
+  __device__ __forceinline__ float skew(const MeshView& m, int j, int f) const {
+    return m.f_skew[(long)j * m.nf + f];
+  }
+  __device__ __forceinline__ float nn2(const MeshView& m, int f) const { return m.f_nn2[f]; }
+  __device__ __forceinline__ float inv_nd(const MeshView& m, int f) const { return m.f_inv_nd[f]; }
+  __device__ __forceinline__ float inv_dpn(const MeshView& m, int f) const {
+    return m.f_inv_dpn[f];
+  }
+  __device__ __forceinline__ float dpn(const MeshView& m, int f) const { return m.f_dpn[f]; }
+  __device__ __forceinline__ float dnn(const MeshView& m, int f) const { return m.f_dnn[f]; }
+  __device__ __forceinline__ float ns(const MeshView& m, int jq, int f) const {
+    return m.f_ns[(long)jq * m.nf + f];
+  }
+  __device__ __forceinline__ float vol(const MeshView& m, int c) const { return m.f_vol[c]; }
+  __device__ __forceinline__ float wd(const CaseView& cv, int c) const { return cv.f_wd[c]; }
+  __device__ __forceinline__ float inv_wd(const CaseView& cv, int c) const {
+    return cv.f_inv_wd[c];
+  }
+  __device__ __forceinline__ float inv_wd2(const CaseView& cv, int c) const {
+    return cv.f_inv_wd2[c];
+  }
+  __device__ __forceinline__ float wdg(const CaseView& cv, int nc, int j, int c) const {
+    return cv.f_wdg[(long)j * nc + c];
+  }
+};
+
+// The plain accessor of a pass's scalar type.
+template <class T>
+struct GeoOf {
+  using type = GeoPlain;
+};
+template <>
+struct GeoOf<DualF> {
+  using type = GeoPlainF;
+};
+
 struct GeoSeed {
   int fcomp;  // seeded face component (GeoFace), -1 for none
   int ccomp;  // seeded cell component (GeoCell), -1 for none
@@ -357,13 +426,14 @@ __global__ void __launch_bounds__(128) k_grad(MeshView m, CaseView cv, Src<T> st
     const unsigned ent = m.cf_face[i];
     const int f = (int)(ent & ~FV_NB_BIT);
     const bool isnb = (ent & FV_NB_BIT) != 0;
-    const double A = isnb ? -m.area[f] : m.area[f];  // the neighbour takes -S_f phi_f
-    double S[DIM];
+    const GS<T> af = gx<T>(m.area, m.f_area, f);
+    const GS<T> A = isnb ? -af : af;  // the neighbour takes -S_f phi_f
+    GS<T> S[DIM];
 #pragma unroll
-    for (int j = 0; j < DIM; ++j) S[j] = m.normal[(long)j * nf + f] * A;
+    for (int j = 0; j < DIM; ++j) S[j] = gx<T>(m.normal, m.f_normal, (long)j * nf + f) * A;
     T phif[NF];
     if (f < m.nfi) {
-      const double g = m.g[f];
+      const GS<T> g = gx<T>(m.g, m.f_g, f);
       const int other = isnb ? m.owner[f] : m.nb[f];
 #pragma unroll
       for (int q = 0; q < NF; ++q) {
@@ -386,7 +456,7 @@ __global__ void __launch_bounds__(128) k_grad(MeshView m, CaseView cv, Src<T> st
 #pragma unroll
       for (int j = 0; j < DIM; ++j) acc[q][j] += S[j] * phif[q];
   }
-  const double inv = m.inv_vol[c];
+  const GS<T> inv = gx<T>(m.inv_vol, m.f_inv_vol, c);
   if (Bg) {
 #pragma unroll
     for (int q = 0; q < NF; ++q)
@@ -421,10 +491,10 @@ __global__ void __launch_bounds__(128) k_gg_skew(MeshView m, const T* X, T* w) {
   if (f >= m.nfi) return;
   const int nc = m.nc, nf = m.nf;
   const int o = m.owner[f], n = m.nb[f];
-  const double g = m.g[f];
-  double sk[DIM];
+  const GS<T> g = gx<T>(m.g, m.f_g, f);
+  GS<T> sk[DIM];
 #pragma unroll
-  for (int j = 0; j < DIM; ++j) sk[j] = m.skew[(long)j * nf + f];
+  for (int j = 0; j < DIM; ++j) sk[j] = gx<T>(m.skew, m.f_skew, (long)j * nf + f);
 #pragma unroll
   for (int q = 0; q < NQ; ++q) {
     T so = sk[0] * X[((long)q * DIM) * nc + o];
@@ -434,7 +504,7 @@ __global__ void __launch_bounds__(128) k_gg_skew(MeshView m, const T* X, T* w) {
       so = so + sk[j] * X[((long)q * DIM + j) * nc + o];
       sn = sn + sk[j] * X[((long)q * DIM + j) * nc + n];
     }
-    w[(long)q * nf + f] = (1.0 - g) * so + g * sn;
+    w[(long)q * nf + f] = (GS<T>(1) - g) * so + g * sn;
   }
 }
 
@@ -452,19 +522,20 @@ __global__ void __launch_bounds__(128) k_gg_sweep(MeshView m, const T* Bg, const
     const unsigned ent = m.cf_face[i];
     const int f = (int)(ent & ~FV_NB_BIT);
     if (f >= m.nfi) continue;  // the correction vanishes on boundary faces
-    const double A = (ent & FV_NB_BIT) ? -m.area[f] : m.area[f];
+    const GS<T> af = gx<T>(m.area, m.f_area, f);
+    const GS<T> A = (ent & FV_NB_BIT) ? -af : af;
 #pragma unroll
     for (int q = 0; q < NQ; ++q) {
       const T wq = w[(long)q * nf + f];
 #pragma unroll
       for (int j = 0; j < DIM; ++j) {
-        const T x = (m.normal[(long)j * nf + f] * A) * wq;
+        const T x = (gx<T>(m.normal, m.f_normal, (long)j * nf + f) * A) * wq;
         corr[q][j] = first ? x : corr[q][j] + x;
       }
     }
     first = false;
   }
-  const double V = m.vol[c], inv = m.inv_vol[c];
+  const GS<T> V = gx<T>(m.vol, m.f_vol, c), inv = gx<T>(m.inv_vol, m.f_inv_vol, c);
 #pragma unroll
   for (int q = 0; q < NQ; ++q)
 #pragma unroll
@@ -591,7 +662,7 @@ __global__ void __launch_bounds__(128) k_closure(MeshView m, CaseView cv, Src<T>
   if (c >= m.nc) return;
   const int nc = m.nc;
   T out[7], gw[DIM];
-  closure_cell<T, DIM>(m, cv, st, par, G, c, GeoPlain{}, out, gw);
+  closure_cell<T, DIM>(m, cv, st, par, G, c, typename GeoOf<T>::type{}, out, gw);
 #pragma unroll
   for (int i = 0; i < 7; ++i) cl[(long)i * nc + c] = out[i];
 #pragma unroll
@@ -608,10 +679,10 @@ __device__ __forceinline__ Dual mu_at(const Par<Dual>& par, const CaseView& cv, 
   return cv.mu_cell ? Dual{cv.mu_cell[c], par.mu.d} : par.mu;
 }
 __device__ __forceinline__ DualF mu_at(const Par<DualF>& par, const CaseView& cv, int c) {
-  return cv.mu_cell ? DualF{(float)cv.mu_cell[c], par.mu.d} : par.mu;
+  return cv.mu_cell ? DualF{cv.f_mu_cell[c], par.mu.d} : par.mu;
 }
 template <class T, bool TURB>
-__device__ __forceinline__ T mu_eff(const Par<T>& par, const CaseView& cv, double rho, const T* cl,
+__device__ __forceinline__ T mu_eff(const Par<T>& par, const CaseView& cv, GS<T> rho, const T* cl,
                                     int nc, int c) {
   if (TURB) return par.mu + rho * cl[2L * nc + c];
   return mu_at(par, cv, c);
@@ -620,7 +691,7 @@ __device__ __forceinline__ T mu_eff(const Par<T>& par, const CaseView& cv, doubl
 // lagged advective momentum flux (rho u)_f . n with the skew-corrected face value
 // (aquaflux/flow/rhie_chow.py:220-271): rho (sum_j n_j u_j,f + sum_jq n_j skew_q (grad u)_jq,f)
 template <class T, int DIM, bool TURB, class S, class GV, class GT>
-__device__ __forceinline__ T mom_normal(const MeshView& m, const S& st, const T* G, double rho,
+__device__ __forceinline__ T mom_normal(const MeshView& m, const S& st, const T* G, GS<T> rho,
                                         int f, int o, int n, GT g, const GV& gv) {
   const int nc = m.nc;
   T mn = cst(0.0, st(o));
@@ -663,13 +734,15 @@ __device__ __forceinline__ T limiter_cell(const MeshView& m, int c, double K, co
     pmax = fv_max(pmax, po);
     pmin = fv_min(pmin, po);
   }
-  const double e2 = m.vol[c] * (K * K * K);
+  const GS<T> e2 = gx<T>(m.vol, m.f_vol, c) * GS<T>(K * K * K);
   T psi = cst(1.0, pc);
   for (int i = b; i < e; ++i) {
     const int f = (int)(m.cf_face[i] & ~FV_NB_BIT);
-    T dm = grad(0) * (m.xf[f] - m.xc[c]);
+    T dm = grad(0) * (gx<T>(m.xf, m.f_xf, f) - gx<T>(m.xc, m.f_xc, c));
 #pragma unroll
-    for (int j = 1; j < DIM; ++j) dm = dm + grad(j) * (m.xf[(long)j * nf + f] - m.xc[(long)j * nc + c]);
+    for (int j = 1; j < DIM; ++j)
+      dm = dm + grad(j) * (gx<T>(m.xf, m.f_xf, (long)j * nf + f) -
+                           gx<T>(m.xc, m.f_xc, (long)j * nc + c));
     const double sign = val(dm) >= 0.0 ? 1.0 : -1.0;
     dm = sign * (fv_abs(dm) + 1e-12);
     const T head = val(dm) > 0.0 ? pmax - pc : pmin - pc;
@@ -718,10 +791,11 @@ __device__ __forceinline__ T upwind_rec(const MeshView& m, const T* G, const T* 
                                         int f, int cu, const T& value) {
   if (!psi) return value;
   const int nc = m.nc, nf = m.nf;
-  T d = G[((long)q * DIM) * nc + cu] * (m.xf[f] - m.xc[cu]);
+  T d = G[((long)q * DIM) * nc + cu] * (gx<T>(m.xf, m.f_xf, f) - gx<T>(m.xc, m.f_xc, cu));
 #pragma unroll
   for (int j = 1; j < DIM; ++j)
-    d = d + G[((long)q * DIM + j) * nc + cu] * (m.xf[(long)j * nf + f] - m.xc[(long)j * nc + cu]);
+    d = d + G[((long)q * DIM + j) * nc + cu] *
+                (gx<T>(m.xf, m.f_xf, (long)j * nf + f) - gx<T>(m.xc, m.f_xc, (long)j * nc + cu));
   return value + psi[(long)a * nc + cu] * d;
 }
 
@@ -739,7 +813,7 @@ __device__ __forceinline__ void apcoef_face(const MeshView& m, const CaseView& c
   const bool interior = f < m.nfi;
   const int n = interior ? m.nb[f] : o;
   const GT g = gv.g(m, f), A = gv.area(m, f);
-  const double rho = cv.rho;
+  const GS<T> rho = rho_of<T>(cv);
   const T mdot = mom_normal<T, DIM, TURB>(m, st, G, rho, f, o, n, g, gv) * A;
   me = mdot;
   const T mo = mu_eff<T, TURB>(par, cv, rho, cl, nc, o);
@@ -770,7 +844,7 @@ __global__ void __launch_bounds__(128) k_apcoef(MeshView m, CaseView cv, Src<T> 
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= m.nf) return;
   T ao, an, mf;
-  apcoef_face<T, DIM, TURB>(m, cv, st, par, G, cl, f, GeoPlain{}, ao, an, mf);
+  apcoef_face<T, DIM, TURB>(m, cv, st, par, G, cl, f, typename GeoOf<T>::type{}, ao, an, mf);
   ac_own[f] = ao;
   ac_nb[f] = an;
   me[f] = mf;
@@ -789,7 +863,7 @@ __global__ void k_dcoeff(MeshView m, const T* ac_own, const T* ac_nb, T* dco) {
     T x = (ent & FV_NB_BIT) ? ac_nb[f] : ac_own[f];
     a = i == b ? x : a + x;
   }
-  dco[c] = m.vol[c] / a;
+  dco[c] = gx<T>(m.vol, m.f_vol, c) / a;
 }
 
 // ---------------------------------------------------------------- k_flux
@@ -805,7 +879,7 @@ struct Aux {
 
 // The fluxes of face f, handed to wr(q, flux_q) for every field q.  `st` reads the state (Src, or
 // a seeded accessor in the Jacobian assembly); aux (double only) receives the face intermediates.
-template <class T, int DIM, bool TURB, class S, class Wr, class GV = GeoPlain>
+template <class T, int DIM, bool TURB, class S, class Wr, class GV = typename GeoOf<T>::type>
 __device__ __forceinline__ void flux_face(const MeshView& m, const CaseView& cv, const S& st,
                                           const Par<T>& par, const T* G, const T* cl, const T* dco,
                                           const T* me, const T* psi, bool recompute_me, int f,
@@ -816,7 +890,7 @@ __device__ __forceinline__ void flux_face(const MeshView& m, const CaseView& cv,
   const int nc = m.nc, nf = m.nf;
   const int o = m.owner[f];
   const GT A = gv.area(m, f);
-  const double rho = cv.rho, irho = 1.0 / cv.rho;
+  const GS<T> rho = rho_of<T>(cv), irho = GS<T>(1) / rho;
   GT nrm[DIM], tP[DIM];
 #pragma unroll
   for (int j = 0; j < DIM; ++j) {
@@ -997,7 +1071,7 @@ __global__ void __launch_bounds__(128) k_flux(MeshView m, CaseView cv, Src<T> st
 // ---------------------------------------------------------------- k_sum
 // SST rows of cell c: k and omega source terms added to the face sums rk / rw, and the omega
 // wall-cell fixation (aquaflux/turbulence/sources.py:60-412, fixed_value.py:124-158).
-template <class T, int DIM, class Acc, class GV = GeoPlain>
+template <class T, int DIM, class Acc, class GV = typename GeoOf<T>::type>
 __device__ __forceinline__ void sst_rows(const MeshView& m, const CaseView& cv, const Acc& st,
                                          const Par<T>& par, const T* cl, const T* G, const T* Gwi,
                                          int c, T& rk, T& rw, const GV& gv = GV{}) {
@@ -1147,10 +1221,16 @@ int dispatch_t(FvCase* cs, const double* state, const double* tangent, int kind,
         cs, Src<double>{state}, Par<double>{cs->mu, cs->inlet_scale, cs->mu * irho}, R, nullptr, s);
   }
   if (kind == FV_TAN_STATE32 || kind == FV_TAN_FROZEN32) {
+    constexpr int NF = Layout<DIM, TURB>::NFLD;
+    const long n = (long)NF * cs->mesh->nc;
+    int rc = fv_case_ensure_f32(cs, s);
+    if (rc == FV_OK) rc = fv_d2f(n, state, cs->f_state, s);
+    if (rc == FV_OK && tangent) rc = fv_d2f(n, tangent, cs->f_tangent, s);
+    if (rc != FV_OK) return rc;
     Par<DualF> pf{{(float)cs->mu, 0.0f}, {(float)cs->inlet_scale, 0.0f},
                   {(float)(cs->mu * irho), 0.0f}};
-    return run<DualF, DIM, TURB>(cs, Src<DualF>{state, tangent}, pf, R, JV, s,
-                                 kind == FV_TAN_FROZEN32);
+    return run<DualF, DIM, TURB>(cs, Src<DualF>{cs->f_state, tangent ? cs->f_tangent : nullptr},
+                                 pf, R, JV, s, kind == FV_TAN_FROZEN32);
   }
   const double dmu = kind == FV_TAN_MU ? 1.0 : 0.0;
   Par<Dual> par{{cs->mu, dmu}, {cs->inlet_scale, kind == FV_TAN_INLET ? 1.0 : 0.0},
@@ -1282,17 +1362,19 @@ size_t fv_jac_face_bytes(int dim, int turb, long nf) {
 }
 
 int fv_case_assemble_frozen(FvCase* cs, const double* state, const int* indptr,
-                            const int* indices, double* values, double* D, int fp32,
+                            const int* indices, void* values, void* D, int fp32,
                             cudaStream_t s) {
   const int dim = cs->mesh->dim;
   const bool turb = cs->desc.turbulent != 0;
   auto go = [&](auto t) {
     using T = decltype(t);
+    GS<T>* v = (GS<T>*)values;
+    GS<T>* d = (GS<T>*)D;
     if (dim == 2)
-      return turb ? assemble_frozen<T, 2, true>(cs, state, indptr, indices, values, D, s)
-                  : assemble_frozen<T, 2, false>(cs, state, indptr, indices, values, D, s);
-    return turb ? assemble_frozen<T, 3, true>(cs, state, indptr, indices, values, D, s)
-                : assemble_frozen<T, 3, false>(cs, state, indptr, indices, values, D, s);
+      return turb ? assemble_frozen<T, 2, true>(cs, state, indptr, indices, v, d, s)
+                  : assemble_frozen<T, 2, false>(cs, state, indptr, indices, v, d, s);
+    return turb ? assemble_frozen<T, 3, true>(cs, state, indptr, indices, v, d, s)
+                : assemble_frozen<T, 3, false>(cs, state, indptr, indices, v, d, s);
   };
   return fp32 ? go(DualF{}) : go(Dual{});
 }
@@ -1316,6 +1398,34 @@ int fv_residual_init_constants() {
   h.ylam = y;
   FV_CUDA_TRY(cudaMemcpyToSymbol(c_sst, &h, sizeof(h)));
   g_const_ready = true;
+  return FV_OK;
+}
+
+int fv_case_ensure_f32(FvCase* c, cudaStream_t s) {
+  FvMesh* m = c->mesh;
+  int rc = fv_mesh_ensure_f32(m, s);
+  if (rc != FV_OK) return rc;
+  const long nc = m->nc, dim = m->dim;
+  if (!c->f32) {
+    // wd (nc), wdg (dim nc), 1/wd and 1/wd^2 (2 nc), per-cell viscosity (nc)
+    FV_CUDA_TRY(cudaMalloc(&c->f32, sizeof(float) * (size_t)(nc * (4 + dim))));
+    FV_CUDA_TRY(cudaMalloc(&c->f_state, sizeof(float) * (size_t)c->nfld * nc));
+    FV_CUDA_TRY(cudaMalloc(&c->f_tangent, sizeof(float) * (size_t)c->nfld * nc));
+    float* p = c->f32;
+    if ((rc = fv_d2f(nc, c->wd, p, s)) != FV_OK) return rc;
+    if ((rc = fv_d2f(dim * nc, c->wdg, p + nc, s)) != FV_OK) return rc;
+    if ((rc = fv_d2f(2 * nc, c->inv_wd, p + (1 + dim) * nc, s)) != FV_OK) return rc;
+    CaseView& v = c->view;
+    v.f_wd = p;
+    v.f_wdg = p + nc;
+    v.f_inv_wd = p + (1 + dim) * nc;
+    v.f_inv_wd2 = p + (2 + dim) * nc;
+    v.f_rho = (float)c->desc.rho;
+  }
+  if (c->mu_cell) {  // the per-cell viscosity can change between calls
+    if ((rc = fv_d2f(nc, c->mu_cell, c->f32 + (3 + dim) * nc, s)) != FV_OK) return rc;
+    c->view.f_mu_cell = c->f32 + (3 + dim) * nc;
+  }
   return FV_OK;
 }
 

@@ -51,7 +51,7 @@ class BlockJacobian:
         self.case = case
         if precision not in (32, 64):
             raise ValueError(f"precision must be 64 or 32, got {precision}")
-        self.precision = precision  # arithmetic of the direct assembly (values stored in fp64)
+        self.precision = precision  # arithmetic and storage of the direct assembly
         mesh = case.dmesh.mesh
         self.n = mesh.n_cells
         self.b = case.n_unknowns // self.n
@@ -71,11 +71,15 @@ class BlockJacobian:
             method = "assemble" if (frozen and reach == 1) else "probe"
         if method == "assemble" and not (frozen and reach == 1):
             raise ValueError("direct assembly builds the frozen reach-1 Jacobian only")
+        if precision == 32 and method != "assemble":
+            raise ValueError("the fp32 Jacobian is built by direct assembly only")
         self.method = method
         self._colouring = None
         self.d_indptr = torch.tensor(self.indptr, device="cuda")
         self.d_indices = torch.tensor(self.indices, device="cuda")
-        self.values = torch.zeros(self.nnzb * self.b * self.b, dtype=torch.float64, device="cuda")
+        # fp32 assembly stores fp32 blocks (the fp32 preconditioner's own precision)
+        self.values = torch.zeros(self.nnzb * self.b * self.b, device="cuda",
+                                  dtype=torch.float32 if precision == 32 else torch.float64)
 
     @property
     def colouring(self):

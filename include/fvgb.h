@@ -173,11 +173,12 @@ int fv_probe_jacobian(FvCase* c, const double* state, int frozen, const int* col
 int fv_assemble_jacobian(FvCase* c, const double* state, const int* indptr, const int* indices,
                          double* values, void* stream);
 /* The same assembly, and the same JVP as fv_jvp, evaluated in fp32 arithmetic (single-precision
- * dual numbers; fp64 state in, fp64 values out): the Jacobian of an fp32 preconditioner and the
- * Krylov operator of a mixed-precision Newton, whose defect R stays fp64.  Agree with the fp64
- * forms to fp32 rounding (~1e-6 relative). */
+ * dual numbers on fp32 copies of the geometry and the state; fp64 state in; fp32 block values
+ * out, fp64 jv out): the Jacobian of an fp32 preconditioner and the Krylov operator of a
+ * mixed-precision Newton, whose defect R stays fp64.  Agree with the fp64 forms to fp32 rounding
+ * (~1e-6 relative). */
 int fv_assemble_jacobian_f32(FvCase* c, const double* state, const int* indptr, const int* indices,
-                             double* values, void* stream);
+                             float* values, void* stream);
 int fv_jvp_f32(FvCase* c, const double* state, const double* v, double* jv, void* stream);
 /* jv = J v + shift * v (the pseudo-transient operator of aquaflux/solve/continuation.py:111-112);
  * `shift` is a device vector of the state's length. */
