@@ -76,6 +76,7 @@ SIGNATURES = {
     "fv_saturation_colouring": (c_int, [c_int, P, P, P, P]),
     "fv_greedy_colouring": (c_int, [c_int, P, P, P, P]),
     "fv_coarsen": (c_int, [c_int, P, P, P, c_int, P, P, P, P, P, P, P]),
+    "fv_colour_aggregates": (c_int, [c_int, P, P, P, c_int, P, P]),
     "fv_cell_pattern": (c_int, [c_int, c_long, P, P, P, P]),
     "fv_aggregate": (c_int, [c_int, P, P, P, P]),
     "fv_galerkin_f32": (c_int, [c_long, c_int, P, P, P, c_int, P, P]),

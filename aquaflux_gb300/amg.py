@@ -74,7 +74,7 @@ def plan_hierarchy(n, indptr, indices, *, min_cells: int = 4000, max_levels: int
     One entry per coarsening: ``agg`` (fine cell -> aggregate), ``mptr``/``mlist`` (members of
     each aggregate), the coarse pattern ``indptr``/``indices`` and, per coarse block, the ordered
     list of fine blocks summed into it (``gptr``/``glist``).  With ``coarse_order="colour"`` the
-    aggregates are numbered colour by colour (distance-1 colouring of the coarse graph): rows of
+    aggregates are numbered colour by colour (first-fit colouring of the aggregate graph): rows of
     one colour are independent, so the coarse ILU(0) sweeps need as many level sets as there are
     colours instead of hundreds.
     """
@@ -89,12 +89,11 @@ def plan_hierarchy(n, indptr, indices, *, min_cells: int = 4000, max_levels: int
         if na >= n * 0.9:  # aggregation stalled
             break
         if coarse_order == "colour":
-            step = _coarsen(n, ip, ix, agg, na, lists=False)
             col = np.empty(na, dtype=np.int32)
             nco = ctypes.c_int(0)
-            check(lib().fv_saturation_colouring(na, ptr(step["indptr"]), ptr(step["indices"]),
-                                                ptr(col), ctypes.byref(nco)))
-            order = np.argsort(col, kind="stable")
+            check(lib().fv_colour_aggregates(n, ptr(ip), ptr(ix), ptr(agg), na, ptr(col),
+                                             ctypes.byref(nco)))
+            order = np.concatenate([np.flatnonzero(col == c) for c in range(nco.value)])
             newid = np.empty(na, dtype=np.int32)
             newid[order] = np.arange(na, dtype=np.int32)
             agg = newid[agg]
@@ -233,7 +232,8 @@ class AmgPreconditioner:
             nco = ctypes.c_int(0)
             check(lib().fv_greedy_colouring(n, ptr(indptr), ptr(indices), ptr(col),
                                             ctypes.byref(nco)))
-            perm = np.argsort(col, kind="stable").astype(np.int32)
+            perm = np.concatenate([np.flatnonzero(col == c)
+                                   for c in range(nco.value)]).astype(np.int32)
             pip = np.empty(n + 1, dtype=np.int32)
             pix = np.empty(int(indptr[-1]), dtype=np.int32)
             bmap = np.empty(int(indptr[-1]), dtype=np.int64)

@@ -65,6 +65,52 @@ extern "C" int fv_aggregate(int n, const int* indptr, const int* indices, int* a
   return FV_OK;
 }
 
+// First-fit greedy colouring of the aggregates (aggregate graph: two aggregates adjacent when a
+// fine block couples their cells), aggregates in index order, read straight from the fine
+// pattern: the colour numbering of the coarse levels without forming the coarse pattern first.
+extern "C" int fv_colour_aggregates(int n, const int* indptr, const int* indices, const int* agg,
+                                    int na, int* colour, int* n_colours) {
+  if (n <= 0 || na <= 0 || !indptr || !indices || !agg || !colour) {
+    fv_set_error("fv_colour_aggregates: bad arguments");
+    return FV_ERR_ARG;
+  }
+  std::vector<int> cnt(na + 1, 0), members(n);
+  for (int i = 0; i < n; ++i) {
+    if (agg[i] < 0 || agg[i] >= na) {
+      fv_set_error("fv_colour_aggregates: aggregate index out of range at cell %d", i);
+      return FV_ERR_ARG;
+    }
+    ++cnt[agg[i] + 1];
+  }
+  for (int a = 0; a < na; ++a) cnt[a + 1] += cnt[a];
+  {
+    std::vector<int> fill(cnt.begin(), cnt.end() - 1);
+    for (int i = 0; i < n; ++i) members[fill[agg[i]]++] = i;
+  }
+  for (int a = 0; a < na; ++a) colour[a] = -1;
+  std::vector<int> seen(64, -1);
+  int ncol = 0;
+  for (int a = 0; a < na; ++a) {
+    for (int m = cnt[a]; m < cnt[a + 1]; ++m) {
+      const int i = members[m];
+      for (int q = indptr[i]; q < indptr[i + 1]; ++q) {
+        const int b = agg[indices[q]];
+        const int c = b == a ? -1 : colour[b];
+        if (c >= 0) {
+          if (c >= (int)seen.size()) seen.resize(2 * c + 2, -1);
+          seen[c] = a;
+        }
+      }
+    }
+    int c = 0;
+    while (c < (int)seen.size() && seen[c] == a) ++c;
+    colour[a] = c;
+    if (c + 1 > ncol) ncol = c + 1;
+  }
+  if (n_colours) *n_colours = ncol;
+  return FV_OK;
+}
+
 // One coarsening step of a block pattern by an aggregation (host): members of every aggregate
 // (ascending fine index), the sorted coarse pattern, and for every coarse block the fine blocks
 // that sum into it (ascending fine block index), i.e. the Galerkin product of the piecewise-
