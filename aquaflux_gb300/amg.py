@@ -74,7 +74,7 @@ def plan_hierarchy(n, indptr, indices, *, min_cells: int = 4000, max_levels: int
     One entry per coarsening: ``agg`` (fine cell -> aggregate), ``mptr``/``mlist`` (members of
     each aggregate), the coarse pattern ``indptr``/``indices`` and, per coarse block, the ordered
     list of fine blocks summed into it (``gptr``/``glist``).  With ``coarse_order="colour"`` the
-    aggregates are numbered colour by colour (first-fit colouring of the aggregate graph): rows of
+    aggregates are numbered colour by colour (saturation colouring of the aggregate graph): rows of
     one colour are independent, so the coarse ILU(0) sweeps need as many level sets as there are
     colours instead of hundreds.
     """

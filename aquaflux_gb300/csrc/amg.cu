@@ -87,28 +87,27 @@ extern "C" int fv_colour_aggregates(int n, const int* indptr, const int* indices
     std::vector<int> fill(cnt.begin(), cnt.end() - 1);
     for (int i = 0; i < n; ++i) members[fill[agg[i]]++] = i;
   }
-  for (int a = 0; a < na; ++a) colour[a] = -1;
-  std::vector<int> seen(64, -1);
-  int ncol = 0;
+  // the aggregate graph: per aggregate the sorted distinct aggregates its members touch
+  // (itself included), i.e. the coarse pattern, built without the block lists
+  std::vector<int> cptr(na + 1, 0), cidx, mark(na, -1), row;
+  cidx.reserve((size_t)indptr[n] / 2 + na);
   for (int a = 0; a < na; ++a) {
+    row.clear();
     for (int m = cnt[a]; m < cnt[a + 1]; ++m) {
       const int i = members[m];
       for (int q = indptr[i]; q < indptr[i + 1]; ++q) {
         const int b = agg[indices[q]];
-        const int c = b == a ? -1 : colour[b];
-        if (c >= 0) {
-          if (c >= (int)seen.size()) seen.resize(2 * c + 2, -1);
-          seen[c] = a;
+        if (mark[b] != a) {
+          mark[b] = a;
+          row.push_back(b);
         }
       }
     }
-    int c = 0;
-    while (c < (int)seen.size() && seen[c] == a) ++c;
-    colour[a] = c;
-    if (c + 1 > ncol) ncol = c + 1;
+    std::sort(row.begin(), row.end());
+    cidx.insert(cidx.end(), row.begin(), row.end());
+    cptr[a + 1] = (int)cidx.size();
   }
-  if (n_colours) *n_colours = ncol;
-  return FV_OK;
+  return fv_saturation_colouring(na, cptr.data(), cidx.data(), colour, n_colours);
 }
 
 // One coarsening step of a block pattern by an aggregation (host): members of every aggregate

@@ -319,8 +319,9 @@ int fv_cell_pattern(int n, long n_pairs, const int* owner, const int* neighbour,
  * ------------------------------------------------------------------------------------------ */
 /* Aggregate the cells of a symmetric cell graph (host CSR); agg[i] in [0, *n_agg). */
 int fv_aggregate(int n, const int* indptr, const int* indices, int* agg, int* n_agg);
-/* First-fit greedy colouring of the aggregates of `agg` (the aggregate graph read from the fine
- * pattern): the colour-by-colour numbering of the coarse levels. */
+/* Saturation-degree colouring (fv_saturation_colouring) of the aggregate graph of `agg`: the
+ * sorted coarse pattern, self included, read from the fine pattern without the block lists.  The
+ * colour-by-colour numbering of the coarse levels. */
 int fv_colour_aggregates(int n, const int* indptr, const int* indices, const int* agg, int na,
                          int* colour, int* n_colours);
 /* One coarsening of a (block) pattern by an aggregation agg (host): mptr (na + 1) / mlist (n)

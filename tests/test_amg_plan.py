@@ -70,6 +70,33 @@ def test_colour_order_gives_shallow_coarse_level_sets():
     assert d_col <= 16 < d_nat
 
 
+def test_aggregate_colouring_is_saturation_colouring_of_the_coarse_pattern():
+    """The coarse-level colouring read from the fine pattern gives the same colours as the
+    saturation colouring of the coarse pattern formed by a full coarsening step."""
+    import ctypes
+
+    from aquaflux_gb300._lib import check, lib, ptr
+    from aquaflux_gb300.amg import _coarsen
+
+    n, ip, ix = _cell_graph(14)
+    agg = np.empty(n, np.int32)
+    na = ctypes.c_int(0)
+    check(lib().fv_aggregate(n, ptr(ip), ptr(ix), ptr(agg), ctypes.byref(na)))
+    na = na.value
+    got, nc_got = np.empty(na, np.int32), ctypes.c_int(0)
+    check(lib().fv_colour_aggregates(n, ptr(ip), ptr(ix), ptr(agg), na, ptr(got),
+                                     ctypes.byref(nc_got)))
+    step = _coarsen(n, ip, ix, agg, na, lists=False)
+    want, nc_want = np.empty(na, np.int32), ctypes.c_int(0)
+    check(lib().fv_saturation_colouring(na, ptr(step["indptr"]), ptr(step["indices"]), ptr(want),
+                                        ctypes.byref(nc_want)))
+    assert np.array_equal(got, want) and nc_got.value == nc_want.value
+    cip, cix = step["indptr"], step["indices"]
+    for a in range(na):  # a proper colouring of the aggregate graph
+        nb = cix[cip[a]:cip[a + 1]]
+        assert np.all(got[nb[nb != a]] != got[a])
+
+
 def test_cell_pattern_equals_the_reach_one_stencil():
     from aquaflux_gb300.colouring import cell_pattern, stencil_pattern
 
