@@ -275,7 +275,9 @@ int fv_ilu0_destroy(FvIlu0* f);
 /* Numeric factorization of new values (device, nnzb * b * b, same dtype as `precision`, or
  * float64 when values_f64 != 0 and precision == 32: converted on the fly). */
 int fv_ilu0_factor(FvIlu0* f, const void* values, int values_f64, void* stream);
-/* x = (LU)^-1 r, or (LU)^-T r when transpose != 0.  Device vectors of `precision`. */
+/* x = (LU)^-1 r, or (LU)^-T r when transpose != 0.  Device vectors of `precision`.  On a stream
+ * under capture the level kernels are recorded into the caller's graph (x may alias r); a
+ * transposed solve needs one uncaptured transposed solve first. */
 int fv_ilu0_apply(FvIlu0* f, const void* r, void* x, int transpose, void* stream);
 /* Copy the factor (device, nnzb * b * b, `precision`) -- combined L (unit diagonal) and U. */
 int fv_ilu0_factor_values(const FvIlu0* f, void* out, void* stream);

@@ -90,6 +90,57 @@ def test_preconditioner_transpose_is_exact(kind, opts):
     assert abs(lhs - rhs) <= 1e-11 * max(abs(lhs), 1.0)
 
 
+@pytest.mark.parametrize("precision,fine_order", [(32, "colour"), (32, "natural"),
+                                                  (64, "natural"), (64, "colour")])
+def test_graph_replayed_vcycle_equals_the_eager_cycle(precision, fine_order):
+    """The V-cycle replayed as one CUDA graph gives bitwise the eager cycle's output: on its first
+    (eager) and second (captured) application, after a refresh at a new state, and after a new
+    shift (which re-forms the fine operator's storage and so re-captures)."""
+    _, case, pg, s = _cavity_pc("amg", precision, fine_order=fine_order)
+    _, _, pe, _ = _cavity_pc("amg", precision, fine_order=fine_order, graph=False)
+    g = torch.Generator(device="cuda").manual_seed(1)
+    rs = [torch.randn(case.n_unknowns, dtype=torch.float64, device="cuda", generator=g)
+          for _ in range(3)]
+    for p in (pg, pe):
+        p.refresh(s)
+    for r in rs:
+        assert torch.equal(pg.apply(r), pe.apply(r))
+    assert pg._graph is not None
+    s2 = s * (1.0 + 0.01 * torch.rand(s.shape, dtype=s.dtype, device="cuda", generator=g))
+    for p in (pg, pe):
+        p.refresh(s2)
+    for r in rs:
+        assert torch.equal(pg.apply(r), pe.apply(r))
+    shift = 0.5 + torch.rand(case.n_unknowns, dtype=torch.float64, device="cuda", generator=g)
+    for p in (pg, pe):
+        p.reshift(shift)
+    for r in rs:
+        assert torch.equal(pg.apply(r), pe.apply(r))
+    assert torch.equal(pg.apply_transpose(rs[0]), pe.apply_transpose(rs[0]))
+
+
+@pytest.mark.parametrize("precision", [32, 64])
+def test_dense_coarsest_level_is_solved_exactly(precision):
+    """A coarsest level of at most ``dense_max`` unknowns is solved by its dense inverse (the
+    reference's coarsest-level inverse): A_c x = b to rounding, and the transpose A_c^T x = b."""
+    wl, case, pc, s = _cavity_pc("amg", precision, coarse_solve="auto")
+    h = pc.h
+    assert h.coarse_solve == "dense" and len(h.levels) >= 2
+    pc.refresh(s)
+    lv = h.levels[-1]
+    g = torch.Generator(device="cuda").manual_seed(2)
+    b = torch.randn(lv.n * h.b, dtype=lv.values.dtype, device="cuda", generator=g)
+    # fp32: the inverse of an operator of condition ~1e5 leaves a relative residual ~1e-2
+    tol = 2e-2 if precision == 32 else 1e-9
+    for transpose in (False, True):
+        x = h.vcycle(len(h.levels) - 1, b, transpose).clone()
+        ax = torch.empty_like(x)
+        lv.spmv(x, ax, transpose)
+        assert float((ax - b).norm()) <= tol * float(b.norm())
+    _, _, pi, _ = _cavity_pc("amg", precision)
+    assert pi.h.coarse_solve == "ilu"
+
+
 @pytest.mark.parametrize("kind", ["ilu", "amg"])
 def test_reshift_equals_a_fresh_shifted_preconditioner(kind):
     """The beta-only refresh (new shift, same materialised Jacobian) gives the preconditioner a

@@ -43,7 +43,8 @@ def test_block_ilu0_fp64_bitwise_equals_scalar_on_cell_major_order():
     np.testing.assert_array_equal(sp_ix, ix)
     np.testing.assert_array_equal(sp_data, data)
     # the transposed solve keeps the reference's operation order (bitwise); the block forward
-    # solve subtracts off-diagonal blocks before in-block terms in its upper sweep (1e-13)
+    # solve subtracts off-diagonal blocks before in-block terms in its upper sweep and multiplies
+    # by the pivots' reciprocals (1e-13)
     np.testing.assert_allclose(f.solve(rhs).cpu().numpy(), x, rtol=1e-13, atol=1e-15)
     np.testing.assert_array_equal(f.solve(rhs, transpose=True).cpu().numpy(), xt)
 
@@ -124,3 +125,31 @@ def test_dot_is_deterministic():
     a, b = dot(x, y), dot(x, y)
     assert float(a) == float(b)
     assert abs(float(a) - float(torch.dot(x, y))) <= 1e-10 * float(torch.dot(x.abs(), y.abs()))
+
+
+@pytest.mark.parametrize("precision", [32, 64])
+def test_block_solve_pivot_quotients_are_correctly_rounded(precision):
+    """The block backward sweep divides by its pivots through a corrected reciprocal; on a matrix
+    of diagonal blocks the solve is x = r / d entry by entry and must equal IEEE division."""
+    from aquaflux_gb300.ilu0 import Ilu0
+
+    b, n = 6, 50000
+    dt = np.float32 if precision == 32 else np.float64
+    span = 12 if precision == 32 else 100
+    rng = np.random.default_rng(7)
+
+    def values(size):
+        return (rng.choice([-1.0, 1.0], size) * 10.0 ** rng.uniform(-span, span, size)).astype(dt)
+
+    d = values(n * b)
+    r = values(n * b)
+    # mantissas near the binade ends, where a quotient from a plain product is often off by one
+    d[:1000] = (1.0 + rng.integers(0, 64, 1000) * np.finfo(dt).eps).astype(dt)
+    r[:1000] = (2.0 - rng.integers(1, 64, 1000) * np.finfo(dt).eps).astype(dt)
+    blocks = np.zeros((n, b, b))
+    blocks[:, np.arange(b), np.arange(b)] = d.reshape(n, b)
+    ip = np.arange(n + 1, dtype=np.int32)
+    ix = np.arange(n, dtype=np.int32)
+    f = Ilu0.from_csr(ip, ix, blocks.reshape(-1), block_size=b, precision=precision)
+    got = f.solve(torch.tensor(r, device="cuda")).cpu().numpy()
+    assert np.array_equal(got, r / d)
