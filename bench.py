@@ -61,6 +61,9 @@ def _args():
     ap.add_argument("--newton-only", default=None, metavar="KIND:PREC:TANGENTS",
                     help="run one Newton solve of that form (e.g. amg:32:32) on the channel and "
                          "print its timings only (for profiling the solve's kernels)")
+    ap.add_argument("--vcycle-only", default=None, metavar="PREC", type=int, choices=[32, 64],
+                    help="time the AMG V-cycle of that precision on the channel's plug-flow "
+                         "Jacobian and run one more in an NVTX range \"vcycle\" (for profiling)")
     return ap.parse_args()
 
 
@@ -86,6 +89,43 @@ def run_newton_only(args) -> dict:
             "converged": res.converged, "newton_steps": res.steps,
             "krylov_iterations": res.krylov_iterations,
             "phase_seconds": {k: round(v, 4) for k, v in res.phase_seconds.items()}}
+
+
+def run_vcycle_only(args) -> dict:
+    """The AMG preconditioner (coloured fine order, the Newton default in 3D) of the --size
+    channel's plug-flow Jacobian: per-level sizes, the V-cycle's time (CUDA events over 20 graph
+    replays after 3 warm-up applications), then one eager V-cycle in the NVTX range "vcycle"."""
+    import torch
+
+    from aquaflux_gb300 import workloads
+    from aquaflux_gb300.amg import AmgPreconditioner
+    from aquaflux_gb300.solve import BlockJacobian
+
+    prec = args.vcycle_only
+    wl = workloads.channel3d(args.size)
+    case = wl.device_case()
+    s = torch.tensor(wl.initial_state(noise=0.02), device="cuda")
+    pc = AmgPreconditioner(BlockJacobian(case, precision=prec), prec)
+    pc.refresh(s)
+    r = torch.randn(case.n_unknowns, dtype=torch.float64, device="cuda",
+                    generator=torch.Generator(device="cuda").manual_seed(0))
+    for _ in range(3):
+        pc.apply(r)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(20):
+        pc.apply(r)
+    e1.record()
+    torch.cuda.synchronize()
+    pc.graph = False
+    torch.cuda.nvtx.range_push("vcycle")  # the profiled region (ncu --nvtx-include "vcycle/")
+    y = pc.apply(r)
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
+    return {"vcycle_only": prec, "cells": wl.mesh.n_cells, "levels": pc.h.sizes,
+            "blocks": [lv.nnzb for lv in pc.h.levels], "ms_per_vcycle": e0.elapsed_time(e1) / 20,
+            "finite": bool(torch.isfinite(y).all())}
 
 
 # ----------------------------------------------------------------------------- clocks
@@ -664,6 +704,10 @@ def main():
     if args.newton_only:
         if rank == 0:
             print(json.dumps(run_newton_only(args)))
+        return
+    if args.vcycle_only:
+        if rank == 0:
+            print(json.dumps(run_vcycle_only(args)))
         return
     out = run_gpu(args, rank, world, local_rank)
     if out is not None:
