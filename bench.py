@@ -45,6 +45,8 @@ def _args():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--size", type=int, default=128, help="cells per axis of the 3D channel")
     ap.add_argument("--cpu-sample", type=int, default=24, help="cells per axis of the CPU sample")
+    ap.add_argument("--ilu-sample", type=int, default=48,
+                    help="cells per axis of the ILU(0) CPU-vs-GPU sample (0: skip)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--step", default="vjp", choices=["vjp", "jvp"])
     ap.add_argument("--no-newton", action="store_true", help="skip the Newton-solve timing")
@@ -275,6 +277,118 @@ def cpu_residual_jvp_rate(size: int, min_seconds: float = 8.0, step: str = "vjp"
                       f"{n} residual+{step.upper()} evaluations in {el:.1f} s"}
 
 
+def bsr_to_scalar_csr(blocks, indptr, indices):
+    """``(indptr, indices, data)`` of the scalar CSR holding every entry of the BSR operator
+    ``blocks`` (nnzb, b, b) on a sorted block pattern: scalar row ``i b + a`` holds entries
+    ``(a, 0..b-1)`` of block row i's blocks, blocks in pattern order (the cell-major scalar layout
+    the reference's ILU(0) kernel factors)."""
+    import numpy as np
+
+    b = blocks.shape[1]
+    ip = np.asarray(indptr, dtype=np.int64)
+    ix = np.asarray(indices, dtype=np.int64)
+    k = np.diff(ip)
+    data = np.empty(blocks.size, dtype=blocks.dtype)
+    cols = np.empty(blocks.size, dtype=np.int32)
+    for kk in np.unique(k):
+        rows = np.flatnonzero(k == kk)
+        q = ip[rows][:, None] + np.arange(kk)  # the rows' blocks, (m, kk)
+        pos = ip[rows][:, None] * b * b + np.arange(kk * b * b)  # their scalar entries
+        data[pos] = blocks[q].transpose(0, 2, 1, 3).reshape(len(rows), -1)
+        c = ix[q][:, None, :, None] * b + np.arange(b)  # (m, 1, kk, b) scalar columns
+        cols[pos] = np.broadcast_to(c, (len(rows), b, kk, b)).reshape(len(rows), -1)
+    sptr = np.concatenate([[0], np.cumsum(np.repeat(k * b, b))]).astype(np.int32)
+    return sptr, cols, data
+
+
+def cpu_ilu0(sptr, scols, sdata, rhs) -> dict:
+    """Factor + solve of the plain-C restatement of the reference's ILU(0) kernel (one core, the
+    reference kernel's operation order) on a scalar CSR operator; factor and solution returned."""
+    import ctypes
+
+    import numpy as np
+
+    from oracle.build_oracle import build_c_oracle
+
+    L = ctypes.CDLL(build_c_oracle())
+    vp = ctypes.c_void_p
+
+    def p(a):
+        return a.ctypes.data_as(vp)
+
+    n = len(sptr) - 1
+    diag = np.zeros(n, dtype=np.int32)
+    bad = ctypes.c_int(-1)
+    if L.ilu0_diagonal_positions(p(sptr), p(scols), n, p(diag), ctypes.byref(bad)) != 0:
+        raise ValueError(f"row {bad.value} stores no diagonal entry")
+    data = np.array(sdata, dtype=np.float64)
+    t0 = time.perf_counter()
+    rc = L.ilu0_factor(p(sptr), p(scols), p(data), p(diag), n, ctypes.byref(bad))
+    t1 = time.perf_counter()
+    if rc != 0:
+        raise ZeroDivisionError(f"ILU(0) met an exactly zero pivot at row {bad.value}")
+    x = np.array(rhs, dtype=np.float64)
+    t2 = time.perf_counter()
+    L.ilu0_solve(p(sptr), p(scols), p(data), p(diag), p(x), n)
+    t3 = time.perf_counter()
+    return {"factor_s": t1 - t0, "solve_s": t3 - t2, "factor": data, "x": x}
+
+
+def ilu_cpu_vs_gpu(size: int) -> dict:
+    """The reference's ILU(0) factor + solve (its C restatement, one core; the kernel is
+    sequential) beside the GPU's fp64 block ILU(0) on the same operator: the fp64 equilibrated
+    cell-major Jacobian of a ``size^3`` sample of the channel at its plug-flow state.  Also checks
+    that the two factors are bitwise equal."""
+    import numpy as np
+    import torch
+
+    from aquaflux_gb300 import workloads
+    from aquaflux_gb300.ilu0 import Ilu0
+    from aquaflux_gb300.solve import BlockJacobian, ShiftedCellMajorOperator
+
+    wl = workloads.channel3d(size)
+    case = wl.device_case()
+    state = torch.tensor(wl.initial_state(noise=0.02), device="cuda")
+    jac = BlockJacobian(case)
+    vals, _ = ShiftedCellMajorOperator(jac, equilibrate=True).assemble(jac.materialize(state))
+    b = jac.b
+    ilu = Ilu0.__new__(Ilu0)
+    ilu._setup(jac.indptr, jac.indices, b, 64)
+    r = torch.randn(jac.n * b, dtype=torch.float64, device="cuda",
+                    generator=torch.Generator(device="cuda").manual_seed(0))
+    for _ in range(2):  # warm: the level schedules' graphs are captured on first use
+        ilu.refactor(vals)
+        x_gpu = ilu.solve(r)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ilu.refactor(vals)
+    torch.cuda.synchronize()
+    factor_ms = (time.perf_counter() - t0) * 1e3
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(5):
+        x_gpu = ilu.solve(r)
+    e1.record()
+    torch.cuda.synchronize()
+    solve_ms = e0.elapsed_time(e1) / 5
+    blocks = vals.cpu().numpy().reshape(-1, b, b)
+    sptr, scols, sdata = bsr_to_scalar_csr(blocks, jac.indptr, jac.indices)
+    cpu = cpu_ilu0(sptr, scols, sdata, r.cpu().numpy())
+    _, _, gfac = bsr_to_scalar_csr(ilu.factor_values().cpu().numpy().reshape(-1, b, b),
+                                   jac.indptr, jac.indices)
+    xg = x_gpu.cpu().numpy()
+    return {"sample": f"{size}^3 channel, fp64 equilibrated cell-major Jacobian at the plug-flow "
+                      f"state ({jac.n} cells, {jac.n * b} rows, {sdata.size} entries)",
+            "cpu": {"factor_s": round(cpu["factor_s"], 4), "solve_s": round(cpu["solve_s"], 4),
+                    "cores": 1, "kind": "port",
+                    "what": "plain-C restatement of the reference's ILU(0) kernel"},
+            "gpu_fp64": {"factor_ms": round(factor_ms, 3), "solve_ms": round(solve_ms, 3)},
+            "factor_speedup": round(cpu["factor_s"] * 1e3 / factor_ms, 1),
+            "solve_speedup": round(cpu["solve_s"] * 1e3 / solve_ms, 1),
+            "factor_bitwise_equal": bool(np.array_equal(gfac, cpu["factor"])),
+            "solve_max_rel_diff": float(np.abs(xg - cpu["x"]).max() / np.abs(cpu["x"]).max())}
+
+
 # ----------------------------------------------------------------------------- GPU arm
 def replica_throughput(ms: float, faces: int, steps: int, world: int, dist, device) -> tuple:
     """The replicas' timing contract: the slowest rank's time (max over ranks) and the whole job's
@@ -452,6 +566,11 @@ def run_gpu(args, rank: int, world: int, local_rank: int) -> dict | None:
         cb = cpu_residual_jvp_rate(args.cpu_sample, step=args.step)
         out["cpu_baseline"] = {"value": round(cb["faces_per_s"] / 1e9, 6), "unit": UNIT,
                                "cores": cb["cores"], "kind": "port", "sample": cb["sample"]}
+        if args.ilu_sample > 0:
+            try:
+                out["cpu_ilu"] = ilu_cpu_vs_gpu(args.ilu_sample)
+            except Exception as e:  # reported, never allowed to lose the headline line
+                out["cpu_ilu"] = {"error": f"{type(e).__name__}: {e}"[:300]}
     return out
 
 
