@@ -347,8 +347,9 @@ class AmgPreconditioner:
         return out
 
     def _vcycle(self, transpose: bool) -> torch.Tensor:
-        """The V-cycle on ``self._b`` into the fine level's ``x``: eager, or a graph replay."""
-        if transpose or not self.graph:
+        """The V-cycle on ``self._b`` into the fine level's ``x``: eager, or a graph replay.
+        Under a caller's own stream capture the cycle is recorded eagerly into that graph."""
+        if transpose or not self.graph or torch.cuda.is_current_stream_capturing():
             return self.h.vcycle(0, self._b, transpose)
         # the graph holds the fine operator's storage address (an fp64 fine level may hold the
         # Jacobian's own tensor): re-capture when it changes, after one eager cycle that builds
