@@ -87,26 +87,43 @@ extern "C" int fv_colour_aggregates(int n, const int* indptr, const int* indices
     std::vector<int> fill(cnt.begin(), cnt.end() - 1);
     for (int i = 0; i < n; ++i) members[fill[agg[i]]++] = i;
   }
+  for (long q = 0; q < indptr[n]; ++q)
+    if (indices[q] < 0 || indices[q] >= n) {
+      fv_set_error("fv_colour_aggregates: column index out of range at entry %ld", q);
+      return FV_ERR_ARG;
+    }
   // the aggregate graph: per aggregate the sorted distinct aggregates its members touch
-  // (itself included), i.e. the coarse pattern, built without the block lists
-  std::vector<int> cptr(na + 1, 0), cidx, mark(na, -1), row;
-  cidx.reserve((size_t)indptr[n] / 2 + na);
-  for (int a = 0; a < na; ++a) {
-    row.clear();
-    for (int m = cnt[a]; m < cnt[a + 1]; ++m) {
-      const int i = members[m];
-      for (int q = indptr[i]; q < indptr[i + 1]; ++q) {
-        const int b = agg[indices[q]];
-        if (mark[b] != a) {
-          mark[b] = a;
-          row.push_back(b);
+  // (itself included), i.e. the coarse pattern, built without the block lists; aggregates are
+  // split into contiguous ranges over the host threads, each range's rows gathered by its thread
+  const long chunk_min = 4096;
+  std::vector<std::vector<int>> part(host_threads());
+  std::vector<int> len(na, 0);
+  host_parallel_for(na, chunk_min, [&](long a0, long a1, int t) {
+    std::vector<int> mark(na, -1), row;
+    std::vector<int>& out = part[t];
+    for (long a = a0; a < a1; ++a) {
+      row.clear();
+      for (int m = cnt[a]; m < cnt[a + 1]; ++m) {
+        const int i = members[m];
+        for (int q = indptr[i]; q < indptr[i + 1]; ++q) {
+          const int b = agg[indices[q]];
+          if (mark[b] != (int)a) {
+            mark[b] = (int)a;
+            row.push_back(b);
+          }
         }
       }
+      std::sort(row.begin(), row.end());
+      out.insert(out.end(), row.begin(), row.end());
+      len[a] = (int)row.size();
     }
-    std::sort(row.begin(), row.end());
-    cidx.insert(cidx.end(), row.begin(), row.end());
-    cptr[a + 1] = (int)cidx.size();
-  }
+  });
+  std::vector<int> cptr(na + 1, 0);
+  for (int a = 0; a < na; ++a) cptr[a + 1] = cptr[a] + len[a];
+  std::vector<int> cidx(cptr[na]);
+  host_parallel_for(na, chunk_min, [&](long a0, long, int t) {  // the same split as above
+    std::copy(part[t].begin(), part[t].end(), cidx.begin() + cptr[a0]);
+  });
   return fv_saturation_colouring(na, cptr.data(), cidx.data(), colour, n_colours);
 }
 

@@ -27,12 +27,8 @@ extern "C" int fv_saturation_colouring(int n, const int* indptr, const int* indi
     if (n_colours) *n_colours = 0;
     return FV_OK;
   }
-  std::vector<long> degree(n);
   long max_degree = 0;
-  for (int v = 0; v < n; ++v) {
-    degree[v] = indptr[v + 1] - indptr[v];
-    if (degree[v] > max_degree) max_degree = degree[v];
-  }
+  for (int v = 0; v < n; ++v) max_degree = std::max<long>(max_degree, indptr[v + 1] - indptr[v]);
   for (long q = 0; q < indptr[n]; ++q)
     if (indices[q] < 0 || indices[q] >= n) {
       fv_set_error("fv_saturation_colouring: neighbour index out of range");
@@ -40,72 +36,69 @@ extern "C" int fv_saturation_colouring(int n, const int* indptr, const int* indi
     }
   const long words = max_degree / 64 + 2;
   const long tie = max_degree + 1;
+  // per vertex: its bucket rank and its links in the bucket's list (one cache line holds four)
+  struct Node {
+    long rank;
+    int next, prev;
+  };
+  std::vector<Node> node(n);
   std::vector<uint64_t> taken((size_t)n * words, 0);
-  std::vector<long> sat(n, 0);
-  std::vector<long> head((size_t)(tie * max_degree + max_degree + 1), -1);
-  std::vector<long> next(n, -1), prev(n, -1);
+  std::vector<int> head((size_t)(tie * max_degree + max_degree + 1), -1);
   for (int v = 0; v < n; ++v) colour[v] = -1;
   long top = 0;
   for (int v = 0; v < n; ++v) {
-    long r = degree[v];
-    long h = head[r];
-    next[v] = h;
-    if (h >= 0) prev[h] = v;
+    const long r = indptr[v + 1] - indptr[v];
+    const int h = head[r];
+    node[v] = Node{r, h, -1};
+    if (h >= 0) node[h].prev = v;
     head[r] = v;
-    if (r > top) top = r;
+    top = std::max(top, r);
   }
   int ncol = 0;
-  std::vector<int> gained;
   for (int step = 0; step < n; ++step) {
     while (head[top] < 0) --top;
-    const long v = head[top];
-    const long f = next[v];
+    const int v = head[top];
+    const int f = node[v].next;
     head[top] = f;
-    if (f >= 0) prev[f] = -1;
+    if (f >= 0) node[f].prev = -1;
     int chosen = -1;
     for (long w = 0; w < words; ++w) {
-      uint64_t freeb = ~taken[(size_t)v * words + w];
+      const uint64_t freeb = ~taken[(size_t)v * words + w];
       if (freeb) {
         chosen = (int)(w * 64 + __builtin_ctzll(freeb));
         break;
       }
     }
     colour[v] = chosen;
-    if (chosen + 1 > ncol) ncol = chosen + 1;
+    ncol = std::max(ncol, chosen + 1);
     const long word = chosen / 64;
     const uint64_t bit = 1ull << (chosen % 64);
-    gained.clear();
+    // every uncoloured neighbour seeing the colour for the first time moves, in CSR order, to the
+    // head of the bucket one saturation higher (a coloured neighbour's bits are never read again)
     for (int q = indptr[v]; q < indptr[v + 1]; ++q) {
       const int u = indices[q];
-      uint64_t& t = taken[(size_t)u * words + word];
-      const bool had = (t & bit) != 0;
-      t |= bit;
-      if (!had) gained.push_back(u);
-    }
-    for (int u : gained) {
       if (colour[u] >= 0) continue;
-      const long r_old = sat[u] * tie + degree[u];
-      sat[u] += 1;
-      const long r_new = sat[u] * tie + degree[u];
-      const long p = prev[u], fo = next[u];
-      if (p >= 0) next[p] = fo;
-      else head[r_old] = fo;
-      if (fo >= 0) prev[fo] = p;
-      const long h = head[r_new];
-      next[u] = h;
-      prev[u] = -1;
-      if (h >= 0) prev[h] = u;
+      uint64_t& t = taken[(size_t)u * words + word];
+      if (t & bit) continue;
+      t |= bit;
+      Node& nu = node[u];
+      const long r_old = nu.rank, r_new = r_old + tie;
+      if (nu.prev >= 0) node[nu.prev].next = nu.next;
+      else head[r_old] = nu.next;
+      if (nu.next >= 0) node[nu.next].prev = nu.prev;
+      const int h = head[r_new];
+      nu.rank = r_new;
+      nu.next = h;
+      nu.prev = -1;
+      if (h >= 0) node[h].prev = u;
       head[r_new] = u;
-      if (r_new > top) top = r_new;
+      top = std::max(top, r_new);
     }
   }
   if (n_colours) *n_colours = ncol;
   return FV_OK;
 }
 
-// Reach-1 cell pattern (host): row i holds i and the cells sharing a face with i, sorted and
-// unique.  Interior faces given as (owner, neighbour) pairs.  indptr (n + 1); indices receives
-// at most n + 2 * n_pairs entries.
 // First-fit greedy colouring in index order (every vertex takes the smallest colour none of its
 // already coloured neighbours has): O(edges), for orderings where the colour count matters more
 // than its minimality (the AMG fine smoother's red-black-like sweeps).
@@ -140,6 +133,9 @@ extern "C" int fv_greedy_colouring(int n, const int* indptr, const int* indices,
   return FV_OK;
 }
 
+// Reach-1 cell pattern (host): row i holds i and the cells sharing a face with i, sorted and
+// unique.  Interior faces given as (owner, neighbour) pairs.  indptr (n + 1); indices receives
+// at most n + 2 * n_pairs entries.
 extern "C" int fv_cell_pattern(int n, long n_pairs, const int* owner, const int* neighbour,
                                int* indptr, int* indices) {
   if (n <= 0 || n_pairs < 0 || (n_pairs > 0 && (!owner || !neighbour)) || !indptr || !indices) {
