@@ -120,8 +120,7 @@ def _coarsen(n, ip, ix, agg, na, lists: bool = True) -> dict:
                            ptr(cix), ptr(gptr), ptr(glist), ctypes.byref(ncb)))
     ncb = int(ncb.value)
     return {"n_coarse": na, "agg": agg, "mptr": mptr, "mlist": mlist, "indptr": cip,
-            "indices": cix[:ncb].copy(), "gptr": gptr[:ncb + 1].copy() if lists else None,
-            "glist": glist}
+            "indices": cix[:ncb], "gptr": gptr[:ncb + 1] if lists else None, "glist": glist}
 
 
 class AmgHierarchy:

@@ -59,7 +59,8 @@ def cell_pattern(owner, nb, n: int) -> tuple[np.ndarray, np.ndarray]:
     indptr = np.empty(n + 1, dtype=np.int32)
     indices = np.empty(n + 2 * owner.size, dtype=np.int32)
     check(lib().fv_cell_pattern(n, owner.size, ptr(owner), ptr(nb), ptr(indptr), ptr(indices)))
-    return indptr, indices[:int(indptr[-1])].copy()
+    nnz = int(indptr[-1])
+    return indptr, (indices if nnz == indices.size else indices[:nnz].copy())
 
 
 def saturation_colouring(conflict: sp.csr_matrix) -> np.ndarray:

@@ -9,6 +9,7 @@
 // constant) tentative prolongation, so P^T A P is an aggregate-to-aggregate sum of fine blocks: the
 // GPU forms each coarse block as the ordered sum of its fine blocks (deterministic, no atomics).
 #include <algorithm>
+#include <memory>
 #include <vector>
 
 #include "host_par.h"
@@ -87,11 +88,10 @@ extern "C" int fv_colour_aggregates(int n, const int* indptr, const int* indices
     std::vector<int> fill(cnt.begin(), cnt.end() - 1);
     for (int i = 0; i < n; ++i) members[fill[agg[i]]++] = i;
   }
-  for (long q = 0; q < indptr[n]; ++q)
-    if (indices[q] < 0 || indices[q] >= n) {
-      fv_set_error("fv_colour_aggregates: column index out of range at entry %ld", q);
-      return FV_ERR_ARG;
-    }
+  if (host_any_outside(indices, indptr[n], 0, n)) {
+    fv_set_error("fv_colour_aggregates: column index out of range");
+    return FV_ERR_ARG;
+  }
   // the aggregate graph: per aggregate the sorted distinct aggregates its members touch
   // (itself included), i.e. the coarse pattern, built without the block lists; aggregates are
   // split into contiguous ranges over the host threads, each range's rows gathered by its thread
@@ -145,11 +145,10 @@ extern "C" int fv_coarsen(int n, const int* indptr, const int* indices, const in
       fv_set_error("fv_coarsen: aggregate index out of range at cell %d", i);
       return FV_ERR_ARG;
     }
-  for (long q = 0; q < nnz; ++q)
-    if (indices[q] < 0 || indices[q] >= n) {
-      fv_set_error("fv_coarsen: column index out of range");
-      return FV_ERR_ARG;
-    }
+  if (host_any_outside(indices, nnz, 0, n)) {
+    fv_set_error("fv_coarsen: column index out of range");
+    return FV_ERR_ARG;
+  }
   // members (counting sort, stable)
   std::vector<int> cnt(na + 1, 0);
   for (int i = 0; i < n; ++i) ++cnt[agg[i] + 1];
@@ -169,7 +168,8 @@ extern "C" int fv_coarsen(int n, const int* indptr, const int* indices, const in
     for (int m = mptr[a]; m < mptr[a + 1]; ++m) c += indptr[mlist[m] + 1] - indptr[mlist[m]];
     fb[a + 1] = fb[a] + c;
   }
-  std::vector<int> scratch(fb[na]);
+  // scratch without value-initialisation: each aggregate's thread writes its part first
+  std::unique_ptr<int[]> scratch(new int[std::max(1L, fb[na])]);
   std::vector<int> width(na);
   const int nth = host_threads();
   std::vector<std::vector<int>> marks(nth), slots(nth);
@@ -177,7 +177,7 @@ extern "C" int fv_coarsen(int n, const int* indptr, const int* indices, const in
     std::vector<int>& mark = marks[t];
     mark.assign(na, -1);
     for (long a = b; a < e; ++a) {
-      int* cols = scratch.data() + fb[a];
+      int* cols = scratch.get() + fb[a];
       int k = 0;
       for (int m = mptr[a]; m < mptr[a + 1]; ++m) {
         const int i = mlist[m];
@@ -208,7 +208,7 @@ extern "C" int fv_coarsen(int n, const int* indptr, const int* indices, const in
     std::vector<long> fill;
     for (long a = b; a < e; ++a) {
       const int k = width[a];
-      const int* cols = scratch.data() + fb[a];
+      const int* cols = scratch.get() + fb[a];
       for (int c = 0; c < k; ++c) cix[cip[a] + c] = cols[c];
       if (!lists) continue;
       for (int c = 0; c < k; ++c) slot[cols[c]] = c;

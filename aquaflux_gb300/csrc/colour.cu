@@ -12,6 +12,7 @@
 // Runs in O(n + m) with a bitset of taken colours per vertex.
 #include <algorithm>
 #include <cstdint>
+#include <memory>
 #include <vector>
 
 #include "host_par.h"
@@ -142,30 +143,71 @@ extern "C" int fv_cell_pattern(int n, long n_pairs, const int* owner, const int*
     fv_set_error("fv_cell_pattern: bad arguments");
     return FV_ERR_ARG;
   }
-  std::vector<long> cnt(n + 1, 0);
-  for (long f = 0; f < n_pairs; ++f) {
-    const int a = owner[f], b = neighbour[f];
-    if (a < 0 || a >= n || b < 0 || b >= n) {
-      fv_set_error("fv_cell_pattern: cell index out of range at pair %ld", f);
+  // 1. every pair chunk counts its two entries (row a: b, row b: a) per destination row range
+  const HostSplit rows = host_split(n, 1 << 16), pairs = host_split(n_pairs, 1 << 16);
+  const long R = rows.nt, P = pairs.nt;
+  std::vector<long> count((size_t)P * R, 0);  // [pair chunk][row range]
+  std::vector<long> bad(P, -1);
+  host_parallel_for(n_pairs, 1 << 16, [&](long f0, long f1, int t) {
+    long* c = count.data() + (size_t)t * R;
+    for (long f = f0; f < f1; ++f) {
+      const int a = owner[f], b = neighbour[f];
+      if (a < 0 || a >= n || b < 0 || b >= n) {
+        bad[t] = f;
+        return;
+      }
+      ++c[a / rows.chunk];
+      ++c[b / rows.chunk];
+    }
+  });
+  for (long t = 0; t < P; ++t)
+    if (bad[t] >= 0) {
+      fv_set_error("fv_cell_pattern: cell index out of range at pair %ld", bad[t]);
       return FV_ERR_ARG;
     }
-    ++cnt[a + 1];
-    ++cnt[b + 1];
-  }
-  for (int i = 0; i < n; ++i) cnt[i + 1] += cnt[i] + 1;  // + the diagonal
-  std::vector<int> tmp(cnt[n]);
-  std::vector<int> width(n);
-  // each thread fills, sorts and de-duplicates the rows of its own range (scanning every pair)
-  host_parallel_for(n, 1 << 16, [&](long r0, long r1, int) {
-    std::vector<long> fill(cnt.begin() + r0, cnt.begin() + r1);
-    for (long i = r0; i < r1; ++i) tmp[fill[i - r0]++] = (int)i;
-    for (long f = 0; f < n_pairs; ++f) {
-      const int a = owner[f], b = neighbour[f];
-      if (a >= r0 && a < r1) tmp[fill[a - r0]++] = b;
-      if (b >= r0 && b < r1) tmp[fill[b - r0]++] = a;
+  // 2. bucket the entries by row range (range-major, pair chunks in order within a range)
+  std::vector<long> off((size_t)P * R + 1, 0), range_start(R + 1, 0);
+  {
+    long pos = 0;
+    for (long k = 0; k < R; ++k) {
+      range_start[k] = pos;
+      for (long t = 0; t < P; ++t) {
+        off[(size_t)t * R + k] = pos;
+        pos += count[(size_t)t * R + k];
+      }
     }
+    range_start[R] = pos;
+  }
+  // scratch without value-initialisation: the threads below touch it first, in parallel
+  std::unique_ptr<int2[]> ent(new int2[std::max(1L, range_start[R])]);
+  host_parallel_for(n_pairs, 1 << 16, [&](long f0, long f1, int t) {
+    long* o = off.data() + (size_t)t * R;
+    for (long f = f0; f < f1; ++f) {
+      const int a = owner[f], b = neighbour[f];
+      ent[o[a / rows.chunk]++] = make_int2(a, b);
+      ent[o[b / rows.chunk]++] = make_int2(b, a);
+    }
+  });
+  // 3. each row range fills, sorts and de-duplicates its own rows (the diagonal included); a
+  // range's rows start after the previous ranges' entries and diagonals, and every per-row
+  // array element is written by the range owning the row only
+  std::vector<long> start(n);
+  std::vector<int> deg(n, 1), width(n);
+  std::unique_ptr<int[]> tmp(new int[range_start[R] + n]);
+  host_parallel_for(n, 1 << 16, [&](long r0, long r1, int k) {
+    for (long e = range_start[k]; e < range_start[k + 1]; ++e) ++deg[ent[e].x];
+    long pos = range_start[k] + r0;
     for (long i = r0; i < r1; ++i) {
-      auto b = tmp.begin() + cnt[i], e = tmp.begin() + cnt[i + 1];
+      start[i] = pos;
+      pos += deg[i];
+    }
+    std::vector<long> fill(start.begin() + r0, start.begin() + r1);
+    for (long i = r0; i < r1; ++i) tmp[fill[i - r0]++] = (int)i;
+    for (long e = range_start[k]; e < range_start[k + 1]; ++e)
+      tmp[fill[ent[e].x - r0]++] = ent[e].y;
+    for (long i = r0; i < r1; ++i) {
+      int* b = tmp.get() + start[i];
+      int* e = b + deg[i];
       std::sort(b, e);
       width[i] = (int)(std::unique(b, e) - b);
     }
@@ -182,7 +224,7 @@ extern "C" int fv_cell_pattern(int n, long n_pairs, const int* owner, const int*
   }
   host_parallel_for(n, 1 << 16, [&](long r0, long r1, int) {
     for (long i = r0; i < r1; ++i)
-      std::copy(tmp.begin() + cnt[i], tmp.begin() + cnt[i] + width[i], indices + indptr[i]);
+      std::copy(tmp.get() + start[i], tmp.get() + start[i] + width[i], indices + indptr[i]);
   });
   return FV_OK;
 }
