@@ -252,11 +252,10 @@ extern "C" int fv_permute_pattern(int n, const int* indptr, const int* indices, 
   // rows keep their widths: offsets first, then the rows in parallel
   out_indptr[0] = 0;
   for (int r = 0; r < n; ++r) out_indptr[r + 1] = out_indptr[r] + (indptr[perm[r] + 1] - indptr[perm[r]]);
-  for (long q = 0; q < indptr[n]; ++q)
-    if (indices[q] < 0 || indices[q] >= n) {
-      fv_set_error("fv_permute_pattern: column index out of range");
-      return FV_ERR_ARG;
-    }
+  if (host_any_outside(indices, indptr[n], 0, n)) {
+    fv_set_error("fv_permute_pattern: column index out of range");
+    return FV_ERR_ARG;
+  }
   host_parallel_for(n, 1 << 15, [&](long r0, long r1, int) {
     std::vector<std::pair<int, long>> row;
     for (long r = r0; r < r1; ++r) {
