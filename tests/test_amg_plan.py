@@ -133,3 +133,41 @@ def test_permuted_pattern_maps_every_block():
     with pytest.raises(Exception):
         check(lib().fv_permute_pattern(n, ptr(ip), ptr(ix), ptr(bad), ptr(pip), ptr(pix),
                                        ptr(bmap)))
+
+
+def test_host_passes_reject_out_of_range_indices():
+    """The pattern passes check their column indices (over the host threads) and report the
+    error instead of reading out of bounds: coarsening, aggregate colouring, permutation and the
+    cell pattern."""
+    import ctypes
+
+    from aquaflux_gb300._lib import FvError, check, lib, ptr
+
+    n, ip, ix = _cell_graph(6)
+    agg = np.empty(n, np.int32)
+    na = ctypes.c_int(0)
+    check(lib().fv_aggregate(n, ptr(ip), ptr(ix), ptr(agg), ctypes.byref(na)))
+    na = na.value
+    bad = ix.copy()
+    bad[len(bad) // 2] = n  # one column past the last cell
+    nnz = int(ip[-1])
+    col, nco = np.empty(na, np.int32), ctypes.c_int(0)
+    with pytest.raises(FvError, match="column index out of range"):
+        check(lib().fv_colour_aggregates(n, ptr(ip), ptr(bad), ptr(agg), na, ptr(col),
+                                         ctypes.byref(nco)))
+    mptr, mlist = np.empty(na + 1, np.int32), np.empty(n, np.int32)
+    cip, cix = np.empty(na + 1, np.int32), np.empty(nnz, np.int32)
+    gptr, glist, ncb = np.empty(nnz + 1, np.int64), np.empty(nnz, np.int64), ctypes.c_long(0)
+    with pytest.raises(FvError, match="column index out of range"):
+        check(lib().fv_coarsen(n, ptr(ip), ptr(bad), ptr(agg), na, ptr(mptr), ptr(mlist),
+                               ptr(cip), ptr(cix), ptr(gptr), ptr(glist), ctypes.byref(ncb)))
+    perm = np.arange(n, dtype=np.int32)
+    pip, pix, bmap = np.empty(n + 1, np.int32), np.empty(nnz, np.int32), np.empty(nnz, np.int64)
+    with pytest.raises(FvError, match="column index out of range"):
+        check(lib().fv_permute_pattern(n, ptr(ip), ptr(bad), ptr(perm), ptr(pip), ptr(pix),
+                                       ptr(bmap)))
+    owner = np.array([0, 1, 2], np.int32)
+    neigh = np.array([1, 2, n], np.int32)
+    cp_ip, cp_ix = np.empty(n + 1, np.int32), np.empty(n + 6, np.int32)
+    with pytest.raises(FvError, match="out of range at pair 2"):
+        check(lib().fv_cell_pattern(n, 3, ptr(owner), ptr(neigh), ptr(cp_ip), ptr(cp_ix)))
