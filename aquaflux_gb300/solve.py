@@ -212,8 +212,17 @@ class KrylovResult:
 
 
 def fgmres(matvec, b: torch.Tensor, precond=None, *, rtol: float = 1e-3, atol: float = 0.0,
-           restart: int = 30, maxiter: int = 300) -> KrylovResult:
-    """Flexible GMRES(restart), right-preconditioned, CGS2 orthogonalisation, fp64."""
+           restart: int = 30, maxiter: int = 300, lag: bool = False) -> KrylovResult:
+    """Flexible GMRES(restart), right-preconditioned, CGS2 orthogonalisation, fp64.
+
+    ``lag=True`` reads each new Hessenberg column back to the host (a pinned buffer) only after
+    the next iteration's work has been queued, so the device is not left idle while the host
+    issues that work; the convergence test then lags by one iteration, and the iteration queued
+    past convergence is discarded (it costs one more preconditioner application and operator
+    product per restart cycle that converges before its last column).  The arithmetic is that of
+    ``lag=False`` except that each new basis vector is divided by its norm held on the device
+    rather than on the host (bitwise the same on CPU tensors; on the GPU the division by a host
+    scalar may round differently)."""
     M = precond if precond is not None else (lambda v: v)
     x = torch.zeros_like(b)
     bnorm = float(torch.linalg.vector_norm(b))
@@ -223,6 +232,7 @@ def fgmres(matvec, b: torch.Tensor, precond=None, *, rtol: float = 1e-3, atol: f
     total = 0
     if beta <= tol:
         return KrylovResult(x, 0, beta, True)
+    on_gpu = b.is_cuda
     while total < maxiter:
         m = min(restart, maxiter - total)
         V = torch.empty(m + 1, b.numel(), dtype=torch.float64, device=b.device)
@@ -233,7 +243,12 @@ def fgmres(matvec, b: torch.Tensor, precond=None, *, rtol: float = 1e-3, atol: f
         g[0] = beta
         V[0] = r / beta
         k_done = 0
-        for j in range(m):
+        hbuf = (torch.empty((m, m + 1), dtype=torch.float64, pin_memory=on_gpu)
+                if lag else None)
+        pending = []  # lagged columns: (j, device column or host view, event)
+
+        def column(j):
+            """Orthogonalise A M v_j against the basis; the new column h (device)."""
             Z[j] = M(V[j])
             w = matvec(Z[j])
             # classical Gram-Schmidt with one re-orthogonalisation (CGS2): two matrix-vector
@@ -244,10 +259,12 @@ def fgmres(matvec, b: torch.Tensor, precond=None, *, rtol: float = 1e-3, atol: f
             h2 = Vj @ w
             w = w - h2 @ Vj
             h = torch.cat([h1 + h2, torch.linalg.vector_norm(w).reshape(1)])
-            hh = h.cpu().numpy()
+            return h, w
+
+        def reduce(j, hh) -> bool:
+            """Givens-reduce column j; True when the cycle stops after it."""
+            nonlocal k_done, total
             H[: j + 2, j] = hh
-            if hh[j + 1] > 0:
-                V[j + 1] = w / hh[j + 1]
             for i in range(j):  # apply the previous rotations
                 t = cs[i] * H[i, j] + sn[i] * H[i + 1, j]
                 H[i + 1, j] = -sn[i] * H[i, j] + cs[i] * H[i + 1, j]
@@ -260,8 +277,39 @@ def fgmres(matvec, b: torch.Tensor, precond=None, *, rtol: float = 1e-3, atol: f
             g[j] = cs[j] * g[j]
             k_done = j + 1
             total += 1
-            if abs(g[j + 1]) <= tol or hh[j + 1] == 0:
-                break
+            return abs(g[j + 1]) <= tol or hh[j + 1] == 0
+
+        for j in range(m):
+            h, w = column(j)
+            if not lag:
+                hh = h.cpu().numpy()
+                if hh[j + 1] > 0:
+                    V[j + 1] = w / hh[j + 1]
+                if reduce(j, hh):
+                    break
+                continue
+            # lagged: normalise on the device (a zero norm only arises where the cycle stops),
+            # queue the column's copy, then reduce the previous column while this one runs
+            V[j + 1] = w / h[j + 1]
+            hbuf[j, : j + 2].copy_(h, non_blocking=True)
+            ev = None
+            if on_gpu:
+                ev = torch.cuda.Event()
+                ev.record()
+            pending.append((j, ev))
+            if len(pending) == 2:
+                jp, evp = pending.pop(0)
+                if evp is not None:
+                    evp.synchronize()
+                if reduce(jp, hbuf[jp, : jp + 2].numpy().copy()):
+                    pending.clear()
+                    break
+        else:
+            for jp, evp in pending:
+                if evp is not None:
+                    evp.synchronize()
+                if reduce(jp, hbuf[jp, : jp + 2].numpy().copy()):
+                    break
         y = np.zeros(k_done)
         for i in range(k_done - 1, -1, -1):
             y[i] = (g[i] - H[i, i + 1:k_done] @ y[i + 1:]) / H[i, i]
@@ -289,7 +337,8 @@ def newton_solve(case, state0, *, rtol: float = 1e-10, atol: float = 1e-12, max_
                  max_krylov: int = 300, precision: int = 32, reach: int = 1, frozen: bool = True,
                  refresh_every: int = 1, line_search_steps: int = 10,
                  preconditioner=None, kind: str = "ilu",
-                 precond_options: dict | None = None, tangents: int = 64) -> NewtonResult:
+                 precond_options: dict | None = None, tangents: int = 64,
+                 krylov_lag: bool = False) -> NewtonResult:
     """Newton's method with FGMRES, preconditioned by ILU(0) of the materialised Jacobian
     (``kind="ilu"``) or by an ILU(0)-smoothed aggregation V-cycle (``kind="amg"``), in fp32 or
     fp64 (``precision``).
@@ -298,7 +347,8 @@ def newton_solve(case, state0, *, rtol: float = 1e-10, atol: float = 1e-12, max_
     ``J v`` (``fv_jvp_f32``) and the preconditioner's Jacobian assembly
     (``fv_assemble_jacobian_f32``).  The residual, the Newton update, the line search and the
     stopping test stay fp64, so the root is the fp64 root; only the linear solves, already
-    inexact at ``linear_rtol``, see fp32 rounding."""
+    inexact at ``linear_rtol``, see fp32 rounding.  ``krylov_lag`` selects the FGMRES variant
+    whose convergence test lags one iteration behind the queued work (``fgmres(lag=True)``)."""
     if tangents not in (32, 64):
         raise ValueError(f"tangents must be 64 or 32, got {tangents}")
     t_all = time.perf_counter()
@@ -338,7 +388,7 @@ def newton_solve(case, state0, *, rtol: float = 1e-10, atol: float = 1e-12, max_
         res = timed("krylov", lambda: fgmres(lambda v: case.jvp(s, v, precision=tangents), -r,
                                              preconditioner.apply,
                                              rtol=linear_rtol, restart=restart,
-                                             maxiter=max_krylov))
+                                             maxiter=max_krylov, lag=krylov_lag))
         its.append(res.iterations)
         delta = res.x
 
