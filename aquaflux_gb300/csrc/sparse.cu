@@ -505,7 +505,8 @@ __global__ void k_ilu_upper_lg(IluView<V> F, const int* rows, int count, V* x) {
   // ncu; fp64: the 128^3 fine-level solve 6.5 ms with divisions, GB300).  The quotient x / d is
   // q = x r corrected once, q + (x - q d) r, with fused multiply-adds: by Markstein's theorem
   // (IBM J. Res. Develop. 34(1), 1990) the correctly rounded quotient, outside the underflow
-  // range.  A lane whose reciprocal overflows (fp32 pivot below ~3e-39) divides.
+  // range (pinned bitwise against IEEE division in both precisions by the sparse-solver tests).
+  // A lane whose reciprocal overflows (fp32 pivot below ~3e-39) divides.
   V piv = V(1);
 #pragma unroll
   for (int c = 0; c < B; ++c)
