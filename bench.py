@@ -12,7 +12,13 @@ timed region.
 oracle restating the reference's residual, autograd JVP, all host threads) on a bounded sample of
 the same workload.
 
-Run: ``python bench.py [--gpus N] [--steps K] [--warmup W] [--size 128]``.
+The line also carries the Newton block (each preconditioner in fp64, fp32 and fp32 + fp32
+tangents), the adjoint objectives, the CPU baseline, and ``cpu_ilu``: the reference's ILU(0)
+kernel (its C restatement, one core) timed beside the GPU's fp64 ILU(0) on a 48^3 Jacobian.
+
+Run: ``python bench.py [--gpus N] [--steps K] [--warmup W] [--size 128]``.  Profiling modes
+(one JSON line each): ``--newton-only KIND:PREC:TANGENTS`` (one Newton solve inside the NVTX
+range "newton"), ``--vcycle-only PREC`` (the AMG V-cycle, one inside the NVTX range "vcycle").
 """
 from __future__ import annotations
 
