@@ -11,7 +11,8 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def _declared():
-    text = open(os.path.join(ROOT, "include", "fvgb.h")).read()
+    with open(os.path.join(ROOT, "include", "fvgb.h")) as fh:
+        text = fh.read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
     return sorted(set(re.findall(r"\b(fv_[a-z0-9_]+)\s*\(", text)))
 

@@ -33,7 +33,7 @@ def _rank(rank, world, port, out):
 
 def test_two_replicas_report_the_slowest_rank_and_the_summed_work():
     world, port = 2, _free_port()
-    out = mp.Manager().dict()
+    out = mp.get_context("spawn").Manager().dict()  # no fork of this multi-threaded process
     mp.spawn(_rank, args=(world, port, out), nprocs=world, join=True)
     for r in range(world):
         ms, value = out[r]
