@@ -149,10 +149,11 @@ class ClockSampler:
         fd, self.path = tempfile.mkstemp(suffix=".csv")
         os.close(fd)
         try:
-            self.proc = subprocess.Popen(
-                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={CLOCK_QUERY}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
-                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+            with open(self.path, "w") as out:  # the child keeps its own descriptor
+                self.proc = subprocess.Popen(
+                    ["nvidia-smi", "-i", str(self.index), f"--query-gpu={CLOCK_QUERY}",
+                     "--format=csv,noheader,nounits", "-lms", "200"],
+                    stdout=out, stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
         return self
