@@ -37,6 +37,7 @@ SIGNATURES = {
     "fv_mesh_create": (c_int, [c_int, c_int, c_int, c_int, P, P, P, P, P, P, P]),
     "fv_mesh_destroy": (c_int, [P]),
     "fv_mesh_set_nodes": (c_int, [P, P, P]),
+    "fv_case_refresh_geometry": (c_int, [P, P]),
     "fv_mesh_geometry": (c_int, [P, P, P, P, P, P, P]),
     "fv_mesh_sizes": (c_int, [P, P, P, P, P]),
     "fv_case_create": (c_int, [P, ctypes.POINTER(FvCaseDesc), P, P, P, P, P, P, P, P, P, P]),

@@ -9,8 +9,9 @@ The reference differentiates its residual closure with ``jax.vjp`` (``aquaflux/s
     (R * w).sum().backward()
 
 ``mu`` and ``inlet_scale`` are 0-d tensors (or floats); ``nodes`` (optional) is an
-``(n_nodes, dim)`` tensor: when given, the mesh geometry is recomputed from it on the device (the
-SST wall distance of a turbulent case stays the one computed at case creation).
+``(n_nodes, dim)`` tensor: when given, the mesh geometry is recomputed from it on the device, and
+for a turbulent case the SST wall distance too (to each cell's nearest wall face found at case
+creation, held fixed -- the function the mesh-coordinate adjoint differentiates).
 """
 from __future__ import annotations
 
@@ -29,8 +30,7 @@ class _Residual(torch.autograd.Function):
         s = torch.as_tensor(state, dtype=torch.float64, device="cuda").contiguous()
         case.set_params(mu=float(mu), inlet_scale=float(inlet_scale))
         if nodes is not None:
-            nd = nodes.detach().to("cuda", torch.float64).contiguous()
-            check(lib().fv_mesh_set_nodes(case.dmesh.handle, ptr(nd), _stream()))
+            case.set_nodes(nodes.detach())
         ctx.case = case
         ctx.has_nodes = nodes is not None
         ctx.devices = (state.device if torch.is_tensor(state) else s.device, mu.device,

@@ -2,7 +2,8 @@
 
 ``nvcc`` compiles the translation units in parallel (one ``-gencode``), then links a shared
 library with a static CUDA runtime, so it loads beside any torch build.  ``sparse.cu`` is compiled
-with ``-fmad=false``: its fp64 ILU(0) must round exactly like the reference's sequential kernel.
+with ``-fmad=false``: its fp64 ILU(0) must round exactly like the reference's sequential kernel;
+``noalloc.cu`` too, so that its transposed SpMV rounds like ``sparse.cu``'s (bitwise the same).
 """
 from __future__ import annotations
 
@@ -16,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 ROOT = os.path.dirname(HERE)
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 UNITS = {"mesh.cu": [], "residual.cu": [], "capi.cu": [], "sparse.cu": ["-fmad=false"],
-         "colour.cu": [], "noalloc.cu": [], "amg.cu": []}
+         "colour.cu": [], "noalloc.cu": ["-fmad=false"], "amg.cu": []}
 
 
 def _nvcc() -> str:

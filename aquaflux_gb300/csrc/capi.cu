@@ -383,6 +383,29 @@ extern "C" int fv_case_set_block_size(FvCase* c, int threads) {
   return FV_OK;
 }
 
+extern "C" int fv_case_refresh_geometry(FvCase* c, void* stream) {
+  if (!c) {
+    fv_set_error("fv_case_refresh_geometry: null case");
+    return FV_ERR_ARG;
+  }
+  if (!c->desc.turbulent) return FV_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  FvMesh* m = c->mesh;
+  int rc = fv_wall_distance_refresh(m, c->swall, c->wnear, c->wd, c->wdg, c->desc.gradient_sweeps,
+                                    c->desc.gradient_relaxation, s);
+  if (rc != FV_OK) return rc;
+  k_inv_distance<<<fv_blocks(m->nc, 256), 256, 0, s>>>(m->nc, c->wd, c->inv_wd);
+  FV_CUDA_TRY(cudaGetLastError());
+  if (c->f32) {  // the fp32 mirrors of the wall distance, its gradient and reciprocals
+    const long nc = m->nc, dim = m->dim;
+    float* p = c->f32;
+    if ((rc = fv_d2f(nc, c->wd, p, s)) != FV_OK) return rc;
+    if ((rc = fv_d2f(dim * nc, c->wdg, p + nc, s)) != FV_OK) return rc;
+    if ((rc = fv_d2f(2 * nc, c->inv_wd, p + (1 + dim) * nc, s)) != FV_OK) return rc;
+  }
+  return FV_OK;
+}
+
 extern "C" int fv_case_wall_distance(const FvCase* c, double* distance, double* gradient,
                                      void* stream) {
   if (!c) {

@@ -194,6 +194,9 @@ enum { FV_TAN_NONE = 0, FV_TAN_STATE = 1, FV_TAN_MU = 2, FV_TAN_INLET = 3, FV_TA
 int fv_wall_distance_compute(FvMesh* m, const unsigned char* swall_dev, int n_wall_faces,
                              double* wd, double* wdg, int gradient_sweeps,
                              double gradient_relaxation, int* nearest_face, cudaStream_t s);
+// The same distance to each cell's kept nearest wall face (after the nodes moved) and its gradient.
+int fv_wall_distance_refresh(FvMesh* m, const unsigned char* swall_dev, const int* nearest,
+                             double* wd, double* wdg, int sweeps, double rel, cudaStream_t s);
 // Corrected Green-Gauss sweeps of one scalar field's gradient (residual.cu): on entry x0 holds
 // rel * B phi / V and num holds B phi; the last iterate lands in x0 or x1 by the sweep count's
 // parity (x0 when sweeps - 1 is even).

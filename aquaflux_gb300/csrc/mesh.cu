@@ -170,6 +170,22 @@ __global__ void k_wall_distance(MeshView m, const double* wall_xf, int n_wall, d
   }
 }
 
+// Distance from each cell centroid to the centroid of its kept nearest SST-wall face (the
+// geometry has moved; the nearest face found at case creation is held, as the mesh-coordinate
+// adjoint differentiates it).
+template <int DIM>
+__global__ void k_wall_distance_near(MeshView m, const int* nearest, double* wd) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nc) return;
+  const int f = nearest[c];
+  double s = 0.0;
+  for (int j = 0; j < DIM; ++j) {
+    double dd = m.xc[(long)j * m.nc + c] - m.xf[(long)j * m.nf + f];
+    s += dd * dd;
+  }
+  wd[c] = sqrt(s);
+}
+
 __global__ void k_gather_wall_xf(int nf, int dim, const unsigned char* swall, const int* slot,
                                  const double* xf, double* wall_xf, int n_wall) {
   int f = blockIdx.x * blockDim.x + threadIdx.x;
@@ -268,6 +284,37 @@ int fv_mesh_compute_geometry(FvMesh* m, cudaStream_t s) {
   return FV_OK;
 }
 
+namespace {
+// Green-Gauss gradient of the wall distance (compact, or corrected with `sweeps` sweeps).
+int wall_distance_gradient(FvMesh* m, const unsigned char* swall_dev, const double* wd,
+                           double* wdg, int sweeps, double rel, cudaStream_t s) {
+  int bc = fv_blocks(m->nc, kThreads);
+  // corrected scheme: B d, the other sweep iterate and the face scratch
+  double *num = nullptr, *galt = nullptr, *wface = nullptr;
+  double* x0 = wdg;
+  if (sweeps >= 2) {
+    FV_CUDA_TRY(cudaMalloc(&num, sizeof(double) * (size_t)m->dim * m->nc));
+    FV_CUDA_TRY(cudaMalloc(&galt, sizeof(double) * (size_t)m->dim * m->nc));
+    FV_CUDA_TRY(cudaMalloc(&wface, sizeof(double) * (size_t)m->nf));
+    if ((sweeps - 1) % 2 != 0) x0 = galt;
+  }
+  const double r0 = sweeps >= 1 ? rel : 1.0;
+  if (m->dim == 2)
+    k_wall_distance_gradient<2><<<bc, kThreads, 0, s>>>(m->view, swall_dev, wd, x0, num, r0);
+  else
+    k_wall_distance_gradient<3><<<bc, kThreads, 0, s>>>(m->view, swall_dev, wd, x0, num, r0);
+  int rc = FV_OK;
+  if (sweeps >= 2)
+    rc = fv_gg_sweeps_scalar(m->view, sweeps, rel, num, x0, x0 == wdg ? galt : wdg, wface, s);
+  FV_CUDA_TRY(cudaGetLastError());
+  FV_CUDA_TRY(cudaStreamSynchronize(s));
+  cudaFree(num);
+  cudaFree(galt);
+  cudaFree(wface);
+  return rc;
+}
+}  // namespace
+
 int fv_wall_distance_compute(FvMesh* m, const unsigned char* swall_dev, int n_wall, double* wd,
                              double* wdg, int sweeps, double rel, int* nearest, cudaStream_t s) {
   if (n_wall <= 0) {
@@ -296,35 +343,26 @@ int fv_wall_distance_compute(FvMesh* m, const unsigned char* swall_dev, int n_wa
                               cudaMemcpyHostToDevice, s));
   int bf = fv_blocks(m->nf, kThreads), bc = fv_blocks(m->nc, kThreads);
   k_gather_wall_xf<<<bf, kThreads, 0, s>>>(m->nf, m->dim, swall_dev, d_slot, m->view.xf, d_wxf, k);
-  // corrected scheme: B d, the other sweep iterate and the face scratch
-  double *num = nullptr, *galt = nullptr, *wface = nullptr;
-  double* x0 = wdg;
-  if (sweeps >= 2) {
-    FV_CUDA_TRY(cudaMalloc(&num, sizeof(double) * (size_t)m->dim * m->nc));
-    FV_CUDA_TRY(cudaMalloc(&galt, sizeof(double) * (size_t)m->dim * m->nc));
-    FV_CUDA_TRY(cudaMalloc(&wface, sizeof(double) * (size_t)m->nf));
-    if ((sweeps - 1) % 2 != 0) x0 = galt;
-  }
-  const double r0 = sweeps >= 1 ? rel : 1.0;
-  if (m->dim == 2) {
+  if (m->dim == 2)
     k_wall_distance<2><<<bc, 256, 0, s>>>(m->view, d_wxf, k, wd, d_slot_face, nearest);
-    k_wall_distance_gradient<2><<<bc, kThreads, 0, s>>>(m->view, swall_dev, wd, x0, num, r0);
-  } else {
+  else
     k_wall_distance<3><<<bc, 256, 0, s>>>(m->view, d_wxf, k, wd, d_slot_face, nearest);
-    k_wall_distance_gradient<3><<<bc, kThreads, 0, s>>>(m->view, swall_dev, wd, x0, num, r0);
-  }
-  int rc = FV_OK;
-  if (sweeps >= 2)
-    rc = fv_gg_sweeps_scalar(m->view, sweeps, rel, num, x0, x0 == wdg ? galt : wdg, wface, s);
-  FV_CUDA_TRY(cudaGetLastError());
-  FV_CUDA_TRY(cudaStreamSynchronize(s));
+  int rc = wall_distance_gradient(m, swall_dev, wd, wdg, sweeps, rel, s);
   cudaFree(d_slot);
   cudaFree(d_slot_face);
   cudaFree(d_wxf);
-  cudaFree(num);
-  cudaFree(galt);
-  cudaFree(wface);
   return rc;
+}
+
+int fv_wall_distance_refresh(FvMesh* m, const unsigned char* swall_dev, const int* nearest,
+                             double* wd, double* wdg, int sweeps, double rel, cudaStream_t s) {
+  int bc = fv_blocks(m->nc, kThreads);
+  if (m->dim == 2)
+    k_wall_distance_near<2><<<bc, kThreads, 0, s>>>(m->view, nearest, wd);
+  else
+    k_wall_distance_near<3><<<bc, kThreads, 0, s>>>(m->view, nearest, wd);
+  FV_CUDA_TRY(cudaGetLastError());
+  return wall_distance_gradient(m, swall_dev, wd, wdg, sweeps, rel, s);
 }
 
 extern "C" int fv_mesh_create(int dim, int n_cells, int n_faces, int n_nodes, const double* nodes,

@@ -2,16 +2,17 @@
 //
 // fv_bsr_spmv_f64(..., transpose = 1) builds a transpose map of the block pattern and allocates
 // device memory for it on every call.  Callers that cannot allocate device memory while they
-// run -- a CUDA-graph capture in progress, an FFI custom call inside a framework whose allocator
-// owns all device memory (an XLA custom call, say), or an embedded solver that forbids allocation
-// after start-up -- use fv_bsr_spmv_t_f64_noalloc instead.  It builds the same transpose map on
+// run -- an FFI custom call inside a framework whose allocator owns all device memory (an XLA
+// custom call, say), or an embedded solver that forbids allocation after start-up -- use
+// fv_bsr_spmv_t_f64_noalloc instead.  It builds the same transpose map on
 // the GPU inside one fixed-size scratch array declared below, which every GPU that loads this
 // library holds until the process exits.
 #include <mutex>
 
 #include "internal.cuh"
 
-// Scratch capacity in ints: the transpose map needs 2 * n_block_rows + 1 + 2 * nnzb of them.
+// Scratch capacity in ints: the transpose map needs 2 * n_block_rows + 1 + 2 * nnzb of them, plus
+// one status word.
 #define FV_NOALLOC_SCRATCH_INTS (4 * 1024 * 1024)  // 16 MiB
 
 static __device__ __align__(256) int g_noalloc_scratch[FV_NOALLOC_SCRATCH_INTS];
@@ -119,10 +120,21 @@ __global__ void k_na_sort(int nbc, long nnzb, const int* tptr, int* tidx, int* t
   }
 }
 
+// Status word: 1 when the pattern does not hold exactly nnzb in-range blocks (nnzb differs from
+// indptr[n], or some column index lies outside [0, n)); the gather then writes NaN everywhere.
+__global__ void k_na_check(int n, long nnzb, const int* ptr, const int* tptr, int* status) {
+  *status = ((long)ptr[n] != nnzb || (long)tptr[n] != nnzb) ? 1 : 0;
+}
+
 __global__ void k_na_gather(int nbc, long nnzb, int b, const int* tptr, const int* tidx,
-                            const int* tblk, const double* val, const double* x, double* y) {
+                            const int* tblk, const int* status, const double* val,
+                            const double* x, double* y) {
   long r = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= (long)nbc * b) return;
+  if (*status) {
+    y[r] = __longlong_as_double(0x7ff8000000000000LL);  // quiet NaN: the pattern was inconsistent
+    return;
+  }
   const int j = (int)(r / b), a = (int)(r % b);
   const long bb = (long)b * b;
   double acc = 0.0;
@@ -144,10 +156,10 @@ extern "C" int fv_bsr_spmv_t_f64_noalloc(int n_block_rows, long nnzb, int b, con
     fv_set_error("fv_bsr_spmv_t_f64_noalloc: bad arguments");
     return FV_ERR_ARG;
   }
-  const long need = 2L * n_block_rows + 1 + 2 * nnzb;
+  const long need = 2L * n_block_rows + 1 + 2 * nnzb + 1;
   if (need > FV_NOALLOC_SCRATCH_INTS) {
     fv_set_error(
-        "fv_bsr_spmv_t_f64_noalloc: the pattern needs %ld scratch ints (2 * n_block_rows + 1 + "
+        "fv_bsr_spmv_t_f64_noalloc: the pattern needs %ld scratch ints (2 * n_block_rows + 2 + "
         "2 * nnzb) but the fixed scratch array holds %d; use fv_bsr_spmv_f64 with transpose = 1",
         need, FV_NOALLOC_SCRATCH_INTS);
     return FV_ERR_ARG;
@@ -161,14 +173,16 @@ extern "C" int fv_bsr_spmv_t_f64_noalloc(int n_block_rows, long nnzb, int b, con
   int* cursor = tptr + n + 1;   // n
   int* tidx = cursor + n;       // nnzb
   int* tblk = tidx + nnzb;      // nnzb
+  int* status = tblk + nnzb;    // 1
   // counts and cursors must start at zero; the map entries are fully overwritten
   k_na_zero<<<fv_blocks(2L * n + 1, 256), 256, 0, s>>>(2L * n + 1, tptr);
   k_na_count<<<fv_blocks(n, 256), 256, 0, s>>>(n, indptr, indices, tptr);
   k_na_scan<<<1, 1024, 0, s>>>(n + 1, tptr);
   k_na_fill<<<fv_blocks(n, 256), 256, 0, s>>>(n, nnzb, indptr, indices, tptr, cursor, tidx, tblk);
+  k_na_check<<<1, 1, 0, s>>>(n, nnzb, indptr, tptr, status);
   k_na_sort<<<fv_blocks(n, 256), 256, 0, s>>>(n, nnzb, tptr, tidx, tblk);
-  k_na_gather<<<fv_blocks((long)n * b, 256), 256, 0, s>>>(n, nnzb, b, tptr, tidx, tblk, values, x,
-                                                         y);
+  k_na_gather<<<fv_blocks((long)n * b, 256), 256, 0, s>>>(n, nnzb, b, tptr, tidx, tblk, status,
+                                                         values, x, y);
   FV_CUDA_TRY(cudaGetLastError());
   return FV_OK;
 }

@@ -1101,12 +1101,27 @@ int spmv(int nbr, int b, const int* indptr, const int* indices, const V* values,
   std::vector<int> hp(nbr + 1);
   FV_CUDA_TRY(cudaMemcpyAsync(hp.data(), indptr, sizeof(int) * (nbr + 1), cudaMemcpyDeviceToHost, s));
   FV_CUDA_TRY(cudaStreamSynchronize(s));
+  for (int i = 0; i < nbr; ++i)
+    if (hp[i] > hp[i + 1] || hp[0] != 0) {
+      fv_set_error("fv_bsr_spmv: indptr is not a non-decreasing offset list from 0");
+      return FV_ERR_ARG;
+    }
   std::vector<int> hi(hp[nbr]);
   FV_CUDA_TRY(cudaMemcpy(hi.data(), indices, sizeof(int) * hp[nbr], cudaMemcpyDeviceToHost));
+  for (int q = 0; q < hp[nbr]; ++q)
+    if (hi[q] < 0 || hi[q] >= nbr) {
+      fv_set_error("fv_bsr_spmv: column index %d at block %d out of range [0, %d)", hi[q], q, nbr);
+      return FV_ERR_ARG;
+    }
   Transpose T;
   build_transpose(nbr, nbr, hp.data(), hi.data(), &T);
-  int *tp, *ti, *tb;
-  if (upload(T.ptr, &tp, s) || upload(T.idx, &ti, s) || upload(T.blk, &tb, s)) return FV_ERR_CUDA;
+  int *tp = nullptr, *ti = nullptr, *tb = nullptr;
+  if (upload(T.ptr, &tp, s) || upload(T.idx, &ti, s) || upload(T.blk, &tb, s)) {
+    cudaFree(tp);
+    cudaFree(ti);
+    cudaFree(tb);
+    return FV_ERR_CUDA;
+  }
   k_bsr_spmv_t<V><<<fv_blocks(rows, kThreads), kThreads, 0, s>>>(nbr, b, tp, ti, tb, values, x, y);
   FV_CUDA_TRY(cudaGetLastError());
   FV_CUDA_TRY(cudaStreamSynchronize(s));

@@ -352,6 +352,12 @@ class FlowCase:
         check(lib().fv_case_profile_end(self._h, ms, len(self.STAGES), ctypes.byref(n)))
         return {k: float(ms[i]) for i, k in enumerate(self.STAGES)}, int(n.value)
 
+    def set_nodes(self, nodes: torch.Tensor) -> None:
+        """Move the mesh nodes: recompute the geometry and (turbulent case) the SST wall
+        distance to each cell's nearest wall face, that face held fixed."""
+        self.dmesh.set_nodes(nodes)
+        check(lib().fv_case_refresh_geometry(self._h, _stream()))
+
     def wall_distance(self):
         C, D = self.n_cells, self.dim
         d = torch.empty(C, dtype=torch.float64, device="cuda")

@@ -290,7 +290,9 @@ def fgmres(matvec, b: torch.Tensor, precond=None, *, rtol: float = 1e-3, atol: f
                 continue
             # lagged: normalise on the device (a zero norm only arises where the cycle stops),
             # queue the column's copy, then reduce the previous column while this one runs
-            V[j + 1] = w / h[j + 1]
+            # (a zero norm -- a breakdown, which stops the cycle -- divides by 1 instead, so the
+            # discarded iteration queued behind it sees finite values)
+            V[j + 1] = w / torch.where(h[j + 1] > 0, h[j + 1], torch.ones_like(h[j + 1]))
             hbuf[j, : j + 2].copy_(h, non_blocking=True)
             ev = None
             if on_gpu:

@@ -58,7 +58,8 @@ int fv_mesh_create(int dim, int n_cells, int n_faces, int n_nodes,
                    const int* neighbour,     /* host (n_faces), -1 = boundary face */
                    void* stream, FvMesh** out);
 int fv_mesh_destroy(FvMesh* mesh);
-/* Replace the node coordinates (device (n_nodes, dim) row-major) and recompute the geometry. */
+/* Replace the node coordinates (device (n_nodes, dim) row-major) and recompute the geometry.
+ * Turbulent cases on this mesh then need fv_case_refresh_geometry (their wall distance). */
 int fv_mesh_set_nodes(FvMesh* mesh, const double* nodes_device, void* stream);
 /* Copy the geometry out in reference face order, device outputs (any may be NULL):
  * area (F), normal (F, dim), face_centroid (F, dim), volume (C), cell_centroid (C, dim). */
@@ -133,6 +134,12 @@ int fv_case_set_viscosity_field(FvCase* c, const double* mu_cell, void* stream);
 int fv_case_set_block_size(FvCase* c, int threads);
 int fv_case_autotune(FvCase* c, const double* state, const double* w, double* out, void* stream,
                      int* best);
+/* After fv_mesh_set_nodes: recompute a turbulent case's SST wall distance (to each cell's nearest
+ * wall face found at case creation, held fixed as the mesh-coordinate adjoint differentiates it),
+ * its gradient and their fp32 mirrors.  No-op for laminar cases.  The reference recomputes
+ * WallDistance from the mesh inside the differentiated residual (aquaflux/mesh/distance.py:52-84,
+ * aquaflux/turbulence/transport.py:86-111). */
+int fv_case_refresh_geometry(FvCase* c, void* stream);
 /* Device copies (C) and (C, dim) of the SST wall distance and its gradient (turbulent cases). */
 int fv_case_wall_distance(const FvCase* c, double* distance, double* gradient, void* stream);
 /* Number of unknowns: (dim + 1) * C, or (dim + 3) * C when turbulent. */
@@ -234,15 +241,18 @@ int fv_bsr_spmv_f64(int n_block_rows, int b, const int* indptr, const int* indic
                     const double* values, const double* x, double* y, int transpose,
                     void* stream);
 /* y = A^T x for a square BSR matrix (fp64) WITHOUT allocating device memory.  No counterpart in
- * the reference: it serves callers that cannot allocate while they run (a CUDA-graph capture, an
- * FFI custom call inside a framework that owns all device memory, an embedded solver that forbids
- * allocation after start-up), where fv_bsr_spmv_f64(transpose = 1) would allocate its transpose
- * map.  The map is built in a fixed 16 MiB static device array that every GPU loading the library
- * holds until exit; patterns needing more than 4,194,304 ints (2 * n_block_rows + 1 + 2 * nnzb)
- * are rejected with FV_ERR_ARG.  nnzb must equal indptr[n_block_rows].  The first call on each
- * device looks the array's address up (cudaGetSymbolAddress) and must come before any stream
- * capture.  All calls share the one array: calls that overlap on the GPU (different streams, or
- * concurrent host threads) race and give wrong results.  Device arrays. */
+ * the reference: it serves callers that cannot allocate while they run (an FFI custom call inside
+ * a framework that owns all device memory, such as an XLA custom call, or an embedded solver that
+ * forbids allocation after start-up), where fv_bsr_spmv_f64(transpose = 1) would allocate its
+ * transpose map.  The map is built in a fixed 16 MiB static device array that every GPU loading
+ * the library holds until exit; patterns needing more than 4,194,304 ints
+ * (2 * n_block_rows + 2 + 2 * nnzb) are rejected with FV_ERR_ARG.  nnzb must equal
+ * indptr[n_block_rows] and every column index must lie in [0, n_block_rows): otherwise every
+ * entry of y is set to NaN (the check runs on the GPU; nothing is read back).  The result is
+ * bitwise that of fv_bsr_spmv_f64(transpose = 1).  The first call on each device looks the
+ * array's address up (cudaGetSymbolAddress) and must come before any stream capture.  All calls
+ * share the one array: calls that overlap on the GPU (different streams, or concurrent host
+ * threads) race and give wrong results.  Device arrays. */
 int fv_bsr_spmv_t_f64_noalloc(int n_block_rows, long nnzb, int b, const int* indptr,
                               const int* indices, const double* values, const double* x,
                               double* y, void* stream);

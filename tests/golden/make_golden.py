@@ -2,7 +2,7 @@
 
 Run from the repository root, in a container that has the reference source checked out:
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <path of the reference checkout>
 
 JAX is not installed there, so the reference's forward code runs on :mod:`refshim` (numpy float64
 stand-ins for ``jax.numpy`` / ``equinox``).  Everything written here is produced by the reference's
@@ -34,7 +34,9 @@ import refshim  # noqa: E402
 
 refshim.install()
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+if len(sys.argv) < 2:
+    sys.exit("usage: make_golden.py <path of the reference checkout>")
+REF = sys.argv[1]
 sys.path.insert(0, REF)
 sys.path.insert(0, os.path.join(REF, "tests"))
 

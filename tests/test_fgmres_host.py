@@ -55,3 +55,18 @@ def test_lagged_fgmres_stops_at_a_breakdown():
     assert p.converged and q.converged and p.iterations == q.iterations == 3
     assert torch.equal(p.x, q.x)
     assert float(torch.linalg.vector_norm(a @ q.x - b)) <= 1e-12
+
+
+def test_lagged_fgmres_breakdown_keeps_the_queued_iteration_finite():
+    """An exact breakdown on the first column (identity operator): the iteration queued behind it
+    must see finite values, so a preconditioner that refuses non-finite input never fires."""
+    n = 8
+    b = torch.arange(1.0, n + 1.0, dtype=torch.float64)
+
+    def strict(v):
+        assert torch.isfinite(v).all(), "preconditioner saw a non-finite vector"
+        return v
+
+    q = fgmres(lambda v: v.clone(), b, strict, rtol=1e-14, restart=5, maxiter=10, lag=True)
+    assert q.converged and q.iterations == 1
+    assert torch.equal(q.x, b)
