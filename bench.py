@@ -56,7 +56,7 @@ def _args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--step", default="vjp", choices=["vjp", "jvp"])
     ap.add_argument("--no-newton", action="store_true", help="skip the Newton-solve timing")
-    ap.add_argument("--newton-kinds", default="amg,amg-natural,ilu",
+    ap.add_argument("--newton-kinds", default="amg,ilu",
                     help="preconditioners timed in the Newton block (comma list of amg (fine "
                          "order by dimension: coloured in 3D), amg-natural, amg-colour, ilu)")
     ap.add_argument("--workload", default="channel3d", choices=["channel3d", "batched"],
@@ -64,8 +64,10 @@ def _args():
                          "calibration sweep (its own JSON line)")
     ap.add_argument("--no-adjoint", action="store_true",
                     help="skip the adjoint objectives' gradients after the Newton solves")
-    ap.add_argument("--newton-oracle-check", action="store_true",
-                    help="also evaluate the converged fp32-preconditioned state with the CPU oracle")
+    ap.add_argument("--no-newton-oracle", action="store_true",
+                    help="skip the CPU oracle's residual of the converged Newton states")
+    ap.add_argument("--no-config1", action="store_true",
+                    help="skip the config-1 cavity Newton solve (GPU beside the CPU oracle)")
     ap.add_argument("--newton-only", default=None, metavar="KIND:PREC:TANGENTS",
                     help="run one Newton solve of that form (e.g. amg:32:32) on the channel and "
                          "print its timings only (for profiling the solve's kernels)")
@@ -187,50 +189,19 @@ class ClockSampler:
 
 
 # ----------------------------------------------------------------------------- algorithmic bytes
-def step_bytes_per_face(wl) -> float:
-    """Compulsory bytes of one residual + JVP evaluation per face.
+def step_bytes_per_face(wl, step: str = "vjp") -> float:
+    """Compulsory bytes of one residual + VJP (or residual + JVP) evaluation per face.
 
     Per face: owner + neighbour indices (8 B) and the area vector and centroid (2 dim 8 B).  Per
-    cell: the state and its tangent (2 n_f 8 B), centroid (dim 8 B), volume (8 B), wall distance
-    (8 B, SST) in; residual and J v (2 n_f 8 B) out.  Each distinct value counted once.
+    cell: the state (n_f 8 B), centroid (dim 8 B), volume (8 B), wall distance (8 B, SST) in and
+    the residual (n_f 8 B) out; the VJP (or JVP) adds its input vector (n_f 8 B) in and its result
+    (n_f 8 B) out.  Each distinct value counted once.  On the 128^3 SST channel: 132.7 B/face.
     """
     m = wl.mesh
     dim, nf = m.dim, m.dim + (3 if wl.sst else 1)
     per_face = 8 + 2 * dim * 8
-    per_cell = 2 * nf * 8 + dim * 8 + 8 + (8 if wl.sst else 0) + 2 * nf * 8
+    per_cell = nf * 8 + dim * 8 + 8 + (8 if wl.sst else 0) + nf * 8 + 2 * nf * 8
     return per_face + per_cell * m.n_cells / m.n_faces
-
-
-def flux_kernel_bytes(wl) -> float:
-    """Compulsory bytes of one launch of the dual-number face-flux kernel (``k_flux<Dual>``).
-
-    Per face: indices (8 B), the geometric factors it reads (area, normal, g, normal distance,
-    dpn, dnn, n.n, d, skew, tP, tN: 5 + 6 dim doubles) and the n_f dual fluxes written (16 B each);
-    per cell: the n_f dual state values, n_f * dim dual gradients, the dual d-coefficient and (SST)
-    the dual F1 and nu_t, each read once.
-    """
-    m = wl.mesh
-    dim, nf = m.dim, m.dim + (3 if wl.sst else 1)
-    per_face = 8 + (6 + 6 * dim) * 8 + nf * 16
-    per_cell = (nf + nf * dim + 1 + (2 if wl.sst else 0)) * 16
-    return m.n_faces * per_face + m.n_cells * per_cell
-
-
-def aflux_kernel_bytes(wl) -> float:
-    """Compulsory bytes of one launch of the adjoint face-flux kernel (``a_flux``, fp64).
-
-    Per face: indices (8 B), the factors it reads (area, normal, tP, tN, skew, dvec, n (x) skew,
-    n.n, 1/nd, g: 4 + 5 dim + dim^2 doubles) and the forward intermediates kept by the flux stage
-    (6 + dim + 8 doubles for SST).  Per cell in: state, gradients, F1, nu_t, the two diffusivities,
-    d, the flux-sum cotangent; out: state, gradient, d, F1 and nu_t adjoints.
-    """
-    m = wl.mesh
-    dim, nf = m.dim, m.dim + (3 if wl.sst else 1)
-    aux = 6 + dim + (8 if wl.sst else 0)
-    per_face = 8 + (4 + 5 * dim + dim * dim + aux) * 8
-    per_cell = (nf + nf * dim + (4 if wl.sst else 0) + 1 + nf) * 8 + \
-        (nf + nf * dim + 1 + (2 if wl.sst else 0)) * 8
-    return m.n_faces * per_face + m.n_cells * per_cell
 
 
 def measured_peaks() -> dict:
@@ -518,16 +489,18 @@ def run_gpu(args, rank: int, world: int, local_rank: int) -> dict | None:
 
     peaks = measured_peaks()
     dom = max(stage_ms, key=stage_ms.get)
-    # roofline of the dominant kernel of this step: its algorithmic bytes per launch over its
-    # CUDA-event duration; DRAM traffic and FP64-pipe utilisation from the committed ncu capture
-    if args.step == "vjp":
-        kname, kstage, kbytes, tkey = "a_flux<3, SST> (adjoint face fluxes)", "a_flux", \
-            aflux_kernel_bytes(wl), "a_flux"
-    else:
-        kname, kstage, kbytes, tkey = "k_flux<Dual, 3, SST> (JVP face fluxes)", "flux", \
-            flux_kernel_bytes(wl), "k_flux_dual"
+    # roofline of the dominant kernel of this step: the step's algorithmic bytes (each distinct
+    # input read once, each output written once: 132.7 B/face for residual + VJP on the SST
+    # channel) over that kernel's average CUDA-event launch duration; DRAM traffic and FP64-pipe
+    # utilisation of the same kernel from the committed ncu capture
+    bpf = step_bytes_per_face(wl, args.step)
+    alg_bytes = bpf * F
+    kname = {"vjp": "a_flux<3, SST> (adjoint face fluxes)",
+             "jvp": "k_flux<Dual, 3, SST> (JVP face fluxes)"}[args.step]
+    kstage, tkey = {"vjp": ("a_flux", "a_flux"), "jvp": ("flux", "k_flux_dual")}[args.step]
     k_avg_ms = stage_ms[kstage] / max(runs, 1)
-    achieved = kbytes / (k_avg_ms * 1e-3) / 1e9
+    achieved = alg_bytes / (k_avg_ms * 1e-3) / 1e9
+    step_gbs = alg_bytes / (ms / args.steps * 1e-3) / 1e9
     traffic, fp64 = None, None
     traffic_path = os.path.join(ROOT, "profiles", "flux_traffic.json")
     if os.path.exists(traffic_path) and args.size == 128:
@@ -535,7 +508,6 @@ def run_gpu(args, rank: int, world: int, local_rank: int) -> dict | None:
             tr = json.load(f).get(tkey, {})
         traffic = tr.get("bytes_128")
         fp64 = tr.get("fp64_pipe_active_pct")
-    bpf = step_bytes_per_face(wl)
     out = {
         "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4),
@@ -556,12 +528,15 @@ def run_gpu(args, rank: int, world: int, local_rank: int) -> dict | None:
         "gpu_launches": (6 + (5 if args.step == "vjp" else 0)) * args.steps,
         "stage_ms_per_step": {k: round(v / max(runs, 1), 4) for k, v in stage_ms.items()},
         "algorithmic_bytes_per_face": round(bpf, 2),
-        "step_achieved_gbs": round(bpf * F / (ms / args.steps * 1e-3) / 1e9, 1),
         "roofline": {"bound": "hbm", "kernel": kname, "dominant_stage": dom,
                      "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": round(achieved / peaks["hbm_gbs"], 4),
                      "traffic": round(traffic) if traffic else None,
-                     "algorithmic_bytes": round(kbytes), "kernel_ms": round(k_avg_ms, 4),
+                     "algorithmic_bytes": round(alg_bytes), "kernel_ms": round(k_avg_ms, 4),
+                     "bytes_rule": f"{bpf:.1f} B/face x {F} faces: the whole step's compulsory "
+                                   "bytes, charged to its dominant kernel's launch duration",
+                     "step_achieved_gbs": round(step_gbs, 1),
+                     "step_frac": round(step_gbs / peaks["hbm_gbs"], 4),
                      "peak_source": f"{peaks['source']} (MEASURED_PEAKS.json hbm_gbs)",
                      "fp64_pipe_active_pct_ncu": fp64,
                      "binding_limit": "fp64 pipe (see profiles/flux_kernels_channel3d_64.md)"},
@@ -578,7 +553,22 @@ def run_gpu(args, rank: int, world: int, local_rank: int) -> dict | None:
                 out["cpu_ilu"] = ilu_cpu_vs_gpu(args.ilu_sample)
             except Exception as e:  # reported, never allowed to lose the headline line
                 out["cpu_ilu"] = {"error": f"{type(e).__name__}: {e}"[:300]}
+        if not args.no_config1:
+            try:
+                out["config1_newton"] = config1_newton(args)
+            except Exception as e:  # reported, never allowed to lose the headline line
+                out["config1_newton"] = {"error": f"{type(e).__name__}: {e}"[:300]}
+    if "newton" in out:  # the headline Newton numbers last, where a truncated tail keeps them
+        out["newton_summary"] = newton_summary(out["newton"], args.newton_kinds.split(","))
     return out
+
+
+def _field_errors(a, b, n_fields: int) -> dict:
+    """max |a - b| / max |b| per field (field-major states) and over all fields."""
+    av, bv = a.view(n_fields, -1), b.view(n_fields, -1)
+    per = [float((av[q] - bv[q]).abs().max() / bv[q].abs().max().clamp_min(1e-300))
+           for q in range(n_fields)]
+    return {"max": max(per), "per_field": [float(f"{e:.3g}") for e in per]}
 
 
 def newton_block(args, wl, case) -> dict:
@@ -589,7 +579,9 @@ def newton_block(args, wl, case) -> dict:
     Every form: fp64 residual, fp64 FGMRES(30) with Krylov orthogonalisation, fp64 Newton update
     and line search, so every form converges to the fp64 root.  Each solve is timed whole, from
     the initial state and including the preconditioner's setup (pattern, hierarchy, factors; the
-    "setup" phase).  Stops at ||R|| <= 1e-12 + 1e-10 ||R0||.
+    "setup" phase).  Stops at ||R|| <= 1e-12 + 1e-10 ||R0||.  Every converged state is then checked
+    against the FP64 CPU oracle (its residual relative to the oracle's ||R(s0)||) and against a
+    tightly converged FP64 root (per-field relative field error).
     """
     import numpy as np
     import torch
@@ -616,10 +608,11 @@ def newton_block(args, wl, case) -> dict:
     # captures), so that the timed solves below measure steady-state work
     from aquaflux_gb300 import workloads
 
+    kinds = args.newton_kinds.split(",")
     warm = workloads.channel3d(16)
     warm_case = warm.device_case()
     forms = ((64, 64), (32, 64), (32, 32))  # (preconditioner precision, tangent precision)
-    for kind in args.newton_kinds.split(","):
+    for kind in kinds:
         for prec, tan in forms:
             solve.newton_solve(warm_case, warm.initial_state(), precision=prec, tangents=tan,
                                kind="amg" if kind.startswith("amg") else kind, max_steps=40)
@@ -630,7 +623,7 @@ def newton_block(args, wl, case) -> dict:
     solve.newton_solve(case, wl.initial_state(), precision=64, kind="amg", max_steps=2)
     torch.cuda.synchronize()
     states = {}
-    for kind in args.newton_kinds.split(","):
+    for kind in kinds:
         for prec, tan in forms:
             torch.cuda.synchronize()
             opts = ({"fine_order": "colour"} if kind == "amg-colour" else
@@ -646,27 +639,104 @@ def newton_block(args, wl, case) -> dict:
                 "phase_seconds": {k: round(v, 3) for k, v in res.phase_seconds.items()}}
             states[(kind, prec, tan)] = res.state
             del res
-        a = states[(kind, 64, 64)]
         for prec, tan in forms[1:]:
             key = f"{kind}_fp{prec}" + ("_fp32_tangents" if tan == 32 else "")
-            b = states[(kind, prec, tan)]
-            out[f"{key}_vs_fp64_field_max_rel_diff"] = float((a - b).abs().max() / a.abs().max())
             out[f"{key}_speedup_vs_fp64"] = round(
                 out[f"{kind}_fp64"]["seconds"] / out[key]["seconds"], 3)
     if not args.no_adjoint:
-        out["adjoint"] = adjoint_block(case, states[(args.newton_kinds.split(",")[0], 32, 64)])
-    if args.newton_oracle_check:
+        out["adjoint"] = adjoint_block(case, states[(kinds[0], 32, 64)])
+    # a tight FP64 root: the fp64 AMG solution refined by Newton with tight linear solves until
+    # the residual stops falling; every form's fields are compared with it
+    nfld = case.n_unknowns // wl.mesh.n_cells
+    first = states[(kinds[0], 64, 64)]
+    tight = solve.newton_solve(case, first, precision=64, kind="amg", rtol=1e-14, atol=0.0,
+                               linear_rtol=1e-8, max_steps=4)
+    r0 = float(torch.linalg.vector_norm(case.residual(s0)))
+    out["tight_root"] = {"rel_residual": tight.residual_norms[-1] / r0,
+                         "newton_steps": tight.steps}
+    for (kind, prec, tan), st in states.items():
+        key = f"{kind}_fp{prec}" + ("_fp32_tangents" if tan == 32 else "")
+        out[key]["field_error_vs_tight_root"] = _field_errors(st, tight.state, nfld)
+    # the FP64 CPU oracle's residual of every converged state, relative to its ||R(s0)||
+    if not args.no_newton_oracle:
         from oracle import fv_oracle as fo
 
         torch.set_num_threads(os.cpu_count() or 1)
+        t0 = time.perf_counter()
         c = fo.make_case(wl.mesh, mu=wl.mu, rho=wl.rho, flow_bc=wl.flow_bc,
                          sst={"nu": wl.mu / wl.rho, "walls": wl.sst["walls"], "k": wl.sst["k"],
                               "omega": wl.sst["omega"]})
         orc = fo.Oracle(c)
-        r0 = float(np.linalg.norm(orc.residual(torch.as_tensor(wl.initial_state())).numpy()))
-        kind = args.newton_kinds.split(",")[0]
-        r32 = float(np.linalg.norm(orc.residual(states[(kind, 32, 64)].cpu()).numpy()))
-        out["fp32_oracle_rel_residual"] = r32 / r0
+        r0o = float(np.linalg.norm(orc.residual(torch.as_tensor(wl.initial_state())).numpy()))
+        for (kind, prec, tan), st in states.items():
+            key = f"{kind}_fp{prec}" + ("_fp32_tangents" if tan == 32 else "")
+            ro = float(np.linalg.norm(orc.residual(st.cpu()).numpy()))
+            out[key]["oracle_rel_residual"] = ro / r0o
+        out["oracle_check_seconds"] = round(time.perf_counter() - t0, 1)
+    return out
+
+
+def config1_newton(args) -> dict:
+    """Config 1 (64 x 64 lid-driven cavity, Re = 100, from rest): the GPU Newton solve in fp64 and
+    with the fp32 ILU(0) preconditioner, beside the CPU oracle's Newton (exact sparse Jacobian,
+    sparse LU; one process, all host threads for the residual products) to the same tolerance,
+    and each GPU root against the CPU root."""
+    import numpy as np
+    import torch
+
+    from aquaflux_gb300 import solve, workloads
+    from oracle import fv_oracle as fo
+    from oracle.newton_oracle import OracleJacobian, newton
+
+    wl = workloads.cavity(64)
+    case = wl.device_case()
+    z = np.zeros(case.n_unknowns)
+    out = {"workload": "64 x 64 lid-driven cavity, Re = 100, zero start, to 1e-10 relative"}
+    states = {}
+    for prec in (64, 32):
+        solve.newton_solve(case, z, precision=prec, max_steps=40)  # warm
+        torch.cuda.synchronize()
+        res = solve.newton_solve(case, z, precision=prec, max_steps=40)
+        states[prec] = res.state.cpu().numpy()
+        out[f"gpu_ilu_fp{prec}"] = {"seconds": round(res.seconds, 3), "newton_steps": res.steps,
+                                   "converged": bool(res.converged)}
+    torch.set_num_threads(os.cpu_count() or 1)
+    orc = fo.Oracle(fo.make_case(wl.mesh, mu=wl.mu, rho=wl.rho, flow_bc=wl.flow_bc,
+                                 pressure_pin=wl.pressure_pin))
+    jac = OracleJacobian(orc, wl.mesh.owner, wl.mesh.neighbour, wl.mesh.n_cells, 3)
+    cpu = newton(orc, jac, z)
+    out["cpu_oracle"] = {"seconds": round(cpu["seconds"], 2), "newton_steps": cpu["steps"],
+                         "converged": bool(cpu["converged"]), "cores": os.cpu_count() or 1,
+                         "kind": "port", "what": "oracle residual, exact sparse Jacobian from "
+                                                 "reverse-mode products, SuperLU solves"}
+    root = cpu["state"]
+    for prec, st in states.items():
+        out[f"gpu_ilu_fp{prec}"]["field_max_rel_diff_vs_cpu_root"] = float(
+            np.abs(st - root).max() / np.abs(root).max())
+    out["gpu_fp32_speedup_vs_cpu"] = round(cpu["seconds"] / out["gpu_ilu_fp32"]["seconds"], 1)
+    return out
+
+
+def newton_summary(nb: dict, kinds: list) -> dict:
+    """The headline Newton numbers, repeated at the end of the JSON line."""
+    out = {}
+    for kind in kinds:
+        f64, f32, t32 = (nb.get(f"{kind}_fp64"), nb.get(f"{kind}_fp32"),
+                         nb.get(f"{kind}_fp32_fp32_tangents"))
+        if not f64:
+            continue
+        out[kind] = {"fp64_s": f64["seconds"], "fp32_precond_s": f32["seconds"],
+                     "fp32_precond_speedup": nb.get(f"{kind}_fp32_speedup_vs_fp64"),
+                     "fp32_precond_fp32_tangents_s": t32["seconds"],
+                     "fp32_precond_fp32_tangents_speedup":
+                         nb.get(f"{kind}_fp32_fp32_tangents_speedup_vs_fp64"),
+                     "max_oracle_rel_residual": max(
+                         (nb[k].get("oracle_rel_residual", float("nan"))
+                          for k in (f"{kind}_fp64", f"{kind}_fp32", f"{kind}_fp32_fp32_tangents")),
+                         default=None),
+                     "max_field_error_vs_tight_root": max(
+                         nb[k]["field_error_vs_tight_root"]["max"]
+                         for k in (f"{kind}_fp64", f"{kind}_fp32", f"{kind}_fp32_fp32_tangents"))}
     return out
 
 

@@ -187,3 +187,50 @@ def test_assembled_jacobian_overwrites_stale_values():
     jac.values.fill_(7.0)
     b = jac.materialize(s)
     assert torch.equal(a, b)
+
+
+@pytest.fixture(scope="module")
+def cavity64_solves():
+    """Config 1: the 64 x 64 lid-driven cavity (Re = 100), solved from the zero state on the GPU
+    with the fp64 and the fp32-preconditioned forms (ILU(0) and AMG)."""
+    from aquaflux_gb300.solve import newton_solve
+
+    m, case = _cavity(64)
+    out = {}
+    for kind, prec in (("ilu", 64), ("ilu", 32), ("amg", 32)):
+        res = newton_solve(case, np.zeros(case.n_unknowns), kind=kind, precision=prec,
+                           max_steps=40)
+        out[(kind, prec)] = res
+    return m, out
+
+
+def test_config1_cavity_64_newton_meets_the_oracle_residual(cavity64_solves):
+    """Every form stops at the reference's tolerance on the oracle's own residual:
+    ||R_oracle(s)|| <= 1e-12 + 1e-10 ||R_oracle(0)||."""
+    m, out = cavity64_solves
+    cd = fo.make_case(m, mu=0.01, rho=1.0, flow_bc=CAVITY_BC, pressure_pin=0)
+    orc = fo.Oracle(cd)
+    r0 = float(np.linalg.norm(orc.residual(torch.zeros(3 * 64 * 64, dtype=torch.float64))))
+    for key, res in out.items():
+        assert res.converged, (key, res.residual_norms)
+        r = orc.residual(torch.as_tensor(res.state.cpu().numpy())).numpy()
+        assert np.linalg.norm(r) <= 1e-12 + 1e-10 * r0, key
+
+
+def test_config1_cavity_64_newton_matches_an_independent_root(cavity64_solves):
+    """The converged fields against an independent FP64 root: the oracle's Newton with the exact
+    sparse Jacobian (reverse-mode products of the oracle) and sparse LU solves, refined from the
+    fp64 GPU solution until its residual stops falling; <= 1e-8 relative for every form."""
+    from oracle.newton_oracle import OracleJacobian, newton
+
+    m, out = cavity64_solves
+    cd = fo.make_case(m, mu=0.01, rho=1.0, flow_bc=CAVITY_BC, pressure_pin=0)
+    orc = fo.Oracle(cd)
+    jac = OracleJacobian(orc, m.owner, m.neighbour, 64 * 64, 3)
+    ref = newton(orc, jac, out[("ilu", 64)].state.cpu().numpy(), rtol=0.0, atol=0.0,
+                 max_steps=3, min_steps=1)
+    root = ref["state"]
+    assert ref["residual_norms"][-1] <= 1e-13
+    for key, res in out.items():
+        s = res.state.cpu().numpy()
+        assert np.abs(s - root).max() <= 1e-8 * np.abs(root).max(), key
