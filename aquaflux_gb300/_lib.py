@@ -74,6 +74,14 @@ SIGNATURES = {
     "fv_ilu0_apply": (c_int, [P, P, P, c_int, P]),
     "fv_ilu0_factor_values": (c_int, [P, P, P]),
     "fv_dot_f64": (c_int, [c_long, P, P, P, P]),
+    "fv_cell_graph": (c_int, [c_int, c_long, P, P, P, P, P, P]),
+    "fv_rcm_permutation": (c_int, [c_int, P, P, P, P, P, P]),
+    "fv_krylov_create": (c_int, [c_int, P]),
+    "fv_krylov_destroy": (c_int, [P]),
+    "fv_krylov_start": (c_int, [P, c_long, P, P, P, P]),
+    "fv_krylov_arnoldi": (c_int, [P, c_int, c_long, P, P, P, P]),
+    "fv_krylov_update": (c_int, [P, c_int, c_long, P, P, P]),
+    "fv_krylov_norm": (c_int, [P, c_long, P, P, P]),
     "fv_saturation_colouring": (c_int, [c_int, P, P, P, P]),
     "fv_greedy_colouring": (c_int, [c_int, P, P, P, P]),
     "fv_coarsen": (c_int, [c_int, P, P, P, c_int, P, P, P, P, P, P, P]),

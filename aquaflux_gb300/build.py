@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 ROOT = os.path.dirname(HERE)
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 UNITS = {"mesh.cu": [], "residual.cu": [], "capi.cu": [], "sparse.cu": ["-fmad=false"],
-         "colour.cu": [], "noalloc.cu": ["-fmad=false"], "amg.cu": []}
+         "colour.cu": [], "noalloc.cu": ["-fmad=false"], "amg.cu": [], "krylov.cu": [], "rcm.cu": []}
 
 
 def _nvcc() -> str:

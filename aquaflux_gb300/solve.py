@@ -211,113 +211,110 @@ class KrylovResult:
     converged: bool
 
 
-def fgmres(matvec, b: torch.Tensor, precond=None, *, rtol: float = 1e-3, atol: float = 0.0,
-           restart: int = 30, maxiter: int = 300, lag: bool = False) -> KrylovResult:
-    """Flexible GMRES(restart), right-preconditioned, CGS2 orthogonalisation, fp64.
+class KrylovWorkspace:
+    """Device storage of FGMRES(m) for vectors of length ``n``, allocated once and reused by every
+    solve given it: the Arnoldi basis ``V`` (m + 1, n), the preconditioned basis ``Z`` (m, n), and
+    the library's Hessenberg / Givens / reduction workspace (``fv_krylov_create``); plus a pinned
+    host buffer the per-iteration residual estimates are copied into."""
 
-    ``lag=True`` reads each new Hessenberg column back to the host (a pinned buffer) only after
-    the next iteration's work has been queued, so the device is not left idle while the host
-    issues that work; the convergence test then lags by one iteration, and the iteration queued
-    past convergence is discarded (it costs one more preconditioner application and operator
-    product per restart cycle that converges before its last column).  The arithmetic is that of
-    ``lag=False`` except that each new basis vector is divided by its norm held on the device
-    rather than on the host (bitwise the same on CPU tensors; on the GPU the division by a host
-    scalar may round differently)."""
+    def __init__(self, n: int, m: int):
+        import ctypes
+
+        self.n, self.m = int(n), int(m)
+        self.V = torch.empty(m + 1, n, dtype=torch.float64, device="cuda")
+        self.Z = torch.empty(m, n, dtype=torch.float64, device="cuda")
+        self.dnorm = torch.zeros(1, dtype=torch.float64, device="cuda")
+        self.est = torch.zeros(m + 1, 2, dtype=torch.float64).pin_memory()
+        h = ctypes.c_void_p()
+        check(lib().fv_krylov_create(m, ctypes.byref(h)))
+        self._h = h
+
+    def norm(self, x: torch.Tensor) -> float:
+        """``||x||`` by the workspace's deterministic reduction (waits for the result)."""
+        check(lib().fv_krylov_norm(self._h, x.numel(), ptr(x), ptr(self.dnorm), _stream()))
+        return float(self.dnorm.item())
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                lib().fv_krylov_destroy(h)
+            except Exception:
+                pass
+
+
+def fgmres(matvec, b: torch.Tensor, precond=None, *, rtol: float = 1e-3, atol: float = 0.0,
+           restart: int = 30, maxiter: int = 300,
+           workspace: KrylovWorkspace | None = None) -> KrylovResult:
+    """Flexible GMRES(restart), right-preconditioned, CGS2 orthogonalisation, fp64, on the device.
+
+    The reference's ``solve_linear`` (``aquaflux/solve/linear.py:199-298``) with lineax GMRES.  Each
+    Arnoldi step is the library's ``fv_krylov_arnoldi`` (deterministic projections, the Hessenberg
+    column, the Givens reduction and the residual estimate ``|g_{j+1}|`` computed on the device);
+    the host copies the two-number estimate into pinned memory and reads it only after the next
+    iteration has been queued, so the device never waits for the host.  The iteration queued past
+    convergence is discarded (its column is not used); near the tolerance, where the estimates'
+    decay predicts convergence at the current column, the host reads that column before queueing
+    another.  Each cycle ends with ``x += Z y`` (``fv_krylov_update``, the triangular solve on the
+    device) and the true residual ``b - A x``.  Results are bitwise identical run to run.
+    """
+    if not b.is_cuda:
+        raise ValueError("fgmres runs on the GPU: b must be a CUDA tensor")
+    n = b.numel()
+    ws = workspace
+    if ws is None or ws.n != n or ws.m < restart:
+        ws = KrylovWorkspace(n, restart)
     M = precond if precond is not None else (lambda v: v)
+    L = lib()
     x = torch.zeros_like(b)
-    bnorm = float(torch.linalg.vector_norm(b))
+    bnorm = ws.norm(b)
     tol = max(atol, rtol * bnorm)
-    r = b.clone()
-    beta = bnorm
-    total = 0
-    if beta <= tol:
-        return KrylovResult(x, 0, beta, True)
-    on_gpu = b.is_cuda
+    if bnorm <= tol:
+        return KrylovResult(x, 0, bnorm, True)
+    r, beta, total = b, bnorm, 0
+    V, Z, est = ws.V, ws.Z, ws.est
     while total < maxiter:
         m = min(restart, maxiter - total)
-        V = torch.empty(m + 1, b.numel(), dtype=torch.float64, device=b.device)
-        Z = torch.empty(m, b.numel(), dtype=torch.float64, device=b.device)
-        H = np.zeros((m + 1, m))
-        cs, sn = np.zeros(m), np.zeros(m)
-        g = np.zeros(m + 1)
-        g[0] = beta
-        V[0] = r / beta
+        check(L.fv_krylov_start(ws._h, n, ptr(r), ptr(V[0]), 0, _stream()))
+        seen = [beta]     # residual estimates read so far in this cycle
         k_done = 0
-        hbuf = (torch.empty((m, m + 1), dtype=torch.float64, pin_memory=on_gpu)
-                if lag else None)
-        pending = []  # lagged columns: (j, device column or host view, event)
+        pending = None    # (column, event) queued but not yet read
 
-        def column(j):
-            """Orthogonalise A M v_j against the basis; the new column h (device)."""
-            Z[j] = M(V[j])
-            w = matvec(Z[j])
-            # classical Gram-Schmidt with one re-orthogonalisation (CGS2): two matrix-vector
-            # products against the basis instead of j + 1 dependent dot products
-            Vj = V[: j + 1]
-            h1 = Vj @ w
-            w = w - h1 @ Vj
-            h2 = Vj @ w
-            w = w - h2 @ Vj
-            h = torch.cat([h1 + h2, torch.linalg.vector_norm(w).reshape(1)])
-            return h, w
-
-        def reduce(j, hh) -> bool:
-            """Givens-reduce column j; True when the cycle stops after it."""
+        def read(jp, ev) -> bool:
+            """Read column jp's estimate; True when the cycle stops after it."""
             nonlocal k_done, total
-            H[: j + 2, j] = hh
-            for i in range(j):  # apply the previous rotations
-                t = cs[i] * H[i, j] + sn[i] * H[i + 1, j]
-                H[i + 1, j] = -sn[i] * H[i, j] + cs[i] * H[i + 1, j]
-                H[i, j] = t
-            den = math.hypot(H[j, j], H[j + 1, j])
-            cs[j], sn[j] = (1.0, 0.0) if den == 0 else (H[j, j] / den, H[j + 1, j] / den)
-            H[j, j] = cs[j] * H[j, j] + sn[j] * H[j + 1, j]
-            H[j + 1, j] = 0.0
-            g[j + 1] = -sn[j] * g[j]
-            g[j] = cs[j] * g[j]
-            k_done = j + 1
+            ev.synchronize()
+            e, hnext = est[jp].tolist()
+            seen.append(e)
+            k_done = jp + 1
             total += 1
-            return abs(g[j + 1]) <= tol or hh[j + 1] == 0
+            return e <= tol or hnext == 0.0
 
+        stop = False
         for j in range(m):
-            h, w = column(j)
-            if not lag:
-                hh = h.cpu().numpy()
-                if hh[j + 1] > 0:
-                    V[j + 1] = w / hh[j + 1]
-                if reduce(j, hh):
-                    break
-                continue
-            # lagged: normalise on the device (a zero norm only arises where the cycle stops),
-            # queue the column's copy, then reduce the previous column while this one runs
-            # (a zero norm -- a breakdown, which stops the cycle -- divides by 1 instead, so the
-            # discarded iteration queued behind it sees finite values)
-            V[j + 1] = w / torch.where(h[j + 1] > 0, h[j + 1], torch.ones_like(h[j + 1]))
-            hbuf[j, : j + 2].copy_(h, non_blocking=True)
-            ev = None
-            if on_gpu:
-                ev = torch.cuda.Event()
-                ev.record()
-            pending.append((j, ev))
-            if len(pending) == 2:
-                jp, evp = pending.pop(0)
-                if evp is not None:
-                    evp.synchronize()
-                if reduce(jp, hbuf[jp, : jp + 2].numpy().copy()):
-                    pending.clear()
-                    break
-        else:
-            for jp, evp in pending:
-                if evp is not None:
-                    evp.synchronize()
-                if reduce(jp, hbuf[jp, : jp + 2].numpy().copy()):
-                    break
-        y = np.zeros(k_done)
-        for i in range(k_done - 1, -1, -1):
-            y[i] = (g[i] - H[i, i + 1:k_done] @ y[i + 1:]) / H[i, i]
-        x = x + torch.as_tensor(y, device=b.device) @ Z[:k_done]
+            if pending is not None and len(seen) >= 2:
+                # the last estimate read and its decay predict the pending column's estimate
+                pred = seen[-1] * min(1.0, seen[-1] / max(seen[-2], 1e-300))
+                if pred <= tol:
+                    stop = read(*pending)
+                    pending = None
+                    if stop:
+                        break
+            Z[j].copy_(M(V[j]))
+            w = matvec(Z[j])
+            check(L.fv_krylov_arnoldi(ws._h, j, n, ptr(V), ptr(w), ptr(est[j]), _stream()))
+            ev = torch.cuda.Event()
+            ev.record()
+            if pending is not None and read(*pending):
+                pending = None
+                stop = True
+                break
+            pending = (j, ev)
+        if not stop and pending is not None:
+            read(*pending)
+        check(L.fv_krylov_update(ws._h, k_done, n, ptr(Z), ptr(x), _stream()))
         r = b - matvec(x)
-        beta = float(torch.linalg.vector_norm(r))
+        beta = ws.norm(r)
         if beta <= tol:
             return KrylovResult(x, total, beta, True)
     return KrylovResult(x, total, beta, False)
@@ -339,8 +336,7 @@ def newton_solve(case, state0, *, rtol: float = 1e-10, atol: float = 1e-12, max_
                  max_krylov: int = 300, precision: int = 32, reach: int = 1, frozen: bool = True,
                  refresh_every: int = 1, line_search_steps: int = 10,
                  preconditioner=None, kind: str = "ilu",
-                 precond_options: dict | None = None, tangents: int = 64,
-                 krylov_lag: bool = False) -> NewtonResult:
+                 precond_options: dict | None = None, tangents: int = 64) -> NewtonResult:
     """Newton's method with FGMRES, preconditioned by ILU(0) of the materialised Jacobian
     (``kind="ilu"``) or by an ILU(0)-smoothed aggregation V-cycle (``kind="amg"``), in fp32 or
     fp64 (``precision``).
@@ -349,8 +345,8 @@ def newton_solve(case, state0, *, rtol: float = 1e-10, atol: float = 1e-12, max_
     ``J v`` (``fv_jvp_f32``) and the preconditioner's Jacobian assembly
     (``fv_assemble_jacobian_f32``).  The residual, the Newton update, the line search and the
     stopping test stay fp64, so the root is the fp64 root; only the linear solves, already
-    inexact at ``linear_rtol``, see fp32 rounding.  ``krylov_lag`` selects the FGMRES variant
-    whose convergence test lags one iteration behind the queued work (``fgmres(lag=True)``)."""
+    inexact at ``linear_rtol``, see fp32 rounding.  The FGMRES bases are allocated once per
+    solve (:class:`KrylovWorkspace`)."""
     if tangents not in (32, 64):
         raise ValueError(f"tangents must be 64 or 32, got {tangents}")
     t_all = time.perf_counter()
@@ -364,6 +360,7 @@ def newton_solve(case, state0, *, rtol: float = 1e-10, atol: float = 1e-12, max_
             preconditioner = AmgPreconditioner(jac, precision, **(precond_options or {}))
         else:
             preconditioner = IluPreconditioner(jac, precision)
+    kws = KrylovWorkspace(s.numel(), restart)
     torch.cuda.synchronize()
     # "setup": pattern, hierarchy plan and factor structures (host work, once per solve here);
     # "precond_setup": the per-refresh materialisation and factorisation
@@ -379,7 +376,7 @@ def newton_solve(case, state0, *, rtol: float = 1e-10, atol: float = 1e-12, max_
         return out
 
     r = timed("residual", case.residual, s)
-    norms = [float(torch.linalg.vector_norm(r))]
+    norms = [kws.norm(r)]
     target = atol + rtol * norms[0]
     its = []
     converged = norms[0] <= target
@@ -390,7 +387,7 @@ def newton_solve(case, state0, *, rtol: float = 1e-10, atol: float = 1e-12, max_
         res = timed("krylov", lambda: fgmres(lambda v: case.jvp(s, v, precision=tangents), -r,
                                              preconditioner.apply,
                                              rtol=linear_rtol, restart=restart,
-                                             maxiter=max_krylov, lag=krylov_lag))
+                                             maxiter=max_krylov, workspace=kws))
         its.append(res.iterations)
         delta = res.x
 
@@ -401,7 +398,7 @@ def newton_solve(case, state0, *, rtol: float = 1e-10, atol: float = 1e-12, max_
             for _ in range(line_search_steps + 1):
                 cand = s + alpha * delta
                 rc = case.residual(cand)
-                nc = float(torch.linalg.vector_norm(rc))
+                nc = kws.norm(rc)
                 if math.isfinite(nc):
                     best = (cand, rc, nc) if best is None or nc < best[2] else best
                     if nc < ref:

@@ -109,15 +109,26 @@ def rcm_permutation(mesh: fm.MeshData) -> np.ndarray:
 
 
 def channel3d(nx: int = 128, ny: int | None = None, nz: int | None = None, *, nu: float = 5e-4,
-              seed: int = 0, renumber: bool = True) -> Workload:
+              seed: int = 0, renumber: bool | str = True) -> Workload:
+    """``renumber``: True or ``"gpu"`` -- random relabelling, then reverse Cuthill-McKee computed
+    on the GPU (:mod:`aquaflux_gb300.reorder`); ``"host"`` -- the same permutation by scipy on
+    the host (the reference's own call; for machines without a GPU); False -- natural order."""
     ny = nx if ny is None else ny
     nz = nx if nz is None else nz
     extent = (2.0, 1.0, 1.0)
     m = fm.structured_grid_3d(nx, ny, nz, *extent)
     m = m.with_nodes(fm.bump_channel_nodes_3d((nx, ny, nz), extent, 0.1, 0.1, seed))
+    if renumber not in (True, False, "gpu", "host"):
+        raise ValueError(f"renumber must be True, False, 'gpu' or 'host', got {renumber!r}")
     if renumber:
         m = fm.permute_cells(m, fm.random_permutation(m.n_cells, seed))
-        m = fm.permute_cells(m, rcm_permutation(m))
+        if renumber == "host":
+            perm = rcm_permutation(m)
+        else:
+            from .reorder import mesh_rcm_permutation
+
+            perm = mesh_rcm_permutation(m)
+        m = fm.permute_cells(m, perm)
     k_in = inlet_k(1.0, 0.05)
     w_in = inlet_omega(k_in, 0.07)
     walls = ["bottom", "top", "back", "front"]

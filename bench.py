@@ -225,7 +225,7 @@ def cpu_residual_jvp_rate(size: int, min_seconds: float = 8.0, step: str = "vjp"
 
     threads = os.cpu_count() or 1
     torch.set_num_threads(threads)
-    wl = workloads.channel3d(size)
+    wl = workloads.channel3d(size, renumber="host")
     walls = wl.sst["walls"]
     case = fo.make_case(wl.mesh, mu=wl.mu, rho=wl.rho, flow_bc=wl.flow_bc,
                         sst={"nu": wl.mu / wl.rho, "walls": walls, "k": wl.sst["k"],

@@ -388,6 +388,47 @@ int fv_dot_f64(long n, const double* x, const double* y, double* out, void* stre
 int fv_segment_dot(int n_seg, const int* seg, int nfld, int nc, const double* a, const double* b,
                    double* out, void* stream);
 
+/* ------------------------------------------------------------------------------------------
+ * Cell renumbering on the GPU.  Replaces ReverseCuthillMcKee.permutation
+ * (aquaflux/mesh/reorder.py:147-159) over cell_adjacency_coo (aquaflux/mesh/graph.py:29-56): the
+ * same permutation as scipy.sparse.csgraph.reverse_cuthill_mckee(symmetric_mode=True).
+ * ------------------------------------------------------------------------------------------ */
+/* Symmetric cell graph of n_pairs interior (owner, neighbour) pairs (device) as sorted,
+ * coalesced CSR: indptr (n + 1), indices (up to 2 n_pairs; indptr[n] used).  work: 2 n + 2 +
+ * 2 n_pairs ints (device).  Pairs out of range or joining a cell to itself are refused. */
+int fv_cell_graph(int n, long n_pairs, const int* owner, const int* neighbour, int* indptr,
+                  int* indices, int* work, void* stream);
+/* perm[old] = new (device, n) of reverse Cuthill-McKee on a sorted symmetric CSR graph (device),
+ * node degrees at most 64.  seed_order (host, n): numpy.argsort of the degrees, the component
+ * seeds' order.  work: 3 n + 1 ints (device). */
+int fv_rcm_permutation(int n, const int* indptr, const int* indices, const long* seed_order,
+                       int* perm, int* work, void* stream);
+
+/* ------------------------------------------------------------------------------------------
+ * Flexible GMRES(m) on the device, fp64, bitwise reproducible (fixed blocking and summation order).
+ * Replaces the lineax GMRES behind solve_linear / relative_residual_gmres
+ * (aquaflux/solve/linear.py:138-298; the inexact forward solve of aquaflux/solve/implicit.py:50).
+ * The caller owns the bases: V (m + 1 rows of n) and Z (m rows of n), device, row-major.  A
+ * workspace holds the Hessenberg matrix, the Givens rotations, the rotated right-hand side g and
+ * the reduction partials; one workspace serves one stream at a time.
+ * ------------------------------------------------------------------------------------------ */
+typedef struct FvKrylov FvKrylov;
+int fv_krylov_create(int m, FvKrylov** out);
+int fv_krylov_destroy(FvKrylov* kr);
+/* Start a cycle from the residual r: beta = ||r||, V0 = r / beta, g = (beta, 0, ...).  est (may
+ * be NULL; device or pinned host) receives (beta, beta). */
+int fv_krylov_start(FvKrylov* kr, long n, const double* r, double* V0, double* est, void* stream);
+/* Arnoldi step j (0 <= j < m) on w = A M v_j: CGS2 against V[0..j], column j of H, Givens
+ * reduction, V[j + 1] = w / ||w|| (w is overwritten).  est (may be NULL; device or pinned host)
+ * receives (|g[j + 1]|, h[j + 1, j]): the residual estimate after j + 1 columns and the new
+ * basis norm (0 at a breakdown). */
+int fv_krylov_arnoldi(FvKrylov* kr, int j, long n, double* V, double* w, double* est,
+                      void* stream);
+/* End a cycle after k columns: y = H[0..k, 0..k)^-1 g[0..k), x += Z[0..k)^T y. */
+int fv_krylov_update(FvKrylov* kr, int k, long n, const double* Z, double* x, void* stream);
+/* out (device) = ||x||, deterministic. */
+int fv_krylov_norm(FvKrylov* kr, long n, const double* x, double* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -10,7 +10,7 @@ from aquaflux_gb300.amg import plan_hierarchy
 
 
 def _cell_graph(n_ax):
-    m = workloads.channel3d(n_ax).mesh
+    m = workloads.channel3d(n_ax, renumber="host").mesh
     o, nb = np.asarray(m.owner), np.asarray(m.neighbour)
     keep = nb >= 0
     n = m.n_cells
@@ -100,7 +100,7 @@ def test_aggregate_colouring_is_saturation_colouring_of_the_coarse_pattern():
 def test_cell_pattern_equals_the_reach_one_stencil():
     from aquaflux_gb300.colouring import cell_pattern, stencil_pattern
 
-    m = workloads.channel3d(10).mesh
+    m = workloads.channel3d(10, renumber="host").mesh
     o, nb = np.asarray(m.owner), np.asarray(m.neighbour)
     keep = nb >= 0
     ip, ix = cell_pattern(o[keep], nb[keep], m.n_cells)
