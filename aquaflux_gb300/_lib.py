@@ -48,6 +48,7 @@ SIGNATURES = {
     "fv_case_profile_begin": (c_int, [P, c_int]),
     "fv_case_profile_end": (c_int, [P, P, c_int, P]),
     "fv_residual": (c_int, [P, P, P, P]),
+    "fv_eddy_viscosity": (c_int, [P, P, P, P]),
     "fv_jvp": (c_int, [P, P, P, P, P, P]),
     "fv_jvp_shift": (c_int, [P, P, P, P, P, P]),
     "fv_jvp_frozen": (c_int, [P, P, P, P, P]),

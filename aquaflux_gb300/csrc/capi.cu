@@ -433,6 +433,15 @@ extern "C" int fv_residual(FvCase* c, const double* state, double* residual, voi
   return fv_case_run(c, physical_state(c, state, s), nullptr, FV_TAN_NONE, residual, nullptr, s);
 }
 
+extern "C" int fv_eddy_viscosity(FvCase* c, const double* state, double* nut, void* stream) {
+  if (!c || !state || !nut || !c->desc.turbulent) {
+    fv_set_error("fv_eddy_viscosity: bad arguments (turbulent cases only)");
+    return FV_ERR_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  return fv_case_eddy_viscosity(c, physical_state(c, state, s), nut, s);
+}
+
 extern "C" int fv_jvp(FvCase* c, const double* state, const double* v, double* residual,
                       double* jv, void* stream) {
   if (!c || !state || !v || !jv) {

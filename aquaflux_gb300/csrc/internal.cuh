@@ -168,6 +168,7 @@ void fv_prof_end_run(FvCase* c);
 // fp32 mirrors for the fp32 dual-number passes (made on first use)
 int fv_d2f(long n, const double* in, float* out, cudaStream_t s);
 int fv_mesh_ensure_f32(FvMesh* m, cudaStream_t s);
+int fv_case_eddy_viscosity(FvCase* cs, const double* state, double* nut, cudaStream_t s);
 int fv_case_ensure_f32(FvCase* c, cudaStream_t s);
 int fv_case_run(FvCase* c, const double* state, const double* tangent, int tangent_kind,
                 double* residual, double* jv, cudaStream_t s);

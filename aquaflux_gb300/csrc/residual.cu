@@ -1429,6 +1429,18 @@ int fv_case_ensure_f32(FvCase* c, cudaStream_t s) {
   return FV_OK;
 }
 
+// nu_t of a (physical) state: one residual evaluation, then the closure's eddy-viscosity row.
+int fv_case_eddy_viscosity(FvCase* cs, const double* state, double* nut, cudaStream_t s) {
+  const int dim = cs->mesh->dim;
+  const long nc = cs->mesh->nc, nf = cs->mesh->nf;
+  int rc = fv_case_run(cs, state, nullptr, FV_TAN_NONE, cs->tmp, nullptr, s);
+  if (rc != FV_OK) return rc;
+  const double* cl = dim == 2 ? work_layout<double, 2, true>(cs->work, nc, nf, psi_count<2, true>(cs)).cl
+                              : work_layout<double, 3, true>(cs->work, nc, nf, psi_count<3, true>(cs)).cl;
+  FV_CUDA_TRY(cudaMemcpyAsync(nut, cl + 2 * nc, sizeof(double) * nc, cudaMemcpyDeviceToDevice, s));
+  return FV_OK;
+}
+
 int fv_case_run(FvCase* cs, const double* state, const double* tangent, int kind, double* R,
                 double* JV, cudaStream_t s) {
   const int dim = cs->mesh->dim;

@@ -29,6 +29,7 @@ import torch
 from ._lib import check, lib, ptr
 from .colouring import block_stencil_colouring, cell_pattern, stencil_pattern
 from .ilu0 import Ilu0
+from .refresh import StepReport
 
 
 def _stream() -> int:
@@ -329,6 +330,7 @@ class NewtonResult:
     krylov_iterations: list
     seconds: float
     phase_seconds: dict
+    refreshes: int = 0  # preconditioner rebuilds (Jacobian materialisations)
 
 
 def newton_solve(case, state0, *, rtol: float = 1e-10, atol: float = 1e-12, max_steps: int = 50,
@@ -336,7 +338,8 @@ def newton_solve(case, state0, *, rtol: float = 1e-10, atol: float = 1e-12, max_
                  max_krylov: int = 300, precision: int = 32, reach: int = 1, frozen: bool = True,
                  refresh_every: int = 1, line_search_steps: int = 10,
                  preconditioner=None, kind: str = "ilu",
-                 precond_options: dict | None = None, tangents: int = 64) -> NewtonResult:
+                 precond_options: dict | None = None, tangents: int = 64,
+                 refresh_trigger=None, drift_measure=None) -> NewtonResult:
     """Newton's method with FGMRES, preconditioned by ILU(0) of the materialised Jacobian
     (``kind="ilu"``) or by an ILU(0)-smoothed aggregation V-cycle (``kind="amg"``), in fp32 or
     fp64 (``precision``).
@@ -346,7 +349,9 @@ def newton_solve(case, state0, *, rtol: float = 1e-10, atol: float = 1e-12, max_
     (``fv_assemble_jacobian_f32``).  The residual, the Newton update, the line search and the
     stopping test stay fp64, so the root is the fp64 root; only the linear solves, already
     inexact at ``linear_rtol``, see fp32 rounding.  The FGMRES bases are allocated once per
-    solve (:class:`KrylovWorkspace`)."""
+    solve (:class:`KrylovWorkspace`).  ``refresh_trigger`` replaces the fixed ``refresh_every``
+    schedule: the preconditioner is rebuilt at the first step and then only when the trigger fires
+    on the step history since the last rebuild (see :func:`pseudo_transient_solve`)."""
     if tangents not in (32, 64):
         raise ValueError(f"tangents must be 64 or 32, got {tangents}")
     t_all = time.perf_counter()
@@ -381,9 +386,14 @@ def newton_solve(case, state0, *, rtol: float = 1e-10, atol: float = 1e-12, max_
     its = []
     converged = norms[0] <= target
     step = 0
+    history, drift_fn, refreshes = [], None, 0
     while not converged and step < max_steps:
-        if step % refresh_every == 0:
+        if (refresh_trigger.should_refresh(history) or refreshes == 0
+                if refresh_trigger is not None else step % refresh_every == 0):
             timed("precond_setup", preconditioner.refresh, s)
+            refreshes += 1
+            history = []
+            drift_fn = drift_measure(s) if drift_measure is not None else None
         res = timed("krylov", lambda: fgmres(lambda v: case.jvp(s, v, precision=tangents), -r,
                                              preconditioner.apply,
                                              rtol=linear_rtol, restart=restart,
@@ -412,8 +422,11 @@ def newton_solve(case, state0, *, rtol: float = 1e-10, atol: float = 1e-12, max_
         converged = nrm <= target
         if not math.isfinite(nrm):
             break
+        history.append(StepReport(len(history), int(res.iterations), nrm, nrm / norms[0],
+                                  drift_fn(s) if drift_fn is not None else 0.0))
     torch.cuda.synchronize()
-    return NewtonResult(s, converged, step, norms, its, time.perf_counter() - t_all, phases)
+    return NewtonResult(s, converged, step, norms, its, time.perf_counter() - t_all, phases,
+                        refreshes)
 
 
 class TransposedPreconditioner:
@@ -526,6 +539,7 @@ class ContinuationResult:
     escalations: int
     krylov_iterations: list
     seconds: float
+    refreshes: int = 0  # Jacobian materialisations (the rest of the steps re-shifted only)
 
 
 def shift_basis(jac: BlockJacobian, velocity_only: bool = False,
@@ -618,6 +632,7 @@ def pseudo_transient_solve(case, state0, *, beta0: float = 2.0, exponent: float 
                            velocity_only: bool = False, measure: str = "euclidean",
                            scaled_tol: float | None = None, k_positive: bool = False,
                            k_floor: float = 0.0, backtrack: int = 0,
+                           refresh_trigger=None, drift_measure=None,
                            log=None) -> ContinuationResult:
     """Pseudo-transient continuation (``PseudoTransientStep``, ``aquaflux/solve/continuation.py:
     333-735``): each step solves ``(J + beta d) delta = -R`` (the true JVP plus the shift,
@@ -637,7 +652,14 @@ def pseudo_transient_solve(case, state0, *, beta0: float = 2.0, exponent: float 
     up to that many times (a backtracking line search along the shifted Newton direction, as
     ``backtracking_line_search`` does for the plain Newton step) before the shift escalates: on
     a saddle-point system a larger momentum shift leaves continuity to the pressure alone and can
-    lengthen the step rather than damp it.  ``log`` receives one dict per attempt."""
+    lengthen the step rather than damp it.  ``log`` receives one dict per attempt.
+
+    ``refresh_trigger`` (a :mod:`aquaflux_gb300.refresh` trigger): the Jacobian is materialised at
+    the first step and again only when the trigger fires on the segment's step history; the steps
+    in between re-form the preconditioner at their own shift from the frozen Jacobian (the
+    beta-only refresh, ``amg_preconditioner.py:909-948``).  Without one the Jacobian is
+    re-materialised at every step.  ``drift_measure``: ``reference_state -> (state -> drift)``
+    (e.g. :func:`aquaflux_gb300.refresh.eddy_viscosity_drift`), re-based at every refresh."""
     from .amg import AmgPreconditioner
 
     t_all = time.perf_counter()
@@ -665,9 +687,14 @@ def pseudo_transient_solve(case, state0, *, beta0: float = 2.0, exponent: float 
     step = 0
     converged = norms[0] <= target
     m0 = m_cur = None
+    history, drift_fn, refreshes = [], None, 0
     while not converged and step < max_steps:
-        pc.shift = zero
-        pc.refresh(s)  # materialise J at s (its diagonal also gives the shift basis)
+        if refresh_trigger is None or refreshes == 0 or refresh_trigger.should_refresh(history):
+            pc.shift = zero
+            pc.refresh(s)  # materialise J at s (its diagonal also gives the shift basis)
+            refreshes += 1
+            history = []
+            drift_fn = drift_measure(s) if drift_measure is not None else None
         if scaled:
             meas = RowScaledMeasure(case, jac, s)
             m_cur = meas(r)
@@ -721,6 +748,8 @@ def pseudo_transient_solve(case, state0, *, beta0: float = 2.0, exponent: float 
         betas.append(beta)
         step += 1
         converged = nc <= target
+        history.append(StepReport(len(history), int(res.iterations), nc, nc / r0,
+                                  drift_fn(s) if drift_fn is not None else 0.0))
     torch.cuda.synchronize()
     return ContinuationResult(s, converged, step, norms, betas, escalations, its,
-                              time.perf_counter() - t_all)
+                              time.perf_counter() - t_all, refreshes)

@@ -148,6 +148,10 @@ long fv_case_n_unknowns(const FvCase* c);
 /* R = residual(state).  MomentumContinuity.residual (aquaflux/flow/momentum.py:880) or
  * CoupledRANS.residual (aquaflux/turbulence/coupled.py:437).  Device in/out. */
 int fv_residual(FvCase* c, const double* state, double* residual, void* stream);
+/* nu_t (C, device) of a turbulent case at state: CoupledRANS.eddy_viscosity
+ * (aquaflux/turbulence/coupled.py), the coefficient the staleness measure eddy_viscosity_drift
+ * (coupled.py:681-717) watches. */
+int fv_eddy_viscosity(FvCase* c, const double* state, double* nut, void* stream);
 /* jv = J(state) v, the directional derivative jax.jvp(R, (state,), (v,)) of
  * aquaflux/solve/newton.py:110-111.  `residual` (may be NULL) receives R(state).  Device. */
 int fv_jvp(FvCase* c, const double* state, const double* v, double* residual, double* jv,

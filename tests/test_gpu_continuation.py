@@ -99,3 +99,51 @@ def test_row_scaled_march_with_backtracking_reaches_the_newton_root():
     assert ref.converged
     a, b = ptc.state.cpu().numpy(), ref.state.cpu().numpy()
     assert np.abs(a - b).max() <= 1e-7 * np.abs(b).max()
+
+
+@pytest.mark.parametrize("trigger", ["cycles", "drift"])
+def test_triggered_refresh_reaches_the_same_root(trigger):
+    """A march whose Jacobian is re-materialised only when a staleness trigger fires (the steps
+    between re-shift the frozen Jacobian) converges to the root of the every-step march; the
+    cycle-growth trigger on the Re = 1000 cavity, the eddy-viscosity drift trigger on an SST
+    channel."""
+    from aquaflux_gb300 import workloads
+    from aquaflux_gb300.refresh import (CoefficientDriftTrigger, CycleGrowthTrigger,
+                                        eddy_viscosity_drift)
+    from aquaflux_gb300.solve import pseudo_transient_solve
+
+    if trigger == "cycles":
+        wl = workloads.cavity(32, mu=1e-3)
+        case = wl.device_case()
+        s0 = np.zeros(case.n_unknowns)
+        kw = dict(refresh_trigger=CycleGrowthTrigger(warmup=2, patience=1,
+                                                     max_residual_ratio=1.0))
+    else:
+        wl = workloads.channel3d(6, nu=1e-2)
+        case = wl.device_case()
+        s0 = wl.initial_state()
+        kw = dict(refresh_trigger=CoefficientDriftTrigger(threshold=0.05, warmup=1),
+                  drift_measure=eddy_viscosity_drift(case))
+    every = pseudo_transient_solve(case, s0, kind="ilu", precision=64, max_steps=300)
+    lazy = pseudo_transient_solve(case, s0, kind="ilu", precision=64, max_steps=300, **kw)
+    assert every.converged and lazy.converged
+    assert every.refreshes == every.steps
+    assert 1 <= lazy.refreshes < lazy.steps
+    a, b = lazy.state.cpu().numpy(), every.state.cpu().numpy()
+    assert np.abs(a - b).max() <= 1e-7 * np.abs(b).max()
+
+
+def test_eddy_viscosity_drift_is_zero_at_its_reference():
+    from aquaflux_gb300 import workloads
+    from aquaflux_gb300.refresh import eddy_viscosity, eddy_viscosity_drift
+
+    wl = workloads.channel3d(6, nu=1e-2)
+    case = wl.device_case()
+    s0 = torch.tensor(wl.initial_state(), device="cuda")
+    nut = eddy_viscosity(case, s0)
+    assert nut.shape == (case.n_cells,) and bool((nut >= 0).all()) and float(nut.max()) > 0
+    drift = eddy_viscosity_drift(case)(s0)
+    assert drift(s0) == 0.0
+    s1 = s0.clone()
+    s1[4 * case.n_cells:5 * case.n_cells] *= 1.5  # k up by half: nu_t moves
+    assert drift(s1) > 0.05

@@ -192,15 +192,17 @@ def test_assembled_jacobian_overwrites_stale_values():
 @pytest.fixture(scope="module")
 def cavity64_solves():
     """Config 1: the 64 x 64 lid-driven cavity (Re = 100), solved from the zero state on the GPU
-    with the fp64 and the fp32-preconditioned forms (ILU(0) and AMG)."""
+    with the fp64 and the fp32-preconditioned forms (ILU(0) and AMG): to the reference's
+    tolerance (1e-10 relative), and on to the root (1e-13 relative)."""
     from aquaflux_gb300.solve import newton_solve
 
     m, case = _cavity(64)
     out = {}
     for kind, prec in (("ilu", 64), ("ilu", 32), ("amg", 32)):
-        res = newton_solve(case, np.zeros(case.n_unknowns), kind=kind, precision=prec,
-                           max_steps=40)
-        out[(kind, prec)] = res
+        for rtol in (1e-10, 1e-13):
+            out[(kind, prec, rtol)] = newton_solve(case, np.zeros(case.n_unknowns), kind=kind,
+                                                   precision=prec, rtol=rtol, atol=0.0,
+                                                   max_steps=60)
     return m, out
 
 
@@ -212,6 +214,8 @@ def test_config1_cavity_64_newton_meets_the_oracle_residual(cavity64_solves):
     orc = fo.Oracle(cd)
     r0 = float(np.linalg.norm(orc.residual(torch.zeros(3 * 64 * 64, dtype=torch.float64))))
     for key, res in out.items():
+        if key[2] != 1e-10:
+            continue
         assert res.converged, (key, res.residual_norms)
         r = orc.residual(torch.as_tensor(res.state.cpu().numpy())).numpy()
         assert np.linalg.norm(r) <= 1e-12 + 1e-10 * r0, key
@@ -219,18 +223,20 @@ def test_config1_cavity_64_newton_meets_the_oracle_residual(cavity64_solves):
 
 def test_config1_cavity_64_newton_matches_an_independent_root(cavity64_solves):
     """The converged fields against an independent FP64 root: the oracle's Newton with the exact
-    sparse Jacobian (reverse-mode products of the oracle) and sparse LU solves, refined from the
-    fp64 GPU solution until its residual stops falling; <= 1e-8 relative for every form."""
+    sparse Jacobian (reverse-mode products of the oracle) and sparse LU solves, from the zero
+    state to the oracle's round-off.  Every GPU form solved on to 1e-13 relative matches it to
+    1e-8; at the reference's 1e-10 the fields are within what that tolerance allows on this
+    operator (the pressure, pinned in one cell, moves most), 1e-6."""
     from oracle.newton_oracle import OracleJacobian, newton
 
     m, out = cavity64_solves
     cd = fo.make_case(m, mu=0.01, rho=1.0, flow_bc=CAVITY_BC, pressure_pin=0)
     orc = fo.Oracle(cd)
     jac = OracleJacobian(orc, m.owner, m.neighbour, 64 * 64, 3)
-    ref = newton(orc, jac, out[("ilu", 64)].state.cpu().numpy(), rtol=0.0, atol=0.0,
-                 max_steps=3, min_steps=1)
+    ref = newton(orc, jac, np.zeros(3 * 64 * 64), rtol=1e-15, atol=0.0, max_steps=12)
     root = ref["state"]
-    assert ref["residual_norms"][-1] <= 1e-13
+    assert ref["residual_norms"][-1] <= 1e-14 * ref["residual_norms"][0]
     for key, res in out.items():
         s = res.state.cpu().numpy()
-        assert np.abs(s - root).max() <= 1e-8 * np.abs(root).max(), key
+        bound = 1e-8 if key[2] == 1e-13 else 1e-6
+        assert np.abs(s - root).max() <= bound * np.abs(root).max(), key
