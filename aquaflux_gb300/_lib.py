@@ -44,6 +44,7 @@ SIGNATURES = {
     "fv_case_destroy": (c_int, [P]),
     "fv_case_set_params": (c_int, [P, c_double, c_double]),
     "fv_case_wall_distance": (c_int, [P, P, P, P]),
+    "fv_case_set_wall_distance": (c_int, [P, P, P]),
     "fv_case_n_unknowns": (c_long, [P]),
     "fv_case_profile_begin": (c_int, [P, c_int]),
     "fv_case_profile_end": (c_int, [P, P, c_int, P]),

@@ -62,7 +62,15 @@ def build_library(verbose: bool = False) -> str:
 
 
 def build_oracle() -> None:
-    """Compile the oracle's C restatement of the ILU(0) kernel -- test infrastructure."""
+    """Compile the test checkers: the oracle's C restatement of the ILU(0) kernel, and the
+    reference's own ILU(0) kernel from its source where this machine has it (``oracle/_ref``;
+    a failure there only leaves the checker unbuilt)."""
+    import sys
+
     script = os.path.join(ROOT, "oracle", "build_oracle.py")
     if os.path.exists(script):
-        subprocess.run(["python3", script], check=True, stdout=subprocess.DEVNULL)
+        subprocess.run([sys.executable, script], check=True, stdout=subprocess.DEVNULL)
+    ref = os.path.join(ROOT, "oracle", "build_ref.py")
+    if os.path.exists(ref):
+        subprocess.run([sys.executable, ref], check=False, stdout=subprocess.DEVNULL,
+                       stderr=subprocess.DEVNULL)

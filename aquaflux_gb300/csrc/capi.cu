@@ -215,13 +215,19 @@ extern "C" int fv_case_create(const FvMesh* mesh, const FvCaseDesc* desc,
   FV_CUDA_TRY(cudaMemsetAsync(c->inv_wd, 0, sizeof(double) * 2 * m->nc, s));
   if (desc->turbulent) {
     FV_CUDA_TRY(cudaMalloc(&c->wnear, sizeof(int) * m->nc));
-    rc = fv_wall_distance_compute(m, c->swall, n_wall, c->wd, c->wdg, desc->gradient_sweeps,
-                                  desc->gradient_relaxation, c->wnear, s);
-    if (rc != FV_OK) {
-      fv_case_destroy(c);
-      return rc;
+    if (n_wall > 0) {
+      rc = fv_wall_distance_compute(m, c->swall, n_wall, c->wd, c->wdg, desc->gradient_sweeps,
+                                    desc->gradient_relaxation, c->wnear, s);
+      if (rc != FV_OK) {
+        fv_case_destroy(c);
+        return rc;
+      }
+      k_inv_distance<<<fv_blocks(m->nc, 256), 256, 0, s>>>(m->nc, c->wd, c->inv_wd);
+    } else {
+      // no SST wall face on this mesh (a partition's local mesh away from the walls): the caller
+      // supplies the distance with fv_case_set_wall_distance before any evaluation
+      c->wd_missing = true;
     }
-    k_inv_distance<<<fv_blocks(m->nc, 256), 256, 0, s>>>(m->nc, c->wd, c->inv_wd);
   }
   // effective schemes: momentum (0 upwind, 1 linear, 2 limited) and k, omega likewise
   const int sadv = desc->scalar_advection == 0 ? desc->advection : desc->scalar_advection - 1;
@@ -389,6 +395,11 @@ extern "C" int fv_case_refresh_geometry(FvCase* c, void* stream) {
     return FV_ERR_ARG;
   }
   if (!c->desc.turbulent) return FV_OK;
+  if (c->wd_external) {
+    fv_set_error("fv_case_refresh_geometry: the wall distance was set by the caller "
+                 "(fv_case_set_wall_distance); set it again for the moved nodes");
+    return FV_ERR_ARG;
+  }
   cudaStream_t s = (cudaStream_t)stream;
   FvMesh* m = c->mesh;
   int rc = fv_wall_distance_refresh(m, c->swall, c->wnear, c->wd, c->wdg, c->desc.gradient_sweeps,
@@ -403,6 +414,31 @@ extern "C" int fv_case_refresh_geometry(FvCase* c, void* stream) {
     if ((rc = fv_d2f(dim * nc, c->wdg, p + nc, s)) != FV_OK) return rc;
     if ((rc = fv_d2f(2 * nc, c->inv_wd, p + (1 + dim) * nc, s)) != FV_OK) return rc;
   }
+  return FV_OK;
+}
+
+extern "C" int fv_case_set_wall_distance(FvCase* c, const double* distance, void* stream) {
+  if (!c || !distance || !c->desc.turbulent) {
+    fv_set_error("fv_case_set_wall_distance: bad arguments (turbulent cases only)");
+    return FV_ERR_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  FvMesh* m = c->mesh;
+  FV_CUDA_TRY(cudaMemcpyAsync(c->wd, distance, sizeof(double) * m->nc, cudaMemcpyDeviceToDevice, s));
+  int rc = fv_wall_distance_gradient(m, c->swall, c->wd, c->wdg, c->desc.gradient_sweeps,
+                                     c->desc.gradient_relaxation, s);
+  if (rc != FV_OK) return rc;
+  k_inv_distance<<<fv_blocks(m->nc, 256), 256, 0, s>>>(m->nc, c->wd, c->inv_wd);
+  FV_CUDA_TRY(cudaGetLastError());
+  if (c->f32) {
+    const long nc = m->nc, dim = m->dim;
+    float* p = c->f32;
+    if ((rc = fv_d2f(nc, c->wd, p, s)) != FV_OK) return rc;
+    if ((rc = fv_d2f(dim * nc, c->wdg, p + nc, s)) != FV_OK) return rc;
+    if ((rc = fv_d2f(2 * nc, c->inv_wd, p + (1 + dim) * nc, s)) != FV_OK) return rc;
+  }
+  c->wd_external = true;
+  c->wd_missing = false;
   return FV_OK;
 }
 

@@ -140,6 +140,8 @@ struct FvCase {
   const int* jac_indptr = nullptr;  // the block pattern last assembled into, and its block count
   long jac_nnzb = 0;
   int* wnear = nullptr;       // (nc) nearest SST wall face (internal index), turbulent cases
+  bool wd_external = false;   // wd set by fv_case_set_wall_distance (wnear no longer describes it)
+  bool wd_missing = false;    // turbulent, no SST wall face, distance not yet set: no evaluation
   NodeAdjoint* nadj = nullptr;  // mesh-coordinate adjoint workspace, allocated on first use
   int tb = 128;                 // threads per block of the residual / JVP / VJP stages (autotuned)
   double* mu_cell = nullptr;    // (nc) per-cell viscosity field (laminar batched instances)
@@ -195,6 +197,9 @@ enum { FV_TAN_NONE = 0, FV_TAN_STATE = 1, FV_TAN_MU = 2, FV_TAN_INLET = 3, FV_TA
 int fv_wall_distance_compute(FvMesh* m, const unsigned char* swall_dev, int n_wall_faces,
                              double* wd, double* wdg, int gradient_sweeps,
                              double gradient_relaxation, int* nearest_face, cudaStream_t s);
+// The Green-Gauss gradient of a given wall distance (the case's scheme).
+int fv_wall_distance_gradient(FvMesh* m, const unsigned char* swall_dev, const double* wd,
+                              double* wdg, int sweeps, double rel, cudaStream_t s);
 // The same distance to each cell's kept nearest wall face (after the nodes moved) and its gradient.
 int fv_wall_distance_refresh(FvMesh* m, const unsigned char* swall_dev, const int* nearest,
                              double* wd, double* wdg, int sweeps, double rel, cudaStream_t s);

@@ -354,6 +354,11 @@ int fv_wall_distance_compute(FvMesh* m, const unsigned char* swall_dev, int n_wa
   return rc;
 }
 
+int fv_wall_distance_gradient(FvMesh* m, const unsigned char* swall_dev, const double* wd,
+                              double* wdg, int sweeps, double rel, cudaStream_t s) {
+  return wall_distance_gradient(m, swall_dev, wd, wdg, sweeps, rel, s);
+}
+
 int fv_wall_distance_refresh(FvMesh* m, const unsigned char* swall_dev, const int* nearest,
                              double* wd, double* wdg, int sweeps, double rel, cudaStream_t s) {
   int bc = fv_blocks(m->nc, kThreads);

@@ -672,6 +672,11 @@ int node_vjp(FvCase* cs, const double* state, const double* W, double* dnodes, c
 
 int fv_case_node_vjp(FvCase* cs, const double* state, const double* w, double* dnodes,
                      cudaStream_t s) {
+  if (cs->wd_external) {
+    fv_set_error("fv_node_vjp: the wall distance was set by the caller (fv_case_set_wall_distance), "
+                 "so its dependence on the nodes is unknown here");
+    return FV_ERR_ARG;
+  }
   if (cs->desc.gradient_sweeps != 0 || cs->view.rec_mom || cs->view.rec_sca) {
     fv_set_error("fv_node_vjp: the mesh-coordinate adjoint supports the compact gradient scheme "
                  "and first-order upwind advection (gradient_sweeps = 0, advection = 0)");

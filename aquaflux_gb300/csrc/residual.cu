@@ -1443,6 +1443,11 @@ int fv_case_eddy_viscosity(FvCase* cs, const double* state, double* nut, cudaStr
 
 int fv_case_run(FvCase* cs, const double* state, const double* tangent, int kind, double* R,
                 double* JV, cudaStream_t s) {
+  if (cs->wd_missing) {
+    fv_set_error("turbulent case without SST wall faces: set its wall distance first "
+                 "(fv_case_set_wall_distance)");
+    return FV_ERR_ARG;
+  }
   const int dim = cs->mesh->dim;
   const bool turb = cs->desc.turbulent != 0;
   if (dim == 2) {

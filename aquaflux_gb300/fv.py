@@ -358,6 +358,13 @@ class FlowCase:
         self.dmesh.set_nodes(nodes)
         check(lib().fv_case_refresh_geometry(self._h, _stream()))
 
+    def set_wall_distance(self, distance) -> None:
+        """Replace the SST wall distance (per cell) and recompute its gradient."""
+        d = torch.as_tensor(distance, dtype=torch.float64, device="cuda").reshape(-1)
+        if d.numel() != self.n_cells:
+            raise ValueError(f"expected {self.n_cells} wall distances, got {d.numel()}")
+        check(lib().fv_case_set_wall_distance(self._h, ptr(d.contiguous()), _stream()))
+
     def wall_distance(self):
         C, D = self.n_cells, self.dim
         d = torch.empty(C, dtype=torch.float64, device="cuda")

@@ -280,11 +280,31 @@ def bsr_to_scalar_csr(blocks, indptr, indices):
 
 
 def cpu_ilu0(sptr, scols, sdata, rhs) -> dict:
-    """Factor + solve of the plain-C restatement of the reference's ILU(0) kernel (one core, the
-    reference kernel's operation order) on a scalar CSR operator; factor and solution returned."""
+    """Factor + solve of the reference's own ILU(0) kernel (``aquaflux/solve/_ilu0.pyx`` built from
+    its source into ``oracle/_ref`` by ``oracle/build_ref.py``; one core, the kernel is sequential)
+    on a scalar CSR operator; where that build is absent, the plain-C restatement of the same
+    kernel.  Factor, solution and which one ran are returned."""
     import ctypes
 
     import numpy as np
+
+    from oracle.build_ref import load_ref
+
+    mod = load_ref()
+    if mod is not None:
+        n = len(sptr) - 1
+        diag = np.asarray(mod.diagonal_positions(sptr, scols, n))
+        data = np.array(sdata, dtype=np.float64)
+        t0 = time.perf_counter()
+        mod.factor(sptr, scols, data, diag, n)
+        t1 = time.perf_counter()
+        x = np.array(rhs, dtype=np.float64)
+        t2 = time.perf_counter()
+        mod.solve(sptr, scols, data, diag, x, n)
+        t3 = time.perf_counter()
+        return {"factor_s": t1 - t0, "solve_s": t3 - t2, "factor": data, "x": x,
+                "kind": "reference", "what": "the reference's compiled ILU(0) kernel "
+                                             "(aquaflux/solve/_ilu0.pyx, built from its source)"}
 
     from oracle.build_oracle import build_c_oracle
 
@@ -309,7 +329,8 @@ def cpu_ilu0(sptr, scols, sdata, rhs) -> dict:
     t2 = time.perf_counter()
     L.ilu0_solve(p(sptr), p(scols), p(data), p(diag), p(x), n)
     t3 = time.perf_counter()
-    return {"factor_s": t1 - t0, "solve_s": t3 - t2, "factor": data, "x": x}
+    return {"factor_s": t1 - t0, "solve_s": t3 - t2, "factor": data, "x": x, "kind": "port",
+            "what": "plain-C restatement of the reference's ILU(0) kernel"}
 
 
 def ilu_cpu_vs_gpu(size: int) -> dict:
@@ -358,8 +379,7 @@ def ilu_cpu_vs_gpu(size: int) -> dict:
     return {"sample": f"{size}^3 channel, fp64 equilibrated cell-major Jacobian at the plug-flow "
                       f"state ({jac.n} cells, {jac.n * b} rows, {sdata.size} entries)",
             "cpu": {"factor_s": round(cpu["factor_s"], 4), "solve_s": round(cpu["solve_s"], 4),
-                    "cores": 1, "kind": "port",
-                    "what": "plain-C restatement of the reference's ILU(0) kernel"},
+                    "cores": 1, "kind": cpu["kind"], "what": cpu["what"]},
             "gpu_fp64": {"factor_ms": round(factor_ms, 3), "solve_ms": round(solve_ms, 3)},
             "factor_speedup": round(cpu["factor_s"] * 1e3 / factor_ms, 1),
             "solve_speedup": round(cpu["solve_s"] * 1e3 / solve_ms, 1),

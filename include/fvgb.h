@@ -140,6 +140,12 @@ int fv_case_autotune(FvCase* c, const double* state, const double* w, double* ou
  * WallDistance from the mesh inside the differentiated residual (aquaflux/mesh/distance.py:52-84,
  * aquaflux/turbulence/transport.py:86-111). */
 int fv_case_refresh_geometry(FvCase* c, void* stream);
+/* Replace a turbulent case's SST wall distance (device, C) and recompute its gradient: a case on
+ * a partition's local mesh takes the global distance, whose nearest wall face may lie outside
+ * it.  The mesh-coordinate adjoint and fv_case_refresh_geometry then refuse the case.  A
+ * turbulent case created on a mesh without SST wall faces evaluates nothing until this is
+ * called. */
+int fv_case_set_wall_distance(FvCase* c, const double* distance, void* stream);
 /* Device copies (C) and (C, dim) of the SST wall distance and its gradient (turbulent cases). */
 int fv_case_wall_distance(const FvCase* c, double* distance, double* gradient, void* stream);
 /* Number of unknowns: (dim + 1) * C, or (dim + 3) * C when turbulent. */

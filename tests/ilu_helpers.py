@@ -68,3 +68,56 @@ def to_bsr(indptr, indices, values, b):
     a = sp.csr_matrix((values, indices, indptr), shape=(n, n)).tobsr(blocksize=(b, b))
     a.sort_indices()
     return a.indptr.astype(np.int32), a.indices.astype(np.int32), a.data.reshape(-1).astype(np.float64)
+
+
+def reference_kernel():
+    """The reference's own compiled ILU(0) module (``oracle/build_ref.py``), or None where it is
+    not built (no reference checkout or generated C on this machine)."""
+    import sys
+
+    sys.path.insert(0, ROOT)
+    from oracle.build_ref import build_ref, load_ref
+
+    try:
+        build_ref()
+    except RuntimeError:
+        return None
+    return load_ref()
+
+
+def reference_factor_solve(mod, indptr, indices, values, rhs):
+    """(diag, factor, solve, solve_transpose) from the reference's compiled kernel."""
+    ip = np.ascontiguousarray(indptr, dtype=np.int32)
+    ix = np.ascontiguousarray(indices, dtype=np.int32)
+    n = len(ip) - 1
+    diag = np.asarray(mod.diagonal_positions(ip, ix, n))
+    data = np.array(values, dtype=np.float64)
+    mod.factor(ip, ix, data, diag, n)
+    x = np.array(rhs, dtype=np.float64)
+    mod.solve(ip, ix, data, diag, x, n)
+    xt = np.array(rhs, dtype=np.float64)
+    mod.solve_transpose(ip, ix, data, diag, xt, n)
+    return diag, data, x, xt
+
+
+def random_block_operator(n_cells, b, seed):
+    """A diagonally dominant cell-major operator on a 3D-grid-like block pattern (scalar CSR)."""
+    import scipy.sparse as sp
+
+    rng = np.random.default_rng(seed)
+    n = n_cells
+    side = max(2, round(n ** (1 / 3)))
+    rows, cols = [np.arange(n)], [np.arange(n)]
+    for off in (1, side, side * side):
+        i = np.arange(n - off)
+        rows += [i, i + off]
+        cols += [i + off, i]
+    r = np.concatenate(rows)
+    c = np.concatenate(cols)
+    blocks = rng.standard_normal((r.size, b, b))
+    blocks[r == c] += np.eye(b) * 4.0 * b
+    coo_r = (r[:, None, None] * b + np.arange(b)[None, :, None]).repeat(b, 2).reshape(-1)
+    coo_c = (c[:, None, None] * b + np.arange(b)[None, None, :]).repeat(b, 1).reshape(-1)
+    A = sp.csr_matrix((blocks.reshape(-1), (coo_r, coo_c)), shape=(n * b, n * b))
+    A.sort_indices()
+    return A.indptr.astype(np.int32), A.indices.astype(np.int32), A.data.astype(np.float64)

@@ -153,3 +153,32 @@ def test_block_solve_pivot_quotients_are_correctly_rounded(precision):
     f = Ilu0.from_csr(ip, ix, blocks.reshape(-1), block_size=b, precision=precision)
     got = f.solve(torch.tensor(r, device="cuda")).cpu().numpy()
     assert np.array_equal(got, r / d)
+
+
+def test_block_ilu0_fp64_bitwise_equals_the_reference_kernel_on_a_channel_jacobian():
+    """The GPU fp64 block ILU(0) of the equilibrated cell-major channel Jacobian against the
+    reference's own compiled kernel (``aquaflux/solve/_ilu0.pyx``, built from its source) on the
+    same scalar operator: factor and transposed solve bit for bit."""
+    import torch
+
+    from aquaflux_gb300 import workloads
+    from aquaflux_gb300.ilu0 import Ilu0
+    from aquaflux_gb300.solve import BlockJacobian, ShiftedCellMajorOperator
+    from tests.ilu_helpers import reference_factor_solve, reference_kernel
+
+    mod = reference_kernel()
+    if mod is None:
+        pytest.skip("the reference's compiled ILU(0) is not built on this machine")
+    wl = workloads.channel3d(10)
+    case = wl.device_case()
+    state = torch.tensor(wl.initial_state(noise=0.02), device="cuda")
+    jac = BlockJacobian(case)
+    vals, _ = ShiftedCellMajorOperator(jac, equilibrate=True).assemble(jac.materialize(state))
+    b = jac.b
+    f = Ilu0.from_csr(jac.indptr, jac.indices, vals.cpu().numpy(), block_size=b, precision=64)
+    sp_ip, sp_ix, sp_vals = to_scalar(jac.indptr, jac.indices, vals.cpu().numpy(), b)
+    rhs = np.random.default_rng(0).standard_normal(len(sp_ip) - 1)
+    _, data, _, xt = reference_factor_solve(mod, sp_ip, sp_ix, sp_vals, rhs)
+    _, _, gfac = to_scalar(jac.indptr, jac.indices, f.factor_values().cpu().numpy(), b)
+    np.testing.assert_array_equal(gfac, data)
+    np.testing.assert_array_equal(f.solve(rhs, transpose=True).cpu().numpy(), xt)
