@@ -5,13 +5,13 @@
 // residual estimate of the rotated least-squares problem as the stopping test.  Here one Arnoldi
 // step is four launches and never returns to the host:
 //   k_proj         h1 = V[0..k)^T w                                  (CGS, first pass)
-//   k_upd_proj     w -= V h1;  h2 = V[0..k)^T w                      (CGS, second pass)
+//   k_upd<true>    w -= V h1;  h2 = V[0..k)^T w                      (CGS, second pass)
 //   k_upd_norm     w -= V h2;  ||w||; the last block writes the Hessenberg column h1 + h2,
 //                  ||w||, applies the previous Givens rotations, forms the new one, and updates
 //                  the rotated right-hand side g (residual estimate |g[j+1]|)
 //   k_scale        V[j+1] = w / ||w||
 // Every reduction is a fixed grid of kRedBlocks blocks over a grid-stride loop, block partials
-// summed in block order by the last block to finish (a ticket counter), so results are bitwise
+// summed in a fixed order by the last block to finish (a ticket counter), so results are bitwise
 // identical run to run.  Up to kChunk basis vectors are handled per launch; a longer basis is
 // processed chunk by chunk with the update and the projection in separate passes.
 #include <algorithm>
@@ -21,33 +21,53 @@
 
 namespace {
 
-constexpr int kThreads = 256;
-constexpr int kRedBlocks = 304;  // 2 x 152 SMs; fixed so the summation order never changes
-constexpr int kChunk = 32;       // basis vectors per launch
+constexpr int kThreads = 256;          // 8 warps
+constexpr int kWarps = kThreads / 32;
+constexpr int kRedBlocks = 4 * 152;     // fixed, so the summation order never changes
+constexpr int kChunk = 32;              // basis vectors per launch
+constexpr int kSlots = kChunk / kWarps; // projections per warp
 
-// Sum the per-thread values a[0..k) over the block; thread 0 returns them in out[0..k).
-template <int KC>
-__device__ __forceinline__ void block_sum(const double (&a)[KC], int k, double* out) {
-  __shared__ double sh[kThreads / 32][KC];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+// The projection kernels walk tiles of kThreads entries (grid-stride over tiles): the tile of w
+// goes to shared memory, then warp u accumulates the dot products of the basis vectors
+// v = u, u + kWarps, ... with it, each lane over 8 coalesced entries of the tile.  Registers stay
+// few (kSlots accumulators), so occupancy is high; every partial sum runs in a fixed order.
+__device__ __forceinline__ void tile_project(long n, long base, int k, const double* __restrict__ V,
+                                             const double* ws, double (&acc)[kSlots]) {
+  const int lane = threadIdx.x & 31, u = threadIdx.x >> 5;
 #pragma unroll
-  for (int v = 0; v < KC; ++v) {
+  for (int t = 0; t < kSlots; ++t) {
+    const int v = u + t * kWarps;
     if (v >= k) break;
-    double x = a[v];
+    const double* row = V + (long)v * n + base;
+    double a = acc[t];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-    if (lane == 0) sh[warp][v] = x;
-  }
-  __syncthreads();
-  if (threadIdx.x < k) {
-    double s = 0.0;
-    for (int w = 0; w < kThreads / 32; ++w) s += sh[w][threadIdx.x];
-    out[threadIdx.x] = s;
+    for (int e = 0; e < kThreads / 32; ++e) {
+      const int i = lane + 32 * e;
+      if (base + i < n) a = fma(row[i], ws[i], a);
+    }
+    acc[t] = a;
   }
 }
 
-// After a block wrote its k partials part[blockIdx.x * k + v]: the last block to finish sums them
-// in block order into res[0..k) and returns true (in every thread of that block).
+// Write this block's partials: part[blockIdx.x * k + v] = the block's sum for vector v.
+__device__ __forceinline__ void write_partials(const double (&acc)[kSlots], int k, double* part) {
+  __shared__ double sh[kChunk];
+  const int lane = threadIdx.x & 31, u = threadIdx.x >> 5;
+#pragma unroll
+  for (int t = 0; t < kSlots; ++t) {
+    const int v = u + t * kWarps;
+    double x = acc[t];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0 && v < k) sh[v] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < k) part[(long)blockIdx.x * k + threadIdx.x] = sh[threadIdx.x];
+}
+
+// After every block wrote its k partials: the last block to finish sums them in a fixed order
+// (warp u sums vectors u, u + kWarps, ...: lane l over blocks l, l + 32, ..., then a fixed
+// shuffle tree) into res[0..k) and returns true (in every thread of that block).
 __device__ __forceinline__ bool last_block_sum(const double* part, int k, unsigned* ticket,
                                                double* res) {
   __shared__ bool last;
@@ -57,10 +77,14 @@ __device__ __forceinline__ bool last_block_sum(const double* part, int k, unsign
   __syncthreads();
   if (!last) return false;
   __threadfence();
-  if (threadIdx.x < k) {
+  const int lane = threadIdx.x & 31, u = threadIdx.x >> 5;
+  const volatile double* vp = part;
+  for (int v = u; v < k; v += kWarps) {
     double s = 0.0;
-    for (int b = 0; b < (int)gridDim.x; ++b) s += ((volatile const double*)part)[b * k + threadIdx.x];
-    res[threadIdx.x] = s;
+    for (int b = lane; b < (int)gridDim.x; b += 32) s += vp[(long)b * k + v];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) res[v] = s;
   }
   __syncthreads();
   if (threadIdx.x == 0) *ticket = 0u;  // ready for the next reduction on this workspace
@@ -71,53 +95,52 @@ __device__ __forceinline__ bool last_block_sum(const double* part, int k, unsign
 __global__ void __launch_bounds__(kThreads) k_proj(long n, int k, const double* __restrict__ V,
                                                    const double* __restrict__ w, double* part,
                                                    unsigned* ticket, double* h) {
-  double acc[kChunk];
+  __shared__ double ws[kThreads];
+  double acc[kSlots];
 #pragma unroll
-  for (int v = 0; v < kChunk; ++v) acc[v] = 0.0;
-  const long stride = (long)gridDim.x * blockDim.x;
-  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-    const double wi = w[i];
-#pragma unroll
-    for (int v = 0; v < kChunk; ++v)
-      if (v < k) acc[v] = fma(V[(long)v * n + i], wi, acc[v]);
+  for (int t = 0; t < kSlots; ++t) acc[t] = 0.0;
+  for (long base = (long)blockIdx.x * kThreads; base < n; base += (long)gridDim.x * kThreads) {
+    const long i = base + threadIdx.x;
+    __syncthreads();
+    ws[threadIdx.x] = i < n ? w[i] : 0.0;
+    __syncthreads();
+    tile_project(n, base, k, V, ws, acc);
   }
-  __shared__ double bs[kChunk];
-  block_sum<kChunk>(acc, k, bs);
-  __syncthreads();
-  if (threadIdx.x < k) part[blockIdx.x * k + threadIdx.x] = bs[threadIdx.x];
+  write_partials(acc, k, part);
   last_block_sum(part, k, ticket, h);
 }
 
-// w -= V[0..k)^T-combination with coefficients c; then (proj) h = V[0..k)^T w of the new w.
+// w -= V[0..k)^T-combination with coefficients c; then (PROJ) h = V[0..k)^T w of the new w, the
+// tile's basis entries read a second time from cache.
 template <bool PROJ>
 __global__ void __launch_bounds__(kThreads) k_upd(long n, int k, const double* __restrict__ V,
                                                   const double* __restrict__ c,
                                                   double* __restrict__ w, double* part,
                                                   unsigned* ticket, double* h) {
   __shared__ double cs[kChunk];
+  __shared__ double ws[kThreads];
   if (threadIdx.x < k) cs[threadIdx.x] = c[threadIdx.x];
-  __syncthreads();
-  double acc[kChunk];
+  double acc[kSlots];
 #pragma unroll
-  for (int v = 0; v < kChunk; ++v) acc[v] = 0.0;
-  const long stride = (long)gridDim.x * blockDim.x;
-  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-    double wi = w[i];
-#pragma unroll
-    for (int v = 0; v < kChunk; ++v)
-      if (v < k) wi = fma(-cs[v], V[(long)v * n + i], wi);
-    w[i] = wi;
-    if (PROJ) {  // the same basis entries again (now in L1), against the updated w
-#pragma unroll
-      for (int v = 0; v < kChunk; ++v)
-        if (v < k) acc[v] = fma(V[(long)v * n + i], wi, acc[v]);
+  for (int t = 0; t < kSlots; ++t) acc[t] = 0.0;
+  for (long base = (long)blockIdx.x * kThreads; base < n; base += (long)gridDim.x * kThreads) {
+    const long i = base + threadIdx.x;
+    __syncthreads();
+    double wi = 0.0;
+    if (i < n) {
+      wi = w[i];
+#pragma unroll 8
+      for (int v = 0; v < k; ++v) wi = fma(-cs[v], V[(long)v * n + i], wi);
+      w[i] = wi;
+    }
+    if (PROJ) {
+      ws[threadIdx.x] = wi;
+      __syncthreads();
+      tile_project(n, base, k, V, ws, acc);
     }
   }
   if (!PROJ) return;
-  __shared__ double bs[kChunk];
-  block_sum<kChunk>(acc, k, bs);
-  __syncthreads();
-  if (threadIdx.x < k) part[blockIdx.x * k + threadIdx.x] = bs[threadIdx.x];
+  write_partials(acc, k, part);
   last_block_sum(part, k, ticket, h);
 }
 
@@ -175,20 +198,26 @@ __global__ void __launch_bounds__(kThreads) k_upd_norm(long n, int k, const doub
   __shared__ double cs[kChunk];
   if (threadIdx.x < k) cs[threadIdx.x] = c[threadIdx.x];
   __syncthreads();
-  double acc[1] = {0.0};
+  double acc = 0.0;
   const long stride = (long)gridDim.x * blockDim.x;
   for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
     double wi = w[i];
-#pragma unroll
-    for (int v = 0; v < kChunk; ++v)
-      if (v < k) wi = fma(-cs[v], V[(long)v * n + i], wi);
+#pragma unroll 8
+    for (int v = 0; v < k; ++v) wi = fma(-cs[v], V[(long)v * n + i], wi);
     if (k > 0) w[i] = wi;
-    acc[0] = fma(wi, wi, acc[0]);
+    acc = fma(wi, wi, acc);
   }
-  __shared__ double bs[1];
-  block_sum<1>(acc, 1, bs);
+  // block sum in a fixed order: warp shuffles, then the warp totals by thread 0
+  __shared__ double sh[kWarps];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
   __syncthreads();
-  if (threadIdx.x == 0) part[blockIdx.x] = bs[0];
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int u = 0; u < kWarps; ++u) t += sh[u];
+    part[blockIdx.x] = t;
+  }
   if (last_block_sum(part, 1, ticket, red) && threadIdx.x == 0) {
     const double nrm = sqrt(red[0]);
     if (mode == NM_COLUMN) {
@@ -230,9 +259,8 @@ __global__ void k_combine(long n, int k, const double* __restrict__ Z, const dou
   __syncthreads();
   for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
     double xi = x[i];
-#pragma unroll
-    for (int v = 0; v < kChunk; ++v)
-      if (v < k) xi = fma(ys[v], Z[(long)v * n + i], xi);
+#pragma unroll 8
+    for (int v = 0; v < k; ++v) xi = fma(ys[v], Z[(long)v * n + i], xi);
     x[i] = xi;
   }
 }
