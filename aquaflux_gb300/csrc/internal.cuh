@@ -109,6 +109,8 @@ struct NodeAdjoint {
   int* node_ent = nullptr;
   int* wall_ptr = nullptr;    // face -> cells whose nearest wall face it is
   int* wall_cell = nullptr;
+  double* sweep = nullptr;    // corrected gradients: forward iterates, their cotangents, scratch
+  double* rec = nullptr;      // limited reconstruction: centroid and limiter partials
 };
 
 struct FvCase {

@@ -16,7 +16,14 @@
 // (nearest wall-face centroid) and its Green-Gauss gradient, the cell volumes / centroids (face
 // areas, normals, centroids) and the face geometry (node coordinates; the owner-outward flip is a
 // constant sign).  Every scatter is a gather over a precomputed incidence list: deterministic.
-// Supports the compact gradient scheme.
+// Advection: first-order upwind and the limited linear upwind reconstruction (the centroids it
+// reads, and the Venkatakrishnan limiters' geometry by seeded dual evaluations, k_nadj_limiter).
+// Gradients: the compact scheme (with its relaxation) and the corrected scheme's swept solve
+// (aquaflux/schemes/gradient.py:618-705, 1122-1337): the forward iterates X_0 .. X_{S-2} are
+// recomputed, the sweeps reversed once more, and each sweep X' = X + rel (B - V X + C(X)) / V
+// contributes the cotangents of 1/V, V and of C(X) = sum_f +-S_f ((1 - g) skew . X_P +
+// g skew . X_N) (S_f, g, skew) at its own input; the numerator B takes rel X0_bar / V plus the
+// sweeps' share (k_nadj_numerator_bar).  The SST wall-distance gradient is reversed the same way.
 
 
 namespace {
@@ -32,11 +39,15 @@ struct Contract {
   __device__ __forceinline__ void operator()(int q, const Dual& x) const { *acc += w[q] * x.d; }
 };
 
+// psi (dual, zero tangents; null without a limited reconstruction): the forward's slope limiters,
+// with them the centroid seeds too -- x_f into xfb, the owner's and neighbour's x_c into recxc
+// ((2, DIM, nf), gathered per cell by k_nadj_centroid_gather).
 template <int DIM, bool TURB>
 __global__ void __launch_bounds__(128) k_nadj_flux(MeshView m, CaseView cv, const double* state,
                                                    Par<Dual> par, const Dual* G, const Dual* cl,
                                                    const Dual* dco, const double* Wt,
-                                                   const double* FLx, double* Fb, double* wdf) {
+                                                   const double* FLx, const Dual* psi, double* Fb,
+                                                   double* wdf, double* xfb, double* recxc) {
   constexpr int NF = Layout<DIM, TURB>::NFLD;
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= m.nf) return;
@@ -49,20 +60,77 @@ __global__ void __launch_bounds__(128) k_nadj_flux(MeshView m, CaseView cv, cons
     FLb[q] = Wt[(long)q * nc + o] - (interior ? Wt[(long)q * nc + m.nb[f]] : 0.0) +
              (FLx ? FLx[(long)q * nf + f] : 0.0);
   const Src<Dual> st{state, nullptr};
-#pragma unroll 1
-  for (int comp = 0; comp < GF_COUNT; ++comp) {
+  auto contract = [&](const GeoSeed& gs) {
     double acc = 0.0;
-    flux_face<Dual, DIM, TURB>(m, cv, st, par, G, cl, dco, (const Dual*)nullptr,
-                               (const Dual*)nullptr, true, f, Contract{FLb, &acc}, nullptr,
-                               GeoSeed{comp, -1, f, -1});
-    Fb[(long)comp * nf + f] += acc;
+    flux_face<Dual, DIM, TURB>(m, cv, st, par, G, cl, dco, (const Dual*)nullptr, psi, true, f,
+                               Contract{FLb, &acc}, nullptr, gs);
+    return acc;
+  };
+#pragma unroll 1
+  for (int comp = 0; comp < GF_COUNT; ++comp) Fb[(long)comp * nf + f] += contract(GeoSeed{comp, -1, f, -1});
+  wdf[f] = (TURB && !interior) ? contract(GeoSeed{-1, GC_WD, -1, o}) : 0.0;
+  if (psi) {
+#pragma unroll 1
+    for (int j = 0; j < DIM; ++j) {
+      xfb[(long)j * nf + f] += contract(GeoSeed{GF_XF + j, -1, f, -1});
+      recxc[(long)j * nf + f] = contract(GeoSeed{-1, GC_XC + j, -1, o});
+      recxc[(long)(DIM + j) * nf + f] = interior ? contract(GeoSeed{-1, GC_XC + j, -1, m.nb[f]}) : 0.0;
+    }
   }
-  double acc = 0.0;
-  if (TURB && !interior)
-    flux_face<Dual, DIM, TURB>(m, cv, st, par, G, cl, dco, (const Dual*)nullptr,
-                               (const Dual*)nullptr, true, f, Contract{FLb, &acc}, nullptr,
-                               GeoSeed{-1, GC_WD, -1, o});
-  wdf[f] = acc;
+}
+
+// The Venkatakrishnan limiters' geometry (limiter_cell reads x_f, x_c and V): per cell and
+// advected field with a limiter, d psi / d(geometry) by seeded dual evaluations contracted with
+// psi_bar -- into Vb, limxc (DIM, nc) and limxf (DIM, ncf: per cell-face entry).
+template <int DIM, bool TURB>
+__global__ void __launch_bounds__(128) k_nadj_limiter(MeshView m, const double* state,
+                                                      const double* G, double Km, double Ks,
+                                                      const double* psib, double* Vb,
+                                                      double* limxc, double* limxf, long ncf) {
+  constexpr int NA = DIM + (TURB ? 2 : 0);
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nc) return;
+  const int nc = m.nc;
+  const int b = m.cf_ptr[c], e = m.cf_ptr[c + 1];
+#pragma unroll 1
+  for (int a = 0; a < NA; ++a) {
+    const double K = a < DIM ? Km : Ks;
+    const double pb = psib[(long)a * nc + c];
+    if (!(K > 0.0) || pb == 0.0) continue;
+    const int q = advected_field<DIM, TURB>(a);
+    auto eval = [&](const GeoSeed& gs) {
+      auto phi = [&](int cell) { return Dual{state[(long)q * nc + cell], 0.0}; };
+      auto grad = [&](int j) { return Dual{G[((long)q * DIM + j) * nc + c], 0.0}; };
+      return limiter_cell<Dual, DIM>(m, c, K, phi, grad, gs).d;
+    };
+    Vb[c] += pb * eval(GeoSeed{-1, GC_VOL, -1, c});
+#pragma unroll 1
+    for (int j = 0; j < DIM; ++j) limxc[(long)j * nc + c] += pb * eval(GeoSeed{-1, GC_XC + j, -1, c});
+#pragma unroll 1
+    for (int i = b; i < e; ++i) {
+      const int f = (int)(m.cf_face[i] & ~FV_NB_BIT);
+      for (int j = 0; j < DIM; ++j) limxf[(long)j * ncf + i] += pb * eval(GeoSeed{GF_XF + j, -1, f, -1});
+    }
+  }
+}
+
+// Cell-centroid cotangents of the reconstruction (recxc, per face and side) and of the limiters
+// (limxc), added to xcb.
+template <int DIM>
+__global__ void k_nadj_centroid_gather(MeshView m, const double* recxc, const double* limxc,
+                                       double* xcb) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nc) return;
+  const int nc = m.nc, nf = m.nf;
+  for (int j = 0; j < DIM; ++j) {
+    double acc = limxc[(long)j * nc + c];
+    for (int i = m.cf_ptr[c]; i < m.cf_ptr[c + 1]; ++i) {
+      const unsigned ent = m.cf_face[i];
+      const int f = (int)(ent & ~FV_NB_BIT);
+      acc += recxc[((long)((ent & FV_NB_BIT) ? DIM : 0) + j) * nf + f];
+    }
+    xcb[(long)j * nc + c] += acc;
+  }
 }
 
 template <int DIM, bool TURB>
@@ -97,10 +165,11 @@ __global__ void __launch_bounds__(128) k_nadj_apcoef(MeshView m, CaseView cv, co
 
 // Green-Gauss: G_c = (1/V_c) sum_f +-S_f phi_f, S_f = n_f A_f, phi_f = lerp(phi_P, phi_N, g_f) or
 // the leading-order boundary value.
+// nbar: the cotangent of the Green-Gauss numerator B phi per cell, (NF, DIM, nc).
 template <int DIM, bool TURB>
 __global__ void __launch_bounds__(128) k_nadj_grad_face(MeshView m, CaseView cv,
                                                         const double* state, Par<double> par,
-                                                        const double* Gb, double* Fb) {
+                                                        const double* nbar, double* Fb) {
   using L = Layout<DIM, TURB>;
   constexpr int NF = L::NFLD;
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
@@ -114,10 +183,9 @@ __global__ void __launch_bounds__(128) k_nadj_grad_face(MeshView m, CaseView cv,
     nrm[j] = m.normal[(long)j * nf + f];
     Sb[j] = 0.0;
   }
-  const double ivo = m.inv_vol[o];
   if (f < m.nfi) {
     const int n = m.nb[f];
-    const double g = m.g[f], ivn = m.inv_vol[n];
+    const double g = m.g[f];
     double gb = 0.0;
 #pragma unroll
     for (int q = 0; q < NF; ++q) {
@@ -126,7 +194,7 @@ __global__ void __launch_bounds__(128) k_nadj_grad_face(MeshView m, CaseView cv,
       double pbar = 0.0;
 #pragma unroll
       for (int j = 0; j < DIM; ++j) {
-        const double y = Gb[((long)q * DIM + j) * nc + o] * ivo - Gb[((long)q * DIM + j) * nc + n] * ivn;
+        const double y = nbar[((long)q * DIM + j) * nc + o] - nbar[((long)q * DIM + j) * nc + n];
         Sb[j] += pf * y;
         pbar += nrm[j] * A * y;
       }
@@ -144,7 +212,7 @@ __global__ void __launch_bounds__(128) k_nadj_grad_face(MeshView m, CaseView cv,
       else if (q == L::K) pb = bscalar(cv.kkind[f], cv.kval[f], po, 0.0);
       else pb = bscalar(cv.wkind[f], cv.wval[f], po, 0.0);
 #pragma unroll
-      for (int j = 0; j < DIM; ++j) Sb[j] += pb * Gb[((long)q * DIM + j) * nc + o] * ivo;
+      for (int j = 0; j < DIM; ++j) Sb[j] += pb * nbar[((long)q * DIM + j) * nc + o];
     }
   }
   double ab = 0.0;
@@ -156,18 +224,226 @@ __global__ void __launch_bounds__(128) k_nadj_grad_face(MeshView m, CaseView cv,
   Fb[(long)GF_AREA * nf + f] += ab;
 }
 
-// 1/V part of the gradients (numerator = G V) and d = V / a_P.
-template <int DIM, bool TURB>
-__global__ void k_nadj_grad_cell(MeshView m, const double* Gb, const double* G, const double* dco,
-                                 const double* dcob, double* ivb, double* Cb) {
-  constexpr int NF = Layout<DIM, TURB>::NFLD;
+// The numerator cotangent of NQ Green-Gauss fields: X0 = rel B / V (the gradient itself for the
+// compact scheme), so B_bar = rel X0_bar / V, plus the swept sweeps' share Bsw (may be null).
+template <int DIM, int NQ>
+__global__ void k_nadj_numerator_bar(MeshView m, const double* X0b, const double* Bsw, double rel,
+                                     double* nbar) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nc) return;
+  const int nc = m.nc;
+  const double r = rel * m.inv_vol[c];
+  for (int k = 0; k < NQ * DIM; ++k) {
+    const long i = (long)k * nc + c;
+    nbar[i] = X0b[i] * r + (Bsw ? Bsw[i] : 0.0);
+  }
+}
+
+// 1/V part of the first gradient iterate X0 = rel B / V: ivb += rel X0_bar . B, with B = X0 V / rel
+// for the compact scheme (Bnum null) or the stored numerator.
+template <int DIM, int NQ>
+__global__ void k_nadj_grad_cell(MeshView m, const double* X0b, const double* X0,
+                                 const double* Bnum, double rel, double* ivb) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= m.nc) return;
   const int nc = m.nc;
   double acc = 0.0;
-  for (int k = 0; k < NF * DIM; ++k) acc += Gb[(long)k * nc + c] * G[(long)k * nc + c];
-  ivb[c] += acc * m.vol[c];
-  Cb[(long)GC_VOL * nc + c] += dcob[c] * dco[c] / m.vol[c];
+  for (int k = 0; k < NQ * DIM; ++k) acc += X0b[(long)k * nc + c] * (Bnum ? Bnum[(long)k * nc + c] : X0[(long)k * nc + c]);
+  ivb[c] += Bnum ? rel * acc : acc * m.vol[c];
+}
+
+// d = V / a_P: the volume part.
+__global__ void k_nadj_dcoeff(MeshView m, const double* dco, const double* dcob, double* Cb) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nc) return;
+  Cb[(long)GC_VOL * m.nc + c] += dcob[c] * dco[c] / m.vol[c];
+}
+
+// X0 = rel B / V.
+template <int DIM, int NQ>
+__global__ void k_nadj_x0(MeshView m, const double* B, double rel, double* X0) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nc) return;
+  const int nc = m.nc;
+  const double iv = m.inv_vol[c];
+  for (int k = 0; k < NQ * DIM; ++k) X0[(long)k * nc + c] = rel * (B[(long)k * nc + c] * iv);
+}
+
+// One swept sweep X' = X + rel (B - (V X - C(X))) / V, its geometry cotangents at input X with
+// output cotangent Y.  Face part (interior faces): w_f = (1 - g) skew . X_P + g skew . X_N (kept
+// in wface for the cell part) and the cotangents of S_f, g, skew from C = sum +-S_f w_f.
+template <int DIM, int NQ>
+__global__ void __launch_bounds__(128) k_nadj_sweep_face(MeshView m, const double* X,
+                                                         const double* Y, double rel, double* Fb,
+                                                         double* wface) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= m.nfi) return;
+  const int nc = m.nc, nf = m.nf;
+  const int o = m.owner[f], n = m.nb[f];
+  const double A = m.area[f], g = m.g[f];
+  const double ro = rel * m.inv_vol[o], rn = rel * m.inv_vol[n];
+  double nrm[DIM], sk[DIM], Sb[DIM], skb[DIM];
+  for (int j = 0; j < DIM; ++j) {
+    nrm[j] = m.normal[(long)j * nf + f];
+    sk[j] = m.skew[(long)j * nf + f];
+    Sb[j] = 0.0;
+    skb[j] = 0.0;
+  }
+  double gb = 0.0;
+  for (int q = 0; q < NQ; ++q) {
+    double so = 0.0, sn = 0.0;
+    for (int j = 0; j < DIM; ++j) {
+      so += sk[j] * X[((long)q * DIM + j) * nc + o];
+      sn += sk[j] * X[((long)q * DIM + j) * nc + n];
+    }
+    const double w = (1.0 - g) * so + g * sn;
+    wface[(long)q * nf + f] = w;
+    double wb = 0.0;
+    for (int j = 0; j < DIM; ++j) {
+      const double D = Y[((long)q * DIM + j) * nc + o] * ro - Y[((long)q * DIM + j) * nc + n] * rn;
+      Sb[j] += D * w;
+      wb += D * nrm[j] * A;
+    }
+    gb += wb * (sn - so);
+    for (int j = 0; j < DIM; ++j)
+      skb[j] += wb * ((1.0 - g) * X[((long)q * DIM + j) * nc + o] + g * X[((long)q * DIM + j) * nc + n]);
+  }
+  double ab = 0.0;
+  for (int j = 0; j < DIM; ++j) {
+    ab += Sb[j] * nrm[j];
+    Fb[(long)(GF_NORMAL + j) * nf + f] += Sb[j] * A;
+    Fb[(long)(GF_SKEW + j) * nf + f] += skb[j];
+  }
+  Fb[(long)GF_AREA * nf + f] += ab;
+  Fb[(long)GF_G * nf + f] += gb;
+}
+
+// ... cell part: C(X) from wface, then the cotangents of 1/V (rel (B - V X + C) . Y) and of V
+// (-rel X . Y / V).
+template <int DIM, int NQ>
+__global__ void __launch_bounds__(128) k_nadj_sweep_cell(MeshView m, const double* X,
+                                                         const double* Y, const double* B,
+                                                         const double* wface, double rel,
+                                                         double* ivb, double* Vb) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nc) return;
+  const int nc = m.nc, nf = m.nf;
+  double corr[NQ][DIM];
+  for (int q = 0; q < NQ; ++q)
+    for (int j = 0; j < DIM; ++j) corr[q][j] = 0.0;
+  bool any = false;
+  for (int i = m.cf_ptr[c]; i < m.cf_ptr[c + 1]; ++i) {
+    const unsigned ent = m.cf_face[i];
+    const int f = (int)(ent & ~FV_NB_BIT);
+    if (f >= m.nfi) continue;
+    any = true;
+    const double A = (ent & FV_NB_BIT) ? -m.area[f] : m.area[f];
+    for (int q = 0; q < NQ; ++q)
+      for (int j = 0; j < DIM; ++j) corr[q][j] += (m.normal[(long)j * nf + f] * A) * wface[(long)q * nf + f];
+  }
+  const double V = m.vol[c];
+  double aiv = 0.0, av = 0.0;
+  for (int q = 0; q < NQ; ++q)
+    for (int j = 0; j < DIM; ++j) {
+      const long k = ((long)q * DIM + j) * nc + c;
+      const double x = X[k], y = Y[k];
+      const double ax = any ? x * V - corr[q][j] : x * V;
+      aiv += (B[k] - ax) * y;
+      av += x * y;
+    }
+  ivb[c] += rel * aiv;
+  Vb[c] += -rel * m.inv_vol[c] * av;
+}
+
+// Buffers of the swept reversal for NQ fields: S - 1 forward iterates, two cotangents, a
+// numerator-sweep accumulator, and the face values.
+struct SweepBufs {
+  double* X;     // (S - 1) iterates X_0 .. X_{S-2}, each (NQ, DIM, nc)
+  double* Y0;
+  double* Y1;
+  double* Bsw;   // sum over the sweeps of rel Y / V: the numerator's share
+  double* nbar;
+  double* wface; // (NQ, nf)
+};
+
+SweepBufs sweep_layout(double* p, int sweeps, int nq, int dim, long nc, long nf) {
+  const long blk = (long)nq * dim * nc;
+  SweepBufs b;
+  b.X = p; p += (long)std::max(sweeps - 1, 1) * blk;
+  b.Y0 = p; p += blk;
+  b.Y1 = p; p += blk;
+  b.Bsw = p; p += blk;
+  b.nbar = p; p += blk;
+  b.wface = p;
+  return b;
+}
+
+size_t sweep_doubles(int sweeps, int nq, int dim, long nc, long nf) {
+  return (size_t)(std::max(sweeps - 1, 1) + 4) * nq * dim * nc + (size_t)nq * nf;
+}
+
+// The corrected scheme's reversal for NQ fields with numerator B (stored) and the cotangent Gb of
+// the last iterate: contributions of every sweep to Fb / ivb / Vb; on return bf.nbar holds the
+// numerator's cotangent and ivb the first iterate's 1/V part.
+template <int DIM, int NQ>
+int sweeps_geometry(const MeshView& m, int sweeps, double rel, const double* B, const double* Gb,
+                    const SweepBufs& bf, double* Fb, double* ivb, double* Vb, cudaStream_t s) {
+  constexpr int TB = 128;
+  const long blk = (long)NQ * DIM * m.nc;
+  const int bc = fv_blocks(m.nc, TB), bfi = fv_blocks(m.nfi > 0 ? m.nfi : 1, TB);
+  // forward iterates X_0 .. X_{S-2}
+  k_nadj_x0<DIM, NQ><<<bc, TB, 0, s>>>(m, B, rel, bf.X);
+  for (int it = 1; it < sweeps - 1; ++it) {
+    if (m.nfi > 0) k_gg_skew<double, DIM, NQ><<<bfi, TB, 0, s>>>(m, bf.X + (it - 1) * blk, bf.wface);
+    k_gg_sweep<double, DIM, NQ><<<bc, TB, 0, s>>>(m, B, bf.X + (it - 1) * blk, bf.wface, rel,
+                                                   bf.X + it * blk);
+  }
+  // backward: sweep k maps X_{k-1} to X_k; Y holds X_k's cotangent
+  FV_CUDA_TRY(cudaMemcpyAsync(bf.Y0, Gb, sizeof(double) * blk, cudaMemcpyDeviceToDevice, s));
+  double* Y = bf.Y0;
+  double* Yn = bf.Y1;
+  MeshView mv = m;
+  for (int k = sweeps - 1; k >= 1; --k) {
+    const double* Xin = bf.X + (k - 1) * blk;
+    if (m.nfi > 0) k_nadj_sweep_face<DIM, NQ><<<bfi, TB, 0, s>>>(mv, Xin, Y, rel, Fb, bf.wface);
+    k_nadj_sweep_cell<DIM, NQ><<<bc, TB, 0, s>>>(mv, Xin, Y, B, bf.wface, rel, ivb, Vb);
+    if (m.nfi > 0) a_gg_skew<DIM, NQ><<<bfi, TB, 0, s>>>(mv, Y, rel, bf.wface);
+    a_gg_sweep<DIM, NQ><<<bc, TB, 0, s>>>(mv, Y, bf.wface, rel, k == sweeps - 1, bf.Bsw, Yn);
+    double* t = Y;
+    Y = Yn;
+    Yn = t;
+  }
+  // Y = X0_bar
+  k_nadj_numerator_bar<DIM, NQ><<<bc, TB, 0, s>>>(mv, Y, bf.Bsw, rel, bf.nbar);
+  k_nadj_grad_cell<DIM, NQ><<<bc, TB, 0, s>>>(mv, Y, bf.X, B, rel, ivb);
+  FV_CUDA_TRY(cudaGetLastError());
+  return FV_OK;
+}
+
+// The wall-distance gradient's numerator sum_f +-S_f d_f (d_f the interpolated distance, 0 on SST
+// walls, the owner's value on other boundaries), (DIM, nc).
+template <int DIM>
+__global__ void k_nadj_wd_numerator(MeshView m, CaseView cv, double* num) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nc) return;
+  const int nc = m.nc, nf = m.nf;
+  double acc[DIM];
+  for (int j = 0; j < DIM; ++j) acc[j] = 0.0;
+  const double phic = cv.wd[c];
+  for (int i = m.cf_ptr[c]; i < m.cf_ptr[c + 1]; ++i) {
+    const unsigned ent = m.cf_face[i];
+    const int f = (int)(ent & ~FV_NB_BIT);
+    double phif;
+    if (f < m.nfi) {
+      const double g = m.g[f];
+      phif = (1.0 - g) * cv.wd[m.owner[f]] + g * cv.wd[m.nb[f]];
+    } else {
+      phif = cv.swall[f] ? 0.0 : phic;
+    }
+    const double sgn = (ent & FV_NB_BIT) ? -phif : phif;
+    for (int j = 0; j < DIM; ++j) acc[j] += (m.normal[(long)j * nf + f] * m.area[f]) * sgn;
+  }
+  for (int j = 0; j < DIM; ++j) num[(long)j * nc + c] = acc[j];
 }
 
 template <int DIM>
@@ -219,30 +495,29 @@ __global__ void __launch_bounds__(128) k_nadj_src(MeshView m, CaseView cv, const
 
 // Wall-distance gradient (compact Green-Gauss of d: Dirichlet 0 on SST walls, the owner value on
 // other boundaries): face part.
+// nb: the cotangent of the gradient's numerator per cell, (DIM, nc).
 template <int DIM>
-__global__ void k_nadj_wdg_face(MeshView m, CaseView cv, const double* Cb, double* Fb,
+__global__ void k_nadj_wdg_face(MeshView m, CaseView cv, const double* nb, double* Fb,
                                 double* dpart) {
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= m.nf) return;
   const int nc = m.nc, nf = m.nf;
   const int o = m.owner[f];
   const double A = m.area[f];
-  const double* yb = Cb + (long)GC_WDG * nc;
   double nrm[DIM], Sb[DIM];
   for (int j = 0; j < DIM; ++j) {
     nrm[j] = m.normal[(long)j * nf + f];
     Sb[j] = 0.0;
   }
-  const double ivo = 1.0 / m.vol[o];
   double pbar = 0.0, d_o = 0.0, d_n = 0.0, po = 0.0, pn = 0.0;
   if (f < m.nfi) {
     const int n = m.nb[f];
-    const double g = m.g[f], ivn = 1.0 / m.vol[n];
+    const double g = m.g[f];
     d_o = cv.wd[o];
     d_n = cv.wd[n];
     const double df = (1.0 - g) * d_o + g * d_n;
     for (int j = 0; j < DIM; ++j) {
-      const double y = yb[(long)j * nc + o] * ivo - yb[(long)j * nc + n] * ivn;
+      const double y = nb[(long)j * nc + o] - nb[(long)j * nc + n];
       Sb[j] += df * y;
       pbar += nrm[j] * A * y;
     }
@@ -252,7 +527,7 @@ __global__ void k_nadj_wdg_face(MeshView m, CaseView cv, const double* Cb, doubl
   } else {
     const double df = cv.swall[f] ? 0.0 : cv.wd[o];
     for (int j = 0; j < DIM; ++j) {
-      const double y = yb[(long)j * nc + o] * ivo;
+      const double y = nb[(long)j * nc + o];
       Sb[j] += df * y;
       pbar += nrm[j] * A * y;
     }
@@ -268,10 +543,9 @@ __global__ void k_nadj_wdg_face(MeshView m, CaseView cv, const double* Cb, doubl
   dpart[(long)nf + f] = pn;
 }
 
-// ... cell part: d cotangent from the faces, and the 1/V of the wall-distance gradient.
+// ... cell part: the d cotangent from the faces (the 1/V part goes through ivb).
 template <int DIM>
-__global__ void k_nadj_wdg_cell(MeshView m, CaseView cv, const double* dpart, double* Cb,
-                                double* Vb) {
+__global__ void k_nadj_wdg_cell(MeshView m, CaseView cv, const double* dpart, double* Cb) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= m.nc) return;
   const int nc = m.nc, nf = m.nf;
@@ -283,10 +557,6 @@ __global__ void k_nadj_wdg_cell(MeshView m, CaseView cv, const double* dpart, do
     db += (ent & FV_NB_BIT) ? dpart[(long)nf + f] : dpart[f];
   }
   Cb[(long)GC_WD * nc + c] += db;
-  // wdg = num / V: d wdg / dV = -wdg / V
-  double acc = 0.0;
-  for (int j = 0; j < DIM; ++j) acc += Cb[(long)(GC_WDG + j) * nc + c] * cv.wdg[(long)j * nc + c];
-  Vb[c] += -acc / m.vol[c];
 }
 
 // Cell scalars: V_bar (with the 1/V cotangent) and the wall-distance cotangent; the nearest wall
@@ -439,8 +709,8 @@ __device__ __forceinline__ int cf_entry(const MeshView& m, int c, int f, bool nb
 // Totals of the face primitives' cotangents (residual stages + factors + cell geometry).
 template <int DIM>
 __global__ void k_nadj_cf_gather(MeshView m, const double* Fb, const double* cfA, const double* cfN,
-                                 const double* cfX, long ncf, double* Ab, double* nbt,
-                                 double* xfb) {
+                                 const double* cfX, const double* limxf, long ncf, double* Ab,
+                                 double* nbt, double* xfb) {
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= m.nf) return;
   const int nf = m.nf;
@@ -455,10 +725,12 @@ __global__ void k_nadj_cf_gather(MeshView m, const double* Fb, const double* cfA
     if (eo >= 0) {
       nb += cfN[(long)j * ncf + eo];
       xb += cfX[(long)j * ncf + eo];
+      if (limxf) xb += limxf[(long)j * ncf + eo];
     }
     if (en >= 0) {
       nb += cfN[(long)j * ncf + en];
       xb += cfX[(long)j * ncf + en];
+      if (limxf) xb += limxf[(long)j * ncf + en];
     }
     nbt[(long)j * nf + f] += nb;
     xfb[(long)j * nf + f] += xb;
@@ -596,6 +868,17 @@ int nadj_setup(FvCase* cs, cudaStream_t s) {
   cs->nadj = na;
   FV_CUDA_TRY(cudaMalloc(&na->dual_work, cs->work_bytes));
   FV_CUDA_TRY(cudaMalloc(&na->buf, sizeof(double) * nadj_doubles(dim, nc, nf, ncf, nfn)));
+  {
+    // gradient reversal: the saved last-iterate cotangent (nfld, dim, nc), the wall-distance
+    // numerator (dim, nc) and the sweep buffers of the flow fields
+    const int sweeps = std::max(cs->desc.gradient_sweeps, 1);
+    const size_t n = (size_t)cs->nfld * dim * nc + (size_t)dim * nc +
+                     sweep_doubles(sweeps, cs->nfld, dim, nc, nf);
+    FV_CUDA_TRY(cudaMalloc(&na->sweep, sizeof(double) * n));
+  }
+  if (cs->view.rec_mom || cs->view.rec_sca)  // recxc (2, dim, nf), limxc (dim, nc), limxf (dim, ncf)
+    FV_CUDA_TRY(cudaMalloc(&na->rec, sizeof(double) * ((size_t)2 * dim * nf + (size_t)dim * nc +
+                                                       (size_t)dim * ncf)));
   FV_CUDA_TRY(cudaMalloc(&na->node_ptr, sizeof(int) * np.size()));
   FV_CUDA_TRY(cudaMalloc(&na->node_ent, sizeof(int) * std::max<long>(nfn, 1)));
   FV_CUDA_TRY(cudaMalloc(&na->wall_ptr, sizeof(int) * wp.size()));
@@ -613,7 +896,14 @@ template <int DIM, bool TURB>
 int node_vjp(FvCase* cs, const double* state, const double* W, double* dnodes, cudaStream_t s) {
   using L = Layout<DIM, TURB>;
   constexpr int NF = L::NFLD;
-  int rc = run_vjp<DIM, TURB>(cs, state, W, nullptr, cs->tmp2, s);  // cotangents of every stage
+  NodeAdjoint* na0 = cs->nadj;
+  const int sweeps = cs->desc.gradient_sweeps;
+  const double rel = sweeps >= 1 ? cs->desc.gradient_relaxation : 1.0;
+  double* gb_last = na0->sweep;                                  // (NF, DIM, nc)
+  double* wd_num = gb_last + (long)NF * DIM * cs->mesh->nc;      // (DIM, nc)
+  double* sweep_area = wd_num + (long)DIM * cs->mesh->nc;
+  // cotangents of every stage (the gradient's saved before the backward sweeps overwrite it)
+  int rc = run_vjp<DIM, TURB>(cs, state, W, nullptr, cs->tmp2, s, sweeps >= 2 ? gb_last : nullptr);
   if (rc != FV_OK) return rc;
   FvMesh* M = cs->mesh;
   const MeshView& m = M->view;
@@ -634,6 +924,14 @@ int node_vjp(FvCase* cs, const double* state, const double* W, double* dnodes, c
   lift(fw.cl, dw.cl, 7 * nc);
   lift(fw.Gwi, dw.Gwi, (long)DIM * nc);
   lift(fw.dco, dw.dco, nc);
+  const long npsi = psi_count<DIM, TURB>(cs);
+  double* recxc = na->rec;
+  double* limxc = recxc ? recxc + 2L * DIM * nf : nullptr;
+  double* limxf = recxc ? limxc + (long)DIM * nc : nullptr;
+  if (npsi) {
+    lift(fw.psi, dw.psi, npsi);
+    FV_CUDA_TRY(cudaMemsetAsync(limxc, 0, sizeof(double) * ((size_t)DIM * nc + (size_t)DIM * ncf), s));
+  }
   FV_CUDA_TRY(cudaMemsetAsync(B.Fb, 0, sizeof(double) * ((size_t)GF_COUNT * nf + (size_t)GC_COUNT * nc + nc), s));
   FV_CUDA_TRY(cudaMemsetAsync(B.Vb, 0, sizeof(double) * nc, s));
   FV_CUDA_TRY(cudaMemsetAsync(B.xfb, 0, sizeof(double) * DIM * nf, s));
@@ -641,26 +939,53 @@ int node_vjp(FvCase* cs, const double* state, const double* W, double* dnodes, c
   const Par<Dual> pd{{cs->mu, 0.0}, {cs->inlet_scale, 0.0}, {cs->mu * irho, 0.0}};
   const Par<double> pdd{cs->mu, cs->inlet_scale, cs->mu * irho};
   k_nadj_flux<DIM, TURB><<<bf, TB, 0, s>>>(m, cv, state, pd, dw.G, dw.cl, dw.dco, aw.Wt, aw.FLx,
-                                           B.Fb, B.wdf);
+                                           npsi ? dw.psi : nullptr, B.Fb, B.wdf, B.xfb, recxc);
   if (aw.FLx && cs->flx_viscous)
     k_nadj_pressure_term<DIM, TURB><<<bf, TB, 0, s>>>(m, cv, state, aw.FLx, B.Fb);
   k_nadj_apcoef<DIM, TURB><<<bf, TB, 0, s>>>(m, cv, state, pd, dw.G, dw.cl, fw.dco, aw.dcob, B.Fb, B.wdf);
-  k_nadj_grad_face<DIM, TURB><<<bf, TB, 0, s>>>(m, cv, state, pdd, aw.Gb, B.Fb);
-  k_nadj_grad_cell<DIM, TURB><<<bc, TB, 0, s>>>(m, aw.Gb, fw.G, fw.dco, aw.dcob, B.ivb, B.Cb);
+  // Green-Gauss gradients of the fields: the swept sweeps' geometry, then the numerator's
+  {
+    SweepBufs sb = sweep_layout(sweep_area, std::max(sweeps, 1), NF, DIM, nc, nf);
+    if (sweeps >= 2) {
+      rc = sweeps_geometry<DIM, NF>(m, sweeps, rel, fw.Bg, gb_last, sb, B.Fb, B.ivb, B.Vb, s);
+      if (rc != FV_OK) return rc;
+    } else {
+      k_nadj_numerator_bar<DIM, NF><<<bc, TB, 0, s>>>(m, aw.Gb, nullptr, rel, sb.nbar);
+      k_nadj_grad_cell<DIM, NF><<<bc, TB, 0, s>>>(m, aw.Gb, fw.G, nullptr, rel, B.ivb);
+    }
+    k_nadj_grad_face<DIM, TURB><<<bf, TB, 0, s>>>(m, cv, state, pdd, sb.nbar, B.Fb);
+  }
+  k_nadj_dcoeff<<<bc, TB, 0, s>>>(m, fw.dco, aw.dcob, B.Cb);
   if constexpr (TURB) {
     k_nadj_closure<DIM><<<bc, TB, 0, s>>>(m, cv, state, pd, dw.G, aw.clb, aw.Gwib, B.Cb, B.Fb);
     k_nadj_src<DIM><<<bc, TB, 0, s>>>(m, cv, state, pd, dw.cl, dw.G, dw.Gwi, W, B.Cb);
-    k_nadj_wdg_face<DIM><<<bf, TB, 0, s>>>(m, cv, B.Cb, B.Fb, B.dpart);
-    k_nadj_wdg_cell<DIM><<<bc, TB, 0, s>>>(m, cv, B.dpart, B.Cb, B.Vb);
+    // the wall-distance gradient, the same scheme as the fields'
+    SweepBufs sd = sweep_layout(sweep_area, std::max(sweeps, 1), 1, DIM, nc, nf);
+    const double* yb = B.Cb + (long)GC_WDG * nc;
+    if (sweeps >= 2) {
+      k_nadj_wd_numerator<DIM><<<bc, TB, 0, s>>>(m, cv, wd_num);
+      rc = sweeps_geometry<DIM, 1>(m, sweeps, rel, wd_num, yb, sd, B.Fb, B.ivb, B.Vb, s);
+      if (rc != FV_OK) return rc;
+    } else {
+      k_nadj_numerator_bar<DIM, 1><<<bc, TB, 0, s>>>(m, yb, nullptr, rel, sd.nbar);
+      k_nadj_grad_cell<DIM, 1><<<bc, TB, 0, s>>>(m, yb, cv.wdg, nullptr, rel, B.ivb);
+    }
+    k_nadj_wdg_face<DIM><<<bf, TB, 0, s>>>(m, cv, sd.nbar, B.Fb, B.dpart);
+    k_nadj_wdg_cell<DIM><<<bc, TB, 0, s>>>(m, cv, B.dpart, B.Cb);
   }
+  if (npsi && (cv.lim_km > 0.0 || cv.lim_ks > 0.0))
+    k_nadj_limiter<DIM, TURB><<<bc, TB, 0, s>>>(m, state, fw.G, cv.lim_km, cv.lim_ks, aw.psib,
+                                                B.Vb, limxc, limxf, ncf);
   k_nadj_cell_chain<DIM, TURB><<<bc, TB, 0, s>>>(m, cv, B.Cb, B.ivb, B.wdf, cs->wnear, B.Vb, B.xcb,
                                                  B.wcon);
+  if (npsi) k_nadj_centroid_gather<DIM><<<bc, TB, 0, s>>>(m, recxc, limxc, B.xcb);
   if constexpr (TURB)
     k_nadj_wall_face<DIM><<<bf, TB, 0, s>>>(m, na->wall_ptr, na->wall_cell, B.wcon, B.xfb);
   k_nadj_factors<DIM><<<bf, TB, 0, s>>>(m, B.Fb, B.nbt, B.xfb, B.xcpart);
   k_nadj_xc_gather<DIM><<<bc, TB, 0, s>>>(m, B.xcpart, B.xcb);
   k_nadj_cell_geom<DIM><<<bc, TB, 0, s>>>(m, B.Vb, B.xcb, B.cfA, B.cfN, B.cfX, ncf);
-  k_nadj_cf_gather<DIM><<<bf, TB, 0, s>>>(m, B.Fb, B.cfA, B.cfN, B.cfX, ncf, B.Ab, B.nbt, B.xfb);
+  k_nadj_cf_gather<DIM><<<bf, TB, 0, s>>>(m, B.Fb, B.cfA, B.cfN, B.cfX, npsi ? limxf : nullptr, ncf,
+                                          B.Ab, B.nbt, B.xfb);
   k_nadj_face_geom<DIM><<<bf, TB, 0, s>>>(m, B.Ab, B.nbt, B.xfb, B.nodepart);
   k_nadj_nodes<<<fv_blocks(M->nn, 256), 256, 0, s>>>(M->nn, DIM, na->node_ptr, na->node_ent,
                                                     B.nodepart, dnodes);
@@ -675,11 +1000,6 @@ int fv_case_node_vjp(FvCase* cs, const double* state, const double* w, double* d
   if (cs->wd_external) {
     fv_set_error("fv_node_vjp: the wall distance was set by the caller (fv_case_set_wall_distance), "
                  "so its dependence on the nodes is unknown here");
-    return FV_ERR_ARG;
-  }
-  if (cs->desc.gradient_sweeps != 0 || cs->view.rec_mom || cs->view.rec_sca) {
-    fv_set_error("fv_node_vjp: the mesh-coordinate adjoint supports the compact gradient scheme "
-                 "and first-order upwind advection (gradient_sweeps = 0, advection = 0)");
     return FV_ERR_ARG;
   }
   int rc = nadj_setup(cs, s);
@@ -700,6 +1020,8 @@ void fv_node_adjoint_free(FvCase* cs) {
   cudaFree(na->node_ent);
   cudaFree(na->wall_ptr);
   cudaFree(na->wall_cell);
+  cudaFree(na->sweep);
+  cudaFree(na->rec);
   delete na;
   cs->nadj = nullptr;
 }

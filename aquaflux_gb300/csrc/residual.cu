@@ -190,6 +190,9 @@ enum GeoFace {
   GF_COUNT = 31
 };
 enum GeoCell { GC_VOL = 0, GC_WD = 1, GC_INV_WD = 2, GC_INV_WD2 = 3, GC_WDG = 4, GC_COUNT = 7 };
+// Centroid seeds (not stored per-factor cotangent rows): face centroid component j of the seeded
+// face (fcomp = GF_XF + j), cell centroid component j of the seeded cell (ccomp = GC_XC + j).
+enum GeoCentroid { GF_XF = 40, GC_XC = 50 };
 
 struct GeoPlain {
   __device__ __forceinline__ double area(const MeshView& m, int f) const { return m.area[f]; }
@@ -229,6 +232,12 @@ struct GeoPlain {
   }
   __device__ __forceinline__ double wdg(const CaseView& cv, int nc, int j, int c) const {
     return cv.wdg[(long)j * nc + c];
+  }
+  __device__ __forceinline__ double xf(const MeshView& m, int j, int f) const {
+    return m.xf[(long)j * m.nf + f];
+  }
+  __device__ __forceinline__ double xc(const MeshView& m, int j, int c) const {
+    return m.xc[(long)j * m.nc + c];
   }
 };
 
@@ -271,6 +280,12 @@ struct GeoPlainF {
   }
   __device__ __forceinline__ float wdg(const CaseView& cv, int nc, int j, int c) const {
     return cv.f_wdg[(long)j * nc + c];
+  }
+  __device__ __forceinline__ float xf(const MeshView& m, int j, int f) const {
+    return m.f_xf[(long)j * m.nf + f];
+  }
+  __device__ __forceinline__ float xc(const MeshView& m, int j, int c) const {
+    return m.f_xc[(long)j * m.nc + c];
   }
 };
 
@@ -346,6 +361,12 @@ struct GeoSeed {
   }
   __device__ __forceinline__ Dual wdg(const CaseView& cv, int nc, int j, int c) const {
     return {cv.wdg[(long)j * nc + c], hc(GC_WDG + j, c)};
+  }
+  __device__ __forceinline__ Dual xf(const MeshView& m, int j, int f) const {
+    return {m.xf[(long)j * m.nf + f], hf(GF_XF + j, f)};
+  }
+  __device__ __forceinline__ Dual xc(const MeshView& m, int j, int c) const {
+    return {m.xc[(long)j * m.nc + c], hc(GC_XC + j, c)};
   }
 };
 
@@ -719,9 +740,9 @@ __device__ __forceinline__ T conductance(T go, T gn, GT A, GT dpn, GT dnn) {
 // dm = grad . (x_f - x_c) (regularised away from 0) and the headroom to the extrema over the cell
 // and its face neighbours, eps^2 = V K^3.  phi(cell) and grad(j) read the field (either may carry
 // a tangent).
-template <class T, int DIM, class PhiFn, class GradFn>
+template <class T, int DIM, class PhiFn, class GradFn, class GV = typename GeoOf<T>::type>
 __device__ __forceinline__ T limiter_cell(const MeshView& m, int c, double K, const PhiFn& phi,
-                                          const GradFn& grad) {
+                                          const GradFn& grad, const GV& gv = GV{}) {
   const int nc = m.nc, nf = m.nf;
   const T pc = phi(c);
   T pmax = pc, pmin = pc;
@@ -734,15 +755,15 @@ __device__ __forceinline__ T limiter_cell(const MeshView& m, int c, double K, co
     pmax = fv_max(pmax, po);
     pmin = fv_min(pmin, po);
   }
-  const GS<T> e2 = gx<T>(m.vol, m.f_vol, c) * GS<T>(K * K * K);
+  using GT = decltype(gv.vol(m, 0));
+  using KT = typename std::conditional<std::is_same<GT, float>::value, float, double>::type;
+  const GT e2 = gv.vol(m, c) * KT(K * K * K);
   T psi = cst(1.0, pc);
   for (int i = b; i < e; ++i) {
     const int f = (int)(m.cf_face[i] & ~FV_NB_BIT);
-    T dm = grad(0) * (gx<T>(m.xf, m.f_xf, f) - gx<T>(m.xc, m.f_xc, c));
+    T dm = grad(0) * (gv.xf(m, 0, f) - gv.xc(m, 0, c));
 #pragma unroll
-    for (int j = 1; j < DIM; ++j)
-      dm = dm + grad(j) * (gx<T>(m.xf, m.f_xf, (long)j * nf + f) -
-                           gx<T>(m.xc, m.f_xc, (long)j * nc + c));
+    for (int j = 1; j < DIM; ++j) dm = dm + grad(j) * (gv.xf(m, j, f) - gv.xc(m, j, c));
     const double sign = val(dm) >= 0.0 ? 1.0 : -1.0;
     dm = sign * (fv_abs(dm) + 1e-12);
     const T head = val(dm) > 0.0 ? pmax - pc : pmin - pc;
@@ -786,16 +807,15 @@ __global__ void __launch_bounds__(128) k_limiter(MeshView m, Src<T> st, const T*
 
 // The advected face value of field q through face f from the upwind cell cu (upwind_value, the
 // cell value; with a limiter, plus psi grad . (x_f - x_cu)).
-template <class T, int DIM>
+template <class T, int DIM, class GV>
 __device__ __forceinline__ T upwind_rec(const MeshView& m, const T* G, const T* psi, int a, int q,
-                                        int f, int cu, const T& value) {
+                                        int f, int cu, const T& value, const GV& gv) {
   if (!psi) return value;
-  const int nc = m.nc, nf = m.nf;
-  T d = G[((long)q * DIM) * nc + cu] * (gx<T>(m.xf, m.f_xf, f) - gx<T>(m.xc, m.f_xc, cu));
+  const int nc = m.nc;
+  T d = G[((long)q * DIM) * nc + cu] * (gv.xf(m, 0, f) - gv.xc(m, 0, cu));
 #pragma unroll
   for (int j = 1; j < DIM; ++j)
-    d = d + G[((long)q * DIM + j) * nc + cu] *
-                (gx<T>(m.xf, m.f_xf, (long)j * nf + f) - gx<T>(m.xc, m.f_xc, (long)j * nc + cu));
+    d = d + G[((long)q * DIM + j) * nc + cu] * (gv.xf(m, j, f) - gv.xc(m, j, cu));
   return value + psi[(long)a * nc + cu] * d;
 }
 
@@ -942,8 +962,8 @@ __device__ __forceinline__ void flux_face(const MeshView& m, const CaseView& cv,
       for (int j = 0; j < DIM; ++j)
         cpn += G[((long)i * DIM + j) * nc + n] * tN[j] - G[((long)i * DIM + j) * nc + o] * tP[j];
       const T* pm = cv.rec_mom ? psi : nullptr;
-      const T up = out ? upwind_rec<T, DIM>(m, G, pm, i, i, f, o, uo)
-                       : upwind_rec<T, DIM>(m, G, pm, i, i, f, n, un);
+      const T up = out ? upwind_rec<T, DIM>(m, G, pm, i, i, f, o, uo, gv)
+                       : upwind_rec<T, DIM>(m, G, pm, i, i, f, n, un, gv);
       wr(i, (pA * nrm[i] - cmo * cpn) + mdot * up);
       if constexpr (KEEP) {
         if (aux) aux[(long)(AX::CPN + i) * nf + f] = cpn;
@@ -965,8 +985,8 @@ __device__ __forceinline__ void flux_face(const MeshView& m, const CaseView& cv,
         const T idn = 1.0 / (gv.dpn(m, f) * gn - go * gv.dnn(m, f));
         const T cs_ = go * gn * A * idn;
         const T* ps = cv.rec_sca ? psi : nullptr;
-        const T up = vout ? upwind_rec<T, DIM>(m, G, ps, DIM + s, q, f, o, phio)
-                          : upwind_rec<T, DIM>(m, G, ps, DIM + s, q, f, n, phin);
+        const T up = vout ? upwind_rec<T, DIM>(m, G, ps, DIM + s, q, f, o, phio, gv)
+                          : upwind_rec<T, DIM>(m, G, ps, DIM + s, q, f, n, phin, gv);
         wr(q, vflux * up - cs_ * cpn);
         if constexpr (KEEP) {
           if (aux) {
@@ -1022,7 +1042,7 @@ __device__ __forceinline__ void flux_face(const MeshView& m, const CaseView& cv,
       T cp = G[((long)i * DIM) * nc + o] * tP[0];
 #pragma unroll
       for (int j = 1; j < DIM; ++j) cp += G[((long)i * DIM + j) * nc + o] * tP[j];
-      const T up = out ? upwind_rec<T, DIM>(m, G, cv.rec_mom ? psi : nullptr, i, i, f, o, uo[i])
+      const T up = out ? upwind_rec<T, DIM>(m, G, cv.rec_mom ? psi : nullptr, i, i, f, o, uo[i], gv)
                        : bu[i];
       wr(i, (pA * nrm[i] - gA * (bu[i] - uo[i] - cp)) + mdot * up);
     }
@@ -1043,7 +1063,7 @@ __device__ __forceinline__ void flux_face(const MeshView& m, const CaseView& cv,
         T gface = go;
         if (s == 0 && cv.swall[f]) gface = (1.0 - wall_weight(par.nu, gv.wd(cv, o), phio)) * go;
         const T up = vout ? upwind_rec<T, DIM>(m, G, cv.rec_sca ? psi : nullptr, DIM + s, q, f, o,
-                                               phio)
+                                               phio, gv)
                           : bphi;
         wr(q, vflux * up - gface * (A * gv.inv_dpn(m, f)) * (bphi - phio - cp));
       }
@@ -1265,9 +1285,11 @@ AdjWork adj_layout(FvCase* cs) {
   return aw;
 }
 
+// gb_save (optional, (NF, DIM, nc)): receives the gradient cotangent before the corrected
+// scheme's backward sweeps overwrite it (the mesh-coordinate adjoint re-runs them).
 template <int DIM, bool TURB>
 int run_vjp(FvCase* cs, const double* state, const double* W, double* R, double* out,
-            cudaStream_t s) {
+            cudaStream_t s, double* gb_save = nullptr) {
   using L = Layout<DIM, TURB>;
   const MeshView& m = cs->mesh->view;
   const CaseView& cv = cs->view;
@@ -1309,6 +1331,9 @@ int run_vjp(FvCase* cs, const double* state, const double* W, double* R, double*
   const int sweeps = cs->desc.gradient_sweeps;
   const double rel = sweeps >= 1 ? cs->desc.gradient_relaxation : 1.0;
   const double* gb0 = aw.Gb;
+  if (gb_save)
+    FV_CUDA_TRY(cudaMemcpyAsync(gb_save, aw.Gb, sizeof(double) * L::NFLD * DIM * nc,
+                                cudaMemcpyDeviceToDevice, s));
   if (sweeps >= 2) gb0 = gg_sweeps_adjoint<DIM, L::NFLD>(m, sweeps, rel, aw, fw.FL, s);
   a_grad_face<DIM, TURB><<<fv_blocks(nf, TB), TB, 0, s>>>(m, cv, aw, gb0,
                                                          sweeps >= 2 ? aw.Bb : nullptr, rel,

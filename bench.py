@@ -528,6 +528,22 @@ def run_gpu(args, rank: int, world: int, local_rank: int) -> dict | None:
             tr = json.load(f).get(tkey, {})
         traffic = tr.get("bytes_128")
         fp64 = tr.get("fp64_pipe_active_pct")
+    clk = clk.summary()
+    # the FP64 pipe's roofline of the step: FP64-pipe instructions per face (ncu) x faces over the
+    # step's time, against 2 instructions per clock per SM at the sampled SM clock
+    fp64_roof = None
+    instr_path = os.path.join(ROOT, "profiles", "fp64_instructions.json")
+    if os.path.exists(instr_path) and args.step == "vjp":
+        with open(instr_path) as f:
+            ins = json.load(f)
+        mhz = clk.get("sm_mhz") or 2070.0
+        peak_gi = ins["pipe_instr_per_clock_per_sm"] * ins["sms"] * mhz * 1e6 / 1e9
+        ach_gi = ins["vjp_step_instr_per_face"] * F / (ms / args.steps * 1e-3) / 1e9
+        fp64_roof = {"instr_per_face": ins["vjp_step_instr_per_face"],
+                     "achieved_ginstr_s": round(ach_gi, 1), "peak_ginstr_s": round(peak_gi, 1),
+                     "frac": round(ach_gi / peak_gi, 4),
+                     "bound_gfaces_s": round(peak_gi / ins["vjp_step_instr_per_face"], 4),
+                     "source": "profiles/fp64_residual_vjp_channel3d_64.md (ncu, 64^3)"}
     out = {
         "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4),
@@ -559,8 +575,9 @@ def run_gpu(args, rank: int, world: int, local_rank: int) -> dict | None:
                      "step_frac": round(step_gbs / peaks["hbm_gbs"], 4),
                      "peak_source": f"{peaks['source']} (MEASURED_PEAKS.json hbm_gbs)",
                      "fp64_pipe_active_pct_ncu": fp64,
-                     "binding_limit": "fp64 pipe (see profiles/flux_kernels_channel3d_64.md)"},
-        "clocks": clk.summary(),
+                     "binding_limit": "fp64 pipe (profiles/fp64_residual_vjp_channel3d_64.md)",
+                     "fp64_pipe": fp64_roof},
+        "clocks": clk,
     }
     if not args.no_newton:
         out["newton"] = newton_block(args, wl, case)

@@ -1,6 +1,9 @@
 """The mesh-coordinate adjoint d/dnodes (w . R) against the oracle's autograd through the geometry
-(laminar 2D / 3D, k-omega SST 2D / 3D with the wall distance following the nodes) and against
-central differences of the GPU residual under moved nodes (laminar)."""
+(laminar 2D / 3D, k-omega SST 2D / 3D with the wall distance following the nodes, the corrected
+Green-Gauss scheme's swept solve for the fields and the wall-distance gradient, the limited and
+unlimited linear-upwind reconstruction with the Venkatakrishnan limiter, the backward-step
+validation configuration) and against central differences of the GPU residual under moved nodes
+(laminar: compact, corrected, limited)."""
 from __future__ import annotations
 
 import numpy as np
@@ -21,7 +24,9 @@ def _oracle_node_grad(case, d, p, s, w):
     return g.numpy()
 
 
-@pytest.mark.parametrize("name", ["cav8", "cavj", "lam3", "sst2", "sst3", "wsst2", "bsst3"])
+@pytest.mark.parametrize("name", ["cav8", "cavj", "lam3", "sst2", "sst3", "wsst2", "bsst3",
+                                  "ccavj", "csst2", "csst3", "lcavj", "ucavj", "lsst2", "psst2",
+                                  "msst2"])
 def test_node_vjp_matches_oracle_autograd(name):
     fc, case, d, p = device_case(name)
     s = d[p + "states"][0 if name != "cav8" else 1]
@@ -32,12 +37,14 @@ def test_node_vjp_matches_oracle_autograd(name):
     assert np.abs(got - ref).max() <= 1e-10 * scale, (name, np.abs(got - ref).max() / scale)
 
 
-def test_node_vjp_matches_central_differences():
-    """Laminar jittered cavity: (w . R(x + h v) - w . R(x - h v)) / 2h against dnodes . v, the
-    residual re-evaluated on the GPU after moving the nodes (geometry recomputed there)."""
+@pytest.mark.parametrize("name", ["cavj", "ccavj", "lcavj"])
+def test_node_vjp_matches_central_differences(name):
+    """Jittered cavity (compact; corrected, 4 sweeps; limited): (w . R(x + h v) - w . R(x - h v)) / 2h
+    against dnodes . v, the residual re-evaluated on the GPU after moving the nodes (geometry
+    recomputed there)."""
     from aquaflux_gb300._lib import check, lib, ptr
 
-    fc, case, d, p = device_case("cavj")
+    fc, case, d, p = device_case(name)
     s = d[p + "states"][0]
     rng = np.random.default_rng(4)
     w = rng.standard_normal(s.size)
@@ -57,9 +64,11 @@ def test_node_vjp_matches_central_differences():
     assert abs(fd - exact) <= 1e-6 * max(abs(exact), 1.0)
 
 
-def test_node_vjp_rejects_corrected_gradients():
+def test_node_vjp_refuses_a_caller_set_wall_distance():
     from aquaflux_gb300._lib import FvError
 
-    fc, case, d, p = device_case("ccavj")
+    fc, case, d, p = device_case("sst2")
+    dist, _ = fc.wall_distance()
+    fc.set_wall_distance(dist)
     with pytest.raises(FvError):
         fc.node_vjp(d[p + "states"][0], np.ones(fc.n_unknowns))
