@@ -62,12 +62,11 @@ __device__ __forceinline__ double rec_dot(const MeshView& m, const double* G, in
 
 // ---------------------------------------------------------------- a_sum
 template <int DIM, bool TURB>
-__global__ void __launch_bounds__(128) a_sum(MeshView m, CaseView cv, Src<double> st, Par<double> par,
+__device__ __forceinline__ void a_sum_at(const int c, MeshView m, CaseView cv, Src<double> st, Par<double> par,
                                              const double* W, const double* cl, const double* G,
                                              const double* Gwi, AdjWork aw) {
   using L = Layout<DIM, TURB>;
   constexpr int NF = L::NFLD;
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= m.nc) return;
   const int nc = m.nc;
   double wr[NF], sb[NF];
@@ -214,6 +213,13 @@ __global__ void __launch_bounds__(128) a_sum(MeshView m, CaseView cv, Src<double
   aw.dcob[c] = 0.0;
 }
 
+template <int DIM, bool TURB>
+__global__ void __launch_bounds__(128) a_sum(MeshView m, CaseView cv, Src<double> st, Par<double> par,
+                                             const double* W, const double* cl, const double* G,
+                                             const double* Gwi, AdjWork aw) {
+  a_sum_at<DIM, TURB>(blockIdx.x * blockDim.x + threadIdx.x, m, cv, st, par, W, cl, G, Gwi, aw);
+}
+
 // momentum-normal flux mn(f) = sum_j n_j ((rho u_j)_f + (rho grad u_j)_f . skew) -- its partial
 // derivatives are n_j w rho (u) and n_j w rho skew_q (grad u), w = 1 - g (owner) or g (neighbour).
 template <int DIM>
@@ -238,13 +244,12 @@ __device__ __forceinline__ void mn_adjoint(const MeshView& m, int f, double wgt,
 //   den = dpn m_n - m_o dnn  (m = mu + rho nu_t);  F_p = mdot;
 //   F_s = (mdot / rho) upwind(phi) - c_s (phi_n - phi_o + ...), c_s from the cell diffusivities.
 template <int DIM, bool TURB, bool FLX = false, bool LIM = false>
-__global__ void __launch_bounds__(128) a_flux(MeshView m, CaseView cv, Src<double> st, Par<double> par,
+__device__ __forceinline__ void a_flux_at(const int c, MeshView m, CaseView cv, Src<double> st, Par<double> par,
                                               const double* G, const double* cl, const double* dco,
                                               const double* me, const double* aux, AdjWork aw) {
   using AX = Aux<DIM, TURB>;
   using L = Layout<DIM, TURB>;
   constexpr int NF = L::NFLD;
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= m.nc) return;
   const int nc = m.nc, nf = m.nf;
   const double rho = cv.rho, irho = 1.0 / cv.rho;
@@ -556,6 +561,13 @@ __global__ void __launch_bounds__(128) a_flux(MeshView m, CaseView cv, Src<doubl
   }
 }
 
+template <int DIM, bool TURB, bool FLX = false, bool LIM = false>
+__global__ void __launch_bounds__(128) a_flux(MeshView m, CaseView cv, Src<double> st, Par<double> par,
+                                              const double* G, const double* cl, const double* dco,
+                                              const double* me, const double* aux, AdjWork aw) {
+  a_flux_at<DIM, TURB, FLX, LIM>(blockIdx.x * blockDim.x + threadIdx.x, m, cv, st, par, G, cl, dco, me, aux, aw);
+}
+
 // ---------------------------------------------------------------- a_limiter
 // Adjoint of the Venkatakrishnan limiters: psi of cell c depends on its own value and gradient and
 // on its face neighbours' values (the stencil extrema); d psi / d(input) by dual numbers seeded on
@@ -633,11 +645,10 @@ __global__ void a_limiter_gather(MeshView m, AdjWork aw) {
 // ---------------------------------------------------------------- a_apcoef
 // a_P(c) = sum of face coefficients; d = V / a_P  =>  abar = -dbar d^2 / V.
 template <int DIM, bool TURB>
-__global__ void __launch_bounds__(128) a_apcoef(MeshView m, CaseView cv, Src<double> st, Par<double> par,
+__device__ __forceinline__ void a_apcoef_at(const int c, MeshView m, CaseView cv, Src<double> st, Par<double> par,
                                                 const double* G, const double* cl, const double* dco,
                                                 const double* me, const double* aux, AdjWork aw) {
   using L = Layout<DIM, TURB>;
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= m.nc) return;
   const int nc = m.nc, nf = m.nf;
   const double rho = cv.rho;
@@ -704,12 +715,18 @@ __global__ void __launch_bounds__(128) a_apcoef(MeshView m, CaseView cv, Src<dou
   }
 }
 
+template <int DIM, bool TURB>
+__global__ void __launch_bounds__(128) a_apcoef(MeshView m, CaseView cv, Src<double> st, Par<double> par,
+                                                const double* G, const double* cl, const double* dco,
+                                                const double* me, const double* aux, AdjWork aw) {
+  a_apcoef_at<DIM, TURB>(blockIdx.x * blockDim.x + threadIdx.x, m, cv, st, par, G, cl, dco, me, aux, aw);
+}
+
 // ---------------------------------------------------------------- a_closure (SST)
 template <int DIM>
-__global__ void __launch_bounds__(128) a_closure(MeshView m, CaseView cv, Src<double> st, Par<double> par,
+__device__ __forceinline__ void a_closure_at(const int c, MeshView m, CaseView cv, Src<double> st, Par<double> par,
                                                  const double* G, const double* cl, AdjWork aw) {
   using L = Layout<DIM, true>;
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= m.nc) return;
   const int nc = m.nc, nf = m.nf;
   const double k = st((long)L::K * nc + c), w = st((long)L::W * nc + c);
@@ -877,6 +894,12 @@ __global__ void __launch_bounds__(128) a_closure(MeshView m, CaseView cv, Src<do
   aw.sb[(long)L::W * nc + c] += wb;
 }
 
+template <int DIM>
+__global__ void __launch_bounds__(128) a_closure(MeshView m, CaseView cv, Src<double> st, Par<double> par,
+                                                 const double* G, const double* cl, AdjWork aw) {
+  a_closure_at<DIM>(blockIdx.x * blockDim.x + threadIdx.x, m, cv, st, par, G, cl, aw);
+}
+
 // ---------------------------------------------------------------- a_grad
 // G_c = (1/V_c) sum_f (+-) S_f phi_f  =>  phib_f = S_f . (Gb_o / V_o - Gb_n / V_n), then each side
 // takes its interpolation weight of phib_f.  The face pass forms phib once per face (into `pb`,
@@ -969,12 +992,11 @@ const double* gg_sweeps_adjoint(const MeshView& m, int sweeps, double rel, const
 // cotangent of the Green-Gauss numerator B phi, nb = rel Gb0 / V (+ Bb when swept).  Gb0 is the
 // cotangent of the first gradient iterate (the gradient itself for the compact scheme).
 template <int DIM, bool TURB>
-__global__ void __launch_bounds__(128) a_grad_face(MeshView m, CaseView cv, AdjWork aw,
+__device__ __forceinline__ void a_grad_face_at(const int f, MeshView m, CaseView cv, AdjWork aw,
                                                    const double* Gb0, const double* Bb, double rel,
                                                    double* pb) {
   using L = Layout<DIM, TURB>;
   constexpr int NF = L::NFLD;
-  const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= m.nf) return;
   const int nc = m.nc, nf = m.nf;
   const int o = m.owner[f];
@@ -1032,11 +1054,17 @@ __global__ void __launch_bounds__(128) a_grad_face(MeshView m, CaseView cv, AdjW
 }
 
 template <int DIM, bool TURB>
-__global__ void __launch_bounds__(128) a_grad(MeshView m, CaseView cv, AdjWork aw, const double* pb,
+__global__ void __launch_bounds__(128) a_grad_face(MeshView m, CaseView cv, AdjWork aw,
+                                                   const double* Gb0, const double* Bb, double rel,
+                                                   double* pb) {
+  a_grad_face_at<DIM, TURB>(blockIdx.x * blockDim.x + threadIdx.x, m, cv, aw, Gb0, Bb, rel, pb);
+}
+
+template <int DIM, bool TURB>
+__device__ __forceinline__ void a_grad_at(const int c, MeshView m, CaseView cv, AdjWork aw, const double* pb,
                                               double* out) {
   using L = Layout<DIM, TURB>;
   constexpr int NF = L::NFLD;
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= m.nc) return;
   const int nc = m.nc, nf = m.nf;
   double acc[NF];
@@ -1068,4 +1096,10 @@ __global__ void __launch_bounds__(128) a_grad(MeshView m, CaseView cv, AdjWork a
   }
 #pragma unroll
   for (int q = 0; q < NF; ++q) out[(long)q * nc + c] = acc[q];
+}
+
+template <int DIM, bool TURB>
+__global__ void __launch_bounds__(128) a_grad(MeshView m, CaseView cv, AdjWork aw, const double* pb,
+                                              double* out) {
+  a_grad_at<DIM, TURB>(blockIdx.x * blockDim.x + threadIdx.x, m, cv, aw, pb, out);
 }

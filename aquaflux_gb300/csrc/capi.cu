@@ -380,6 +380,76 @@ extern "C" int fv_case_autotune(FvCase* c, const double* state, const double* w,
   return FV_OK;
 }
 
+extern "C" int fv_case_set_persistent(FvCase* c, int enable, int block, int chunk) {
+  if (!c || (enable && (block < 32 || block > 128 || block % 32 != 0 || chunk < 1 || chunk > 64))) {
+    fv_set_error("fv_case_set_persistent: block must be a multiple of 32 in [32, 128] and chunk "
+                 "in [1, 64]");
+    return FV_ERR_ARG;
+  }
+  c->persistent = enable ? 1 : 0;
+  if (enable) {
+    c->pblock = block;
+    c->pchunk = chunk;
+  }
+  return FV_OK;
+}
+
+extern "C" int fv_case_autotune_persistent(FvCase* c, const double* state, const double* w,
+                                           double* out, void* stream, int* best_block,
+                                           int* best_chunk, float* best_ms) {
+  if (!c || !state || !w || !out) {
+    fv_set_error("fv_case_autotune_persistent: bad arguments");
+    return FV_ERR_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  state = physical_state(c, state, s);
+  const int blocks[2] = {64, 128};
+  const int chunks[4] = {1, 2, 4, 8};
+  cudaEvent_t e0, e1;
+  FV_CUDA_TRY(cudaEventCreate(&e0));
+  FV_CUDA_TRY(cudaEventCreate(&e1));
+  float best = 1e30f;
+  int bb = 128, bc = 1;
+  const int was = c->persistent;
+  c->persistent = 1;
+  for (int i = 0; i < 2; ++i)
+    for (int k = 0; k < 4; ++k) {
+      c->pblock = blocks[i];
+      c->pchunk = chunks[k];
+      int rc = fv_case_vjp_run(c, state, w, nullptr, out, s);  // warm-up
+      if (rc != FV_OK) {
+        c->persistent = was;
+        return rc;
+      }
+      cudaEventRecord(e0, s);
+      for (int r = 0; r < 3; ++r) {
+        rc = fv_case_vjp_run(c, state, w, nullptr, out, s);
+        if (rc != FV_OK) {
+          c->persistent = was;
+          return rc;
+        }
+      }
+      cudaEventRecord(e1, s);
+      FV_CUDA_TRY(cudaEventSynchronize(e1));
+      float ms = 0.0f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (ms < best) {
+        best = ms;
+        bb = blocks[i];
+        bc = chunks[k];
+      }
+    }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  c->pblock = bb;
+  c->pchunk = bc;
+  c->persistent = was;
+  if (best_block) *best_block = bb;
+  if (best_chunk) *best_chunk = bc;
+  if (best_ms) *best_ms = best / 3.0f;
+  return FV_OK;
+}
+
 extern "C" int fv_case_set_block_size(FvCase* c, int threads) {
   if (!c || threads < 32 || threads > 128 || threads % 32 != 0) {
     fv_set_error("fv_case_set_block_size: threads must be a multiple of 32 in [32, 128]");

@@ -146,6 +146,9 @@ struct FvCase {
   bool wd_missing = false;    // turbulent, no SST wall face, distance not yet set: no evaluation
   NodeAdjoint* nadj = nullptr;  // mesh-coordinate adjoint workspace, allocated on first use
   int tb = 128;                 // threads per block of the residual / JVP / VJP stages (autotuned)
+  int persistent = 0;           // residual + VJP as one cooperative launch (compact, upwind cases)
+  int pchunk = 1;               // ... consecutive cells / faces per thread per stage
+  int pblock = 128;             // ... threads per block
   double* mu_cell = nullptr;    // (nc) per-cell viscosity field (laminar batched instances)
   double* flx = nullptr;        // (nfld, nf) weights of a face-flux functional (internal order)
   bool flx_active = false;      // the adjoints add flx to their face-flux cotangents

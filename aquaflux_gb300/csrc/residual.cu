@@ -21,6 +21,7 @@
 //               advection.py:99-187, turbulence/transport.py:581-718)
 //   k_sum       cell  conservative face-to-cell sums, pressure pin, SST sources and the omega
 //               wall-cell fixation (turbulence/sources.py:60-412, fixed_value.py:124-158)
+#include <cooperative_groups.h>
 #include <type_traits>
 
 #include "geom.cuh"
@@ -427,11 +428,10 @@ Work<T> work_layout(void* base, long nc, long nf, long npsi = 0) {
 // B phi itself (the right-hand side of the corrected scheme's sweeps).  rel = 1 and Bg = null is
 // the compact scheme.
 template <class T, int DIM, bool TURB>
-__global__ void __launch_bounds__(128) k_grad(MeshView m, CaseView cv, Src<T> st, Par<T> par, T* G,
+__device__ __forceinline__ void k_grad_at(const int c, MeshView m, CaseView cv, Src<T> st, Par<T> par, T* G,
                                               T* Bg, double rel) {
   using L = Layout<DIM, TURB>;
   constexpr int NF = L::NFLD;
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= m.nc) return;
   const int nc = m.nc, nf = m.nf;
   T phic[NF];
@@ -497,6 +497,12 @@ __global__ void __launch_bounds__(128) k_grad(MeshView m, CaseView cv, Src<T> st
 #pragma unroll
       for (int j = 0; j < DIM; ++j) G[((long)q * DIM + j) * nc + c] = acc[q][j] * inv;
   }
+}
+
+template <class T, int DIM, bool TURB>
+__global__ void __launch_bounds__(128) k_grad(MeshView m, CaseView cv, Src<T> st, Par<T> par, T* G,
+                                              T* Bg, double rel) {
+  k_grad_at<T, DIM, TURB>(blockIdx.x * blockDim.x + threadIdx.x, m, cv, st, par, G, Bg, rel);
 }
 
 // ---------------------------------------------------------------- corrected Green-Gauss sweeps
@@ -677,9 +683,8 @@ __device__ __forceinline__ void closure_cell(const MeshView& m, const CaseView& 
 }
 
 template <class T, int DIM>
-__global__ void __launch_bounds__(128) k_closure(MeshView m, CaseView cv, Src<T> st, Par<T> par,
+__device__ __forceinline__ void k_closure_at(const int c, MeshView m, CaseView cv, Src<T> st, Par<T> par,
                                                  const T* G, T* cl, T* Gwi) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= m.nc) return;
   const int nc = m.nc;
   T out[7], gw[DIM];
@@ -688,6 +693,12 @@ __global__ void __launch_bounds__(128) k_closure(MeshView m, CaseView cv, Src<T>
   for (int i = 0; i < 7; ++i) cl[(long)i * nc + c] = out[i];
 #pragma unroll
   for (int j = 0; j < DIM; ++j) Gwi[(long)j * nc + c] = gw[j];
+}
+
+template <class T, int DIM>
+__global__ void __launch_bounds__(128) k_closure(MeshView m, CaseView cv, Src<T> st, Par<T> par,
+                                                 const T* G, T* cl, T* Gwi) {
+  k_closure_at<T, DIM>(blockIdx.x * blockDim.x + threadIdx.x, m, cv, st, par, G, cl, Gwi);
 }
 
 // effective dynamic viscosity mu + rho nu_t (aquaflux/flow/momentum.py:357-368)
@@ -858,10 +869,9 @@ __device__ __forceinline__ void apcoef_face(const MeshView& m, const CaseView& c
 }
 
 template <class T, int DIM, bool TURB>
-__global__ void __launch_bounds__(128) k_apcoef(MeshView m, CaseView cv, Src<T> st, Par<T> par,
+__device__ __forceinline__ void k_apcoef_at(const int f, MeshView m, CaseView cv, Src<T> st, Par<T> par,
                                                 const T* G, const T* cl, T* ac_own, T* ac_nb,
                                                 T* me) {
-  const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= m.nf) return;
   T ao, an, mf;
   apcoef_face<T, DIM, TURB>(m, cv, st, par, G, cl, f, typename GeoOf<T>::type{}, ao, an, mf);
@@ -870,10 +880,16 @@ __global__ void __launch_bounds__(128) k_apcoef(MeshView m, CaseView cv, Src<T> 
   me[f] = mf;
 }
 
+template <class T, int DIM, bool TURB>
+__global__ void __launch_bounds__(128) k_apcoef(MeshView m, CaseView cv, Src<T> st, Par<T> par,
+                                                const T* G, const T* cl, T* ac_own, T* ac_nb,
+                                                T* me) {
+  k_apcoef_at<T, DIM, TURB>(blockIdx.x * blockDim.x + threadIdx.x, m, cv, st, par, G, cl, ac_own, ac_nb, me);
+}
+
 // ---------------------------------------------------------------- k_dcoeff
 template <class T>
-__global__ void k_dcoeff(MeshView m, const T* ac_own, const T* ac_nb, T* dco) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void k_dcoeff_at(const int c, MeshView m, const T* ac_own, const T* ac_nb, T* dco) {
   if (c >= m.nc) return;
   const int b = m.cf_ptr[c], e = m.cf_ptr[c + 1];
   T a;
@@ -884,6 +900,11 @@ __global__ void k_dcoeff(MeshView m, const T* ac_own, const T* ac_nb, T* dco) {
     a = i == b ? x : a + x;
   }
   dco[c] = gx<T>(m.vol, m.f_vol, c) / a;
+}
+
+template <class T>
+__global__ void k_dcoeff(MeshView m, const T* ac_own, const T* ac_nb, T* dco) {
+  k_dcoeff_at<T>(blockIdx.x * blockDim.x + threadIdx.x, m, ac_own, ac_nb, dco);
 }
 
 // ---------------------------------------------------------------- k_flux
@@ -1079,13 +1100,19 @@ struct FluxStore {
 };
 
 template <class T, int DIM, bool TURB>
-__global__ void __launch_bounds__(128) k_flux(MeshView m, CaseView cv, Src<T> st, Par<T> par,
+__device__ __forceinline__ void k_flux_at(const int f, MeshView m, CaseView cv, Src<T> st, Par<T> par,
                                               const T* G, const T* cl, const T* dco, const T* me,
                                               const T* psi, bool recompute_me, T* FL, double* aux) {
-  const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= m.nf) return;
   flux_face<T, DIM, TURB>(m, cv, st, par, G, cl, dco, me, psi, recompute_me, f,
                           FluxStore<T>{FL, m.nf, f}, aux);
+}
+
+template <class T, int DIM, bool TURB>
+__global__ void __launch_bounds__(128) k_flux(MeshView m, CaseView cv, Src<T> st, Par<T> par,
+                                              const T* G, const T* cl, const T* dco, const T* me,
+                                              const T* psi, bool recompute_me, T* FL, double* aux) {
+  k_flux_at<T, DIM, TURB>(blockIdx.x * blockDim.x + threadIdx.x, m, cv, st, par, G, cl, dco, me, psi, recompute_me, FL, aux);
 }
 
 // ---------------------------------------------------------------- k_sum
@@ -1133,11 +1160,10 @@ __device__ __forceinline__ void sst_rows(const MeshView& m, const CaseView& cv, 
 }
 
 template <class T, int DIM, bool TURB>
-__global__ void __launch_bounds__(128) k_sum(MeshView m, CaseView cv, Src<T> st, Par<T> par, const T* FL, const T* cl,
+__device__ __forceinline__ void k_sum_at(const int c, MeshView m, CaseView cv, Src<T> st, Par<T> par, const T* FL, const T* cl,
                                              const T* G, const T* Gwi, double* R, double* JV) {
   using L = Layout<DIM, TURB>;
   constexpr int NF = L::NFLD;
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= m.nc) return;
   const int nc = m.nc, nf = m.nf;
   T r[NF];
@@ -1157,6 +1183,12 @@ __global__ void __launch_bounds__(128) k_sum(MeshView m, CaseView cv, Src<T> st,
   if constexpr (TURB) sst_rows<T, DIM>(m, cv, st, par, cl, G, Gwi, c, r[L::K], r[L::W]);
 #pragma unroll
   for (int q = 0; q < NF; ++q) put<T>(R, JV, (long)q * nc + c, r[q]);
+}
+
+template <class T, int DIM, bool TURB>
+__global__ void __launch_bounds__(128) k_sum(MeshView m, CaseView cv, Src<T> st, Par<T> par, const T* FL, const T* cl,
+                                             const T* G, const T* Gwi, double* R, double* JV) {
+  k_sum_at<T, DIM, TURB>(blockIdx.x * blockDim.x + threadIdx.x, m, cv, st, par, FL, cl, G, Gwi, R, JV);
 }
 
 // Zero the tangent of n dual values (the "frozen" JVP holds gradients, closure and a_P fixed).
@@ -1285,11 +1317,124 @@ AdjWork adj_layout(FvCase* cs) {
   return aw;
 }
 
+// ---------------------------------------------------------------- one persistent launch
+// The whole residual + VJP evaluation of a case with compact gradients and first-order upwind
+// advection as ONE cooperative launch: the stages of run<double> and of the adjoint in order, each
+// over its cells or faces, separated by grid-wide barriers (cooperative_groups grid sync; the
+// cooperative launch guarantees every block is resident).  Each thread takes `chunk` consecutive
+// cells / faces per step of a grid-stride loop.  Every cell or face is computed by the same body
+// as in the stage-per-launch path, so the result is bitwise the same.
+struct PersistentVjp {
+  Work<double> w;
+  AdjWork aw;
+  const double* W;
+  double* aux;
+  double* R;
+  double* out;
+  double rel;
+  int chunk;
+};
+
+template <int DIM, bool TURB>
+__global__ void __launch_bounds__(128) k_persistent_vjp(MeshView m, CaseView cv, Src<double> st,
+                                                        Par<double> par, PersistentVjp a) {
+  namespace cg = cooperative_groups;
+  cg::grid_group grid = cg::this_grid();
+  const long nthr = (long)gridDim.x * blockDim.x;
+  const long tid = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int chunk = a.chunk;
+  auto each = [&](long n, auto&& fn) {
+    for (long base = tid * chunk; base < n; base += nthr * chunk)
+      for (int k = 0; k < chunk && base + k < n; ++k) fn((int)(base + k));
+  };
+  const Work<double>& w = a.w;
+  const AdjWork& aw = a.aw;
+  each(m.nc, [&](int c) { k_grad_at<double, DIM, TURB>(c, m, cv, st, par, w.G, nullptr, a.rel); });
+  grid.sync();
+  if constexpr (TURB) {
+    each(m.nc, [&](int c) { k_closure_at<double, DIM>(c, m, cv, st, par, w.G, w.cl, w.Gwi); });
+    grid.sync();
+  }
+  each(m.nf, [&](int f) {
+    k_apcoef_at<double, DIM, TURB>(f, m, cv, st, par, w.G, w.cl, w.acown, w.acnb, w.me);
+  });
+  grid.sync();
+  each(m.nc, [&](int c) { k_dcoeff_at<double>(c, m, w.acown, w.acnb, w.dco); });
+  grid.sync();
+  each(m.nf, [&](int f) {
+    k_flux_at<double, DIM, TURB>(f, m, cv, st, par, w.G, w.cl, w.dco, w.me, nullptr, false, w.FL,
+                                 a.aux);
+  });
+  grid.sync();
+  each(m.nc, [&](int c) {
+    k_sum_at<double, DIM, TURB>(c, m, cv, st, par, w.FL, w.cl, w.G, w.Gwi, a.R, nullptr);
+  });
+  grid.sync();
+  each(m.nc, [&](int c) { a_sum_at<DIM, TURB>(c, m, cv, st, par, a.W, w.cl, w.G, w.Gwi, aw); });
+  grid.sync();
+  each(m.nc, [&](int c) {
+    a_flux_at<DIM, TURB>(c, m, cv, st, par, w.G, w.cl, w.dco, w.me, a.aux, aw);
+  });
+  grid.sync();
+  each(m.nc, [&](int c) {
+    a_apcoef_at<DIM, TURB>(c, m, cv, st, par, w.G, w.cl, w.dco, w.me, a.aux, aw);
+  });
+  grid.sync();
+  if constexpr (TURB) {
+    each(m.nc, [&](int c) { a_closure_at<DIM>(c, m, cv, st, par, w.G, w.cl, aw); });
+    grid.sync();
+  }
+  each(m.nf, [&](int f) { a_grad_face_at<DIM, TURB>(f, m, cv, aw, aw.Gb, nullptr, a.rel, w.FL); });
+  grid.sync();
+  each(m.nc, [&](int c) { a_grad_at<DIM, TURB>(c, m, cv, aw, w.FL, a.out); });
+}
+
+// Whether the case's schemes are those the persistent kernel runs.
+bool persistent_supported(const FvCase* cs) {
+  return cs->desc.gradient_sweeps <= 1 && !cs->view.rec_mom && !cs->view.rec_sca &&
+         !cs->flx_active;
+}
+
+template <int DIM, bool TURB>
+int run_vjp_persistent(FvCase* cs, const double* state, const double* W, double* R, double* out,
+                       cudaStream_t s) {
+  const MeshView& m = cs->mesh->view;
+  const long nc = m.nc, nf = m.nf;
+  PersistentVjp a;
+  a.w = work_layout<double, DIM, TURB>(cs->work, nc, nf, 0);
+  a.aw = adj_layout<DIM, TURB>(cs);
+  a.W = W;
+  a.aux = cs->aux;
+  a.R = R ? R : cs->tmp;
+  a.out = out;
+  a.rel = cs->desc.gradient_sweeps >= 1 ? cs->desc.gradient_relaxation : 1.0;
+  a.chunk = cs->pchunk;
+  Src<double> st{state};
+  Par<double> par{cs->mu, cs->inlet_scale, cs->mu / cs->desc.rho};
+  const MeshView mv = m;
+  const CaseView cv = cs->view;
+  auto kern = k_persistent_vjp<DIM, TURB>;
+  int dev = 0, sms = 0, per_sm = 0;
+  FV_CUDA_TRY(cudaGetDevice(&dev));
+  FV_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  FV_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, cs->pblock, 0));
+  if (per_sm < 1) {
+    fv_set_error("persistent residual + VJP: no block of %d threads fits on an SM", cs->pblock);
+    return FV_ERR_ARG;
+  }
+  void* args[] = {(void*)&mv, (void*)&cv, (void*)&st, (void*)&par, (void*)&a};
+  FV_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)kern, dim3(per_sm * sms),
+                                          dim3(cs->pblock), args, 0, s));
+  return FV_OK;
+}
+
 // gb_save (optional, (NF, DIM, nc)): receives the gradient cotangent before the corrected
 // scheme's backward sweeps overwrite it (the mesh-coordinate adjoint re-runs them).
 template <int DIM, bool TURB>
 int run_vjp(FvCase* cs, const double* state, const double* W, double* R, double* out,
             cudaStream_t s, double* gb_save = nullptr) {
+  if (cs->persistent && !gb_save && persistent_supported(cs))
+    return run_vjp_persistent<DIM, TURB>(cs, state, W, R, out, s);
   using L = Layout<DIM, TURB>;
   const MeshView& m = cs->mesh->view;
   const CaseView& cv = cs->view;

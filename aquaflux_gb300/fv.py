@@ -269,6 +269,21 @@ class FlowCase:
                                      ctypes.byref(best)))
         return int(best.value)
 
+    def set_persistent(self, enable: bool = True, block: int = 128, chunk: int = 1) -> None:
+        """Evaluate residual + VJP as one persistent cooperative launch (``fv_case_set_persistent``;
+        compact gradients, first-order upwind)."""
+        check(lib().fv_case_set_persistent(self._h, int(bool(enable)), int(block), int(chunk)))
+
+    def autotune_persistent(self, state, w) -> tuple[int, int, float]:
+        """``(block, chunk, ms)`` of the fastest persistent launch at ``state`` / ``w``."""
+        s, ww = self._vec(state), self._vec(w)
+        out = torch.empty_like(s)
+        b, c, t = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_float(0.0)
+        check(lib().fv_case_autotune_persistent(self._h, ptr(s), ptr(ww), ptr(out), _stream(),
+                                                ctypes.byref(b), ctypes.byref(c),
+                                                ctypes.byref(t)))
+        return b.value, c.value, t.value
+
     def set_block_size(self, threads: int) -> None:
         check(lib().fv_case_set_block_size(self._h, int(threads)))
 

@@ -66,6 +66,8 @@ def _args():
                     help="skip the adjoint objectives' gradients after the Newton solves")
     ap.add_argument("--no-newton-oracle", action="store_true",
                     help="skip the CPU oracle's residual of the converged Newton states")
+    ap.add_argument("--no-batched", action="store_true",
+                    help="skip the batched sweep's residual + VJP timing (graph vs persistent)")
     ap.add_argument("--no-config1", action="store_true",
                     help="skip the config-1 cavity Newton solve (GPU beside the CPU oracle)")
     ap.add_argument("--newton-only", default=None, metavar="KIND:PREC:TANGENTS",
@@ -595,6 +597,11 @@ def run_gpu(args, rank: int, world: int, local_rank: int) -> dict | None:
                 out["config1_newton"] = config1_newton(args)
             except Exception as e:  # reported, never allowed to lose the headline line
                 out["config1_newton"] = {"error": f"{type(e).__name__}: {e}"[:300]}
+    if not args.no_batched:
+        try:
+            out["batched"] = batched_step_timing()
+        except Exception as e:  # reported, never allowed to lose the headline line
+            out["batched"] = {"error": f"{type(e).__name__}: {e}"[:300]}
     if "newton" in out:  # the headline Newton numbers last, where a truncated tail keeps them
         out["newton_summary"] = newton_summary(out["newton"], args.newton_kinds.split(","))
     return out
@@ -844,6 +851,63 @@ def adjoint_block(case, state) -> dict:
     return out
 
 
+def batched_step_timing(steps: int = 20, warmup: int = 5) -> dict:
+    """The batched calibration sweep's residual + VJP over all 64 instances (one disjoint-union
+    case): the stage-per-launch step replayed as one CUDA graph, and the same step as one
+    persistent cooperative launch (block size and per-thread chunk autotuned); results bitwise
+    equal."""
+    import torch
+
+    from aquaflux_gb300 import workloads
+    from aquaflux_gb300._lib import check, lib, ptr
+
+    bw = workloads.batched_channels(64, seed=0)
+    case = bw.workload.device_case()
+    m = bw.workload.mesh
+    s = torch.tensor(bw.initial_state(), device="cuda")
+    w = torch.randn(case.n_unknowns, dtype=torch.float64, device="cuda",
+                    generator=torch.Generator(device="cuda").manual_seed(0))
+    best_tb = case.autotune(s, w)
+    out_g = torch.empty_like(s)
+    out_p = torch.empty_like(s)
+
+    def step(out):
+        check(lib().fv_vjp(case.handle, ptr(s), ptr(w), 0, ptr(out),
+                           torch.cuda.current_stream().cuda_stream))
+
+    def timed(fn):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    for _ in range(3):
+        step(out_g)
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        step(out_g)
+    ms_graph = timed(graph.replay)
+    block, chunk, _ = case.autotune_persistent(s, w)
+    case.set_persistent(True, block, chunk)
+    ms_pers = timed(lambda: step(out_p))
+    case.set_persistent(False)
+    return {"workload": f"64 2D laminar channels, n in [{int(bw.sizes.min())}, "
+                        f"{int(bw.sizes.max())}], {m.n_cells} cells, {m.n_faces} faces",
+            "graph_of_stage_launches_ms": round(ms_graph, 4), "stage_block_size": best_tb,
+            "persistent_launch_ms": round(ms_pers, 4), "persistent_block": block,
+            "persistent_chunk": chunk,
+            "gfaces_s_graph": round(m.n_faces / (ms_graph * 1e-3) / 1e9, 4),
+            "gfaces_s_persistent": round(m.n_faces / (ms_pers * 1e-3) / 1e9, 4),
+            "bitwise_equal": bool(torch.equal(out_g, out_p))}
+
+
 def run_batched(args) -> dict:
     """The batched calibration sweep: 64 uneven 2D laminar channels side by side in one
     disjoint-union case.  Residual + VJP of all instances, one launch per stage, captured once in a
@@ -890,6 +954,22 @@ def run_batched(args) -> dict:
     torch.cuda.synchronize()
     assert torch.equal(ref, out_buf)
     gfaces = m.n_faces / (ms * 1e-3) / 1e9
+    # the same step as one persistent cooperative launch (autotuned block and chunk)
+    pblock, pchunk, _ = case.autotune_persistent(s, w)
+    case.set_persistent(True, pblock, pchunk)
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(args.steps):
+        step()
+    e1.record()
+    torch.cuda.synchronize()
+    ms_p = e0.elapsed_time(e1) / args.steps
+    persistent = {"ms_per_step": round(ms_p, 4), "block": pblock, "chunk": pchunk,
+                  "gfaces_s": round(m.n_faces / (ms_p * 1e-3) / 1e9, 4),
+                  "bitwise_equal_graph": bool(torch.equal(ref, out_buf))}
+    case.set_persistent(False)
     # the calibration: Newton for all instances at once, then one adjoint for all gradients
     warm = workloads.batched_channels(4, n_min=8, n_max=16, seed=1)
     wc = warm.workload.device_case()
@@ -915,6 +995,7 @@ def run_batched(args) -> dict:
                                f"{int(bw.sizes.max())}], {m.n_cells} cells, {m.n_faces} faces",
                    "graph": "one CUDA graph replay per step", "block_size": best_tb},
         "instances_per_s": round(64.0 / (ms * 1e-3), 1),
+        "persistent_launch": persistent,
         "calibration": {"newton_seconds": round(t_newton, 3), "converged": bool(res.converged),
                         "newton_steps": res.steps,
                         "krylov_iterations": int(sum(res.krylov_iterations)),

@@ -132,6 +132,16 @@ int fv_case_set_viscosity_field(FvCase* c, const double* mu_cell, void* stream);
  * results do not depend on it).  fv_case_autotune times the residual + VJP step at state / w for
  * 32, 64, 96 and 128 and keeps the fastest (best receives it; out: n_unknowns scratch). */
 int fv_case_set_block_size(FvCase* c, int threads);
+/* Residual + VJP (fv_vjp) as ONE persistent cooperative launch (all stages in one kernel,
+ * grid-wide barriers between them; compact gradients and first-order upwind; bitwise the
+ * stage-per-launch result): enable != 0 with `block` threads per block (multiple of 32 in
+ * [32, 128]) and `chunk` consecutive cells / faces per thread per stage (1 .. 64).  The batched
+ * calibration sweep's instances run side by side in one such launch.  fv_case_autotune_persistent
+ * times every (block in {64, 128}) x (chunk in {1, 2, 4, 8}) at state / w, keeps the fastest
+ * (without enabling the path) and returns it with its time per evaluation. */
+int fv_case_set_persistent(FvCase* c, int enable, int block, int chunk);
+int fv_case_autotune_persistent(FvCase* c, const double* state, const double* w, double* out,
+                                void* stream, int* best_block, int* best_chunk, float* best_ms);
 int fv_case_autotune(FvCase* c, const double* state, const double* w, double* out, void* stream,
                      int* best);
 /* After fv_mesh_set_nodes: recompute a turbulent case's SST wall distance (to each cell's nearest

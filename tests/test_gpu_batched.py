@@ -95,3 +95,33 @@ def test_autotune_keeps_results_bitwise():
     for tb in (32, 64, 128):
         case.set_block_size(tb)
         assert torch.equal(case.vjp(s, w), ref)
+
+
+@pytest.mark.parametrize("which", ["batched", "sst_channel"])
+def test_persistent_launch_is_bitwise_the_stage_launches(which):
+    """Residual + VJP as one persistent cooperative launch (every stage in one kernel, grid-wide
+    barriers between them) equals the stage-per-launch evaluation bit for bit, for every block size
+    and chunk the autotuner tries, on the batched instances and on an SST channel."""
+    from aquaflux_gb300 import workloads
+
+    if which == "batched":
+        bw = _small()
+        case = bw.workload.device_case()
+        s = torch.tensor(bw.initial_state(), device="cuda")
+    else:
+        wl = workloads.channel3d(10)
+        case = wl.device_case()
+        s = torch.tensor(wl.initial_state(noise=0.05), device="cuda")
+    w = torch.randn(case.n_unknowns, dtype=torch.float64, device="cuda",
+                    generator=torch.Generator(device="cuda").manual_seed(1))
+    r0, g0 = case.vjp(s, w, return_residual=True)
+    for block in (64, 128):
+        for chunk in (1, 2, 4, 8):
+            case.set_persistent(True, block, chunk)
+            r1, g1 = case.vjp(s, w, return_residual=True)
+            assert torch.equal(r1, r0) and torch.equal(g1, g0), (block, chunk)
+    case.set_persistent(False)
+    block, chunk, ms = case.autotune_persistent(s, w)
+    assert block in (64, 128) and chunk in (1, 2, 4, 8) and ms > 0
+    r2, g2 = case.vjp(s, w, return_residual=True)  # the tuner leaves the path off
+    assert torch.equal(g2, g0)
