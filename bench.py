@@ -50,7 +50,10 @@ def _args():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--size", type=int, default=128, help="cells per axis of the 3D channel")
-    ap.add_argument("--cpu-sample", type=int, default=24, help="cells per axis of the CPU sample")
+    ap.add_argument("--cpu-sample", type=int, default=40,
+                    help="cells per axis of the CPU sample (a reference-arm step)")
+    ap.add_argument("--no-reference-full-size", dest="reference_full_size", action="store_false",
+                    help="skip the reference arm's one full-size CPU evaluation")
     ap.add_argument("--ilu-sample", type=int, default=48,
                     help="cells per axis of the ILU(0) CPU-vs-GPU sample (0: skip)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -1008,6 +1011,42 @@ def run_batched(args) -> dict:
     }
 
 
+def cpu_full_size_rate(size: int, step: str = "vjp") -> dict:
+    """One residual + VJP (or JVP) of the CPU oracle on the full ``size^3`` channel (all host
+    threads), timed after one untimed evaluation: the reference algorithm's CPU throughput at the
+    benchmark's own size."""
+    import numpy as np
+    import torch
+
+    from aquaflux_gb300 import workloads
+    from oracle import fv_oracle as fo
+
+    torch.set_num_threads(os.cpu_count() or 1)
+    wl = workloads.channel3d(size, renumber="host")
+    case = fo.make_case(wl.mesh, mu=wl.mu, rho=wl.rho, flow_bc=wl.flow_bc,
+                        sst={"nu": wl.mu / wl.rho, "walls": wl.sst["walls"], "k": wl.sst["k"],
+                             "omega": wl.sst["omega"]})
+    orc = fo.Oracle(case)
+    s = wl.initial_state(seed=1, noise=0.05)
+    v = np.random.default_rng(2).standard_normal(s.size)
+
+    def one():
+        if step == "vjp":
+            x = torch.as_tensor(s).requires_grad_(True)
+            r = orc.residual(x)
+            torch.autograd.grad(r, x, torch.as_tensor(v))
+        else:
+            orc.residual(torch.as_tensor(s))
+            orc.jvp(s, v)
+
+    one()
+    t0 = time.perf_counter()
+    one()
+    el = time.perf_counter() - t0
+    return {"faces_per_s": wl.mesh.n_faces / el, "seconds": el, "cores": os.cpu_count() or 1,
+            "faces": wl.mesh.n_faces}
+
+
 def run_reference(args) -> dict:
     cb = cpu_residual_jvp_rate(args.cpu_sample, min_seconds=4.0, step=args.step)
     rates = [cb["faces_per_s"]]
@@ -1015,6 +1054,12 @@ def run_reference(args) -> dict:
         rates.append(cpu_residual_jvp_rate(args.cpu_sample, min_seconds=2.0,
                                            step=args.step)["faces_per_s"])
     v = statistics.median(rates) / 1e9
+    full = None
+    if args.reference_full_size:
+        try:
+            full = cpu_full_size_rate(args.size, step=args.step)
+        except Exception as e:  # reported, never allowed to lose the line
+            full = {"error": f"{type(e).__name__}: {e}"[:200]}
     return {
         "impl": "reference", "metric": METRIC, "value": round(v, 6), "unit": UNIT, "n_gpus": 0,
         "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
@@ -1026,6 +1071,13 @@ def run_reference(args) -> dict:
                          "sample": cb["sample"]},
         "e2e": {"value": round(v, 6), "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
+        "full_size": None if full is None else (
+            full if "error" in full else
+            {"value": round(full["faces_per_s"] / 1e9, 6), "unit": UNIT,
+             "seconds_per_evaluation": round(full["seconds"], 2), "faces": full["faces"],
+             "cores": full["cores"],
+             "what": f"one residual + {args.step.upper()} of the CPU oracle on the full "
+                     f"{args.size}^3 channel"}),
     }
 
 
