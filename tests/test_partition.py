@@ -161,3 +161,25 @@ def test_two_gloo_ranks_equal_serial(tmp_path):
         assert _rel(got[k], want[k]) <= 1e-12, k
     assert dots[0] == dots[1]
     assert abs(dots[0] - float(np.dot(v, w))) <= 1e-12 * abs(float(np.dot(np.abs(v), np.abs(w))))
+
+
+def test_halo_plans_pair_up():
+    """What rank p receives from q is what q sends to p: the same global cells, in the same order."""
+    from aquaflux_gb300.partition import halo_plans
+
+    m = _mesh(16)
+    owner = partition_cells(m.n_cells, 4)
+    parts = build_partitions(m, owner, 3)
+    plans = halo_plans(parts, owner)
+    for p in parts:
+        for q, local in plans[p.rank].recv.items():
+            want = p.cells[local]
+            qp = parts[q]
+            sent = qp.cells[qp.owned][plans[q].send[p.rank]]
+            assert np.array_equal(want, sent)
+            assert np.all(owner[want] == q)
+    # every ghost is received from exactly its owner
+    for p in parts:
+        got = np.concatenate([p.cells[v] for v in plans[p.rank].recv.values()]) \
+            if plans[p.rank].recv else np.zeros(0, dtype=np.int64)
+        assert np.array_equal(np.sort(got), np.sort(p.cells[p.ghosts]))
