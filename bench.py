@@ -605,6 +605,11 @@ def run_gpu(args, rank: int, world: int, local_rank: int) -> dict | None:
             out["batched"] = batched_step_timing()
         except Exception as e:  # reported, never allowed to lose the headline line
             out["batched"] = {"error": f"{type(e).__name__}: {e}"[:300]}
+    if not args.no_cpu_baseline:
+        try:
+            out["renumbering"] = renumbering_block(args.size)
+        except Exception as e:  # reported, never allowed to lose the headline line
+            out["renumbering"] = {"error": f"{type(e).__name__}: {e}"[:300]}
     if "newton" in out:  # the headline Newton numbers last, where a truncated tail keeps them
         out["newton_summary"] = newton_summary(out["newton"], args.newton_kinds.split(","))
     return out
@@ -852,6 +857,34 @@ def adjoint_block(case, state) -> dict:
     torch.cuda.synchronize()
     out["node_vjp_ms"] = round((time.perf_counter() - t0) * 1e3, 2)
     return out
+
+
+def renumbering_block(size: int) -> dict:
+    """Reverse Cuthill-McKee of the randomly relabelled ``size^3`` channel: on the GPU (the cell
+    graph and the level-by-level sweeps; host argsort of the degrees and the copies included)
+    beside scipy's ``reverse_cuthill_mckee`` on the host (the reference's own call, one core),
+    with the permutations compared."""
+    import numpy as np
+    import torch
+
+    from aquaflux_gb300 import mesh as fm
+    from aquaflux_gb300 import workloads
+    from aquaflux_gb300.reorder import mesh_rcm_permutation
+
+    m = workloads.channel3d(size, renumber=False).mesh
+    m = fm.permute_cells(m, fm.random_permutation(m.n_cells, 0))
+    mesh_rcm_permutation(m)  # warm
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    gpu = mesh_rcm_permutation(m)
+    torch.cuda.synchronize()
+    t_gpu = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    ref = workloads.rcm_permutation(m)
+    t_cpu = time.perf_counter() - t0
+    return {"cells": m.n_cells, "gpu_ms": round(t_gpu * 1e3, 1),
+            "scipy_ms": round(t_cpu * 1e3, 1), "cpu_kind": "reference",
+            "bitwise_equal": bool(np.array_equal(gpu, ref))}
 
 
 def batched_step_timing(steps: int = 20, warmup: int = 5) -> dict:
