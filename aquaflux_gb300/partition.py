@@ -330,7 +330,12 @@ class DistributedResidual:
         return out.reshape(-1)
 
     def dot(self, a: torch.Tensor, b: torch.Tensor) -> float:
-        part = torch.dot(a, b).reshape(1).to(torch.float64)
+        if a.is_cuda:  # the library's fixed-order reduction (fv_dot_f64): reproducible partials
+            from .sparse import dot as device_dot
+
+            part = device_dot(a.contiguous(), b.contiguous()).reshape(1)
+        else:
+            part = torch.dot(a, b).reshape(1).to(torch.float64)
         parts = [torch.empty_like(part) for _ in range(self.world)]
         self.dist.all_gather(parts, part)
         total = parts[0].clone()
