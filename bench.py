@@ -538,17 +538,19 @@ def run_gpu(args, rank: int, world: int, local_rank: int) -> dict | None:
     # step's time, against 2 instructions per clock per SM at the sampled SM clock
     fp64_roof = None
     instr_path = os.path.join(ROOT, "profiles", "fp64_instructions.json")
-    if os.path.exists(instr_path) and args.step == "vjp":
+    if os.path.exists(instr_path):
         with open(instr_path) as f:
             ins = json.load(f)
+        per_face = ins["vjp_step_instr_per_face" if args.step == "vjp" else "jvp_step_instr_per_face"]
         mhz = clk.get("sm_mhz") or 2070.0
         peak_gi = ins["pipe_instr_per_clock_per_sm"] * ins["sms"] * mhz * 1e6 / 1e9
-        ach_gi = ins["vjp_step_instr_per_face"] * F / (ms / args.steps * 1e-3) / 1e9
-        fp64_roof = {"instr_per_face": ins["vjp_step_instr_per_face"],
+        ach_gi = per_face * F / (ms / args.steps * 1e-3) / 1e9
+        fp64_roof = {"instr_per_face": per_face,
                      "achieved_ginstr_s": round(ach_gi, 1), "peak_ginstr_s": round(peak_gi, 1),
                      "frac": round(ach_gi / peak_gi, 4),
-                     "bound_gfaces_s": round(peak_gi / ins["vjp_step_instr_per_face"], 4),
-                     "source": "profiles/fp64_residual_vjp_channel3d_64.md (ncu, 64^3)"}
+                     "bound_gfaces_s": round(peak_gi / per_face, 4),
+                     "source": "profiles/fp64_%s_channel3d_64.md (ncu, 64^3)"
+                               % ("residual_vjp" if args.step == "vjp" else "jvp")}
     out = {
         "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4),
