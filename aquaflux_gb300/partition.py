@@ -280,9 +280,11 @@ class DistributedResidual:
 
     def _exchange(self, payloads: dict, shapes: dict) -> dict:
         """Send ``payloads[q]`` to every q, receive a tensor of ``shapes[q]`` from every q."""
-        reqs, got = [], {}
+        reqs, got, held = [], {}, []
         for q, t in payloads.items():
-            reqs.append(self.dist.isend(t.contiguous(), q))
+            buf = t.contiguous()
+            held.append(buf)  # alive until every request has completed
+            reqs.append(self.dist.isend(buf, q))
         for q, n in shapes.items():
             buf = torch.empty(n, dtype=torch.float64, device=self.device)
             got[q] = buf
