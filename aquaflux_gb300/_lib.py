@@ -59,6 +59,7 @@ SIGNATURES = {
     "fv_case_set_viscosity_field": (c_int, [P, P, P]),
     "fv_case_set_block_size": (c_int, [P, c_int]),
     "fv_case_set_persistent": (c_int, [P, c_int, c_int, c_int]),
+    "fv_case_set_cell_order": (c_int, [P, c_int, P]),
     "fv_case_autotune_persistent": (c_int, [P, P, P, P, P, P, P, P]),
     "fv_case_autotune": (c_int, [P, P, P, P, P, P]),
     "fv_segment_dot": (c_int, [c_int, P, c_int, c_int, P, P, P, P]),

@@ -217,7 +217,7 @@ template <int DIM, bool TURB>
 __global__ void __launch_bounds__(128) a_sum(MeshView m, CaseView cv, Src<double> st, Par<double> par,
                                              const double* W, const double* cl, const double* G,
                                              const double* Gwi, AdjWork aw) {
-  a_sum_at<DIM, TURB>(blockIdx.x * blockDim.x + threadIdx.x, m, cv, st, par, W, cl, G, Gwi, aw);
+  a_sum_at<DIM, TURB>(stage_cell(m, cv), m, cv, st, par, W, cl, G, Gwi, aw);
 }
 
 // momentum-normal flux mn(f) = sum_j n_j ((rho u_j)_f + (rho grad u_j)_f . skew) -- its partial
@@ -296,9 +296,11 @@ __device__ __forceinline__ void a_flux_at(const int c, MeshView m, CaseView cv, 
       const int n = m.nb[f];
       const double g = m.g[f];
       const double wgt = isnb ? g : 1.0 - g;  // this side's interpolation weight
-      double tN[DIM];
+      // this side's correction vector: tP on the owner side, tN on the neighbour side (the two
+      // sides run one code path on selected operands, so a warp mixing them does not diverge)
+      double tS[DIM];
 #pragma unroll
-      for (int j = 0; j < DIM; ++j) tN[j] = m.tN[(long)j * nf + f];
+      for (int j = 0; j < DIM; ++j) tS[j] = isnb ? m.tN[(long)j * nf + f] : tP[j];
       double FLb[NF];
 #pragma unroll
       for (int q = 0; q < NF; ++q) {
@@ -329,17 +331,13 @@ __device__ __forceinline__ void a_flux_at(const int c, MeshView m, CaseView cv, 
           }
         }
         mdotb += fb * up;
-        const double k1 = fb * cmo;  // F_i = ... - c cpn
+        // F_i = ... - c cpn: +k1 on the owner's state and gradient, -k1 on the neighbour's; the
+        // upwind term goes to the upwind side
+        const double k1 = isnb ? -(fb * cmo) : fb * cmo;
         cb -= fb * cpn;
-        if (!isnb) {
-          sb[i] += k1 + (out ? fb * mdot : 0.0);
+        sb[i] += k1 + (out != isnb ? fb * mdot : 0.0);
 #pragma unroll
-          for (int j = 0; j < DIM; ++j) Gb[i][j] += k1 * tP[j];
-        } else {
-          sb[i] += -k1 + (!out ? fb * mdot : 0.0);
-#pragma unroll
-          for (int j = 0; j < DIM; ++j) Gb[i][j] -= k1 * tN[j];
-        }
+        for (int j = 0; j < DIM; ++j) Gb[i][j] += k1 * tS[j];
         pfb += fb * nrm[i] * A;
       }
       if (TURB) ntb += cb * aux[(isnb ? 5L : 4L) * nf + f] * rho;
@@ -370,16 +368,10 @@ __device__ __forceinline__ void a_flux_at(const int c, MeshView m, CaseView cv, 
             }
           }
           mdotb += fb * up * irho;
-          const double k1 = fb * cs_;
-          if (!isnb) {
-            sb[q] += k1 + (vout ? fb * vflux : 0.0);
+          const double k1 = isnb ? -(fb * cs_) : fb * cs_;
+          sb[q] += k1 + (vout != isnb ? fb * vflux : 0.0);
 #pragma unroll
-            for (int j = 0; j < DIM; ++j) Gb[q][j] += k1 * tP[j];
-          } else {
-            sb[q] += -k1 + (!vout ? fb * vflux : 0.0);
-#pragma unroll
-            for (int j = 0; j < DIM; ++j) Gb[q][j] -= k1 * tN[j];
-          }
+          for (int j = 0; j < DIM; ++j) Gb[q][j] += k1 * tS[j];
           const double gXb = -fb * cpn * aux[(b0 + (isnb ? 2 : 1)) * nf + f];
           // gamma_X = nu + (sig_out + F1 (sig_in - sig_out)) nu_t
           F1b += gXb * (in - ou) * ntX;
@@ -389,7 +381,7 @@ __device__ __forceinline__ void a_flux_at(const int c, MeshView m, CaseView cv, 
       // mdot = me - rho A dhat damping
       const double dhatb = -mdotb * (rho * A) * damping;
       const double dampb = -mdotb * (rho * A) * dhat;
-      sb[L::P] += isnb ? dampb * inv_nd : -dampb * inv_nd;
+      sb[L::P] += (isnb ? dampb : -dampb) * inv_nd;
 #pragma unroll
       for (int j = 0; j < DIM; ++j) gpfb[j] -= dampb * inv_nd * m.dvec[(long)j * nf + f];
 #pragma unroll
@@ -565,7 +557,7 @@ template <int DIM, bool TURB, bool FLX = false, bool LIM = false>
 __global__ void __launch_bounds__(128) a_flux(MeshView m, CaseView cv, Src<double> st, Par<double> par,
                                               const double* G, const double* cl, const double* dco,
                                               const double* me, const double* aux, AdjWork aw) {
-  a_flux_at<DIM, TURB, FLX, LIM>(blockIdx.x * blockDim.x + threadIdx.x, m, cv, st, par, G, cl, dco, me, aux, aw);
+  a_flux_at<DIM, TURB, FLX, LIM>(stage_cell(m, cv), m, cv, st, par, G, cl, dco, me, aux, aw);
 }
 
 // ---------------------------------------------------------------- a_limiter
@@ -719,7 +711,7 @@ template <int DIM, bool TURB>
 __global__ void __launch_bounds__(128) a_apcoef(MeshView m, CaseView cv, Src<double> st, Par<double> par,
                                                 const double* G, const double* cl, const double* dco,
                                                 const double* me, const double* aux, AdjWork aw) {
-  a_apcoef_at<DIM, TURB>(blockIdx.x * blockDim.x + threadIdx.x, m, cv, st, par, G, cl, dco, me, aux, aw);
+  a_apcoef_at<DIM, TURB>(stage_cell(m, cv), m, cv, st, par, G, cl, dco, me, aux, aw);
 }
 
 // ---------------------------------------------------------------- a_closure (SST)
@@ -897,7 +889,7 @@ __device__ __forceinline__ void a_closure_at(const int c, MeshView m, CaseView c
 template <int DIM>
 __global__ void __launch_bounds__(128) a_closure(MeshView m, CaseView cv, Src<double> st, Par<double> par,
                                                  const double* G, const double* cl, AdjWork aw) {
-  a_closure_at<DIM>(blockIdx.x * blockDim.x + threadIdx.x, m, cv, st, par, G, cl, aw);
+  a_closure_at<DIM>(stage_cell(m, cv), m, cv, st, par, G, cl, aw);
 }
 
 // ---------------------------------------------------------------- a_grad
@@ -1101,5 +1093,5 @@ __device__ __forceinline__ void a_grad_at(const int c, MeshView m, CaseView cv, 
 template <int DIM, bool TURB>
 __global__ void __launch_bounds__(128) a_grad(MeshView m, CaseView cv, AdjWork aw, const double* pb,
                                               double* out) {
-  a_grad_at<DIM, TURB>(blockIdx.x * blockDim.x + threadIdx.x, m, cv, aw, pb, out);
+  a_grad_at<DIM, TURB>(stage_cell(m, cv), m, cv, aw, pb, out);
 }

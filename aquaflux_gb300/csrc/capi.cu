@@ -1,5 +1,9 @@
 // C ABI for cases: boundary tables, SST wall data, and the residual / JVP entry points.
+#include <algorithm>
+#include <cstdint>
 #include <cstring>
+#include <map>
+#include <unordered_map>
 #include <vector>
 
 #include "internal.cuh"
@@ -118,6 +122,64 @@ static void chain_state(FvCase* c, double* v, cudaStream_t s) {
                                                         c->desc.scalar_transform, c->phys, v);
 }
 
+
+// Warp-coherent order of the cell stages.  The control flow of a cell-centric stage follows the
+// cell's face list: at each position an interior face the cell owns, an interior face it is the
+// neighbour of, or a boundary face with its (flow, k, omega, SST-wall) table entry.  Cells with
+// the same pattern take the same branches, so the order groups them: patterns ascending, natural
+// order inside a group.  On a renumbered mesh the natural order interleaves the few boundary and
+// wall patterns with the interior one in nearly every warp, and a diverged warp issues the
+// floating-point work of every branch its lanes take.
+static int build_cell_order(FvCase* c, const signed char* flow_kind, const signed char* k_kind,
+                     const signed char* omega_kind, const unsigned char* sst_wall,
+                     cudaStream_t s) {
+  const FvMesh* m = c->mesh;
+  const int nc = m->nc, nfi = m->nfi, nf = m->nf;
+  std::map<uint32_t, int> types;  // boundary table entry -> pattern symbol 2, 3, ... (max 15)
+  std::vector<unsigned char> bsym(nf - nfi);
+  for (int i = nfi; i < nf; ++i) {
+    const int r = m->h_face_old[i];
+    const uint32_t key = (uint32_t)(unsigned char)flow_kind[r] |
+                         (uint32_t)(unsigned char)(k_kind ? k_kind[r] : -1) << 8 |
+                         (uint32_t)(unsigned char)(omega_kind ? omega_kind[r] : -1) << 16 |
+                         (uint32_t)(sst_wall && sst_wall[r] ? 1 : 0) << 24;
+    const int id = types.emplace(key, (int)types.size()).first->second;
+    bsym[i - nfi] = (unsigned char)std::min(2 + id, 15);
+  }
+  // pattern code: face count in the top byte, 4 bits per position for the first 14 faces
+  std::vector<uint64_t> code(nc);
+  for (int cell = 0; cell < nc; ++cell) {
+    const int b = m->h_cf_ptr[cell], e = m->h_cf_ptr[cell + 1];
+    uint64_t v = (uint64_t)std::min(e - b, 255) << 56;
+    for (int p = 0; p < e - b && p < 14; ++p) {
+      const unsigned ent = m->h_cf_face[b + p];
+      const int f = (int)(ent & ~FV_NB_BIT);
+      const uint64_t sym = f < nfi ? ((ent & FV_NB_BIT) ? 1 : 0) : bsym[f - nfi];
+      v |= sym << (4 * p);
+    }
+    code[cell] = v;
+  }
+  std::unordered_map<uint64_t, int> cls;
+  for (int cell = 0; cell < nc; ++cell) cls.emplace(code[cell], 0);
+  std::vector<uint64_t> keys;
+  keys.reserve(cls.size());
+  for (const auto& kv : cls) keys.push_back(kv.first);
+  std::sort(keys.begin(), keys.end());
+  for (size_t i = 0; i < keys.size(); ++i) cls[keys[i]] = (int)i;
+  std::vector<int> start(keys.size() + 1, 0), cid(nc);
+  for (int cell = 0; cell < nc; ++cell) {
+    cid[cell] = cls[code[cell]];
+    start[cid[cell] + 1]++;
+  }
+  for (size_t i = 0; i < keys.size(); ++i) start[i + 1] += start[i];
+  std::vector<int> order(nc);
+  for (int cell = 0; cell < nc; ++cell) order[start[cid[cell]]++] = cell;
+  if (!c->sched) FV_CUDA_TRY(cudaMalloc(&c->sched, sizeof(int) * nc));
+  FV_CUDA_TRY(cudaMemcpyAsync(c->sched, order.data(), sizeof(int) * nc, cudaMemcpyHostToDevice, s));
+  FV_CUDA_TRY(cudaStreamSynchronize(s));
+  c->n_cell_classes = (int)keys.size();
+  return FV_OK;
+}
 
 extern "C" int fv_case_create(const FvMesh* mesh, const FvCaseDesc* desc,
                               const signed char* flow_kind, const double* flow_vel,
@@ -246,6 +308,13 @@ extern "C" int fv_case_create(const FvMesh* mesh, const FvCaseDesc* desc,
     FV_CUDA_TRY(cudaMalloc(&c->phys, sizeof(double) * (size_t)c->nfld * m->nc));
     FV_CUDA_TRY(cudaMalloc(&c->tphys, sizeof(double) * (size_t)c->nfld * m->nc));
   }
+  rc = build_cell_order(c, flow_kind, desc->turbulent ? k_kind : nullptr,
+                        desc->turbulent ? omega_kind : nullptr, desc->turbulent ? sst_wall : nullptr,
+                        s);
+  if (rc != FV_OK) {
+    fv_case_destroy(c);
+    return rc;
+  }
   CaseView& v = c->view;
   v.log_w = (desc->scalar_transform & 2) != 0;
   v.rec_mom = desc->advection >= 1;
@@ -270,6 +339,7 @@ extern "C" int fv_case_create(const FvMesh* mesh, const FvCaseDesc* desc,
   v.inv_wd = c->inv_wd;
   v.inv_wd2 = c->inv_wd + m->nc;
   v.mu_cell = nullptr;
+  v.sched = c->sched;
   FV_CUDA_TRY(cudaStreamSynchronize(s));
   *out = c;
   return FV_OK;
@@ -297,6 +367,7 @@ extern "C" int fv_case_destroy(FvCase* c) {
   cudaFree(c->dscalar);
   cudaFree(c->jac_face);
   cudaFree(c->wnear);
+  cudaFree(c->sched);
   fv_node_adjoint_free(c);
   cudaFree(c->flx);
   cudaFree(c->mu_cell);
@@ -377,6 +448,16 @@ extern "C" int fv_case_autotune(FvCase* c, const double* state, const double* w,
   cudaEventDestroy(e1);
   c->tb = best_tb;
   if (best) *best = best_tb;
+  return FV_OK;
+}
+
+extern "C" int fv_case_set_cell_order(FvCase* c, int coherent, int* n_classes) {
+  if (!c) {
+    fv_set_error("fv_case_set_cell_order: bad arguments");
+    return FV_ERR_ARG;
+  }
+  c->view.sched = coherent ? c->sched : nullptr;
+  if (n_classes) *n_classes = c->n_cell_classes;
   return FV_OK;
 }
 

@@ -99,6 +99,7 @@ struct CaseView {
   float f_rho;
   int rec_mom, rec_sca;       // linear-upwind reconstruction of the momentum / the k, omega faces
   double lim_km, lim_ks;      // their Venkatakrishnan constants (0: unlimited, psi = 1)
+  const int* sched;           // (nc) the cell each thread of a cell stage evaluates, or null
 };
 
 // Workspace of the mesh-coordinate adjoint (residual.cu), allocated on its first use.
@@ -149,6 +150,8 @@ struct FvCase {
   int persistent = 0;           // residual + VJP as one cooperative launch (compact, upwind cases)
   int pchunk = 1;               // ... consecutive cells / faces per thread per stage
   int pblock = 128;             // ... threads per block
+  int* sched = nullptr;         // (nc) warp-coherent cell order of the cell stages
+  int n_cell_classes = 0;       // distinct face-list patterns it groups
   double* mu_cell = nullptr;    // (nc) per-cell viscosity field (laminar batched instances)
   double* flx = nullptr;        // (nfld, nf) weights of a face-flux functional (internal order)
   bool flx_active = false;      // the adjoints add flx to their face-flux cotangents

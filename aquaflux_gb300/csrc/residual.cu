@@ -49,6 +49,19 @@ template <>
 struct IsF32<DualF> : std::true_type {};
 template <class T>
 using GS = typename std::conditional<IsF32<T>::value, float, double>::type;
+// The cell a thread of a cell-centric stage evaluates.  With the case's warp-coherent order the
+// threads walk the cells grouped by the pattern of their face lists (owner / neighbour / boundary
+// kind at each position), so the 32 lanes of a warp take the same branches; without it, the
+// natural order.  A cell's arithmetic does not depend on which thread runs it, so both orders give
+// bitwise the same result.  The fp32 dual-number passes keep the natural order: they are not
+// bound by the floating-point issue rate that divergence wastes, and the indirection costs them.
+template <class T = double>
+__device__ __forceinline__ int stage_cell(const MeshView& m, const CaseView& cv) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if constexpr (IsF32<T>::value) return t;
+  else return (cv.sched != nullptr && t < m.nc) ? __ldg(cv.sched + t) : t;
+}
+
 template <class T>
 __device__ __forceinline__ GS<T> gx(const double* d, const float* f, long i) {
   if constexpr (IsF32<T>::value) return f[i];
@@ -456,10 +469,12 @@ __device__ __forceinline__ void k_grad_at(const int c, MeshView m, CaseView cv, 
     if (f < m.nfi) {
       const GS<T> g = gx<T>(m.g, m.f_g, f);
       const int other = isnb ? m.owner[f] : m.nb[f];
+      // owner value first: the operands are selected, not the interpolation (one code path for
+      // both sides of a face, no if-converted duplicate of the dual-number arithmetic)
 #pragma unroll
       for (int q = 0; q < NF; ++q) {
         const T po = st((long)q * nc + other);
-        phif[q] = isnb ? lerp(po, phic[q], g) : lerp(phic[q], po, g);
+        phif[q] = lerp(isnb ? po : phic[q], isnb ? phic[q] : po, g);
       }
     } else {
       const signed char kind = cv.fkind[f];
@@ -502,7 +517,7 @@ __device__ __forceinline__ void k_grad_at(const int c, MeshView m, CaseView cv, 
 template <class T, int DIM, bool TURB>
 __global__ void __launch_bounds__(128) k_grad(MeshView m, CaseView cv, Src<T> st, Par<T> par, T* G,
                                               T* Bg, double rel) {
-  k_grad_at<T, DIM, TURB>(blockIdx.x * blockDim.x + threadIdx.x, m, cv, st, par, G, Bg, rel);
+  k_grad_at<T, DIM, TURB>(stage_cell<T>(m, cv), m, cv, st, par, G, Bg, rel);
 }
 
 // ---------------------------------------------------------------- corrected Green-Gauss sweeps
@@ -698,7 +713,7 @@ __device__ __forceinline__ void k_closure_at(const int c, MeshView m, CaseView c
 template <class T, int DIM>
 __global__ void __launch_bounds__(128) k_closure(MeshView m, CaseView cv, Src<T> st, Par<T> par,
                                                  const T* G, T* cl, T* Gwi) {
-  k_closure_at<T, DIM>(blockIdx.x * blockDim.x + threadIdx.x, m, cv, st, par, G, cl, Gwi);
+  k_closure_at<T, DIM>(stage_cell<T>(m, cv), m, cv, st, par, G, cl, Gwi);
 }
 
 // effective dynamic viscosity mu + rho nu_t (aquaflux/flow/momentum.py:357-368)
@@ -1188,7 +1203,7 @@ __device__ __forceinline__ void k_sum_at(const int c, MeshView m, CaseView cv, S
 template <class T, int DIM, bool TURB>
 __global__ void __launch_bounds__(128) k_sum(MeshView m, CaseView cv, Src<T> st, Par<T> par, const T* FL, const T* cl,
                                              const T* G, const T* Gwi, double* R, double* JV) {
-  k_sum_at<T, DIM, TURB>(blockIdx.x * blockDim.x + threadIdx.x, m, cv, st, par, FL, cl, G, Gwi, R, JV);
+  k_sum_at<T, DIM, TURB>(stage_cell<T>(m, cv), m, cv, st, par, FL, cl, G, Gwi, R, JV);
 }
 
 // Zero the tangent of n dual values (the "frozen" JVP holds gradients, closure and a_P fixed).

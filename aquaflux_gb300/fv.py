@@ -287,6 +287,14 @@ class FlowCase:
     def set_block_size(self, threads: int) -> None:
         check(lib().fv_case_set_block_size(self._h, int(threads)))
 
+    def set_cell_order(self, coherent: bool = True) -> int:
+        """Thread-to-cell order of the cell-centric stages (``fv_case_set_cell_order``): grouped by
+        face-list pattern so that warps do not diverge (default), or natural.  Bitwise the same
+        results; returns the number of distinct patterns."""
+        n = ctypes.c_int(0)
+        check(lib().fv_case_set_cell_order(self._h, int(bool(coherent)), ctypes.byref(n)))
+        return n.value
+
     def functional_weights(self, spec: dict) -> torch.Tensor:
         """Weights of a face-flux functional: ``spec = {patch: {field: weight}}`` puts ``weight``
         on the ``field`` flux of every face of ``patch`` (fields: 0..dim-1 momentum, dim

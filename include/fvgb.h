@@ -140,6 +140,13 @@ int fv_case_set_block_size(FvCase* c, int threads);
  * times every (block in {64, 128}) x (chunk in {1, 2, 4, 8}) at state / w, keeps the fastest
  * (without enabling the path) and returns it with its time per evaluation. */
 int fv_case_set_persistent(FvCase* c, int enable, int block, int chunk);
+/* Order in which the threads of the cell-centric stages (gradients, closure, face sums and their
+ * adjoints) take the cells.  coherent != 0 (the default of fv_case_create): cells grouped by the
+ * pattern of their face lists -- owner / neighbour / boundary table entry at each position -- so
+ * that the lanes of a warp take the same branches; 0: the natural order.  Results are bitwise the
+ * same either way.  n_classes (optional) receives the number of distinct patterns.  No reference
+ * counterpart: an evaluation-order choice of this implementation. */
+int fv_case_set_cell_order(FvCase* c, int coherent, int* n_classes);
 int fv_case_autotune_persistent(FvCase* c, const double* state, const double* w, double* out,
                                 void* stream, int* best_block, int* best_chunk, float* best_ms);
 int fv_case_autotune(FvCase* c, const double* state, const double* w, double* out, void* stream,
