@@ -344,11 +344,13 @@ def newton_solve(case, state0, *, rtol: float = 1e-10, atol: float = 1e-12, max_
     (``kind="ilu"``) or by an ILU(0)-smoothed aggregation V-cycle (``kind="amg"``), in fp32 or
     fp64 (``precision``).
 
-    ``tangents=32`` evaluates the dual-number passes in fp32 arithmetic: the Krylov operator
-    ``J v`` (``fv_jvp_f32``) and the preconditioner's Jacobian assembly
-    (``fv_assemble_jacobian_f32``).  The residual, the Newton update, the line search and the
-    stopping test stay fp64, so the root is the fp64 root; only the linear solves, already
-    inexact at ``linear_rtol``, see fp32 rounding.  The FGMRES bases are allocated once per
+    ``precision=32`` builds the whole preconditioner in fp32: the frozen Jacobian it is formed
+    from is assembled by fp32 dual numbers (``fv_assemble_jacobian_f32``; the values are stored
+    in fp32 either way), then factored and applied in fp32.  ``tangents=32`` also evaluates the
+    Krylov operator ``J v`` in fp32 arithmetic (``fv_jvp_f32``).  The residual, the Newton
+    update, the Krylov orthogonalisation, the line search and the stopping test stay fp64, so the
+    root is the fp64 root; only the linear solves, already inexact at ``linear_rtol``, see fp32
+    rounding.  The FGMRES bases are allocated once per
     solve (:class:`KrylovWorkspace`).  ``refresh_trigger`` replaces the fixed ``refresh_every``
     schedule: the preconditioner is rebuilt at the first step and then only when the trigger fires
     on the step history since the last rebuild (see :func:`pseudo_transient_solve`)."""
@@ -358,7 +360,7 @@ def newton_solve(case, state0, *, rtol: float = 1e-10, atol: float = 1e-12, max_
     s = torch.as_tensor(state0, dtype=torch.float64, device="cuda").clone()
     if preconditioner is None:
         jac = BlockJacobian(case, reach=reach, frozen=frozen,
-                            precision=32 if (tangents == 32 and frozen and reach == 1) else 64)
+                            precision=32 if (precision == 32 and frozen and reach == 1) else 64)
         if kind == "amg":
             from .amg import AmgPreconditioner
 

@@ -58,6 +58,9 @@ def _args():
                     help="cells per axis of the ILU(0) CPU-vs-GPU sample (0: skip)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--step", default="vjp", choices=["vjp", "jvp"])
+    ap.add_argument("--cell-order", default="coherent", choices=["coherent", "natural"],
+                    help="thread-to-cell order of the cell stages (fv_case_set_cell_order): "
+                         "grouped by face-list pattern (default) or the mesh's natural order")
     ap.add_argument("--no-newton", action="store_true", help="skip the Newton-solve timing")
     ap.add_argument("--newton-kinds", default="amg,ilu",
                     help="preconditioners timed in the Newton block (comma list of amg (fine "
@@ -420,6 +423,7 @@ def run_gpu(args, rank: int, world: int, local_rank: int) -> dict | None:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
     wl = workloads.channel3d(args.size)
     case = wl.device_case()
+    n_cell_classes = case.set_cell_order(args.cell_order == "coherent")
     F = wl.mesh.n_faces
     state = torch.tensor(wl.initial_state(seed=rank, noise=0.05), device="cuda")
     vec = torch.tensor(np.random.default_rng(100 + rank).standard_normal(state.numel()),
@@ -561,6 +565,7 @@ def run_gpu(args, rank: int, world: int, local_rank: int) -> dict | None:
                    "step": STEP_DESC[args.step],
                    "cells": wl.mesh.n_cells, "faces": F,
                    "l2": "working set > 2 GB per step (inputs larger than the 129 MB L2)",
+                   "cell_order": f"{args.cell_order} ({n_cell_classes} face-list patterns)",
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": round(world * F * args.steps / (e2e_ms * 1e-3) / 1e9, 4), "unit": UNIT,
                 "h2d_bytes_per_step": 2 * state.numel() * 8,
@@ -627,8 +632,9 @@ def _field_errors(a, b, n_fields: int) -> dict:
 
 def newton_block(args, wl, case) -> dict:
     """Newton-solve seconds for each preconditioner kind (aggregation-AMG V-cycle, ILU(0)) in three
-    forms: fp64 throughout; an fp32 preconditioner; an fp32 preconditioner with the dual-number
-    passes (the Krylov operator J v and the preconditioner's Jacobian assembly) in fp32.
+    forms: fp64 throughout; an fp32 preconditioner (its frozen Jacobian assembled by fp32 dual
+    numbers, factored and applied in fp32) with the fp64 Krylov operator J v; the same with J v
+    in fp32 as well ("fp32 tangents").
 
     Every form: fp64 residual, fp64 FGMRES(30) with Krylov orthogonalisation, fp64 Newton update
     and line search, so every form converges to the fp64 root.  Each solve is timed whole, from
