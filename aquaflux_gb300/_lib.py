@@ -74,6 +74,7 @@ SIGNATURES = {
     "fv_bsr_spmv_f32": (c_int, [c_int, c_int, P, P, P, P, P, c_int, P]),
     "fv_bsr_spmv_t_f64_noalloc": (c_int, [c_int, c_long, c_int, P, P, P, P, P, P]),
     "fv_ilu0_create": (c_int, [c_int, c_int, P, P, c_int, P, P]),
+    "fv_ilu0_clone": (c_int, [P, c_int, P, P]),
     "fv_ilu0_destroy": (c_int, [P]),
     "fv_ilu0_factor": (c_int, [P, P, c_int, P]),
     "fv_ilu0_apply": (c_int, [P, P, P, c_int, P]),

@@ -30,18 +30,29 @@ def _stream() -> int:
 
 
 class _Level:
-    def __init__(self, n, b, indptr, indices, precision):
+    """One level's operator storage, smoother and work vectors.  ``kept``: the connectivity-only
+    part of this level (device pattern, a structure-only ILU(0) template) from an earlier
+    hierarchy on the same pattern, reused as is; an empty dict is filled for later ones."""
+
+    def __init__(self, n, b, indptr, indices, precision, kept: dict | None = None):
         self.n, self.b = n, b
         self.sfx = "f32" if precision == 32 else "f64"
         dtype = torch.float32 if precision == 32 else torch.float64
         self.indptr = np.ascontiguousarray(indptr, dtype=np.int32)
         self.indices = np.ascontiguousarray(indices, dtype=np.int32)
         self.nnzb = int(self.indptr[-1])
-        self.d_indptr = torch.tensor(self.indptr, device="cuda")
-        self.d_indices = torch.tensor(self.indices, device="cuda")
+        if kept:
+            self.d_indptr, self.d_indices = kept["d_indptr"], kept["d_indices"]
+            self.ilu = kept["ilu"].clone(precision)
+        else:
+            self.d_indptr = torch.tensor(self.indptr, device="cuda")
+            self.d_indices = torch.tensor(self.indices, device="cuda")
+            self.ilu = Ilu0.__new__(Ilu0)
+            self.ilu._setup(self.indptr, self.indices, b, precision)
+            if kept is not None:
+                kept.update(d_indptr=self.d_indptr, d_indices=self.d_indices,
+                            ilu=self.ilu.clone(0))
         self.values = torch.zeros(self.nnzb * b * b, dtype=dtype, device="cuda")
-        self.ilu = Ilu0.__new__(Ilu0)
-        self.ilu._setup(self.indptr, self.indices, b, precision)
         self.x = torch.zeros(n * b, dtype=dtype, device="cuda")
         self.r = torch.zeros_like(self.x)
         self.t = torch.zeros_like(self.x)
@@ -141,7 +152,8 @@ class AmgHierarchy:
 
     def __init__(self, n, b, indptr, indices, *, min_cells: int = 4000, max_levels: int = 10,
                  sweeps: int = 1, coarse_sweeps: int = 4, coarse_order: str = "colour",
-                 precision: int = 32, coarse_solve: str = "ilu", dense_max: int = 4096):
+                 precision: int = 32, coarse_solve: str = "ilu", dense_max: int = 4096,
+                 plan=None, kept: dict | None = None):
         if precision not in (32, 64):
             raise ValueError(f"precision must be 32 or 64, got {precision}")
         if coarse_solve not in ("auto", "dense", "ilu"):
@@ -149,18 +161,33 @@ class AmgHierarchy:
         self.b, self.sweeps, self.coarse_sweeps = b, sweeps, coarse_sweeps
         self.precision = precision
         self.sfx = "f32" if precision == 32 else "f64"
-        with ThreadPoolExecutor(1) as pool:
-            plan = pool.submit(plan_hierarchy, n, indptr, indices, min_cells=min_cells,
-                               max_levels=max_levels, coarse_order=coarse_order)
-            self.levels = [_Level(n, b, indptr, indices, precision)]
-            plan = plan.result()
-        for step in plan:
+        # kept["levels"][l]: level l's connectivity-only device structures, shared by every
+        # hierarchy on this pattern (filled by the first)
+        klv = None if kept is None else kept.setdefault("levels", [])
+        kl = (lambda i: None if klv is None else
+              (klv[i] if i < len(klv) else klv.append({}) or klv[i]))
+        if plan is None:
+            with ThreadPoolExecutor(1) as pool:
+                plan = pool.submit(plan_hierarchy, n, indptr, indices, min_cells=min_cells,
+                                   max_levels=max_levels, coarse_order=coarse_order)
+                self.levels = [_Level(n, b, indptr, indices, precision, kl(0))]
+                plan = plan.result()
+        else:  # a given plan (a list, or the future of one still being made)
+            self.levels = [_Level(n, b, indptr, indices, precision, kl(0))]
+            plan = plan.result() if hasattr(plan, "result") else plan
+        for i, step in enumerate(plan):
             fine = self.levels[-1]
-            fine.coarse = {k: torch.tensor(step[k], device="cuda")
-                           for k in ("agg", "mptr", "mlist", "gptr", "glist")}
-            fine.coarse["n_coarse_blocks"] = int(step["gptr"].size - 1)
+            kf = kl(i)
+            if kf is not None and "coarse" in kf:
+                fine.coarse = dict(kf["coarse"])
+            else:
+                fine.coarse = {k: torch.tensor(step[k], device="cuda")
+                               for k in ("agg", "mptr", "mlist", "gptr", "glist")}
+                fine.coarse["n_coarse_blocks"] = int(step["gptr"].size - 1)
+                if kf is not None:
+                    kf["coarse"] = dict(fine.coarse)
             self.levels.append(_Level(step["n_coarse"], b, step["indptr"], step["indices"],
-                                      precision))
+                                      precision, kl(i + 1)))
         last = self.levels[-1]
         nd = last.n * b
         self.dense = None
@@ -286,19 +313,28 @@ class AmgPreconditioner:
         if fine_order == "auto":
             fine_order = "colour" if jac.case.dim == 3 else "natural"
         self.fine_order = fine_order
+        # connectivity-only products, built once per case (FlowCase.pattern_plan)
+        cache = getattr(jac.case, "pattern_plan", None)
+        plan_key = tuple(sorted((k, kw[k]) for k in ("min_cells", "max_levels", "coarse_order")
+                                if k in kw))
+        cached = (lambda key, build: cache((key, jac.reach) + plan_key, build)
+                  ) if cache is not None else (lambda key, build: build())
         if fine_order == "colour":
-            col = np.empty(n, dtype=np.int32)
-            nco = ctypes.c_int(0)
-            check(lib().fv_greedy_colouring(n, ptr(indptr), ptr(indices), ptr(col),
-                                            ctypes.byref(nco)))
-            perm = np.concatenate([np.flatnonzero(col == c)
-                                   for c in range(nco.value)]).astype(np.int32)
-            pip = np.empty(n + 1, dtype=np.int32)
-            pix = np.empty(int(indptr[-1]), dtype=np.int32)
-            bmap = np.empty(int(indptr[-1]), dtype=np.int64)
-            check(lib().fv_permute_pattern(n, ptr(indptr), ptr(indices), ptr(perm), ptr(pip),
-                                           ptr(pix), ptr(bmap)))
-            self.n_colours = int(nco.value)
+            def colour_order():
+                col = np.empty(n, dtype=np.int32)
+                nco = ctypes.c_int(0)
+                check(lib().fv_greedy_colouring(n, ptr(indptr), ptr(indices), ptr(col),
+                                                ctypes.byref(nco)))
+                perm = np.concatenate([np.flatnonzero(col == c)
+                                       for c in range(nco.value)]).astype(np.int32)
+                pip = np.empty(n + 1, dtype=np.int32)
+                pix = np.empty(int(indptr[-1]), dtype=np.int32)
+                bmap = np.empty(int(indptr[-1]), dtype=np.int64)
+                check(lib().fv_permute_pattern(n, ptr(indptr), ptr(indices), ptr(perm),
+                                               ptr(pip), ptr(pix), ptr(bmap)))
+                return perm, pip, pix, bmap, int(nco.value)
+
+            perm, pip, pix, bmap, self.n_colours = cached("amg_fine_colour_order", colour_order)
             self._perm = torch.tensor(perm, device="cuda")
             self._bmap = torch.tensor(bmap, device="cuda")
             indptr, indices = pip, pix
@@ -309,7 +345,21 @@ class AmgPreconditioner:
                                                                 device="cuda")
         self.op = (ShiftedCellMajorOperator(jac, equilibrate=equilibrate, precision=64)
                    if (shift is not None or equilibrate) else None)
-        self.h = AmgHierarchy(n, b, indptr, indices, precision=precision, **kw)
+        # the aggregation plan runs on a worker thread (overlapping the fine level's ILU(0)
+        # structures on first use); later preconditioners on this case reuse it
+        plan_kw = {k: kw[k] for k in ("min_cells", "max_levels", "coarse_order") if k in kw}
+
+        def hierarchy_plan():
+            pool = ThreadPoolExecutor(1)
+            fut = pool.submit(plan_hierarchy, n, indptr, indices, **plan_kw)
+            pool.shutdown(wait=False)
+            return fut
+
+        plan = cached("amg_hierarchy_plan_" + fine_order, hierarchy_plan)
+        kept = (cached("amg_hierarchy_structures_" + fine_order, dict) if cache is not None
+                else None)
+        self.h = AmgHierarchy(n, b, indptr, indices, precision=precision, plan=plan, kept=kept,
+                              **kw)
         self._f64 = int(precision == 64)
         self._b = torch.empty(n * b, dtype=self.h.levels[0].x.dtype, device="cuda")
         self.graph = bool(graph)
@@ -358,9 +408,20 @@ class AmgPreconditioner:
             if self._eager_key != key:
                 self._eager_key = key
                 return self.h.vcycle(0, self._b)
+            # captured on a side stream through capture_begin / capture_end: the torch.cuda.graph
+            # context manager would empty the caching allocator at every capture, and the next
+            # solve would then re-allocate its multi-GB bases and levels from the driver
             g = torch.cuda.CUDAGraph()
-            with torch.cuda.graph(g):
-                self.h.vcycle(0, self._b)
+            main = torch.cuda.current_stream()
+            side = torch.cuda.Stream()
+            side.wait_stream(main)
+            with torch.cuda.stream(side):
+                g.capture_begin()
+                try:
+                    self.h.vcycle(0, self._b)
+                finally:
+                    g.capture_end()
+            main.wait_stream(side)
             self._graph, self._graph_key = g, key
         self._graph.replay()
         return self.h.levels[0].x

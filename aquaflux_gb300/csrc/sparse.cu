@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <type_traits>
+#include <memory>
 #include <vector>
 
 #include "internal.cuh"
@@ -642,8 +643,9 @@ struct FvIlu0 {
   void* work = nullptr;                      // (n * b) vector the captured sweeps run on
   cudaGraphExec_t apply_exec[2] = {nullptr, nullptr};  // forward / transposed solve
   cudaGraphExec_t factor_exec = nullptr;
-  // host copy of the pattern: the transposed-solve structures are built on first use
-  std::vector<int> h_ptr, h_idx, h_diag;
+  // host copy of the pattern (shared by clones): the transposed-solve structures are built on
+  // first use
+  std::shared_ptr<const std::vector<int>> h_ptr, h_idx, h_diag;
 };
 
 namespace {
@@ -796,7 +798,7 @@ int ensure_transpose(FvIlu0* f, cudaStream_t s) {
   if (f->tptr) return FV_OK;
   const int n = f->n;
   Transpose T;
-  build_transpose(n, n, f->h_ptr.data(), f->h_idx.data(), &T);
+  build_transpose(n, n, f->h_ptr->data(), f->h_idx->data(), &T);
   std::vector<int> rows;
   levels(n, true, [&](int i, auto&& use) {  // U^T: column i depends on rows j < i with (j, i)
     for (int q = T.ptr[i]; q < T.ptr[i + 1]; ++q)
@@ -908,10 +910,10 @@ extern "C" int fv_ilu0_create(int n, int b, const int* indptr, const int* indice
     for (int q = diag[i] + 1; q < indptr[i + 1]; ++q) use(indices[q]);
   }, &rows, &f->lv_bwd);
   if (upload(rows, &f->rows_bwd, s)) return FV_ERR_CUDA;
-  f->h_ptr.assign(indptr, indptr + n + 1);
-  f->h_idx.assign(indices, indices + nnzb);
-  f->h_diag = diag;
-  if (upload(f->h_ptr, &f->ptr, s) || upload(f->h_idx, &f->idx, s) || upload(diag, &f->diag, s))
+  f->h_ptr = std::make_shared<const std::vector<int>>(indptr, indptr + n + 1);
+  f->h_idx = std::make_shared<const std::vector<int>>(indices, indices + nnzb);
+  f->h_diag = std::make_shared<const std::vector<int>>(diag);
+  if (upload(*f->h_ptr, &f->ptr, s) || upload(*f->h_idx, &f->idx, s) || upload(diag, &f->diag, s))
     return FV_ERR_CUDA;
   size_t vs = precision == 64 ? sizeof(double) : sizeof(float);
   FV_CUDA_TRY(cudaMalloc(&f->val, vs * (size_t)nnzb * b * b));
@@ -944,8 +946,67 @@ extern "C" int fv_ilu0_destroy(FvIlu0* f) {
   return FV_OK;
 }
 
+namespace {
+// Device copy of n ints (nothing when the source is absent).
+int copy_ints(const int* src, size_t n, int** dst, cudaStream_t s) {
+  if (!src) return FV_OK;
+  FV_CUDA_TRY(cudaMalloc(dst, sizeof(int) * std::max<size_t>(1, n)));
+  FV_CUDA_TRY(cudaMemcpyAsync(*dst, src, sizeof(int) * n, cudaMemcpyDeviceToDevice, s));
+  return FV_OK;
+}
+}  // namespace
+
+extern "C" int fv_ilu0_clone(const FvIlu0* src, int precision, void* stream, FvIlu0** out) {
+  if (!src || !out || (precision != 0 && precision != 32 && precision != 64)) {
+    fv_set_error("fv_ilu0_clone: bad arguments (precision 0, 32 or 64)");
+    return FV_ERR_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  FvIlu0* f = new FvIlu0();
+  f->n = src->n;
+  f->b = src->b;
+  f->nnzb = src->nnzb;
+  f->precision = precision;
+  f->lv_fwd = src->lv_fwd;
+  f->lv_bwd = src->lv_bwd;
+  f->lv_tfwd = src->lv_tfwd;
+  f->lv_tbwd = src->lv_tbwd;
+  f->h_ptr = src->h_ptr;
+  f->h_idx = src->h_idx;
+  f->h_diag = src->h_diag;
+  const size_t n = src->n, nnzb = src->nnzb;
+  int rc = FV_OK;
+  rc |= copy_ints(src->ptr, n + 1, &f->ptr, s);
+  rc |= copy_ints(src->idx, nnzb, &f->idx, s);
+  rc |= copy_ints(src->diag, n, &f->diag, s);
+  rc |= copy_ints(src->rows_fwd, n, &f->rows_fwd, s);
+  rc |= copy_ints(src->rows_bwd, n, &f->rows_bwd, s);
+  if (src->tptr) {
+    rc |= copy_ints(src->tptr, n + 1, &f->tptr, s);
+    rc |= copy_ints(src->tidx, nnzb, &f->tidx, s);
+    rc |= copy_ints(src->tblk, nnzb, &f->tblk, s);
+    rc |= copy_ints(src->rows_tfwd, n, &f->rows_tfwd, s);
+    rc |= copy_ints(src->rows_tbwd, n, &f->rows_tbwd, s);
+  }
+  if (rc == FV_OK && precision != 0) {
+    const size_t vs = precision == 64 ? sizeof(double) : sizeof(float);
+    if (cudaMalloc(&f->val, vs * nnzb * f->b * f->b) != cudaSuccess ||
+        cudaMalloc(&f->zero_flag, sizeof(unsigned long long)) != cudaSuccess ||
+        cudaMalloc(&f->work, vs * n * f->b) != cudaSuccess)
+      rc = FV_ERR_CUDA;
+  }
+  if (rc == FV_OK && cudaStreamSynchronize(s) != cudaSuccess) rc = FV_ERR_CUDA;
+  if (rc != FV_OK) {
+    fv_set_error("fv_ilu0_clone: device allocation or copy failed");
+    fv_ilu0_destroy(f);
+    return FV_ERR_CUDA;
+  }
+  *out = f;
+  return FV_OK;
+}
+
 extern "C" int fv_ilu0_factor(FvIlu0* f, const void* values, int values_f64, void* stream) {
-  if (!f || !values) {
+  if (!f || !values || !f->val) {
     fv_set_error("fv_ilu0_factor: bad arguments");
     return FV_ERR_ARG;
   }
@@ -963,7 +1024,7 @@ extern "C" int fv_ilu0_factor(FvIlu0* f, const void* values, int values_f64, voi
 }
 
 extern "C" int fv_ilu0_apply(FvIlu0* f, const void* r, void* x, int transpose, void* stream) {
-  if (!f || !r || !x) {
+  if (!f || !r || !x || !f->val) {
     fv_set_error("fv_ilu0_apply: bad arguments");
     return FV_ERR_ARG;
   }
@@ -973,7 +1034,7 @@ extern "C" int fv_ilu0_apply(FvIlu0* f, const void* r, void* x, int transpose, v
 }
 
 extern "C" int fv_ilu0_factor_values(const FvIlu0* f, void* out, void* stream) {
-  if (!f || !out) {
+  if (!f || !out || !f->val) {
     fv_set_error("fv_ilu0_factor_values: bad arguments");
     return FV_ERR_ARG;
   }

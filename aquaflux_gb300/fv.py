@@ -375,6 +375,18 @@ class FlowCase:
         check(lib().fv_case_profile_end(self._h, ms, len(self.STAGES), ctypes.byref(n)))
         return {k: float(ms[i]) for i, k in enumerate(self.STAGES)}, int(n.value)
 
+    def pattern_plan(self, key, build):
+        """A product of the mesh's connectivity alone -- a Jacobian sparsity pattern, a colouring
+        order, an aggregation hierarchy's host plan -- built by ``build()`` on first use and kept
+        for every later solve on this case, as the mesh geometry is (moving the nodes keeps it).
+        The reference hoists the same pattern-dependent structures out of its refreshes and
+        solves (``aquaflux/solve/amg_preconditioner.py:740-760``: the probe ``plan`` and gather
+        ``structure``, built once)."""
+        plans = self.__dict__.setdefault("_pattern_plans", {})
+        if key not in plans:
+            plans[key] = build()
+        return plans[key]
+
     def set_nodes(self, nodes: torch.Tensor) -> None:
         """Move the mesh nodes: recompute the geometry and (turbulent case) the SST wall
         distance to each cell's nearest wall face, that face held fixed."""

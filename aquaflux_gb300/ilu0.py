@@ -78,6 +78,22 @@ class Ilu0:
             _raise(e)
         self._h = h
 
+    def clone(self, precision: int | None = None) -> "Ilu0":
+        """A factor object on the same pattern, without analysing it again (``fv_ilu0_clone``):
+        ``precision`` 32 / 64 (default: this one's) gives a factor ready for :meth:`refactor`;
+        0 a structure-only template to clone later factors from."""
+        prec = self._precision if precision is None else int(precision)
+        obj = Ilu0.__new__(Ilu0)
+        obj._indptr, obj._indices = self._indptr, self._indices
+        obj._n, obj._b = self._n, self._b
+        obj._precision = prec
+        obj._dtype = torch.float64 if prec == 64 else torch.float32
+        obj._nvals = self._nvals
+        h = ctypes.c_void_p()
+        check(lib().fv_ilu0_clone(self._h, prec, _stream(), ctypes.byref(h)))
+        obj._h = h
+        return obj
+
     @property
     def nnz(self) -> int:
         return self._nvals

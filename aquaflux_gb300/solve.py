@@ -59,13 +59,17 @@ class BlockJacobian:
         interior = mesh.neighbour >= 0
         self._own, self._nb = mesh.owner[interior], mesh.neighbour[interior]
         self.reach = reach
-        if reach == 1:
-            self.indptr, self.indices = cell_pattern(self._own, self._nb, self.n)
-        else:
+        def pattern():
+            if reach == 1:
+                return cell_pattern(self._own, self._nb, self.n)
             pat = stencil_pattern(self._own, self._nb, self.n, reach).tocsr()
             pat.sort_indices()
-            self.indptr = np.ascontiguousarray(pat.indptr, dtype=np.int32)
-            self.indices = np.ascontiguousarray(pat.indices, dtype=np.int32)
+            return (np.ascontiguousarray(pat.indptr, dtype=np.int32),
+                    np.ascontiguousarray(pat.indices, dtype=np.int32))
+
+        plan = getattr(case, "pattern_plan", None)
+        self.indptr, self.indices = (plan(("jacobian_pattern", reach), pattern) if plan
+                                     else pattern())
         self.nnzb = int(self.indptr[-1])
         self.frozen = frozen
         if method is None:

@@ -309,6 +309,12 @@ typedef struct FvIlu0 FvIlu0;
 int fv_ilu0_create(int n_block_rows, int b, const int* indptr, const int* indices, int precision,
                    void* stream, FvIlu0** out);
 int fv_ilu0_destroy(FvIlu0* f);
+/* A factor object on the same pattern as `src` without analysing it again: the level sets and
+ * device pattern are copied on the device, the host pattern is shared.  precision 32 or 64 gives
+ * a factor ready for fv_ilu0_factor; precision 0 a structure-only template (it cannot factor or
+ * solve) to clone later factors from.  No reference counterpart: the reference re-analyses the
+ * pattern of every ILU(0) it builds (aquaflux/solve/_ilu0.pyx:35-65). */
+int fv_ilu0_clone(const FvIlu0* src, int precision, void* stream, FvIlu0** out);
 /* Numeric factorization of new values (device, nnzb * b * b, same dtype as `precision`, or
  * float64 when values_f64 != 0 and precision == 32: converted on the fly). */
 int fv_ilu0_factor(FvIlu0* f, const void* values, int values_f64, void* stream);

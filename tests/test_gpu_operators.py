@@ -184,3 +184,27 @@ def test_batched_jvp_equals_single_jvps():
     out = case.jvp_batch(s, vs)
     for i in range(3):
         assert torch.equal(out[i], case.jvp(s, vs[i]))
+
+
+@pytest.mark.parametrize("precision", [32, 64])
+def test_preconditioners_on_one_case_share_its_kept_plan(precision):
+    """The second AMG preconditioner on a case reuses the case's connectivity-only plan and level
+    structures (FlowCase.pattern_plan, ILU(0) clones) and applies bitwise what the first does, in
+    both precisions and through the transpose."""
+    from aquaflux_gb300.amg import AmgPreconditioner
+    from aquaflux_gb300.solve import BlockJacobian
+
+    wl, case, p1, s = _cavity_pc("amg", precision)
+    plans = dict(case._pattern_plans)
+    p2 = AmgPreconditioner(BlockJacobian(case), precision, min_cells=150)
+    assert case._pattern_plans.keys() == plans.keys()
+    kept = [v for k, v in plans.items() if k[0].startswith("amg_hierarchy_structures")]
+    assert kept and len(kept[0]["levels"]) == len(p1.h.levels) > 1
+    assert p2.h.levels[0].d_indices is p1.h.levels[0].d_indices
+    for p in (p1, p2):
+        p.refresh(s)
+    g = torch.Generator(device="cuda").manual_seed(2)
+    r = torch.randn(case.n_unknowns, dtype=torch.float64, device="cuda", generator=g)
+    for _ in range(2):  # eager, then the graph replay
+        assert torch.equal(p1.apply(r), p2.apply(r))
+    assert torch.equal(p1.apply_transpose(r), p2.apply_transpose(r))

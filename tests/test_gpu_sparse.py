@@ -182,3 +182,31 @@ def test_block_ilu0_fp64_bitwise_equals_the_reference_kernel_on_a_channel_jacobi
     _, _, gfac = to_scalar(jac.indptr, jac.indices, f.factor_values().cpu().numpy(), b)
     np.testing.assert_array_equal(gfac, data)
     np.testing.assert_array_equal(f.solve(rhs, transpose=True).cpu().numpy(), xt)
+
+
+@pytest.mark.parametrize("precision", [32, 64])
+def test_cloned_ilu0_equals_a_fresh_factor_bitwise(precision):
+    """fv_ilu0_clone: a factor on the same pattern without re-analysis -- from a factor or from a
+    structure-only template, after the source's transposed structures exist or before -- gives
+    bitwise the fresh factor's values, solves and transposed solves; a template refuses to factor
+    or solve."""
+    from aquaflux_gb300._lib import FvError
+    from aquaflux_gb300.ilu0 import Ilu0
+
+    d = golden("ilu0")
+    ip, ix, vals = cell_major(d["ilu_indptr"], d["ilu_indices"], d["ilu_values"], 40, 3)
+    bp, bi, bv = to_bsr(ip, ix, vals, 3)
+    rhs = d["ilu_rhs"]
+    fresh = Ilu0.from_csr(bp, bi, bv, block_size=3, precision=precision)
+    template = fresh.clone(0)
+    fresh.solve(rhs, transpose=True)  # the source now holds the transposed structures too
+    for src in (fresh, template):
+        c = src.clone(precision)
+        c.refactor(bv)
+        assert torch.equal(c.factor_values(), fresh.factor_values())
+        assert torch.equal(c.solve(rhs), fresh.solve(rhs))
+        assert torch.equal(c.solve(rhs, transpose=True), fresh.solve(rhs, transpose=True))
+    with pytest.raises(FvError):
+        template.refactor(bv)
+    with pytest.raises(FvError):
+        template.solve(rhs)
