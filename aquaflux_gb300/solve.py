@@ -435,6 +435,70 @@ def newton_solve(case, state0, *, rtol: float = 1e-10, atol: float = 1e-12, max_
                         refreshes)
 
 
+def reynolds_scales(n_points: int, ratio: float = 10.0) -> tuple[float, ...]:
+    """The molecular-viscosity factors of a Reynolds continuation, ``(ratio ** N, ..., ratio,
+    1.0)`` for ``N = n_points`` (``GeometricReynoldsSchedule.scales``,
+    ``aquaflux/turbulence/reynolds.py:96-132``): one decade of Reynolds number per point by
+    default, ending at the target."""
+    if n_points < 0:
+        raise ValueError(f"n_points must be >= 0, got {n_points}")
+    return tuple(float(ratio ** (n_points - i)) for i in range(n_points + 1))
+
+
+@dataclasses.dataclass
+class ReynoldsContinuationResult:
+    state: torch.Tensor      # the target-Reynolds root
+    converged: bool          # the target solve's convergence
+    points: list             # per point: viscosity scale, Newton steps, Krylov iterations, seconds
+    seconds: float
+
+
+def reynolds_continuation(case, state0, n_points: int, *, ratio: float = 10.0,
+                          intermediate_rtol: float | None = 1e-2,
+                          intermediate_atol: float | None = None,
+                          **newton_kwargs) -> ReynoldsContinuationResult:
+    """Newton's method by Reynolds-number continuation (``solve_reynolds_continuation``,
+    ``aquaflux/turbulence/reynolds.py:144-338``): ``n_points`` lower-Reynolds solves, the case's
+    molecular viscosity scaled by :func:`reynolds_scales`, each seeded by the previous converged
+    state and converged loosely (``intermediate_rtol`` / ``intermediate_atol`` replace ``rtol`` /
+    ``atol`` there), then the solve at the case's own viscosity with the caller's tolerances.  The
+    path changes, the root does not.  A lower point that fails raises ``RuntimeError`` naming it;
+    the case's viscosity is restored in every outcome."""
+    scales = reynolds_scales(n_points, ratio)
+    mu0 = case.mu
+    t0 = time.perf_counter()
+    seed = state0
+    points = []
+    ramp = dict(newton_kwargs)
+    if intermediate_rtol is not None:
+        ramp["rtol"] = intermediate_rtol
+    if intermediate_atol is not None:
+        ramp["atol"] = intermediate_atol
+    try:
+        for i, scale in enumerate(scales[:-1]):
+            case.set_params(mu=mu0 * scale)
+            res = newton_solve(case, seed, **ramp)
+            points.append({"viscosity_scale": scale, "converged": bool(res.converged),
+                           "newton_steps": res.steps,
+                           "krylov_iterations": int(sum(res.krylov_iterations)),
+                           "seconds": round(res.seconds, 3)})
+            if not res.converged:
+                raise RuntimeError(
+                    f"Reynolds-continuation point {i + 1} of {n_points} (molecular viscosity "
+                    f"scaled by {scale:g}, i.e. Reynolds number reduced by {scale:g}x) failed to "
+                    f"converge. Increase n_points for a gentler ramp, or check the case at this "
+                    f"Reynolds number directly.")
+            seed = res.state
+    finally:
+        case.set_params(mu=mu0)
+    res = newton_solve(case, seed, **newton_kwargs)
+    points.append({"viscosity_scale": 1.0, "converged": bool(res.converged),
+                   "newton_steps": res.steps, "krylov_iterations": int(sum(res.krylov_iterations)),
+                   "seconds": round(res.seconds, 3)})
+    return ReynoldsContinuationResult(res.state, bool(res.converged), points,
+                                      time.perf_counter() - t0)
+
+
 class TransposedPreconditioner:
     """``M^T`` of a preconditioner with an exact transposed application (``apply_transpose``: the
     transposed ILU(0) solve, or the transposed V-cycle), as the reference's

@@ -147,3 +147,28 @@ def test_eddy_viscosity_drift_is_zero_at_its_reference():
     s1 = s0.clone()
     s1[4 * case.n_cells:5 * case.n_cells] *= 1.5  # k up by half: nu_t moves
     assert drift(s1) > 0.05
+
+
+def test_reynolds_continuation_reaches_the_direct_root_and_restores_the_viscosity():
+    """solve_reynolds_continuation (aquaflux/turbulence/reynolds.py:144-338): the lower-Reynolds
+    points change the path, not the root; a point that fails raises and the case keeps its own
+    viscosity either way."""
+    from aquaflux_gb300 import workloads
+    from aquaflux_gb300.solve import newton_solve, reynolds_continuation
+
+    wl = workloads.channel3d(8, renumber=False)
+    case = wl.device_case()
+    mu0 = case.mu
+    direct = newton_solve(case, wl.initial_state(), precision=64, rtol=1e-13, atol=0.0)
+    cont = reynolds_continuation(case, wl.initial_state(), 1, precision=64, rtol=1e-13,
+                                 atol=0.0)
+    assert direct.converged and cont.converged
+    assert case.mu == mu0
+    assert [p["viscosity_scale"] for p in cont.points] == [10.0, 1.0]
+    assert all(p["converged"] for p in cont.points)
+    diff = (cont.state - direct.state).abs().max() / direct.state.abs().max()
+    assert float(diff) <= 1e-8
+    with pytest.raises(RuntimeError, match="point 1 of 2"):
+        reynolds_continuation(case, wl.initial_state(), 2, precision=64, max_steps=1,
+                              intermediate_rtol=1e-14)
+    assert case.mu == mu0

@@ -1,4 +1,5 @@
 """Host-side pieces of the forward march that need no GPU."""
+import pytest
 import torch
 
 from aquaflux_gb300.solve import positive_projection
@@ -20,3 +21,15 @@ def test_positive_projection_clips_only_decreasing_entries():
     assert torch.isclose(floored[2], torch.tensor(-0.9 * (1e-3 + 1.0), dtype=torch.float64))
     zero = positive_projection(phi, torch.zeros(5, dtype=torch.float64), 0, 5)
     assert bool((zero == 0).all())
+
+
+def test_reynolds_scales_are_geometric_and_end_at_the_target():
+    """GeometricReynoldsSchedule.scales (aquaflux/turbulence/reynolds.py:96-132)."""
+    from aquaflux_gb300.solve import reynolds_scales
+
+    assert reynolds_scales(0) == (1.0,)
+    assert reynolds_scales(1) == (10.0, 1.0)
+    assert reynolds_scales(2) == (100.0, 10.0, 1.0)
+    assert reynolds_scales(2, ratio=3.0) == (9.0, 3.0, 1.0)
+    with pytest.raises(ValueError):
+        reynolds_scales(-1)
