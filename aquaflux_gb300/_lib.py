@@ -62,6 +62,7 @@ SIGNATURES = {
     "fv_case_set_cell_order": (c_int, [P, c_int, P]),
     "fv_case_autotune_persistent": (c_int, [P, P, P, P, P, P, P, P]),
     "fv_case_autotune": (c_int, [P, P, P, P, P, P]),
+    "fv_case_block_sizes": (c_int, [P, P, c_int]),
     "fv_segment_dot": (c_int, [c_int, P, c_int, c_int, P, P, P, P]),
     "fv_face_functional": (c_int, [P, P, P, c_int, P, P, P, P, P]),
     "fv_assemble_jacobian": (c_int, [P, P, P, P, P, P]),

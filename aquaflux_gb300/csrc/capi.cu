@@ -418,36 +418,63 @@ extern "C" int fv_case_autotune(FvCase* c, const double* state, const double* w,
     fv_set_error("fv_case_autotune: bad arguments");
     return FV_ERR_ARG;
   }
+  if (c->prof_max_runs) {
+    fv_set_error("fv_case_autotune: a stage profile (fv_case_profile_begin) is open");
+    return FV_ERR_ARG;
+  }
   cudaStream_t s = (cudaStream_t)stream;
   state = physical_state(c, state, s);
+  // every stage at each candidate, timed stage by stage through the profiling marks; each stage
+  // keeps its own fastest (the uniform fastest is returned)
   const int cand[4] = {32, 64, 96, 128};
-  cudaEvent_t e0, e1;
-  FV_CUDA_TRY(cudaEventCreate(&e0));
-  FV_CUDA_TRY(cudaEventCreate(&e1));
-  float best_ms = 1e30f;
-  int best_tb = c->tb;
-  for (int k = 0; k < 4; ++k) {
+  const int persistent = c->persistent;
+  c->persistent = 0;
+  float best_total = 1e30f, stage_best[FV_MAX_STAGES];
+  int best_tb = c->tb, stage_tb[FV_MAX_STAGES];
+  for (int j = 0; j < FV_MAX_STAGES; ++j) {
+    stage_best[j] = 1e30f;
+    stage_tb[j] = c->tbs[j];
+  }
+  int rc = FV_OK;
+  for (int k = 0; k < 4 && rc == FV_OK; ++k) {
     c->tb = cand[k];
-    int rc = fv_case_vjp_run(c, state, w, nullptr, out, s);  // warm-up
-    if (rc != FV_OK) return rc;
-    cudaEventRecord(e0, s);
-    for (int r = 0; r < 3; ++r) {
-      rc = fv_case_vjp_run(c, state, w, nullptr, out, s);
-      if (rc != FV_OK) return rc;
+    for (int j = 0; j < FV_MAX_STAGES; ++j) c->tbs[j] = cand[k];
+    rc = fv_case_vjp_run(c, state, w, nullptr, out, s);  // warm-up
+    if (rc != FV_OK) break;
+    rc = fv_case_profile_begin(c, 3);
+    for (int r = 0; r < 3 && rc == FV_OK; ++r) rc = fv_case_vjp_run(c, state, w, nullptr, out, s);
+    float ms[FV_MAX_STAGES];
+    int runs = 0;
+    const int rc2 = fv_case_profile_end(c, ms, FV_MAX_STAGES, &runs);
+    if (rc == FV_OK) rc = rc2;
+    if (rc != FV_OK) break;
+    float total = 0.0f;
+    for (int j = 0; j < FV_MAX_STAGES; ++j) {
+      total += ms[j];
+      if (ms[j] < stage_best[j]) {
+        stage_best[j] = ms[j];
+        stage_tb[j] = cand[k];
+      }
     }
-    cudaEventRecord(e1, s);
-    FV_CUDA_TRY(cudaEventSynchronize(e1));
-    float ms = 0.0f;
-    cudaEventElapsedTime(&ms, e0, e1);
-    if (ms < best_ms) {
-      best_ms = ms;
+    if (total < best_total) {
+      best_total = total;
       best_tb = cand[k];
     }
   }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
+  c->persistent = persistent;
   c->tb = best_tb;
+  for (int j = 0; j < FV_MAX_STAGES; ++j) c->tbs[j] = stage_tb[j];
+  if (rc != FV_OK) return rc;
   if (best) *best = best_tb;
+  return FV_OK;
+}
+
+extern "C" int fv_case_block_sizes(const FvCase* c, int* threads, int n) {
+  if (!c || !threads || n <= 0) {
+    fv_set_error("fv_case_block_sizes: bad arguments");
+    return FV_ERR_ARG;
+  }
+  for (int j = 0; j < n && j < FV_MAX_STAGES; ++j) threads[j] = c->tbs[j];
   return FV_OK;
 }
 
@@ -537,6 +564,7 @@ extern "C" int fv_case_set_block_size(FvCase* c, int threads) {
     return FV_ERR_ARG;
   }
   c->tb = threads;
+  for (int j = 0; j < FV_MAX_STAGES; ++j) c->tbs[j] = threads;
   return FV_OK;
 }
 

@@ -114,6 +114,7 @@ struct NodeAdjoint {
   double* rec = nullptr;      // limited reconstruction: centroid and limiter partials
 };
 
+#define FV_MAX_STAGES 12
 struct FvCase {
   FvMesh* mesh = nullptr;
   FvCaseDesc desc{};
@@ -147,6 +148,8 @@ struct FvCase {
   bool wd_missing = false;    // turbulent, no SST wall face, distance not yet set: no evaluation
   NodeAdjoint* nadj = nullptr;  // mesh-coordinate adjoint workspace, allocated on first use
   int tb = 128;                 // threads per block of the residual / JVP / VJP stages (autotuned)
+  int tbs[FV_MAX_STAGES] = {128, 128, 128, 128, 128, 128, 128, 128, 128, 128, 128, 128};
+                                // ... per stage (the profiling marks' order), tuned one by one
   int persistent = 0;           // residual + VJP as one cooperative launch (compact, upwind cases)
   int pchunk = 1;               // ... consecutive cells / faces per thread per stage
   int pblock = 128;             // ... threads per block
@@ -168,7 +171,6 @@ struct FvCase {
   int prof_max_runs = 0, prof_runs = 0, prof_stages = 0;
   std::vector<int> prof_run_marks;  // boundaries recorded per run
 };
-#define FV_MAX_STAGES 12
 // Record the stage boundary `k` of the current profiled run (no-op when profiling is off);
 // fv_prof_end_run closes the run.  Boundaries 0..6 delimit the six forward stages, 7..11 the
 // five adjoint stages of a VJP.

@@ -1232,7 +1232,7 @@ void gradient_stage(FvCase* cs, Src<T> st, Par<T> par, const Work<T>& w, cudaStr
   const MeshView& m = cs->mesh->view;
   const CaseView& cv = cs->view;
   constexpr int NF = Layout<DIM, TURB>::NFLD;
-  const int TB = cs->tb;
+  const int TB = cs->tbs[0];
   const int bc = fv_blocks(m.nc, TB);
   const int sweeps = cs->desc.gradient_sweeps;
   const double rel = sweeps >= 1 ? cs->desc.gradient_relaxation : 1.0;
@@ -1253,26 +1253,29 @@ int run(FvCase* cs, Src<T> st, Par<T> par, double* R, double* JV, cudaStream_t s
   const CaseView& cv = cs->view;
   const long nc = m.nc, nf = m.nf;
   Work<T> w = work_layout<T, DIM, TURB>(cs->work, nc, nf, psi_count<DIM, TURB>(cs));
-  const int TB = cs->tb;
-  const int bc = fv_blocks(nc, TB), bf = fv_blocks(nf, TB);
+  // each stage at its own block size (the index is the stage's profiling mark)
+  const int* tb = cs->tbs;
+  auto bc = [&](int k) { return fv_blocks(nc, tb[k]); };
+  auto bf = [&](int k) { return fv_blocks(nf, tb[k]); };
   fv_prof_mark(cs, 0, s);
   gradient_stage<T, DIM, TURB>(cs, st, par, w, s);
   fv_prof_mark(cs, 1, s);
-  if (TURB) k_closure<T, DIM><<<bc, TB, 0, s>>>(m, cv, st, par, w.G, w.cl, w.Gwi);
+  if (TURB) k_closure<T, DIM><<<bc(1), tb[1], 0, s>>>(m, cv, st, par, w.G, w.cl, w.Gwi);
   fv_prof_mark(cs, 2, s);
-  k_apcoef<T, DIM, TURB><<<bf, TB, 0, s>>>(m, cv, st, par, w.G, w.cl, w.acown, w.acnb, w.me);
+  k_apcoef<T, DIM, TURB><<<bf(2), tb[2], 0, s>>>(m, cv, st, par, w.G, w.cl, w.acown, w.acnb,
+                                                 w.me);
   fv_prof_mark(cs, 3, s);
-  k_dcoeff<T><<<bc, TB, 0, s>>>(m, w.acown, w.acnb, w.dco);
+  k_dcoeff<T><<<bc(3), tb[3], 0, s>>>(m, w.acown, w.acnb, w.dco);
   const long npsi = psi_count<DIM, TURB>(cs);
   if (npsi)
-    k_limiter<T, DIM, TURB><<<bc, TB, 0, s>>>(m, st, w.G, cv.lim_km, cv.lim_ks, w.psi);
+    k_limiter<T, DIM, TURB><<<bc(3), tb[3], 0, s>>>(m, st, w.G, cv.lim_km, cv.lim_ks, w.psi);
   // G, closure, Gwi, a_P, d and the slope limiters
   if (frozen) freeze<T>(w.G, (long)(w.psi + npsi - w.G), s);
   fv_prof_mark(cs, 4, s);
-  k_flux<T, DIM, TURB><<<bf, TB, 0, s>>>(m, cv, st, par, w.G, w.cl, w.dco, w.me,
-                                         npsi ? w.psi : nullptr, frozen, w.FL, aux);
+  k_flux<T, DIM, TURB><<<bf(4), tb[4], 0, s>>>(m, cv, st, par, w.G, w.cl, w.dco, w.me,
+                                               npsi ? w.psi : nullptr, frozen, w.FL, aux);
   fv_prof_mark(cs, 5, s);
-  k_sum<T, DIM, TURB><<<bc, TB, 0, s>>>(m, cv, st, par, w.FL, w.cl, w.G, w.Gwi, R, JV);
+  k_sum<T, DIM, TURB><<<bc(5), tb[5], 0, s>>>(m, cv, st, par, w.FL, w.cl, w.G, w.Gwi, R, JV);
   fv_prof_mark(cs, 6, s);
   if (end_profile_run) fv_prof_end_run(cs);
   FV_CUDA_TRY(cudaGetLastError());
@@ -1465,28 +1468,31 @@ int run_vjp(FvCase* cs, const double* state, const double* W, double* R, double*
   double* Gwi = fw.Gwi;
   double* dco = fw.dco;
   AdjWork aw = adj_layout<DIM, TURB>(cs);
-  const int TB = cs->tb;
-  const int bc = fv_blocks(nc, TB);
-  a_sum<DIM, TURB><<<bc, TB, 0, s>>>(m, cv, st, par, W, cl, G, Gwi, aw);
+  const int* tb = cs->tbs;  // each stage at its own block size (its profiling mark's index)
+  auto bc = [&](int k) { return fv_blocks(nc, tb[k]); };
+  a_sum<DIM, TURB><<<bc(6), tb[6], 0, s>>>(m, cv, st, par, W, cl, G, Gwi, aw);
   fv_prof_mark(cs, 7, s);
   const bool lim = psi_count<DIM, TURB>(cs) > 0;
   if (lim) aw.psi = fw.psi;
   if (aw.FLx && lim)
-    a_flux<DIM, TURB, true, true><<<bc, TB, 0, s>>>(m, cv, st, par, G, cl, dco, fw.me, cs->aux, aw);
+    a_flux<DIM, TURB, true, true><<<bc(7), tb[7], 0, s>>>(m, cv, st, par, G, cl, dco, fw.me,
+                                                          cs->aux, aw);
   else if (aw.FLx)
-    a_flux<DIM, TURB, true><<<bc, TB, 0, s>>>(m, cv, st, par, G, cl, dco, fw.me, cs->aux, aw);
+    a_flux<DIM, TURB, true><<<bc(7), tb[7], 0, s>>>(m, cv, st, par, G, cl, dco, fw.me, cs->aux,
+                                                    aw);
   else if (lim)
-    a_flux<DIM, TURB, false, true><<<bc, TB, 0, s>>>(m, cv, st, par, G, cl, dco, fw.me, cs->aux, aw);
+    a_flux<DIM, TURB, false, true><<<bc(7), tb[7], 0, s>>>(m, cv, st, par, G, cl, dco, fw.me,
+                                                           cs->aux, aw);
   else
-    a_flux<DIM, TURB><<<bc, TB, 0, s>>>(m, cv, st, par, G, cl, dco, fw.me, cs->aux, aw);
+    a_flux<DIM, TURB><<<bc(7), tb[7], 0, s>>>(m, cv, st, par, G, cl, dco, fw.me, cs->aux, aw);
   if (lim && (cv.lim_km > 0.0 || cv.lim_ks > 0.0)) {
-    a_limiter<DIM, TURB><<<bc, TB, 0, s>>>(m, st, G, cv.lim_km, cv.lim_ks, aw);
-    a_limiter_gather<DIM, TURB><<<bc, TB, 0, s>>>(m, aw);
+    a_limiter<DIM, TURB><<<bc(7), tb[7], 0, s>>>(m, st, G, cv.lim_km, cv.lim_ks, aw);
+    a_limiter_gather<DIM, TURB><<<bc(7), tb[7], 0, s>>>(m, aw);
   }
   fv_prof_mark(cs, 8, s);
-  a_apcoef<DIM, TURB><<<bc, TB, 0, s>>>(m, cv, st, par, G, cl, dco, fw.me, cs->aux, aw);
+  a_apcoef<DIM, TURB><<<bc(8), tb[8], 0, s>>>(m, cv, st, par, G, cl, dco, fw.me, cs->aux, aw);
   fv_prof_mark(cs, 9, s);
-  if (TURB) a_closure<DIM><<<bc, TB, 0, s>>>(m, cv, st, par, G, cl, aw);
+  if (TURB) a_closure<DIM><<<bc(9), tb[9], 0, s>>>(m, cv, st, par, G, cl, aw);
   fv_prof_mark(cs, 10, s);
   const int sweeps = cs->desc.gradient_sweeps;
   const double rel = sweeps >= 1 ? cs->desc.gradient_relaxation : 1.0;
@@ -1495,10 +1501,10 @@ int run_vjp(FvCase* cs, const double* state, const double* W, double* R, double*
     FV_CUDA_TRY(cudaMemcpyAsync(gb_save, aw.Gb, sizeof(double) * L::NFLD * DIM * nc,
                                 cudaMemcpyDeviceToDevice, s));
   if (sweeps >= 2) gb0 = gg_sweeps_adjoint<DIM, L::NFLD>(m, sweeps, rel, aw, fw.FL, s);
-  a_grad_face<DIM, TURB><<<fv_blocks(nf, TB), TB, 0, s>>>(m, cv, aw, gb0,
-                                                         sweeps >= 2 ? aw.Bb : nullptr, rel,
-                                                         fw.FL);
-  a_grad<DIM, TURB><<<bc, TB, 0, s>>>(m, cv, aw, fw.FL, out);
+  a_grad_face<DIM, TURB><<<fv_blocks(nf, tb[10]), tb[10], 0, s>>>(m, cv, aw, gb0,
+                                                                 sweeps >= 2 ? aw.Bb : nullptr,
+                                                                 rel, fw.FL);
+  a_grad<DIM, TURB><<<bc(10), tb[10], 0, s>>>(m, cv, aw, fw.FL, out);
   fv_prof_mark(cs, 11, s);
   fv_prof_end_run(cs);
   FV_CUDA_TRY(cudaGetLastError());

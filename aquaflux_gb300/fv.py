@@ -261,7 +261,8 @@ class FlowCase:
         return out
 
     def autotune(self, state, w) -> int:
-        """Pick the stage kernels' block size by timing the residual + VJP step (``fv_case_autotune``)."""
+        """Pick the stage kernels' block sizes by timing the residual + VJP step, each stage its own
+        fastest (``fv_case_autotune``); returns the fastest uniform size."""
         s, ww = self._vec(state), self._vec(w)
         out = torch.empty_like(s)
         best = ctypes.c_int(0)
@@ -286,6 +287,13 @@ class FlowCase:
 
     def set_block_size(self, threads: int) -> None:
         check(lib().fv_case_set_block_size(self._h, int(threads)))
+
+    def block_sizes(self) -> list[int]:
+        """Threads per block of each stage kernel (``fv_case_block_sizes``; the stages of
+        :attr:`STAGES`)."""
+        out = (ctypes.c_int * len(self.STAGES))()
+        check(lib().fv_case_block_sizes(self._h, out, len(self.STAGES)))
+        return list(out)
 
     def set_cell_order(self, coherent: bool = True) -> int:
         """Thread-to-cell order of the cell-centric stages (``fv_case_set_cell_order``): grouped by

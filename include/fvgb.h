@@ -129,9 +129,13 @@ int fv_case_set_params(FvCase* c, double mu, double inlet_scale);
  * (fv_segment_dot) is that instance's derivative. */
 int fv_case_set_viscosity_field(FvCase* c, const double* mu_cell, void* stream);
 /* Threads per block of the residual / JVP / VJP stage kernels (a multiple of 32 in [32, 128];
- * results do not depend on it).  fv_case_autotune times the residual + VJP step at state / w for
- * 32, 64, 96 and 128 and keeps the fastest (best receives it; out: n_unknowns scratch). */
+ * results do not depend on it): fv_case_set_block_size sets every stage.  fv_case_autotune times
+ * the residual + VJP step at state / w with every stage at 32, 64, 96 and 128 threads, stage by
+ * stage (the profiling marks), keeps each stage's fastest, and returns the fastest uniform size
+ * in best (out: n_unknowns scratch; no stage profile may be open).  fv_case_block_sizes copies
+ * the per-stage sizes (stages in the order of fv_case_profile_end's). */
 int fv_case_set_block_size(FvCase* c, int threads);
+int fv_case_block_sizes(const FvCase* c, int* threads, int n);
 /* Residual + VJP (fv_vjp) as ONE persistent cooperative launch (all stages in one kernel,
  * grid-wide barriers between them; compact gradients and first-order upwind; bitwise the
  * stage-per-launch result): enable != 0 with `block` threads per block (multiple of 32 in

@@ -1,6 +1,7 @@
-"""The warp-coherent cell order of the cell-centric stages changes which thread evaluates a cell,
-never the arithmetic: residual, JVP (fp64 and fp32 tangents), VJP, the face-flux functional's
-gradient and the node adjoint are bitwise the natural order's."""
+"""Evaluation-order choices change which thread evaluates a cell or face, never the arithmetic: the
+warp-coherent cell order and the per-stage block sizes of the autotuner give residual, JVP (fp64
+and fp32 tangents), VJP and the node adjoint bitwise equal to the natural order at one block
+size."""
 from __future__ import annotations
 
 import numpy as np
@@ -65,3 +66,23 @@ def test_node_adjoint_is_bitwise_order_independent():
     fc.set_cell_order(True)
     b = fc.node_vjp(s, w).cpu().numpy()
     assert np.array_equal(a, b)
+
+
+def test_per_stage_block_sizes_are_bitwise_neutral():
+    from aquaflux_gb300 import workloads
+
+    wl = workloads.channel3d(10, renumber="host")
+    fc = wl.device_case()
+    rng = np.random.default_rng(11)
+    s = wl.initial_state() * (1.0 + 0.05 * rng.standard_normal(fc.n_unknowns))
+    v = rng.standard_normal(fc.n_unknowns)
+    w = rng.standard_normal(fc.n_unknowns)
+    fc.set_block_size(128)
+    assert fc.block_sizes() == [128] * len(fc.STAGES)
+    ref = _evaluations(fc, s, v, w)
+    best = fc.autotune(s, w)
+    sizes = fc.block_sizes()
+    assert best in (32, 64, 96, 128) and all(t in (32, 64, 96, 128) for t in sizes)
+    got = _evaluations(fc, s, v, w)
+    for k in ref:
+        assert np.array_equal(ref[k], got[k]), k
