@@ -479,6 +479,41 @@ __global__ void k_ilu_lower_lg(IluView<V> F, const int* rows, int count, V* y) {
   if (live) y[(long)i * B + a] = acc;
 }
 
+// The in-block upper solve of one block row (lane a holds entry a of the row's right-hand side,
+// D the lane's row of the diagonal block).  Every lane forms the correctly rounded reciprocal r
+// of its own pivot d up front (all lanes at once), so the dependent chain needs no division: a
+// division there runs on one lane in eight at each step (fp32: 87 us of a 155 us diagonal-only
+// sweep of 1M block rows under ncu; fp64: the 128^3 fine-level solve 6.5 ms with divisions,
+// GB300).  The quotient x / d is q = x r corrected once, q + (x - q d) r, with fused
+// multiply-adds: by Markstein's theorem (IBM J. Res. Develop. 34(1), 1990) the correctly rounded
+// quotient, outside the underflow range (pinned bitwise against IEEE division in both precisions
+// by the sparse-solver tests).  A lane whose reciprocal overflows (fp32 pivot below ~3e-39)
+// divides.
+template <class V, int B>
+__device__ __forceinline__ V upper_block_solve(V acc, const V (&D)[B], int a, bool live,
+                                               unsigned mask) {
+  V piv = V(1);
+#pragma unroll
+  for (int c = 0; c < B; ++c)
+    if (a == c) piv = D[c];
+  const V rpiv = V(1) / piv;
+  const bool rfin = isfinite(rpiv);
+#pragma unroll
+  for (int c = B - 1; c >= 0; --c) {
+    if (a == c) {
+      if (rfin) {
+        const V q = acc * rpiv;
+        acc = fma_rn(fma_rn(-q, piv, acc), rpiv, q);
+      } else {
+        acc = acc / piv;
+      }
+    }
+    const V vc = __shfl_sync(mask, acc, c, FV_LG);
+    if (live && a < c) acc -= D[c] * vc;
+  }
+  return acc;
+}
+
 // Backward sweep of one level (U x = y).
 template <class V, int B>
 __global__ void k_ilu_upper_lg(IluView<V> F, const int* rows, int count, V* x) {
@@ -500,34 +535,41 @@ __global__ void k_ilu_upper_lg(IluView<V> F, const int* rows, int count, V* x) {
     }
   V D[B];
   if (live) load_seg<B>(F.val + (long)F.diag[i] * BB + (long)a * B, D);
-  // Every lane forms the correctly rounded reciprocal r of its own pivot d up front (all lanes
-  // at once), so the dependent chain below needs no division: a division there runs on one lane
-  // in eight at each step (fp32: 87 us of a 155 us diagonal-only sweep of 1M block rows under
-  // ncu; fp64: the 128^3 fine-level solve 6.5 ms with divisions, GB300).  The quotient x / d is
-  // q = x r corrected once, q + (x - q d) r, with fused multiply-adds: by Markstein's theorem
-  // (IBM J. Res. Develop. 34(1), 1990) the correctly rounded quotient, outside the underflow
-  // range (pinned bitwise against IEEE division in both precisions by the sparse-solver tests).
-  // A lane whose reciprocal overflows (fp32 pivot below ~3e-39) divides.
-  V piv = V(1);
-#pragma unroll
-  for (int c = 0; c < B; ++c)
-    if (a == c) piv = D[c];
-  const V rpiv = V(1) / piv;
-  const bool rfin = isfinite(rpiv);
-#pragma unroll
-  for (int c = B - 1; c >= 0; --c) {
-    if (a == c) {
-      if (rfin) {
-        const V q = acc * rpiv;
-        acc = fma_rn(fma_rn(-q, piv, acc), rpiv, q);
-      } else {
-        acc = acc / piv;
-      }
-    }
-    const V vc = __shfl_sync(mask, acc, c, FV_LG);
-    if (live && a < c) acc -= D[c] * vc;
-  }
+  acc = upper_block_solve<V, B>(acc, D, a, live, mask);
   if (live) x[(long)i * B + a] = acc;
+}
+
+// The last forward level followed by the first backward level on the same rows, one kernel: when
+// those rows own no upper blocks (the second colour of a two-colour order), a row's backward step
+// is the in-block upper solve of its own forward result, with the diagonal block already in
+// registers.  The same operations in the same order as the two separate sweeps.
+template <class V, int B>
+__global__ void k_ilu_lower_upper_lg(IluView<V> F, const int* rows, int count, V* y) {
+  const int gid = (blockIdx.x * blockDim.x + threadIdx.x) / FV_LG;
+  const int a = threadIdx.x & (FV_LG - 1);
+  if (gid >= count) return;
+  const unsigned mask = lg_mask();
+  const int i = rows[gid];
+  const bool live = a < B;
+  constexpr long BB = (long)B * B;
+  V acc = live ? y[(long)i * B + a] : V(0);
+  if (live)
+    for (int q = F.ptr[i]; q < F.diag[i]; ++q) {
+      V L[B], yj[B];
+      load_seg<B>(F.val + (long)q * BB + (long)a * B, L);
+      load_seg<B>(y + (long)F.idx[q] * B, yj);
+#pragma unroll
+      for (int c = 0; c < B; ++c) acc -= L[c] * yj[c];
+    }
+  V D[B];
+  if (live) load_seg<B>(F.val + (long)F.diag[i] * BB + (long)a * B, D);
+#pragma unroll
+  for (int c = 0; c < B; ++c) {
+    const V vc = __shfl_sync(mask, acc, c, FV_LG);
+    if (live && a > c) acc -= D[c] * vc;
+  }
+  acc = upper_block_solve<V, B>(acc, D, a, live, mask);
+  if (live) y[(long)i * B + a] = acc;
 }
 
 template <class V>
@@ -641,6 +683,7 @@ struct FvIlu0 {
   int* rows_tbwd = nullptr;  // L^T order
   std::vector<int> lv_fwd, lv_bwd, lv_tfwd, lv_tbwd;
   void* work = nullptr;                      // (n * b) vector the captured sweeps run on
+  bool fuse_fb = false;  // the last forward level's rows are the first backward level's (fused)
   cudaGraphExec_t apply_exec[2] = {nullptr, nullptr};  // forward / transposed solve
   cudaGraphExec_t factor_exec = nullptr;
   // host copy of the pattern (shared by clones): the transposed-solve structures are built on
@@ -707,16 +750,22 @@ void launch_apply_levels(FvIlu0* f, int transpose, V* x, cudaStream_t s) {
   const bool lg = f->b > 1;
   auto grid = [&](int cnt) { return lg ? fv_blocks((long)cnt * FV_LG, 128) : fv_blocks(cnt, 128); };
   if (!transpose) {
+    const size_t last = f->lv_fwd.size() - 2;
     for (size_t l = 0; l + 1 < f->lv_fwd.size(); ++l) {
       const int cnt = f->lv_fwd[l + 1] - f->lv_fwd[l];
       if (!cnt) continue;
-      if (lg)
+      if (lg && f->fuse_fb && l == last)
+        with_block_size(f->b, [&](auto B) {
+          k_ilu_lower_upper_lg<V, B()><<<grid(cnt), 128, 0, s>>>(F, f->rows_fwd + f->lv_fwd[l],
+                                                                 cnt, x);
+        });
+      else if (lg)
         with_block_size(f->b, [&](auto B) {
           k_ilu_lower_lg<V, B()><<<grid(cnt), 128, 0, s>>>(F, f->rows_fwd + f->lv_fwd[l], cnt, x);
         });
       else k_ilu_lower<V><<<grid(cnt), 128, 0, s>>>(F, f->rows_fwd + f->lv_fwd[l], cnt, x);
     }
-    for (size_t l = 0; l + 1 < f->lv_bwd.size(); ++l) {
+    for (size_t l = f->fuse_fb ? 1 : 0; l + 1 < f->lv_bwd.size(); ++l) {
       const int cnt = f->lv_bwd[l + 1] - f->lv_bwd[l];
       if (!cnt) continue;
       if (lg)
@@ -906,10 +955,18 @@ extern "C" int fv_ilu0_create(int n, int b, const int* indptr, const int* indice
     for (int q = indptr[i]; q < diag[i]; ++q) use(indices[q]);
   }, &rows, &f->lv_fwd);
   if (upload(rows, &f->rows_fwd, s)) return FV_ERR_CUDA;
+  const size_t nf = f->lv_fwd.size();
+  std::vector<int> fwd_last(rows.begin() + f->lv_fwd[nf - 2], rows.begin() + f->lv_fwd[nf - 1]);
   levels(n, false, [&](int i, auto&& use) {
     for (int q = diag[i] + 1; q < indptr[i + 1]; ++q) use(indices[q]);
   }, &rows, &f->lv_bwd);
   if (upload(rows, &f->rows_bwd, s)) return FV_ERR_CUDA;
+  // fused last forward / first backward level when they hold the same rows (the first backward
+  // level's rows own no upper blocks by construction)
+  std::vector<int> bwd_first(rows.begin() + f->lv_bwd[0], rows.begin() + f->lv_bwd[1]);
+  std::sort(fwd_last.begin(), fwd_last.end());
+  std::sort(bwd_first.begin(), bwd_first.end());
+  f->fuse_fb = b > 1 && nf > 2 && f->lv_bwd.size() > 2 && fwd_last == bwd_first;
   f->h_ptr = std::make_shared<const std::vector<int>>(indptr, indptr + n + 1);
   f->h_idx = std::make_shared<const std::vector<int>>(indices, indices + nnzb);
   f->h_diag = std::make_shared<const std::vector<int>>(diag);
@@ -971,6 +1028,7 @@ extern "C" int fv_ilu0_clone(const FvIlu0* src, int precision, void* stream, FvI
   f->lv_bwd = src->lv_bwd;
   f->lv_tfwd = src->lv_tfwd;
   f->lv_tbwd = src->lv_tbwd;
+  f->fuse_fb = src->fuse_fb;
   f->h_ptr = src->h_ptr;
   f->h_idx = src->h_idx;
   f->h_diag = src->h_diag;

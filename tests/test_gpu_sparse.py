@@ -210,3 +210,53 @@ def test_cloned_ilu0_equals_a_fresh_factor_bitwise(precision):
         template.refactor(bv)
     with pytest.raises(FvError):
         template.solve(rhs)
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+def test_two_colour_block_ilu0_fused_sweep(precision):
+    """A red-black numbered 2D grid: the second colour's rows are the last forward and the first
+    backward level, solved by one fused sweep.  fp64: factor bitwise the oracle's, solve within
+    1e-13, transposed solve bitwise; fp32 within its rounding; the fused solve is bitwise the one
+    of the same factor cloned from a structure-only template (same kernels) and run to run."""
+    import scipy.sparse as sp
+
+    from aquaflux_gb300.ilu0 import Ilu0
+
+    nx, ny, b = 12, 10, 3
+    rng = np.random.default_rng(4)
+    cells = [(i, j) for i in range(nx) for j in range(ny)]
+    order = sorted(range(nx * ny), key=lambda c: ((cells[c][0] + cells[c][1]) % 2, c))
+    new = np.empty(nx * ny, dtype=np.int64)
+    new[order] = np.arange(nx * ny)
+    rows, cols = [], []
+    for c, (i, j) in enumerate(cells):
+        for di, dj in ((0, 0), (1, 0), (-1, 0), (0, 1), (0, -1)):
+            if 0 <= i + di < nx and 0 <= j + dj < ny:
+                rows.append(new[c])
+                cols.append(new[(i + di) * ny + (j + dj)])
+    pat = sp.coo_matrix((np.ones(len(rows)), (rows, cols)), shape=(nx * ny,) * 2).tocsr()
+    pat.sort_indices()
+    nb = pat.nnz
+    blocks = rng.standard_normal((nb, b, b)) * 0.3
+    bi = pat.indices.astype(np.int32)
+    bp = pat.indptr.astype(np.int32)
+    for r in range(nx * ny):
+        q = bp[r] + int(np.searchsorted(bi[bp[r]:bp[r + 1]], r))
+        blocks[q] += np.eye(b) * 4.0
+    a = sp.bsr_matrix((blocks, bi, bp), shape=(nx * ny * b,) * 2).tocsr()
+    a.sort_indices()
+    rhs = rng.standard_normal(nx * ny * b)
+    _, data, x, xt = oracle_factor_solve(a.indptr, a.indices, a.data, rhs)
+    f = Ilu0.from_csr(bp, bi, blocks.reshape(-1), block_size=b, precision=precision)
+    got = f.solve(rhs).cpu().numpy()
+    assert np.array_equal(got, f.solve(rhs).cpu().numpy())
+    c = f.clone(0).clone(precision)
+    c.refactor(blocks.reshape(-1))
+    assert np.array_equal(got, c.solve(rhs).cpu().numpy())
+    if precision == 64:
+        sp_ip, sp_ix, sp_data = to_scalar(bp, bi, f.factor_values().cpu().numpy(), b)
+        np.testing.assert_array_equal(sp_data, data)
+        np.testing.assert_allclose(got, x, rtol=1e-13, atol=1e-15)
+        np.testing.assert_array_equal(f.solve(rhs, transpose=True).cpu().numpy(), xt)
+    else:
+        np.testing.assert_allclose(got, x, rtol=2e-5, atol=1e-6)
