@@ -53,6 +53,8 @@ SIGNATURES = {
     "fv_jvp": (c_int, [P, P, P, P, P, P]),
     "fv_jvp_shift": (c_int, [P, P, P, P, P, P]),
     "fv_jvp_frozen": (c_int, [P, P, P, P, P]),
+    "fv_linearise": (c_int, [P, P, P, P]),
+    "fv_jvp_linearised": (c_int, [P, P, P, P, P, P]),
     "fv_probe_jacobian": (c_int, [P, P, c_int, P, c_int, P, P, P, P]),
     "fv_jvp_batch": (c_int, [P, P, P, c_int, P, P]),
     "fv_node_vjp": (c_int, [P, P, P, P, P]),

@@ -368,6 +368,10 @@ extern "C" int fv_case_destroy(FvCase* c) {
   cudaFree(c->jac_face);
   cudaFree(c->wnear);
   cudaFree(c->sched);
+  cudaFree(c->lin_aux);
+  cudaFree(c->lin_fl);
+  cudaFree(c->lin_ac);
+  cudaFree(c->lin_g);
   fv_node_adjoint_free(c);
   cudaFree(c->flx);
   cudaFree(c->mu_cell);
@@ -389,6 +393,7 @@ extern "C" int fv_case_set_params(FvCase* c, double mu, double inlet_scale) {
   }
   c->mu = mu;
   c->inlet_scale = inlet_scale;
+  c->lin_valid = 0;
   return FV_OK;
 }
 
@@ -397,6 +402,7 @@ extern "C" int fv_case_set_viscosity_field(FvCase* c, const double* mu_cell, voi
     fv_set_error("fv_case_set_viscosity_field: null case");
     return FV_ERR_ARG;
   }
+  c->lin_valid = 0;
   if (!mu_cell) {
     c->view.mu_cell = nullptr;
     return FV_OK;
@@ -573,6 +579,7 @@ extern "C" int fv_case_refresh_geometry(FvCase* c, void* stream) {
     fv_set_error("fv_case_refresh_geometry: null case");
     return FV_ERR_ARG;
   }
+  c->lin_valid = 0;
   if (!c->desc.turbulent) return FV_OK;
   if (c->wd_external) {
     fv_set_error("fv_case_refresh_geometry: the wall distance was set by the caller "
@@ -603,6 +610,7 @@ extern "C" int fv_case_set_wall_distance(FvCase* c, const double* distance, void
   }
   cudaStream_t s = (cudaStream_t)stream;
   FvMesh* m = c->mesh;
+  c->lin_valid = 0;
   FV_CUDA_TRY(cudaMemcpyAsync(c->wd, distance, sizeof(double) * m->nc, cudaMemcpyDeviceToDevice, s));
   int rc = fv_wall_distance_gradient(m, c->swall, c->wd, c->wdg, c->desc.gradient_sweeps,
                                      c->desc.gradient_relaxation, s);
@@ -666,6 +674,34 @@ extern "C" int fv_jvp(FvCase* c, const double* state, const double* v, double* r
   cudaStream_t s = (cudaStream_t)stream;
   state = physical_state(c, state, s);
   return fv_case_run(c, state, physical_tangent(c, v, s), FV_TAN_STATE, residual, jv, s);
+}
+
+extern "C" int fv_linearise(FvCase* c, const double* state, double* residual, void* stream) {
+  if (!c || !state) {
+    fv_set_error("fv_linearise: bad arguments");
+    return FV_ERR_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  return fv_case_linearise(c, physical_state(c, state, s), residual ? residual : c->tmp2, s);
+}
+
+extern "C" int fv_jvp_linearised(FvCase* c, const double* state, const double* v,
+                                 double* residual, double* jv, void* stream) {
+  if (!c || !state || !v || !jv) {
+    fv_set_error("fv_jvp_linearised: bad arguments");
+    return FV_ERR_ARG;
+  }
+  if (!c->lin_valid) {
+    fv_set_error("fv_jvp_linearised: no linearisation held; call fv_linearise at this state "
+                 "(again after any parameter, viscosity-field or geometry change)");
+    return FV_ERR_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  state = physical_state(c, state, s);
+  c->lin_use = 1;
+  const int rc = fv_case_run(c, state, physical_tangent(c, v, s), FV_TAN_STATE, residual, jv, s);
+  c->lin_use = 0;
+  return rc;
 }
 
 extern "C" int fv_jvp_frozen(FvCase* c, const double* state, const double* v, double* jv,

@@ -155,6 +155,12 @@ struct FvCase {
   int pblock = 128;             // ... threads per block
   int* sched = nullptr;         // (nc) warp-coherent cell order of the cell stages
   int n_cell_classes = 0;       // distinct face-list patterns it groups
+  double* lin_aux = nullptr;    // face intermediates of the held linearisation (fv_case_linearise)
+  double* lin_fl = nullptr;     // ... and its primal face fluxes (nfld, nf)
+  double* lin_ac = nullptr;     // ... its face coefficients and mass-flux estimates (3, nf)
+  double* lin_g = nullptr;      // ... its gradients (nfld, dim, nc)
+  int lin_valid = 0;            // a linearisation is held (parameter / geometry changes clear it)
+  int lin_use = 0;              // the running dual-number pass takes its flux stage from it
   double* mu_cell = nullptr;    // (nc) per-cell viscosity field (laminar batched instances)
   double* flx = nullptr;        // (nfld, nf) weights of a face-flux functional (internal order)
   bool flx_active = false;      // the adjoints add flx to their face-flux cotangents
@@ -186,6 +192,9 @@ int fv_case_run(FvCase* c, const double* state, const double* tangent, int tange
                 double* residual, double* jv, cudaStream_t s);
 int fv_case_vjp_run(FvCase* c, const double* state, const double* w, double* residual, double* out,
                     cudaStream_t s);
+// The residual at a (physical) state with its face intermediates and primal face fluxes kept for
+// the linearised JVP (residual.cu); refuses limited reconstruction.
+int fv_case_linearise(FvCase* c, const double* state, double* residual, cudaStream_t s);
 // Frozen reach-1 Jacobian by per-face forward-mode derivatives (residual.cu); D holds
 // fv_jac_face_bytes.
 // Mesh-coordinate adjoint dL/dnodes of L = w . R(state, nodes) (residual.cu).

@@ -898,8 +898,108 @@ __device__ __forceinline__ void k_apcoef_at(const int f, MeshView m, CaseView cv
 template <class T, int DIM, bool TURB>
 __global__ void __launch_bounds__(128) k_apcoef(MeshView m, CaseView cv, Src<T> st, Par<T> par,
                                                 const T* G, const T* cl, T* ac_own, T* ac_nb,
-                                                T* me) {
-  k_apcoef_at<T, DIM, TURB>(blockIdx.x * blockDim.x + threadIdx.x, m, cv, st, par, G, cl, ac_own, ac_nb, me);
+                                                T* me, int face0 = 0) {
+  k_apcoef_at<T, DIM, TURB>(face0 + blockIdx.x * blockDim.x + threadIdx.x, m, cv, st, par, G, cl, ac_own, ac_nb, me);
+}
+
+// The interior faces' momentum-diagonal coefficients and mass-flux estimate of a state-tangent
+// dual-number pass at a held linearisation: the momentum-normal flux is linear in the velocities
+// and their gradients, the conductance's tangent comes from its kept partial derivatives in the
+// cell viscosities, max(., 0) follows the kept sign of the estimate (JAX's tie rule); the primal
+// values are the kept ones (lin: owner coefficient, neighbour coefficient, estimate).
+template <int DIM, bool TURB>
+__global__ void __launch_bounds__(128) k_apcoef_tangent(MeshView m, CaseView cv, Src<Dual> st,
+                                                        const Dual* G, const Dual* cl,
+                                                        const double* aux, const double* lin,
+                                                        Dual* ac_own, Dual* ac_nb, Dual* me) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= m.nfi) return;
+  const long nc = m.nc, nf = m.nf;
+  const int o = m.owner[f], n = m.nb[f];
+  const double g = m.g[f], A = m.area[f], rho = cv.rho;
+  double mn_t = 0.0;
+#pragma unroll
+  for (int j = 0; j < DIM; ++j) {
+    mn_t += m.normal[(long)j * nf + f] * lerp(st((long)j * nc + o).d, st((long)j * nc + n).d, g);
+#pragma unroll
+    for (int q = 0; q < DIM; ++q)
+      mn_t += m.ns[(long)(j * DIM + q) * nf + f] *
+              lerp(G[((long)j * DIM + q) * nc + o].d, G[((long)j * DIM + q) * nc + n].d, g);
+  }
+  const double me_t = (rho * mn_t) * A;
+  const double mo_t = TURB ? rho * cl[2L * nc + o].d : 0.0;
+  const double mn_c = TURB ? rho * cl[2L * nc + n].d : 0.0;
+  const double visc_t = aux[4L * nf + f] * mo_t + aux[5L * nf + f] * mn_c;
+  const double e = lin[2L * nf + f];
+  const double pp = e > 0.0 ? me_t : (e < 0.0 ? 0.0 : 0.5 * me_t);
+  const double pm = e < 0.0 ? -me_t : (e > 0.0 ? 0.0 : 0.5 * -me_t);
+  ac_own[f] = Dual{lin[f], visc_t + pp};
+  ac_nb[f] = Dual{lin[(long)nf + f], visc_t + pm};
+  me[f] = Dual{e, me_t};
+}
+
+// The compact Green-Gauss gradients of a state-tangent dual-number pass at a held linearisation:
+// the scheme is linear, so the tangents are the face-value tangents' gradients (boundary values by
+// the dual-number closures) and the primal gradients are the kept ones.
+template <int DIM, bool TURB>
+__global__ void __launch_bounds__(128) k_grad_tangent(MeshView m, CaseView cv, Src<Dual> st,
+                                                      Par<Dual> par, const double* Gp, Dual* G) {
+  using L = Layout<DIM, TURB>;
+  constexpr int NF = L::NFLD;
+  const int c = stage_cell<Dual>(m, cv);
+  if (c >= m.nc) return;
+  const int nc = m.nc, nf = m.nf;
+  Dual phic[NF];
+#pragma unroll
+  for (int q = 0; q < NF; ++q) phic[q] = st((long)q * nc + c);
+  double acc[NF][DIM];
+#pragma unroll
+  for (int q = 0; q < NF; ++q)
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) acc[q][j] = 0.0;
+  const int b = m.cf_ptr[c], e = m.cf_ptr[c + 1];
+  for (int i = b; i < e; ++i) {
+    const unsigned ent = m.cf_face[i];
+    const int f = (int)(ent & ~FV_NB_BIT);
+    const bool isnb = (ent & FV_NB_BIT) != 0;
+    const double af = m.area[f];
+    const double A = isnb ? -af : af;
+    double S[DIM];
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) S[j] = m.normal[(long)j * nf + f] * A;
+    double phif[NF];
+    if (f < m.nfi) {
+      const double g = m.g[f];
+      const int other = isnb ? m.owner[f] : m.nb[f];
+#pragma unroll
+      for (int q = 0; q < NF; ++q) {
+        const double po = st((long)q * nc + other).d;
+        phif[q] = lerp(isnb ? po : phic[q].d, isnb ? phic[q].d : po, g);
+      }
+    } else {
+      const signed char kind = cv.fkind[f];
+#pragma unroll
+      for (int j = 0; j < DIM; ++j) phif[j] = bvel(cv, nf, f, j, kind, phic[j], par).d;
+      phif[L::P] = bpress(cv, f, kind, phic[L::P]).d;
+      if (TURB) {
+        const Dual z = cst(0.0, phic[0]);
+        phif[L::K] = bscalar(cv.kkind[f], cv.kval[f], phic[L::K], z).d;
+        phif[L::W] = bscalar(cv.wkind[f], cv.wval[f], phic[L::W], z).d;
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < NF; ++q)
+#pragma unroll
+      for (int j = 0; j < DIM; ++j) acc[q][j] += S[j] * phif[q];
+  }
+  const double inv = m.inv_vol[c];
+#pragma unroll
+  for (int q = 0; q < NF; ++q)
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) {
+      const long k = ((long)q * DIM + j) * nc + c;
+      G[k] = Dual{Gp[k], acc[q][j] * inv};
+    }
 }
 
 // ---------------------------------------------------------------- k_dcoeff
@@ -1126,8 +1226,91 @@ __device__ __forceinline__ void k_flux_at(const int f, MeshView m, CaseView cv, 
 template <class T, int DIM, bool TURB>
 __global__ void __launch_bounds__(128) k_flux(MeshView m, CaseView cv, Src<T> st, Par<T> par,
                                               const T* G, const T* cl, const T* dco, const T* me,
-                                              const T* psi, bool recompute_me, T* FL, double* aux) {
-  k_flux_at<T, DIM, TURB>(blockIdx.x * blockDim.x + threadIdx.x, m, cv, st, par, G, cl, dco, me, psi, recompute_me, FL, aux);
+                                              const T* psi, bool recompute_me, T* FL, double* aux,
+                                              int face0 = 0) {
+  k_flux_at<T, DIM, TURB>(face0 + blockIdx.x * blockDim.x + threadIdx.x, m, cv, st, par, G, cl, dco, me, psi, recompute_me, FL, aux);
+}
+
+// The interior face fluxes of a state-tangent dual-number pass at a held linearisation (first-order
+// upwind): the primal face intermediates the double pass kept (mass flux, pressure damping,
+// interpolated d, conductances and their partial derivatives in the cell diffusivities, the
+// cross-diffusion numerators) stand in for their recomputation, so only the tangent arithmetic of
+// flux_face runs -- the forward-mode counterpart of the adjoint's use of the same intermediates.
+// The primal fluxes are the kept ones.  Mass-flux estimate, gradients, closure and d arrive as dual
+// numbers from the pass's earlier stages.
+template <int DIM, bool TURB>
+__global__ void __launch_bounds__(128) k_flux_tangent(MeshView m, CaseView cv, Src<Dual> st,
+                                                      const Dual* G, const Dual* cl,
+                                                      const Dual* dco, const Dual* me,
+                                                      const double* aux, const double* flp,
+                                                      Dual* FL) {
+  using L = Layout<DIM, TURB>;
+  using AX = Aux<DIM, TURB>;
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= m.nfi) return;
+  const long nc = m.nc, nf = m.nf;
+  const int o = m.owner[f], n = m.nb[f];
+  const double A = m.area[f], g = m.g[f];
+  const double rho = cv.rho, irho = 1.0 / cv.rho;
+  const double mdot = aux[0L * nf + f], damping = aux[1L * nf + f], dhat = aux[2L * nf + f];
+  const double cmo = aux[3L * nf + f], dcdo = aux[4L * nf + f], dcdn = aux[5L * nf + f];
+  double gd = 0.0, gs = 0.0;
+#pragma unroll
+  for (int j = 0; j < DIM; ++j) {
+    const double gpf = lerp(G[((long)L::P * DIM + j) * nc + o].d, G[((long)L::P * DIM + j) * nc + n].d, g);
+    gd += gpf * m.dvec[(long)j * nf + f];
+    gs += gpf * m.skew[(long)j * nf + f];
+  }
+  const double dhat_t = m.nn2[f] * lerp(dco[o].d, dco[n].d, g);
+  const Dual po = st((long)L::P * nc + o), pn = st((long)L::P * nc + n);
+  const double damp_t = ((pn.d - po.d) - gd) * m.inv_nd[f];
+  const double mdot_t = me[f].d - (rho * A) * (dhat_t * damping + dhat * damp_t);
+  const double pA_t = (lerp(po.d, pn.d, g) + gs) * A;
+  // d(mu + rho nu_t) for a state tangent (the molecular viscosity is a parameter)
+  const double mo_t = TURB ? rho * cl[2L * nc + o].d : 0.0;
+  const double mn_t = TURB ? rho * cl[2L * nc + n].d : 0.0;
+  const double cmo_t = dcdo * mo_t + dcdn * mn_t;
+  const bool out = mdot >= 0.0;
+  double tP[DIM], tN[DIM];
+#pragma unroll
+  for (int j = 0; j < DIM; ++j) {
+    tP[j] = m.tP[(long)j * nf + f];
+    tN[j] = m.tN[(long)j * nf + f];
+  }
+#pragma unroll
+  for (int i = 0; i < DIM; ++i) {
+    const Dual uo = st((long)i * nc + o), un = st((long)i * nc + n);
+    double cpn_t = un.d - uo.d;
+#pragma unroll
+    for (int j = 0; j < DIM; ++j)
+      cpn_t += G[((long)i * DIM + j) * nc + n].d * tN[j] - G[((long)i * DIM + j) * nc + o].d * tP[j];
+    const double cpn = aux[(long)(AX::CPN + i) * nf + f];
+    const double up = out ? uo.v : un.v, up_t = out ? uo.d : un.d;
+    const double ft = (pA_t * m.normal[(long)i * nf + f] - (cmo_t * cpn + cmo * cpn_t)) +
+                      (mdot_t * up + mdot * up_t);
+    FL[(long)i * nf + f] = Dual{flp[(long)i * nf + f], ft};
+  }
+  FL[(long)L::P * nf + f] = Dual{flp[(long)L::P * nf + f], mdot_t};
+  if (TURB) {
+    const double vflux = mdot * irho, vflux_t = mdot_t * irho;
+    const bool vout = vflux >= 0.0;
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+      const int q = s == 0 ? L::K : L::W;
+      const long b0 = AX::S0 + 4 * s;
+      const double go_t = cl[(4L + s) * nc + o].d, gn_t = cl[(4L + s) * nc + n].d;
+      const Dual phio = st((long)q * nc + o), phin = st((long)q * nc + n);
+      double cpn_t = phin.d - phio.d;
+#pragma unroll
+      for (int j = 0; j < DIM; ++j)
+        cpn_t += G[((long)q * DIM + j) * nc + n].d * tN[j] - G[((long)q * DIM + j) * nc + o].d * tP[j];
+      const double cs = aux[b0 * nf + f], cpn = aux[(b0 + 3) * nf + f];
+      const double cs_t = aux[(b0 + 1) * nf + f] * go_t + aux[(b0 + 2) * nf + f] * gn_t;
+      const double up = vout ? phio.v : phin.v, up_t = vout ? phio.d : phin.d;
+      const double ft = (vflux_t * up + vflux * up_t) - (cs_t * cpn + cs * cpn_t);
+      FL[(long)q * nf + f] = Dual{flp[(long)q * nf + f], ft};
+    }
+  }
 }
 
 // ---------------------------------------------------------------- k_sum
@@ -1257,13 +1440,39 @@ int run(FvCase* cs, Src<T> st, Par<T> par, double* R, double* JV, cudaStream_t s
   const int* tb = cs->tbs;
   auto bc = [&](int k) { return fv_blocks(nc, tb[k]); };
   auto bf = [&](int k) { return fv_blocks(nf, tb[k]); };
+  // a held linearisation (a state-tangent dual-number pass, first-order upwind): the linear
+  // compact gradients and the interior faces' coefficient and flux stages take their primal
+  // values from it and compute only tangents
+  bool lin = false;
+  if constexpr (std::is_same<T, Dual>::value) lin = cs->lin_use && !frozen && !psi_count<DIM, TURB>(cs);
   fv_prof_mark(cs, 0, s);
-  gradient_stage<T, DIM, TURB>(cs, st, par, w, s);
+  if constexpr (std::is_same<T, Dual>::value) {
+    if (lin && cs->desc.gradient_sweeps == 0)  // the compact scheme (no relaxation factor)
+      k_grad_tangent<DIM, TURB><<<bc(0), tb[0], 0, s>>>(m, cv, st, par, cs->lin_g, w.G);
+    else
+      gradient_stage<T, DIM, TURB>(cs, st, par, w, s);
+  } else {
+    gradient_stage<T, DIM, TURB>(cs, st, par, w, s);
+  }
   fv_prof_mark(cs, 1, s);
   if (TURB) k_closure<T, DIM><<<bc(1), tb[1], 0, s>>>(m, cv, st, par, w.G, w.cl, w.Gwi);
   fv_prof_mark(cs, 2, s);
-  k_apcoef<T, DIM, TURB><<<bf(2), tb[2], 0, s>>>(m, cv, st, par, w.G, w.cl, w.acown, w.acnb,
-                                                 w.me);
+  if constexpr (std::is_same<T, Dual>::value) {
+    if (lin) {
+      if (m.nfi > 0)
+        k_apcoef_tangent<DIM, TURB><<<fv_blocks(m.nfi, tb[2]), tb[2], 0, s>>>(
+            m, cv, st, w.G, w.cl, cs->lin_aux, cs->lin_ac, w.acown, w.acnb, w.me);
+      if (nf > m.nfi)
+        k_apcoef<T, DIM, TURB><<<fv_blocks(nf - m.nfi, tb[2]), tb[2], 0, s>>>(
+            m, cv, st, par, w.G, w.cl, w.acown, w.acnb, w.me, m.nfi);
+    } else {
+      k_apcoef<T, DIM, TURB><<<bf(2), tb[2], 0, s>>>(m, cv, st, par, w.G, w.cl, w.acown, w.acnb,
+                                                     w.me);
+    }
+  } else {
+    k_apcoef<T, DIM, TURB><<<bf(2), tb[2], 0, s>>>(m, cv, st, par, w.G, w.cl, w.acown, w.acnb,
+                                                   w.me);
+  }
   fv_prof_mark(cs, 3, s);
   k_dcoeff<T><<<bc(3), tb[3], 0, s>>>(m, w.acown, w.acnb, w.dco);
   const long npsi = psi_count<DIM, TURB>(cs);
@@ -1272,8 +1481,23 @@ int run(FvCase* cs, Src<T> st, Par<T> par, double* R, double* JV, cudaStream_t s
   // G, closure, Gwi, a_P, d and the slope limiters
   if (frozen) freeze<T>(w.G, (long)(w.psi + npsi - w.G), s);
   fv_prof_mark(cs, 4, s);
-  k_flux<T, DIM, TURB><<<bf(4), tb[4], 0, s>>>(m, cv, st, par, w.G, w.cl, w.dco, w.me,
-                                               npsi ? w.psi : nullptr, frozen, w.FL, aux);
+  bool flux_done = false;
+  if constexpr (std::is_same<T, Dual>::value) {
+    if (lin) {
+      // a held linearisation: the interior faces' tangent fluxes from its kept intermediates, the
+      // boundary faces by the full dual-number flux
+      if (m.nfi > 0)
+        k_flux_tangent<DIM, TURB><<<fv_blocks(m.nfi, tb[4]), tb[4], 0, s>>>(
+            m, cv, st, w.G, w.cl, w.dco, w.me, cs->lin_aux, cs->lin_fl, w.FL);
+      if (nf > m.nfi)
+        k_flux<T, DIM, TURB><<<fv_blocks(nf - m.nfi, tb[4]), tb[4], 0, s>>>(
+            m, cv, st, par, w.G, w.cl, w.dco, w.me, nullptr, false, w.FL, nullptr, m.nfi);
+      flux_done = true;
+    }
+  }
+  if (!flux_done)
+    k_flux<T, DIM, TURB><<<bf(4), tb[4], 0, s>>>(m, cv, st, par, w.G, w.cl, w.dco, w.me,
+                                                 npsi ? w.psi : nullptr, frozen, w.FL, aux);
   fv_prof_mark(cs, 5, s);
   k_sum<T, DIM, TURB><<<bc(5), tb[5], 0, s>>>(m, cv, st, par, w.FL, w.cl, w.G, w.Gwi, R, JV);
   fv_prof_mark(cs, 6, s);
@@ -1537,6 +1761,52 @@ int fv_case_vjp_run(FvCase* cs, const double* state, const double* W, double* R,
   if (dim == 2)
     return turb ? run_vjp<2, true>(cs, state, W, R, out, s) : run_vjp<2, false>(cs, state, W, R, out, s);
   return turb ? run_vjp<3, true>(cs, state, W, R, out, s) : run_vjp<3, false>(cs, state, W, R, out, s);
+}
+
+namespace {
+template <int DIM, bool TURB>
+int linearise(FvCase* cs, const double* state, double* R, cudaStream_t s) {
+  const long nc = cs->mesh->nc, nf = cs->mesh->nf;
+  constexpr int NF = Layout<DIM, TURB>::NFLD;
+  if (psi_count<DIM, TURB>(cs) > 0) {
+    fv_set_error("fv_case_linearise: the linearised JVP covers first-order upwind advection only");
+    return FV_ERR_ARG;
+  }
+  if (!cs->lin_aux) FV_CUDA_TRY(cudaMalloc(&cs->lin_aux, fv_aux_bytes(DIM, TURB, nf)));
+  if (!cs->lin_fl) FV_CUDA_TRY(cudaMalloc(&cs->lin_fl, sizeof(double) * NF * nf));
+  if (!cs->lin_ac) FV_CUDA_TRY(cudaMalloc(&cs->lin_ac, sizeof(double) * 3 * nf));
+  if (!cs->lin_g) FV_CUDA_TRY(cudaMalloc(&cs->lin_g, sizeof(double) * NF * DIM * nc));
+  cs->lin_valid = 0;
+  const double irho = 1.0 / cs->desc.rho;
+  int rc = run<double, DIM, TURB>(cs, Src<double>{state},
+                                  Par<double>{cs->mu, cs->inlet_scale, cs->mu * irho}, R, nullptr,
+                                  s, false, true, cs->lin_aux);
+  if (rc != FV_OK) return rc;
+  Work<double> w = work_layout<double, DIM, TURB>(cs->work, nc, nf, psi_count<DIM, TURB>(cs));
+  FV_CUDA_TRY(cudaMemcpyAsync(cs->lin_fl, w.FL, sizeof(double) * NF * nf,
+                              cudaMemcpyDeviceToDevice, s));
+  FV_CUDA_TRY(cudaMemcpyAsync(cs->lin_ac, w.acown, sizeof(double) * nf, cudaMemcpyDeviceToDevice, s));
+  FV_CUDA_TRY(cudaMemcpyAsync(cs->lin_ac + nf, w.acnb, sizeof(double) * nf,
+                              cudaMemcpyDeviceToDevice, s));
+  FV_CUDA_TRY(cudaMemcpyAsync(cs->lin_ac + 2 * nf, w.me, sizeof(double) * nf,
+                              cudaMemcpyDeviceToDevice, s));
+  FV_CUDA_TRY(cudaMemcpyAsync(cs->lin_g, w.G, sizeof(double) * NF * DIM * nc,
+                              cudaMemcpyDeviceToDevice, s));
+  cs->lin_valid = 1;
+  return FV_OK;
+}
+}  // namespace
+
+int fv_case_linearise(FvCase* cs, const double* state, double* R, cudaStream_t s) {
+  if (cs->wd_missing) {
+    fv_set_error("turbulent case without SST wall faces: set its wall distance first "
+                 "(fv_case_set_wall_distance)");
+    return FV_ERR_ARG;
+  }
+  const int dim = cs->mesh->dim;
+  const bool turb = cs->desc.turbulent != 0;
+  if (dim == 2) return turb ? linearise<2, true>(cs, state, R, s) : linearise<2, false>(cs, state, R, s);
+  return turb ? linearise<3, true>(cs, state, R, s) : linearise<3, false>(cs, state, R, s);
 }
 
 size_t fv_residual_work_bytes(int dim, int turb, long nc, long nf, int sweeps, int advection) {

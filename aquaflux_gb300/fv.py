@@ -251,6 +251,23 @@ class FlowCase:
         check(lib().fv_jvp(self._h, ptr(s), ptr(vv), ptr(r), ptr(jv), _stream()))
         return (r, jv) if return_residual else jv
 
+    def linearise(self, state, out: torch.Tensor | None = None) -> torch.Tensor:
+        """``R(state)``, holding the evaluation's face intermediates for :meth:`jvp_linearised`
+        (``fv_linearise``; first-order upwind advection only)."""
+        s = self._vec(state)
+        r = torch.empty_like(s) if out is None else out
+        check(lib().fv_linearise(self._h, ptr(s), ptr(r), _stream()))
+        return r
+
+    def jvp_linearised(self, state, v) -> torch.Tensor:
+        """``J(state) v`` at the state last passed to :meth:`linearise` (``fv_jvp_linearised``:
+        the interior faces' flux tangents from the held intermediates; the same product as
+        :meth:`jvp` within rounding)."""
+        s, vv = self._vec(state), self._vec(v)
+        jv = torch.empty_like(s)
+        check(lib().fv_jvp_linearised(self._h, ptr(s), ptr(vv), 0, ptr(jv), _stream()))
+        return jv
+
     def node_vjp(self, state, w) -> torch.Tensor:
         """``d/dnodes (w . R(state, nodes))``, shape ``(n_nodes, dim)`` (the mesh-coordinate
         adjoint; compact gradient scheme)."""

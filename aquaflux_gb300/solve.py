@@ -343,7 +343,8 @@ def newton_solve(case, state0, *, rtol: float = 1e-10, atol: float = 1e-12, max_
                  refresh_every: int = 1, line_search_steps: int = 10,
                  preconditioner=None, kind: str = "ilu",
                  precond_options: dict | None = None, tangents: int = 64,
-                 refresh_trigger=None, drift_measure=None) -> NewtonResult:
+                 refresh_trigger=None, drift_measure=None,
+                 linearised: bool | None = None) -> NewtonResult:
     """Newton's method with FGMRES, preconditioned by ILU(0) of the materialised Jacobian
     (``kind="ilu"``) or by an ILU(0)-smoothed aggregation V-cycle (``kind="amg"``), in fp32 or
     fp64 (``precision``).
@@ -357,9 +358,16 @@ def newton_solve(case, state0, *, rtol: float = 1e-10, atol: float = 1e-12, max_
     rounding.  The FGMRES bases are allocated once per
     solve (:class:`KrylovWorkspace`).  ``refresh_trigger`` replaces the fixed ``refresh_every``
     schedule: the preconditioner is rebuilt at the first step and then only when the trigger fires
-    on the step history since the last rebuild (see :func:`pseudo_transient_solve`)."""
+    on the step history since the last rebuild (see :func:`pseudo_transient_solve`).
+
+    ``linearised`` (fp64 tangents): the Krylov operator is the linearised JVP
+    (``case.linearise`` at each Newton iterate, the residual evaluations keeping their face
+    intermediates, then ``case.jvp_linearised``; the same product within rounding, ``jax.linearize``
+    rather than ``jax.jvp``).  ``None`` (default) uses it where the case allows it (first-order
+    upwind advection), ``False`` never."""
     if tangents not in (32, 64):
         raise ValueError(f"tangents must be 64 or 32, got {tangents}")
+    from ._lib import FvError
     t_all = time.perf_counter()
     s = torch.as_tensor(state0, dtype=torch.float64, device="cuda").clone()
     if preconditioner is None:
@@ -386,7 +394,19 @@ def newton_solve(case, state0, *, rtol: float = 1e-10, atol: float = 1e-12, max_
         phases[key] += time.perf_counter() - t0
         return out
 
-    r = timed("residual", case.residual, s)
+    lin = tangents == 64 and linearised is not False
+    lin_point = None  # the iterate whose evaluation the case holds for the linearised JVP
+    if lin:
+        try:
+            r = timed("residual", case.linearise, s)
+            lin_point = s
+        except FvError:
+            if linearised:
+                raise
+            lin = False
+    if not lin:
+        r = timed("residual", case.residual, s)
+    evaluate = case.linearise if lin else case.residual
     norms = [kws.norm(r)]
     target = atol + rtol * norms[0]
     its = []
@@ -400,27 +420,37 @@ def newton_solve(case, state0, *, rtol: float = 1e-10, atol: float = 1e-12, max_
             refreshes += 1
             history = []
             drift_fn = drift_measure(s) if drift_measure is not None else None
-        res = timed("krylov", lambda: fgmres(lambda v: case.jvp(s, v, precision=tangents), -r,
-                                             preconditioner.apply,
+        if lin and lin_point is not s:  # the accepted iterate was not the last one evaluated
+            r = timed("residual", case.linearise, s)
+            lin_point = s
+        matvec = ((lambda v: case.jvp_linearised(s, v)) if lin else
+                  (lambda v: case.jvp(s, v, precision=tangents)))
+        res = timed("krylov", lambda: fgmres(matvec, -r, preconditioner.apply,
                                              rtol=linear_rtol, restart=restart,
                                              maxiter=max_krylov, workspace=kws))
         its.append(res.iterations)
         delta = res.x
 
         def search():
+            nonlocal lin_point
             ref = norms[-1]
             best = None
             alpha = 1.0
             for _ in range(line_search_steps + 1):
                 cand = s + alpha * delta
-                rc = case.residual(cand)
+                rc = evaluate(cand)
+                lin_point = cand
                 nc = kws.norm(rc)
                 if math.isfinite(nc):
                     best = (cand, rc, nc) if best is None or nc < best[2] else best
                     if nc < ref:
                         return cand, rc, nc
                 alpha *= 0.5
-            return best if best is not None else (s + alpha * delta, case.residual(s + alpha * delta), float("nan"))
+            if best is not None:
+                return best
+            cand = s + alpha * delta
+            lin_point = cand
+            return cand, evaluate(cand), float("nan")
 
         s, r, nrm = timed("line_search", search)
         norms.append(nrm)

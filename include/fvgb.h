@@ -183,6 +183,18 @@ int fv_eddy_viscosity(FvCase* c, const double* state, double* nut, void* stream)
  * aquaflux/solve/newton.py:110-111.  `residual` (may be NULL) receives R(state).  Device. */
 int fv_jvp(FvCase* c, const double* state, const double* v, double* residual, double* jv,
            void* stream);
+/* The linearised Jacobian-vector product (jax.linearize's split of the reference's
+ * jax.jvp(residual_fn, (phi,), (v,)), aquaflux/solve/newton.py:110-111): fv_linearise evaluates the
+ * residual at `state` (into `residual`, device, may be NULL) and holds the face intermediates and
+ * primal face fluxes of that evaluation; fv_jvp_linearised then gives J(state) v (and the residual)
+ * with the interior faces' flux stage computed from them -- the tangent arithmetic only -- and every
+ * other stage as fv_jvp does.  `state` must be the linearised one.  A change of parameters, of the
+ * viscosity field, of the wall distance or of the geometry (fv_case_refresh_geometry) drops the
+ * linearisation; fv_jvp_linearised then refuses until fv_linearise runs again.  First-order upwind
+ * advection only (a limited reconstruction is refused by fv_linearise). */
+int fv_linearise(FvCase* c, const double* state, double* residual, void* stream);
+int fv_jvp_linearised(FvCase* c, const double* state, const double* v, double* residual,
+                      double* jv, void* stream);
 /* jv = J_direct v: the derivative with the gradients, the SST closure fields and the momentum
  * diagonal a_P held at their values for `state` (a reach-1 operator: the "frozen" Jacobian the
  * preconditioner is built from).  No reference counterpart as an entry point; it is the
