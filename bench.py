@@ -38,7 +38,9 @@ sys.path.insert(0, ROOT)
 METRIC = "Newton-solve s & residual+VJP Gfaces/s at 2M cells: FP32-precond vs FP64, 1 GB300"
 UNIT = "Gfaces/s"
 STEP_DESC = {"vjp": "residual + VJP (hand-written adjoint) at a fixed state",
-             "jvp": "residual + JVP (Krylov operator) at a fixed state"}
+             "jvp": "residual + JVP (dual numbers) at a fixed state",
+             "jvp-linearised": "residual + JVP at a held linearisation (the Newton solve's Krylov "
+                               "operator: fv_linearise once, then fv_jvp_linearised)"}
 CLOCK_QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
                "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
                "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -58,7 +60,7 @@ def _args():
     ap.add_argument("--ilu-sample", type=int, default=48,
                     help="cells per axis of the ILU(0) CPU-vs-GPU sample (0: skip)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--step", default="vjp", choices=["vjp", "jvp"])
+    ap.add_argument("--step", default="vjp", choices=["vjp", "jvp", "jvp-linearised"])
     ap.add_argument("--cell-order", default="coherent", choices=["coherent", "natural"],
                     help="thread-to-cell order of the cell stages (fv_case_set_cell_order): "
                          "grouped by face-list pattern (default) or the mesh's natural order")
@@ -439,7 +441,9 @@ def run_gpu(args, rank: int, world: int, local_rank: int) -> dict | None:
     L = lib()
     stream = torch.cuda.current_stream()
 
-    fn = L.fv_vjp if args.step == "vjp" else L.fv_jvp
+    fn = {"vjp": L.fv_vjp, "jvp": L.fv_jvp, "jvp-linearised": L.fv_jvp_linearised}[args.step]
+    if args.step == "jvp-linearised":
+        case.linearise(state)  # held for every timed step (the same state values throughout)
 
     def step():
         check(fn(case.handle, ptr(state), ptr(vec), ptr(r), ptr(jv), stream.cuda_stream))
@@ -530,8 +534,10 @@ def run_gpu(args, rank: int, world: int, local_rank: int) -> dict | None:
     bpf = step_bytes_per_face(wl, args.step)
     alg_bytes = bpf * F
     kname = {"vjp": "a_flux<3, SST> (adjoint face fluxes)",
-             "jvp": "k_flux<Dual, 3, SST> (JVP face fluxes)"}[args.step]
-    kstage, tkey = {"vjp": ("a_flux", "a_flux"), "jvp": ("flux", "k_flux_dual")}[args.step]
+             "jvp": "k_flux<Dual, 3, SST> (JVP face fluxes)",
+             "jvp-linearised": "k_flux_tangent<3, SST> (JVP face-flux tangents)"}[args.step]
+    kstage, tkey = {"vjp": ("a_flux", "a_flux"), "jvp": ("flux", "k_flux_dual"),
+                    "jvp-linearised": ("flux", "k_flux_tangent")}[args.step]
     k_avg_ms = stage_ms[kstage] / max(runs, 1)
     achieved = alg_bytes / (k_avg_ms * 1e-3) / 1e9
     step_gbs = alg_bytes / (ms / args.steps * 1e-3) / 1e9
@@ -547,10 +553,13 @@ def run_gpu(args, rank: int, world: int, local_rank: int) -> dict | None:
     # step's time, against 2 instructions per clock per SM at the sampled SM clock
     fp64_roof = None
     instr_path = os.path.join(ROOT, "profiles", "fp64_instructions.json")
+    per_face = None
     if os.path.exists(instr_path):
         with open(instr_path) as f:
             ins = json.load(f)
-        per_face = ins["vjp_step_instr_per_face" if args.step == "vjp" else "jvp_step_instr_per_face"]
+        per_face = ins.get({"vjp": "vjp_step_instr_per_face", "jvp": "jvp_step_instr_per_face",
+                            "jvp-linearised": "jvp_linearised_step_instr_per_face"}[args.step])
+    if per_face:
         mhz = clk.get("sm_mhz") or 2070.0
         peak_gi = ins["pipe_instr_per_clock_per_sm"] * ins["sms"] * mhz * 1e6 / 1e9
         ach_gi = per_face * F / (ms / args.steps * 1e-3) / 1e9
@@ -559,7 +568,8 @@ def run_gpu(args, rank: int, world: int, local_rank: int) -> dict | None:
                      "frac": round(ach_gi / peak_gi, 4),
                      "bound_gfaces_s": round(peak_gi / per_face, 4),
                      "source": "profiles/fp64_%s_channel3d_64.md (ncu, 64^3)"
-                               % ("residual_vjp" if args.step == "vjp" else "jvp")}
+                               % {"vjp": "residual_vjp", "jvp": "jvp",
+                                  "jvp-linearised": "jvp_linearised"}[args.step]}
     out = {
         "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4),
@@ -579,7 +589,9 @@ def run_gpu(args, rank: int, world: int, local_rank: int) -> dict | None:
                 "copies": "every step's inputs in and results out over pinned host memory, "
                           "overlapping the neighbouring steps' compute (double-buffered, "
                           "three streams)"},
-        "gpu_launches": (6 + (5 if args.step == "vjp" else 0)) * args.steps,
+        # stage kernels per step: 6 forward (+ 5 adjoint for the VJP; + the boundary faces'
+        # coefficient and flux launches of the linearised JVP)
+        "gpu_launches": (6 + {"vjp": 5, "jvp": 0, "jvp-linearised": 2}[args.step]) * args.steps,
         "stage_ms_per_step": {k: round(v / max(runs, 1), 4) for k, v in stage_ms.items()},
         "algorithmic_bytes_per_face": round(bpf, 2),
         "roofline": {"bound": "hbm", "kernel": kname, "dominant_stage": dom,
@@ -683,6 +695,31 @@ def newton_block(args, wl, case) -> dict:
             jt["n_probes"] = jac.n_probes
         del jac
     out["jacobian_ms"] = jt
+    # the Krylov operator at the plug-flow state: the dual-number JVP, the linearisation (one
+    # residual keeping its face intermediates) and the linearised JVP the fp64-tangent forms use
+    v0 = torch.randn(s0.numel(), dtype=torch.float64, device="cuda",
+                     generator=torch.Generator(device="cuda").manual_seed(3))
+
+    def per_call_ms(fn, k=20):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(k):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return round(e0.elapsed_time(e1) / k, 3)
+
+    kops = {"jvp_dual_numbers": per_call_ms(lambda: case.jvp(s0, v0)),
+            "jvp_fp32_tangents": per_call_ms(lambda: case.jvp(s0, v0, precision=32)),
+            "linearise": per_call_ms(lambda: case.linearise(s0))}
+    kops["jvp_linearised"] = per_call_ms(lambda: case.jvp_linearised(s0, v0))
+    ref = case.jvp(s0, v0)
+    kops["linearised_max_rel_diff"] = float((case.jvp_linearised(s0, v0) - ref).abs().max()
+                                            / ref.abs().max())
+    out["krylov_operator_ms"] = kops
     # untimed warm-up of every solver path on a small channel (library initialisation, graph
     # captures), so that the timed solves below measure steady-state work
     from aquaflux_gb300 import workloads
