@@ -58,6 +58,8 @@ SIGNATURES = {
     "fv_probe_jacobian": (c_int, [P, P, c_int, P, c_int, P, P, P, P]),
     "fv_jvp_batch": (c_int, [P, P, P, c_int, P, P]),
     "fv_node_vjp": (c_int, [P, P, P, P, P]),
+    "fv_hold_forward": (c_int, [P, P, P, P]),
+    "fv_vjp_held": (c_int, [P, P, P, P, P]),
     "fv_case_set_viscosity_field": (c_int, [P, P, P]),
     "fv_case_set_block_size": (c_int, [P, c_int]),
     "fv_case_set_persistent": (c_int, [P, c_int, c_int, c_int]),

@@ -165,6 +165,7 @@ int assemble_frozen(FvCase* cs, const double* state, const int* indptr, const in
   const CaseView& cv = cs->view;
   const long nc = m.nc, nf = m.nf;
   constexpr int NF = Layout<DIM, TURB>::NFLD;
+  cs->fwd_valid = 0;  // the workspace is about to hold this pass
   Work<T> w = work_layout<T, DIM, TURB>(cs->work, nc, nf, psi_count<DIM, TURB>(cs));
   const S* sv;  // the state in the pass's precision
   if constexpr (std::is_same<S, float>::value) {

@@ -394,6 +394,7 @@ extern "C" int fv_case_set_params(FvCase* c, double mu, double inlet_scale) {
   c->mu = mu;
   c->inlet_scale = inlet_scale;
   c->lin_valid = 0;
+  c->fwd_valid = 0;
   return FV_OK;
 }
 
@@ -403,6 +404,7 @@ extern "C" int fv_case_set_viscosity_field(FvCase* c, const double* mu_cell, voi
     return FV_ERR_ARG;
   }
   c->lin_valid = 0;
+  c->fwd_valid = 0;
   if (!mu_cell) {
     c->view.mu_cell = nullptr;
     return FV_OK;
@@ -580,6 +582,7 @@ extern "C" int fv_case_refresh_geometry(FvCase* c, void* stream) {
     return FV_ERR_ARG;
   }
   c->lin_valid = 0;
+  c->fwd_valid = 0;
   if (!c->desc.turbulent) return FV_OK;
   if (c->wd_external) {
     fv_set_error("fv_case_refresh_geometry: the wall distance was set by the caller "
@@ -611,6 +614,7 @@ extern "C" int fv_case_set_wall_distance(FvCase* c, const double* distance, void
   cudaStream_t s = (cudaStream_t)stream;
   FvMesh* m = c->mesh;
   c->lin_valid = 0;
+  c->fwd_valid = 0;
   FV_CUDA_TRY(cudaMemcpyAsync(c->wd, distance, sizeof(double) * m->nc, cudaMemcpyDeviceToDevice, s));
   int rc = fv_wall_distance_gradient(m, c->swall, c->wd, c->wdg, c->desc.gradient_sweeps,
                                      c->desc.gradient_relaxation, s);
@@ -873,6 +877,27 @@ extern "C" int fv_vjp(FvCase* c, const double* state, const double* w, double* r
   }
   cudaStream_t s = (cudaStream_t)stream;
   int rc = fv_case_vjp_run(c, physical_state(c, state, s), w, residual, vjp, s);
+  if (rc == FV_OK) chain_state(c, vjp, s);
+  return rc;
+}
+
+extern "C" int fv_hold_forward(FvCase* c, const double* state, double* residual, void* stream) {
+  if (!c || !state) {
+    fv_set_error("fv_hold_forward: bad arguments");
+    return FV_ERR_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  return fv_case_hold_forward(c, physical_state(c, state, s), residual, s);
+}
+
+extern "C" int fv_vjp_held(FvCase* c, const double* state, const double* w, double* vjp,
+                           void* stream) {
+  if (!c || !state || !w || !vjp) {
+    fv_set_error("fv_vjp_held: bad arguments");
+    return FV_ERR_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  int rc = fv_case_vjp_held(c, physical_state(c, state, s), w, vjp, s);
   if (rc == FV_OK) chain_state(c, vjp, s);
   return rc;
 }

@@ -161,6 +161,7 @@ struct FvCase {
   double* lin_g = nullptr;      // ... its gradients (nfld, dim, nc)
   int lin_valid = 0;            // a linearisation is held (parameter / geometry changes clear it)
   int lin_use = 0;              // the running dual-number pass takes its flux stage from it
+  int fwd_valid = 0;            // work / aux hold the double forward pass of the last VJP's state
   double* mu_cell = nullptr;    // (nc) per-cell viscosity field (laminar batched instances)
   double* flx = nullptr;        // (nfld, nf) weights of a face-flux functional (internal order)
   bool flx_active = false;      // the adjoints add flx to their face-flux cotangents
@@ -195,6 +196,10 @@ int fv_case_vjp_run(FvCase* c, const double* state, const double* w, double* res
 // The residual at a (physical) state with its face intermediates and primal face fluxes kept for
 // the linearised JVP (residual.cu); refuses limited reconstruction.
 int fv_case_linearise(FvCase* c, const double* state, double* residual, cudaStream_t s);
+// The VJP's forward pass at a (physical) state, held in the workspace for fv_case_vjp_held, which
+// runs only the adjoint stages (residual.cu).  Any other evaluation drops the hold.
+int fv_case_hold_forward(FvCase* c, const double* state, double* residual, cudaStream_t s);
+int fv_case_vjp_held(FvCase* c, const double* state, const double* w, double* out, cudaStream_t s);
 // Frozen reach-1 Jacobian by per-face forward-mode derivatives (residual.cu); D holds
 // fv_jac_face_bytes.
 // Mesh-coordinate adjoint dL/dnodes of L = w . R(state, nodes) (residual.cu).

@@ -1141,6 +1141,7 @@ int face_functional(FvCase* cs, const double* state, const double* wref, int vis
     for (int i = 0; i < 2; ++i) {
       rc = fv_case_run(cs, state, nullptr, kinds[i], nullptr, cs->tmp2, s);
       if (rc != FV_OK) return rc;
+      cs->fwd_valid = 0;  // the workspace is about to hold a dual-number pass
       Work<Dual> dw = work_layout<Dual, DIM, TURB>(cs->work, nc, nf, psi_count<DIM, TURB>(cs));
       k_functional_partial<DIM, TURB, Dual><<<kFnBlocks, 256, 0, s>>>(m, cv, state, cs->flx, dw.FL,
                                                                       0, 1, cs->red);

@@ -1435,6 +1435,7 @@ int run(FvCase* cs, Src<T> st, Par<T> par, double* R, double* JV, cudaStream_t s
   const MeshView& m = cs->mesh->view;
   const CaseView& cv = cs->view;
   const long nc = m.nc, nf = m.nf;
+  cs->fwd_valid = 0;  // the workspace is about to hold this pass
   Work<T> w = work_layout<T, DIM, TURB>(cs->work, nc, nf, psi_count<DIM, TURB>(cs));
   // each stage at its own block size (the index is the stage's profiling mark)
   const int* tb = cs->tbs;
@@ -1674,17 +1675,33 @@ int run_vjp_persistent(FvCase* cs, const double* state, const double* W, double*
 // scheme's backward sweeps overwrite it (the mesh-coordinate adjoint re-runs them).
 template <int DIM, bool TURB>
 int run_vjp(FvCase* cs, const double* state, const double* W, double* R, double* out,
-            cudaStream_t s, double* gb_save = nullptr) {
-  if (cs->persistent && !gb_save && persistent_supported(cs))
+            cudaStream_t s, double* gb_save = nullptr, bool held = false) {
+  if (held) {
+    if (!cs->fwd_valid) {
+      fv_set_error("fv_vjp_held: no forward pass held; call fv_hold_forward at this state (again "
+                   "after any other evaluation or a parameter, viscosity-field, wall-distance or "
+                   "geometry change)");
+      return FV_ERR_ARG;
+    }
+  } else if (cs->persistent && !gb_save && persistent_supported(cs)) {
+    cs->fwd_valid = 0;
     return run_vjp_persistent<DIM, TURB>(cs, state, W, R, out, s);
+  }
   using L = Layout<DIM, TURB>;
   const MeshView& m = cs->mesh->view;
   const CaseView& cv = cs->view;
   const long nc = m.nc, nf = m.nf;
   Src<double> st{state};
   Par<double> par{cs->mu, cs->inlet_scale, cs->mu / cs->desc.rho};
-  int rc = run<double, DIM, TURB>(cs, st, par, R ? R : cs->tmp, nullptr, s, false, false, cs->aux);
-  if (rc != FV_OK) return rc;
+  if (held) {
+    // the forward stages' profiling marks at one instant: they took no time in this call
+    for (int k = 0; k <= 6; ++k) fv_prof_mark(cs, k, s);
+  } else {
+    int rc = run<double, DIM, TURB>(cs, st, par, R ? R : cs->tmp, nullptr, s, false, false,
+                                    cs->aux);
+    if (rc != FV_OK) return rc;
+    cs->fwd_valid = 1;  // the adjoint stages below read but do not change it
+  }
   // forward workspace (double layout, as written by run<double>)
   Work<double> fw = work_layout<double, DIM, TURB>(cs->work, nc, nf, psi_count<DIM, TURB>(cs));
   double* G = fw.G;
@@ -1761,6 +1778,40 @@ int fv_case_vjp_run(FvCase* cs, const double* state, const double* W, double* R,
   if (dim == 2)
     return turb ? run_vjp<2, true>(cs, state, W, R, out, s) : run_vjp<2, false>(cs, state, W, R, out, s);
   return turb ? run_vjp<3, true>(cs, state, W, R, out, s) : run_vjp<3, false>(cs, state, W, R, out, s);
+}
+
+namespace {
+template <int DIM, bool TURB>
+int hold_forward(FvCase* cs, const double* state, double* R, cudaStream_t s) {
+  Par<double> par{cs->mu, cs->inlet_scale, cs->mu / cs->desc.rho};
+  int rc = run<double, DIM, TURB>(cs, Src<double>{state}, par, R ? R : cs->tmp, nullptr, s, false,
+                                  true, cs->aux);
+  if (rc == FV_OK) cs->fwd_valid = 1;
+  return rc;
+}
+}  // namespace
+
+int fv_case_hold_forward(FvCase* cs, const double* state, double* R, cudaStream_t s) {
+  if (cs->wd_missing) {
+    fv_set_error("turbulent case without SST wall faces: set its wall distance first "
+                 "(fv_case_set_wall_distance)");
+    return FV_ERR_ARG;
+  }
+  const int dim = cs->mesh->dim;
+  const bool turb = cs->desc.turbulent != 0;
+  if (dim == 2) return turb ? hold_forward<2, true>(cs, state, R, s) : hold_forward<2, false>(cs, state, R, s);
+  return turb ? hold_forward<3, true>(cs, state, R, s) : hold_forward<3, false>(cs, state, R, s);
+}
+
+int fv_case_vjp_held(FvCase* cs, const double* state, const double* W, double* out,
+                     cudaStream_t s) {
+  const int dim = cs->mesh->dim;
+  const bool turb = cs->desc.turbulent != 0;
+  if (dim == 2)
+    return turb ? run_vjp<2, true>(cs, state, W, nullptr, out, s, nullptr, true)
+                : run_vjp<2, false>(cs, state, W, nullptr, out, s, nullptr, true);
+  return turb ? run_vjp<3, true>(cs, state, W, nullptr, out, s, nullptr, true)
+              : run_vjp<3, false>(cs, state, W, nullptr, out, s, nullptr, true);
 }
 
 namespace {

@@ -268,6 +268,21 @@ class FlowCase:
         check(lib().fv_jvp_linearised(self._h, ptr(s), ptr(vv), 0, ptr(jv), _stream()))
         return jv
 
+    def hold_forward(self, state, out: torch.Tensor | None = None) -> torch.Tensor:
+        """``R(state)``, holding the VJP's forward pass for :meth:`vjp_held` (``fv_hold_forward``)."""
+        s = self._vec(state)
+        r = torch.empty_like(s) if out is None else out
+        check(lib().fv_hold_forward(self._h, ptr(s), ptr(r), _stream()))
+        return r
+
+    def vjp_held(self, state, w) -> torch.Tensor:
+        """``w^T J(state)`` by the adjoint stages alone, at the state of the held forward pass
+        (``fv_vjp_held``; bitwise :meth:`vjp`)."""
+        s, ww = self._vec(state), self._vec(w)
+        out = torch.empty_like(s)
+        check(lib().fv_vjp_held(self._h, ptr(s), ptr(ww), ptr(out), _stream()))
+        return out
+
     def node_vjp(self, state, w) -> torch.Tensor:
         """``d/dnodes (w . R(state, nodes))``, shape ``(n_nodes, dim)`` (the mesh-coordinate
         adjoint; compact gradient scheme)."""

@@ -554,7 +554,7 @@ def implicit_adjoint(case, state, g, *, rtol: float = 1e-10, precision: int = 64
                      preconditioner=None) -> AdjointResult:
     """Implicit-function-theorem gradient at a converged root (``_implicit_solve_bwd``,
     ``aquaflux/solve/implicit.py:733-761``): solve ``J^T lam = g`` with FGMRES on the hand-written
-    VJP and the transposed ILU(0) preconditioner (the reference's tight 1e-10 adjoint solve,
+    VJP (its forward pass held once, ``case.hold_forward``) and the transposed ILU(0) preconditioner (the reference's tight 1e-10 adjoint solve,
     ``aquaflux/solve/linear.py:40-42``), then ``dL/dtheta = -lam^T dR/dtheta`` for
     ``theta = (mu, inlet_scale)``.  ``preconditioner``: any with ``refresh`` and
     ``apply_transpose`` (ILU(0) by default; the AMG V-cycle has an exact transpose too)."""
@@ -564,7 +564,10 @@ def implicit_adjoint(case, state, g, *, rtol: float = 1e-10, precision: int = 64
         preconditioner = IluPreconditioner(BlockJacobian(case, reach=1, frozen=True), precision)
     preconditioner.refresh(s)
     mt = TransposedPreconditioner(preconditioner)
-    res = fgmres(lambda w: case.vjp(s, w), gv, mt.apply, rtol=rtol, restart=restart,
+    # the forward pass held once (the preconditioner's refresh above is the last other evaluation):
+    # every Krylov product then runs the adjoint stages only
+    case.hold_forward(s)
+    res = fgmres(lambda w: case.vjp_held(s, w), gv, mt.apply, rtol=rtol, restart=restart,
                  maxiter=max_krylov)
     dparams = -case.param_vjp(s, res.x)
     return AdjointResult(res.x, dparams, res.iterations, res.converged)

@@ -246,6 +246,16 @@ int fv_vjp(FvCase* c, const double* state, const double* w, double* residual, do
 /* Parameter cotangents w^T dR/dtheta for theta = (mu, inlet_scale): the vjp_theta of
  * aquaflux/solve/implicit.py:759-760.  `out` is a device array of 2 doubles. */
 int fv_param_vjp(FvCase* c, const double* state, const double* w, double* out, void* stream);
+/* The VJP's forward pass held for repeated products at one state (the adjoint solve's operator
+ * w -> J^T w: aquaflux/solve/implicit.py:733-761 applies jax.vjp's pullback, built once, at every
+ * Krylov step): fv_hold_forward evaluates the residual at `state` (into `residual`, may be NULL)
+ * keeping the forward intermediates the adjoint stages read; fv_vjp_held then runs the adjoint
+ * stages only -- bitwise fv_vjp's result.  `state` must be the held one.  Any other evaluation on
+ * the case (residual, JVP, Jacobian assembly, node adjoint ...) or a parameter, viscosity-field,
+ * wall-distance or geometry change drops the hold; fv_vjp_held then refuses.  fv_vjp itself leaves
+ * its forward pass held. */
+int fv_hold_forward(FvCase* c, const double* state, double* residual, void* stream);
+int fv_vjp_held(FvCase* c, const double* state, const double* w, double* vjp, void* stream);
 /* dnodes = d/dnodes (w . R(state, nodes)): the mesh-coordinate adjoint (the node-coordinate part
  * of theta_bar in _implicit_solve_bwd, aquaflux/solve/implicit.py:733-761), through the face
  * areas, normals and centroids, the cell volumes and centroids, every factor derived from them and

@@ -1,6 +1,8 @@
-"""The linearised JVP (``fv_linearise`` + ``fv_jvp_linearised``: the interior faces' flux tangents
-from the face intermediates a held residual evaluation kept) against the dual-number JVP, on every
-first-order-upwind reference case; its refusals; Newton on it."""
+"""Products at a held evaluation: the linearised JVP (``fv_linearise`` + ``fv_jvp_linearised``:
+tangent-only flux, coefficient and gradient stages from the intermediates a held residual
+evaluation kept) against the dual-number JVP on every first-order-upwind reference case, and the
+held-forward VJP (``fv_hold_forward`` + ``fv_vjp_held``) bitwise against ``fv_vjp``; their
+refusals; Newton and the IFT adjoint on them."""
 from __future__ import annotations
 
 import numpy as np
@@ -64,3 +66,63 @@ def test_newton_on_the_linearised_jvp_reaches_the_dual_number_root():
     assert a.converged and b.converged and a.steps == b.steps
     diff = (a.state - b.state).abs().max() / b.state.abs().max()
     assert float(diff) <= 1e-9
+
+
+@pytest.mark.parametrize("name", ["cavj", "lam3", "sst3", "csst3", "lcavj", "bsst3", "psst2"])
+def test_held_forward_vjp_is_bitwise_the_vjp(name):
+    """fv_hold_forward + fv_vjp_held: the adjoint stages alone on the held forward pass give
+    bitwise fv_vjp's product (every scheme: corrected gradients, limited reconstruction, log
+    scalars), repeatedly."""
+    from aquaflux_gb300._lib import FvError
+
+    fc, case, d, p = device_case(name)
+    s = d[p + "states"][0]
+    rng = np.random.default_rng(17)
+    r = fc.hold_forward(s)
+    assert torch.equal(r, fc.residual(s))
+    with pytest.raises(FvError):  # the residual evaluation dropped the hold
+        fc.vjp_held(s, np.ones(s.size))
+    fc.hold_forward(s)
+    for _ in range(2):
+        w = rng.standard_normal(s.size)
+        got = fc.vjp_held(s, w)
+        assert torch.equal(got, fc.vjp(s, w))  # fv_vjp leaves its forward pass held
+
+
+def test_held_forward_refusals():
+    from aquaflux_gb300._lib import FvError
+
+    fc, case, d, p = device_case("sst2")
+    s = d[p + "states"][0]
+    w = np.ones(s.size)
+    with pytest.raises(FvError):  # nothing held yet
+        fc.vjp_held(s, w)
+    fc.hold_forward(s)
+    fc.vjp_held(s, w)
+    fc.jvp(s, w)  # another evaluation overwrites the held pass
+    with pytest.raises(FvError):
+        fc.vjp_held(s, w)
+    fc.hold_forward(s)
+    fc.set_params(mu=fc.mu * 1.1)
+    with pytest.raises(FvError):
+        fc.vjp_held(s, w)
+
+
+def test_implicit_adjoint_on_the_held_forward_pass():
+    """The IFT adjoint solve (now on the held forward pass) equals FGMRES on plain VJPs bitwise."""
+    from aquaflux_gb300 import workloads
+    from aquaflux_gb300.solve import (BlockJacobian, IluPreconditioner, TransposedPreconditioner,
+                                      fgmres, implicit_adjoint, newton_solve)
+
+    wl = workloads.channel3d(8, renumber=False)
+    case = wl.device_case()
+    root = newton_solve(case, wl.initial_state(), precision=64, rtol=1e-12).state
+    g = torch.randn(case.n_unknowns, dtype=torch.float64, device="cuda",
+                    generator=torch.Generator(device="cuda").manual_seed(5))
+    a = implicit_adjoint(case, root, g, rtol=1e-10)
+    pc = IluPreconditioner(BlockJacobian(case, reach=1, frozen=True), 64)
+    pc.refresh(root)
+    b = fgmres(lambda w: case.vjp(root, w), g, TransposedPreconditioner(pc).apply, rtol=1e-10,
+               restart=30, maxiter=1000)
+    assert a.converged and a.krylov_iterations == b.iterations
+    assert torch.equal(a.lam, b.x)
