@@ -296,10 +296,10 @@ class AmgPreconditioner:
     iterations, each V-cycle ~4x cheaper), and the natural order in 2D, where the coloured smoother
     stalls on laminar saddle-point systems.  Coarse levels are always colour-numbered.
 
-    ``graph=True`` (default) replays the forward V-cycle as one CUDA graph, captured on the
-    second application after each re-form of the fine operator's storage: the coarse levels are
+    ``graph=True`` (default) replays the V-cycle as one CUDA graph, captured on the second
+    application after each re-form of the fine operator's storage: the coarse levels are
     hundreds of launches of a few microseconds each, which the host would otherwise issue one by
-    one.  The transposed cycle runs eagerly.
+    one.  The forward and the transposed cycle (the IFT adjoint's) keep a graph each.
     """
 
     def __init__(self, jac, precision: int = 32, *, fine_order: str = "auto", shift=None,
@@ -363,7 +363,10 @@ class AmgPreconditioner:
         self._f64 = int(precision == 64)
         self._b = torch.empty(n * b, dtype=self.h.levels[0].x.dtype, device="cuda")
         self.graph = bool(graph)
-        self._graph = self._graph_key = self._eager_key = None
+        # per direction (False: forward, True: transposed): the captured cycle and the fine
+        # storage address it was captured on, and the address of the last eager cycle
+        self._graphs: dict = {}
+        self._eager_keys: dict = {}
 
     def _form(self, values):
         if self.op is not None:
@@ -396,18 +399,21 @@ class AmgPreconditioner:
         return out
 
     def _vcycle(self, transpose: bool) -> torch.Tensor:
-        """The V-cycle on ``self._b`` into the fine level's ``x``: eager, or a graph replay.
-        Under a caller's own stream capture the cycle is recorded eagerly into that graph."""
-        if transpose or not self.graph or torch.cuda.is_current_stream_capturing():
+        """The V-cycle (or its transpose) on ``self._b`` into the fine level's ``x``: eager, or a
+        graph replay.  Under a caller's own stream capture the cycle is recorded eagerly into that
+        graph."""
+        if not self.graph or torch.cuda.is_current_stream_capturing():
             return self.h.vcycle(0, self._b, transpose)
         # the graph holds the fine operator's storage address (an fp64 fine level may hold the
         # Jacobian's own tensor): re-capture when it changes, after one eager cycle that builds
-        # the smoothers' solve structures outside the capture
+        # the smoothers' (transposed) solve structures and the transposed products' maps outside
+        # the capture
         key = self.h.levels[0].values.data_ptr()
-        if self._graph is None or self._graph_key != key:
-            if self._eager_key != key:
-                self._eager_key = key
-                return self.h.vcycle(0, self._b)
+        held = self._graphs.get(transpose)
+        if held is None or held[1] != key:
+            if self._eager_keys.get(transpose) != key:
+                self._eager_keys[transpose] = key
+                return self.h.vcycle(0, self._b, transpose)
             # captured on a side stream through capture_begin / capture_end: the torch.cuda.graph
             # context manager would empty the caching allocator at every capture, and the next
             # solve would then re-allocate its multi-GB bases and levels from the driver
@@ -418,12 +424,12 @@ class AmgPreconditioner:
             with torch.cuda.stream(side):
                 g.capture_begin()
                 try:
-                    self.h.vcycle(0, self._b)
+                    self.h.vcycle(0, self._b, transpose)
                 finally:
                     g.capture_end()
             main.wait_stream(side)
-            self._graph, self._graph_key = g, key
-        self._graph.replay()
+            held = self._graphs[transpose] = (g, key)
+        held[0].replay()
         return self.h.levels[0].x
 
     def apply_transpose(self, r: torch.Tensor) -> torch.Tensor:

@@ -135,6 +135,42 @@ __global__ void k_bsr_spmv_t(int nbc, int b, const int* __restrict__ tptr, const
   y[r] = acc;
 }
 
+// The same transposed product with a compile-time block size: the same products accumulated in
+// the same order (bitwise the runtime-size kernel's result), the loops unrolled.
+template <class V, int B>
+__global__ void k_bsr_spmv_tb(int nbc, const int* __restrict__ tptr, const int* __restrict__ tidx,
+                              const int* __restrict__ tblk, const V* __restrict__ val,
+                              const V* __restrict__ x, V* __restrict__ y) {
+  const long r = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= (long)nbc * B) return;
+  const int j = (int)(r / B), a = (int)(r % B);
+  constexpr long BB = (long)B * B;
+  V acc = 0;
+  for (int q = tptr[j]; q < tptr[j + 1]; ++q) {
+    const V* blk = val + (long)tblk[q] * BB + a;
+    V xs[B];
+    load_seg<B>(x + (long)tidx[q] * B, xs);
+#pragma unroll
+    for (int c = 0; c < B; ++c) acc += blk[(long)c * B] * xs[c];
+  }
+  y[r] = acc;
+}
+
+// y = A^T x through a device transpose map, the compile-time-size kernel for b in 2 .. 8 (x
+// 16-byte aligned: its segments are read with vector loads).
+template <class V>
+void launch_spmv_t(int n, int b, const int* tp, const int* ti, const int* tb, const V* values,
+                   const V* x, V* y, cudaStream_t s) {
+  const long rows = (long)n * b;
+  if (b >= 2 && b <= 8 && (uintptr_t)x % 16 == 0)
+    with_block_size(b, [&](auto B) {
+      k_bsr_spmv_tb<V, B()><<<fv_blocks(rows, kThreads), kThreads, 0, s>>>(n, tp, ti, tb, values,
+                                                                           x, y);
+    });
+  else
+    k_bsr_spmv_t<V><<<fv_blocks(rows, kThreads), kThreads, 0, s>>>(n, b, tp, ti, tb, values, x, y);
+}
+
 // Host-built transpose of a BSR pattern (cached per pattern pointer for the SpMV entry points).
 struct Transpose {
   std::vector<int> ptr, idx, blk;
@@ -572,59 +608,101 @@ __global__ void k_ilu_lower_upper_lg(IluView<V> F, const int* rows, int count, V
   if (live) y[(long)i * B + a] = acc;
 }
 
-template <class V>
+// The in-block lower solve of U^T's diagonal block D^T (lane a holds entry a of the right-hand
+// side, Dc the lane's column of D: Dc[c] = D(c, a)): step c divides entry c by its pivot D(c, c),
+// then every later entry a > c takes -D(c, a) times it.  The division is the reciprocal quotient
+// of upper_block_solve (every lane's reciprocal formed up front, one fused correction: the
+// correctly rounded quotient, the same value as the division).
+template <class V, int B>
+__device__ __forceinline__ V lower_t_block_solve(V acc, const V (&Dc)[B], int a, bool live,
+                                                 unsigned mask) {
+  V piv = V(1);
+#pragma unroll
+  for (int c = 0; c < B; ++c)
+    if (a == c) piv = Dc[c];
+  const V rpiv = V(1) / piv;
+  const bool rfin = isfinite(rpiv);
+#pragma unroll
+  for (int c = 0; c < B; ++c) {
+    if (a == c) {
+      if (rfin) {
+        const V q = acc * rpiv;
+        acc = fma_rn(fma_rn(-q, piv, acc), rpiv, q);
+      } else {
+        acc = acc / piv;
+      }
+    }
+    const V vc = __shfl_sync(mask, acc, c, FV_LG);
+    if (live && a > c) acc -= Dc[c] * vc;
+  }
+  return acc;
+}
+
+// Forward sweep of one level of the transposed solve, U^T z = r: block row i of U^T gathers the
+// blocks (j, i) of U, j < i, through the transpose map (column a of each block for lane a), in
+// the map's ascending-row order, then the in-block lower solve with D^T.
+template <class V, int B>
 __global__ void k_ilu_upper_t_lg(IluView<V> F, const int* tptr, const int* tidx, const int* tblk,
                                  const int* rows, int count, V* z) {
   const int gid = (blockIdx.x * blockDim.x + threadIdx.x) / FV_LG;
   const int a = threadIdx.x & (FV_LG - 1);
   if (gid >= count) return;
   const unsigned mask = lg_mask();
-  const int i = rows[gid], b = F.b;
-  const bool live = a < b;
-  const long bb = (long)b * b;
-  V acc = live ? z[(long)i * b + a] : V(0);
+  const int i = rows[gid];
+  const bool live = a < B;
+  constexpr long BB = (long)B * B;
+  V acc = live ? z[(long)i * B + a] : V(0);
   if (live)
     for (int q = tptr[i]; q < tptr[i + 1]; ++q) {
       const int j = tidx[q];
       if (j >= i) continue;
-      const V* U = F.val + (long)tblk[q] * bb;  // block (j, i)
-      const V* zj = z + (long)j * b;
-      for (int c = 0; c < b; ++c) acc -= U[(long)c * b + a] * zj[c];
+      const V* U = F.val + (long)tblk[q] * BB + a;  // column a of block (j, i)
+      V zj[B];
+      load_seg<B>(z + (long)j * B, zj);
+#pragma unroll
+      for (int c = 0; c < B; ++c) acc -= U[(long)c * B] * zj[c];
     }
-  const V* D = F.val + (long)F.diag[i] * bb;
-  for (int c = 0; c < b; ++c) {
-    if (a == c) acc = acc / D[(long)c * b + c];
-    const V vc = __shfl_sync(mask, acc, c, FV_LG);
-    if (live && a > c) acc -= D[(long)c * b + a] * vc;
-  }
-  if (live) z[(long)i * b + a] = acc;
+  V Dc[B];
+  const V* D = F.val + (long)F.diag[i] * BB + a;
+#pragma unroll
+  for (int c = 0; c < B; ++c) Dc[c] = live ? D[(long)c * B] : V(0);
+  acc = lower_t_block_solve<V, B>(acc, Dc, a, live, mask);
+  if (live) z[(long)i * B + a] = acc;
 }
 
-template <class V>
+// Backward sweep of one level of the transposed solve, L^T x = z (unit diagonal): the blocks
+// (k, i) of L, k > i, in descending-row order, then the in-block unit upper solve.
+template <class V, int B>
 __global__ void k_ilu_lower_t_lg(IluView<V> F, const int* tptr, const int* tidx, const int* tblk,
                                  const int* rows, int count, V* x) {
   const int gid = (blockIdx.x * blockDim.x + threadIdx.x) / FV_LG;
   const int a = threadIdx.x & (FV_LG - 1);
   if (gid >= count) return;
   const unsigned mask = lg_mask();
-  const int i = rows[gid], b = F.b;
-  const bool live = a < b;
-  const long bb = (long)b * b;
-  V acc = live ? x[(long)i * b + a] : V(0);
+  const int i = rows[gid];
+  const bool live = a < B;
+  constexpr long BB = (long)B * B;
+  V acc = live ? x[(long)i * B + a] : V(0);
   if (live)
     for (int q = tptr[i + 1] - 1; q >= tptr[i]; --q) {
       const int k = tidx[q];
       if (k <= i) continue;
-      const V* L = F.val + (long)tblk[q] * bb;  // block (k, i)
-      const V* xk = x + (long)k * b;
-      for (int c = b - 1; c >= 0; --c) acc -= L[(long)c * b + a] * xk[c];
+      const V* L = F.val + (long)tblk[q] * BB + a;  // column a of block (k, i)
+      V xk[B];
+      load_seg<B>(x + (long)k * B, xk);
+#pragma unroll
+      for (int c = B - 1; c >= 0; --c) acc -= L[(long)c * B] * xk[c];
     }
-  const V* D = F.val + (long)F.diag[i] * bb;
-  for (int c = b - 1; c >= 0; --c) {
+  V Dc[B];
+  const V* D = F.val + (long)F.diag[i] * BB + a;
+#pragma unroll
+  for (int c = 0; c < B; ++c) Dc[c] = live ? D[(long)c * B] : V(0);
+#pragma unroll
+  for (int c = B - 1; c >= 0; --c) {
     const V vc = __shfl_sync(mask, acc, c, FV_LG);
-    if (live && a < c) acc -= D[(long)c * b + a] * vc;
+    if (live && a < c) acc -= Dc[c] * vc;
   }
-  if (live) x[(long)i * b + a] = acc;
+  if (live) x[(long)i * B + a] = acc;
 }
 
 template <class V>
@@ -779,14 +857,22 @@ void launch_apply_levels(FvIlu0* f, int transpose, V* x, cudaStream_t s) {
       const int cnt = f->lv_tfwd[l + 1] - f->lv_tfwd[l];
       if (!cnt) continue;
       const int* rows = f->rows_tfwd + f->lv_tfwd[l];
-      if (lg) k_ilu_upper_t_lg<V><<<grid(cnt), 128, 0, s>>>(F, f->tptr, f->tidx, f->tblk, rows, cnt, x);
+      if (lg)
+        with_block_size(f->b, [&](auto B) {
+          k_ilu_upper_t_lg<V, B()><<<grid(cnt), 128, 0, s>>>(F, f->tptr, f->tidx, f->tblk, rows,
+                                                             cnt, x);
+        });
       else k_ilu_upper_t<V><<<grid(cnt), 128, 0, s>>>(F, f->tptr, f->tidx, f->tblk, rows, cnt, x);
     }
     for (size_t l = 0; l + 1 < f->lv_tbwd.size(); ++l) {
       const int cnt = f->lv_tbwd[l + 1] - f->lv_tbwd[l];
       if (!cnt) continue;
       const int* rows = f->rows_tbwd + f->lv_tbwd[l];
-      if (lg) k_ilu_lower_t_lg<V><<<grid(cnt), 128, 0, s>>>(F, f->tptr, f->tidx, f->tblk, rows, cnt, x);
+      if (lg)
+        with_block_size(f->b, [&](auto B) {
+          k_ilu_lower_t_lg<V, B()><<<grid(cnt), 128, 0, s>>>(F, f->tptr, f->tidx, f->tblk, rows,
+                                                             cnt, x);
+        });
       else k_ilu_lower_t<V><<<grid(cnt), 128, 0, s>>>(F, f->tptr, f->tidx, f->tblk, rows, cnt, x);
     }
   }
@@ -878,6 +964,10 @@ int ilu_apply(FvIlu0* f, const V* r, V* x, int transpose, cudaStream_t s) {
     if (t && !f->tptr) {
       fv_set_error("fv_ilu0_apply: the transposed-solve structures are built by a transposed "
                    "solve outside stream capture first");
+      return FV_ERR_ARG;
+    }
+    if ((uintptr_t)x % 16 != 0) {  // the level kernels read x's block segments as vectors
+      fv_set_error("fv_ilu0_apply: under stream capture x must be 16-byte aligned");
       return FV_ERR_ARG;
     }
     if ((const void*)x != (const void*)r)
@@ -1241,7 +1331,7 @@ int spmv(int nbr, int b, const int* indptr, const int* indices, const V* values,
     cudaFree(tb);
     return FV_ERR_CUDA;
   }
-  k_bsr_spmv_t<V><<<fv_blocks(rows, kThreads), kThreads, 0, s>>>(nbr, b, tp, ti, tb, values, x, y);
+  launch_spmv_t<V>(nbr, b, tp, ti, tb, values, x, y, s);
   FV_CUDA_TRY(cudaGetLastError());
   FV_CUDA_TRY(cudaStreamSynchronize(s));
   cudaFree(tp);
@@ -1281,13 +1371,12 @@ extern "C" int fv_bsr_spmv_t_mapped(int n, int b, const int* tptr, const int* ti
     return FV_ERR_ARG;
   }
   cudaStream_t s = (cudaStream_t)stream;
-  const long rows = (long)n * b;
   if (f64)
-    k_bsr_spmv_t<double><<<fv_blocks(rows, kThreads), kThreads, 0, s>>>(
-        n, b, tptr, tidx, tblk, (const double*)values, (const double*)x, (double*)y);
+    launch_spmv_t<double>(n, b, tptr, tidx, tblk, (const double*)values, (const double*)x,
+                          (double*)y, s);
   else
-    k_bsr_spmv_t<float><<<fv_blocks(rows, kThreads), kThreads, 0, s>>>(
-        n, b, tptr, tidx, tblk, (const float*)values, (const float*)x, (float*)y);
+    launch_spmv_t<float>(n, b, tptr, tidx, tblk, (const float*)values, (const float*)x, (float*)y,
+                         s);
   FV_CUDA_TRY(cudaGetLastError());
   return FV_OK;
 }

@@ -93,9 +93,10 @@ def test_preconditioner_transpose_is_exact(kind, opts):
 @pytest.mark.parametrize("precision,fine_order", [(32, "colour"), (32, "natural"),
                                                   (64, "natural"), (64, "colour")])
 def test_graph_replayed_vcycle_equals_the_eager_cycle(precision, fine_order):
-    """The V-cycle replayed as one CUDA graph gives bitwise the eager cycle's output: on its first
-    (eager) and second (captured) application, after a refresh at a new state, and after a new
-    shift (which re-forms the fine operator's storage and so re-captures)."""
+    """The V-cycle and its transpose, each replayed as one CUDA graph, give bitwise the eager
+    cycle's output: on the first (eager) and second (captured) application, after a refresh at a
+    new state, and after a new shift (which re-forms the fine operator's storage and so
+    re-captures)."""
     _, case, pg, s = _cavity_pc("amg", precision, fine_order=fine_order)
     _, _, pe, _ = _cavity_pc("amg", precision, fine_order=fine_order, graph=False)
     g = torch.Generator(device="cuda").manual_seed(1)
@@ -105,18 +106,20 @@ def test_graph_replayed_vcycle_equals_the_eager_cycle(precision, fine_order):
         p.refresh(s)
     for r in rs:
         assert torch.equal(pg.apply(r), pe.apply(r))
-    assert pg._graph is not None
+        assert torch.equal(pg.apply_transpose(r), pe.apply_transpose(r))
+    assert set(pg._graphs) == {False, True}
     s2 = s * (1.0 + 0.01 * torch.rand(s.shape, dtype=s.dtype, device="cuda", generator=g))
     for p in (pg, pe):
         p.refresh(s2)
     for r in rs:
         assert torch.equal(pg.apply(r), pe.apply(r))
+        assert torch.equal(pg.apply_transpose(r), pe.apply_transpose(r))
     shift = 0.5 + torch.rand(case.n_unknowns, dtype=torch.float64, device="cuda", generator=g)
     for p in (pg, pe):
         p.reshift(shift)
     for r in rs:
         assert torch.equal(pg.apply(r), pe.apply(r))
-    assert torch.equal(pg.apply_transpose(rs[0]), pe.apply_transpose(rs[0]))
+        assert torch.equal(pg.apply_transpose(r), pe.apply_transpose(r))
 
 
 @pytest.mark.parametrize("precision", [32, 64])
@@ -207,4 +210,4 @@ def test_preconditioners_on_one_case_share_its_kept_plan(precision):
     r = torch.randn(case.n_unknowns, dtype=torch.float64, device="cuda", generator=g)
     for _ in range(2):  # eager, then the graph replay
         assert torch.equal(p1.apply(r), p2.apply(r))
-    assert torch.equal(p1.apply_transpose(r), p2.apply_transpose(r))
+        assert torch.equal(p1.apply_transpose(r), p2.apply_transpose(r))

@@ -117,6 +117,28 @@ def test_bsr_spmv_matches_scipy(b, transpose):
     np.testing.assert_allclose(got32.cpu().numpy(), want, rtol=1e-4, atol=1e-4)
 
 
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_transposed_spmv_block_size_kernels_agree_bitwise(dtype):
+    """The transposed product's compile-time-size kernel (x 16-byte aligned) and its runtime-size
+    kernel (x at an 8- or 4-byte offset) accumulate the same products in the same order."""
+    import scipy.sparse as sp
+
+    from aquaflux_gb300.sparse import bsr_spmv
+
+    b, nb = 6, 400
+    a = sp.random(nb, nb, density=0.02, random_state=3, format="csr") + sp.eye(nb)
+    a.sort_indices()
+    g = torch.Generator(device="cuda").manual_seed(3)
+    vals = torch.randn(a.nnz * b * b, dtype=dtype, device="cuda", generator=g)
+    buf = torch.randn(nb * b + 1, dtype=dtype, device="cuda", generator=g)
+    x_off = buf[1:]
+    x_al = x_off.clone()
+    assert x_al.data_ptr() % 16 == 0 and x_off.data_ptr() % 16 != 0
+    y_al = bsr_spmv(a.indptr, a.indices, vals, b, x_al, transpose=True)
+    y_off = bsr_spmv(a.indptr, a.indices, vals, b, x_off, transpose=True)
+    assert torch.equal(y_al, y_off)
+
+
 def test_dot_is_deterministic():
     from aquaflux_gb300.sparse import dot
 
@@ -129,8 +151,9 @@ def test_dot_is_deterministic():
 
 @pytest.mark.parametrize("precision", [32, 64])
 def test_block_solve_pivot_quotients_are_correctly_rounded(precision):
-    """The block backward sweep divides by its pivots through a corrected reciprocal; on a matrix
-    of diagonal blocks the solve is x = r / d entry by entry and must equal IEEE division."""
+    """The block backward sweep and the transposed forward sweep divide by their pivots through a
+    corrected reciprocal; on a matrix of diagonal blocks both solves are x = r / d entry by entry
+    and must equal IEEE division."""
     from aquaflux_gb300.ilu0 import Ilu0
 
     b, n = 6, 50000
@@ -153,6 +176,8 @@ def test_block_solve_pivot_quotients_are_correctly_rounded(precision):
     f = Ilu0.from_csr(ip, ix, blocks.reshape(-1), block_size=b, precision=precision)
     got = f.solve(torch.tensor(r, device="cuda")).cpu().numpy()
     assert np.array_equal(got, r / d)
+    got_t = f.solve(torch.tensor(r, device="cuda"), transpose=True).cpu().numpy()
+    assert np.array_equal(got_t, r / d)
 
 
 def test_block_ilu0_fp64_bitwise_equals_the_reference_kernel_on_a_channel_jacobian():
