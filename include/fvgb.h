@@ -345,8 +345,9 @@ int fv_ilu0_clone(const FvIlu0* src, int precision, void* stream, FvIlu0** out);
  * float64 when values_f64 != 0 and precision == 32: converted on the fly). */
 int fv_ilu0_factor(FvIlu0* f, const void* values, int values_f64, void* stream);
 /* x = (LU)^-1 r, or (LU)^-T r when transpose != 0.  Device vectors of `precision`.  On a stream
- * under capture the level kernels are recorded into the caller's graph (x may alias r); a
- * transposed solve needs one uncaptured transposed solve first. */
+ * under capture the level kernels are recorded into the caller's graph (x may alias r, and must be
+ * 16-byte aligned: FV_ERR_ARG otherwise); a transposed solve needs one uncaptured transposed solve
+ * first. */
 int fv_ilu0_apply(FvIlu0* f, const void* r, void* x, int transpose, void* stream);
 /* Copy the factor (device, nnzb * b * b, `precision`) -- combined L (unit diagonal) and U. */
 int fv_ilu0_factor_values(const FvIlu0* f, void* out, void* stream);
