@@ -372,6 +372,10 @@ extern "C" int fv_case_destroy(FvCase* c) {
   cudaFree(c->lin_fl);
   cudaFree(c->lin_ac);
   cudaFree(c->lin_g);
+  cudaFree(c->lin_r);
+  cudaFree(c->lin_cl);
+  cudaFree(c->lin_cc);
+  cudaFree(c->lin_src);
   fv_node_adjoint_free(c);
   cudaFree(c->flx);
   cudaFree(c->mu_cell);
@@ -703,9 +707,12 @@ extern "C" int fv_jvp_linearised(FvCase* c, const double* state, const double* v
   cudaStream_t s = (cudaStream_t)stream;
   state = physical_state(c, state, s);
   c->lin_use = 1;
-  const int rc = fv_case_run(c, state, physical_tangent(c, v, s), FV_TAN_STATE, residual, jv, s);
+  const int rc = fv_case_run(c, state, physical_tangent(c, v, s), FV_TAN_STATE, nullptr, jv, s);
   c->lin_use = 0;
-  return rc;
+  if (rc != FV_OK || !residual) return rc;
+  FV_CUDA_TRY(cudaMemcpyAsync(residual, c->lin_r, sizeof(double) * c->nfld * c->mesh->nc,
+                              cudaMemcpyDeviceToDevice, s));
+  return FV_OK;
 }
 
 extern "C" int fv_jvp_frozen(FvCase* c, const double* state, const double* v, double* jv,

@@ -159,6 +159,10 @@ struct FvCase {
   double* lin_fl = nullptr;     // ... and its primal face fluxes (nfld, nf)
   double* lin_ac = nullptr;     // ... its face coefficients and mass-flux estimates (3, nf)
   double* lin_g = nullptr;      // ... its gradients (nfld, dim, nc)
+  double* lin_r = nullptr;      // ... its residual (nfld, nc)
+  double* lin_cl = nullptr;     // ... its SST closure fields (7, nc)
+  double* lin_cc = nullptr;     // ... the off-wall closure and source forms (29, nc)
+  double* lin_src = nullptr;    // a product's off-wall k / omega source tangents (2, nc)
   int lin_valid = 0;            // a linearisation is held (parameter / geometry changes clear it)
   int lin_use = 0;              // the running dual-number pass takes its flux stage from it
   int fwd_valid = 0;            // work / aux hold the double forward pass of the last VJP's state

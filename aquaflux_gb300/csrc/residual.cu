@@ -1389,6 +1389,279 @@ __global__ void __launch_bounds__(128) k_sum(MeshView m, CaseView cv, Src<T> st,
   k_sum_at<T, DIM, TURB>(stage_cell<T>(m, cv), m, cv, st, par, FL, cl, G, Gwi, R, JV);
 }
 
+// ---------------------------------------------------------------- linearised SST closure
+// Off the wall, the closure fields and the k / omega source terms of a cell depend on the state
+// through four scalars only: k, omega, the strain rate S and grad k . grad omega.  At a held
+// linearisation their tangents are therefore linear forms in those four tangents, tabulated once
+// per linearisation (k_lin_closure_coef) and applied by every Krylov product (k_closure_lin,
+// k_sum_lin) instead of the dual-number closure and source rows.  Wall cells (wall functions,
+// omega fixation) keep the dual-number path.
+
+// A value with N tangent directions, under the dual number's rules (max / min split the tangent
+// at a tie; safe_sqrt and the k >= 0 clamp give a zero tangent where they clamp).
+template <int N>
+struct DualV {
+  double v, d[N];
+};
+template <int N>
+__device__ __forceinline__ double val(const DualV<N>& x) { return x.v; }
+template <int N>
+__device__ __forceinline__ DualV<N> cst(double x, const DualV<N>&) {
+  DualV<N> r;
+  r.v = x;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = 0.0;
+  return r;
+}
+template <int N>
+__device__ __forceinline__ DualV<N> lin_comb(double v, double a, const DualV<N>& x, double b,
+                                            const DualV<N>& y) {  // value v, tangent a x' + b y'
+  DualV<N> r;
+  r.v = v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = a * x.d[i] + b * y.d[i];
+  return r;
+}
+template <int N>
+__device__ __forceinline__ DualV<N> scaled(double v, double a, const DualV<N>& x) {
+  DualV<N> r;
+  r.v = v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = a * x.d[i];
+  return r;
+}
+template <int N>
+__device__ __forceinline__ DualV<N> operator+(const DualV<N>& a, const DualV<N>& b) {
+  return lin_comb(a.v + b.v, 1.0, a, 1.0, b);
+}
+template <int N>
+__device__ __forceinline__ DualV<N> operator-(const DualV<N>& a, const DualV<N>& b) {
+  return lin_comb(a.v - b.v, 1.0, a, -1.0, b);
+}
+template <int N>
+__device__ __forceinline__ DualV<N> operator*(const DualV<N>& a, const DualV<N>& b) {
+  return lin_comb(a.v * b.v, b.v, a, a.v, b);
+}
+template <int N>
+__device__ __forceinline__ DualV<N> operator/(const DualV<N>& a, const DualV<N>& b) {
+  const double r = 1.0 / b.v, q = a.v * r;
+  return lin_comb(q, r, a, -q * r, b);
+}
+template <int N>
+__device__ __forceinline__ DualV<N> operator+(const DualV<N>& a, double b) { return scaled(a.v + b, 1.0, a); }
+template <int N>
+__device__ __forceinline__ DualV<N> operator+(double a, const DualV<N>& b) { return scaled(a + b.v, 1.0, b); }
+template <int N>
+__device__ __forceinline__ DualV<N> operator-(const DualV<N>& a, double b) { return scaled(a.v - b, 1.0, a); }
+template <int N>
+__device__ __forceinline__ DualV<N> operator-(double a, const DualV<N>& b) { return scaled(a - b.v, -1.0, b); }
+template <int N>
+__device__ __forceinline__ DualV<N> operator*(const DualV<N>& a, double b) { return scaled(a.v * b, b, a); }
+template <int N>
+__device__ __forceinline__ DualV<N> operator*(double a, const DualV<N>& b) { return scaled(a * b.v, a, b); }
+template <int N>
+__device__ __forceinline__ DualV<N> operator/(const DualV<N>& a, double b) {
+  const double r = 1.0 / b;
+  return scaled(a.v * r, r, a);
+}
+template <int N>
+__device__ __forceinline__ DualV<N> operator/(double a, const DualV<N>& b) {
+  const double r = 1.0 / b.v, q = a * r;
+  return scaled(q, -q * r, b);
+}
+template <int N>
+__device__ __forceinline__ DualV<N> fv_max(const DualV<N>& a, const DualV<N>& b) {
+  if (a.v > b.v) return a;
+  if (a.v < b.v) return b;
+  return lin_comb(a.v, 0.5, a, 0.5, b);
+}
+template <int N>
+__device__ __forceinline__ DualV<N> fv_min(const DualV<N>& a, const DualV<N>& b) {
+  if (a.v < b.v) return a;
+  if (a.v > b.v) return b;
+  return lin_comb(a.v, 0.5, a, 0.5, b);
+}
+template <int N>
+__device__ __forceinline__ DualV<N> fv_sqrt(const DualV<N>& x) {
+  const double r = sqrt(x.v);
+  return scaled(r, 0.5 / r, x);
+}
+template <int N>
+__device__ __forceinline__ DualV<N> fv_tanh(const DualV<N>& x) {
+  const double t = tanh(x.v);
+  return scaled(t, 1.0 - t * t, x);
+}
+
+// The off-wall SST closure of closure_cell and source rows of sst_rows as functions of (S, k,
+// omega, grad k . grad omega), the same formulas: out = (F1, nu_t, k diffusivity, omega
+// diffusivity, F2, k source, omega source), the sources as they enter the face sums.
+template <class T>
+__device__ __forceinline__ void sst_off_wall(T S, T k, T w, T dot_kw, double nu, double id,
+                                             double id2, double V, T (&out)[7]) {
+  const T kp = pos(k);
+  const T iw = 1.0 / w;
+  const T cd = fv_max((2.0 * SIGMA_W2) * dot_kw * iw, cst(CROSS_FLOOR, w));
+  const T sk = safe_sqrt(kp);
+  const T vt = ((500.0 * id2) * nu) * iw;
+  const T c1 = sk * iw * (id / BETA_STAR);
+  const T arg1 = fv_min(fv_max(c1, vt), (4.0 * SIGMA_W2 * id2) * kp / cd);
+  const T a1sq = arg1 * arg1;
+  const T F1 = fv_tanh(a1sq * a1sq);
+  const T arg2 = fv_max(2.0 * c1, vt);
+  const T F2 = fv_tanh(arg2 * arg2);
+  const T nut = A1 * kp / fv_max(A1 * w, S * F2);
+  out[0] = F1;
+  out[1] = nut;
+  out[2] = nu + (SIGMA_K2 + F1 * (SIGMA_K1 - SIGMA_K2)) * nut;
+  out[3] = nu + (SIGMA_W2 + F1 * (SIGMA_W1 - SIGMA_W2)) * nut;
+  out[4] = F2;
+  const T limit = (PROD_RATIO * BETA_STAR) * kp * w;
+  const T lim = fv_min(nut * (S * S), limit);
+  out[5] = BETA_STAR * V * k * w - lim * V;
+  const T alpha = ALPHA_2 + F1 * (ALPHA_1 - ALPHA_2);
+  const T cap = limit / fv_max(nut, cst(NUT_FLOOR, nut));
+  const T beta = BETA_2 + F1 * (BETA_1 - BETA_2);
+  const T cross = (2.0 * SIGMA_W2) * (1.0 - F1) * dot_kw / w;
+  out[6] = V * (beta * (w * w) - alpha * fv_min(S * S, cap) - cross);
+}
+
+// Coefficients per cell (LIN_NCOEF rows of nc): 2 / S (the strain rate's tangent is
+// 2 / S sum_ij s_ij (grad u)'_ij, 0 where S = 0), then for each output of sst_off_wall its
+// linear form in (k', omega', S', (grad k . grad omega)').
+constexpr int LIN_NCOEF = 29;
+
+// At a held linearisation: keep the closure fields (hcl, 7 rows of nc) and tabulate the off-wall
+// cells' coefficients from the evaluation's state, gradients and closure fields.
+template <int DIM>
+__global__ void k_lin_closure_coef(MeshView m, CaseView cv, const double* state, const double* G,
+                                   const double* cl, double nu, double* hcl, double* cc) {
+  using L = Layout<DIM, true>;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nc) return;
+  const long nc = m.nc;
+#pragma unroll
+  for (int q = 0; q < 7; ++q) hcl[q * nc + c] = cl[q * nc + c];
+  if (cv.wcell[c]) return;
+  const GeoPlain gv{};
+  const double S = cl[c];
+  cc[c] = S > 0.0 ? 2.0 / S : 0.0;
+  double dot = G[((long)L::K * DIM) * nc + c] * G[((long)L::W * DIM) * nc + c];
+#pragma unroll
+  for (int j = 1; j < DIM; ++j)
+    dot += G[((long)L::K * DIM + j) * nc + c] * G[((long)L::W * DIM + j) * nc + c];
+  DualV<4> in[4];
+  const double v0[4] = {state[(long)L::K * nc + c], state[(long)L::W * nc + c], S, dot};
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    in[a].v = v0[a];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) in[a].d[i] = a == i ? 1.0 : 0.0;
+  }
+  DualV<4> out[7];
+  sst_off_wall<DualV<4>>(in[2], in[0], in[1], in[3], nu, gv.inv_wd(cv, c), gv.inv_wd2(cv, c),
+                         gv.vol(m, c), out);
+#pragma unroll
+  for (int q = 0; q < 7; ++q)
+#pragma unroll
+    for (int i = 0; i < 4; ++i) cc[(1L + 4 * q + i) * nc + c] = out[q].d[i];
+}
+
+// The closure stage of a Krylov product at the held linearisation: off the wall, the held fields
+// with tangents from the tabulated forms, the omega gradient passed through, and the k / omega
+// source tangents (src, 2 rows of nc) for k_sum_lin; wall cells by the dual-number closure.
+template <int DIM>
+__global__ void __launch_bounds__(128) k_closure_lin(MeshView m, CaseView cv, Src<Dual> st,
+                                                     Par<Dual> par, const Dual* G,
+                                                     const double* hcl, const double* cc, Dual* cl,
+                                                     Dual* Gwi, double* src) {
+  using L = Layout<DIM, true>;
+  const int c = stage_cell<Dual>(m, cv);
+  if (c >= m.nc) return;
+  if (cv.wcell[c]) {
+    k_closure_at<Dual, DIM>(c, m, cv, st, par, G, cl, Gwi);
+    return;
+  }
+  const long nc = m.nc;
+  double gv[DIM][DIM], gd[DIM][DIM];
+#pragma unroll
+  for (int i = 0; i < DIM; ++i)
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) {
+      const Dual g = G[((long)i * DIM + j) * nc + c];
+      gv[i][j] = g.v;
+      gd[i][j] = g.d;
+    }
+  double ss = 0.0;
+#pragma unroll
+  for (int i = 0; i < DIM; ++i)
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) ss += (0.5 * (gv[i][j] + gv[j][i])) * gd[i][j];
+  const double t[4] = {st.t ? st.t[(long)L::K * nc + c] : 0.0,
+                       st.t ? st.t[(long)L::W * nc + c] : 0.0, cc[c] * ss, 0.0};
+  double ddot = 0.0;
+#pragma unroll
+  for (int j = 0; j < DIM; ++j) {
+    const Dual gk = G[((long)L::K * DIM + j) * nc + c], gw = G[((long)L::W * DIM + j) * nc + c];
+    ddot += gk.d * gw.v + gk.v * gw.d;
+    Gwi[(long)j * nc + c] = gw;
+  }
+  auto form = [&](int q) {
+    const double* a = cc + (1L + 4 * q) * nc + c;
+    return a[0] * t[0] + a[nc] * t[1] + a[2 * nc] * t[2] + a[3 * nc] * ddot;
+  };
+  cl[c] = Dual{hcl[c], t[2]};
+  cl[nc + c] = Dual{hcl[nc + c], form(0)};
+  cl[2 * nc + c] = Dual{hcl[2 * nc + c], form(1)};
+  cl[3 * nc + c] = Dual{hcl[3 * nc + c], 0.0};  // the wall shear rate: 0 off the wall
+  cl[4 * nc + c] = Dual{hcl[4 * nc + c], form(2)};
+  cl[5 * nc + c] = Dual{hcl[5 * nc + c], form(3)};
+  cl[6 * nc + c] = Dual{hcl[6 * nc + c], form(4)};
+  src[c] = form(5);
+  src[nc + c] = form(6);
+}
+
+// The face sums of a Krylov product at the held linearisation: tangents only (the product's
+// output), the pin row, the k / omega source tangents of k_closure_lin off the wall and the
+// dual-number source rows on it.
+template <int DIM, bool TURB>
+__global__ void __launch_bounds__(128) k_sum_lin(MeshView m, CaseView cv, Src<Dual> st,
+                                                 Par<Dual> par, const Dual* FL, const Dual* cl,
+                                                 const Dual* G, const Dual* Gwi,
+                                                 const double* src, double* JV) {
+  using L = Layout<DIM, TURB>;
+  constexpr int NF = L::NFLD;
+  const int c = stage_cell<Dual>(m, cv);
+  if (c >= m.nc) return;
+  const long nc = m.nc, nf = m.nf;
+  double r[NF];
+  const int b = m.cf_ptr[c], e = m.cf_ptr[c + 1];
+  for (int i = b; i < e; ++i) {
+    const unsigned ent = m.cf_face[i];
+    const int f = (int)(ent & ~FV_NB_BIT);
+    const bool isnb = (ent & FV_NB_BIT) != 0;
+#pragma unroll
+    for (int q = 0; q < NF; ++q) {
+      double x = FL[(long)q * nf + f].d;
+      if (isnb) x = -x;
+      r[q] = i == b ? x : r[q] + x;
+    }
+  }
+  if (c == cv.pin) r[L::P] = st.t ? st.t[(long)L::P * nc + c] : 0.0;
+  if constexpr (TURB) {
+    if (cv.wcell[c]) {
+      Dual rk{0.0, r[L::K]}, rw{0.0, r[L::W]};
+      sst_rows<Dual, DIM>(m, cv, st, par, cl, G, Gwi, c, rk, rw);
+      r[L::K] = rk.d;
+      r[L::W] = rw.d;
+    } else {
+      r[L::K] += src[c];
+      r[L::W] += src[nc + c];
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < NF; ++q) JV[(long)q * nc + c] = r[q];
+}
+
 // Zero the tangent of n dual values (the "frozen" JVP holds gradients, closure and a_P fixed).
 __global__ void k_freeze(long n, Dual* x) {
   long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1446,6 +1719,9 @@ int run(FvCase* cs, Src<T> st, Par<T> par, double* R, double* JV, cudaStream_t s
   // values from it and compute only tangents
   bool lin = false;
   if constexpr (std::is_same<T, Dual>::value) lin = cs->lin_use && !frozen && !psi_count<DIM, TURB>(cs);
+  // ... and the closure and face-sum stages from its tabulated closure forms (the product only:
+  // fv_jvp_linearised returns the residual the linearisation held)
+  const bool lin_sum = lin && R == nullptr && (!TURB || cs->lin_cc != nullptr);
   fv_prof_mark(cs, 0, s);
   if constexpr (std::is_same<T, Dual>::value) {
     if (lin && cs->desc.gradient_sweeps == 0)  // the compact scheme (no relaxation factor)
@@ -1456,7 +1732,17 @@ int run(FvCase* cs, Src<T> st, Par<T> par, double* R, double* JV, cudaStream_t s
     gradient_stage<T, DIM, TURB>(cs, st, par, w, s);
   }
   fv_prof_mark(cs, 1, s);
-  if (TURB) k_closure<T, DIM><<<bc(1), tb[1], 0, s>>>(m, cv, st, par, w.G, w.cl, w.Gwi);
+  if (TURB) {
+    bool done = false;
+    if constexpr (std::is_same<T, Dual>::value) {
+      if (lin_sum) {
+        k_closure_lin<DIM><<<bc(1), tb[1], 0, s>>>(m, cv, st, par, w.G, cs->lin_cl, cs->lin_cc,
+                                                   w.cl, w.Gwi, cs->lin_src);
+        done = true;
+      }
+    }
+    if (!done) k_closure<T, DIM><<<bc(1), tb[1], 0, s>>>(m, cv, st, par, w.G, w.cl, w.Gwi);
+  }
   fv_prof_mark(cs, 2, s);
   if constexpr (std::is_same<T, Dual>::value) {
     if (lin) {
@@ -1500,7 +1786,16 @@ int run(FvCase* cs, Src<T> st, Par<T> par, double* R, double* JV, cudaStream_t s
     k_flux<T, DIM, TURB><<<bf(4), tb[4], 0, s>>>(m, cv, st, par, w.G, w.cl, w.dco, w.me,
                                                  npsi ? w.psi : nullptr, frozen, w.FL, aux);
   fv_prof_mark(cs, 5, s);
-  k_sum<T, DIM, TURB><<<bc(5), tb[5], 0, s>>>(m, cv, st, par, w.FL, w.cl, w.G, w.Gwi, R, JV);
+  bool summed = false;
+  if constexpr (std::is_same<T, Dual>::value) {
+    if (lin_sum) {
+      k_sum_lin<DIM, TURB><<<bc(5), tb[5], 0, s>>>(m, cv, st, par, w.FL, w.cl, w.G, w.Gwi,
+                                                   cs->lin_src, JV);
+      summed = true;
+    }
+  }
+  if (!summed)
+    k_sum<T, DIM, TURB><<<bc(5), tb[5], 0, s>>>(m, cv, st, par, w.FL, w.cl, w.G, w.Gwi, R, JV);
   fv_prof_mark(cs, 6, s);
   if (end_profile_run) fv_prof_end_run(cs);
   FV_CUDA_TRY(cudaGetLastError());
@@ -1843,6 +2138,16 @@ int linearise(FvCase* cs, const double* state, double* R, cudaStream_t s) {
                               cudaMemcpyDeviceToDevice, s));
   FV_CUDA_TRY(cudaMemcpyAsync(cs->lin_g, w.G, sizeof(double) * NF * DIM * nc,
                               cudaMemcpyDeviceToDevice, s));
+  if (!cs->lin_r) FV_CUDA_TRY(cudaMalloc(&cs->lin_r, sizeof(double) * NF * nc));
+  FV_CUDA_TRY(cudaMemcpyAsync(cs->lin_r, R, sizeof(double) * NF * nc, cudaMemcpyDeviceToDevice, s));
+  if constexpr (TURB) {
+    if (!cs->lin_cl) FV_CUDA_TRY(cudaMalloc(&cs->lin_cl, sizeof(double) * 7 * nc));
+    if (!cs->lin_cc) FV_CUDA_TRY(cudaMalloc(&cs->lin_cc, sizeof(double) * LIN_NCOEF * nc));
+    if (!cs->lin_src) FV_CUDA_TRY(cudaMalloc(&cs->lin_src, sizeof(double) * 2 * nc));
+    k_lin_closure_coef<DIM><<<fv_blocks(nc, 128), 128, 0, s>>>(
+        cs->mesh->view, cs->view, state, w.G, w.cl, cs->mu * irho, cs->lin_cl, cs->lin_cc);
+    FV_CUDA_TRY(cudaGetLastError());
+  }
   cs->lin_valid = 1;
   return FV_OK;
 }

@@ -185,10 +185,12 @@ int fv_jvp(FvCase* c, const double* state, const double* v, double* residual, do
            void* stream);
 /* The linearised Jacobian-vector product (jax.linearize's split of the reference's
  * jax.jvp(residual_fn, (phi,), (v,)), aquaflux/solve/newton.py:110-111): fv_linearise evaluates the
- * residual at `state` (into `residual`, device, may be NULL) and holds the face intermediates and
- * primal face fluxes of that evaluation; fv_jvp_linearised then gives J(state) v (and the residual)
- * with the interior faces' flux stage computed from them -- the tangent arithmetic only -- and every
- * other stage as fv_jvp does.  `state` must be the linearised one.  A change of parameters, of the
+ * residual at `state` (into `residual`, device, may be NULL) and holds that evaluation's face
+ * intermediates, primal face fluxes, gradients, residual and (SST) the off-wall cells' closure and
+ * source tangents as linear forms in (k', omega', S', (grad k . grad omega)'); fv_jvp_linearised then
+ * gives J(state) v (and, when `residual` is not NULL, the held residual) with the interior faces'
+ * flux, coefficient and compact-gradient stages, the off-wall closure and the face sums computed as
+ * tangents only, every other stage as fv_jvp does.  `state` must be the linearised one.  A change of parameters, of the
  * viscosity field, of the wall distance or of the geometry (fv_case_refresh_geometry) drops the
  * linearisation; fv_jvp_linearised then refuses until fv_linearise runs again.  First-order upwind
  * advection only (a limited reconstruction is refused by fv_linearise). */

@@ -17,6 +17,8 @@ pytestmark = pytest.mark.gpu
 @pytest.mark.parametrize("name", ["cav8", "cavj", "lam3", "sst2", "sst3", "ccavj", "csst2",
                                   "csst3", "wsst2", "bsst3"])
 def test_linearised_jvp_equals_the_dual_number_jvp(name):
+    from aquaflux_gb300._lib import check, lib, ptr
+
     fc, case, d, p = device_case(name)
     rng = np.random.default_rng(13)
     for s in d[p + "states"][:2]:
@@ -27,8 +29,39 @@ def test_linearised_jvp_equals_the_dual_number_jvp(name):
         ref = fc.jvp(s, v)
         scale = float(ref.abs().max())
         assert float((got - ref).abs().max()) <= 1e-12 * scale
-        # bitwise run to run
+        # field by field too: the k and omega rows (off-wall closure and source tangents from
+        # the tabulated forms) against their own scale
+        nf = got.numel() // fc.n_cells
+        for q, (a, b) in enumerate(zip(got.view(nf, -1), ref.view(nf, -1))):
+            assert float((a - b).abs().max()) <= 1e-11 * float(b.abs().max()) + 1e-300, (name, q)
+        # bitwise run to run; with a residual asked for, the held one and the same product
         assert torch.equal(got, fc.jvp_linearised(s, v))
+        sv, vv = fc._vec(s), fc._vec(v)
+        rr, jv = torch.empty_like(r), torch.empty_like(r)
+        check(lib().fv_jvp_linearised(fc._h, ptr(sv), ptr(vv), ptr(rr), ptr(jv),
+                                      torch.cuda.current_stream().cuda_stream))
+        assert torch.equal(rr, r) and torch.equal(jv, got)
+
+
+def test_linearised_sst_channel_with_wall_and_off_wall_cells():
+    """The 3D SST channel at a perturbed state (wall-function cells beside the walls, off-wall
+    cells inside, k clipped at zero in some cells): the linearised product, whose off-wall closure
+    and source tangents come from the forms tabulated at the linearisation, against the dual-number
+    JVP field by field; and again after a second linearisation at another state."""
+    from aquaflux_gb300 import workloads
+
+    wl = workloads.channel3d(8, renumber="host")
+    fc = wl.device_case()
+    rng = np.random.default_rng(21)
+    n = fc.n_cells
+    for seed in (0, 1):
+        s = wl.initial_state(seed=seed, noise=0.05 + 0.05 * seed)
+        s[4 * n:4 * n + n // 10] = 0.0  # k exactly at the clamp (the tie rule) in a tenth of cells
+        v = rng.standard_normal(s.size)
+        fc.linearise(s)
+        got, ref = fc.jvp_linearised(s, v), fc.jvp(s, v)
+        for q, (a, b) in enumerate(zip(got.view(6, -1), ref.view(6, -1))):
+            assert float((a - b).abs().max()) <= 1e-11 * float(b.abs().max()), q
 
 
 def test_linearised_jvp_refusals():
