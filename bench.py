@@ -39,8 +39,9 @@ METRIC = "Newton-solve s & residual+VJP Gfaces/s at 2M cells: FP32-precond vs FP
 UNIT = "Gfaces/s"
 STEP_DESC = {"vjp": "residual + VJP (hand-written adjoint) at a fixed state",
              "jvp": "residual + JVP (dual numbers) at a fixed state",
-             "jvp-linearised": "residual + JVP at a held linearisation (the Newton solve's Krylov "
-                               "operator: fv_linearise once, then fv_jvp_linearised)"}
+             "jvp-linearised": "JVP at a held linearisation, the held residual copied out (the "
+                               "Newton solve's Krylov operator: fv_linearise once, then "
+                               "fv_jvp_linearised)"}
 CLOCK_QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
                "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
                "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
