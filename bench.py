@@ -4,7 +4,9 @@ Workload: the 2,097,152-cell 3D channel with a bump, coupled (u, v, w, p) + k-om
 (``aquaflux_gb300.workloads.channel3d(128)``: 6,340,608 faces, seeded bump / jitter, randomly
 permuted then RCM-renumbered cells).  One step (default ``--step vjp``) = one evaluation of the
 residual and its vector-Jacobian product (hand-written adjoint kernels) at a fixed state;
-``--step jvp`` times the residual + Jacobian-vector product (the Krylov operator) instead.  ``value`` is faces processed per second (Gfaces/s) with inputs resident in HBM;
+``--step jvp`` times the residual + Jacobian-vector product (dual numbers) instead, and
+``--step jvp-linearised`` the Newton solve's Krylov operator (the product at a held
+linearisation).  ``value`` is faces processed per second (Gfaces/s) with inputs resident in HBM;
 ``e2e`` is the same step through the C ABI with host (pinned) inputs / outputs copied inside the
 timed region.
 
@@ -13,8 +15,9 @@ oracle restating the reference's residual, autograd JVP, all host threads) on a 
 the same workload.
 
 The line also carries the Newton block (each preconditioner in fp64, fp32 and fp32 + fp32
-tangents), the adjoint objectives, the CPU baseline, and ``cpu_ilu``: the reference's ILU(0)
-kernel (its C restatement, one core) timed beside the GPU's fp64 ILU(0) on a 48^3 Jacobian.
+tangents), the adjoint objectives, the CPU baseline, and ``cpu_ilu``: the reference's compiled
+ILU(0) kernel (built from its source; its plain-C restatement where that build is absent; one
+core) timed beside the GPU's fp64 ILU(0) on a 48^3 Jacobian.
 
 Run: ``python bench.py [--gpus N] [--steps K] [--warmup W] [--size 128]``.  Profiling modes
 (one JSON line each): ``--newton-only KIND:PREC:TANGENTS`` (one Newton solve inside the NVTX
