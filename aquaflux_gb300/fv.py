@@ -252,7 +252,8 @@ class FlowCase:
         return (r, jv) if return_residual else jv
 
     def linearise(self, state, out: torch.Tensor | None = None) -> torch.Tensor:
-        """``R(state)``, holding the evaluation's face intermediates for :meth:`jvp_linearised`
+        """``R(state)``, holding the evaluation's face intermediates, gradients, residual and (SST)
+        the off-wall closure and source tangents as linear forms, for :meth:`jvp_linearised`
         (``fv_linearise``; first-order upwind advection only)."""
         s = self._vec(state)
         r = torch.empty_like(s) if out is None else out
@@ -261,8 +262,9 @@ class FlowCase:
 
     def jvp_linearised(self, state, v) -> torch.Tensor:
         """``J(state) v`` at the state last passed to :meth:`linearise` (``fv_jvp_linearised``:
-        the interior faces' flux tangents from the held intermediates; the same product as
-        :meth:`jvp` within rounding)."""
+        the interior faces' flux, coefficient and compact-gradient stages, the off-wall closure and
+        the face sums as tangents from the held linearisation; the same product as :meth:`jvp`
+        within rounding)."""
         s, vv = self._vec(state), self._vec(v)
         jv = torch.empty_like(s)
         check(lib().fv_jvp_linearised(self._h, ptr(s), ptr(vv), 0, ptr(jv), _stream()))
