@@ -1,6 +1,7 @@
 """Partitioned residual on the CPU: owned + ghost-layer partitions, the residual / JVP / VJP
-evaluated partition by partition (the oracle as each partition's evaluator) equal the serial
-oracle's, in one process and across two ``gloo`` ranks exchanging ghost rows point to point
+evaluated partition by partition (the oracle as each partition's evaluator; for the SST channel
+with the global wall distance) equal the serial oracle's, in one process and across two ``gloo``
+ranks exchanging ghost rows point to point
 (the reference's distributed = serial check, ``tests/unit/test_distributed.py:22-75``, there to
 1e-10 / 1e-9, here to 1e-12)."""
 from __future__ import annotations
@@ -183,3 +184,62 @@ def test_halo_plans_pair_up():
         got = np.concatenate([p.cells[v] for v in plans[p.rank].recv.values()]) \
             if plans[p.rank].recv else np.zeros(0, dtype=np.int64)
         assert np.array_equal(np.sort(got), np.sort(p.cells[p.ghosts]))
+
+
+def _sst_oracle_local(wl, part, global_d):
+    """The oracle on a partition of an SST workload, with the global wall distance on its cells
+    and that distance's Green-Gauss gradient formed on the local mesh (walls Dirichlet 0, every
+    other boundary, the cut included, zero gradient), as ``fv_case_set_wall_distance`` does."""
+    from aquaflux_gb300.partition import local_sst
+
+    sst = dict(local_sst(wl.sst, part), nu=wl.mu / wl.rho)
+    case = fo.make_case(part.mesh, mu=wl.mu, rho=wl.rho, flow_bc=local_flow_bc(wl.flow_bc, part),
+                        sst=sst)
+    orc = fo.Oracle(case)
+    geo = fo.geometry(orc.topo, orc.nodes)
+    d = torch.as_tensor(np.asarray(global_d)[part.cells], dtype=torch.float64)
+    is_wall = np.zeros(orc.topo.n_faces, dtype=bool)
+    is_wall[case["sst"]["wall_faces"]] = True
+    bvals = torch.where(torch.as_tensor(is_wall), torch.zeros(orc.topo.n_faces, dtype=torch.float64),
+                        d[orc.topo.owner])
+    orc.wall_d = d
+    orc.wall_dgrad = fo.gg_gradient(fo.Metrics(orc.topo, geo), d, bvals, case.get("gradient"))
+
+    class Local:
+        def residual(self, s):
+            return orc.residual(torch.as_tensor(s, dtype=torch.float64)).detach()
+
+        def jvp(self, s, v):
+            return orc.jvp(s, v)
+
+        def vjp(self, s, w):
+            return orc.vjp(s, w).detach()
+
+    return Local()
+
+
+def test_partitioned_sst_channel_equals_serial():
+    """The coupled SST channel split into three slabs along its length, each evaluated on its own
+    mesh with the global wall distance: residual, JVP and VJP equal the serial oracle's."""
+    from aquaflux_gb300 import workloads
+
+    wl = workloads.channel3d(4, 4, 24, renumber=False)  # slabs along the channel
+    m = wl.mesh
+    sst = dict(wl.sst, nu=wl.mu / wl.rho)
+    serial = fo.Oracle(fo.make_case(m, mu=wl.mu, rho=wl.rho, flow_bc=wl.flow_bc, sst=sst))
+    gd = serial.wall_d.numpy()
+    n_parts = 3
+    parts = build_partitions(m, partition_cells(m.n_cells, n_parts), ghost_layers_needed())
+    assert all(any(w in p.mesh.patches for w in wl.sst["walls"]) for p in parts)
+    # proper subsets: a partition's own nearest wall is not always the global one (the local
+    # distance alone leaves ~5e-6 relative errors in the owned rows)
+    assert all(p.cells.size < m.n_cells for p in parts)
+    pr = PartitionedResidual(m, 6, n_parts, ghost_layers_needed(),
+                             lambda p: _sst_oracle_local(wl, p, gd), device="cpu")
+    rng = np.random.default_rng(5)
+    s = wl.initial_state(seed=2, noise=0.05)
+    v = rng.standard_normal(s.size)
+    w = rng.standard_normal(s.size)
+    assert _rel(pr.residual(s), serial.residual(torch.as_tensor(s)).detach()) <= 1e-12
+    assert _rel(pr.jvp(s, v), serial.jvp(s, v)) <= 1e-12
+    assert _rel(pr.vjp(s, w), serial.vjp(s, w).detach()) <= 1e-12
