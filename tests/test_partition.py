@@ -108,21 +108,35 @@ def test_too_few_ghost_layers_break_the_owned_rows():
     assert _rel(pr.residual(s), serial.residual(torch.as_tensor(s)).detach()) > 1e-10
 
 
-def _rank_main(rank, world, port, out_dir):
+def _gloo_problem(which):
+    """(mesh, fields, ghost layers, make_local, serial oracle, state) of a two-rank test."""
+    if which == "cavity":
+        spec = SPECS["corrected"]
+        m = _mesh(20)
+        s = np.random.default_rng(1).standard_normal(3 * m.n_cells) * 0.3
+        return m, 3, _layers(spec), (lambda p: OracleLocal(p, spec)), _serial(m, spec), s
+    from aquaflux_gb300 import workloads
+
+    wl = workloads.channel3d(4, 4, 24, renumber=False)
+    serial = fo.Oracle(fo.make_case(wl.mesh, mu=wl.mu, rho=wl.rho, flow_bc=wl.flow_bc,
+                                    sst=dict(wl.sst, nu=wl.mu / wl.rho)))
+    gd = serial.wall_d.numpy()
+    return (wl.mesh, 6, ghost_layers_needed(), (lambda p: _sst_oracle_local(wl, p, gd)), serial,
+            wl.initial_state(seed=2, noise=0.05))
+
+
+def _rank_main(rank, world, port, out_dir, which):
     import torch.distributed as dist
 
     os.environ["MASTER_ADDR"] = "127.0.0.1"
     os.environ["MASTER_PORT"] = str(port)
     dist.init_process_group("gloo", rank=rank, world_size=world)
     try:
-        spec = SPECS["corrected"]
-        m = _mesh(20)
-        dr = DistributedResidual(m, 3, _layers(spec), lambda p: OracleLocal(p, spec), rank=rank,
-                                 world=world)
+        m, nfld, layers, make_local, _, s = _gloo_problem(which)
+        dr = DistributedResidual(m, nfld, layers, make_local, rank=rank, world=world)
         rng = np.random.default_rng(1)
-        s = rng.standard_normal(3 * m.n_cells) * 0.3
-        v = rng.standard_normal(3 * m.n_cells)
-        w = rng.standard_normal(3 * m.n_cells)
+        v = rng.standard_normal(s.size)
+        w = rng.standard_normal(s.size)
         so, vo, wo = dr.owned_of(s), dr.owned_of(v), dr.owned_of(w)
         res = {"r": dr.residual(so), "jv": dr.jvp(so, vo), "g": dr.vjp(so, wo),
                "dot": torch.tensor(dr.dot(vo, wo), dtype=torch.float64), "cells": torch.as_tensor(
@@ -132,7 +146,10 @@ def _rank_main(rank, world, port, out_dir):
         dist.destroy_process_group()
 
 
-def test_two_gloo_ranks_equal_serial(tmp_path):
+@pytest.mark.parametrize("which", ["cavity", "sst"])
+def test_two_gloo_ranks_equal_serial(tmp_path, which):
+    """Two gloo ranks: the corrected-gradient cavity, and the SST channel with the global wall
+    distance."""
     import socket
 
     import torch.multiprocessing as mp
@@ -140,23 +157,21 @@ def test_two_gloo_ranks_equal_serial(tmp_path):
     with socket.socket() as sk:
         sk.bind(("127.0.0.1", 0))
         port = sk.getsockname()[1]
-    mp.start_processes(_rank_main, args=(2, port, str(tmp_path)), nprocs=2, start_method="spawn")
-    spec = SPECS["corrected"]
-    m = _mesh(20)
-    serial = _serial(m, spec)
+    mp.start_processes(_rank_main, args=(2, port, str(tmp_path), which), nprocs=2,
+                       start_method="spawn")
+    m, nfld, _, _, serial, s = _gloo_problem(which)
     rng = np.random.default_rng(1)
-    s = rng.standard_normal(3 * m.n_cells) * 0.3
-    v = rng.standard_normal(3 * m.n_cells)
-    w = rng.standard_normal(3 * m.n_cells)
+    v = rng.standard_normal(s.size)
+    w = rng.standard_normal(s.size)
     want = {"r": serial.residual(torch.as_tensor(s)).detach().numpy(),
             "jv": serial.jvp(s, v).numpy(), "g": serial.vjp(s, w).detach().numpy()}
-    got = {k: np.zeros(3 * m.n_cells) for k in want}
+    got = {k: np.zeros(s.size) for k in want}
     dots = []
     for rank in range(2):
         res = torch.load(os.path.join(tmp_path, f"rank{rank}.pt"))
         cells = res["cells"].numpy()
         for k in want:
-            got[k].reshape(3, -1)[:, cells] = res[k].numpy().reshape(3, -1)
+            got[k].reshape(nfld, -1)[:, cells] = res[k].numpy().reshape(nfld, -1)
         dots.append(float(res["dot"]))
     for k in want:
         assert _rel(got[k], want[k]) <= 1e-12, k
