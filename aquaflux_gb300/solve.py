@@ -26,7 +26,7 @@ import time
 import numpy as np
 import torch
 
-from ._lib import check, lib, ptr
+from ._lib import FvError, check, lib, ptr
 from .colouring import block_stencil_colouring, cell_pattern, stencil_pattern
 from .ilu0 import Ilu0
 from .refresh import StepReport
@@ -567,8 +567,18 @@ def implicit_adjoint(case, state, g, *, rtol: float = 1e-10, precision: int = 64
     # the forward pass held once (the preconditioner's refresh above is the last other evaluation):
     # every Krylov product then runs the adjoint stages only
     case.hold_forward(s)
-    res = fgmres(lambda w: case.vjp_held(s, w), gv, mt.apply, rtol=rtol, restart=restart,
-                 maxiter=max_krylov)
+
+    def adjoint_product(w):
+        try:
+            return case.vjp_held(s, w)
+        except FvError as e:
+            if "no forward pass held" not in str(e):
+                raise
+            # a preconditioner that evaluates the case dropped the hold: hold it again
+            case.hold_forward(s)
+            return case.vjp_held(s, w)
+
+    res = fgmres(adjoint_product, gv, mt.apply, rtol=rtol, restart=restart, maxiter=max_krylov)
     dparams = -case.param_vjp(s, res.x)
     return AdjointResult(res.x, dparams, res.iterations, res.converged)
 

@@ -159,3 +159,38 @@ def test_implicit_adjoint_on_the_held_forward_pass():
                restart=30, maxiter=1000)
     assert a.converged and a.krylov_iterations == b.iterations
     assert torch.equal(a.lam, b.x)
+
+
+def test_implicit_adjoint_holds_again_after_a_preconditioner_evaluates_the_case():
+    """A preconditioner of the caller's that evaluates the residual in every application drops the
+    held forward pass each time: the adjoint solve holds it again and gives bitwise the same
+    result."""
+    from aquaflux_gb300 import workloads
+    from aquaflux_gb300.solve import (BlockJacobian, IluPreconditioner, implicit_adjoint,
+                                      newton_solve)
+
+    wl = workloads.channel3d(8, renumber=False)
+    case = wl.device_case()
+    root = newton_solve(case, wl.initial_state(), precision=64, rtol=1e-12).state
+    g = torch.randn(case.n_unknowns, dtype=torch.float64, device="cuda",
+                    generator=torch.Generator(device="cuda").manual_seed(5))
+
+    class Evaluating:
+        def __init__(self):
+            self.pc = IluPreconditioner(BlockJacobian(case, reach=1, frozen=True), 64)
+            self.applications = 0
+
+        def refresh(self, s):
+            self.pc.refresh(s)
+
+        def apply_transpose(self, r):
+            self.applications += 1
+            case.residual(root)  # drops the held forward pass
+            return self.pc.apply_transpose(r)
+
+    ev = Evaluating()
+    a = implicit_adjoint(case, root, g, rtol=1e-10, preconditioner=ev)
+    b = implicit_adjoint(case, root, g, rtol=1e-10)
+    assert ev.applications > 1
+    assert a.converged and a.krylov_iterations == b.krylov_iterations
+    assert torch.equal(a.lam, b.lam)
