@@ -109,6 +109,7 @@ SIGNATURES = {
     "fv_from_cells": (c_int, [c_int, c_int, P, P, P, c_int, P, P]),
     "fv_bsr_transpose_map": (c_int, [c_int, P, P, P, P, P]),
     "fv_bsr_spmv_t_mapped": (c_int, [c_int, c_int, P, P, P, P, P, P, c_int, P]),
+    "fv_bsr_transpose_blocks": (c_int, [c_long, c_int, P, P, P, c_int, P]),
     "fv_bsr_shift_equilibrate": (c_int, [c_int, c_int, P, P, P, P, c_int, P, P, P, c_int, P]),
     "fv_restrict_f64": (c_int, [c_int, c_int, P, P, P, P, P]),
     "fv_prolong_add_f64": (c_int, [c_int, c_int, P, P, P, P]),

@@ -58,7 +58,17 @@ class _Level:
         self.t = torch.zeros_like(self.x)
         self.rhs = torch.zeros_like(self.x)  # right-hand side when this is a coarse level
         self.coarse = None  # transfer data to the next level
-        self._tmap = None  # transpose map, built on the first transposed product
+        # the transpose (map and transposed blocks), built on the first transposed product and
+        # re-formed with the values after every refresh
+        self._tmap = None
+        self._tvals = None
+
+    def transpose_values(self) -> None:
+        """Re-form the transposed blocks from ``values`` (nothing before a transposed product)."""
+        if self._tvals is not None:
+            check(lib().fv_bsr_transpose_blocks(self.nnzb, self.b, ptr(self._tmap[2]),
+                                                ptr(self.values), ptr(self._tvals),
+                                                int(self.sfx == "f64"), _stream()))
 
     def spmv(self, x, y, transpose: bool = False):
         if not transpose:
@@ -73,10 +83,13 @@ class _Level:
             check(lib().fv_bsr_transpose_map(self.n, ptr(self.indptr), ptr(self.indices), ptr(tp),
                                              ptr(ti), ptr(tb)))
             self._tmap = [torch.tensor(a, device="cuda") for a in (tp, ti, tb)]
-        tp, ti, tb = self._tmap
-        check(lib().fv_bsr_spmv_t_mapped(self.n, self.b, ptr(tp), ptr(ti), ptr(tb),
-                                         ptr(self.values), ptr(x), ptr(y),
-                                         int(self.sfx == "f64"), _stream()))
+            self._tvals = torch.empty_like(self.values)
+            self.transpose_values()
+        # A^T x as the forward product on A^T's pattern and transposed blocks: the products of
+        # the mapped transposed kernel in the same order, read row-wise
+        tp, ti, _ = self._tmap
+        check(getattr(lib(), "fv_bsr_spmv_" + self.sfx)(
+            self.n, self.b, ptr(tp), ptr(ti), ptr(self._tvals), ptr(x), ptr(y), 0, _stream()))
 
 
 def plan_hierarchy(n, indptr, indices, *, min_cells: int = 4000, max_levels: int = 10,
@@ -245,6 +258,8 @@ class AmgHierarchy:
                 self._invert_coarsest()
             else:
                 coarse.ilu.refactor(coarse.values)
+        for lv in self.levels:
+            lv.transpose_values()
 
     def _smooth(self, lv, b_vec, x, sweeps, from_zero, transpose=False):
         if from_zero:

@@ -171,6 +171,20 @@ void launch_spmv_t(int n, int b, const int* tp, const int* ti, const int* tb, co
     k_bsr_spmv_t<V><<<fv_blocks(rows, kThreads), kThreads, 0, s>>>(n, b, tp, ti, tb, values, x, y);
 }
 
+// tval[q] = val[tblk[q]]^T: the blocks of A in the order of A^T's pattern, each transposed, so
+// that row a of block q of A^T is contiguous (the transposed sweeps and products read it with
+// the forward kernels' vector loads).
+template <class V>
+__global__ void k_transpose_blocks(long nnzb, int b, const int* __restrict__ tblk,
+                                   const V* __restrict__ val, V* __restrict__ tval) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long bb = (long)b * b;
+  if (t >= nnzb * bb) return;
+  const long q = t / bb;
+  const int e = (int)(t - q * bb), r = e / b, c = e - r * b;
+  tval[t] = val[(long)tblk[q] * bb + (long)c * b + r];
+}
+
 // Host-built transpose of a BSR pattern (cached per pattern pointer for the SpMV entry points).
 struct Transpose {
   std::vector<int> ptr, idx, blk;
@@ -638,12 +652,13 @@ __device__ __forceinline__ V lower_t_block_solve(V acc, const V (&Dc)[B], int a,
   return acc;
 }
 
-// Forward sweep of one level of the transposed solve, U^T z = r: block row i of U^T gathers the
-// blocks (j, i) of U, j < i, through the transpose map (column a of each block for lane a), in
-// the map's ascending-row order, then the in-block lower solve with D^T.
+// Forward sweep of one level of the transposed solve, U^T z = r: block row i of U^T takes the
+// blocks (j, i) of U, j < i (positions tptr[i] .. tdiag[i] of the transpose, ascending j), row a
+// of each transposed block (column a of the block of U) for lane a, then the in-block lower solve
+// with D^T -- the operations and their order of the reference's transposed solve.
 template <class V, int B>
-__global__ void k_ilu_upper_t_lg(IluView<V> F, const int* tptr, const int* tidx, const int* tblk,
-                                 const int* rows, int count, V* z) {
+__global__ void k_ilu_upper_t_lg(IluView<V> F, const int* tptr, const int* tidx, const int* tdiag,
+                                 const V* tval, const int* rows, int count, V* z) {
   const int gid = (blockIdx.x * blockDim.x + threadIdx.x) / FV_LG;
   const int a = threadIdx.x & (FV_LG - 1);
   if (gid >= count) return;
@@ -653,28 +668,28 @@ __global__ void k_ilu_upper_t_lg(IluView<V> F, const int* tptr, const int* tidx,
   constexpr long BB = (long)B * B;
   V acc = live ? z[(long)i * B + a] : V(0);
   if (live)
-    for (int q = tptr[i]; q < tptr[i + 1]; ++q) {
-      const int j = tidx[q];
-      if (j >= i) continue;
-      const V* U = F.val + (long)tblk[q] * BB + a;  // column a of block (j, i)
-      V zj[B];
-      load_seg<B>(z + (long)j * B, zj);
+    for (int q = tptr[i]; q < tdiag[i]; ++q) {
+      V Ut[B], zj[B];
+      load_seg<B>(tval + (long)q * BB + (long)a * B, Ut);
+      load_seg<B>(z + (long)tidx[q] * B, zj);
 #pragma unroll
-      for (int c = 0; c < B; ++c) acc -= U[(long)c * B] * zj[c];
+      for (int c = 0; c < B; ++c) acc -= Ut[c] * zj[c];
     }
-  V Dc[B];
-  const V* D = F.val + (long)F.diag[i] * BB + a;
+  V Dc[B];  // Dc[c] = D(c, a): row a of D^T
+  if (live) load_seg<B>(tval + (long)tdiag[i] * BB + (long)a * B, Dc);
+  else
 #pragma unroll
-  for (int c = 0; c < B; ++c) Dc[c] = live ? D[(long)c * B] : V(0);
+    for (int c = 0; c < B; ++c) Dc[c] = V(0);
   acc = lower_t_block_solve<V, B>(acc, Dc, a, live, mask);
   if (live) z[(long)i * B + a] = acc;
 }
 
 // Backward sweep of one level of the transposed solve, L^T x = z (unit diagonal): the blocks
-// (k, i) of L, k > i, in descending-row order, then the in-block unit upper solve.
+// (k, i) of L, k > i (positions tptr[i + 1] - 1 down to tdiag[i] + 1), then the in-block unit
+// upper solve.
 template <class V, int B>
-__global__ void k_ilu_lower_t_lg(IluView<V> F, const int* tptr, const int* tidx, const int* tblk,
-                                 const int* rows, int count, V* x) {
+__global__ void k_ilu_lower_t_lg(IluView<V> F, const int* tptr, const int* tidx, const int* tdiag,
+                                 const V* tval, const int* rows, int count, V* x) {
   const int gid = (blockIdx.x * blockDim.x + threadIdx.x) / FV_LG;
   const int a = threadIdx.x & (FV_LG - 1);
   if (gid >= count) return;
@@ -684,19 +699,18 @@ __global__ void k_ilu_lower_t_lg(IluView<V> F, const int* tptr, const int* tidx,
   constexpr long BB = (long)B * B;
   V acc = live ? x[(long)i * B + a] : V(0);
   if (live)
-    for (int q = tptr[i + 1] - 1; q >= tptr[i]; --q) {
-      const int k = tidx[q];
-      if (k <= i) continue;
-      const V* L = F.val + (long)tblk[q] * BB + a;  // column a of block (k, i)
-      V xk[B];
-      load_seg<B>(x + (long)k * B, xk);
+    for (int q = tptr[i + 1] - 1; q > tdiag[i]; --q) {
+      V Lt[B], xk[B];
+      load_seg<B>(tval + (long)q * BB + (long)a * B, Lt);
+      load_seg<B>(x + (long)tidx[q] * B, xk);
 #pragma unroll
-      for (int c = B - 1; c >= 0; --c) acc -= L[(long)c * B] * xk[c];
+      for (int c = B - 1; c >= 0; --c) acc -= Lt[c] * xk[c];
     }
   V Dc[B];
-  const V* D = F.val + (long)F.diag[i] * BB + a;
+  if (live) load_seg<B>(tval + (long)tdiag[i] * BB + (long)a * B, Dc);
+  else
 #pragma unroll
-  for (int c = 0; c < B; ++c) Dc[c] = live ? D[(long)c * B] : V(0);
+    for (int c = 0; c < B; ++c) Dc[c] = V(0);
 #pragma unroll
   for (int c = B - 1; c >= 0; --c) {
     const V vc = __shfl_sync(mask, acc, c, FV_LG);
@@ -752,7 +766,9 @@ struct FvIlu0 {
   int n = 0, b = 0, nnzb = 0, precision = 64;
   int *ptr = nullptr, *idx = nullptr, *diag = nullptr;
   int *tptr = nullptr, *tidx = nullptr, *tblk = nullptr;
+  int* tdiag = nullptr;   // position of the diagonal block in each row of the transpose
   void* val = nullptr;
+  void* tval = nullptr;   // (b > 1) the factor's blocks transposed, in the transpose's order
   unsigned long long* zero_flag = nullptr;
   // level sets: rows grouped by level (device), level boundaries (host)
   int* rows_fwd = nullptr;   // L / factor order
@@ -859,8 +875,8 @@ void launch_apply_levels(FvIlu0* f, int transpose, V* x, cudaStream_t s) {
       const int* rows = f->rows_tfwd + f->lv_tfwd[l];
       if (lg)
         with_block_size(f->b, [&](auto B) {
-          k_ilu_upper_t_lg<V, B()><<<grid(cnt), 128, 0, s>>>(F, f->tptr, f->tidx, f->tblk, rows,
-                                                             cnt, x);
+          k_ilu_upper_t_lg<V, B()><<<grid(cnt), 128, 0, s>>>(F, f->tptr, f->tidx, f->tdiag,
+                                                             (const V*)f->tval, rows, cnt, x);
         });
       else k_ilu_upper_t<V><<<grid(cnt), 128, 0, s>>>(F, f->tptr, f->tidx, f->tblk, rows, cnt, x);
     }
@@ -870,8 +886,8 @@ void launch_apply_levels(FvIlu0* f, int transpose, V* x, cudaStream_t s) {
       const int* rows = f->rows_tbwd + f->lv_tbwd[l];
       if (lg)
         with_block_size(f->b, [&](auto B) {
-          k_ilu_lower_t_lg<V, B()><<<grid(cnt), 128, 0, s>>>(F, f->tptr, f->tidx, f->tblk, rows,
-                                                             cnt, x);
+          k_ilu_lower_t_lg<V, B()><<<grid(cnt), 128, 0, s>>>(F, f->tptr, f->tidx, f->tdiag,
+                                                             (const V*)f->tval, rows, cnt, x);
         });
       else k_ilu_lower_t<V><<<grid(cnt), 128, 0, s>>>(F, f->tptr, f->tidx, f->tblk, rows, cnt, x);
     }
@@ -909,6 +925,12 @@ int ilu_factor(FvIlu0* f, cudaStream_t s) {
     if (rc != FV_OK) return rc;
   }
   FV_CUDA_TRY(cudaGraphLaunch(f->factor_exec, s));
+  if (f->tval) {  // a transposed solve was asked for: keep its transposed blocks current
+    const long nv = (long)f->nnzb * f->b * f->b;
+    k_transpose_blocks<V><<<fv_blocks(nv, kThreads), kThreads, 0, s>>>(f->nnzb, f->b, f->tblk,
+                                                                      (const V*)f->val,
+                                                                      (V*)f->tval);
+  }
   FV_CUDA_TRY(cudaGetLastError());
   unsigned long long flag;
   FV_CUDA_TRY(cudaMemcpyAsync(&flag, f->zero_flag, sizeof(flag), cudaMemcpyDeviceToHost, s));
@@ -947,6 +969,23 @@ int ensure_transpose(FvIlu0* f, cudaStream_t s) {
   if (upload(rows, &f->rows_tbwd, s)) return FV_ERR_CUDA;
   if (upload(T.ptr, &f->tptr, s) || upload(T.idx, &f->tidx, s) || upload(T.blk, &f->tblk, s))
     return FV_ERR_CUDA;
+  if (f->b > 1) {  // the lane-group sweeps read the factor's blocks transposed
+    std::vector<int> td(n, -1);
+    for (int i = 0; i < n; ++i)
+      for (int q = T.ptr[i]; q < T.ptr[i + 1]; ++q)
+        if (T.idx[q] == i) td[i] = q;
+    if (upload(td, &f->tdiag, s)) return FV_ERR_CUDA;
+    const long nv = (long)f->nnzb * f->b * f->b;
+    const size_t vs = f->precision == 64 ? sizeof(double) : sizeof(float);
+    FV_CUDA_TRY(cudaMalloc(&f->tval, vs * (size_t)nv));
+    if (f->precision == 64)
+      k_transpose_blocks<double><<<fv_blocks(nv, kThreads), kThreads, 0, s>>>(
+          f->nnzb, f->b, f->tblk, (const double*)f->val, (double*)f->tval);
+    else
+      k_transpose_blocks<float><<<fv_blocks(nv, kThreads), kThreads, 0, s>>>(
+          f->nnzb, f->b, f->tblk, (const float*)f->val, (float*)f->tval);
+    FV_CUDA_TRY(cudaGetLastError());
+  }
   FV_CUDA_TRY(cudaStreamSynchronize(s));
   return FV_OK;
 }
@@ -1079,7 +1118,9 @@ extern "C" int fv_ilu0_destroy(FvIlu0* f) {
   cudaFree(f->tptr);
   cudaFree(f->tidx);
   cudaFree(f->tblk);
+  cudaFree(f->tdiag);
   cudaFree(f->val);
+  cudaFree(f->tval);
   cudaFree(f->zero_flag);
   cudaFree(f->rows_fwd);
   cudaFree(f->rows_bwd);
@@ -1135,12 +1176,16 @@ extern "C" int fv_ilu0_clone(const FvIlu0* src, int precision, void* stream, FvI
     rc |= copy_ints(src->tblk, nnzb, &f->tblk, s);
     rc |= copy_ints(src->rows_tfwd, n, &f->rows_tfwd, s);
     rc |= copy_ints(src->rows_tbwd, n, &f->rows_tbwd, s);
+    rc |= copy_ints(src->tdiag, n, &f->tdiag, s);
   }
   if (rc == FV_OK && precision != 0) {
     const size_t vs = precision == 64 ? sizeof(double) : sizeof(float);
     if (cudaMalloc(&f->val, vs * nnzb * f->b * f->b) != cudaSuccess ||
         cudaMalloc(&f->zero_flag, sizeof(unsigned long long)) != cudaSuccess ||
         cudaMalloc(&f->work, vs * n * f->b) != cudaSuccess)
+      rc = FV_ERR_CUDA;
+    // the transposed blocks, filled by the clone's factorisations
+    if (rc == FV_OK && f->tdiag && cudaMalloc(&f->tval, vs * nnzb * f->b * f->b) != cudaSuccess)
       rc = FV_ERR_CUDA;
   }
   if (rc == FV_OK && cudaStreamSynchronize(s) != cudaSuccess) rc = FV_ERR_CUDA;
@@ -1377,6 +1422,24 @@ extern "C" int fv_bsr_spmv_t_mapped(int n, int b, const int* tptr, const int* ti
   else
     launch_spmv_t<float>(n, b, tptr, tidx, tblk, (const float*)values, (const float*)x, (float*)y,
                          s);
+  FV_CUDA_TRY(cudaGetLastError());
+  return FV_OK;
+}
+
+extern "C" int fv_bsr_transpose_blocks(long nnzb, int b, const int* tblk, const void* values,
+                                       void* tvalues, int f64, void* stream) {
+  if (nnzb <= 0 || b <= 0 || !tblk || !values || !tvalues) {
+    fv_set_error("fv_bsr_transpose_blocks: bad arguments");
+    return FV_ERR_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  const long nv = nnzb * b * b;
+  if (f64)
+    k_transpose_blocks<double><<<fv_blocks(nv, kThreads), kThreads, 0, s>>>(
+        nnzb, b, tblk, (const double*)values, (double*)tvalues);
+  else
+    k_transpose_blocks<float><<<fv_blocks(nv, kThreads), kThreads, 0, s>>>(
+        nnzb, b, tblk, (const float*)values, (float*)tvalues);
   FV_CUDA_TRY(cudaGetLastError());
   return FV_OK;
 }

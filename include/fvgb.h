@@ -319,9 +319,16 @@ int fv_bsr_spmv_f32(int n_block_rows, int b, const int* indptr, const int* indic
 int fv_bsr_transpose_map(int n, const int* indptr, const int* indices, int* tptr, int* tidx,
                          int* tblk);
 /* y = A^T x through that map (device; fp64 when f64 != 0, else fp32; allocates nothing): the
- * transposed products of the exact V-cycle transpose. */
+ * transposed products of the exact V-cycle transpose (aquaflux/solve/ilu_inverse.py:275-308). */
 int fv_bsr_spmv_t_mapped(int n, int b, const int* tptr, const int* tidx, const int* tblk,
                          const void* values, const void* x, void* y, int f64, void* stream);
+/* tvalues[q] = values[tblk[q]]^T for the nnzb blocks of a map from fv_bsr_transpose_map (device;
+ * fp64 when f64 != 0, else fp32): A^T in BSR with b x b row-major blocks on the pattern (tptr,
+ * tidx), so that fv_bsr_spmv_f64 / _f32 with transpose = 0 on it gives A^T x -- the same products
+ * in the same order as fv_bsr_spmv_t_mapped, bitwise, with the forward kernel's row-wise vector
+ * loads.  No reference counterpart (the reference transposes through jax.linear_transpose). */
+int fv_bsr_transpose_blocks(long nnzb, int b, const int* tblk, const void* values, void* tvalues,
+                            int f64, void* stream);
 
 /* ------------------------------------------------------------------------------------------
  * Zero-fill ILU(0) over a BSR pattern.  Replaces Ilu0 (aquaflux/solve/ilu0.py:153-255) and the

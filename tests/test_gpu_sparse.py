@@ -139,6 +139,40 @@ def test_transposed_spmv_block_size_kernels_agree_bitwise(dtype):
     assert torch.equal(y_al, y_off)
 
 
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_transposed_blocks_give_the_mapped_transposed_product_bitwise(dtype):
+    """fv_bsr_transpose_blocks + the forward product on A^T's pattern (what the V-cycle's
+    transposed products run) against fv_bsr_spmv_t_mapped: the same products, the same order."""
+    import scipy.sparse as sp
+
+    from aquaflux_gb300._lib import check, lib, ptr
+
+    b, nb = 6, 300
+    a = sp.random(nb, nb, density=0.03, random_state=8, format="csr") + sp.eye(nb)
+    a.sort_indices()
+    ip, ix = a.indptr.astype(np.int32), a.indices.astype(np.int32)
+    nnzb = int(ip[-1])
+    tp, ti, tb = (np.empty(n, dtype=np.int32) for n in (nb + 1, nnzb, nnzb))
+    check(lib().fv_bsr_transpose_map(nb, ptr(ip), ptr(ix), ptr(tp), ptr(ti), ptr(tb)))
+    tp, ti, tb = (torch.tensor(v, device="cuda") for v in (tp, ti, tb))
+    g = torch.Generator(device="cuda").manual_seed(8)
+    vals = torch.randn(nnzb * b * b, dtype=dtype, device="cuda", generator=g)
+    x = torch.randn(nb * b, dtype=dtype, device="cuda", generator=g)
+    f64 = int(dtype == torch.float64)
+    st = torch.cuda.current_stream().cuda_stream
+    want = torch.empty_like(x)
+    check(lib().fv_bsr_spmv_t_mapped(nb, b, ptr(tp), ptr(ti), ptr(tb), ptr(vals), ptr(x),
+                                     ptr(want), f64, st))
+    tvals = torch.empty_like(vals)
+    check(lib().fv_bsr_transpose_blocks(nnzb, b, ptr(tb), ptr(vals), ptr(tvals), f64, st))
+    got = torch.empty_like(x)
+    fn = lib().fv_bsr_spmv_f64 if f64 else lib().fv_bsr_spmv_f32
+    check(fn(nb, b, ptr(tp), ptr(ti), ptr(tvals), ptr(x), ptr(got), 0, st))
+    assert torch.equal(got, want)
+    blocks = vals.view(nnzb, b, b)[tb.long()].transpose(1, 2).reshape(-1)
+    assert torch.equal(tvals, blocks)
+
+
 def test_dot_is_deterministic():
     from aquaflux_gb300.sparse import dot
 
