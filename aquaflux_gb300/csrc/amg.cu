@@ -25,6 +25,7 @@ extern "C" int fv_aggregate(int n, const int* indptr, const int* indices, int* a
     fv_set_error("fv_aggregate: bad arguments");
     return FV_ERR_ARG;
   }
+  if (!fv_offsets_ok("fv_aggregate", n, indptr)) return FV_ERR_ARG;
   for (int i = 0; i < n; ++i) agg[i] = -1;
   int na = 0;
   for (int i = 0; i < n; ++i) {
@@ -75,6 +76,7 @@ extern "C" int fv_colour_aggregates(int n, const int* indptr, const int* indices
     fv_set_error("fv_colour_aggregates: bad arguments");
     return FV_ERR_ARG;
   }
+  if (!fv_offsets_ok("fv_colour_aggregates", n, indptr)) return FV_ERR_ARG;
   std::vector<int> cnt(na + 1, 0), members(n);
   for (int i = 0; i < n; ++i) {
     if (agg[i] < 0 || agg[i] >= na) {
@@ -139,6 +141,7 @@ extern "C" int fv_coarsen(int n, const int* indptr, const int* indices, const in
     fv_set_error("fv_coarsen: bad arguments");
     return FV_ERR_ARG;
   }
+  if (!fv_offsets_ok("fv_coarsen", n, indptr)) return FV_ERR_ARG;
   const long nnz = indptr[n];
   for (int i = 0; i < n; ++i)
     if (agg[i] < 0 || agg[i] >= na) {
@@ -241,6 +244,7 @@ extern "C" int fv_permute_pattern(int n, const int* indptr, const int* indices, 
     fv_set_error("fv_permute_pattern: bad arguments");
     return FV_ERR_ARG;
   }
+  if (!fv_offsets_ok("fv_permute_pattern", n, indptr)) return FV_ERR_ARG;
   std::vector<int> iperm(n, -1);
   for (int r = 0; r < n; ++r) {
     if (perm[r] < 0 || perm[r] >= n || iperm[perm[r]] >= 0) {

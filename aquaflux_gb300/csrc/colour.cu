@@ -28,6 +28,7 @@ extern "C" int fv_saturation_colouring(int n, const int* indptr, const int* indi
     if (n_colours) *n_colours = 0;
     return FV_OK;
   }
+  if (!fv_offsets_ok("fv_saturation_colouring", n, indptr)) return FV_ERR_ARG;
   long max_degree = 0;
   for (int v = 0; v < n; ++v) max_degree = std::max<long>(max_degree, indptr[v + 1] - indptr[v]);
   for (long q = 0; q < indptr[n]; ++q)
@@ -109,6 +110,7 @@ extern "C" int fv_greedy_colouring(int n, const int* indptr, const int* indices,
     fv_set_error("fv_greedy_colouring: bad arguments");
     return FV_ERR_ARG;
   }
+  if (n > 0 && !fv_offsets_ok("fv_greedy_colouring", n, indptr)) return FV_ERR_ARG;
   int ncol = 0;
   std::vector<int> seen(64, -1);
   for (int v = 0; v < n; ++v) colour[v] = -1;

@@ -212,3 +212,12 @@ static inline int fv_blocks(long n, int threads) { return (int)((n + threads - 1
 
 // Records a formatted message returned by ``fv_last_error``.
 void fv_set_error(const char* fmt, ...);
+
+// A CSR offset list of n rows (host): it starts at 0 and never decreases; otherwise records
+// "<who>: indptr is not a non-decreasing offset list from 0" and returns false.
+inline bool fv_offsets_ok(const char* who, int n, const int* indptr) {
+  bool ok = indptr[0] == 0;
+  for (int i = 0; ok && i < n; ++i) ok = indptr[i] <= indptr[i + 1];
+  if (!ok) fv_set_error("%s: indptr is not a non-decreasing offset list from 0", who);
+  return ok;
+}

@@ -1394,11 +1394,7 @@ extern "C" int fv_bsr_transpose_map(int n, const int* indptr, const int* indices
     fv_set_error("fv_bsr_transpose_map: bad arguments");
     return FV_ERR_ARG;
   }
-  for (int i = 0; i < n; ++i)
-    if (indptr[0] != 0 || indptr[i] > indptr[i + 1]) {
-      fv_set_error("fv_bsr_transpose_map: indptr is not a non-decreasing offset list from 0");
-      return FV_ERR_ARG;
-    }
+  if (!fv_offsets_ok("fv_bsr_transpose_map", n, indptr)) return FV_ERR_ARG;
   for (int q = 0; q < indptr[n]; ++q)
     if (indices[q] < 0 || indices[q] >= n) {
       fv_set_error("fv_bsr_transpose_map: column index out of range");

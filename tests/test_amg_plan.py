@@ -171,3 +171,44 @@ def test_host_passes_reject_out_of_range_indices():
     cp_ip, cp_ix = np.empty(n + 1, np.int32), np.empty(n + 6, np.int32)
     with pytest.raises(FvError, match="out of range at pair 2"):
         check(lib().fv_cell_pattern(n, 3, ptr(owner), ptr(neigh), ptr(cp_ip), ptr(cp_ix)))
+
+
+def test_host_graph_routines_refuse_a_decreasing_offset_list():
+    """Every host routine that walks a CSR pattern checks its offsets first (a decreasing indptr
+    would make it read past the index array): aggregation, aggregate colouring, coarsening,
+    permutation, both colourings and the transpose map."""
+    import ctypes
+
+    from aquaflux_gb300._lib import FvError, check, lib, ptr
+
+    n, ip, ix = _cell_graph(6)
+    agg = np.zeros(n, np.int32)
+    na = ctypes.c_int(0)
+    check(lib().fv_aggregate(n, ptr(ip), ptr(ix), ptr(agg), ctypes.byref(na)))
+    na = na.value
+    bad = ip.copy()
+    bad[n // 2] = bad[n // 2 + 1] + 1  # one row "ends" before it starts
+    nnz = int(ip[-1])
+    i32 = lambda k: np.empty(k, np.int32)  # noqa: E731
+    i64 = lambda k: np.empty(k, np.int64)  # noqa: E731
+    calls = {
+        "fv_aggregate": lambda: lib().fv_aggregate(n, ptr(bad), ptr(ix), ptr(i32(n)),
+                                                   ctypes.byref(ctypes.c_int(0))),
+        "fv_colour_aggregates": lambda: lib().fv_colour_aggregates(
+            n, ptr(bad), ptr(ix), ptr(agg), na, ptr(i32(na)), ctypes.byref(ctypes.c_int(0))),
+        "fv_coarsen": lambda: lib().fv_coarsen(
+            n, ptr(bad), ptr(ix), ptr(agg), na, ptr(i32(na + 1)), ptr(i32(n)), ptr(i32(na + 1)),
+            ptr(i32(nnz)), ptr(i64(nnz + 1)), ptr(i64(nnz)), ctypes.byref(ctypes.c_long(0))),
+        "fv_permute_pattern": lambda: lib().fv_permute_pattern(
+            n, ptr(bad), ptr(ix), ptr(np.arange(n, dtype=np.int32)), ptr(i32(n + 1)),
+            ptr(i32(nnz)), ptr(i64(nnz))),
+        "fv_saturation_colouring": lambda: lib().fv_saturation_colouring(
+            n, ptr(bad), ptr(ix), ptr(i32(n)), ctypes.byref(ctypes.c_int(0))),
+        "fv_greedy_colouring": lambda: lib().fv_greedy_colouring(
+            n, ptr(bad), ptr(ix), ptr(i32(n)), ctypes.byref(ctypes.c_int(0))),
+        "fv_bsr_transpose_map": lambda: lib().fv_bsr_transpose_map(
+            n, ptr(bad), ptr(ix), ptr(i32(n + 1)), ptr(i32(nnz)), ptr(i32(nnz))),
+    }
+    for name, call in calls.items():
+        with pytest.raises(FvError, match=name + ": indptr is not a non-decreasing"):
+            check(call())
